@@ -1,0 +1,285 @@
+// k_icp.cu -- projective point-to-plane ICP.
+//
+// One launch per ICP iteration: every thread associates a few pixels and
+// accumulates the 27 upper-triangular terms of [J^T J | J^T r] (+ an inlier
+// count) as compensated float pairs; warps and the block combine the pairs;
+// each block writes its partials; the last block to finish sums the partials
+// in block order (deterministic), and, in the pipeline form, solves the 6x6
+// system in FP64 and updates the device-resident pose.
+//
+// Built with -fmad=false so the per-pixel association and terms are the same
+// IEEE float operations as the CPU oracle: inlier sets match exactly.
+#include "tde_common.cuh"
+#include "tde_icp.cuh"
+
+namespace tde {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kPixPerThread = 4;
+
+struct f2 { float hi, lo; };
+
+// Knuth TwoSum: hi + lo == a + b exactly.
+__device__ __forceinline__ f2 two_sum(float a, float b) {
+    float s = a + b;
+    float bp = s - a;
+    float ap = s - bp;
+    float e = (a - ap) + (b - bp);
+    return f2{s, e};
+}
+__device__ __forceinline__ f2 add_ff(f2 a, f2 b) {
+    f2 s = two_sum(a.hi, b.hi);
+    float lo = s.lo + (a.lo + b.lo);
+    return two_sum(s.hi, lo);
+}
+__device__ __forceinline__ f2 add_f(f2 a, float b) {
+    f2 s = two_sum(a.hi, b);
+    s.lo = s.lo + a.lo;
+    return two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ float3 mv(const float *M, float3 v) {
+    float a = 0.f; a += M[0] * v.x; a += M[1] * v.y; a += M[2] * v.z;
+    float b = 0.f; b += M[3] * v.x; b += M[4] * v.y; b += M[5] * v.z;
+    float c = 0.f; c += M[6] * v.x; c += M[7] * v.y; c += M[8] * v.z;
+    return make_float3(a, b, c);
+}
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) {
+    float d = 0.f; d += a.x * b.x; d += a.y * b.y; d += a.z * b.z; return d;
+}
+__device__ __forceinline__ float3 ld3(const float *p, size_t i) {
+    return make_float3(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2));
+}
+
+// Per-pixel association; returns false when the pixel is rejected.
+__device__ __forceinline__ bool associate(const IcpArgs &a, const IcpPose &P, int x, int y, float row[7]) {
+    const size_t i = (size_t)y * a.W + x;
+    float3 n = ld3(a.ncur, i);
+    if (isnan(n.x)) return false;
+    float3 v = ld3(a.vcur, i);
+    float3 rv = mv(P.R_cur, v);
+    float3 vg = make_float3(rv.x + P.t_cur[0], rv.y + P.t_cur[1], rv.z + P.t_cur[2]);
+    float3 vcp = mv(P.R_prev_inv, make_float3(vg.x - P.t_prev[0], vg.y - P.t_prev[1], vg.z - P.t_prev[2]));
+    if (!(vcp.z > 0.f)) return false;
+    int u = __float2int_rn(vcp.x * a.fx / vcp.z + a.cx);
+    int w = __float2int_rn(vcp.y * a.fy / vcp.z + a.cy);
+    if (u < 0 || w < 0 || u >= a.W || w >= a.H) return false;
+    const size_t j = (size_t)w * a.W + u;
+    float3 np = ld3(a.nprev, j);
+    if (isnan(np.x)) return false;
+    float3 vp = ld3(a.vprev, j);
+    float3 dv = make_float3(vp.x - vg.x, vp.y - vg.y, vp.z - vg.z);
+    if (sqrtf(dot3(dv, dv)) > a.dist_thresh) return false;
+    float3 ng = mv(P.R_cur, n);
+    float3 cr = cross3(ng, np);
+    if (sqrtf(dot3(cr, cr)) >= a.angle_thresh) return false;
+    float3 c = cross3(vg, np);
+    row[0] = c.x; row[1] = c.y; row[2] = c.z;
+    row[3] = np.x; row[4] = np.y; row[5] = np.z;
+    row[6] = dot3(np, dv);
+    return true;
+}
+
+// FP64 Cholesky solve of the 6x6 system and pose update (thread 0 of the last
+// block).  Returns false when A is not positive definite.
+__device__ bool solve_and_update(IcpState *st) {
+    double A[6][6], b[6];
+    int s = 0;
+    for (int k = 0; k < 6; ++k)
+        for (int j = k; j < 7; ++j) {
+            double v = st->sums[s++];
+            if (j == 6) b[k] = v; else { A[k][j] = v; A[j][k] = v; }
+        }
+    double L[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double acc = A[i][j];
+            for (int k = 0; k < j; ++k) acc -= L[i][k] * L[j][k];
+            if (i == j) {
+                if (!(acc > 1e-30)) return false;
+                L[i][i] = sqrt(acc);
+            } else {
+                L[i][j] = acc / L[j][j];
+            }
+        }
+    double yv[6], x[6];
+    for (int i = 0; i < 6; ++i) {
+        double acc = b[i];
+        for (int k = 0; k < i; ++k) acc -= L[i][k] * yv[k];
+        yv[i] = acc / L[i][i];
+    }
+    for (int i = 5; i >= 0; --i) {
+        double acc = yv[i];
+        for (int k = i + 1; k < 6; ++k) acc -= L[k][i] * x[k];
+        x[i] = acc / L[i][i];
+    }
+    double Rinc[9];
+    so3_exp(x, Rinc);
+    double Rn[9], tn[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c)
+            Rn[3 * r + c] = Rinc[3 * r] * st->R[c] + Rinc[3 * r + 1] * st->R[3 + c] + Rinc[3 * r + 2] * st->R[6 + c];
+        tn[r] = Rinc[3 * r] * st->t[0] + Rinc[3 * r + 1] * st->t[1] + Rinc[3 * r + 2] * st->t[2] + x[3 + r];
+    }
+    for (int k = 0; k < 9; ++k) { st->R[k] = Rn[k]; st->pose.R_cur[k] = (float)Rn[k]; }
+    for (int k = 0; k < 3; ++k) { st->t[k] = tn[k]; st->pose.t_cur[k] = (float)tn[k]; }
+    for (int k = 0; k < 6; ++k) st->x[k] = x[k];
+    return true;
+}
+
+template <bool SOLVE>
+__global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState *__restrict__ st,
+                                                       float *__restrict__ gbuf, float *__restrict__ mbuf) {
+    __shared__ IcpPose P;
+    __shared__ f2 red[kThreads / 32][kIcpTerms];
+    __shared__ unsigned ticket;
+    const int tid = threadIdx.x;
+    if (tid == 0) P = st->pose;
+    __syncthreads();
+
+    f2 acc[kIcpTerms];
+    #pragma unroll
+    for (int t = 0; t < kIcpTerms; ++t) acc[t] = f2{0.f, 0.f};
+
+    const int npix = a.W * a.H;
+    const int base = blockIdx.x * kThreads * kPixPerThread + tid;
+    #pragma unroll 1
+    for (int k = 0; k < kPixPerThread; ++k) {
+        int p = base + k * kThreads;
+        if (p >= npix) break;
+        int y = p / a.W, x = p - y * a.W;
+        float row[7];
+        if (associate(a, P, x, y, row)) {
+            int t = 0;
+            #pragma unroll
+            for (int i = 0; i < 6; ++i)
+                #pragma unroll
+                for (int j = i; j < 7; ++j) acc[t] = add_f(acc[t], row[i] * row[j]), ++t;
+            acc[27] = add_f(acc[27], 1.f);
+        }
+    }
+    // warp reduction of the pairs
+    #pragma unroll
+    for (int t = 0; t < kIcpTerms; ++t) {
+        f2 v = acc[t];
+        #pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            f2 o{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
+            v = add_ff(v, o);
+        }
+        acc[t] = v;
+    }
+    const int warp = tid >> 5, lane = tid & 31;
+    if (lane == 0) {
+        #pragma unroll
+        for (int t = 0; t < kIcpTerms; ++t) red[warp][t] = acc[t];
+    }
+    __syncthreads();
+    const int nb = gridDim.x;
+    if (tid < kIcpTerms) {
+        f2 v = red[0][tid];
+        for (int w = 1; w < kThreads / 32; ++w) v = add_ff(v, red[w][tid]);
+        gbuf[(size_t)tid * nb + blockIdx.x] = v.hi;
+        gbuf[(size_t)(kIcpTerms + tid) * nb + blockIdx.x] = v.lo;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) ticket = atomicAdd(&st->counter, 1u);
+    __syncthreads();
+    if (ticket != (unsigned)nb - 1) return;
+
+    // ---- last block: deterministic cross-block sum, one warp per term ----
+    __threadfence();
+    for (int t = warp; t < kIcpTerms; t += kThreads / 32) {
+        f2 v{0.f, 0.f};
+        for (int b = lane; b < nb; b += 32) {
+            f2 o{__ldcg(gbuf + (size_t)t * nb + b), __ldcg(gbuf + (size_t)(kIcpTerms + t) * nb + b)};
+            v = add_ff(v, o);
+        }
+        #pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            f2 o{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
+            v = add_ff(v, o);
+        }
+        if (lane == 0) {
+            st->sums[t] = (double)v.hi + (double)v.lo;
+            if (mbuf && t < 27) mbuf[t] = v.hi + v.lo;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        st->counter = 0u;
+        st->inliers = (int)st->sums[27];
+        if (SOLVE) {
+            bool ok = st->inliers >= kIcpMinInliers && solve_and_update(st);
+            if (!ok) st->status |= kIcpStatusSolveFailed;
+            st->iterations += 1;
+        }
+    }
+}
+
+// transform_estimation.cl:4-53: group g sums its row of the partial buffer.
+__global__ void transform_estimation_kernel(const float *__restrict__ gbuf, float *__restrict__ out, int len,
+                                            int stride) {
+    __shared__ float s[256];
+    const int tid = threadIdx.x;
+    const size_t start = (size_t)blockIdx.x * stride;
+    float sum = 0.f;
+    for (int i = tid; i < len; i += 256) sum += gbuf[start + i];
+    s[tid] = sum;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (tid < off) s[tid] = s[tid] + s[tid + off];
+        __syncthreads();
+    }
+    if (tid == 0) out[blockIdx.x] = s[0];
+}
+
+__global__ void clean_buff_kernel(float *__restrict__ g, int width) {
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= width) return;
+    for (int i = 0; i < 27; ++i) g[(size_t)i * width + id] = 0.f;
+}
+
+__global__ void icp_begin_frame_kernel(IcpState *st) {
+    // the previous frame's pose becomes the association reference
+    for (int k = 0; k < 9; ++k) st->pose.R_prev_inv[k] = (float)st->R[3 * (k % 3) + k / 3];
+    for (int k = 0; k < 3; ++k) st->pose.t_prev[k] = (float)st->t[k];
+    st->status = 0;
+    st->iterations = 0;
+}
+
+}  // namespace
+
+size_t icp_gbuf_floats(int W, int H) {
+    size_t nb = div_up((unsigned)(W * H), (unsigned)(kThreads * kPixPerThread));
+    return 2 * kIcpTerms * nb;
+}
+
+int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, cudaStream_t stream) {
+    unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * kPixPerThread));
+    if (solve) icp_kernel<true><<<nb, kThreads, 0, stream>>>(a, st, gbuf, mbuf);
+    else icp_kernel<false><<<nb, kThreads, 0, stream>>>(a, st, gbuf, mbuf);
+    return check_launch("estimate_combined");
+}
+
+int launch_icp_begin_frame(IcpState *st, cudaStream_t stream) {
+    icp_begin_frame_kernel<<<1, 1, 0, stream>>>(st);
+    return check_launch("icp_begin_frame");
+}
+
+int launch_transform_estimation(const float *gbuf, float *out, int len, int stride, cudaStream_t stream) {
+    transform_estimation_kernel<<<27, 256, 0, stream>>>(gbuf, out, len, stride);
+    return check_launch("transform_estimation");
+}
+
+int launch_clean_buff(float *g, int width, cudaStream_t stream) {
+    clean_buff_kernel<<<div_up(width, 256), 256, 0, stream>>>(g, width);
+    return check_launch("clean_buff");
+}
+
+}  // namespace tde

@@ -1,0 +1,308 @@
+// k_raycast.cu -- model prediction: TSDF ray march (raycast), model-map
+// pyramid (resize) and rigid map transform.
+//
+// Built with -fmad=false: every float expression below is evaluated as the
+// same sequence of IEEE-rounded multiplies and adds the reference kernel
+// (GPU/opencl/raycast.cl) performs, so vertex/normal maps match the
+// reference bit for bit on the same volume.
+#include "tde_common.cuh"
+#include "tde_launch.cuh"
+
+namespace tde {
+namespace {
+
+struct RayParams {
+    tde_point3f t;          // ray origin (camera centre, volume frame)
+    tde_matrix3f R;         // camera -> volume rotation
+    float time_step;        // (float)((double)trunc * 0.8), raycast.cl:209
+    float max_time;         // 3 * (Vx + Vy + Vz), raycast.cl:251
+    tde_intrinsics intr;
+    tde_round_buffer rb;
+    tde_point3f cell;
+    size_t n;               // voxel count (F32 plane offset)
+    const CamPose *dpose;   // when set, t and R are read from here
+};
+
+struct f3 { float x, y, z; };
+
+__device__ __forceinline__ f3 mat_vec(const tde_matrix3f &M, f3 v) {
+    // multiply() in elementary_matrix_template.h:30-39: dot starting from 0.
+    f3 r;
+    float a = 0.f; a += M.row[0].x * v.x; a += M.row[0].y * v.y; a += M.row[0].z * v.z; r.x = a;
+    float b = 0.f; b += M.row[1].x * v.x; b += M.row[1].y * v.y; b += M.row[1].z * v.z; r.y = b;
+    float c = 0.f; c += M.row[2].x * v.x; c += M.row[2].y * v.y; c += M.row[2].z * v.z; r.z = c;
+    return r;
+}
+
+__device__ __forceinline__ f3 normalized(f3 v) {
+    float d = 0.f; d += v.x * v.x; d += v.y * v.y; d += v.z * v.z;
+    float rs = 1.f / sqrtf(d);
+    return f3{v.x * rs, v.y * rs, v.z * rs};
+}
+
+// ray_start + ray_dir * t, component-wise (add_3f after the scale).
+__device__ __forceinline__ f3 along(const tde_point3f &o, f3 d, float t) {
+    return f3{o.x + d.x * t, o.y + d.y * t, o.z + d.z * t};
+}
+
+__device__ __forceinline__ int floor_sat(float v) { return __float2int_rd(v); }  // convert_int_sat_rtn
+
+template <int FMT>
+__device__ __forceinline__ float read_tsdf(const void *vol, const RayParams &p, int x, int y, int z) {
+    return TsdfStore<FMT>::value(vol, voxel_address(x, y, z, p.rb), p.n);
+}
+
+// interpolateTrilineary: raycast.cl:95-145.
+template <int FMT>
+__device__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
+    const tde_point3i &N = p.rb.voxels_size;
+    int gx = floor_sat(pt.x / p.cell.x), gy = floor_sat(pt.y / p.cell.y), gz = floor_sat(pt.z / p.cell.z);
+    if (gx <= 0 || gx >= N.x - 1) return __int_as_float(0x7fffffff);
+    if (gy <= 0 || gy >= N.y - 1) return __int_as_float(0x7fffffff);
+    if (gz <= 0 || gz >= N.z - 1) return __int_as_float(0x7fffffff);
+    float vx = ((float)gx + 0.5f) * p.cell.x;
+    float vy = ((float)gy + 0.5f) * p.cell.y;
+    float vz = ((float)gz + 0.5f) * p.cell.z;
+    gx = (pt.x < vx) ? gx - 1 : gx;
+    gy = (pt.y < vy) ? gy - 1 : gy;
+    gz = (pt.z < vz) ? gz - 1 : gz;
+    float a = pt.x / p.cell.x - ((float)gx + 0.5f); if (a < 0) { gx--; a += 1.0f; }
+    float b = pt.y / p.cell.y - ((float)gy + 0.5f); if (b < 0) { gy--; b += 1.0f; }
+    float c = pt.z / p.cell.z - ((float)gz + 0.5f); if (c < 0) { gz--; c += 1.0f; }
+    float r000 = read_tsdf<FMT>(vol, p, gx, gy, gz), r001 = read_tsdf<FMT>(vol, p, gx, gy, gz + 1);
+    float r010 = read_tsdf<FMT>(vol, p, gx, gy + 1, gz), r011 = read_tsdf<FMT>(vol, p, gx, gy + 1, gz + 1);
+    float r100 = read_tsdf<FMT>(vol, p, gx + 1, gy, gz), r101 = read_tsdf<FMT>(vol, p, gx + 1, gy, gz + 1);
+    float r110 = read_tsdf<FMT>(vol, p, gx + 1, gy + 1, gz), r111 = read_tsdf<FMT>(vol, p, gx + 1, gy + 1, gz + 1);
+    float one_a = 1.f - a, one_b = 1.f - b, one_c = 1.f - c;
+    float x0 = one_b * (r000 * one_c + r001 * c) + b * (r010 * one_c + r011 * c);
+    float x1 = one_b * (r100 * one_c + r101 * c) + b * (r110 * one_c + r111 * c);
+    return one_a * x0 + a * x1;
+}
+
+// Number of march samples whose addresses are issued together.  The samples
+// are independent of each other's values, so their loads overlap; the
+// zero-crossing logic then consumes them in order exactly as a one-sample
+// loop would.
+constexpr int kBatch = 4;
+
+template <int FMT>
+__global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
+                                                     float *__restrict__ nmap, RayParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = p.intr.cols, H = p.intr.rows;
+    if (p.dpose) {
+        __shared__ float s_pose[12];
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+        if (tid < 12) s_pose[tid] = tid < 9 ? p.dpose->R[tid] : p.dpose->t[tid - 9];
+        __syncthreads();
+        p.R = tde_matrix3f{{{s_pose[0], s_pose[1], s_pose[2]}, {s_pose[3], s_pose[4], s_pose[5]},
+                            {s_pose[6], s_pose[7], s_pose[8]}}};
+        p.t = tde_point3f{s_pose[9], s_pose[10], s_pose[11]};
+    }
+    if (x >= W || y >= H) return;
+    const size_t pix = (size_t)W * y + x;
+    const float qnan = __int_as_float(0x7fffffff);
+    float vx_out = qnan, vy_out = qnan, vz_out = qnan;
+    float nx_out = qnan, ny_out = qnan, nz_out = qnan;
+
+    const tde_point3i N = p.rb.voxels_size;
+    const tde_point3f V = p.rb.volume_size;
+    const float step = p.time_step;
+
+    f3 rnu{((float)x - p.intr.cx) / p.intr.fx, ((float)y - p.intr.cy) / p.intr.fy, 1.f};
+    f3 rn2 = mat_vec(p.R, rnu);
+    f3 ray_next{rn2.x + p.t.x, rn2.y + p.t.y, rn2.z + p.t.z};
+    f3 dir = normalized(f3{ray_next.x - p.t.x, ray_next.y - p.t.y, ray_next.z - p.t.z});
+    dir.x = (dir.x == 0.f) ? 1e-15f : dir.x;
+    dir.y = (dir.y == 0.f) ? 1e-15f : dir.y;
+    dir.z = (dir.z == 0.f) ? 1e-15f : dir.z;
+
+    // getMinTime / getMaxTime: raycast.cl:153-171
+    float txmin = ((dir.x > 0 ? 0.f : V.x) - p.t.x) / dir.x;
+    float tymin = ((dir.y > 0 ? 0.f : V.y) - p.t.y) / dir.y;
+    float tzmin = ((dir.z > 0 ? 0.f : V.z) - p.t.z) / dir.z;
+    float t_start = cl_fmax(cl_fmax(txmin, tymin), tzmin);
+    float txmax = ((dir.x > 0 ? V.x : 0.f) - p.t.x) / dir.x;
+    float tymax = ((dir.y > 0 ? V.y : 0.f) - p.t.y) / dir.y;
+    float tzmax = ((dir.z > 0 ? V.z : 0.f) - p.t.z) / dir.z;
+    float t_exit = cl_fmin(cl_fmin(txmax, tymax), tzmax);
+    t_start = cl_fmax(t_start, 0.f);
+
+    if (!(t_start >= t_exit)) {
+        float time_curr = t_start;
+        f3 pu = along(p.t, dir, time_curr);
+        int gx = floor_sat(pu.x / p.cell.x), gy = floor_sat(pu.y / p.cell.y), gz = floor_sat(pu.z / p.cell.z);
+        gx = max(0, min(gx, N.x - 1));
+        gy = max(0, min(gy, N.y - 1));
+        gz = max(0, min(gz, N.z - 1));
+        float tsdf = read_tsdf<FMT>(vol, p, gx, gy, gz);
+
+        bool done = false;
+        while (!done && time_curr < p.max_time) {
+            // Issue up to kBatch sample loads of the next steps.
+            float ts[kBatch];
+            float vals[kBatch];
+            int nvalid = 0;  // samples in range, in order; the first out-of-range one ends the ray
+            {
+                float tc = time_curr;
+                #pragma unroll
+                for (int k = 0; k < kBatch; ++k) {
+                    ts[k] = tc;
+                    vals[k] = 0.f;
+                    tc = tc + step;
+                }
+            }
+            bool stop_after = false;
+            #pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                if (nvalid == k && !stop_after) {
+                    if (!(ts[k] < p.max_time)) { stop_after = true; }
+                    else {
+                        float ct = ts[k] + step;
+                        f3 q = along(p.t, dir, ct);
+                        int sx = floor_sat(q.x / p.cell.x), sy = floor_sat(q.y / p.cell.y), sz = floor_sat(q.z / p.cell.z);
+                        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < N.x && sy < N.y && sz < N.z) {
+                            vals[k] = read_tsdf<FMT>(vol, p, sx, sy, sz);
+                            nvalid = k + 1;
+                        } else {
+                            stop_after = true;
+                        }
+                    }
+                }
+            }
+            // Consume the samples in order.
+            #pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                if (done) break;
+                if (k >= nvalid) { done = true; break; }  // out of volume or out of time
+                time_curr = ts[k];
+                float tsdf_prev = tsdf;
+                tsdf = vals[k];
+                if (tsdf_prev < 0.f && tsdf > 0.f) { done = true; break; }
+                if (tsdf_prev > 0.f && tsdf < 0.f) {
+                    done = true;
+                    float ct = time_curr + step;
+                    float Ftdt = trilinear<FMT>(vol, p, along(p.t, dir, ct));
+                    if (isnan(Ftdt)) break;
+                    float Ft = trilinear<FMT>(vol, p, along(p.t, dir, time_curr));
+                    if (isnan(Ft)) break;
+                    float Ts = time_curr - step * Ft / (Ftdt - Ft);
+                    f3 vf = along(p.t, dir, Ts);
+                    vx_out = vf.x; vy_out = vf.y; vz_out = vf.z;
+                    f3 p3 = along(p.t, dir, time_curr);
+                    int hx = floor_sat(p3.x / p.cell.x), hy = floor_sat(p3.y / p.cell.y), hz = floor_sat(p3.z / p.cell.z);
+                    if (hx > 1 && hy > 1 && hz > 1 && hx < N.x - 2 && hy < N.y - 2 && hz < N.z - 2) {
+                        f3 tt = vf; tt.x = tt.x + p.cell.x; float Fx1 = trilinear<FMT>(vol, p, tt);
+                        tt = vf; tt.x = tt.x - p.cell.x; float Fx2 = trilinear<FMT>(vol, p, tt);
+                        tt = vf; tt.y = tt.y + p.cell.y; float Fy1 = trilinear<FMT>(vol, p, tt);
+                        tt = vf; tt.y = tt.y - p.cell.y; float Fy2 = trilinear<FMT>(vol, p, tt);
+                        tt = vf; tt.z = tt.z + p.cell.z; float Fz1 = trilinear<FMT>(vol, p, tt);
+                        tt = vf; tt.z = tt.z - p.cell.z; float Fz2 = trilinear<FMT>(vol, p, tt);
+                        f3 n = normalized(f3{Fx1 - Fx2, Fy1 - Fy2, Fz1 - Fz2});
+                        nx_out = n.x; ny_out = n.y; nz_out = n.z;
+                    }
+                    break;
+                }
+            }
+            if (!done) {
+                // every sample of the batch was consumed without a decision
+                time_curr = ts[kBatch - 1] + step;
+            }
+        }
+    }
+    vmap[3 * pix + 0] = vx_out; vmap[3 * pix + 1] = vy_out; vmap[3 * pix + 2] = vz_out;
+    nmap[3 * pix + 0] = nx_out; nmap[3 * pix + 1] = ny_out; nmap[3 * pix + 2] = nz_out;
+}
+
+// resize_vertex_map / resize_normal_map (absent from the reference; named at
+// common/inc/constants.h:175-176): 2x2 block mean, all four valid.
+template <bool NORMAL>
+__global__ void resize_map_kernel(const float *__restrict__ src, float *__restrict__ dst, int sc, int sr) {
+    const int dc = sc >> 1, dr = sr >> 1;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= dc || y >= dr) return;
+    const float qnan = __int_as_float(0x7fffffff);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    bool ok = true;
+    #pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+        #pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+            size_t i = 3 * ((size_t)(2 * y + dy) * sc + (2 * x + dx));
+            float a = src[i], b = src[i + 1], c = src[i + 2];
+            ok = ok && !isnan(a);
+            sx = sx + a; sy = sy + b; sz = sz + c;
+        }
+    float ox = qnan, oy = qnan, oz = qnan;
+    if (ok) {
+        if (NORMAL) {
+            float d = 0.f; d += sx * sx; d += sy * sy; d += sz * sz;
+            float rs = 1.f / sqrtf(d);
+            ox = sx * rs; oy = sy * rs; oz = sz * rs;
+        } else {
+            ox = sx * 0.25f; oy = sy * 0.25f; oz = sz * 0.25f;
+        }
+    }
+    size_t o = 3 * ((size_t)y * dc + x);
+    dst[o] = ox; dst[o + 1] = oy; dst[o + 2] = oz;
+}
+
+// transform_map.cl:6-65
+__global__ void transform_maps_kernel(const float *__restrict__ vs, const float *__restrict__ ns, float *vd,
+                                      float *nd, const tde_matrix3f R, const tde_point3f t, int W, int H) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const float qnan = __int_as_float(0x7fffffff);
+    size_t i = 3 * ((size_t)y * W + x);
+    f3 v{vs[i], vs[i + 1], vs[i + 2]};
+    f3 vo{qnan, qnan, qnan};
+    if (!isnan(v.x)) {
+        f3 r = mat_vec(R, v);
+        vo = f3{r.x + t.x, r.y + t.y, r.z + t.z};
+    }
+    f3 n{ns[i], ns[i + 1], ns[i + 2]};
+    f3 no{qnan, qnan, qnan};
+    if (!isnan(n.x)) no = mat_vec(R, n);
+    vd[i] = vo.x; vd[i + 1] = vo.y; vd[i + 2] = vo.z;
+    nd[i] = no.x; nd[i + 1] = no.y; nd[i + 2] = no.z;
+}
+
+}  // namespace
+
+int launch_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f &t,
+                   const tde_matrix3f &R, float trunc, const tde_intrinsics &intr, const tde_round_buffer &rb,
+                   const tde_point3f &cell, const CamPose *dpose, cudaStream_t stream) {
+    RayParams p;
+    p.dpose = dpose;
+    p.t = t; p.R = R;
+    p.time_step = (float)((double)trunc * 0.8);
+    p.max_time = 3.f * ((rb.volume_size.x + rb.volume_size.y) + rb.volume_size.z);
+    p.intr = intr; p.rb = rb; p.cell = cell; p.n = voxel_count(rb);
+    dim3 block(32, 8);
+    dim3 grid(div_up(intr.cols, 32), div_up(intr.rows, 8));
+    return dispatch_format(format, [&](auto F) {
+        raycast_kernel<decltype(F)::value><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+        return check_launch("raycast");
+    });
+}
+
+int launch_resize_map(const float *src, float *dst, int sc, int sr, bool normal, cudaStream_t stream) {
+    dim3 block(32, 8);
+    dim3 grid(div_up(sc >> 1, 32), div_up(sr >> 1, 8));
+    if (normal) resize_map_kernel<true><<<grid, block, 0, stream>>>(src, dst, sc, sr);
+    else resize_map_kernel<false><<<grid, block, 0, stream>>>(src, dst, sc, sr);
+    return check_launch("resize_map");
+}
+
+int launch_transform_maps(const float *vs, const float *ns, float *vd, float *nd, const tde_matrix3f &R,
+                          const tde_point3f &t, int W, int H, cudaStream_t stream) {
+    dim3 block(32, 8);
+    dim3 grid(div_up(W, 32), div_up(H, 8));
+    transform_maps_kernel<<<grid, block, 0, stream>>>(vs, ns, vd, nd, R, t, W, H);
+    return check_launch("transform_maps");
+}
+
+}  // namespace tde

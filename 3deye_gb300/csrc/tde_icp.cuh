@@ -1,0 +1,60 @@
+// tde_icp.cuh -- ICP launch arguments and the device-resident pose state.
+#pragma once
+#include "tde_common.cuh"
+
+namespace tde {
+
+constexpr int kIcpTerms = 28;        // 27 system terms + inlier count
+constexpr int kIcpMinInliers = 6;    // fewer pairs cannot constrain 6 DoF
+constexpr int kIcpStatusSolveFailed = 1;
+
+// Float pose consumed by the association: current estimate (camera ->
+// global) and the previous frame's inverse (global -> previous camera).
+struct IcpPose {
+    float R_cur[9], t_cur[3];
+    float R_prev_inv[9], t_prev[3];
+};
+
+// Device-resident ICP state.  R/t carry the estimate in FP64; `pose` is its
+// float mirror read by the kernels.
+struct IcpState {
+    double R[9], t[3];
+    double sums[kIcpTerms];
+    double x[6];
+    IcpPose pose;
+    int status, inliers, iterations, pad0;
+    unsigned counter;  // blocks done in the running launch (reset by the last block)
+    unsigned pad1[3];
+};
+
+struct IcpArgs {
+    const float *vcur, *ncur, *vprev, *nprev;
+    int W, H;
+    float fx, fy, cx, cy;
+    float dist_thresh, angle_thresh;
+};
+
+// exp of the rotation part x[0..2] (Rodrigues), row-major 3x3.
+__host__ __device__ inline void so3_exp(const double *x, double *R) {
+    double wx = x[0], wy = x[1], wz = x[2];
+    double th2 = wx * wx + wy * wy + wz * wz;
+    double A, B;
+    if (th2 < 1e-20) {
+        A = 1.0 - th2 / 6.0;
+        B = 0.5 - th2 / 24.0;
+    } else {
+        double th = sqrt(th2);
+        A = sin(th) / th;
+        B = (1.0 - cos(th)) / th2;
+    }
+    // R = I + A [w]x + B ([w]x)^2,  ([w]x)^2 = w w^T - th2 I
+    R[0] = 1.0 + B * (wx * wx - th2); R[1] = -A * wz + B * wx * wy;       R[2] = A * wy + B * wx * wz;
+    R[3] = A * wz + B * wx * wy;       R[4] = 1.0 + B * (wy * wy - th2); R[5] = -A * wx + B * wy * wz;
+    R[6] = -A * wy + B * wx * wz;      R[7] = A * wx + B * wy * wz;       R[8] = 1.0 + B * (wz * wz - th2);
+}
+
+size_t icp_gbuf_floats(int W, int H);
+int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, cudaStream_t stream);
+int launch_icp_begin_frame(IcpState *st, cudaStream_t stream);
+
+}  // namespace tde

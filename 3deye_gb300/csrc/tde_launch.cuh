@@ -1,0 +1,26 @@
+// tde_launch.cuh -- internal launchers of the depth and raycast kernels.
+#pragma once
+#include "tde_common.cuh"
+#include "tde_integrate.cuh"
+
+namespace tde {
+
+int launch_bilateral(const uint16_t *src, uint16_t *dst, int W, int H, float ss, float sc, uint32_t max_mm,
+                     float *vmap, const tde_intrinsics *intr, cudaStream_t stream);
+int launch_pyramid(const uint16_t *src, uint16_t *dst, int sW, int sH, float sigma_color, float *vmap,
+                   const tde_intrinsics *intr_dst, cudaStream_t stream);
+int launch_scale_depth(const uint16_t *depth, float *scaled, const tde_intrinsics &intr, cudaStream_t stream);
+int launch_vertex_map(const uint16_t *depth, float *vmap, const tde_intrinsics &intr, cudaStream_t stream);
+int launch_normal_map(const float *vmap, float *nmap, int W, int H, cudaStream_t stream);
+
+int launch_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f &t,
+                   const tde_matrix3f &R, float trunc, const tde_intrinsics &intr, const tde_round_buffer &rb,
+                   const tde_point3f &cell, const CamPose *dpose, cudaStream_t stream);
+int launch_resize_map(const float *src, float *dst, int sc, int sr, bool normal, cudaStream_t stream);
+int launch_transform_maps(const float *vs, const float *ns, float *vd, float *nd, const tde_matrix3f &R,
+                          const tde_point3f &t, int W, int H, cudaStream_t stream);
+int launch_transform_estimation(const float *gbuf, float *out, int len, int stride, cudaStream_t stream);
+int launch_clean_buff(float *g, int width, cudaStream_t stream);
+int launch_tsdf_init(void *vol, int fmt, size_t n, cudaStream_t stream);
+
+}  // namespace tde

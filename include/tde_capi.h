@@ -1,0 +1,261 @@
+/*
+ * tde_capi.h -- C-ABI of the GB300 KinectFusion per-frame pipeline.
+ *
+ * This is the drop-in boundary for 3deye's OpenCL path.  Every entry point
+ * takes plain device pointers, sizes and POD structs whose layouts are byte-
+ * identical to the reference's shared host/device types; no torch or CUDA
+ * types appear in the signatures (a stream is an opaque `void *`, NULL meaning
+ * the legacy default stream).  Each call validates its arguments, enqueues its
+ * kernels on the given stream and returns a status code; nothing blocks unless
+ * the comment says so.  The C++ layer in include/3deye/ restores the
+ * reference's free-function API (opencl_wrappers.h) on top of these calls.
+ *
+ * Reference citations are paths inside the 3deye project.
+ */
+#ifndef TDE_CAPI_H
+#define TDE_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes.  The reference aborts (common/inc/opencl_utils.h:22-50) or   */
+/* throws on misuse; here every call reports instead.                         */
+/* ------------------------------------------------------------------------ */
+#define TDE_OK 0
+#define TDE_ERR_INVALID_ARG (-1)  /* null pointer, bad size, bad format      */
+#define TDE_ERR_OOM (-2)          /* device allocation failed                */
+#define TDE_ERR_CUDA (-3)         /* a CUDA runtime call failed              */
+#define TDE_ERR_DEVICE_TIMEOUT (-4) /* a bounded device-side wait gave up    */
+#define TDE_ERR_CAPACITY (-5)     /* output buffer smaller than the result   */
+#define TDE_ERR_NOT_FOUND (-6)    /* unknown kernel name                     */
+#define TDE_ERR_UNSUPPORTED (-7)  /* configuration outside the supported set */
+
+/* Last error message of the calling thread ("" when none). */
+const char *tde_last_error(void);
+/* Library version string. */
+const char *tde_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Shared POD types (layout pinned by static_assert in the implementation).  */
+/* ------------------------------------------------------------------------ */
+/* point_3f / vector_3f: common/inc/elementary_points.h:35-41 */
+typedef struct tde_point3f { float x, y, z; } tde_point3f;
+/* point_3i: common/inc/elementary_points.h:43-48 */
+typedef struct tde_point3i { int x, y, z; } tde_point3i;
+/* matrix_3f, three rows: common/inc/types/elementary_matrix_template.h:1-3 */
+typedef struct tde_matrix3f { tde_point3f row[3]; } tde_matrix3f;
+/* intrinsics: common/inc/types/intrinsics.h:8-26 */
+typedef struct tde_intrinsics { float fx, fy, cx, cy; int cols, rows; } tde_intrinsics;
+/* round_buffer (72 bytes): common/inc/types/round_buffer.h:25-63 */
+typedef struct tde_round_buffer {
+    int start_index, end_index, buffer_length;
+    tde_point3i origin_GRID;
+    tde_point3f origin_GRID_global;
+    tde_point3f origin_metric;
+    tde_point3f volume_size;
+    tde_point3i voxels_size;
+} tde_round_buffer;
+/* Tsdf {short value; short weight;}: common/inc/types/base_points.h:75-78 */
+typedef struct tde_tsdf_i16 { int16_t value; int16_t weight; } tde_tsdf_i16;
+/* Color {uchar r,g,b,w}: common/inc/types/base_points.h:87-99 */
+typedef struct tde_color { uint8_t r, g, b, w; } tde_color;
+/* XYZI {float x,y,z,w}: common/inc/types/base_points.h:135-157 */
+typedef struct tde_xyzi { float x, y, z, w; } tde_xyzi;
+
+/* Vertex and normal maps are Point_XYZ / Point_NXYZ arrays: three floats per
+ * pixel, row-major, NaN marking an invalid pixel (base_points.h:172-186). */
+
+/* ------------------------------------------------------------------------ */
+/* TSDF storage formats.                                                     */
+/*   TDE_TSDF_I16: the reference record {int16 v, int16 w}; f = v / 32767,   */
+/*                 v = clamp(rtz(f * 32767), +-32767) (GPU/opencl/raycast.cl:9-27). */
+/*   TDE_TSDF_F16: {binary16 f, uint16 w}, 4 bytes per voxel.                 */
+/*   TDE_TSDF_F32: two planes in one buffer: float f[N], then uint16 w[N].    */
+/* Voxel (x,y,z) lives at calculate_address (raycast.cl:29-47): cyclic over  */
+/* origin_GRID, x fastest.                                                    */
+/* ------------------------------------------------------------------------ */
+#define TDE_TSDF_I16 0
+#define TDE_TSDF_F16 1
+#define TDE_TSDF_F32 2
+
+/* Bytes a volume of this format and size occupies (0 on bad arguments). */
+size_t tde_tsdf_volume_bytes(int format, const tde_round_buffer *rb);
+
+/* init_tsdf (named at common/inc/constants.h:168): every voxel f = 0, w = 0. */
+int tde_tsdf_init(void *volume, int format, const tde_round_buffer *rb, void *stream);
+
+/* round_buffer(point_3i voxels, point_3f metric) constructor semantics:
+ * common/src/round_buffer.cpp:5-40,84-89 (origins zero, start_index 0,
+ * buffer_length = voxel count). Host-only. */
+int tde_round_buffer_init(tde_round_buffer *rb, tde_point3i voxels, tde_point3f metric_size);
+
+/* determine_extract_step(depth, step, num_of_steps, divisor):
+ * common/src/mem_utils.cpp:43-85.  Depth must be 128, 256 or 512
+ * (TDE_ERR_UNSUPPORTED otherwise, where the reference throws).  Host-only. */
+int tde_determine_extract_step(unsigned depth, int divisor, unsigned *step, unsigned *num_of_steps);
+
+/* ======================================================================== */
+/* a1/a2: depth preprocessing                                                */
+/* ======================================================================== */
+/* Apply_Billateral_Filtration: common/src/opencl_wrappers.cpp:216-235,
+ * kernel GPU/opencl/compute_bilateral_filtering.cl:8-57.  13x13 window
+ * [c-6, min(c+7, W-1)) as the reference, weight exp(-(d2*0.5/ss^2 +
+ * dz2*0.5/sc^2)), result rte(sum1/sum2) clamped to [0, 32767] and set to 0
+ * above max_distance_mm (the reference's intended output; it writes sum1).
+ * Pass sigma_space = 4.5, sigma_color = 30 for the reference constants
+ * (common/inc/common_defines.h:20-23).  `max_distance_mm` is an integer in
+ * millimetres where the reference host passes float bits (opencl_wrappers.cpp:231). */
+int tde_bilateral_filter(const uint16_t *depth, uint16_t *filtered, int cols, int rows,
+                         float sigma_space, float sigma_color, uint32_t max_distance_mm, void *stream);
+
+/* Create_Pyramid: opencl_wrappers.cpp:245-271 (kernel compute_depth_pyramid,
+ * absent from the reference).  dst is (src_cols>>1) x (src_rows>>1): the mean
+ * of the valid pixels of the 5x5 window around (2x,2y) whose depth differs
+ * from the centre by less than 3*sigma_color mm; 0 when the centre is 0. */
+int tde_depth_pyramid_level(const uint16_t *src, uint16_t *dst, int src_cols, int src_rows,
+                            float sigma_color, void *stream);
+
+/* Fused bilateral + pyramid: one launch writes levels[0..num_levels-1]
+ * (level l has cols>>l x rows>>l pixels).  Same results as the two calls above. */
+int tde_bilateral_pyramid(const uint16_t *depth, uint16_t *const *levels, int num_levels, int cols,
+                          int rows, float sigma_space, float sigma_color, uint32_t max_distance_mm,
+                          void *stream);
+
+/* ======================================================================== */
+/* a3/a4: vertex and normal maps                                             */
+/* ======================================================================== */
+/* Create_Vertex_Maps (one level): opencl_wrappers.cpp:281-305, intrinsics of
+ * the level from intrinsics::operator() (common/src/intrinsics.cpp:7-18).
+ * v = (z (u-cx)/fx, z (v-cy)/fy, z), z = depth_mm / 1000; NaN where depth 0. */
+int tde_vertex_map(const uint16_t *depth, float *vmap, const tde_intrinsics *intr_level, void *stream);
+
+/* Create_Normal_Maps (one level): opencl_wrappers.cpp:315-343 (kernel
+ * compute_normal_map_eigen, absent).  Normal = eigenvector of the smallest
+ * eigenvalue of the covariance of the valid vertices in the 7x7 window
+ * (at least 24 valid), oriented towards the camera (n.v < 0); NaN otherwise. */
+int tde_normal_map(const float *vmap, float *nmap, int cols, int rows, void *stream);
+
+/* ======================================================================== */
+/* a5/a6: ICP                                                                */
+/* ======================================================================== */
+/* Floats of scratch that tde_estimate_combined needs for its per-block
+ * partial sums at a cols x rows level. */
+size_t tde_estimate_combined_gbuf_floats(int cols, int rows);
+
+/* Estimate_Combined: opencl_wrappers.cpp:364-438 (kernel estimate_combined,
+ * absent; stage two transform_estimation.cl:4-53).  Projective point-to-plane
+ * association of the current maps (camera frame) against the previous model
+ * maps (global frame) with the current pose (R_cur, t_cur) and the previous
+ * pose inverse (R_prev_inv, t_prev); rejects pairs farther than dist_thresh
+ * metres or with sin(angle) >= angle_thresh.  Writes the 27 sums
+ * [A00..A05 b0 A11..A15 b1 ... A55 b5] (the unpack order of
+ * opencl_wrappers.cpp:426-437) to mbuf (device, 27 floats) in one launch,
+ * using gbuf (device, tde_estimate_combined_gbuf_floats floats) as scratch.
+ * Sums are compensated FP32. */
+int tde_estimate_combined(const float *vmap_cur, const float *nmap_cur, const float *vmap_prev_g,
+                          const float *nmap_prev_g, const tde_matrix3f *R_cur, const tde_point3f *t_cur,
+                          const tde_matrix3f *R_prev_inv, const tde_point3f *t_prev,
+                          const tde_intrinsics *intr, float dist_thresh, float angle_thresh,
+                          float *gbuf, float *mbuf, void *stream);
+
+/* transform_estimation (GPU/opencl/transform_estimation.cl:4-53): out[g] =
+ * sum of gbuf[g*group_stride .. g*group_stride + buf_length), g = 0..26.
+ * The reference hard-codes group_stride = 1200. */
+int tde_transform_estimation(const float *gbuf, float *out, int buf_length, int group_stride, void *stream);
+
+/* Clean_Buff (opencl_wrappers.cpp:994-1006, clean_buff.cl:4-11): zero 27 rows
+ * of `width` floats. */
+int tde_clean_buff(float *gbuf, int width, void *stream);
+
+/* Host FP64 solve of the 27-sum system and pose update (the missing L4 step;
+ * the reference's only solve is the RGBD one at opencl_wrappers.cpp:1282-1326).
+ * x = A^-1 b by Cholesky; R <- exp([w]x) R, t <- exp([w]x) t + v with
+ * x = (w, v).  Returns TDE_ERR_INVALID_ARG if A is not positive definite. */
+int tde_icp_solve_update_host(const float *mbuf27, double *R9, double *t3, double *x6);
+
+/* ======================================================================== */
+/* a7: TSDF integration                                                      */
+/* ======================================================================== */
+/* scale_depth (kernel absent; called at opencl_wrappers.cpp:37-43):
+ * scaled = depth_mm / 1000 * sqrt(((x-cx)/fx)^2 + ((y-cy)/fy)^2 + 1). */
+int tde_scale_depth(const uint16_t *depth, float *scaled, const tde_intrinsics *intr, void *stream);
+
+/* Integrate_Tsdf_Data: opencl_wrappers.cpp:21-64 (kernel
+ * integrate_tsdf_volume, absent).  Voxel (x,y,z) centre is
+ * ((x+.5)cs.x, (y+.5)cs.y, (z+.5)cs.z) in volume coordinates; the camera
+ * centre t and R_inv (world->camera rotation) are in the same frame.  Voxels
+ * that project outside the image, onto an invalid pixel, or lie more than
+ * trunc behind the surface are not touched.  Others get
+ * f = (f w + min(1, sdf/trunc)) / (w + 1), w = min(w + 1, max_weight).
+ * MAX_TSDF_WEIGHT is 128 (common/inc/common_defines.h:10). */
+int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, float trunc,
+                       const tde_matrix3f *R_inv, const tde_point3f *t, const tde_intrinsics *intr,
+                       const tde_point3f *cell_size, const tde_round_buffer *rb, int max_weight,
+                       void *stream);
+
+/* ======================================================================== */
+/* a8/a9: raycast and model maps                                             */
+/* ======================================================================== */
+/* Raycast: opencl_wrappers.cpp:66-95, kernel GPU/opencl/raycast.cl:182-405.
+ * Same march (step 0.8 trunc), zero-crossing test, secant refinement and
+ * central-difference normals as the reference, evaluated with the same IEEE
+ * float operations.  Writes global-frame vertex and normal maps. */
+int tde_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t,
+                const tde_matrix3f *R, float trunc, const tde_intrinsics *intr,
+                const tde_round_buffer *rb, const tde_point3f *cell_size, void *stream);
+
+/* Resize_Vertex_Map / Resize_Normal_Map: opencl_wrappers.cpp:97-146 (kernels
+ * absent).  `src_cols` x `src_rows` is the source level; dst is half size.
+ * Vertex: mean of the 2x2 block if all four are valid, else NaN.  Normal: the
+ * normalised mean under the same rule. */
+int tde_resize_vertex_map(const float *src, float *dst, int src_cols, int src_rows, void *stream);
+int tde_resize_normal_map(const float *src, float *dst, int src_cols, int src_rows, void *stream);
+
+/* Transform_Maps: opencl_wrappers.cpp:148-179, kernel transform_map.cl:6-65.
+ * v' = R v + t, n' = R n, NaN passes through. */
+int tde_transform_maps(const float *vmap_src, const float *nmap_src, float *vmap_dst, float *nmap_dst,
+                       const tde_matrix3f *R, const tde_point3f *t, int cols, int rows, void *stream);
+
+/* ======================================================================== */
+/* a10-a12: cyclic volume, slab extraction, slab cleaning                    */
+/* ======================================================================== */
+/* Scratch bytes tde_extract_slice needs for a volume with this round buffer. */
+size_t tde_extract_slice_scratch_bytes(const tde_round_buffer *rb);
+
+/* Extract_Slice: opencl_wrappers.cpp:856-964 with kernels
+ * scan_slice_of_both_volumes.cl:76-208 and extract_slice_as_cloud.cl:72-201.
+ * Voxels in the "black zone" (scan_slice_of_both_volumes.cl:63-74) emit a
+ * point for each sign change towards +x, +y, +z (both voxels with w != 0 and
+ * f != 1; the +z test stops at the chunk end z+1 < chunk_end) and one for a
+ * set colour.  Output order is the reference's: z chunks of
+ * determine_extract_step(depth, divisor 4) in order; in each chunk the +x,
+ * +y, +z and colour points, each group in (z, y, x) raster order.  Points are
+ * {x+dx, y+dy, z+dz, 1.0f} in voxel units; colors[i] is the colour of the
+ * voxel a point names.  `color_volume` may be NULL (no colour points, zero
+ * colours); `colors` and `weights` (the named voxel's weight) may be NULL.
+ * The total point count goes to *count_device (device uint32).  Points past
+ * `capacity` are not written; the host wrapper reads the count and retries.
+ * Bit-exact with the reference on the scan's predicate set. */
+int tde_extract_slice(const void *volume, int format, const tde_color *color_volume,
+                      tde_point3i min_bounds, tde_point3i max_bounds, const tde_round_buffer *rb,
+                      void *scratch, size_t scratch_bytes, tde_xyzi *points, tde_color *colors,
+                      float *weights, uint32_t capacity, uint32_t *count_device, void *stream);
+
+/* Clean_Tsdf_Slice: opencl_wrappers.cpp:835-854 (kernel clean_tsdf_slice,
+ * absent): black-zone voxels get f = 0, w = 0. */
+int tde_clean_tsdf_slice(void *volume, int format, tde_point3i min_bounds, tde_point3i max_bounds,
+                         const tde_round_buffer *rb, void *stream);
+
+/* Clean_Color_Slice: opencl_wrappers.cpp:814-833, clean_color_slice.cl:41-67. */
+int tde_clean_color_slice(tde_color *color_volume, tde_point3i min_bounds, tde_point3i max_bounds,
+                          const tde_round_buffer *rb, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TDE_CAPI_H */

@@ -1,0 +1,246 @@
+"""Python access to the CPU oracle (liboracle.so) and, when built, to the
+reference's own kernels compiled as C (oracle/_ref/*.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() (as the
+checker) and bench.py's CPU-baseline leg.  Operates on numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+REF_DIR = HERE / "_ref"
+
+
+class Intr(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("cols", C.c_int), ("rows", C.c_int)]
+
+    def level(self, l):
+        d = float(1 << l)
+        return Intr(self.fx / d, self.fy / d, self.cx / d, self.cy / d, self.cols >> l, self.rows >> l)
+
+
+class RB(C.Structure):
+    _fields_ = [("start_index", C.c_int), ("end_index", C.c_int), ("buffer_length", C.c_int),
+                ("origin_GRID", C.c_int * 3), ("origin_GRID_global", C.c_float * 3),
+                ("origin_metric", C.c_float * 3), ("volume_size", C.c_float * 3), ("voxels_size", C.c_int * 3)]
+
+
+def make_rb(voxels, metric, origin=(0, 0, 0)) -> RB:
+    rb = RB()
+    rb.voxels_size[:] = list(voxels)
+    rb.volume_size[:] = [float(v) for v in metric]
+    rb.origin_GRID[:] = list(origin)
+    rb.buffer_length = int(voxels[0]) * int(voxels[1]) * int(voxels[2])
+    return rb
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "oracle arrays must be C-contiguous"
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} missing: run __graft_entry__.build()")
+    return C.CDLL(str(LIB_PATH))
+
+
+lib = _load()
+P, I, F, SZ = C.c_void_p, C.c_int, C.c_float, C.c_size_t
+pI, pRB = C.POINTER(Intr), C.POINTER(RB)
+_sigs = {
+    "or_voxel_address": (SZ, [I, I, I, pRB]),
+    "or_float_to_half": (C.c_uint16, [F]),
+    "or_half_to_float": (F, [C.c_uint16]),
+    "or_raycast": (I, [P, I, P, P, P, P, F, pI, pRB, P]),
+    "or_bilateral": (I, [P, P, I, I, F, F, C.c_uint32, P]),
+    "or_pyramid": (I, [P, P, I, I, F]),
+    "or_scale_depth": (I, [P, P, pI]),
+    "or_vertex_map": (I, [P, P, pI]),
+    "or_normal_map": (I, [P, P, I, I]),
+    "or_icp_terms": (I, [P, P, P, P, P, pI, F, F, P, P]),
+    "or_icp_solve": (I, [P, P, P, P]),
+    "or_integrate": (I, [P, P, I, F, P, P, pI, P, pRB, I, P]),
+    "or_resize_map": (I, [P, P, I, I, I]),
+    "or_transform_maps": (I, [P, P, P, P, P, P, I, I]),
+    "or_transform_estimation": (I, [P, P, I, I]),
+    "or_extract_slice": (C.c_int64, [P, I, P, P, P, pRB, I, P, P, P, C.c_int64]),
+    "or_clean_tsdf_slice": (I, [P, I, P, P, pRB]),
+    "or_clean_color_slice": (I, [P, P, P, pRB]),
+    "or_set_threads": (I, [I]),
+    "or_render_depth": (I, [P, I, P, pI, P]),
+    "or_apply_noise": (I, [P, P, I, I, C.c_uint32, C.c_uint32, F, F]),
+}
+for _n, (_r, _a) in _sigs.items():
+    _f = getattr(lib, _n)
+    _f.restype, _f.argtypes = _r, _a
+
+F32 = np.float32
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def volume_bytes(fmt, rb: RB) -> int:
+    n = rb.voxels_size[0] * rb.voxels_size[1] * rb.voxels_size[2]
+    return n * (6 if fmt == 2 else 4)
+
+
+def set_threads(n: int) -> int:
+    return lib.or_set_threads(n)
+
+
+def raycast(vol, fmt, rb, intr, R, t, trunc, cell):
+    vm = np.empty((intr.rows, intr.cols, 3), F32)
+    nm = np.empty_like(vm)
+    lib.or_raycast(_p(vol), fmt, _p(vm), _p(nm), _p(f32(t)), _p(f32(R)), trunc, C.byref(intr), C.byref(rb),
+                   _p(f32(cell)))
+    return vm, nm
+
+
+def bilateral(src, sigma_space=4.5, sigma_color=30.0, max_mm=32767, want_ratio=False):
+    H, W = src.shape
+    dst = np.empty_like(src)
+    ratio = np.empty((H, W), F32) if want_ratio else None
+    lib.or_bilateral(_p(np.ascontiguousarray(src)), _p(dst), W, H, sigma_space, sigma_color, max_mm, _p(ratio))
+    return (dst, ratio) if want_ratio else dst
+
+
+def pyramid(src, sigma_color=30.0):
+    H, W = src.shape
+    dst = np.empty((H >> 1, W >> 1), np.uint16)
+    lib.or_pyramid(_p(np.ascontiguousarray(src)), _p(dst), W, H, sigma_color)
+    return dst
+
+
+def scale_depth(depth, intr):
+    out = np.empty((intr.rows, intr.cols), F32)
+    lib.or_scale_depth(_p(np.ascontiguousarray(depth)), _p(out), C.byref(intr))
+    return out
+
+
+def vertex_map(depth, intr):
+    out = np.empty((intr.rows, intr.cols, 3), F32)
+    lib.or_vertex_map(_p(np.ascontiguousarray(depth)), _p(out), C.byref(intr))
+    return out
+
+
+def normal_map(vmap):
+    H, W, _ = vmap.shape
+    out = np.empty_like(vmap)
+    lib.or_normal_map(_p(f32(vmap)), _p(out), W, H)
+    return out
+
+
+def icp_terms(vcur, ncur, vprev, nprev, pose24, intr, dist=0.1, angle=0.34202014):
+    sums = np.zeros(28, np.float64)
+    mask = np.zeros((intr.rows, intr.cols), np.uint8)
+    lib.or_icp_terms(_p(f32(vcur)), _p(f32(ncur)), _p(f32(vprev)), _p(f32(nprev)), _p(f32(pose24)), C.byref(intr),
+                     dist, angle, _p(sums), _p(mask))
+    return sums, mask
+
+
+def icp_solve(sums, R, t):
+    R = np.ascontiguousarray(R, np.float64).copy()
+    t = np.ascontiguousarray(t, np.float64).copy()
+    x = np.zeros(6, np.float64)
+    st = lib.or_icp_solve(_p(np.ascontiguousarray(sums, np.float64)), _p(R), _p(t), _p(x))
+    return st, R, t, x
+
+
+def integrate(depth_scaled, vol, fmt, trunc, R_inv, t, intr, cell, rb, max_weight=128):
+    stats = np.zeros(2, np.uint64)
+    lib.or_integrate(_p(f32(depth_scaled)), _p(vol), fmt, trunc, _p(f32(R_inv)), _p(f32(t)), C.byref(intr),
+                     _p(f32(cell)), C.byref(rb), max_weight, _p(stats))
+    return stats
+
+
+def resize_map(src, normal):
+    H, W, _ = src.shape
+    dst = np.empty((H >> 1, W >> 1, 3), F32)
+    lib.or_resize_map(_p(f32(src)), _p(dst), W, H, int(normal))
+    return dst
+
+
+def transform_maps(vs, ns, R, t):
+    H, W, _ = vs.shape
+    vd, nd = np.empty_like(vs), np.empty_like(ns)
+    lib.or_transform_maps(_p(f32(vs)), _p(f32(ns)), _p(vd), _p(nd), _p(f32(R)), _p(f32(t)), W, H)
+    return vd, nd
+
+
+def transform_estimation(gbuf, length, stride=1200):
+    out = np.empty(27, F32)
+    lib.or_transform_estimation(_p(f32(gbuf)), _p(out), length, stride)
+    return out
+
+
+def chunk_depth(depth: int) -> int:
+    """determine_extract_step(depth, divisor 4) of common/src/mem_utils.cpp:43-85;
+    64-voxel chunks for other depths divisible by 64, else one chunk."""
+    table = {512: 64, 256: 32, 128: 16}
+    if depth in table:
+        return table[depth]
+    return 64 if depth % 64 == 0 else depth
+
+
+def extract_slice(vol, fmt, color, mn, mx, rb, capacity=None, weights=False):
+    step = chunk_depth(rb.voxels_size[2])
+    mn_a, mx_a = np.array(mn, np.int32), np.array(mx, np.int32)
+    cp = _p(np.ascontiguousarray(color)) if color is not None else None
+    n = lib.or_extract_slice(_p(vol), fmt, cp, _p(mn_a), _p(mx_a), C.byref(rb), step, None, None, None, 0)
+    cap = n if capacity is None else capacity
+    pts = np.zeros((max(cap, 1), 4), F32)
+    cols = np.zeros((max(cap, 1), 4), np.uint8)
+    wts = np.zeros(max(cap, 1), F32) if weights else None
+    lib.or_extract_slice(_p(vol), fmt, cp, _p(mn_a), _p(mx_a), C.byref(rb), step, _p(pts), _p(cols), _p(wts), cap)
+    k = min(n, cap)
+    return pts[:k], cols[:k], (wts[:k] if weights else None), n
+
+
+def clean_tsdf_slice(vol, fmt, mn, mx, rb):
+    lib.or_clean_tsdf_slice(_p(vol), fmt, _p(np.array(mn, np.int32)), _p(np.array(mx, np.int32)), C.byref(rb))
+
+
+def clean_color_slice(color, mn, mx, rb):
+    lib.or_clean_color_slice(_p(color), _p(np.array(mn, np.int32)), _p(np.array(mx, np.int32)), C.byref(rb))
+
+
+def render_depth(scene, pose12, intr):
+    out = np.empty((intr.rows, intr.cols), F32)
+    sc = np.ascontiguousarray(scene, np.float64)
+    lib.or_render_depth(_p(sc), sc.shape[0], _p(np.ascontiguousarray(pose12, np.float64)), C.byref(intr), _p(out))
+    return out
+
+
+def apply_noise(depth_m, seed, frame, max_range=4.0, dropout=0.02):
+    H, W = depth_m.shape
+    out = np.empty((H, W), np.uint16)
+    lib.or_apply_noise(_p(f32(depth_m)), _p(out), W, H, seed & 0xFFFFFFFF, frame & 0xFFFFFFFF, max_range, dropout)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# The reference's kernels compiled as C (present only where the reference
+# tree was available at build time).
+# ---------------------------------------------------------------------------
+def ref_available() -> bool:
+    return (REF_DIR / "ref_raycast.so").exists()
+
+
+_ref_cache = {}
+
+
+def ref(name: str) -> C.CDLL:
+    if name not in _ref_cache:
+        _ref_cache[name] = C.CDLL(str(REF_DIR / f"ref_{name}.so"))
+    return _ref_cache[name]

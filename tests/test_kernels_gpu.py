@@ -1,0 +1,277 @@
+"""CUDA kernels through the C-ABI against the CPU oracle and the golden
+vectors of the reference kernels.  Tolerances are stated per test; integer,
+index and float paths evaluated with identical IEEE operations are compared
+bit for bit."""
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+syn = importlib.import_module("3deye_gb300.synth")
+
+
+def T(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def N(t):
+    return t.detach().cpu().numpy()
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32))
+
+
+def tintr(tde, o):
+    return tde.Intrinsics(o.fx, o.fy, o.cx, o.cy, o.cols, o.rows)
+
+
+def trb(tde, o):
+    rb = tde.round_buffer(tuple(o.voxels_size), tuple(o.volume_size), tuple(o.origin_GRID))
+    return rb
+
+
+# ---------------------------------------------------------------------------
+# shared small scene
+# ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def small(orc):
+    cfg = syn.small_config("c1", frames=6, cols=160, rows=120, voxels=64)
+    scene = syn.make_scene(cfg, 1000)
+    traj = syn.make_trajectory(cfg, 2000)
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    depths = [orc.apply_noise(orc.render_depth(scene, traj[i], intr), 3000, i) for i in range(cfg.frames)]
+    return cfg, scene, traj, intr, depths
+
+
+def pose_parts(p12):
+    R = p12[:9].reshape(3, 3).astype(np.float32)
+    t = p12[9:].astype(np.float32)
+    return R, t
+
+
+def oracle_volume(orc, cfg, intr, depths, traj, fmt, origin=(0, 0, 0), nframes=3):
+    rb = orc.make_rb((cfg.voxels,) * 3, (cfg.volume_m,) * 3, origin)
+    vol = np.zeros(orc.volume_bytes(fmt, rb), np.uint8)
+    cell = np.full(3, cfg.cell, np.float32)
+    for i in range(nframes):
+        R, t = pose_parts(traj[i])
+        sd = orc.scale_depth(depths[i], intr)
+        orc.integrate(sd, vol, fmt, cfg.trunc_m, np.ascontiguousarray(R.T), t, intr, cell, rb)
+    return vol, rb, cell
+
+
+# ---------------------------------------------------------------------------
+# raycast
+# ---------------------------------------------------------------------------
+def test_raycast_golden_bit_exact(tde, orc, cuda):
+    g = np.load(GOLDEN / "raycast.npz")
+    for i in range(int(g["ncases"])):
+        k = lambda s: g[f"c{i}_{s}"]
+        Nv, V = int(k("N")), float(k("V"))
+        fx, fy, cx, cy, W, H = k("intr")
+        intr = tde.Intrinsics(fx, fy, cx, cy, int(W), int(H))
+        rb = tde.round_buffer((Nv, Nv, Nv), (V, V, V), tuple(int(v) for v in k("origin")))
+        vol = T(k("vol"), cuda)
+        vm, nm = tde.raycast(vol, tde.TSDF_I16, rb, intr, k("R"), k("t"), float(k("trunc")), (V / Nv,) * 3)
+        assert bits_equal(N(vm), k("vmap")), f"case {i}: vertex map differs from the reference kernel"
+        assert bits_equal(N(nm), k("nmap")), f"case {i}: normal map differs from the reference kernel"
+
+
+@pytest.mark.parametrize("fmt", [0, 1, 2])
+@pytest.mark.parametrize("origin", [(0, 0, 0), (7, 50, 21)])
+def test_integrate_and_raycast_match_oracle(tde, orc, cuda, small, fmt, origin):
+    import torch
+    cfg, scene, traj, intr, depths = small
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt, origin)
+    rb = trb(tde, rb_o)
+    ti = tintr(tde, intr)
+    vol = torch.zeros(tde.tsdf_volume_bytes(fmt, rb), dtype=torch.uint8, device=cuda)
+    tde.tsdf_init(vol, fmt, rb)
+    for i in range(3):
+        R, t = pose_parts(traj[i])
+        sd = tde.scale_depth(T(depths[i], cuda), ti)
+        assert bits_equal(N(sd), orc.scale_depth(depths[i], intr))
+        tde.integrate_tsdf(sd, vol, fmt, cfg.trunc_m, R.T.copy(), t, ti, cell, rb, 128)
+    torch.cuda.synchronize()
+    assert np.array_equal(N(vol), vol_o), "TSDF volume differs from the oracle"
+    R, t = pose_parts(traj[4])
+    vm, nm = tde.raycast(vol, fmt, rb, ti, R, t, cfg.trunc_m, cell)
+    vmo, nmo = orc.raycast(vol_o, fmt, rb_o, intr, R, t, cfg.trunc_m, cell)
+    assert np.isfinite(vmo[..., 0]).sum() > 1000
+    assert bits_equal(N(vm), vmo) and bits_equal(N(nm), nmo)
+
+
+# ---------------------------------------------------------------------------
+# depth preprocessing
+# ---------------------------------------------------------------------------
+def test_bilateral_golden(tde, cuda):
+    g = np.load(GOLDEN / "bilateral.npz")
+    src = T(g["src"], cuda)
+    for name in ("a", "b"):
+        out = N(tde.bilateral_filter(src, None, 4.5, 30.0, int(g[f"{name}_maxd"])))
+        d = np.abs(out.astype(np.int32) - g[f"{name}_intended"].astype(np.int32))
+        # __expf weights vs the reference's exp: results within 1 mm, nearly all exact
+        assert d.max() <= 1
+        assert (d == 0).mean() >= 0.995
+
+
+def test_pyramid_vertex_normal_maps(tde, orc, cuda, small):
+    cfg, scene, traj, intr, depths = small
+    d0 = T(depths[0], cuda)
+    f0 = tde.bilateral_filter(d0, None, cfg.sigma_space, cfg.sigma_color, cfg.max_depth_mm)
+    fo = orc.bilateral(depths[0], cfg.sigma_space, cfg.sigma_color, cfg.max_depth_mm)
+    d = np.abs(N(f0).astype(np.int32) - fo.astype(np.int32))
+    assert d.max() <= 1 and (d == 0).mean() > 0.995
+    f0n = N(f0)
+    lvl = f0
+    lvl_o = f0n
+    for l in range(3):
+        il = intr.level(l)
+        if l > 0:
+            lvl = tde.depth_pyramid_level(lvl, cfg.sigma_color)
+            lvl_o = orc.pyramid(lvl_o, cfg.sigma_color)
+            assert np.array_equal(N(lvl), lvl_o), f"pyramid level {l}"
+        vm = tde.vertex_map(lvl, tintr(tde, il))
+        vmo = orc.vertex_map(lvl_o, il)
+        assert bits_equal(N(vm), vmo), f"vertex map level {l}"
+        nm = N(tde.normal_map(vm))
+        nmo = orc.normal_map(vmo)
+        va, vb = np.isfinite(nm[..., 0]), np.isfinite(nmo[..., 0])
+        assert (va == vb).mean() > 0.999, "normal validity masks"
+        both = va & vb
+        assert both.sum() > 100
+        cosang = np.clip((nm[both] * nmo[both]).sum(-1), -1, 1)
+        ang = np.arccos(cosang)
+        # FP32 closed-form eigenvectors vs FP64 Jacobi: tolerance 1e-2 rad on 99.5% of pixels
+        assert np.quantile(ang, 0.995) < 1e-2, np.quantile(ang, [0.5, 0.99, 0.995, 1.0])
+
+
+def test_resize_and_transform_maps(tde, orc, cuda):
+    g = np.load(GOLDEN / "transform_map.npz")
+    vd, nd = tde.transform_maps(T(g["vs"], cuda), T(g["ns"], cuda), g["R"], g["t"])
+    assert bits_equal(N(vd), g["vd"]) and bits_equal(N(nd), g["nd"])
+    rng = np.random.default_rng(1)
+    v = rng.normal(0, 1, (60, 80, 3)).astype(np.float32)
+    v[rng.uniform(size=(60, 80)) < 0.05, 0] = np.nan
+    assert bits_equal(N(tde.resize_vertex_map(T(v, cuda))), orc.resize_map(v, False))
+    assert bits_equal(N(tde.resize_normal_map(T(v, cuda))), orc.resize_map(v, True))
+
+
+# ---------------------------------------------------------------------------
+# ICP
+# ---------------------------------------------------------------------------
+def test_transform_estimation_golden(tde, cuda):
+    import torch
+    g = np.load(GOLDEN / "transform_estimation.npz")
+    gb = T(g["gbuf"], cuda)
+    for L in (1200, 300, 19):
+        out = N(tde.transform_estimation(gb, L, 1200))
+        np.testing.assert_allclose(out, g[f"out_{L}"], rtol=1e-4, atol=1e-4)
+    cb = T(g["clean_in"], cuda)
+    tde.clean_buff(cb, 300)
+    torch.cuda.synchronize()
+    assert np.array_equal(N(cb), g["clean_out"])
+
+
+def test_estimate_combined_matches_oracle(tde, orc, cuda, small):
+    cfg, scene, traj, intr, depths = small
+    fmt = 2
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt)
+    R1, t1 = pose_parts(traj[2])
+    vprev, nprev = orc.raycast(vol_o, fmt, rb_o, intr, R1, t1, cfg.trunc_m, cell)
+    dcur = orc.bilateral(depths[3], cfg.sigma_space, cfg.sigma_color, cfg.max_depth_mm)
+    vcur = orc.vertex_map(dcur, intr)
+    ncur = N(tde.normal_map(T(vcur, cuda)))  # same normals on both sides
+    R3, t3 = pose_parts(traj[3])
+    Rc = R1 + 0.0
+    tc = t1 + np.float32(0.003)
+    pose = np.concatenate([Rc.ravel(), tc, R1.T.ravel(), t1]).astype(np.float32)
+    sums, mask = orc.icp_terms(vcur, ncur, vprev, nprev, pose, intr, cfg.dist_thresh, cfg.angle_thresh)
+    assert sums[27] > 1000
+    m = N(tde.estimate_combined(T(vcur, cuda), T(ncur, cuda), T(vprev, cuda), T(nprev, cuda), Rc, tc, R1.T.copy(),
+                                t1, tde.Intrinsics(intr.fx, intr.fy, intr.cx, intr.cy, intr.cols, intr.rows),
+                                cfg.dist_thresh, cfg.angle_thresh))
+    ref = sums[:27]
+    scale = np.abs(ref).max()
+    # compensated FP32 (TwoSum pairs) vs FP64 sums of the same float terms
+    np.testing.assert_allclose(m, ref, rtol=1e-6, atol=1e-7 * scale)
+
+
+# ---------------------------------------------------------------------------
+# slab extraction / cleaning
+# ---------------------------------------------------------------------------
+def slice_golden(tde):
+    g = np.load(GOLDEN / "slices.npz")
+    W, H, D = (int(v) for v in g["dims"])
+    rb = tde.round_buffer((W, H, D), (2.0, 2.0, 2.0), tuple(int(v) for v in g["origin"]))
+    return g, rb
+
+
+def test_extract_slice_golden_bit_exact(tde, cuda):
+    g, rb = slice_golden(tde)
+    tsdf, color = T(g["tsdf"], cuda), T(g["color"], cuda)
+    for ci in range(int(g["ncases"])):
+        pts, cols, _, n = tde.extract_slice(tsdf, tde.TSDF_I16, color, g[f"c{ci}_mn"], g[f"c{ci}_mx"], rb)
+        assert n == int(g[f"c{ci}_count"])
+        assert np.array_equal(N(pts).view(np.uint32), g[f"c{ci}_points"].view(np.uint32))
+        assert np.array_equal(N(cols), g[f"c{ci}_colors"])
+
+
+def test_extract_slice_capacity_and_no_color(tde, orc, cuda):
+    g, rb = slice_golden(tde)
+    tsdf = T(g["tsdf"], cuda)
+    mn, mx = g["c1_mn"], g["c1_mx"]
+    full = g["c1_points"]
+    pts, cols, _, n = tde.extract_slice(tsdf, tde.TSDF_I16, T(g["color"], cuda), mn, mx, rb, capacity=100)
+    assert n == len(full) and len(pts) == 100
+    assert np.array_equal(N(pts).view(np.uint32), full[:100].view(np.uint32))
+    ob = orc.make_rb(tuple(rb.voxels_size.__getattribute__(a) for a in "xyz"), (2.0, 2.0, 2.0),
+                     tuple(int(v) for v in g["origin"]))
+    po, co, wo, no = orc.extract_slice(np.ascontiguousarray(g["tsdf"]), 0, None, mn, mx, ob, weights=True)
+    pts, cols, w, n = tde.extract_slice(tsdf, tde.TSDF_I16, None, mn, mx, rb, weights=True)
+    assert n == no and np.array_equal(N(pts), po) and np.array_equal(N(w), wo)
+    assert not N(cols).any()
+
+
+def test_extract_slice_empty_zone(tde, cuda):
+    g, rb = slice_golden(tde)
+    pts, cols, _, n = tde.extract_slice(T(g["tsdf"], cuda), 0, T(g["color"], cuda), (-50, -50, -50),
+                                        (-60, -60, -60), rb)
+    assert n == 0 and len(pts) == 0
+
+
+@pytest.mark.parametrize("fmt", [1, 2])
+def test_extract_and_clean_formats_match_oracle(tde, orc, cuda, small, fmt):
+    import torch
+    cfg, scene, traj, intr, depths = small
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt, origin=(3, 60, 9))
+    rb = trb(tde, rb_o)
+    mn, mx = (10, 70, -1000), (20, 75, -1001)
+    po, co, wo, no = orc.extract_slice(vol_o, fmt, None, mn, mx, rb_o, weights=True)
+    assert no > 50
+    vol = T(vol_o, cuda)
+    pts, cols, w, n = tde.extract_slice(vol, fmt, None, mn, mx, rb, weights=True)
+    assert n == no and np.array_equal(N(pts), po) and np.array_equal(N(w), wo)
+    orc.clean_tsdf_slice(vol_o, fmt, mn, mx, rb_o)
+    tde.clean_tsdf_slice(vol, fmt, mn, mx, rb)
+    torch.cuda.synchronize()
+    assert np.array_equal(N(vol), vol_o)
+
+
+def test_clean_color_slice_golden(tde, cuda):
+    import torch
+    g, rb = slice_golden(tde)
+    for ci in range(int(g["ncases"])):
+        c = T(g["color"], cuda)
+        tde.clean_color_slice(c, g[f"c{ci}_mn"], g[f"c{ci}_mx"], rb)
+        torch.cuda.synchronize()
+        assert np.array_equal(N(c), g[f"c{ci}_color_cleaned"])
