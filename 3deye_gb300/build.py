@@ -70,12 +70,15 @@ def build_library(verbose: bool = False) -> Path:
         objs.append(obj)
         if not _stale(obj, [src, Path(__file__)] + headers):
             continue
+        if u.endswith(".cpp"):
+            # host-only C++ (the reference API layer): no CUDA headers
+            cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",
+                   "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)]
+            jobs.append(cmd)
+            continue
         cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
                "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-I", str(CSRC),
                "-c", str(src), "-o", str(obj)]
-        if u.endswith(".cpp"):
-            cmd.insert(1, "-x")
-            cmd.insert(2, "cu")
         if u in NO_FMAD:
             cmd.append("-fmad=false")
         jobs.append(cmd)

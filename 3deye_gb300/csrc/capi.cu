@@ -354,4 +354,43 @@ int tde_clean_color_slice(tde_color *color_volume, tde_point3i min_bounds, tde_p
     return launch_clean_color_slice(color_volume, min_bounds, max_bounds, *rb, as_stream(stream));
 }
 
+// ---------------------------------------------------------------------------
+int tde_device_malloc(void **ptr, size_t bytes) {
+    TDE_REQUIRE(ptr, "device_malloc: null");
+    cudaError_t e = cudaMalloc(ptr, bytes ? bytes : 1);
+    if (e != cudaSuccess)
+        return set_error(e == cudaErrorMemoryAllocation ? TDE_ERR_OOM : TDE_ERR_CUDA, "device_malloc(%zu): %s", bytes,
+                         cudaGetErrorString(e));
+    return TDE_OK;
+}
+
+int tde_device_free(void *ptr) {
+    cudaError_t e = cudaFree(ptr);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "device_free: %s", cudaGetErrorString(e));
+    return TDE_OK;
+}
+
+int tde_memcpy(void *dst, const void *src, size_t bytes, int kind) {
+    TDE_REQUIRE((dst && src) || bytes == 0, "memcpy: null pointer");
+    TDE_REQUIRE(kind >= 0 && kind <= 2, "memcpy: bad kind %d", kind);
+    const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost
+                                                                              : cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaMemcpy(dst, src, bytes, k);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "memcpy: %s", cudaGetErrorString(e));
+    return TDE_OK;
+}
+
+int tde_memset(void *ptr, int value, size_t bytes) {
+    TDE_REQUIRE(ptr || bytes == 0, "memset: null pointer");
+    cudaError_t e = cudaMemset(ptr, value, bytes);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+    return TDE_OK;
+}
+
+int tde_device_synchronize(void) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "synchronize: %s", cudaGetErrorString(e));
+    return TDE_OK;
+}
+
 }  // extern "C"

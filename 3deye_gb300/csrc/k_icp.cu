@@ -55,29 +55,41 @@ __device__ __forceinline__ float3 ld3(const float *p, size_t i) {
     return make_float3(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2));
 }
 
-// Per-pixel association; returns false when the pixel is rejected.
-__device__ __forceinline__ bool associate(const IcpArgs &a, const IcpPose &P, int x, int y, float row[7]) {
-    const size_t i = (size_t)y * a.W + x;
-    float3 n = ld3(a.ncur, i);
-    if (isnan(n.x)) return false;
-    float3 v = ld3(a.vcur, i);
-    float3 rv = mv(P.R_cur, v);
-    float3 vg = make_float3(rv.x + P.t_cur[0], rv.y + P.t_cur[1], rv.z + P.t_cur[2]);
-    float3 vcp = mv(P.R_prev_inv, make_float3(vg.x - P.t_prev[0], vg.y - P.t_prev[1], vg.z - P.t_prev[2]));
-    if (!(vcp.z > 0.f)) return false;
-    int u = __float2int_rn(vcp.x * a.fx / vcp.z + a.cx);
-    int w = __float2int_rn(vcp.y * a.fy / vcp.z + a.cy);
-    if (u < 0 || w < 0 || u >= a.W || w >= a.H) return false;
-    const size_t j = (size_t)w * a.W + u;
-    float3 np = ld3(a.nprev, j);
+// Per-pixel association, split in two so a thread can issue the loads of all
+// its pixels before it needs any of them.
+struct Assoc {
+    float3 vg;    // current vertex, global frame
+    float3 ng;    // current normal, global frame
+    int j;        // model pixel, -1 when rejected
+};
+
+__device__ __forceinline__ Assoc project(const IcpArgs &a, const IcpPose &P, int p) {
+    Assoc r;
+    r.j = -1;
+    const float3 n = ld3(a.ncur, (size_t)p);
+    const float3 v = ld3(a.vcur, (size_t)p);
+    if (isnan(n.x)) return r;
+    const float3 rv = mv(P.R_cur, v);
+    r.vg = make_float3(rv.x + P.t_cur[0], rv.y + P.t_cur[1], rv.z + P.t_cur[2]);
+    const float3 vcp = mv(P.R_prev_inv, make_float3(r.vg.x - P.t_prev[0], r.vg.y - P.t_prev[1], r.vg.z - P.t_prev[2]));
+    if (!(vcp.z > 0.f)) return r;
+    const int u = __float2int_rn(vcp.x * a.fx / vcp.z + a.cx);
+    const int w = __float2int_rn(vcp.y * a.fy / vcp.z + a.cy);
+    if (u < 0 || w < 0 || u >= a.W || w >= a.H) return r;
+    r.ng = mv(P.R_cur, n);
+    r.j = w * a.W + u;
+    return r;
+}
+
+// Tests against the model point and writes the Jacobian row [vg x np, np]
+// and residual np . (vp - vg); false when the pair is rejected.
+__device__ __forceinline__ bool pair_terms(const IcpArgs &a, const Assoc &s, float3 np, float3 vp, float row[7]) {
     if (isnan(np.x)) return false;
-    float3 vp = ld3(a.vprev, j);
-    float3 dv = make_float3(vp.x - vg.x, vp.y - vg.y, vp.z - vg.z);
+    const float3 dv = make_float3(vp.x - s.vg.x, vp.y - s.vg.y, vp.z - s.vg.z);
     if (sqrtf(dot3(dv, dv)) > a.dist_thresh) return false;
-    float3 ng = mv(P.R_cur, n);
-    float3 cr = cross3(ng, np);
+    const float3 cr = cross3(s.ng, np);
     if (sqrtf(dot3(cr, cr)) >= a.angle_thresh) return false;
-    float3 c = cross3(vg, np);
+    const float3 c = cross3(s.vg, np);
     row[0] = c.x; row[1] = c.y; row[2] = c.z;
     row[3] = np.x; row[4] = np.y; row[5] = np.z;
     row[6] = dot3(np, dv);
@@ -94,7 +106,7 @@ __device__ bool solve_and_update(IcpState *st) {
             double v = st->sums[s++];
             if (j == 6) b[k] = v; else { A[k][j] = v; A[j][k] = v; }
         }
-    double L[6][6];
+    double L[6][6], inv_d[6];
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j <= i; ++j) {
             double acc = A[i][j];
@@ -102,20 +114,21 @@ __device__ bool solve_and_update(IcpState *st) {
             if (i == j) {
                 if (!(acc > 1e-30)) return false;
                 L[i][i] = sqrt(acc);
+                inv_d[i] = 1.0 / L[i][i];
             } else {
-                L[i][j] = acc / L[j][j];
+                L[i][j] = acc * inv_d[j];
             }
         }
     double yv[6], x[6];
     for (int i = 0; i < 6; ++i) {
         double acc = b[i];
         for (int k = 0; k < i; ++k) acc -= L[i][k] * yv[k];
-        yv[i] = acc / L[i][i];
+        yv[i] = acc * inv_d[i];
     }
     for (int i = 5; i >= 0; --i) {
         double acc = yv[i];
         for (int k = i + 1; k < 6; ++k) acc -= L[k][i] * x[k];
-        x[i] = acc / L[i][i];
+        x[i] = acc * inv_d[i];
     }
     double Rinc[9];
     so3_exp(x, Rinc);
@@ -131,57 +144,83 @@ __device__ bool solve_and_update(IcpState *st) {
     return true;
 }
 
+// Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
+// five butterfly stages, each halving the values a lane keeps, leave lane l
+// with the warp total of term l as a float-float pair (31 compensated adds
+// and 62 shuffles instead of 32 x 5 of each).
+__device__ __forceinline__ f2 warp_transpose_reduce(const float (&s)[32], int lane) {
+    f2 v[16];
+    {
+        const bool up = lane & 16;
+        #pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const float send = up ? s[i] : s[i + 16];
+            const float keep = up ? s[i + 16] : s[i];
+            v[i] = two_sum(keep, __shfl_xor_sync(0xffffffffu, send, 16));
+        }
+    }
+    #pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) {
+        const bool up = lane & o;
+        #pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const f2 send = up ? v[i] : v[i + o];
+            const f2 keep = up ? v[i + o] : v[i];
+            const f2 recv{__shfl_xor_sync(0xffffffffu, send.hi, o), __shfl_xor_sync(0xffffffffu, send.lo, o)};
+            v[i] = add_ff(keep, recv);
+        }
+    }
+    return v[0];
+}
+
 template <bool SOLVE>
 __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState *__restrict__ st,
                                                        float *__restrict__ gbuf, float *__restrict__ mbuf) {
     __shared__ IcpPose P;
-    __shared__ f2 red[kThreads / 32][kIcpTerms];
+    __shared__ f2 red[kThreads / 32][32];
     __shared__ unsigned ticket;
     const int tid = threadIdx.x;
-    if (tid == 0) P = st->pose;
+    const int lane = tid & 31, warp = tid >> 5;
+    if (tid < (int)(sizeof(IcpPose) / sizeof(float)))
+        reinterpret_cast<float *>(&P)[tid] = reinterpret_cast<const float *>(&st->pose)[tid];
     __syncthreads();
 
-    f2 acc[kIcpTerms];
+    float s[32];
     #pragma unroll
-    for (int t = 0; t < kIcpTerms; ++t) acc[t] = f2{0.f, 0.f};
+    for (int t = 0; t < 32; ++t) s[t] = 0.f;
 
     const int npix = a.W * a.H;
     const int base = blockIdx.x * kThreads * kPixPerThread + tid;
-    #pragma unroll 1
+    Assoc as[kPixPerThread];
+    #pragma unroll
     for (int k = 0; k < kPixPerThread; ++k) {
-        int p = base + k * kThreads;
-        if (p >= npix) break;
-        int y = p / a.W, x = p - y * a.W;
+        const int p = base + k * kThreads;
+        if (p < npix) as[k] = project(a, P, p);
+        else as[k].j = -1;
+    }
+    float3 np[kPixPerThread], vp[kPixPerThread];
+    #pragma unroll
+    for (int k = 0; k < kPixPerThread; ++k)
+        if (as[k].j >= 0) { np[k] = ld3(a.nprev, (size_t)as[k].j); vp[k] = ld3(a.vprev, (size_t)as[k].j); }
+    #pragma unroll
+    for (int k = 0; k < kPixPerThread; ++k) {
         float row[7];
-        if (associate(a, P, x, y, row)) {
+        if (as[k].j >= 0 && pair_terms(a, as[k], np[k], vp[k], row)) {
             int t = 0;
             #pragma unroll
             for (int i = 0; i < 6; ++i)
                 #pragma unroll
-                for (int j = i; j < 7; ++j) acc[t] = add_f(acc[t], row[i] * row[j]), ++t;
-            acc[27] = add_f(acc[27], 1.f);
+                for (int j = i; j < 7; ++j) { s[t] = s[t] + row[i] * row[j]; ++t; }
+            s[27] = s[27] + 1.f;
         }
     }
-    // warp reduction of the pairs
-    #pragma unroll
-    for (int t = 0; t < kIcpTerms; ++t) {
-        f2 v = acc[t];
-        #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            f2 o{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
-            v = add_ff(v, o);
-        }
-        acc[t] = v;
-    }
-    const int warp = tid >> 5, lane = tid & 31;
-    if (lane == 0) {
-        #pragma unroll
-        for (int t = 0; t < kIcpTerms; ++t) red[warp][t] = acc[t];
-    }
+    const f2 wsum = warp_transpose_reduce(s, lane);
+    red[warp][lane] = wsum;
     __syncthreads();
     const int nb = gridDim.x;
     if (tid < kIcpTerms) {
         f2 v = red[0][tid];
+        #pragma unroll
         for (int w = 1; w < kThreads / 32; ++w) v = add_ff(v, red[w][tid]);
         gbuf[(size_t)tid * nb + blockIdx.x] = v.hi;
         gbuf[(size_t)(kIcpTerms + tid) * nb + blockIdx.x] = v.lo;

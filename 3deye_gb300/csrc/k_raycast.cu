@@ -88,12 +88,15 @@ constexpr int kBatch = 4;
 template <int FMT>
 __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
                                                      float *__restrict__ nmap, RayParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    // 16x16 pixels per block; each warp takes an 8x4 tile so its rays start
+    // close together and sample neighbouring voxels.
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
     const int W = p.intr.cols, H = p.intr.rows;
     if (p.dpose) {
         __shared__ float s_pose[12];
-        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
         if (tid < 12) s_pose[tid] = tid < 9 ? p.dpose->R[tid] : p.dpose->t[tid - 9];
         __syncthreads();
         p.R = tde_matrix3f{{{s_pose[0], s_pose[1], s_pose[2]}, {s_pose[3], s_pose[4], s_pose[5]},
@@ -281,8 +284,8 @@ int launch_raycast(const void *volume, int format, float *vmap, float *nmap, con
     p.time_step = (float)((double)trunc * 0.8);
     p.max_time = 3.f * ((rb.volume_size.x + rb.volume_size.y) + rb.volume_size.z);
     p.intr = intr; p.rb = rb; p.cell = cell; p.n = voxel_count(rb);
-    dim3 block(32, 8);
-    dim3 grid(div_up(intr.cols, 32), div_up(intr.rows, 8));
+    dim3 block(256);
+    dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, 16));
     return dispatch_format(format, [&](auto F) {
         raycast_kernel<decltype(F)::value><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
         return check_launch("raycast");

@@ -1,0 +1,465 @@
+// pipeline.cu -- the per-frame loop (tde_pipeline.h): buffers, the launch
+// sequence of one frame, its CUDA-graph capture, live timing.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/tde_pipeline.h"
+#include "tde_common.cuh"
+#include "tde_icp.cuh"
+#include "tde_integrate.cuh"
+#include "tde_launch.cuh"
+
+namespace tde {
+namespace {
+
+struct FrameOut {
+    double pose[12];
+    int status;
+    int inliers;
+};
+
+// Snapshot of the previous frame's pose, in the ICP state's spare fields.
+struct PrevPose {
+    double R[9], t[3];
+};
+
+__global__ void begin_frame_kernel(IcpState *st, PrevPose *prev) {
+    for (int k = 0; k < 9; ++k) {
+        prev->R[k] = st->R[k];
+        st->pose.R_prev_inv[k] = (float)st->R[3 * (k % 3) + k / 3];
+        st->pose.R_cur[k] = (float)st->R[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+        prev->t[k] = st->t[k];
+        st->pose.t_prev[k] = (float)st->t[k];
+        st->pose.t_cur[k] = (float)st->t[k];
+    }
+    st->status = 0;
+    st->iterations = 0;
+    st->counter = 0u;
+}
+
+// Accept or reject the frame's ICP estimate and publish the camera pose.
+__global__ void finalize_kernel(IcpState *st, const PrevPose *prev, CamPose *cam, FrameOut *out, int tracked) {
+    int status = 0;
+    if (tracked && (st->status & kIcpStatusSolveFailed)) {
+        for (int k = 0; k < 9; ++k) st->R[k] = prev->R[k];
+        for (int k = 0; k < 3; ++k) st->t[k] = prev->t[k];
+        status |= TDE_FRAME_TRACKING_LOST;
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            cam->R[3 * r + c] = (float)st->R[3 * r + c];
+            cam->R_inv[3 * r + c] = (float)st->R[3 * c + r];
+        }
+    for (int k = 0; k < 3; ++k) cam->t[k] = (float)st->t[k];
+    cam->tracking_ok = status == 0;
+    for (int k = 0; k < 9; ++k) out->pose[k] = st->R[k];
+    for (int k = 0; k < 3; ++k) out->pose[9 + k] = st->t[k];
+    out->status = status;
+    out->inliers = st->inliers;
+}
+
+enum Segment { SEG_TRACK_FIRST, SEG_TRACK, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE, SEG_COUNT };
+
+}  // namespace
+}  // namespace tde
+
+using namespace tde;
+
+struct tde_pipeline {
+    tde_pipeline_config cfg;
+    tde_round_buffer rb;
+    tde_point3f cell;
+    cudaStream_t stream = nullptr;
+    int levels = 3;
+    tde_intrinsics intr[3];
+    // device buffers
+    uint16_t *raw = nullptr;
+    uint16_t *depth[3] = {};
+    float *scaled = nullptr;
+    float *vcur[3] = {}, *ncur[3] = {}, *vmod[3] = {}, *nmod[3] = {};
+    float *gbuf = nullptr;
+    IcpState *st = nullptr;
+    PrevPose *prev = nullptr;
+    CamPose *cam = nullptr;
+    FrameOut *out = nullptr;
+    unsigned long long *stats = nullptr;
+    void *volume = nullptr;
+    // graphs: per segment and the whole frame
+    cudaGraphExec_t seg_exec[SEG_COUNT] = {};
+    cudaGraphExec_t full_exec[2] = {};  // [first frame, tracked frame]
+    bool captured = false;
+    int frames = 0;
+    // timing
+    int timing_cap = 0, timing_n = 0;
+    std::vector<cudaEvent_t> ev;  // 4 per timed frame
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return set_error(e == cudaErrorMemoryAllocation ? TDE_ERR_OOM : TDE_ERR_CUDA, "%s: %s", what,
+                     cudaGetErrorString(e));
+}
+
+#define TDE_CUDA(call, what)                           \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+#define TDE_TRY(call)                                  \
+    do {                                               \
+        int s_ = (call);                               \
+        if (s_ != TDE_OK) return s_;                   \
+    } while (0)
+
+template <class T> int dalloc(T **p, size_t count, const char *what) {
+    TDE_CUDA(cudaMalloc((void **)p, count * sizeof(T)), what);
+    return TDE_OK;
+}
+
+int record_segment(tde_pipeline *p, Segment seg) {
+    const tde_pipeline_config &c = p->cfg;
+    cudaStream_t s = p->stream;
+    const int W = c.intr.cols, H = c.intr.rows;
+    switch (seg) {
+    case SEG_TRACK_FIRST:
+    case SEG_TRACK: {
+        TDE_TRY(launch_bilateral(p->raw, p->depth[0], W, H, c.sigma_space, c.sigma_color, c.max_depth_mm, p->vcur[0],
+                                 &p->intr[0], s));
+        for (int l = 1; l < p->levels; ++l)
+            TDE_TRY(launch_pyramid(p->depth[l - 1], p->depth[l], p->intr[l - 1].cols, p->intr[l - 1].rows,
+                                   c.sigma_color, p->vcur[l], &p->intr[l], s));
+        for (int l = 0; l < p->levels; ++l)
+            TDE_TRY(launch_normal_map(p->vcur[l], p->ncur[l], p->intr[l].cols, p->intr[l].rows, s));
+        begin_frame_kernel<<<1, 1, 0, s>>>(p->st, p->prev);
+        TDE_TRY(check_launch("begin_frame"));
+        if (seg == SEG_TRACK) {
+            for (int l = p->levels - 1; l >= 0; --l) {
+                IcpArgs a;
+                a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
+                a.W = p->intr[l].cols; a.H = p->intr[l].rows;
+                a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
+                a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
+                for (int it = 0; it < c.icp_iters[l]; ++it) TDE_TRY(launch_icp(a, p->st, p->gbuf, nullptr, true, s));
+            }
+        }
+        finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_TRACK);
+        TDE_TRY(check_launch("finalize_pose"));
+        return launch_scale_depth(p->raw, p->scaled, p->intr[0], s);
+    }
+    case SEG_INTEGRATE: {
+        IntegrateParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.trunc = c.trunc; P.max_weight = c.max_weight; P.intr = p->intr[0]; P.rb = p->rb; P.cell = p->cell;
+        P.n = voxel_count(p->rb); P.dpose = p->cam;
+        return launch_integrate(p->scaled, p->volume, c.tsdf_format, P, p->stats, s);
+    }
+    case SEG_RAYCAST: {
+        tde_point3f t0{0, 0, 0};
+        tde_matrix3f R0{};
+        return launch_raycast(p->volume, c.tsdf_format, p->vmod[0], p->nmod[0], t0, R0, c.trunc, p->intr[0], p->rb,
+                              p->cell, p->cam, s);
+    }
+    case SEG_RESIZE:
+        for (int l = 1; l < p->levels; ++l) {
+            TDE_TRY(launch_resize_map(p->vmod[l - 1], p->vmod[l], p->intr[l - 1].cols, p->intr[l - 1].rows, false, s));
+            TDE_TRY(launch_resize_map(p->nmod[l - 1], p->nmod[l], p->intr[l - 1].cols, p->intr[l - 1].rows, true, s));
+        }
+        return TDE_OK;
+    default:
+        return set_error(TDE_ERR_INVALID_ARG, "bad segment");
+    }
+}
+
+int capture(tde_pipeline *p, const Segment *segs, int n, cudaGraphExec_t *exec) {
+    cudaGraph_t g = nullptr;
+    TDE_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int st = TDE_OK;
+    for (int i = 0; i < n && st == TDE_OK; ++i) st = record_segment(p, segs[i]);
+    cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+    if (st != TDE_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+    return TDE_OK;
+}
+
+void drop_graphs(tde_pipeline *p) {
+    for (auto &x : p->seg_exec)
+        if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    for (auto &x : p->full_exec)
+        if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    p->captured = false;
+}
+
+int capture_all(tde_pipeline *p) {
+    drop_graphs(p);
+    for (int sgi = 0; sgi < SEG_COUNT; ++sgi) {
+        Segment sg = (Segment)sgi;
+        TDE_TRY(capture(p, &sg, 1, &p->seg_exec[sgi]));
+    }
+    const Segment first[] = {SEG_TRACK_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
+    const Segment track[] = {SEG_TRACK, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
+    TDE_TRY(capture(p, first, 4, &p->full_exec[0]));
+    TDE_TRY(capture(p, track, 4, &p->full_exec[1]));
+    p->captured = true;
+    return TDE_OK;
+}
+
+int run_segment(tde_pipeline *p, Segment s) {
+    if (p->cfg.use_graphs) {
+        TDE_CUDA(cudaGraphLaunch(p->seg_exec[s], p->stream), "graph launch");
+        return TDE_OK;
+    }
+    return record_segment(p, s);
+}
+
+int write_pose(tde_pipeline *p, const double *pose12) {
+    IcpState h;
+    std::memset(&h, 0, sizeof(h));
+    for (int k = 0; k < 9; ++k) h.R[k] = pose12[k];
+    for (int k = 0; k < 3; ++k) h.t[k] = pose12[9 + k];
+    for (int k = 0; k < 9; ++k) h.pose.R_cur[k] = (float)pose12[k];
+    for (int k = 0; k < 3; ++k) h.pose.t_cur[k] = (float)pose12[9 + k];
+    TDE_CUDA(cudaMemcpyAsync(p->st, &h, sizeof(h), cudaMemcpyHostToDevice, p->stream), "pose upload");
+    TDE_CUDA(cudaStreamSynchronize(p->stream), "pose upload");
+    return TDE_OK;
+}
+
+void release(tde_pipeline *p) {
+    if (!p) return;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    drop_graphs(p);
+    for (auto e : p->ev) cudaEventDestroy(e);
+    cudaFree(p->raw);
+    for (int l = 0; l < 3; ++l) {
+        cudaFree(p->depth[l]); cudaFree(p->vcur[l]); cudaFree(p->ncur[l]); cudaFree(p->vmod[l]); cudaFree(p->nmod[l]);
+    }
+    cudaFree(p->scaled); cudaFree(p->gbuf); cudaFree(p->st); cudaFree(p->prev); cudaFree(p->cam); cudaFree(p->out);
+    cudaFree(p->stats); cudaFree(p->volume);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, tde_pipeline **out) {
+    if (!cfg || !pose12 || !out) return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: null argument");
+    const tde_pipeline_config &c = *cfg;
+    if (c.intr.cols <= 0 || c.intr.rows <= 0 || !(c.intr.fx > 0.f) || !(c.intr.fy > 0.f))
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: bad intrinsics");
+    if (c.icp_levels < 1 || c.icp_levels > 3) return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: icp_levels");
+    if (!valid_format(c.tsdf_format)) return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: tsdf_format");
+    if (!(c.trunc > 0.f) || c.max_weight < 1 || c.max_weight > 32767 || !(c.sigma_space > 0.f) ||
+        !(c.sigma_color > 0.f))
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: bad filter / truncation parameters");
+    if ((c.intr.cols >> (c.icp_levels - 1)) < 8 || (c.intr.rows >> (c.icp_levels - 1)) < 8)
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: image too small for the pyramid");
+    for (int l = 0; l < c.icp_levels; ++l)
+        if (c.icp_iters[l] < 0 || c.icp_iters[l] > 100) return set_error(TDE_ERR_INVALID_ARG, "pipeline_create: icp_iters");
+    tde_pipeline *p = new (std::nothrow) tde_pipeline();
+    if (!p) return set_error(TDE_ERR_OOM, "pipeline_create: host allocation");
+    p->cfg = c;
+    p->levels = c.icp_levels;
+    int st = tde_round_buffer_init(&p->rb, c.voxels, c.volume_size);
+    if (st == TDE_OK && !valid_round_buffer(&p->rb)) st = set_error(TDE_ERR_INVALID_ARG, "pipeline_create: volume size");
+    if (st != TDE_OK) { delete p; return st; }
+    p->cell = tde_point3f{c.volume_size.x / c.voxels.x, c.volume_size.y / c.voxels.y, c.volume_size.z / c.voxels.z};
+    for (int l = 0; l < 3; ++l) {
+        int div = 1 << l;
+        p->intr[l] = tde_intrinsics{c.intr.fx / div, c.intr.fy / div, c.intr.cx / div, c.intr.cy / div,
+                                    c.intr.cols >> l, c.intr.rows >> l};
+    }
+    auto fail = [&](int code) { release(p); return code; };
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "stream"));
+    const size_t npx = (size_t)c.intr.cols * c.intr.rows;
+    if ((st = dalloc(&p->raw, npx, "raw depth")) || (st = dalloc(&p->scaled, npx, "scaled depth"))) return fail(st);
+    for (int l = 0; l < p->levels; ++l) {
+        size_t n = (size_t)p->intr[l].cols * p->intr[l].rows;
+        if ((st = dalloc(&p->depth[l], n, "depth pyramid")) || (st = dalloc(&p->vcur[l], 3 * n, "vertex map")) ||
+            (st = dalloc(&p->ncur[l], 3 * n, "normal map")) || (st = dalloc(&p->vmod[l], 3 * n, "model vertices")) ||
+            (st = dalloc(&p->nmod[l], 3 * n, "model normals")))
+            return fail(st);
+    }
+    if ((st = dalloc(&p->gbuf, icp_gbuf_floats(c.intr.cols, c.intr.rows), "icp partials")) ||
+        (st = dalloc(&p->st, 1, "icp state")) || (st = dalloc(&p->prev, 1, "prev pose")) ||
+        (st = dalloc(&p->cam, 1, "camera pose")) || (st = dalloc(&p->out, 1, "frame out")) ||
+        (st = dalloc(&p->stats, 2, "stats")))
+        return fail(st);
+    e = cudaMemsetAsync(p->stats, 0, 2 * sizeof(unsigned long long), p->stream);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "stats"));
+    if (!c.integrate_stats) { cudaFree(p->stats); p->stats = nullptr; }
+    // model maps start empty (NaN) so the first ICP finds nothing before a raycast
+    const size_t vb = tde_tsdf_volume_bytes(c.tsdf_format, &p->rb);
+    e = cudaMalloc(&p->volume, vb);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "TSDF volume"));
+    if ((st = launch_tsdf_init(p->volume, c.tsdf_format, voxel_count(p->rb), p->stream))) return fail(st);
+    if ((st = write_pose(p, pose12))) return fail(st);
+    if (c.use_graphs && (st = capture_all(p))) return fail(st);
+    *out = p;
+    return TDE_OK;
+}
+
+int tde_pipeline_destroy(tde_pipeline *p) {
+    release(p);
+    return TDE_OK;
+}
+
+void *tde_pipeline_stream(tde_pipeline *p) { return p ? (void *)p->stream : nullptr; }
+
+int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose_out12,
+                         int *status_out) {
+    if (!p || !depth) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enqueue: null argument");
+    const size_t bytes = (size_t)p->cfg.intr.cols * p->cfg.intr.rows * sizeof(uint16_t);
+    TDE_CUDA(cudaMemcpyAsync(p->raw, depth, bytes, depth_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             p->stream),
+             "depth upload");
+    const bool first = p->frames == 0;
+    const bool timed = p->timing_n < p->timing_cap;
+    if (p->cfg.use_graphs && !timed) {
+        TDE_CUDA(cudaGraphLaunch(p->full_exec[first ? 0 : 1], p->stream), "graph launch");
+    } else {
+        TDE_TRY(run_segment(p, first ? SEG_TRACK_FIRST : SEG_TRACK));
+        cudaEvent_t *ev = timed ? &p->ev[4 * p->timing_n] : nullptr;
+        if (ev) TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
+        TDE_TRY(run_segment(p, SEG_INTEGRATE));
+        if (ev) TDE_CUDA(cudaEventRecord(ev[1], p->stream), "event");
+        if (ev) TDE_CUDA(cudaEventRecord(ev[2], p->stream), "event");
+        TDE_TRY(run_segment(p, SEG_RAYCAST));
+        if (ev) TDE_CUDA(cudaEventRecord(ev[3], p->stream), "event");
+        TDE_TRY(run_segment(p, SEG_RESIZE));
+        if (timed) p->timing_n++;
+    }
+    if (pose_out12)
+        TDE_CUDA(cudaMemcpyAsync(pose_out12, p->out->pose, sizeof(p->out->pose), cudaMemcpyDeviceToHost, p->stream),
+                 "pose download");
+    if (status_out)
+        TDE_CUDA(cudaMemcpyAsync(status_out, &p->out->status, sizeof(int), cudaMemcpyDeviceToHost, p->stream),
+                 "status download");
+    p->frames++;
+    return TDE_OK;
+}
+
+int tde_pipeline_sync(tde_pipeline *p) {
+    if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_sync: null");
+    TDE_CUDA(cudaStreamSynchronize(p->stream), "pipeline sync");
+    return TDE_OK;
+}
+
+int tde_pipeline_process(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose12, int *status) {
+    TDE_TRY(tde_pipeline_enqueue(p, depth, depth_on_device, nullptr, nullptr));
+    TDE_TRY(tde_pipeline_sync(p));
+    FrameOut o;
+    TDE_CUDA(cudaMemcpy(&o, p->out, sizeof(o), cudaMemcpyDeviceToHost), "frame out");
+    if (pose12) std::memcpy(pose12, o.pose, sizeof(o.pose));
+    if (status) *status = o.status;
+    return TDE_OK;
+}
+
+int tde_pipeline_pose(tde_pipeline *p, double *pose12) {
+    if (!p || !pose12) return set_error(TDE_ERR_INVALID_ARG, "pipeline_pose: null");
+    TDE_TRY(tde_pipeline_sync(p));
+    IcpState h;
+    TDE_CUDA(cudaMemcpy(&h, p->st, sizeof(h), cudaMemcpyDeviceToHost), "pose");
+    std::memcpy(pose12, h.R, 9 * sizeof(double));
+    std::memcpy(pose12 + 9, h.t, 3 * sizeof(double));
+    return TDE_OK;
+}
+
+int tde_pipeline_volume(tde_pipeline *p, void **volume, tde_round_buffer *rb) {
+    if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_volume: null");
+    if (volume) *volume = p->volume;
+    if (rb) *rb = p->rb;
+    return TDE_OK;
+}
+
+int tde_pipeline_model_maps(tde_pipeline *p, int level, const float **vmap, const float **nmap) {
+    if (!p || level < 0 || level >= p->levels) return set_error(TDE_ERR_INVALID_ARG, "pipeline_model_maps: level");
+    if (vmap) *vmap = p->vmod[level];
+    if (nmap) *nmap = p->nmod[level];
+    return TDE_OK;
+}
+
+int tde_pipeline_frame_maps(tde_pipeline *p, int level, const uint16_t **depth, const float **vmap,
+                            const float **nmap) {
+    if (!p || level < 0 || level >= p->levels) return set_error(TDE_ERR_INVALID_ARG, "pipeline_frame_maps: level");
+    if (depth) *depth = p->depth[level];
+    if (vmap) *vmap = p->vcur[level];
+    if (nmap) *nmap = p->ncur[level];
+    return TDE_OK;
+}
+
+int tde_pipeline_frame_count(tde_pipeline *p) { return p ? p->frames : 0; }
+
+int tde_pipeline_enable_timing(tde_pipeline *p, int capacity) {
+    if (!p || capacity < 0) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enable_timing: bad argument");
+    TDE_TRY(tde_pipeline_sync(p));
+    for (auto e : p->ev) cudaEventDestroy(e);
+    p->ev.assign((size_t)4 * capacity, nullptr);
+    for (auto &e : p->ev) TDE_CUDA(cudaEventCreate(&e), "event create");
+    p->timing_cap = capacity;
+    p->timing_n = 0;
+    return TDE_OK;
+}
+
+int tde_pipeline_timings(tde_pipeline *p, float *integrate_ms, float *raycast_ms, int capacity) {
+    if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_timings: null");
+    TDE_TRY(tde_pipeline_sync(p));
+    int n = p->timing_n < capacity ? p->timing_n : capacity;
+    for (int i = 0; i < n; ++i) {
+        if (integrate_ms) TDE_CUDA(cudaEventElapsedTime(&integrate_ms[i], p->ev[4 * i], p->ev[4 * i + 1]), "elapsed");
+        if (raycast_ms) TDE_CUDA(cudaEventElapsedTime(&raycast_ms[i], p->ev[4 * i + 2], p->ev[4 * i + 3]), "elapsed");
+    }
+    return n;
+}
+
+int tde_pipeline_integrate_stats(tde_pipeline *p, uint64_t *rw, int reset) {
+    if (!p || !rw) return set_error(TDE_ERR_INVALID_ARG, "pipeline_integrate_stats: null");
+    if (!p->stats) return set_error(TDE_ERR_UNSUPPORTED, "pipeline_integrate_stats: created without integrate_stats");
+    TDE_TRY(tde_pipeline_sync(p));
+    unsigned long long h[2];
+    TDE_CUDA(cudaMemcpy(h, p->stats, sizeof(h), cudaMemcpyDeviceToHost), "stats");
+    rw[0] = h[0];
+    rw[1] = h[1];
+    if (reset) TDE_CUDA(cudaMemset(p->stats, 0, sizeof(h)), "stats reset");
+    return TDE_OK;
+}
+
+int tde_pipeline_launches_per_frame(tde_pipeline *p) {
+    if (!p) return 0;
+    int icp = 0;
+    for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
+    // bilateral, pyramid levels, normal maps, begin, ICP, finalize, scale,
+    // integrate, raycast, 2 resizes per coarser level
+    return 1 + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
+}
+
+int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {
+    if (!p || !valid_round_buffer(rb)) return set_error(TDE_ERR_INVALID_ARG, "pipeline_set_round_buffer: bad argument");
+    if (rb->voxels_size.x != p->rb.voxels_size.x || rb->voxels_size.y != p->rb.voxels_size.y ||
+        rb->voxels_size.z != p->rb.voxels_size.z)
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_set_round_buffer: the volume resolution cannot change");
+    TDE_TRY(tde_pipeline_sync(p));
+    p->rb = *rb;
+    if (p->cfg.use_graphs) return capture_all(p);
+    return TDE_OK;
+}
+
+int tde_pipeline_set_pose(tde_pipeline *p, const double *pose12) {
+    if (!p || !pose12) return set_error(TDE_ERR_INVALID_ARG, "pipeline_set_pose: null");
+    TDE_TRY(tde_pipeline_sync(p));
+    return write_pose(p, pose12);
+}
+
+}  // extern "C"

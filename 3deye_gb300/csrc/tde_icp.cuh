@@ -43,9 +43,10 @@ __host__ __device__ inline void so3_exp(const double *x, double *R) {
         A = 1.0 - th2 / 6.0;
         B = 0.5 - th2 / 24.0;
     } else {
-        double th = sqrt(th2);
-        A = sin(th) / th;
-        B = (1.0 - cos(th)) / th2;
+        double th = sqrt(th2), sn, cs;
+        sincos(th, &sn, &cs);
+        A = sn / th;
+        B = (1.0 - cs) / th2;
     }
     // R = I + A [w]x + B ([w]x)^2,  ([w]x)^2 = w w^T - th2 I
     R[0] = 1.0 + B * (wx * wx - th2); R[1] = -A * wz + B * wx * wy;       R[2] = A * wy + B * wx * wz;

@@ -1,0 +1,394 @@
+// wrappers.cpp -- the reference's C++ API (include/3deye/) over the C-ABI.
+//
+// Compiled by the host C++ compiler without CUDA headers: the reference
+// defines its own global `dim3`, so this layer reaches the GPU only through
+// tde_capi.h.  Every function completes its GPU work before returning, as the
+// reference's clFinish-after-launch does (common/src/opencl_helper.cpp:662-672).
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/3deye/gpu_array.h"
+#include "../../include/3deye/kernel_manager.h"
+#include "../../include/3deye/matrix.h"
+#include "../../include/3deye/opencl_wrappers.h"
+
+namespace {
+
+int g_tsdf_format = TDE_TSDF_I16;
+
+void check(int status, const char *what) {
+    if (status != TDE_OK) throw std::runtime_error(std::string(what) + ": " + tde_last_error());
+}
+
+void sync(const char *what) { check(tde_device_synchronize(), what); }
+
+const tde_intrinsics *I(const intrinsics &in) { return reinterpret_cast<const tde_intrinsics *>(&in); }
+const tde_matrix3f *M(const matrix_3f &m) { return reinterpret_cast<const tde_matrix3f *>(&m); }
+const tde_point3f *V(const point_3f &p) { return reinterpret_cast<const tde_point3f *>(&p); }
+tde_point3i P3(const point_3i &p) { return tde_point3i{p.x, p.y, p.z}; }
+const tde_round_buffer *RB(const round_buffer *rb) {
+    if (!rb) throw std::runtime_error("null round_buffer");
+    return rb->c_abi();
+}
+
+void *dev(gpu_array_base *a, const char *what) {
+    if (!a || !a->device()) throw std::runtime_error(std::string(what) + ": buffer not allocated on the device");
+    return a->device();
+}
+
+const char *const kKnown[] = {
+    "compute_bilateral_filtering", "compute_depth_pyramid", "compute_vertex_map", "compute_normal_map_eigen",
+    "estimate_combined", "transform_estimation", "clean_buff", "scale_depth", "integrate_tsdf_volume", "raycast",
+    "resize_vertex_map", "resize_normal_map", "transform_map", "scan_slice_of_both_volumes", "extract_slice_as_cloud",
+    "scan_slice_of_tsdf_volume", "extract_tsdf_slice_as_cloud", "scan_pow2", "scan_subarrays", "clean_tsdf_slice",
+    "clean_color_slice", "init_tsdf"};
+
+string base_name(const string &n) {
+    if (n.size() > 3 && n.compare(n.size() - 3, 3, ".cl") == 0) return n.substr(0, n.size() - 3);
+    return n;
+}
+
+// Slab extraction through the C-ABI: count, size, extract (the reference
+// counts, scans and extracts per chunk, opencl_wrappers.cpp:885-955).
+void extract(point_3i mn, point_3i mx, round_buffer *rb, gpu_array_base *vol, gpu_array_base *color,
+             matrix<Point_XYZI> &pts_out, matrix<Point_Color> *cols_out) {
+    const tde_round_buffer *r = RB(rb);
+    size_t sb = tde_extract_slice_scratch_bytes(r);
+    if (!sb) throw std::runtime_error("Extract_Slice: bad round_buffer");
+    void *scratch = nullptr, *cnt = nullptr, *pts = nullptr, *cols = nullptr;
+    check(tde_device_malloc(&scratch, sb), "Extract_Slice");
+    auto release = [&] {
+        tde_device_free(scratch); tde_device_free(cnt); tde_device_free(pts); tde_device_free(cols);
+    };
+    try {
+        check(tde_device_malloc(&cnt, sizeof(uint32_t)), "Extract_Slice");
+        const tde_color *cv = color ? static_cast<const tde_color *>(dev(color, "Extract_Slice colour")) : nullptr;
+        check(tde_extract_slice(dev(vol, "Extract_Slice"), g_tsdf_format, cv, P3(mn), P3(mx), r, scratch, sb, nullptr,
+                                nullptr, nullptr, 0, static_cast<uint32_t *>(cnt), nullptr),
+              "Extract_Slice");
+        uint32_t n = 0;
+        check(tde_memcpy(&n, cnt, sizeof(n), 1), "Extract_Slice");
+        if (n) {
+            check(tde_device_malloc(&pts, (size_t)n * sizeof(tde_xyzi)), "Extract_Slice");
+            if (cols_out) check(tde_device_malloc(&cols, (size_t)n * sizeof(tde_color)), "Extract_Slice");
+            check(tde_extract_slice(dev(vol, "Extract_Slice"), g_tsdf_format, cv, P3(mn), P3(mx), r, scratch, sb,
+                                    static_cast<tde_xyzi *>(pts), static_cast<tde_color *>(cols), nullptr, n,
+                                    static_cast<uint32_t *>(cnt), nullptr),
+                  "Extract_Slice");
+            matrix<Point_XYZI> part(n);
+            check(tde_memcpy(part.data, pts, (size_t)n * sizeof(tde_xyzi), 1), "Extract_Slice");
+            pts_out.extend_from(part);
+            if (cols_out) {
+                matrix<Point_Color> cpart(n);
+                check(tde_memcpy(cpart.data, cols, (size_t)n * sizeof(tde_color), 1), "Extract_Slice");
+                cols_out->extend_from(cpart);
+            }
+        }
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+}
+
+}  // namespace
+
+void tde_cxx_throw_if(int status, const char *what) { check(status, what); }
+
+// ---------------------------------------------------------------------------
+// gpu_array_base (common/src/gpu_array_base.cpp:5-186)
+// ---------------------------------------------------------------------------
+gpu_array_base::~gpu_array_base() { dev_free(); }
+
+void gpu_array_base::set_size(const dim3 &s) {
+    if (s.x == 0 || s.y == 0 || s.z == 0) throw std::runtime_error("gpu_array::set_size: a dimension is zero");
+    sizes = s;
+    total_size = (unsigned)(s.x * s.y * s.z);
+}
+
+void gpu_array_base::dev_alloc() {
+    if (device_ptr) return;
+    check(tde_device_malloc(&device_ptr, bytes()), "gpu_array::dev_alloc");
+    need_to_prepare = false;
+}
+
+void gpu_array_base::dev_free() {
+    if (device_ptr) {
+        tde_device_free(device_ptr);
+        device_ptr = nullptr;
+    }
+}
+
+void gpu_array_base::memcpy_to_dev(void *host_src) {
+    check(tde_memcpy(device_ptr, host_src, bytes(), 0), "gpu_array::memcpy_to_dev");
+}
+
+void gpu_array_base::memcpy_from_dev(void *host_dst) {
+    check(tde_memcpy(host_dst, device_ptr, bytes(), 1), "gpu_array::memcpy_from_dev");
+}
+
+void gpu_array_base::copy_to(gpu_array_base *dst) {
+    if (!dst || dst->bytes() < bytes()) throw std::runtime_error("gpu_array::copy_to: destination too small");
+    check(tde_memcpy(dst->device(), device_ptr, bytes(), 2), "gpu_array::copy_to");
+}
+
+// ---------------------------------------------------------------------------
+// round_buffer (common/src/round_buffer.cpp:5-74)
+// ---------------------------------------------------------------------------
+round_buffer::round_buffer() { set_default_values(); }
+round_buffer::round_buffer(const dim3 &d) {
+    set_default_values();
+    set_voxels_size(d.width, d.height, d.depth);
+    set_memory_index();
+}
+round_buffer::round_buffer(size_t w, size_t h, size_t d) {
+    set_default_values();
+    set_voxels_size(w, h, d);
+    set_memory_index();
+}
+round_buffer::round_buffer(point_3i voxels, point_3f metric) {
+    set_default_values();
+    voxels_size = voxels;
+    volume_size = metric;
+    set_memory_index();
+}
+void round_buffer::set_default_values() {
+    origin_GRID = make_point_3i(0, 0, 0);
+    origin_GRID_global = make_point_3f(0.f, 0.f, 0.f);
+    origin_metric = origin_GRID_global;
+    voxels_size = make_point_3i(512, 512, 512);
+    volume_size = make_point_3f(3.f, 3.f, 3.f);
+    end_index = 0;
+    set_memory_index();
+}
+void round_buffer::set_voxels_size(size_t w, size_t h, size_t d) {
+    voxels_size.x = (int)w;
+    voxels_size.y = (int)h;
+    voxels_size.z = (int)d;
+}
+void round_buffer::set_memory_index() {
+    start_index = 0;
+    buffer_length = voxels_size.x * voxels_size.y * voxels_size.z;
+}
+
+// ---------------------------------------------------------------------------
+// kernel_manager / opencl_kernel
+// ---------------------------------------------------------------------------
+bool tde_kernel_known(const string &name) {
+    string b = base_name(name);
+    for (const char *k : kKnown)
+        if (b == k) return true;
+    return false;
+}
+
+opencl_kernel::opencl_kernel(const string &name, profiling_level) : kernel_name(base_name(name)) {
+    if (!tde_kernel_known(kernel_name)) throw std::runtime_error("Kernel " + name + " Not found!");
+}
+opencl_kernel::~opencl_kernel() {}
+void opencl_kernel::free_args() { num_args = 0; }
+
+kernel_manager::kernel_manager(const string &p, vector<string> &names) : path(p) {
+    for (const string &n : names) {
+        string b = base_name(n);
+        if (!kernels.count(b)) kernels[b] = new opencl_kernel(b);
+    }
+}
+kernel_manager::~kernel_manager() {
+    for (auto &kv : kernels) delete kv.second;
+}
+opencl_kernel *kernel_manager::Get_Kernel(string &name) {
+    auto it = kernels.find(base_name(name));
+    if (it == kernels.end()) throw std::runtime_error("Kernel " + name + " Not found!");
+    it->second->free_args();
+    return it->second;
+}
+opencl_kernel *kernel_manager::Get_Kernel(const char *name) {
+    string s(name);
+    return Get_Kernel(s);
+}
+
+// ---------------------------------------------------------------------------
+// opencl_wrappers (common/src/opencl_wrappers.cpp)
+// ---------------------------------------------------------------------------
+void Set_Tsdf_Storage_Format(int f) {
+    if (f != TDE_TSDF_I16 && f != TDE_TSDF_F16 && f != TDE_TSDF_F32)
+        throw std::runtime_error("Set_Tsdf_Storage_Format: unknown format");
+    g_tsdf_format = f;
+}
+int Get_Tsdf_Storage_Format() { return g_tsdf_format; }
+
+// opencl_wrappers.cpp:21-64
+void Integrate_Tsdf_Data(gpu_array_base *gDepth_Frame, gpu_array_base *gDepth_Frame_Scaled,
+                         gpu_array_base *gTsdf_Volume, intrinsics &Intr, matrix_3f &Rotation_Inverse,
+                         vector_3f &Translation, float Truncation_Distance, point_3f &Cell_Size,
+                         round_buffer *Tsdf_Buffer, kernel_manager *, int) {
+    check(tde_scale_depth(static_cast<const uint16_t *>(dev(gDepth_Frame, "Integrate_Tsdf_Data")),
+                          static_cast<float *>(dev(gDepth_Frame_Scaled, "Integrate_Tsdf_Data")), I(Intr), nullptr),
+          "Integrate_Tsdf_Data");
+    check(tde_integrate_tsdf(static_cast<const float *>(gDepth_Frame_Scaled->device()),
+                             dev(gTsdf_Volume, "Integrate_Tsdf_Data"), g_tsdf_format, Truncation_Distance,
+                             M(Rotation_Inverse), V(Translation), I(Intr), V(Cell_Size), RB(Tsdf_Buffer),
+                             MAX_TSDF_WEIGHT, nullptr),
+          "Integrate_Tsdf_Data");
+    sync("Integrate_Tsdf_Data");
+}
+
+// opencl_wrappers.cpp:66-95
+void Raycast(gpu_array_base *gTsdf_Volume, gpu_array_base *Vertex_Map, gpu_array_base *Normal_Map,
+             round_buffer *Round_Buffer, vector_3f &Translation, matrix_3f &Rotation, float Truncation_Distance,
+             intrinsics &Intr, point_3f &Cell_Size, opencl_kernel *) {
+    check(tde_raycast(dev(gTsdf_Volume, "Raycast"), g_tsdf_format, static_cast<float *>(dev(Vertex_Map, "Raycast")),
+                      static_cast<float *>(dev(Normal_Map, "Raycast")), V(Translation), M(Rotation),
+                      Truncation_Distance, I(Intr), RB(Round_Buffer), V(Cell_Size), nullptr),
+          "Raycast");
+    sync("Raycast");
+}
+
+// opencl_wrappers.cpp:97-146; Intr describes the source (finer) level.
+void Resize_Vertex_Map(gpu_array_base *in, gpu_array_base *out, intrinsics &Intr, opencl_kernel *) {
+    check(tde_resize_vertex_map(static_cast<const float *>(dev(in, "Resize_Vertex_Map")),
+                                static_cast<float *>(dev(out, "Resize_Vertex_Map")), Intr.cols, Intr.rows, nullptr),
+          "Resize_Vertex_Map");
+    sync("Resize_Vertex_Map");
+}
+
+void Resize_Normal_Map(gpu_array_base *in, gpu_array_base *out, intrinsics &Intr, opencl_kernel *) {
+    check(tde_resize_normal_map(static_cast<const float *>(dev(in, "Resize_Normal_Map")),
+                                static_cast<float *>(dev(out, "Resize_Normal_Map")), Intr.cols, Intr.rows, nullptr),
+          "Resize_Normal_Map");
+    sync("Resize_Normal_Map");
+}
+
+// opencl_wrappers.cpp:148-179
+void Transform_Maps(gpu_array_base *vs, gpu_array_base *ns, gpu_array_base *vd, gpu_array_base *nd,
+                    matrix_3f &Rotation, vector_3f &Translation, intrinsics &Intr, opencl_kernel *) {
+    check(tde_transform_maps(static_cast<const float *>(dev(vs, "Transform_Maps")),
+                             static_cast<const float *>(dev(ns, "Transform_Maps")),
+                             static_cast<float *>(dev(vd, "Transform_Maps")), static_cast<float *>(dev(nd, "Transform_Maps")),
+                             M(Rotation), V(Translation), Intr.cols, Intr.rows, nullptr),
+          "Transform_Maps");
+    sync("Transform_Maps");
+}
+
+void Integrate_Colors(gpu_array_base *, gpu_array_base *, gpu_array_base *, intrinsics &, matrix_3f &, vector_3f &,
+                      float, int, point_3f, round_buffer *, opencl_kernel *) {
+    throw std::runtime_error("Integrate_Colors: colour integration is not available in this build");
+}
+
+// opencl_wrappers.cpp:216-235; Trunc_Dist is the maximum depth in millimetres.
+void Apply_Billateral_Filtration(gpu_array_base *gDepth, const intrinsics &Intr, float Trunc_Dist, opencl_kernel *,
+                                 gpu_array_base *gDepth_Filtered) {
+    uint32_t maxd = Trunc_Dist > 0.f ? (uint32_t)Trunc_Dist : 0u;
+    check(tde_bilateral_filter(static_cast<const uint16_t *>(dev(gDepth, "Apply_Billateral_Filtration")),
+                               static_cast<uint16_t *>(dev(gDepth_Filtered, "Apply_Billateral_Filtration")), Intr.cols,
+                               Intr.rows, DEFAULT_SIGMA_SPACE, DEFAULT_SIGMA_COLOR, maxd, nullptr),
+          "Apply_Billateral_Filtration");
+    sync("Apply_Billateral_Filtration");
+}
+
+// opencl_wrappers.cpp:245-271
+void Create_Pyramid(vector<gpu_array_base *> &pyr, int levels, intrinsics Intr, kernel_manager *) {
+    if ((int)pyr.size() < levels) throw std::runtime_error("Create_Pyramid: fewer buffers than levels");
+    for (int i = 1; i < levels; ++i)
+        check(tde_depth_pyramid_level(static_cast<const uint16_t *>(dev(pyr[i - 1], "Create_Pyramid")),
+                                      static_cast<uint16_t *>(dev(pyr[i], "Create_Pyramid")), Intr.cols >> (i - 1),
+                                      Intr.rows >> (i - 1), DEFAULT_SIGMA_COLOR, nullptr),
+              "Create_Pyramid");
+    sync("Create_Pyramid");
+}
+
+// opencl_wrappers.cpp:281-305
+void Create_Vertex_Maps(vector<gpu_array_base *> &depths, vector<gpu_array_base *> &vertexes, intrinsics Intr,
+                        int levels, kernel_manager *) {
+    for (int i = 0; i < levels; ++i) {
+        intrinsics li = Intr(i);
+        check(tde_vertex_map(static_cast<const uint16_t *>(dev(depths.at(i), "Create_Vertex_Maps")),
+                             static_cast<float *>(dev(vertexes.at(i), "Create_Vertex_Maps")), I(li), nullptr),
+              "Create_Vertex_Maps");
+    }
+    sync("Create_Vertex_Maps");
+}
+
+// opencl_wrappers.cpp:315-343
+void Create_Normal_Maps(vector<gpu_array_base *> &vertexes, vector<gpu_array_base *> &normals, intrinsics Intr,
+                        int levels, kernel_manager *) {
+    for (int i = 0; i < levels; ++i)
+        check(tde_normal_map(static_cast<const float *>(dev(vertexes.at(i), "Create_Normal_Maps")),
+                             static_cast<float *>(dev(normals.at(i), "Create_Normal_Maps")), Intr.cols >> i,
+                             Intr.rows >> i, nullptr),
+              "Create_Normal_Maps");
+    sync("Create_Normal_Maps");
+}
+
+// opencl_wrappers.cpp:364-438: sums on the GPU, 27 floats back, unpacked
+// into the symmetric A (6x6) and b (6) exactly as the reference does.
+void Estimate_Combined(matrix_3f &Rotation_Current, vector_3f &Translation_Current, gpu_array_base *vcur,
+                       gpu_array_base *ncur, matrix_3f &Rotation_Previous_Inverse, vector_3f &Translation_Previous,
+                       intrinsics &Intr, gpu_array_base *vprev, gpu_array_base *nprev, float Distance_Threshold,
+                       float Angle_Threshold, gpu_array_base *gbuf, gpu_array_base *gMBuf, double *A, double *b,
+                       kernel_manager *) {
+    const size_t need = tde_estimate_combined_gbuf_floats(Intr.cols, Intr.rows) * sizeof(float);
+    if (!gbuf || gbuf->bytes() < need)
+        throw std::runtime_error("Estimate_Combined: gbuf smaller than tde_estimate_combined_gbuf_floats()");
+    if (!gMBuf || gMBuf->bytes() < 27 * sizeof(float)) throw std::runtime_error("Estimate_Combined: gMBuf < 27 floats");
+    check(tde_estimate_combined(static_cast<const float *>(dev(vcur, "Estimate_Combined")),
+                                static_cast<const float *>(dev(ncur, "Estimate_Combined")),
+                                static_cast<const float *>(dev(vprev, "Estimate_Combined")),
+                                static_cast<const float *>(dev(nprev, "Estimate_Combined")), M(Rotation_Current),
+                                V(Translation_Current), M(Rotation_Previous_Inverse), V(Translation_Previous), I(Intr),
+                                Distance_Threshold, Angle_Threshold, static_cast<float *>(dev(gbuf, "Estimate_Combined")),
+                                static_cast<float *>(dev(gMBuf, "Estimate_Combined")), nullptr),
+          "Estimate_Combined");
+    float mbuf[27];
+    check(tde_memcpy(mbuf, gMBuf->device(), sizeof(mbuf), 1), "Estimate_Combined");
+    int shift = 0;
+    for (int k = 0; k < 6; ++k)
+        for (int j = k; j < 7; ++j) {
+            float value = mbuf[shift++];
+            if (j == 6) b[k] = value;
+            else A[j * 6 + k] = A[k * 6 + j] = value;
+        }
+}
+
+void Extract_Tsdf_Volume(round_buffer *, const point_3f &, gpu_array_base *, kernel_manager *, matrix<Point_XYZI> &) {
+    throw std::runtime_error("Extract_Tsdf_Volume: whole-volume export is not available in this build");
+}
+
+// opencl_wrappers.cpp:583-683 (three planes: +x, +y, +z)
+void Extract_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer, point_3f &,
+                        gpu_array_base *gTsdf_Volume, kernel_manager *, matrix<Point_XYZI> &cloud) {
+    extract(Min_Bounds, Max_Bounds, Round_Buffer, gTsdf_Volume, nullptr, cloud, nullptr);
+}
+
+// opencl_wrappers.cpp:856-964
+void Extract_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer, gpu_array_base *gTsdf_Volume,
+                   gpu_array_base *gColor_Volume, point_3f, kernel_manager *, matrix<Point_XYZI> &Vertex_Slice,
+                   matrix<Point_Color> &Color_Slice) {
+    extract(Min_Bounds, Max_Bounds, Round_Buffer, gTsdf_Volume, gColor_Volume, Vertex_Slice, &Color_Slice);
+}
+
+// opencl_wrappers.cpp:835-854
+void Clean_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
+                      gpu_array_base *gTsdf_Volume, opencl_kernel *) {
+    check(tde_clean_tsdf_slice(dev(gTsdf_Volume, "Clean_Tsdf_Slice"), g_tsdf_format, P3(Min_Bounds), P3(Max_Bounds),
+                               RB(Round_Buffer), nullptr),
+          "Clean_Tsdf_Slice");
+    sync("Clean_Tsdf_Slice");
+}
+
+// opencl_wrappers.cpp:814-833
+void Clean_Color_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
+                       gpu_array_base *gColor_Volume, opencl_kernel *) {
+    check(tde_clean_color_slice(static_cast<tde_color *>(dev(gColor_Volume, "Clean_Color_Slice")), P3(Min_Bounds),
+                                P3(Max_Bounds), RB(Round_Buffer), nullptr),
+          "Clean_Color_Slice");
+    sync("Clean_Color_Slice");
+}
+
+// opencl_wrappers.cpp:994-1006: zero 27 rows of gPtr->height() floats.
+void Clean_Buff(gpu_array_base *gPtr, opencl_kernel *) {
+    int width = (int)gPtr->height();
+    check(tde_clean_buff(static_cast<float *>(dev(gPtr, "Clean_Buff")), width, nullptr), "Clean_Buff");
+    sync("Clean_Buff");
+}

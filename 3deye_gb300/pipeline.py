@@ -1,0 +1,161 @@
+"""Host-side handle of the per-frame pipeline (include/tde_pipeline.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._capi import Intrinsics, Point3f, Point3i, RoundBuffer, check, declare, lib
+
+P, I, F = C.c_void_p, C.c_int, C.c_float
+
+
+class PipelineConfig(C.Structure):
+    _fields_ = [("intr", Intrinsics), ("voxels", Point3i), ("volume_size", Point3f), ("tsdf_format", I),
+                ("trunc", F), ("max_weight", I), ("sigma_space", F), ("sigma_color", F),
+                ("max_depth_mm", C.c_uint32), ("icp_levels", I), ("icp_iters", I * 3), ("dist_thresh", F),
+                ("angle_thresh", F), ("use_graphs", I), ("integrate_stats", I)]
+
+
+declare("tde_pipeline_create", I, [C.POINTER(PipelineConfig), P, C.POINTER(P)])
+declare("tde_pipeline_destroy", I, [P])
+declare("tde_pipeline_stream", P, [P])
+declare("tde_pipeline_enqueue", I, [P, P, I, P, P])
+declare("tde_pipeline_sync", I, [P])
+declare("tde_pipeline_process", I, [P, P, I, P, P])
+declare("tde_pipeline_pose", I, [P, P])
+declare("tde_pipeline_volume", I, [P, C.POINTER(P), C.POINTER(RoundBuffer)])
+declare("tde_pipeline_model_maps", I, [P, I, C.POINTER(P), C.POINTER(P)])
+declare("tde_pipeline_frame_maps", I, [P, I, C.POINTER(P), C.POINTER(P), C.POINTER(P)])
+declare("tde_pipeline_frame_count", I, [P])
+declare("tde_pipeline_enable_timing", I, [P, I])
+declare("tde_pipeline_timings", I, [P, P, P, I])
+declare("tde_pipeline_integrate_stats", I, [P, P, I])
+declare("tde_pipeline_launches_per_frame", I, [P])
+declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
+declare("tde_pipeline_set_pose", I, [P, P])
+
+
+def config_from(cfg, use_graphs=True, integrate_stats=False, levels=3) -> PipelineConfig:
+    c = PipelineConfig()
+    c.intr = Intrinsics(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    c.voxels = Point3i(cfg.voxels, cfg.voxels, cfg.voxels)
+    c.volume_size = Point3f(cfg.volume_m, cfg.volume_m, cfg.volume_m)
+    c.tsdf_format = cfg.tsdf_format
+    c.trunc = cfg.trunc_m
+    c.max_weight = cfg.max_weight
+    c.sigma_space = cfg.sigma_space
+    c.sigma_color = cfg.sigma_color
+    c.max_depth_mm = cfg.max_depth_mm
+    c.icp_levels = levels
+    for l in range(3):
+        c.icp_iters[l] = cfg.icp_iters[l] if l < len(cfg.icp_iters) else 0
+    c.dist_thresh = cfg.dist_thresh
+    c.angle_thresh = cfg.angle_thresh
+    c.use_graphs = int(use_graphs)
+    c.integrate_stats = int(integrate_stats)
+    return c
+
+
+class Pipeline:
+    """One KinectFusion reconstruction on the current CUDA device."""
+
+    def __init__(self, cfg, pose12, use_graphs=True, integrate_stats=False):
+        self.cfg = cfg
+        self._c = config_from(cfg, use_graphs, integrate_stats)
+        self._h = P()
+        pose = np.ascontiguousarray(pose12, np.float64)
+        check(lib.tde_pipeline_create(C.byref(self._c), pose.ctypes.data_as(P), C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib.tde_pipeline_destroy(self._h)
+            self._h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib.tde_pipeline_stream(self._h)
+
+    def enqueue(self, depth_ptr: int, on_device: bool, pose_out_ptr=None, status_out_ptr=None):
+        check(lib.tde_pipeline_enqueue(self._h, depth_ptr, int(on_device), pose_out_ptr, status_out_ptr))
+
+    def process(self, depth) -> tuple[np.ndarray, int]:
+        """Blocking: depth is a numpy uint16 array or a CUDA tensor."""
+        pose = np.zeros(12, np.float64)
+        st = C.c_int()
+        if isinstance(depth, np.ndarray):
+            d = np.ascontiguousarray(depth, np.uint16)
+            check(lib.tde_pipeline_process(self._h, d.ctypes.data_as(P), 0, pose.ctypes.data_as(P), C.byref(st)))
+        else:
+            check(lib.tde_pipeline_process(self._h, depth.data_ptr(), 1, pose.ctypes.data_as(P), C.byref(st)))
+        return pose, st.value
+
+    def sync(self):
+        check(lib.tde_pipeline_sync(self._h))
+
+    def pose(self) -> np.ndarray:
+        out = np.zeros(12, np.float64)
+        check(lib.tde_pipeline_pose(self._h, out.ctypes.data_as(P)))
+        return out
+
+    def volume(self):
+        v, rb = P(), RoundBuffer()
+        check(lib.tde_pipeline_volume(self._h, C.byref(v), C.byref(rb)))
+        return v.value, rb
+
+    def model_maps(self, level=0):
+        v, n = P(), P()
+        check(lib.tde_pipeline_model_maps(self._h, level, C.byref(v), C.byref(n)))
+        return v.value, n.value
+
+    def frame_maps(self, level=0):
+        d, v, n = P(), P(), P()
+        check(lib.tde_pipeline_frame_maps(self._h, level, C.byref(d), C.byref(v), C.byref(n)))
+        return d.value, v.value, n.value
+
+    def enable_timing(self, capacity: int):
+        check(lib.tde_pipeline_enable_timing(self._h, capacity))
+
+    def timings(self, capacity: int):
+        a = np.zeros(capacity, np.float32)
+        b = np.zeros(capacity, np.float32)
+        n = lib.tde_pipeline_timings(self._h, a.ctypes.data_as(P), b.ctypes.data_as(P), capacity)
+        if n < 0:
+            check(n)
+        return a[:n], b[:n]
+
+    def integrate_stats(self, reset=False):
+        out = np.zeros(2, np.uint64)
+        check(lib.tde_pipeline_integrate_stats(self._h, out.ctypes.data_as(P), int(reset)))
+        return int(out[0]), int(out[1])
+
+    def launches_per_frame(self) -> int:
+        return lib.tde_pipeline_launches_per_frame(self._h)
+
+    def set_round_buffer(self, rb: RoundBuffer):
+        check(lib.tde_pipeline_set_round_buffer(self._h, C.byref(rb)))
+
+    def set_pose(self, pose12):
+        p = np.ascontiguousarray(pose12, np.float64)
+        check(lib.tde_pipeline_set_pose(self._h, p.ctypes.data_as(P)))
+
+
+def ate_rmse(est: np.ndarray, gt: np.ndarray, align: bool = False) -> float:
+    """Absolute trajectory error (Sturm et al. 2012): RMS of camera-centre
+    differences, optionally after a least-squares rigid alignment (Horn)."""
+    a = np.asarray(est)[:, 9:12]
+    b = np.asarray(gt)[:, 9:12]
+    if align:
+        ma, mb = a.mean(0), b.mean(0)
+        H = (a - ma).T @ (b - mb)
+        U, _, Vt = np.linalg.svd(H)
+        D = np.diag([1, 1, np.sign(np.linalg.det(Vt.T @ U.T))])
+        R = Vt.T @ D @ U.T
+        a = (R @ (a - ma).T).T + mb
+    return float(np.sqrt(np.mean(np.sum((a - b) ** 2, axis=1))))

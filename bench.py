@@ -1,0 +1,369 @@
+"""Benchmark of the per-frame KinectFusion pipeline (plain path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 640x480 / 512^3 FP16+u16 TSDF sequence (seeded synthetic scene,
+orbit and Kinect noise; frames = W + K of one contiguous sequence; one step
+is one frame).  The first W frames warm up (frame 0 initialises the model).
+
+Reported (one JSON line, rank 0):
+  value      frames/s with the depth frames already resident in HBM;
+  e2e        frames/s through the C-ABI pipeline with depth in pinned host
+             memory: every step copies its frame host->device and the frame's
+             pose device->host inside the timed region;
+  roofline   integration kernel (the HBM-bound sweep): algorithmic bytes per
+             launch (4 B/voxel read + 4 B/voxel written for the voxels the
+             update touches, counted live, + the scaled depth map) over its
+             CUDA-event launch time, against MEASURED_PEAKS.json hbm_gbs;
+  cpu_baseline  the CPU oracle of the same pipeline on this host's cores.
+N > 1 runs independent replicas (sequence seed = rank): scaling "weak".
+
+--impl reference runs the CPU implementation of the path (the oracle port:
+the reference's OpenCL kernels cannot run on this host -- no CPU OpenCL
+runtime -- and its host library does not build) on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "frames/s 640x480 @512³ TSDF (plain vs learned-refine, equal ATE); kernel GB/s vs HBM"
+WORKLOAD = "c2"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=590)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-frames", type=int, default=4, help="frames of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """DRAM bytes per integration launch from the committed ncu summary."""
+    p = ROOT / "profiles" / "integrate_c2_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+def make_frames(tde, syn, cfg, nframes, seed_k, dev):
+    """Render the sequence on the GPU sensor; returns (device uint16 [n,H,W], gt poses)."""
+    import numpy as np
+    import torch
+    s_scene, s_traj, s_noise = syn.seeds(seed_k)
+    scene = syn.make_scene(cfg, s_scene)
+    traj = syn.make_trajectory(cfg, s_traj, nframes)
+    tde.lib.tde_synth_depth.restype = C.c_int
+    tde.lib.tde_synth_depth.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(tde.Intrinsics), C.c_uint32,
+                                        C.c_uint32, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    d_scene = torch.from_numpy(scene).to(dev)
+    intr = tde.Intrinsics(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    frames = torch.empty((nframes, cfg.rows, cfg.cols), dtype=torch.uint16, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    for i in range(nframes):
+        pose = np.ascontiguousarray(traj[i])
+        tde.check(tde.lib.tde_synth_depth(d_scene.data_ptr(), scene.shape[0], pose.ctypes.data_as(C.c_void_p),
+                                          C.byref(intr), s_noise, i, cfg.max_depth_mm / 1000.0, 0.02,
+                                          frames[i].data_ptr(), None, stream))
+    torch.cuda.synchronize()
+    return frames, traj, scene
+
+
+def barrier_sync(ws):
+    import torch
+    torch.cuda.synchronize()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_run(cfg, frames_np, traj, nframes):
+    """Oracle pipeline on the host's cores over the first frames."""
+    from oracle import oracle as orc
+    from oracle.pipeline import OraclePipeline
+    cores = orc.set_threads(os.cpu_count() or 1)
+    op = OraclePipeline(cfg, traj[0])
+    op.process(frames_np[0])  # model initialisation, untimed
+    t0 = time.perf_counter()
+    for i in range(1, nframes + 1):
+        op.process(frames_np[i])
+    dt = time.perf_counter() - t0
+    return nframes / dt, cores, dt
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+    tde = importlib.import_module("3deye_gb300")
+    syn = importlib.import_module("3deye_gb300.synth")
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = syn.CONFIGS[WORKLOAD]
+    W, K = args.warmup, args.steps
+    n = W + K
+    frames, traj, _ = make_frames(tde, syn, cfg, n, rank, dev)
+
+    # CPU baseline (rank 0, N = 1 only), before the timed GPU passes
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        fnp = frames[: args.cpu_frames + 1].cpu().numpy()
+        v, cores, dt = cpu_baseline_run(cfg, fnp, traj, args.cpu_frames)
+        cpu = {"value": round(v, 4), "unit": "frames/s", "cores": cores, "kind": "port",
+               "sample": f"frames 1-{args.cpu_frames} of the same sequence through the CPU oracle pipeline "
+                         f"(640x480, 512^3, {cores} OpenMP threads, {dt:.1f} s)"}
+
+    # ---- pass A: frames resident in HBM -----------------------------------
+    p = pl.Pipeline(cfg, traj[0], use_graphs=True, integrate_stats=True)
+    launches = p.launches_per_frame()
+    base = frames.data_ptr()
+    fbytes = cfg.rows * cfg.cols * 2
+    for i in range(W):
+        p.enqueue(base + i * fbytes, True)
+    p.sync()
+    p.integrate_stats(reset=True)
+    p.enable_timing(K)
+    stream = torch.cuda.ExternalStream(p.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier_sync(ws)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for i in range(W, n):
+            p.enqueue(base + i * fbytes, True)
+        e1.record(stream)
+        p.sync()
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ws, ms)
+    integ_ms, ray_ms = p.timings(K)
+    n_read, n_written = p.integrate_stats()
+    pose_a = p.pose()
+    p.close()
+
+    # ---- pass B: end to end through the C-ABI from pinned host memory -------
+    host_frames = torch.empty(frames.shape, dtype=torch.uint16, pin_memory=True)
+    host_frames.copy_(frames.cpu())
+    poses = torch.zeros((n, 12), dtype=torch.float64, pin_memory=True)
+    status = torch.zeros(n, dtype=torch.int32, pin_memory=True)
+    q = pl.Pipeline(cfg, traj[0], use_graphs=True)
+    hb, pb, sb = host_frames.data_ptr(), poses.data_ptr(), status.data_ptr()
+    for i in range(W):
+        q.enqueue(hb + i * fbytes, False, pb + i * 96, sb + i * 4)
+    q.sync()
+    qs = torch.cuda.ExternalStream(q.stream)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier_sync(ws)
+    f0.record(qs)
+    for i in range(W, n):
+        q.enqueue(hb + i * fbytes, False, pb + i * 96, sb + i * 4)
+    f1.record(qs)
+    q.sync()
+    e2e_ms = max_over_ranks(ws, f0.elapsed_time(f1))
+    q.close()
+    est = poses.numpy().copy()
+    lost = int((status.numpy() != 0).sum())
+    deterministic = bool(np.array_equal(est[-1], pose_a))
+    ate = pl.ate_rmse(est, traj)
+
+    if rank != 0:
+        return None
+    hbm, peak_kind = load_peaks()
+    S = 4 if cfg.tsdf_format in (0, 1) else 6
+    k_int = len(integ_ms)
+    int_avg_ms = float(np.mean(integ_ms)) if k_int else float("nan")
+    ray_avg_ms = float(np.mean(ray_ms)) if len(ray_ms) else float("nan")
+    alg_bytes = (S * (n_read + n_written) + 4 * cfg.rows * cfg.cols * k_int) / max(k_int, 1)
+    achieved = alg_bytes / (int_avg_ms * 1e-3) / 1e9
+    traffic = load_traffic()
+    fps = ws * K / (ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": round(fps, 2), "unit": "frames/s", "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": round(ms / K, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (TSDF stored f16+u16)", "data": "synthetic (seeded procedural scene, orbit, Kinect noise)",
+        "config": {"workload": "640x480 depth, 512^3 TSDF over 3 m (fp16+u16), ICP 3 levels 10/5/4, "
+                               f"frames {W}+{K} of one sequence", "global_batch": 1, "frames": n,
+                   "l2": "inputs larger than L2 (512 MiB TSDF volume swept every frame)",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "e2e": {"value": round(ws * K / (e2e_ms * 1e-3), 2), "unit": "frames/s", "h2d_bytes_per_step": fbytes,
+                "d2h_bytes_per_step": 96 + 4},
+        "roofline": {"kernel": "integrate_kernel<fp16>", "bound": "hbm", "achieved": round(achieved, 1),
+                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "traffic": (traffic or {}).get("dram_bytes_per_launch"),
+                     "alg_bytes_per_launch": int(alg_bytes), "avg_launch_ms": round(int_avg_ms, 5),
+                     "voxels_read_per_launch": int(n_read / max(k_int, 1)),
+                     "voxels_written_per_launch": int(n_written / max(k_int, 1))},
+        "kernels_ms_per_frame": {"integrate": round(int_avg_ms, 5), "raycast": round(ray_avg_ms, 5)},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches * K,
+        "ate_m": {"vs_ground_truth": round(ate, 6), "frames_tracking_lost": lost, "deterministic": deterministic},
+    }
+    return line
+
+
+def run_reference(args, ws, rank, local):
+    """CPU implementation of the path on the host cores (rank 0 only)."""
+    if rank != 0:
+        return None
+    import numpy as np
+    syn = importlib.import_module("3deye_gb300.synth")
+    from oracle import oracle as orc
+    from oracle.pipeline import OraclePipeline
+    cfg = syn.CONFIGS[WORKLOAD]
+    cores = orc.set_threads(os.cpu_count() or 1)
+    W, K = args.warmup, args.steps
+    s_scene, s_traj, s_noise = syn.seeds(0)
+    scene = syn.make_scene(cfg, s_scene)
+    budget_s = float(os.environ.get("TDE_REF_BUDGET_S", "150"))
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    traj = syn.make_trajectory(cfg, s_traj, W + K)
+    frames = lambda i: orc.apply_noise(orc.render_depth(scene, traj[i], intr), s_noise, i)
+    op = OraclePipeline(cfg, traj[0])
+    warm = min(W, 2)
+    for i in range(warm):
+        op.process(frames(i))
+    done, t_total = 0, 0.0
+    for i in range(warm, warm + K):
+        d = frames(i)
+        t0 = time.perf_counter()
+        op.process(d)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total > budget_s:
+            break
+    fps = done / t_total
+    sample = (f"{done} of {K} frames (after {warm} warm-up) of the 640x480 / 512^3 sequence through the CPU oracle "
+              f"pipeline, {cores} OpenMP threads, {t_total:.1f} s; the reference's OpenCL kernels need a CPU OpenCL "
+              "runtime absent from this host")
+    return {"metric": METRIC, "value": round(fps, 4), "unit": "frames/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": round(1e3 * t_total / done, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, orbit, Kinect noise)",
+            "config": {"workload": "640x480 depth, 512^3 TSDF over 3 m (fp16+u16), ICP 3 levels 10/5/4",
+                       "global_batch": 1, "parallelism": "cpu"},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init(args)
+    line = run_reference(args, ws, rank, local) if args.impl == "reference" else run_ours(args, ws, rank, local)
+    if line is not None:
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

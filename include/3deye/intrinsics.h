@@ -1,0 +1,2 @@
+/* intrinsics.h -- the reference header name; the types live in tde_types.h. */
+#include "tde_types.h"

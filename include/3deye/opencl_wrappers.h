@@ -1,0 +1,95 @@
+/*
+ * opencl_wrappers.h -- the reference's stage-level free functions
+ * (common/inc/opencl_wrappers.h:10-293) with identical names and parameter
+ * lists, implemented on the GB300 kernels through the C-ABI (../tde_capi.h).
+ *
+ * Semantics follow the reference: every call completes before it returns
+ * (the reference runs clFinish after each launch, opencl_helper.cpp:662-672)
+ * and results that the reference reads back (the ICP sums, slab clouds) are on
+ * the host on return.  `opencl_kernel *` / `kernel_manager *` arguments are
+ * accepted and not needed.  Failures throw std::runtime_error.
+ *
+ * Stages whose kernels the reference does not ship either follow the
+ * KinectFusion method (documented in tde_capi.h) or, outside this path
+ * (colour integration, whole-volume export, shading, RGBD odometry), throw
+ * std::runtime_error("... not available").
+ */
+#ifndef TDE_3DEYE_OPENCL_WRAPPERS_H
+#define TDE_3DEYE_OPENCL_WRAPPERS_H
+
+#include <vector>
+
+#include "kernel_manager.h"
+#include "matrix.h"
+#include "tde_types.h"
+
+using std::vector;
+
+/* TSDF storage of volumes passed to the functions below (TDE_TSDF_I16 is the
+ * reference's Point_Tsdf record and the default). */
+void Set_Tsdf_Storage_Format(int tde_tsdf_format);
+int Get_Tsdf_Storage_Format();
+
+void Integrate_Tsdf_Data(gpu_array_base *gDepth_Frame, gpu_array_base *gDepth_Frame_Scaled,
+                         gpu_array_base *gTsdf_Color_Volume, intrinsics &Intr, matrix_3f &Rotation_Inverse,
+                         vector_3f &Translation, float Truncation_Distance, point_3f &Cell_Size,
+                         round_buffer *Tsdf_Buffer, kernel_manager *Gpu_Methods, int DBG_Frame_Num);
+
+void Raycast(gpu_array_base *gTsdf_Color_Volume, gpu_array_base *Vertex_Map, gpu_array_base *Normal_Map,
+             round_buffer *Round_Buffer, vector_3f &Translation, matrix_3f &Rotation, float Truncation_Distance,
+             intrinsics &Intr, point_3f &Cell_Size, opencl_kernel *raycast_kernel);
+
+void Resize_Vertex_Map(gpu_array_base *Vertex_Map_In, gpu_array_base *Vertex_Map_Out, intrinsics &Intr,
+                       opencl_kernel *resize_vertex_kernel);
+
+void Resize_Normal_Map(gpu_array_base *Normal_Map_In, gpu_array_base *Normal_Map_Out, intrinsics &Intr,
+                       opencl_kernel *resize_normal_kernel);
+
+void Transform_Maps(gpu_array_base *Vertex_Map_Src, gpu_array_base *Normal_Map_Src, gpu_array_base *Vertex_Map_Dst,
+                    gpu_array_base *Normal_Map_Dst, matrix_3f &Rotation, vector_3f &Translation, intrinsics &Intr,
+                    opencl_kernel *transform_maps_kernel);
+
+void Integrate_Colors(gpu_array_base *gTsdf_Color_Volume, gpu_array_base *gRGB_Frame, gpu_array_base *Vertex_Map,
+                      intrinsics &Intr, matrix_3f &Rotation_Inverse, vector_3f &Translation,
+                      float Truncation_Distance, int Max_Weight, point_3f Cell_Size, round_buffer *Round_Buffer,
+                      opencl_kernel *integrate_colors_kernel);
+
+void Apply_Billateral_Filtration(gpu_array_base *gDepth, const intrinsics &Intr, float Trunc_Dist,
+                                 opencl_kernel *billateral_filtering_kernel, gpu_array_base *gDepth_Filtered);
+
+void Create_Pyramid(vector<gpu_array_base *> &depth_pyramids, int Num_Of_Pyramid_Level, intrinsics Intr,
+                    kernel_manager *Gpu_Methods);
+
+void Create_Vertex_Maps(vector<gpu_array_base *> &depths, vector<gpu_array_base *> &vertexes, intrinsics Intr,
+                        int Pyramid_Level_Num, kernel_manager *Gpu_Methods);
+
+void Create_Normal_Maps(vector<gpu_array_base *> &vertexes, vector<gpu_array_base *> &normals, intrinsics Intr,
+                        int Pyramid_Level_Num, kernel_manager *Gpu_Methods);
+
+void Estimate_Combined(matrix_3f &Rotation_Current, vector_3f &Translation_Current,
+                       gpu_array_base *Vertex_Map_Current, gpu_array_base *Normal_Map_Current,
+                       matrix_3f &Rotation_Previous_Inverse, vector_3f &Translation_Previous, intrinsics &Intr,
+                       gpu_array_base *Vertex_Map_Previous, gpu_array_base *Normal_Map_Previous,
+                       float Distance_Threshold, float Angle_Threshold, gpu_array_base *gbuf, gpu_array_base *gMBuf,
+                       double *A, double *b, kernel_manager *Gpu_Methods);
+
+void Extract_Tsdf_Volume(round_buffer *Round_Buffer, const point_3f &Cell_Size, gpu_array_base *gTsdf_Volume,
+                         kernel_manager *Gpu_Methods, matrix<Point_XYZI> &Resulting_Cloud_Parallel);
+
+void Extract_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer, point_3f &Cell_Size,
+                        gpu_array_base *gTsdf_Volume, kernel_manager *Gpu_Methods,
+                        matrix<Point_XYZI> &Resulting_Tsdf_Cloud);
+
+void Extract_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer, gpu_array_base *gTsdf_Volume,
+                   gpu_array_base *gColor_Volume, point_3f Cell_Size, kernel_manager *Gpu_Methods,
+                   matrix<Point_XYZI> &Vertex_Slice, matrix<Point_Color> &Color_Slice);
+
+void Clean_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
+                      gpu_array_base *gTsdf_Volume, opencl_kernel *clean_tsdf_kernel);
+
+void Clean_Color_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
+                       gpu_array_base *gColor_Volume, opencl_kernel *clean_color_kernel);
+
+void Clean_Buff(gpu_array_base *gPtr, opencl_kernel *clean_buff_kernel);
+
+#endif

@@ -255,6 +255,18 @@ int tde_clean_tsdf_slice(void *volume, int format, tde_point3i min_bounds, tde_p
 int tde_clean_color_slice(tde_color *color_volume, tde_point3i min_bounds, tde_point3i max_bounds,
                           const tde_round_buffer *rb, void *stream);
 
+/* ======================================================================== */
+/* Device memory helpers for hosts that do not include the CUDA headers      */
+/* (the C++ layer of include/3deye/ replaces gpu_array_base's cl_mem          */
+/* allocation, common/src/opencl_helper.cpp:344-420, with these).            */
+/* ======================================================================== */
+int tde_device_malloc(void **ptr, size_t bytes);
+int tde_device_free(void *ptr);
+/* kind: 0 host->device, 1 device->host, 2 device->device; synchronous. */
+int tde_memcpy(void *dst, const void *src, size_t bytes, int kind);
+int tde_memset(void *ptr, int value, size_t bytes);
+int tde_device_synchronize(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,102 @@
+/*
+ * tde_pipeline.h -- the per-frame KinectFusion loop on one GPU.
+ *
+ * The reference names this layer (the `fusion` application, Makefile:1-7) but
+ * does not ship it; its order follows the wrapper set of
+ * common/inc/opencl_wrappers.h: bilateral filter + pyramid, vertex and normal
+ * maps, coarse-to-fine ICP (10/5/4 iterations), TSDF integration, raycast of
+ * the model and its map pyramid.
+ *
+ * GB300 design: everything stays on the device; the ICP solve and the pose
+ * update run in FP64 inside the last block of each ICP launch, so one frame is
+ * a fixed sequence of launches with no host round trip.  That sequence is
+ * captured once into CUDA graphs and replayed every frame.  A frame's only
+ * host traffic is the depth upload and the pose download.
+ */
+#ifndef TDE_PIPELINE_H
+#define TDE_PIPELINE_H
+
+#include "tde_capi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tde_pipeline tde_pipeline;
+
+typedef struct tde_pipeline_config {
+    tde_intrinsics intr;         /* level-0 camera */
+    tde_point3i voxels;          /* TSDF resolution */
+    tde_point3f volume_size;     /* metres */
+    int tsdf_format;             /* TDE_TSDF_* */
+    float trunc;                 /* truncation distance, metres */
+    int max_weight;              /* MAX_TSDF_WEIGHT = 128 */
+    float sigma_space;           /* bilateral, pixels */
+    float sigma_color;           /* bilateral and pyramid, millimetres */
+    uint32_t max_depth_mm;       /* depth beyond this is invalid */
+    int icp_levels;              /* 1..3 */
+    int icp_iters[3];            /* per level, level 0 finest: 10, 5, 4 */
+    float dist_thresh;           /* DEFAULT_DISTANCE_THRESHOLD 0.1 m */
+    float angle_thresh;          /* sin(20 deg), DEFAULT_ANGLE_THRESHOLD */
+    int use_graphs;              /* capture each frame's launches into CUDA graphs */
+    int integrate_stats;         /* count voxels read / written by integration */
+} tde_pipeline_config;
+
+/* Frame status bits. */
+#define TDE_FRAME_TRACKING_LOST 1  /* an ICP solve failed: the previous pose was kept */
+
+/* Create a pipeline on the current device.  pose12: initial camera pose,
+ * row-major R (camera -> volume frame) then t (camera centre), FP64. */
+int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, tde_pipeline **out);
+int tde_pipeline_destroy(tde_pipeline *p);
+/* The stream all of the pipeline's work runs on. */
+void *tde_pipeline_stream(tde_pipeline *p);
+
+/* Enqueue one frame.  `depth` is cols x rows uint16 millimetres, on the host
+ * (pinned for an asynchronous upload) or on the device.  When pose_out12 is
+ * not NULL it must be pinned host memory of 12 doubles: the frame's pose is
+ * copied there asynchronously, and *status_out (pinned int, may be NULL) gets
+ * the frame status; the caller synchronises (tde_pipeline_sync) before
+ * reading.  Nothing blocks. */
+int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose_out12,
+                         int *status_out);
+/* Block until all enqueued work is done. */
+int tde_pipeline_sync(tde_pipeline *p);
+/* Blocking convenience: enqueue, wait, return the pose (any host memory). */
+int tde_pipeline_process(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose12,
+                         int *status);
+
+/* Current pose (synchronises). */
+int tde_pipeline_pose(tde_pipeline *p, double *pose12);
+/* The TSDF volume and its round buffer (device pointer, owned by the pipeline). */
+int tde_pipeline_volume(tde_pipeline *p, void **volume, tde_round_buffer *rb);
+/* Model maps (global frame) of pyramid level l from the last raycast. */
+int tde_pipeline_model_maps(tde_pipeline *p, int level, const float **vmap, const float **nmap);
+/* Current-frame filtered depth / vertex / normal maps of level l. */
+int tde_pipeline_frame_maps(tde_pipeline *p, int level, const uint16_t **depth, const float **vmap,
+                            const float **nmap);
+/* Frames processed so far. */
+int tde_pipeline_frame_count(tde_pipeline *p);
+
+/* Live per-kernel timing: with capacity > 0, CUDA events bracket the
+ * integration and raycast launches of the next `capacity` frames. */
+int tde_pipeline_enable_timing(tde_pipeline *p, int capacity);
+/* Milliseconds of the integration and raycast launches of the timed frames
+ * (synchronises); returns the number of frames written. */
+int tde_pipeline_timings(tde_pipeline *p, float *integrate_ms, float *raycast_ms, int capacity);
+/* Voxels read and written by integration since the last reset (needs
+ * integrate_stats; synchronises). */
+int tde_pipeline_integrate_stats(tde_pipeline *p, uint64_t *read_written2, int reset);
+/* Number of kernel launches one tracked frame performs. */
+int tde_pipeline_launches_per_frame(tde_pipeline *p);
+
+/* Replace the volume origin bookkeeping after a cyclic shift (the caller has
+ * extracted and cleaned the outgoing slab); re-captures the graphs. */
+int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb);
+/* Overwrite the current pose (e.g. after a shift of the volume frame). */
+int tde_pipeline_set_pose(tde_pipeline *p, const double *pose12);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,98 @@
+"""The per-frame pipeline (include/tde_pipeline.h) on the GPU against the CPU
+oracle pipeline (FP64 ICP sums and solve) and against itself (graph replay
+vs eager launches, asynchronous vs blocking API)."""
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+syn = importlib.import_module("3deye_gb300.synth")
+
+
+@pytest.fixture(scope="module")
+def seq(orc):
+    cfg = syn.small_config("c1", frames=14, cols=160, rows=120, voxels=96, fmt=2)
+    scene = syn.make_scene(cfg, 1000)
+    traj = syn.make_trajectory(cfg, 2000)
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    depths = [orc.apply_noise(orc.render_depth(scene, traj[i], intr), 3000, i) for i in range(cfg.frames)]
+    return cfg, traj, depths
+
+
+def run_gpu(cfg, traj, depths, use_graphs=True):
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    p = pl.Pipeline(cfg, traj[0], use_graphs=use_graphs)
+    poses, stats = [], []
+    for d in depths:
+        pose, st = p.process(d)
+        poses.append(pose)
+        stats.append(st)
+    p.close()
+    return np.array(poses), stats
+
+
+def test_graph_replay_equals_eager_launches(cuda, seq):
+    cfg, traj, depths = seq
+    a, sa = run_gpu(cfg, traj, depths, True)
+    b, sb = run_gpu(cfg, traj, depths, False)
+    assert np.array_equal(a, b) and sa == sb
+
+
+def test_trajectory_matches_fp64_oracle(cuda, orc, seq):
+    from oracle.pipeline import OraclePipeline
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    gpu, st = run_gpu(cfg, traj, depths)
+    op = OraclePipeline(cfg, traj[0])
+    ref = np.array([op.process(d) for d in depths])
+    assert not any(st) and not any(op.lost)
+    # ATE of the GPU trajectory against the FP64 oracle run: <= 1e-3 m
+    assert pl.ate_rmse(gpu, ref) <= 1e-3, pl.ate_rmse(gpu, ref)
+    # and both track the ground truth
+    assert pl.ate_rmse(gpu, traj) < 0.02, pl.ate_rmse(gpu, traj)
+    Rg = gpu[-1, :9].reshape(3, 3)
+    np.testing.assert_allclose(Rg @ Rg.T, np.eye(3), atol=1e-9)
+
+
+def test_async_enqueue_matches_blocking(cuda, seq):
+    import torch
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    ref, _ = run_gpu(cfg, traj, depths)
+    host = torch.from_numpy(np.stack(depths)).pin_memory()
+    poses = torch.zeros((len(depths), 12), dtype=torch.float64).pin_memory()
+    status = torch.zeros(len(depths), dtype=torch.int32).pin_memory()
+    p = pl.Pipeline(cfg, traj[0], integrate_stats=True)
+    p.enable_timing(len(depths))
+    fb = cfg.rows * cfg.cols * 2
+    for i in range(len(depths)):
+        p.enqueue(host.data_ptr() + i * fb, False, poses.data_ptr() + 96 * i, status.data_ptr() + 4 * i)
+    p.sync()
+    assert np.array_equal(poses.numpy(), ref)
+    assert not status.numpy().any()
+    ti, tr = p.timings(len(depths))
+    assert len(ti) == len(depths) and (ti > 0).all() and (tr > 0).all()
+    r, w = p.integrate_stats()
+    assert r > 0 and 0 < w <= r
+    assert p.launches_per_frame() == 34
+    p.close()
+
+
+def test_tracking_loss_keeps_previous_pose(cuda, seq):
+    """A frame with no valid depth cannot be registered: the pipeline reports
+    it and keeps the previous pose (failure made on the host, no GPU fault)."""
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    p = pl.Pipeline(cfg, traj[0])
+    for d in depths[:3]:
+        pose, st = p.process(d)
+        assert st == 0
+    blank = np.zeros_like(depths[3])
+    pose2, st2 = p.process(blank)
+    assert st2 & 1
+    assert np.array_equal(pose2, pose)
+    pose3, st3 = p.process(depths[4])
+    assert st3 == 0
+    p.close()
