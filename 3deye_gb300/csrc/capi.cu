@@ -7,6 +7,7 @@
 
 #include "tde_common.cuh"
 #include "tde_icp.cuh"
+#include "tde_integrate.cuh"
 #include "tde_launch.cuh"
 #include "tde_slab.cuh"
 
@@ -270,9 +271,9 @@ int tde_scale_depth(const uint16_t *depth, float *scaled, const tde_intrinsics *
     return launch_scale_depth(depth, scaled, *intr, as_stream(stream));
 }
 
-int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
-                       const tde_point3f *t, const tde_intrinsics *intr, const tde_point3f *cell,
-                       const tde_round_buffer *rb, int max_weight, void *stream) {
+static int integrate_checks(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
+                            const tde_point3f *t, const tde_intrinsics *intr, const tde_point3f *cell,
+                            const tde_round_buffer *rb, int max_weight) {
     TDE_REQUIRE(depth_scaled && volume, "integrate: null buffer");
     TDE_REQUIRE(valid_format(format), "integrate: bad format %d", format);
     TDE_REQUIRE(R_inv && t && cell, "integrate: null pose/cell");
@@ -281,12 +282,60 @@ int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, floa
     TDE_REQUIRE(trunc > 0.f && std::isfinite(trunc), "integrate: bad truncation distance");
     TDE_REQUIRE(max_weight >= 1 && max_weight <= 32767, "integrate: bad max weight %d", max_weight);
     TDE_REQUIRE(cell->x > 0.f && cell->y > 0.f && cell->z > 0.f, "integrate: bad cell size");
+    return TDE_OK;
+}
+
+static IntegrateParams integrate_params(float trunc, const tde_matrix3f *R_inv, const tde_point3f *t,
+                                        const tde_intrinsics *intr, const tde_point3f *cell, const tde_round_buffer *rb,
+                                        int max_weight) {
     IntegrateParams P;
     std::memcpy(P.R_inv, &R_inv->row[0].x, sizeof(P.R_inv));
     P.t[0] = t->x; P.t[1] = t->y; P.t[2] = t->z;
     P.trunc = trunc; P.max_weight = max_weight; P.intr = *intr; P.rb = *rb; P.cell = *cell;
     P.n = voxel_count(*rb); P.dpose = nullptr;
-    return launch_integrate(depth_scaled, volume, format, P, nullptr, as_stream(stream));
+    return P;
+}
+
+size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows) {
+    if (cols <= 0 || rows <= 0) return 0;
+    return depth_max_floats(cols, rows) * sizeof(float);
+}
+
+size_t tde_brick_flags_bytes(const tde_round_buffer *rb) {
+    if (!valid_round_buffer(rb)) return 0;
+    return brick_count(*rb);
+}
+
+int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
+                          const tde_point3f *t, const tde_intrinsics *intr, const tde_point3f *cell,
+                          const tde_round_buffer *rb, int max_weight, void *scratch, size_t scratch_bytes,
+                          uint8_t *brick_flags, void *stream) {
+    int st = integrate_checks(depth_scaled, volume, format, trunc, R_inv, t, intr, cell, rb, max_weight);
+    if (st) return st;
+    TDE_REQUIRE(scratch && scratch_bytes >= tde_integrate_tsdf_scratch_bytes(intr->cols, intr->rows),
+                "integrate: scratch smaller than tde_integrate_tsdf_scratch_bytes()");
+    cudaStream_t s = as_stream(stream);
+    float *dmax = static_cast<float *>(scratch);
+    if ((st = launch_depth_max(depth_scaled, intr->cols, intr->rows, dmax, s))) return st;
+    IntegrateParams P = integrate_params(trunc, R_inv, t, intr, cell, rb, max_weight);
+    return launch_integrate(depth_scaled, volume, format, P, dmax, brick_flags, nullptr, s);
+}
+
+int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
+                       const tde_point3f *t, const tde_intrinsics *intr, const tde_point3f *cell,
+                       const tde_round_buffer *rb, int max_weight, void *stream) {
+    int st = integrate_checks(depth_scaled, volume, format, trunc, R_inv, t, intr, cell, rb, max_weight);
+    if (st) return st;
+    cudaStream_t s = as_stream(stream);
+    const size_t sb = tde_integrate_tsdf_scratch_bytes(intr->cols, intr->rows);
+    void *scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    if (e != cudaSuccess) return set_error(TDE_ERR_OOM, "integrate: scratch: %s", cudaGetErrorString(e));
+    st = tde_integrate_tsdf_ex(depth_scaled, volume, format, trunc, R_inv, t, intr, cell, rb, max_weight, scratch, sb,
+                               nullptr, stream);
+    e = cudaFreeAsync(scratch, s);
+    if (st == TDE_OK && e != cudaSuccess) return set_error(TDE_ERR_CUDA, "integrate: %s", cudaGetErrorString(e));
+    return st;
 }
 
 int tde_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t, const tde_matrix3f *R,

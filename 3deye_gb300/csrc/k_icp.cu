@@ -96,51 +96,118 @@ __device__ __forceinline__ bool pair_terms(const IcpArgs &a, const Assoc &s, flo
     return true;
 }
 
-// FP64 Cholesky solve of the 6x6 system and pose update (thread 0 of the last
-// block).  Returns false when A is not positive definite.
-__device__ bool solve_and_update(IcpState *st) {
-    double A[6][6], b[6];
-    int s = 0;
-    for (int k = 0; k < 6; ++k)
-        for (int j = k; j < 7; ++j) {
-            double v = st->sums[s++];
-            if (j == 6) b[k] = v; else { A[k][j] = v; A[j][k] = v; }
-        }
-    double L[6][6], inv_d[6];
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j <= i; ++j) {
-            double acc = A[i][j];
-            for (int k = 0; k < j; ++k) acc -= L[i][k] * L[j][k];
-            if (i == j) {
-                if (!(acc > 1e-30)) return false;
-                L[i][i] = sqrt(acc);
-                inv_d[i] = 1.0 / L[i][i];
-            } else {
-                L[i][j] = acc * inv_d[j];
+// ---------------------------------------------------------------------------
+// FP64 solve and pose update, run by one warp of the last block.
+//
+// GB300 executes FP64 at a small fraction of the FP32 rate (a dependent DFMA
+// takes ~64 cycles, a double reciprocal ~430, sqrt ~670, sincos ~1600), so the
+// solve is arranged for latency: LDL^T instead of Cholesky (no square roots),
+// one row per lane so the row updates of a column issue as one instruction,
+// reciprocals from an FP32 seed and two Newton steps, and the SO(3)
+// exponential from its Taylor series when the rotation step is small.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rcp64(double d) {
+    double y = (double)__frcp_rn((float)d);
+    y = y * fma(-d, y, 2.0);
+    y = y * fma(-d, y, 2.0);
+    return y;
+}
+
+// A(theta) = sin(theta)/theta, B(theta) = (1 - cos(theta))/theta^2.
+__device__ __forceinline__ void rodrigues_coeffs(double th2, double &A, double &B) {
+    if (th2 < 1e-2) {  // theta < 0.1: truncation below 1e-17
+        A = fma(th2, fma(th2, fma(th2, fma(th2, 1.0 / 362880.0, -1.0 / 5040.0), 1.0 / 120.0), -1.0 / 6.0), 1.0);
+        B = fma(th2, fma(th2, fma(th2, fma(th2, 1.0 / 3628800.0, -1.0 / 40320.0), 1.0 / 720.0), -1.0 / 24.0), 0.5);
+    } else {
+        double th = sqrt(th2), sn, cs;
+        sincos(th, &sn, &cs);
+        A = sn / th;
+        B = (1.0 - cs) / th2;
+    }
+}
+
+// Returns false (pose unchanged) when A is not positive definite.
+__device__ bool warp_solve_and_update(IcpState *st, const double *sums, int lane) {
+    __shared__ double L[6][6], D[6], z[6], x[6], Rinc[9];
+    __shared__ int ok;
+    // lane i < 6 owns row i of [A | b]
+    double a[6], bi = 0.0;
+    #pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = 0.0;
+    if (lane < 6) {
+        int s = 0;
+        for (int k = 0; k < 6; ++k)
+            for (int j = k; j < 7; ++j, ++s) {
+                if (k == lane) { if (j == 6) bi = sums[s]; else a[j] = sums[s]; }
+                else if (j == lane) a[k] = sums[s];
             }
+    }
+    if (lane == 0) ok = 1;
+    __syncwarp();
+    #pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        // t_i = A_ij - sum_k L_ik L_jk D_k
+        double t = a[j];
+        #pragma unroll
+        for (int k = 0; k < j; ++k)
+            if (lane < 6) t = fma(-(lane > k ? L[lane][k] : 0.0), L[j][k] * D[k], t);
+        if (lane == j) {
+            D[j] = t;
+            if (!(t > 1e-30)) ok = 0;
         }
-    double yv[6], x[6];
-    for (int i = 0; i < 6; ++i) {
-        double acc = b[i];
-        for (int k = 0; k < i; ++k) acc -= L[i][k] * yv[k];
-        yv[i] = acc * inv_d[i];
+        __syncwarp();
+        const double inv = rcp64(D[j]);
+        if (lane > j && lane < 6) L[lane][j] = t * inv;
+        if (lane == j) L[j][j] = 1.0;
+        __syncwarp();
     }
-    for (int i = 5; i >= 0; --i) {
-        double acc = yv[i];
-        for (int k = i + 1; k < 6; ++k) acc -= L[k][i] * x[k];
-        x[i] = acc * inv_d[i];
+    if (!ok) return false;
+    // L z = b (lane i accumulates as z_k arrive), then y = z / D, L^T x = y
+    double acc = bi;
+    #pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        if (lane == k) z[k] = acc;
+        __syncwarp();
+        if (lane > k && lane < 6) acc = fma(-L[lane][k], z[k], acc);
     }
-    double Rinc[9];
-    so3_exp(x, Rinc);
-    double Rn[9], tn[3];
-    for (int r = 0; r < 3; ++r) {
-        for (int c = 0; c < 3; ++c)
-            Rn[3 * r + c] = Rinc[3 * r] * st->R[c] + Rinc[3 * r + 1] * st->R[3 + c] + Rinc[3 * r + 2] * st->R[6 + c];
-        tn[r] = Rinc[3 * r] * st->t[0] + Rinc[3 * r + 1] * st->t[1] + Rinc[3 * r + 2] * st->t[2] + x[3 + r];
+    __syncwarp();
+    acc = lane < 6 ? z[lane] * rcp64(D[lane]) : 0.0;
+    #pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        if (lane == k) x[k] = acc;
+        __syncwarp();
+        if (lane < k) acc = fma(-L[k][lane], x[k], acc);
     }
-    for (int k = 0; k < 9; ++k) { st->R[k] = Rn[k]; st->pose.R_cur[k] = (float)Rn[k]; }
-    for (int k = 0; k < 3; ++k) { st->t[k] = tn[k]; st->pose.t_cur[k] = (float)tn[k]; }
-    for (int k = 0; k < 6; ++k) st->x[k] = x[k];
+    __syncwarp();
+    // Rinc = I + A [w]x + B (w w^T - th2 I), lanes 0..8 one entry each
+    const double wx = x[0], wy = x[1], wz = x[2];
+    const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
+    double Ac, Bc;
+    rodrigues_coeffs(th2, Ac, Bc);
+    if (lane < 9) {
+        const int r = lane / 3, c = lane % 3;
+        const double w[3] = {wx, wy, wz};
+        double e = Bc * w[r] * w[c];
+        if (r == c) e += fma(-Bc, th2, 1.0);
+        // skew part: [w]x = [[0,-wz,wy],[wz,0,-wx],[-wy,wx,0]]
+        const double sk = (r == 0 && c == 1) ? -wz : (r == 0 && c == 2) ? wy : (r == 1 && c == 0) ? wz
+                        : (r == 1 && c == 2) ? -wx : (r == 2 && c == 0) ? -wy : (r == 2 && c == 1) ? wx : 0.0;
+        Rinc[lane] = fma(Ac, sk, e);
+    }
+    __syncwarp();
+    // R <- Rinc R, t <- Rinc t + v (lanes 0..8 rotation, 9..11 translation)
+    double out = 0.0;
+    if (lane < 9) {
+        const int r = lane / 3, c = lane % 3;
+        out = fma(Rinc[3 * r], st->R[c], fma(Rinc[3 * r + 1], st->R[3 + c], Rinc[3 * r + 2] * st->R[6 + c]));
+    } else if (lane < 12) {
+        const int r = lane - 9;
+        out = fma(Rinc[3 * r], st->t[0], fma(Rinc[3 * r + 1], st->t[1], fma(Rinc[3 * r + 2], st->t[2], x[3 + r])));
+    }
+    __syncwarp();
+    if (lane < 9) { st->R[lane] = out; st->pose.R_cur[lane] = (float)out; }
+    else if (lane < 12) { st->t[lane - 9] = out; st->pose.t_cur[lane - 9] = (float)out; }
+    if (lane < 6) st->x[lane] = x[lane];
     return true;
 }
 
@@ -232,6 +299,7 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
     if (ticket != (unsigned)nb - 1) return;
 
     // ---- last block: deterministic cross-block sum, one warp per term ----
+    __shared__ double s_sums[kIcpTerms];
     __threadfence();
     for (int t = warp; t < kIcpTerms; t += kThreads / 32) {
         f2 v{0.f, 0.f};
@@ -245,16 +313,20 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
             v = add_ff(v, o);
         }
         if (lane == 0) {
-            st->sums[t] = (double)v.hi + (double)v.lo;
+            s_sums[t] = (double)v.hi + (double)v.lo;
             if (mbuf && t < 27) mbuf[t] = v.hi + v.lo;
         }
     }
     __syncthreads();
-    if (tid == 0) {
+    if (warp != 0) return;
+    if (lane < kIcpTerms) st->sums[lane] = s_sums[lane];
+    const int inliers = (int)s_sums[27];
+    bool ok = true;
+    if (SOLVE) ok = inliers >= kIcpMinInliers && warp_solve_and_update(st, s_sums, lane);
+    if (lane == 0) {
         st->counter = 0u;
-        st->inliers = (int)st->sums[27];
+        st->inliers = inliers;
         if (SOLVE) {
-            bool ok = st->inliers >= kIcpMinInliers && solve_and_update(st);
             if (!ok) st->status |= kIcpStatusSolveFailed;
             st->iterations += 1;
         }

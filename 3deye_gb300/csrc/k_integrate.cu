@@ -2,13 +2,19 @@
 // common/src/opencl_wrappers.cpp:21-64; the reference kernel
 // integrate_tsdf_volume is absent, this follows the KinectFusion update).
 //
-// One thread per (x, y) voxel column, sweeping z.  The z range whose voxels
-// can land inside the image in front of the camera is bounded analytically per
-// column (each image edge is a linear inequality in z); the bound is widened
-// by a tolerance and only limits which voxels are evaluated -- the per-voxel
-// test below, identical to the CPU oracle's, decides.  Voxels more than
-// `trunc` behind the observed surface are neither read nor written; a voxel
-// whose record does not change is not written.
+// Work is organised in 8^3-voxel bricks.  Each thread of a block first tests
+// one brick against the frame: the brick's voxel-centre box is projected
+// (8 corners) and, if it lies entirely behind the camera, outside the image,
+// or farther from the camera than the largest observed depth over the pixels
+// it covers plus the truncation distance, none of its voxels can pass the
+// per-voxel test, so the brick is dropped.  The block then sweeps its
+// surviving bricks one warp per brick and applies the per-voxel update --
+// the same IEEE float operations, in the same order, as the CPU oracle, which
+// visits every voxel.  Culling only removes voxels the exact test rejects, so
+// volumes are bit-identical.
+//
+// The maximum observed depth per screen tile comes from a 5-level pyramid
+// (16..256-pixel tiles) built by depth_max_kernel each frame.
 //
 // Built with -fmad=false so every voxel decision and value equals the oracle's.
 #include "tde_common.cuh"
@@ -17,81 +23,165 @@
 namespace tde {
 namespace {
 
-constexpr int kZBatch = 4;
+constexpr int kBrick = 8;
+constexpr int kBricksPerBlock = 256;
 
-__device__ __forceinline__ void bound_linear(float p, float q, float tol, float &lo, float &hi) {
-    // keep z with p + q z >= -tol
-    if (fabsf(q) < 1e-20f) {
-        if (p < -tol) { lo = 1.f; hi = 0.f; }
-        return;
+// ---------------------------------------------------------------------------
+// Max scaled depth per 16x16 tile (level 0) and per 32..256 tiles (levels 1-4,
+// by atomicMax on the bit pattern: non-negative floats order like ints).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) depth_max_kernel(const float *__restrict__ depth, int W, int H,
+                                                        DepthMaxPyramid pyr) {
+    __shared__ float red[8];
+    const int tx = blockIdx.x, ty = blockIdx.y;
+    const int x = tx * 16 + (threadIdx.x & 15), y = ty * 16 + (threadIdx.x >> 4);
+    float m = 0.f;
+    if (x < W && y < H) m = fmaxf(0.f, depth[(size_t)y * W + x]);
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < 8; ++i) m = fmaxf(m, red[i]);
+        pyr.level[0][ty * pyr.tiles_x[0] + tx] = m;
+        for (int l = 1; l < kDepthMaxLevels; ++l)
+            atomicMax(reinterpret_cast<int *>(&pyr.level[l][(ty >> l) * pyr.tiles_x[l] + (tx >> l)]), __float_as_int(m));
     }
-    float z = (-tol - p) / q;
-    if (q > 0.f) lo = fmaxf(lo, z); else hi = fminf(hi, z);
+}
+
+// Largest observed depth over pixel rectangle [u0,u1]x[v0,v1] (inclusive,
+// inside the image); the level is chosen so the rectangle meets <= 2x2 tiles.
+__device__ __forceinline__ float rect_max_depth(const DepthMaxPyramid &pyr, int u0, int v0, int u1, int v1) {
+    const int ext = max(u1 - u0, v1 - v0) + 1;
+    int l = 0;
+    while (l < kDepthMaxLevels - 1 && (16 << l) < ext) ++l;
+    if ((16 << l) < ext) return 3.0e38f;  // larger than the coarsest tile: never cull on depth
+    const int s = 4 + l;  // log2 tile size
+    float m = 0.f;
+    for (int ty = v0 >> s; ty <= (v1 >> s); ++ty)
+        for (int tx = u0 >> s; tx <= (u1 >> s); ++tx) m = fmaxf(m, pyr.level[l][ty * pyr.tiles_x[l] + tx]);
+    return m;
+}
+
+struct Pose {
+    float Ri[9];
+    float t[3];
+};
+
+// True when no voxel of brick (bx,by,bz) can pass the per-voxel test.
+__device__ bool brick_culled(const IntegrateParams &P, const Pose &q, const DepthMaxPyramid &pyr, int bx, int by,
+                             int bz) {
+    const tde_point3i &Nv = P.rb.voxels_size;
+    const int x0 = bx * kBrick, y0 = by * kBrick, z0 = bz * kBrick;
+    const int x1 = min(x0 + kBrick, Nv.x) - 1, y1 = min(y0 + kBrick, Nv.y) - 1, z1 = min(z0 + kBrick, Nv.z) - 1;
+    // voxel-centre box, camera-relative
+    const float lo[3] = {((float)x0 + 0.5f) * P.cell.x - q.t[0], ((float)y0 + 0.5f) * P.cell.y - q.t[1],
+                         ((float)z0 + 0.5f) * P.cell.z - q.t[2]};
+    const float hi[3] = {((float)x1 + 0.5f) * P.cell.x - q.t[0], ((float)y1 + 0.5f) * P.cell.y - q.t[1],
+                         ((float)z1 + 0.5f) * P.cell.z - q.t[2]};
+    float umin = 3e38f, umax = -3e38f, vmin = 3e38f, vmax = -3e38f;
+    int behind = 0;
+    bool near_plane = false;
+    #pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const float gx = (c & 1) ? hi[0] : lo[0], gy = (c & 2) ? hi[1] : lo[1], gz = (c & 4) ? hi[2] : lo[2];
+        const float vx = q.Ri[0] * gx + q.Ri[1] * gy + q.Ri[2] * gz;
+        const float vy = q.Ri[3] * gx + q.Ri[4] * gy + q.Ri[5] * gz;
+        const float vz = q.Ri[6] * gx + q.Ri[7] * gy + q.Ri[8] * gz;
+        if (vz <= 0.f) ++behind;
+        if (vz < 1e-4f) { near_plane = true; continue; }
+        const float iz = 1.f / vz;
+        const float u = P.intr.fx * vx * iz + P.intr.cx, v = P.intr.fy * vy * iz + P.intr.cy;
+        umin = fminf(umin, u); umax = fmaxf(umax, u); vmin = fminf(vmin, v); vmax = fmaxf(vmax, v);
+    }
+    if (behind == 8) return true;  // convex hull behind the camera plane
+    if (near_plane) return false;  // projection unbounded: keep
+    const int W = P.intr.cols, H = P.intr.rows;
+    if (umax < -1.f || vmax < -1.f || umin > (float)W || vmin > (float)H) return true;  // outside the image
+    const int u0 = max(0, (int)floorf(umin) - 1), u1 = min(W - 1, (int)ceilf(umax) + 1);
+    const int v0 = max(0, (int)floorf(vmin) - 1), v1 = min(H - 1, (int)ceilf(vmax) + 1);
+    if (u0 > u1 || v0 > v1) return true;
+    const float dmax = rect_max_depth(pyr, u0, v0, u1, v1);
+    // nearest distance from the camera centre to the box
+    float d2 = 0.f;
+    #pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float d = fmaxf(0.f, fmaxf(lo[a], -hi[a]));
+        d2 += d * d;
+    }
+    return sqrtf(d2) > dmax + P.trunc + 1e-3f + 1e-4f * dmax;
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(256) integrate_kernel(const float *__restrict__ depth, void *__restrict__ vol,
-                                                        const IntegrateParams P,
-                                                        unsigned long long *__restrict__ stats) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const tde_round_buffer &rb = P.rb;
-    __shared__ float s_pose[12];
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
+                                                               const IntegrateParams P, const DepthMaxPyramid pyr,
+                                                               uint8_t *__restrict__ neg_flags,
+                                                               unsigned long long *__restrict__ stats) {
+    __shared__ Pose q;
+    __shared__ int s_list[kBricksPerBlock];
+    __shared__ int s_wbase[kBricksPerBlock / 32];
+    __shared__ int s_n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid < 12) {
-        if (P.dpose) s_pose[tid] = tid < 9 ? P.dpose->R_inv[tid] : P.dpose->t[tid - 9];
-        else s_pose[tid] = tid < 9 ? P.R_inv[tid] : P.t[tid - 9];
+        float v;
+        if (P.dpose) v = tid < 9 ? P.dpose->R_inv[tid] : P.dpose->t[tid - 9];
+        else v = tid < 9 ? P.R_inv[tid] : P.t[tid - 9];
+        if (tid < 9) q.Ri[tid] = v; else q.t[tid - 9] = v;
     }
     __syncthreads();
-    unsigned n_read = 0, n_written = 0;
-    if (x < rb.voxels_size.x && y < rb.voxels_size.y) {
-        float Ri[9];
-        #pragma unroll
-        for (int k = 0; k < 9; ++k) Ri[k] = s_pose[k];
-        const float tx = s_pose[9], ty = s_pose[10], tz = s_pose[11];
-        const float gx = ((float)x + 0.5f) * P.cell.x - tx;
-        const float gy = ((float)y + 0.5f) * P.cell.y - ty;
-        const int W = P.intr.cols, H = P.intr.rows;
-        const int Nz = rb.voxels_size.z;
-
-        // --- conservative z interval ------------------------------------
-        // v(z) = c + z d  (camera frame), d = R_inv[:,2] * cell.z
-        const float hz = 0.5f * P.cell.z - tz;
-        float cxv = Ri[0] * gx + Ri[1] * gy + Ri[2] * hz;
-        float cyv = Ri[3] * gx + Ri[4] * gy + Ri[5] * hz;
-        float czv = Ri[6] * gx + Ri[7] * gy + Ri[8] * hz;
-        float dxv = Ri[2] * P.cell.z, dyv = Ri[5] * P.cell.z, dzv = Ri[8] * P.cell.z;
-        float lo = 0.f, hi = (float)(Nz - 1);
-        const float scale = fabsf(cxv) + fabsf(cyv) + fabsf(czv) + (fabsf(dxv) + fabsf(dyv) + fabsf(dzv)) * (float)Nz;
-        const float tol = 1e-4f * scale * (P.intr.fx + P.intr.fy + (float)(W + H)) + 1e-6f;
-        bound_linear(czv, dzv, 1e-4f * scale + 1e-6f, lo, hi);                           // v.z > 0
-        const float fx = P.intr.fx, fy = P.intr.fy, ccx = P.intr.cx, ccy = P.intr.cy;
-        bound_linear(fx * cxv + (ccx + 0.5f) * czv, fx * dxv + (ccx + 0.5f) * dzv, tol, lo, hi);   // u >= -0.5
-        bound_linear(-(fx * cxv + (ccx - (float)W + 0.5f) * czv), -(fx * dxv + (ccx - (float)W + 0.5f) * dzv), tol, lo, hi);
-        bound_linear(fy * cyv + (ccy + 0.5f) * czv, fy * dyv + (ccy + 0.5f) * dzv, tol, lo, hi);
-        bound_linear(-(fy * cyv + (ccy - (float)H + 0.5f) * czv), -(fy * dyv + (ccy - (float)H + 0.5f) * dzv), tol, lo, hi);
-        int z0 = 0, z1 = -1;
-        if (lo <= hi) {
-            z0 = max(0, (int)floorf(lo) - 2);
-            z1 = min(Nz - 1, (int)ceilf(hi) + 2);
+    const tde_point3i &Nv = P.rb.voxels_size;
+    const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick, nbz = (Nv.z + kBrick - 1) / kBrick;
+    const int nbricks = nbx * nby * nbz;
+    // --- cull: one brick per thread, survivors listed in brick order ---
+    {
+        const int b = blockIdx.x * kBricksPerBlock + tid;
+        bool keep = false;
+        if (b < nbricks) {
+            const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+            keep = !brick_culled(P, q, pyr, bx, by, bz);
         }
-
-        const float ntrunc = -P.trunc;
-        for (int zb = z0; zb <= z1; zb += kZBatch) {
-            size_t idx[kZBatch];
-            float sdfv[kZBatch];
-            bool take[kZBatch];
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) s_wbase[warp] = __popc(m);
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0;
+            for (int w = 0; w < kBricksPerBlock / 32; ++w) { int c = s_wbase[w]; s_wbase[w] = acc; acc += c; }
+            s_n = acc;
+        }
+        __syncthreads();
+        if (keep) s_list[s_wbase[warp] + __popc(m & ((1u << lane) - 1u))] = b;
+        __syncthreads();
+    }
+    // --- sweep the surviving bricks, one warp per brick ---
+    typedef TsdfStore<FMT> S;
+    const float ntrunc = -P.trunc;
+    const int W = P.intr.cols, H = P.intr.rows;
+    const float fx = P.intr.fx, fy = P.intr.fy, ccx = P.intr.cx, ccy = P.intr.cy;
+    unsigned n_read = 0, n_written = 0;
+    for (int i = warp; i < s_n; i += kBricksPerBlock / 32) {
+        const int b = s_list[i];
+        const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+        const int x = bx * kBrick + (lane & 7);
+        const float gx = ((float)x + 0.5f) * P.cell.x - q.t[0];
+        #pragma unroll 1
+        for (int j0 = 0; j0 < 16; j0 += 4) {
+            size_t idx[4];
+            float sdfv[4];
+            bool take[4];
+            int zz[4], yy[4];
             #pragma unroll
-            for (int k = 0; k < kZBatch; ++k) {
-                const int z = zb + k;
-                take[k] = false;
-                sdfv[k] = 0.f;
-                idx[k] = 0;
-                if (z > z1) continue;
-                const float gz = ((float)z + 0.5f) * P.cell.z - tz;
-                float vx = 0.f; vx += Ri[0] * gx; vx += Ri[1] * gy; vx += Ri[2] * gz;
-                float vy = 0.f; vy += Ri[3] * gx; vy += Ri[4] * gy; vy += Ri[5] * gz;
-                float vz = 0.f; vz += Ri[6] * gx; vz += Ri[7] * gy; vz += Ri[8] * gz;
+            for (int k = 0; k < 4; ++k) {
+                const int j = j0 + k;
+                const int y = by * kBrick + (lane >> 3) + 4 * (j & 1);
+                const int z = bz * kBrick + (j >> 1);
+                yy[k] = y; zz[k] = z;
+                take[k] = false; sdfv[k] = 0.f; idx[k] = 0;
+                if (x >= Nv.x || y >= Nv.y || z >= Nv.z) continue;
+                const float gy = ((float)y + 0.5f) * P.cell.y - q.t[1];
+                const float gz = ((float)z + 0.5f) * P.cell.z - q.t[2];
+                float vx = 0.f; vx += q.Ri[0] * gx; vx += q.Ri[1] * gy; vx += q.Ri[2] * gz;
+                float vy = 0.f; vy += q.Ri[3] * gx; vy += q.Ri[4] * gy; vy += q.Ri[5] * gz;
+                float vz = 0.f; vz += q.Ri[6] * gx; vz += q.Ri[7] * gy; vz += q.Ri[8] * gz;
                 if (!(vz > 0.f)) continue;
                 const int u = __float2int_rn(vx * fx / vz + ccx);
                 const int v = __float2int_rn(vy * fy / vz + ccy);
@@ -103,15 +193,14 @@ __global__ void __launch_bounds__(256) integrate_kernel(const float *__restrict_
                 if (!(sdf >= ntrunc)) continue;
                 take[k] = true;
                 sdfv[k] = sdf;
-                idx[k] = voxel_address(x, y, z, rb);
+                idx[k] = voxel_address(x, y, z, P.rb);
             }
-            typedef TsdfStore<FMT> S;
-            typename S::Raw raw[kZBatch];
+            typename S::Raw raw[4];
             #pragma unroll
-            for (int k = 0; k < kZBatch; ++k)
+            for (int k = 0; k < 4; ++k)
                 if (take[k]) raw[k] = S::load_raw(vol, idx[k], P.n);
             #pragma unroll
-            for (int k = 0; k < kZBatch; ++k) {
+            for (int k = 0; k < 4; ++k) {
                 if (!take[k]) continue;
                 ++n_read;
                 float fo;
@@ -125,6 +214,12 @@ __global__ void __launch_bounds__(256) integrate_kernel(const float *__restrict_
                 if (!S::same(rn, raw[k])) {
                     S::store_raw(vol, idx[k], P.n, rn);
                     ++n_written;
+                    if (neg_flags) {
+                        float fs;
+                        int ws;
+                        S::decode(rn, fs, ws);
+                        if (fs < 0.f) neg_flags[physical_brick(x, yy[k], zz[k], P.rb)] = 1;
+                    }
                 }
             }
         }
@@ -136,7 +231,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const float *__restrict_
             r += __shfl_down_sync(0xffffffffu, r, off);
             w += __shfl_down_sync(0xffffffffu, w, off);
         }
-        if ((threadIdx.x & 31) == 0 && (r | w)) {
+        if (lane == 0 && (r | w)) {
             atomicAdd(stats, (unsigned long long)r);
             atomicAdd(stats + 1, (unsigned long long)w);
         }
@@ -145,12 +240,50 @@ __global__ void __launch_bounds__(256) integrate_kernel(const float *__restrict_
 
 }  // namespace
 
+size_t depth_max_floats(int W, int H) {
+    size_t n = 0;
+    for (int l = 0; l < kDepthMaxLevels; ++l) {
+        const int t = 16 << l;
+        n += (size_t)((W + t - 1) / t) * ((H + t - 1) / t);
+    }
+    return n;
+}
+
+DepthMaxPyramid depth_max_layout(float *base, int W, int H) {
+    DepthMaxPyramid p;
+    size_t off = 0;
+    for (int l = 0; l < kDepthMaxLevels; ++l) {
+        const int t = 16 << l;
+        p.tiles_x[l] = (W + t - 1) / t;
+        p.level[l] = base + off;
+        off += (size_t)p.tiles_x[l] * ((H + t - 1) / t);
+    }
+    return p;
+}
+
+int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cudaStream_t stream) {
+    DepthMaxPyramid pyr = depth_max_layout(scratch, W, H);
+    // levels >= 1 are atomicMax targets: start them at +0
+    const size_t l0 = (size_t)pyr.tiles_x[0] * ((H + 15) / 16);
+    cudaError_t e = cudaMemsetAsync(scratch + l0, 0, (depth_max_floats(W, H) - l0) * sizeof(float), stream);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "depth_max: %s", cudaGetErrorString(e));
+    dim3 grid(div_up(W, 16), div_up(H, 16));
+    depth_max_kernel<<<grid, 256, 0, stream>>>(depth_scaled, W, H, pyr);
+    return check_launch("depth_max");
+}
+
+size_t brick_count(const tde_round_buffer &rb) {
+    return (size_t)((rb.voxels_size.x + kBrick - 1) / kBrick) * ((rb.voxels_size.y + kBrick - 1) / kBrick) *
+           ((rb.voxels_size.z + kBrick - 1) / kBrick);
+}
+
 int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P,
-                     unsigned long long *stats, cudaStream_t stream) {
-    dim3 block(32, 8);
-    dim3 grid(div_up(P.rb.voxels_size.x, 32), div_up(P.rb.voxels_size.y, 8));
+                     const float *depth_max, uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream) {
+    const DepthMaxPyramid pyr = depth_max_layout(const_cast<float *>(depth_max), P.intr.cols, P.intr.rows);
+    const unsigned blocks = div_up((unsigned)brick_count(P.rb), kBricksPerBlock);
     return dispatch_format(format, [&](auto F) {
-        integrate_kernel<decltype(F)::value><<<grid, block, 0, stream>>>(depth_scaled, volume, P, stats);
+        integrate_bricks_kernel<decltype(F)::value><<<blocks, 256, 0, stream>>>(depth_scaled, volume, P, pyr,
+                                                                               neg_flags, stats);
         return check_launch("integrate_tsdf");
     });
 }

@@ -54,7 +54,7 @@ __device__ __forceinline__ float read_tsdf(const void *vol, const RayParams &p, 
 
 // interpolateTrilineary: raycast.cl:95-145.
 template <int FMT>
-__device__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
+__device__ __noinline__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
     const tde_point3i &N = p.rb.voxels_size;
     int gx = floor_sat(pt.x / p.cell.x), gy = floor_sat(pt.y / p.cell.y), gz = floor_sat(pt.z / p.cell.z);
     if (gx <= 0 || gx >= N.x - 1) return __int_as_float(0x7fffffff);
@@ -77,6 +77,42 @@ __device__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
     float x0 = one_b * (r000 * one_c + r001 * c) + b * (r010 * one_c + r011 * c);
     float x1 = one_b * (r100 * one_c + r101 * c) + b * (r110 * one_c + r111 * c);
     return one_a * x0 + a * x1;
+}
+
+// Zero crossing between time_curr and time_curr + step: secant refinement of
+// the hit and central-difference normal (raycast.cl:280-401).  Kept out of
+// line: it runs once per ray, and inlining it would bloat the march loop past
+// the instruction cache.
+template <int FMT>
+__device__ __noinline__ void refine_surface(const void *vol, const RayParams &p, f3 dir, float time_curr,
+                                            float &vx_out, float &vy_out, float &vz_out, float &nx_out,
+                                            float &ny_out, float &nz_out) {
+    const tde_point3i N = p.rb.voxels_size;
+    const float step = p.time_step;
+    float ct = time_curr + step;
+    float Ftdt = trilinear<FMT>(vol, p, along(p.t, dir, ct));
+    if (isnan(Ftdt)) return;
+    float Ft = trilinear<FMT>(vol, p, along(p.t, dir, time_curr));
+    if (isnan(Ft)) return;
+    float Ts = time_curr - step * Ft / (Ftdt - Ft);
+    f3 vf = along(p.t, dir, Ts);
+    vx_out = vf.x; vy_out = vf.y; vz_out = vf.z;
+    f3 p3 = along(p.t, dir, time_curr);
+    int hx = floor_sat(p3.x / p.cell.x), hy = floor_sat(p3.y / p.cell.y), hz = floor_sat(p3.z / p.cell.z);
+    if (hx > 1 && hy > 1 && hz > 1 && hx < N.x - 2 && hy < N.y - 2 && hz < N.z - 2) {
+        float F[6];
+        #pragma unroll 1
+        for (int k = 0; k < 6; ++k) {
+            f3 tt = vf;
+            const int axis = k >> 1;
+            const float d = axis == 0 ? p.cell.x : axis == 1 ? p.cell.y : p.cell.z;
+            float &c = axis == 0 ? tt.x : axis == 1 ? tt.y : tt.z;
+            c = (k & 1) ? c - d : c + d;
+            F[k] = trilinear<FMT>(vol, p, tt);
+        }
+        f3 n = normalized(f3{F[0] - F[1], F[2] - F[3], F[4] - F[5]});
+        nx_out = n.x; ny_out = n.y; nz_out = n.z;
+    }
 }
 
 // Number of march samples whose addresses are issued together.  The samples
@@ -185,26 +221,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                 if (tsdf_prev < 0.f && tsdf > 0.f) { done = true; break; }
                 if (tsdf_prev > 0.f && tsdf < 0.f) {
                     done = true;
-                    float ct = time_curr + step;
-                    float Ftdt = trilinear<FMT>(vol, p, along(p.t, dir, ct));
-                    if (isnan(Ftdt)) break;
-                    float Ft = trilinear<FMT>(vol, p, along(p.t, dir, time_curr));
-                    if (isnan(Ft)) break;
-                    float Ts = time_curr - step * Ft / (Ftdt - Ft);
-                    f3 vf = along(p.t, dir, Ts);
-                    vx_out = vf.x; vy_out = vf.y; vz_out = vf.z;
-                    f3 p3 = along(p.t, dir, time_curr);
-                    int hx = floor_sat(p3.x / p.cell.x), hy = floor_sat(p3.y / p.cell.y), hz = floor_sat(p3.z / p.cell.z);
-                    if (hx > 1 && hy > 1 && hz > 1 && hx < N.x - 2 && hy < N.y - 2 && hz < N.z - 2) {
-                        f3 tt = vf; tt.x = tt.x + p.cell.x; float Fx1 = trilinear<FMT>(vol, p, tt);
-                        tt = vf; tt.x = tt.x - p.cell.x; float Fx2 = trilinear<FMT>(vol, p, tt);
-                        tt = vf; tt.y = tt.y + p.cell.y; float Fy1 = trilinear<FMT>(vol, p, tt);
-                        tt = vf; tt.y = tt.y - p.cell.y; float Fy2 = trilinear<FMT>(vol, p, tt);
-                        tt = vf; tt.z = tt.z + p.cell.z; float Fz1 = trilinear<FMT>(vol, p, tt);
-                        tt = vf; tt.z = tt.z - p.cell.z; float Fz2 = trilinear<FMT>(vol, p, tt);
-                        f3 n = normalized(f3{Fx1 - Fx2, Fy1 - Fy2, Fz1 - Fz2});
-                        nx_out = n.x; ny_out = n.y; nz_out = n.z;
-                    }
+                    refine_surface<FMT>(vol, p, dir, time_curr, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
                     break;
                 }
             }

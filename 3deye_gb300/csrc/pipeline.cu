@@ -87,6 +87,8 @@ struct tde_pipeline {
     CamPose *cam = nullptr;
     FrameOut *out = nullptr;
     unsigned long long *stats = nullptr;
+    float *dmax = nullptr;        // per-tile maximum depth (integration culling)
+    uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     void *volume = nullptr;
     // graphs: per segment and the whole frame
     cudaGraphExec_t seg_exec[SEG_COUNT] = {};
@@ -149,14 +151,15 @@ int record_segment(tde_pipeline *p, Segment seg) {
         }
         finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_TRACK);
         TDE_TRY(check_launch("finalize_pose"));
-        return launch_scale_depth(p->raw, p->scaled, p->intr[0], s);
+        TDE_TRY(launch_scale_depth(p->raw, p->scaled, p->intr[0], s));
+        return launch_depth_max(p->scaled, W, H, p->dmax, s);
     }
     case SEG_INTEGRATE: {
         IntegrateParams P;
         std::memset(&P, 0, sizeof(P));
         P.trunc = c.trunc; P.max_weight = c.max_weight; P.intr = p->intr[0]; P.rb = p->rb; P.cell = p->cell;
         P.n = voxel_count(p->rb); P.dpose = p->cam;
-        return launch_integrate(p->scaled, p->volume, c.tsdf_format, P, p->stats, s);
+        return launch_integrate(p->scaled, p->volume, c.tsdf_format, P, p->dmax, p->negflags, p->stats, s);
     }
     case SEG_RAYCAST: {
         tde_point3f t0{0, 0, 0};
@@ -244,7 +247,7 @@ void release(tde_pipeline *p) {
         cudaFree(p->depth[l]); cudaFree(p->vcur[l]); cudaFree(p->ncur[l]); cudaFree(p->vmod[l]); cudaFree(p->nmod[l]);
     }
     cudaFree(p->scaled); cudaFree(p->gbuf); cudaFree(p->st); cudaFree(p->prev); cudaFree(p->cam); cudaFree(p->out);
-    cudaFree(p->stats); cudaFree(p->volume);
+    cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->dmax); cudaFree(p->negflags);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -295,8 +298,12 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     if ((st = dalloc(&p->gbuf, icp_gbuf_floats(c.intr.cols, c.intr.rows), "icp partials")) ||
         (st = dalloc(&p->st, 1, "icp state")) || (st = dalloc(&p->prev, 1, "prev pose")) ||
         (st = dalloc(&p->cam, 1, "camera pose")) || (st = dalloc(&p->out, 1, "frame out")) ||
-        (st = dalloc(&p->stats, 2, "stats")))
+        (st = dalloc(&p->stats, 2, "stats")) ||
+        (st = dalloc(&p->dmax, depth_max_floats(c.intr.cols, c.intr.rows), "depth max")) ||
+        (st = dalloc(&p->negflags, brick_count(p->rb), "brick flags")))
         return fail(st);
+    e = cudaMemsetAsync(p->negflags, 0, brick_count(p->rb), p->stream);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "brick flags"));
     e = cudaMemsetAsync(p->stats, 0, 2 * sizeof(unsigned long long), p->stream);
     if (e != cudaSuccess) return fail(cuda_fail(e, "stats"));
     if (!c.integrate_stats) { cudaFree(p->stats); p->stats = nullptr; }
@@ -441,8 +448,8 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p) {
     int icp = 0;
     for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
     // bilateral, pyramid levels, normal maps, begin, ICP, finalize, scale,
-    // integrate, raycast, 2 resizes per coarser level
-    return 1 + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
+    // depth max, integrate, raycast, 2 resizes per coarser level
+    return 1 + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
 }
 
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {

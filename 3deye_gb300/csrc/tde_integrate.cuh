@@ -25,7 +25,29 @@ struct IntegrateParams {
     const CamPose *dpose;  // when set, R_inv and t are read from here
 };
 
+// Max observed depth per screen tile: level l has (16 << l)-pixel tiles.
+constexpr int kDepthMaxLevels = 5;
+struct DepthMaxPyramid {
+    float *level[kDepthMaxLevels];
+    int tiles_x[kDepthMaxLevels];
+};
+
+// Physical 8^3 brick holding logical voxel (x, y, z) (cyclic volume).
+__host__ __device__ __forceinline__ size_t physical_brick(int x, int y, int z, const tde_round_buffer &rb) {
+    const int px = wrap_mod(x + rb.origin_GRID.x, rb.voxels_size.x);
+    const int py = wrap_mod(y + rb.origin_GRID.y, rb.voxels_size.y);
+    const int pz = wrap_mod(z + rb.origin_GRID.z, rb.voxels_size.z);
+    const size_t nbx = (size_t)(rb.voxels_size.x + 7) / 8, nby = (size_t)(rb.voxels_size.y + 7) / 8;
+    return (size_t)(px >> 3) + nbx * ((size_t)(py >> 3) + nby * (size_t)(pz >> 3));
+}
+
+size_t depth_max_floats(int W, int H);
+size_t brick_count(const tde_round_buffer &rb);
+int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cudaStream_t stream);
+// neg_flags (may be null): per physical brick, set to 1 when a write leaves a
+// negative value there; a 0 therefore guarantees the brick holds no negative
+// TSDF value.
 int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P,
-                     unsigned long long *stats, cudaStream_t stream);
+                     const float *depth_max, uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream);
 
 }  // namespace tde

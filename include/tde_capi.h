@@ -120,8 +120,8 @@ int tde_bilateral_filter(const uint16_t *depth, uint16_t *filtered, int cols, in
 int tde_depth_pyramid_level(const uint16_t *src, uint16_t *dst, int src_cols, int src_rows,
                             float sigma_color, void *stream);
 
-/* Fused bilateral + pyramid: one launch writes levels[0..num_levels-1]
- * (level l has cols>>l x rows>>l pixels).  Same results as the two calls above. */
+/* Bilateral filter then pyramid: writes levels[0..num_levels-1] (level l has
+ * cols>>l x rows>>l pixels), enqueuing the two calls above in sequence. */
 int tde_bilateral_pyramid(const uint16_t *depth, uint16_t *const *levels, int num_levels, int cols,
                           int rows, float sigma_space, float sigma_color, uint32_t max_distance_mm,
                           void *stream);
@@ -190,13 +190,29 @@ int tde_scale_depth(const uint16_t *depth, float *scaled, const tde_intrinsics *
  * ((x+.5)cs.x, (y+.5)cs.y, (z+.5)cs.z) in volume coordinates; the camera
  * centre t and R_inv (world->camera rotation) are in the same frame.  Voxels
  * that project outside the image, onto an invalid pixel, or lie more than
- * trunc behind the surface are not touched.  Others get
+ * trunc behind the surface are not touched (whole 8^3 bricks that provably
+ * qualify are skipped without being read).  Others get
  * f = (f w + min(1, sdf/trunc)) / (w + 1), w = min(w + 1, max_weight).
  * MAX_TSDF_WEIGHT is 128 (common/inc/common_defines.h:10). */
 int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, float trunc,
                        const tde_matrix3f *R_inv, const tde_point3f *t, const tde_intrinsics *intr,
                        const tde_point3f *cell_size, const tde_round_buffer *rb, int max_weight,
                        void *stream);
+
+/* Integrate_Tsdf_Data with caller-provided memory: `scratch` (device,
+ * tde_integrate_tsdf_scratch_bytes) holds the frame's per-tile maximum depth
+ * used to skip 8^3 bricks that lie entirely more than trunc behind the
+ * observed surface; tde_integrate_tsdf allocates it on the stream itself.
+ * `brick_flags` (device, tde_brick_flags_bytes, zero-initialised with the
+ * volume; may be NULL) gets a 1 for every physical brick that receives a
+ * negative value -- a 0 proves the brick has none, which the pipeline's
+ * raycast uses to skip loads.  Same results as tde_integrate_tsdf. */
+size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows);
+size_t tde_brick_flags_bytes(const tde_round_buffer *rb);
+int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, float trunc,
+                          const tde_matrix3f *R_inv, const tde_point3f *t, const tde_intrinsics *intr,
+                          const tde_point3f *cell_size, const tde_round_buffer *rb, int max_weight,
+                          void *scratch, size_t scratch_bytes, uint8_t *brick_flags, void *stream);
 
 /* ======================================================================== */
 /* a8/a9: raycast and model maps                                             */

@@ -110,6 +110,55 @@ def test_integrate_and_raycast_match_oracle(tde, orc, cuda, small, fmt, origin):
     assert bits_equal(N(vm), vmo) and bits_equal(N(nm), nmo)
 
 
+@pytest.mark.parametrize("fmt", [0, 1, 2])
+def test_integrate_ex_brick_flags_are_sound(tde, orc, cuda, small, fmt):
+    """tde_integrate_tsdf_ex with caller scratch gives the same volume, and a
+    zero brick flag proves the physical brick holds no negative value."""
+    import ctypes as C
+    import torch
+    cfg, scene, traj, intr, depths = small
+    origin = (5, 17, 60)
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt, origin, nframes=4)
+    rb = trb(tde, rb_o)
+    ti = tintr(tde, intr)
+    L = tde.lib
+    L.tde_integrate_tsdf_scratch_bytes.restype = C.c_size_t
+    L.tde_brick_flags_bytes.restype = C.c_size_t
+    L.tde_brick_flags_bytes.argtypes = [C.POINTER(tde.RoundBuffer)]
+    L.tde_integrate_tsdf_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.POINTER(tde.Matrix3f),
+                                        C.POINTER(tde.Point3f), C.POINTER(tde.Intrinsics), C.POINTER(tde.Point3f),
+                                        C.POINTER(tde.RoundBuffer), C.c_int, C.c_void_p, C.c_size_t, C.c_void_p,
+                                        C.c_void_p]
+    sb = L.tde_integrate_tsdf_scratch_bytes(intr.cols, intr.rows)
+    scratch = torch.empty(sb, dtype=torch.uint8, device=cuda)
+    nbr = L.tde_brick_flags_bytes(C.byref(rb))
+    flags = torch.zeros(nbr, dtype=torch.uint8, device=cuda)
+    vol = tde.new_volume(fmt, rb)
+    for i in range(4):
+        R, t = pose_parts(traj[i])
+        sd = tde.scale_depth(T(depths[i], cuda), ti)
+        Ri, tt, cs = tde.mat3(R.T.copy()), tde.vec3(t), tde.vec3(cell)
+        tde.check(L.tde_integrate_tsdf_ex(sd.data_ptr(), vol.data_ptr(), fmt, cfg.trunc_m, C.byref(Ri), C.byref(tt),
+                                          C.byref(ti), C.byref(cs), C.byref(rb), 128, scratch.data_ptr(), sb,
+                                          flags.data_ptr(), tde.stream_ptr()))
+    torch.cuda.synchronize()
+    assert np.array_equal(N(vol), vol_o)
+    Nv = cfg.voxels
+    n = Nv ** 3
+    if fmt == 0:
+        vals = vol_o.view(np.int16).reshape(-1, 2)[:, 0].astype(np.float32)
+    elif fmt == 1:
+        vals = vol_o.view(np.float16).reshape(-1, 2)[:, 0].astype(np.float32)
+    else:
+        vals = vol_o[: 4 * n].view(np.float32)
+    phys = vals.reshape(Nv, Nv, Nv)  # storage order: z, y, x
+    nb = Nv // 8
+    neg = (phys < 0).reshape(nb, 8, nb, 8, nb, 8).any(axis=(1, 3, 5))  # [bz, by, bx]
+    f = N(flags).reshape(nb, nb, nb).astype(bool)
+    assert neg.any()
+    assert not (neg & ~f).any(), "a brick with a negative value has flag 0"
+
+
 # ---------------------------------------------------------------------------
 # depth preprocessing
 # ---------------------------------------------------------------------------
