@@ -200,7 +200,7 @@ int tde_estimate_combined(const float *vmap_cur, const float *nmap_cur, const fl
     a.W = intr->cols; a.H = intr->rows;
     a.fx = intr->fx; a.fy = intr->fy; a.cx = intr->cx; a.cy = intr->cy;
     a.dist_thresh = dist_thresh; a.angle_thresh = angle_thresh;
-    int st_code = launch_icp(a, st, gbuf, mbuf, false, s);
+    int st_code = launch_icp(a, st, gbuf, mbuf, false, false, s);
     if (st_code) return st_code;
     // the host copy of h must outlive the async copy above
     e = cudaStreamSynchronize(s);
@@ -296,9 +296,9 @@ static IntegrateParams integrate_params(float trunc, const tde_matrix3f *R_inv, 
     return P;
 }
 
-size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows) {
-    if (cols <= 0 || rows <= 0) return 0;
-    return depth_max_floats(cols, rows) * sizeof(float);
+size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows, const tde_round_buffer *rb) {
+    if (cols <= 0 || rows <= 0 || !valid_round_buffer(rb)) return 0;
+    return integrate_scratch_bytes(cols, rows, *rb);
 }
 
 size_t tde_brick_flags_bytes(const tde_round_buffer *rb) {
@@ -312,13 +312,13 @@ int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, f
                           uint8_t *brick_flags, void *stream) {
     int st = integrate_checks(depth_scaled, volume, format, trunc, R_inv, t, intr, cell, rb, max_weight);
     if (st) return st;
-    TDE_REQUIRE(scratch && scratch_bytes >= tde_integrate_tsdf_scratch_bytes(intr->cols, intr->rows),
+    TDE_REQUIRE(scratch && scratch_bytes >= tde_integrate_tsdf_scratch_bytes(intr->cols, intr->rows, rb),
                 "integrate: scratch smaller than tde_integrate_tsdf_scratch_bytes()");
+    TDE_REQUIRE((reinterpret_cast<uintptr_t>(scratch) & 255) == 0, "integrate: scratch must be 256-byte aligned");
     cudaStream_t s = as_stream(stream);
-    float *dmax = static_cast<float *>(scratch);
-    if ((st = launch_depth_max(depth_scaled, intr->cols, intr->rows, dmax, s))) return st;
+    if ((st = launch_depth_max(depth_scaled, intr->cols, intr->rows, static_cast<float *>(scratch), s))) return st;
     IntegrateParams P = integrate_params(trunc, R_inv, t, intr, cell, rb, max_weight);
-    return launch_integrate(depth_scaled, volume, format, P, dmax, brick_flags, nullptr, s);
+    return launch_integrate(depth_scaled, volume, format, P, scratch, brick_flags, nullptr, s);
 }
 
 int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
@@ -327,7 +327,7 @@ int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, floa
     int st = integrate_checks(depth_scaled, volume, format, trunc, R_inv, t, intr, cell, rb, max_weight);
     if (st) return st;
     cudaStream_t s = as_stream(stream);
-    const size_t sb = tde_integrate_tsdf_scratch_bytes(intr->cols, intr->rows);
+    const size_t sb = tde_integrate_tsdf_scratch_bytes(intr->cols, intr->rows, rb);
     void *scratch = nullptr;
     cudaError_t e = cudaMallocAsync(&scratch, sb, s);
     if (e != cudaSuccess) return set_error(TDE_ERR_OOM, "integrate: scratch: %s", cudaGetErrorString(e));

@@ -17,30 +17,38 @@ __global__ void __launch_bounds__(kBX *kBY) bilateral_kernel(const uint16_t *__r
                                                              float inv_half_ss, float inv_half_sc,
                                                              uint32_t max_mm, float *__restrict__ vmap,
                                                              float fx, float fy, float cx, float cy) {
-    __shared__ uint16_t tile[kTileH][kTileW + 2];
+    // depths staged as floats: int->float conversion runs at a quarter of the
+    // FMA rate, so it is done once per pixel instead of three times per tap
+    __shared__ float tile[kTileH][kTileW + 1];
+    __shared__ float s_space[2 * kBR + 1][2 * kBR + 1];
     const int bx0 = blockIdx.x * kBX - kBR, by0 = blockIdx.y * kBY - kBR;
     const int tid = threadIdx.y * kBX + threadIdx.x;
     for (int i = tid; i < kTileH * kTileW; i += kBX * kBY) {
         int ty = i / kTileW, tx = i - ty * kTileW;
         int gx = bx0 + tx, gy = by0 + ty;
-        tile[ty][tx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? src[(size_t)gy * W + gx] : (uint16_t)0;
+        tile[ty][tx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? (float)src[(size_t)gy * W + gx] : 0.f;
+    }
+    if (tid < (2 * kBR + 1) * (2 * kBR + 1)) {
+        const int dy = tid / (2 * kBR + 1) - kBR, dx = tid % (2 * kBR + 1) - kBR;
+        s_space[dy + kBR][dx + kBR] = (float)(dx * dx + dy * dy) * inv_half_ss;
     }
     __syncthreads();
     const int col = blockIdx.x * kBX + threadIdx.x, row = blockIdx.y * kBY + threadIdx.y;
     if (col >= W || row >= H) return;
-    const int value = tile[threadIdx.y + kBR][threadIdx.x + kBR];
+    const float value = tile[threadIdx.y + kBR][threadIdx.x + kBR];
     const int max_x = min(col + kBR + 1, W - 1), max_y = min(row + kBR + 1, H - 1);
     const int min_x = max(col - kBR, 0), min_y = max(row - kBR, 0);
     float sum1 = 0.f, sum2 = 0.f;
     for (int cy = min_y; cy < max_y; ++cy) {
-        const uint16_t *trow = &tile[cy - by0][0];
-        const int dy2 = (row - cy) * (row - cy);
+        const float *trow = &tile[cy - by0][0];
+        const float *srow = &s_space[cy - row + kBR][0];
         for (int cx = min_x; cx < max_x; ++cx) {
-            int tmp = trow[cx - bx0];
-            int space2 = (col - cx) * (col - cx) + dy2;
-            int color2 = (value - tmp) * (value - tmp);
-            float w = __expf(-((float)space2 * inv_half_ss + (float)color2 * inv_half_sc));
-            sum1 = fmaf((float)tmp, w, sum1);
+            const float tmp = trow[cx - bx0];
+            // |value - tmp| <= 65535: the square is exact in float up to 2^24,
+            // beyond which the weight underflows to 0 either way
+            const float d = value - tmp;
+            const float w = __expf(-(srow[cx - col + kBR] + (d * d) * inv_half_sc));
+            sum1 = fmaf(tmp, w, sum1);
             sum2 += w;
         }
     }

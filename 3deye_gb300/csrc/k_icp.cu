@@ -2,10 +2,12 @@
 //
 // One launch per ICP iteration: every thread associates a few pixels and
 // accumulates the 27 upper-triangular terms of [J^T J | J^T r] (+ an inlier
-// count) as compensated float pairs; warps and the block combine the pairs;
-// each block writes its partials; the last block to finish sums the partials
-// in block order (deterministic), and, in the pipeline form, solves the 6x6
-// system in FP64 and updates the device-resident pose.
+// count); a warp transpose-reduction with TwoSum pairs and a block pass give
+// each block's totals as float-float values; each block adds them, converted
+// exactly to 126-bit fixed point, into integer accumulators with atomics --
+// integer addition is associative, so the grid total is the same bits in any
+// block order; the last block to finish reads the totals and, in the pipeline
+// form, solves the 6x6 system to FP64 accuracy and updates the device pose.
 //
 // Built with -fmad=false so the per-pixel association and terms are the same
 // IEEE float operations as the CPU oracle: inlier sets match exactly.
@@ -17,6 +19,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kPixPerThread = 4;
+constexpr int kTailSlices = 9;  // 9 x 28 = 252 threads of the last block
 
 struct f2 { float hi, lo; };
 
@@ -63,11 +66,9 @@ struct Assoc {
     int j;        // model pixel, -1 when rejected
 };
 
-__device__ __forceinline__ Assoc project(const IcpArgs &a, const IcpPose &P, int p) {
+__device__ __forceinline__ Assoc project(const IcpArgs &a, const IcpPose &P, float3 n, float3 v) {
     Assoc r;
     r.j = -1;
-    const float3 n = ld3(a.ncur, (size_t)p);
-    const float3 v = ld3(a.vcur, (size_t)p);
     if (isnan(n.x)) return r;
     const float3 rv = mv(P.R_cur, v);
     r.vg = make_float3(rv.x + P.t_cur[0], rv.y + P.t_cur[1], rv.z + P.t_cur[2]);
@@ -126,44 +127,46 @@ __device__ __forceinline__ void rodrigues_coeffs(double th2, double &A, double &
     }
 }
 
-// Returns false (pose unchanged) when A is not positive definite.
-__device__ bool warp_solve_and_update(IcpState *st, const double *sums, int lane) {
-    __shared__ double L[6][6], D[6], z[6], x[6], Rinc[9];
-    __shared__ int ok;
-    // lane i < 6 owns row i of [A | b]
-    double a[6], bi = 0.0;
-    #pragma unroll
-    for (int k = 0; k < 6; ++k) a[k] = 0.0;
+// Loads the unpacked system into shared memory (lanes 0..5, one row each).
+__device__ __forceinline__ void unpack_system(const double *sums, int lane, double (&A)[6][6], double (&b)[6]) {
     if (lane < 6) {
         int s = 0;
         for (int k = 0; k < 6; ++k)
             for (int j = k; j < 7; ++j, ++s) {
-                if (k == lane) { if (j == 6) bi = sums[s]; else a[j] = sums[s]; }
-                else if (j == lane) a[k] = sums[s];
+                if (k == lane) { if (j == 6) b[lane] = sums[s]; else A[lane][j] = sums[s]; }
+                else if (j == lane) A[lane][k] = sums[s];
             }
     }
+    __syncwarp();
+}
+
+// FP64 LDL^T solve, one row per lane.  False when A is not positive definite.
+__device__ bool fp64_ldlt_solve(const double (&A)[6][6], const double (&b)[6], int lane, double (&xo)[6]) {
+    // E_jk = L_jk D_k is kept beside L so each column costs one FMA chain
+    __shared__ double L[6][6], E[6][6], D[6], z[6];
+    __shared__ int ok;
     if (lane == 0) ok = 1;
     __syncwarp();
     #pragma unroll
     for (int j = 0; j < 6; ++j) {
-        // t_i = A_ij - sum_k L_ik L_jk D_k
-        double t = a[j];
+        // t_i = A_ij - sum_k L_ik E_jk
+        double t = lane < 6 ? A[lane][j] : 0.0;
         #pragma unroll
         for (int k = 0; k < j; ++k)
-            if (lane < 6) t = fma(-(lane > k ? L[lane][k] : 0.0), L[j][k] * D[k], t);
+            if (lane > k && lane < 6) t = fma(-L[lane][k], E[j][k], t);
         if (lane == j) {
             D[j] = t;
             if (!(t > 1e-30)) ok = 0;
         }
         __syncwarp();
         const double inv = rcp64(D[j]);
-        if (lane > j && lane < 6) L[lane][j] = t * inv;
+        if (lane > j && lane < 6) { L[lane][j] = t * inv; E[lane][j] = t; }
         if (lane == j) L[j][j] = 1.0;
         __syncwarp();
     }
     if (!ok) return false;
     // L z = b (lane i accumulates as z_k arrive), then y = z / D, L^T x = y
-    double acc = bi;
+    double acc = lane < 6 ? b[lane] : 0.0;
     #pragma unroll
     for (int k = 0; k < 6; ++k) {
         if (lane == k) z[k] = acc;
@@ -174,11 +177,21 @@ __device__ bool warp_solve_and_update(IcpState *st, const double *sums, int lane
     acc = lane < 6 ? z[lane] * rcp64(D[lane]) : 0.0;
     #pragma unroll
     for (int k = 5; k >= 0; --k) {
-        if (lane == k) x[k] = acc;
+        if (lane == k) xo[k] = acc;
         __syncwarp();
-        if (lane < k) acc = fma(-L[k][lane], x[k], acc);
+        if (lane < k) acc = fma(-L[k][lane], xo[k], acc);
     }
     __syncwarp();
+    return true;
+}
+
+// Solve and apply the update to the device pose; false (pose unchanged) when
+// A is not positive definite.
+__device__ bool warp_solve_and_update(IcpState *st, const double *sums, int lane) {
+    __shared__ double A[6][6], b[6], Rinc[9];
+    unpack_system(sums, lane, A, b);
+    __shared__ double x[6];
+    if (!fp64_ldlt_solve(A, b, lane, x)) return false;
     // Rinc = I + A [w]x + B (w w^T - th2 I), lanes 0..8 one entry each
     const double wx = x[0], wy = x[1], wz = x[2];
     const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
@@ -209,6 +222,34 @@ __device__ bool warp_solve_and_update(IcpState *st, const double *sums, int lane
     else if (lane < 12) { st->t[lane - 9] = out; st->pose.t_cur[lane - 9] = (float)out; }
     if (lane < 6) st->x[lane] = x[lane];
     return true;
+}
+
+// ---------------------------------------------------------------------------
+// Exact fixed point: value * 2^64 as a 128-bit integer.  A float is M * 2^(E-150)
+// with a 24-bit M, so the product is M shifted by E - 86; bits below 2^-64
+// are dropped (truncation toward zero), nothing else is rounded.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ __int128 to_fixed(float f) {
+    const unsigned u = __float_as_uint(f);
+    const int E = (int)((u >> 23) & 0xffu);
+    if (E == 0 || E == 0xff) return 0;  // zero, subnormal (< 1.2e-38), or not finite
+    const unsigned long long M = (unsigned long long)((u & 0x7fffffu) | 0x800000u);
+    const int sh = E - 86;
+    __int128 q;
+    if (sh >= 0) q = sh > 100 ? ((__int128)1 << 124) : ((__int128)M << sh);  // saturate far beyond any sum
+    else q = sh > -24 ? (__int128)(M >> -sh) : 0;
+    return (u >> 31) ? -q : q;
+}
+
+// Sum of the three 42-bit limbs modulo 2^126, read as a signed value.
+__device__ __forceinline__ double from_fixed(unsigned long long a0, unsigned long long a1, unsigned long long a2) {
+    unsigned __int128 S = (unsigned __int128)a0 + ((unsigned __int128)a1 << 42) + ((unsigned __int128)a2 << 84);
+    S &= ((unsigned __int128)1 << 126) - 1;
+    __int128 v = (__int128)S;
+    if ((S >> 125) & 1) v -= (__int128)1 << 126;
+    const long long hi = (long long)(v >> 64);  // floor(v / 2^64)
+    const unsigned long long lo = (unsigned long long)v;
+    return (double)hi + (double)lo * 0x1p-64;
 }
 
 // Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
@@ -248,6 +289,25 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
     __shared__ unsigned ticket;
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
+    // Let the next ICP launch start: it only reads this launch's results
+    // (pose, accumulators, counter) after its own griddepcontrol.wait.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+
+    const int npix = a.W * a.H;
+    const int base = blockIdx.x * kThreads * kPixPerThread + tid;
+    // this thread's current-frame maps do not depend on the pose: load them
+    // before waiting for the previous iteration
+    float3 nc[kPixPerThread], vc[kPixPerThread];
+    const float qnan = __int_as_float(0x7fffffff);
+    #pragma unroll
+    for (int k = 0; k < kPixPerThread; ++k) {
+        const int p = base + k * kThreads;
+        if (p < npix) { nc[k] = ld3(a.ncur, (size_t)p); vc[k] = ld3(a.vcur, (size_t)p); }
+        else { nc[k] = make_float3(qnan, qnan, qnan); vc[k] = nc[k]; }
+    }
+    // wait for the previous launch in the stream (a no-op without a
+    // programmatic dependency)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (tid < (int)(sizeof(IcpPose) / sizeof(float)))
         reinterpret_cast<float *>(&P)[tid] = reinterpret_cast<const float *>(&st->pose)[tid];
     __syncthreads();
@@ -255,16 +315,9 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
     float s[32];
     #pragma unroll
     for (int t = 0; t < 32; ++t) s[t] = 0.f;
-
-    const int npix = a.W * a.H;
-    const int base = blockIdx.x * kThreads * kPixPerThread + tid;
     Assoc as[kPixPerThread];
     #pragma unroll
-    for (int k = 0; k < kPixPerThread; ++k) {
-        const int p = base + k * kThreads;
-        if (p < npix) as[k] = project(a, P, p);
-        else as[k].j = -1;
-    }
+    for (int k = 0; k < kPixPerThread; ++k) as[k] = project(a, P, nc[k], vc[k]);
     float3 np[kPixPerThread], vp[kPixPerThread];
     #pragma unroll
     for (int k = 0; k < kPixPerThread; ++k)
@@ -284,38 +337,41 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
     const f2 wsum = warp_transpose_reduce(s, lane);
     red[warp][lane] = wsum;
     __syncthreads();
-    const int nb = gridDim.x;
     if (tid < kIcpTerms) {
         f2 v = red[0][tid];
         #pragma unroll
         for (int w = 1; w < kThreads / 32; ++w) v = add_ff(v, red[w][tid]);
-        gbuf[(size_t)tid * nb + blockIdx.x] = v.hi;
-        gbuf[(size_t)(kIcpTerms + tid) * nb + blockIdx.x] = v.lo;
+        const unsigned __int128 q = (unsigned __int128)(to_fixed(v.hi) + to_fixed(v.lo));
+        const unsigned long long m42 = (1ull << 42) - 1ull;
+        unsigned long long *acc = st->acc[blockIdx.x % kIcpAccCopies][tid];
+        atomicAdd(acc + 0, (unsigned long long)q & m42);
+        atomicAdd(acc + 1, (unsigned long long)(q >> 42) & m42);
+        atomicAdd(acc + 2, (unsigned long long)(q >> 84) & m42);
     }
     __threadfence();
     __syncthreads();
     if (tid == 0) ticket = atomicAdd(&st->counter, 1u);
     __syncthreads();
-    if (ticket != (unsigned)nb - 1) return;
+    if (ticket != (unsigned)gridDim.x - 1) return;
 
-    // ---- last block: deterministic cross-block sum, one warp per term ----
+    // ---- last block: read the exact integer totals, reset them, solve ----
     __shared__ double s_sums[kIcpTerms];
     __threadfence();
-    for (int t = warp; t < kIcpTerms; t += kThreads / 32) {
-        f2 v{0.f, 0.f};
-        for (int b = lane; b < nb; b += 32) {
-            f2 o{__ldcg(gbuf + (size_t)t * nb + b), __ldcg(gbuf + (size_t)(kIcpTerms + t) * nb + b)};
-            v = add_ff(v, o);
-        }
+    if (tid < kIcpTerms) {
+        unsigned long long a[kIcpAccCopies][3];
         #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            f2 o{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
-            v = add_ff(v, o);
+        for (int c = 0; c < kIcpAccCopies; ++c)
+            #pragma unroll
+            for (int l = 0; l < 3; ++l) a[c][l] = __ldcg(&st->acc[c][tid][l]);
+        unsigned long long a0 = 0, a1 = 0, a2 = 0;
+        #pragma unroll
+        for (int c = 0; c < kIcpAccCopies; ++c) {
+            a0 += a[c][0]; a1 += a[c][1]; a2 += a[c][2];
+            st->acc[c][tid][0] = 0ull; st->acc[c][tid][1] = 0ull; st->acc[c][tid][2] = 0ull;
         }
-        if (lane == 0) {
-            s_sums[t] = (double)v.hi + (double)v.lo;
-            if (mbuf && t < 27) mbuf[t] = v.hi + v.lo;
-        }
+        const double d = from_fixed(a0, a1, a2);
+        s_sums[tid] = d;
+        if (mbuf && tid < 27) mbuf[tid] = (float)d;
     }
     __syncthreads();
     if (warp != 0) return;
@@ -367,14 +423,27 @@ __global__ void icp_begin_frame_kernel(IcpState *st) {
 }  // namespace
 
 size_t icp_gbuf_floats(int W, int H) {
-    size_t nb = div_up((unsigned)(W * H), (unsigned)(kThreads * kPixPerThread));
-    return 2 * kIcpTerms * nb;
+    // cross-block sums go through the state's integer accumulators
+    (void)W;
+    (void)H;
+    return 64;
 }
 
-int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, cudaStream_t stream) {
-    unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * kPixPerThread));
-    if (solve) icp_kernel<true><<<nb, kThreads, 0, stream>>>(a, st, gbuf, mbuf);
-    else icp_kernel<false><<<nb, kThreads, 0, stream>>>(a, st, gbuf, mbuf);
+int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, bool overlap_previous,
+               cudaStream_t stream) {
+    const unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * kPixPerThread));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nb);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = overlap_previous ? 1 : 0;
+    cudaError_t e = solve ? cudaLaunchKernelEx(&cfg, icp_kernel<true>, a, st, gbuf, mbuf)
+                          : cudaLaunchKernelEx(&cfg, icp_kernel<false>, a, st, gbuf, mbuf);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "estimate_combined: %s", cudaGetErrorString(e));
     return check_launch("estimate_combined");
 }
 

@@ -2,13 +2,13 @@
 // common/src/opencl_wrappers.cpp:21-64; the reference kernel
 // integrate_tsdf_volume is absent, this follows the KinectFusion update).
 //
-// Work is organised in 8^3-voxel bricks.  Each thread of a block first tests
-// one brick against the frame: the brick's voxel-centre box is projected
-// (8 corners) and, if it lies entirely behind the camera, outside the image,
-// or farther from the camera than the largest observed depth over the pixels
-// it covers plus the truncation distance, none of its voxels can pass the
-// per-voxel test, so the brick is dropped.  The block then sweeps its
-// surviving bricks one warp per brick and applies the per-voxel update --
+// Work is organised in 8^3-voxel bricks.  A first kernel tests each brick
+// against the frame: the brick's voxel-centre box is projected (8 corners)
+// and, if it lies entirely behind the camera, outside the image, or farther
+// from the camera than the largest observed depth over the pixels it covers
+// plus the truncation distance, none of its voxels can pass the per-voxel
+// test, so the brick is dropped.  A second kernel sweeps the surviving bricks,
+// one warp per brick, and applies the per-voxel update --
 // the same IEEE float operations, in the same order, as the CPU oracle, which
 // visits every voxel.  Culling only removes voxels the exact test rejects, so
 // volumes are bit-identical.
@@ -20,11 +20,12 @@
 #include "tde_common.cuh"
 #include "tde_integrate.cuh"
 
+#include <algorithm>
+
 namespace tde {
 namespace {
 
 constexpr int kBrick = 8;
-constexpr int kBricksPerBlock = 256;
 
 // ---------------------------------------------------------------------------
 // Max scaled depth per 16x16 tile (level 0) and per 32..256 tiles (levels 1-4,
@@ -112,16 +113,13 @@ __device__ bool brick_culled(const IntegrateParams &P, const Pose &q, const Dept
     return sqrtf(d2) > dmax + P.trunc + 1e-3f + 1e-4f * dmax;
 }
 
-template <int FMT>
-__global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
-                                                               const IntegrateParams P, const DepthMaxPyramid pyr,
-                                                               uint8_t *__restrict__ neg_flags,
-                                                               unsigned long long *__restrict__ stats) {
+// One thread per brick: surviving bricks are appended to a global list (its
+// order varies run to run; every brick owns disjoint voxels, so the result
+// does not depend on it).
+__global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams P, const DepthMaxPyramid pyr,
+                                                          int *__restrict__ list, int *__restrict__ count) {
     __shared__ Pose q;
-    __shared__ int s_list[kBricksPerBlock];
-    __shared__ int s_wbase[kBricksPerBlock / 32];
-    __shared__ int s_n;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (tid < 12) {
         float v;
         if (P.dpose) v = tid < 9 ? P.dpose->R_inv[tid] : P.dpose->t[tid - 9];
@@ -131,35 +129,44 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
     __syncthreads();
     const tde_point3i &Nv = P.rb.voxels_size;
     const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick, nbz = (Nv.z + kBrick - 1) / kBrick;
-    const int nbricks = nbx * nby * nbz;
-    // --- cull: one brick per thread, survivors listed in brick order ---
-    {
-        const int b = blockIdx.x * kBricksPerBlock + tid;
-        bool keep = false;
-        if (b < nbricks) {
-            const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
-            keep = !brick_culled(P, q, pyr, bx, by, bz);
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) s_wbase[warp] = __popc(m);
-        __syncthreads();
-        if (tid == 0) {
-            int acc = 0;
-            for (int w = 0; w < kBricksPerBlock / 32; ++w) { int c = s_wbase[w]; s_wbase[w] = acc; acc += c; }
-            s_n = acc;
-        }
-        __syncthreads();
-        if (keep) s_list[s_wbase[warp] + __popc(m & ((1u << lane) - 1u))] = b;
-        __syncthreads();
+    const int b = blockIdx.x * blockDim.x + tid;
+    bool keep = false;
+    if (b < nbx * nby * nbz) keep = !brick_culled(P, q, pyr, b % nbx, (b / nbx) % nby, b / (nbx * nby));
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = b;
+}
+
+// One warp per surviving brick (16 voxels per lane), grid-strided over the
+// list so the work spreads over every SM whatever the scene's layout.
+template <int FMT>
+__global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
+                                                               const IntegrateParams P, const int *__restrict__ list,
+                                                               const int *__restrict__ count,
+                                                               uint8_t *__restrict__ neg_flags,
+                                                               unsigned long long *__restrict__ stats) {
+    __shared__ Pose q;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < 12) {
+        float v;
+        if (P.dpose) v = tid < 9 ? P.dpose->R_inv[tid] : P.dpose->t[tid - 9];
+        else v = tid < 9 ? P.R_inv[tid] : P.t[tid - 9];
+        if (tid < 9) q.Ri[tid] = v; else q.t[tid - 9] = v;
     }
-    // --- sweep the surviving bricks, one warp per brick ---
+    __syncthreads();
+    const tde_point3i &Nv = P.rb.voxels_size;
+    const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick;
     typedef TsdfStore<FMT> S;
     const float ntrunc = -P.trunc;
     const int W = P.intr.cols, H = P.intr.rows;
     const float fx = P.intr.fx, fy = P.intr.fy, ccx = P.intr.cx, ccy = P.intr.cy;
+    const int n_list = *count;
+    const int gwarp = (blockIdx.x * blockDim.x + tid) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned n_read = 0, n_written = 0;
-    for (int i = warp; i < s_n; i += kBricksPerBlock / 32) {
-        const int b = s_list[i];
+    for (int i = gwarp; i < n_list; i += nwarps) {
+        const int b = list[i];
         const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
         const int x = bx * kBrick + (lane & 7);
         const float gx = ((float)x + 0.5f) * P.cell.x - q.t[0];
@@ -235,6 +242,7 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
             atomicAdd(stats, (unsigned long long)r);
             atomicAdd(stats + 1, (unsigned long long)w);
         }
+        if (blockIdx.x == 0 && tid == 0) atomicAdd(stats + 2, (unsigned long long)n_list);
     }
 }
 
@@ -277,12 +285,32 @@ size_t brick_count(const tde_round_buffer &rb) {
            ((rb.voxels_size.z + kBrick - 1) / kBrick);
 }
 
-int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P,
-                     const float *depth_max, uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream) {
-    const DepthMaxPyramid pyr = depth_max_layout(const_cast<float *>(depth_max), P.intr.cols, P.intr.rows);
-    const unsigned blocks = div_up((unsigned)brick_count(P.rb), kBricksPerBlock);
+size_t integrate_scratch_bytes(int W, int H, const tde_round_buffer &rb) {
+    // depth-max pyramid, then (aligned) the brick counter and the brick list
+    const size_t dm = ((depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
+    return dm + 256 + brick_count(rb) * sizeof(int);
+}
+
+int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P, void *scratch,
+                     uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream) {
+    const int W = P.intr.cols, H = P.intr.rows;
+    float *dmax = static_cast<float *>(scratch);
+    const size_t dm = ((depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
+    int *count = reinterpret_cast<int *>(static_cast<char *>(scratch) + dm);
+    int *list = reinterpret_cast<int *>(static_cast<char *>(scratch) + dm + 256);
+    const DepthMaxPyramid pyr = depth_max_layout(dmax, W, H);
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "integrate: %s", cudaGetErrorString(e));
+    const unsigned nb = (unsigned)brick_count(P.rb);
+    cull_bricks_kernel<<<div_up(nb, 256u), 256, 0, stream>>>(P, pyr, list, count);
+    int st = check_launch("integrate/cull");
+    if (st) return st;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned blocks = std::min(div_up(nb, 8u), (unsigned)sms * 8u);
     return dispatch_format(format, [&](auto F) {
-        integrate_bricks_kernel<decltype(F)::value><<<blocks, 256, 0, stream>>>(depth_scaled, volume, P, pyr,
+        integrate_bricks_kernel<decltype(F)::value><<<blocks, 256, 0, stream>>>(depth_scaled, volume, P, list, count,
                                                                                neg_flags, stats);
         return check_launch("integrate_tsdf");
     });

@@ -63,6 +63,9 @@ __global__ void finalize_kernel(IcpState *st, const PrevPose *prev, CamPose *cam
 }
 
 enum Segment { SEG_TRACK_FIRST, SEG_TRACK, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE, SEG_COUNT };
+// Events per timed frame: before tracking, after tracking, after integration,
+// after raycast, after the model pyramid.
+constexpr int kEvents = 5;
 
 }  // namespace
 }  // namespace tde
@@ -87,7 +90,7 @@ struct tde_pipeline {
     CamPose *cam = nullptr;
     FrameOut *out = nullptr;
     unsigned long long *stats = nullptr;
-    float *dmax = nullptr;        // per-tile maximum depth (integration culling)
+    void *iscratch = nullptr;     // integration: per-tile maximum depth + brick list
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     void *volume = nullptr;
     // graphs: per segment and the whole frame
@@ -97,7 +100,7 @@ struct tde_pipeline {
     int frames = 0;
     // timing
     int timing_cap = 0, timing_n = 0;
-    std::vector<cudaEvent_t> ev;  // 4 per timed frame
+    std::vector<cudaEvent_t> ev;  // kEvents per timed frame
 };
 
 namespace {
@@ -146,20 +149,21 @@ int record_segment(tde_pipeline *p, Segment seg) {
                 a.W = p->intr[l].cols; a.H = p->intr[l].rows;
                 a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
                 a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
-                for (int it = 0; it < c.icp_iters[l]; ++it) TDE_TRY(launch_icp(a, p->st, p->gbuf, nullptr, true, s));
+                for (int it = 0; it < c.icp_iters[l]; ++it)
+                    TDE_TRY(launch_icp(a, p->st, p->gbuf, nullptr, true, true, s));
             }
         }
         finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_TRACK);
         TDE_TRY(check_launch("finalize_pose"));
         TDE_TRY(launch_scale_depth(p->raw, p->scaled, p->intr[0], s));
-        return launch_depth_max(p->scaled, W, H, p->dmax, s);
+        return launch_depth_max(p->scaled, W, H, static_cast<float *>(p->iscratch), s);
     }
     case SEG_INTEGRATE: {
         IntegrateParams P;
         std::memset(&P, 0, sizeof(P));
         P.trunc = c.trunc; P.max_weight = c.max_weight; P.intr = p->intr[0]; P.rb = p->rb; P.cell = p->cell;
         P.n = voxel_count(p->rb); P.dpose = p->cam;
-        return launch_integrate(p->scaled, p->volume, c.tsdf_format, P, p->dmax, p->negflags, p->stats, s);
+        return launch_integrate(p->scaled, p->volume, c.tsdf_format, P, p->iscratch, p->negflags, p->stats, s);
     }
     case SEG_RAYCAST: {
         tde_point3f t0{0, 0, 0};
@@ -247,7 +251,7 @@ void release(tde_pipeline *p) {
         cudaFree(p->depth[l]); cudaFree(p->vcur[l]); cudaFree(p->ncur[l]); cudaFree(p->vmod[l]); cudaFree(p->nmod[l]);
     }
     cudaFree(p->scaled); cudaFree(p->gbuf); cudaFree(p->st); cudaFree(p->prev); cudaFree(p->cam); cudaFree(p->out);
-    cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->dmax); cudaFree(p->negflags);
+    cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->iscratch); cudaFree(p->negflags);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -298,13 +302,14 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     if ((st = dalloc(&p->gbuf, icp_gbuf_floats(c.intr.cols, c.intr.rows), "icp partials")) ||
         (st = dalloc(&p->st, 1, "icp state")) || (st = dalloc(&p->prev, 1, "prev pose")) ||
         (st = dalloc(&p->cam, 1, "camera pose")) || (st = dalloc(&p->out, 1, "frame out")) ||
-        (st = dalloc(&p->stats, 2, "stats")) ||
-        (st = dalloc(&p->dmax, depth_max_floats(c.intr.cols, c.intr.rows), "depth max")) ||
+        (st = dalloc(&p->stats, 3, "stats")) ||
+        (st = dalloc(reinterpret_cast<char **>(&p->iscratch), integrate_scratch_bytes(c.intr.cols, c.intr.rows, p->rb),
+                     "integration scratch")) ||
         (st = dalloc(&p->negflags, brick_count(p->rb), "brick flags")))
         return fail(st);
     e = cudaMemsetAsync(p->negflags, 0, brick_count(p->rb), p->stream);
     if (e != cudaSuccess) return fail(cuda_fail(e, "brick flags"));
-    e = cudaMemsetAsync(p->stats, 0, 2 * sizeof(unsigned long long), p->stream);
+    e = cudaMemsetAsync(p->stats, 0, 3 * sizeof(unsigned long long), p->stream);
     if (e != cudaSuccess) return fail(cuda_fail(e, "stats"));
     if (!c.integrate_stats) { cudaFree(p->stats); p->stats = nullptr; }
     // model maps start empty (NaN) so the first ICP finds nothing before a raycast
@@ -337,15 +342,16 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
     if (p->cfg.use_graphs && !timed) {
         TDE_CUDA(cudaGraphLaunch(p->full_exec[first ? 0 : 1], p->stream), "graph launch");
     } else {
-        TDE_TRY(run_segment(p, first ? SEG_TRACK_FIRST : SEG_TRACK));
-        cudaEvent_t *ev = timed ? &p->ev[4 * p->timing_n] : nullptr;
+        cudaEvent_t *ev = timed ? &p->ev[kEvents * p->timing_n] : nullptr;
         if (ev) TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
-        TDE_TRY(run_segment(p, SEG_INTEGRATE));
+        TDE_TRY(run_segment(p, first ? SEG_TRACK_FIRST : SEG_TRACK));
         if (ev) TDE_CUDA(cudaEventRecord(ev[1], p->stream), "event");
+        TDE_TRY(run_segment(p, SEG_INTEGRATE));
         if (ev) TDE_CUDA(cudaEventRecord(ev[2], p->stream), "event");
         TDE_TRY(run_segment(p, SEG_RAYCAST));
         if (ev) TDE_CUDA(cudaEventRecord(ev[3], p->stream), "event");
         TDE_TRY(run_segment(p, SEG_RESIZE));
+        if (ev) TDE_CUDA(cudaEventRecord(ev[4], p->stream), "event");
         if (timed) p->timing_n++;
     }
     if (pose_out12)
@@ -413,7 +419,7 @@ int tde_pipeline_enable_timing(tde_pipeline *p, int capacity) {
     if (!p || capacity < 0) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enable_timing: bad argument");
     TDE_TRY(tde_pipeline_sync(p));
     for (auto e : p->ev) cudaEventDestroy(e);
-    p->ev.assign((size_t)4 * capacity, nullptr);
+    p->ev.assign((size_t)kEvents * capacity, nullptr);
     for (auto &e : p->ev) TDE_CUDA(cudaEventCreate(&e), "event create");
     p->timing_cap = capacity;
     p->timing_n = 0;
@@ -421,13 +427,20 @@ int tde_pipeline_enable_timing(tde_pipeline *p, int capacity) {
 }
 
 int tde_pipeline_timings(tde_pipeline *p, float *integrate_ms, float *raycast_ms, int capacity) {
+    return tde_pipeline_stage_timings(p, nullptr, integrate_ms, raycast_ms, nullptr, capacity);
+}
+
+int tde_pipeline_stage_timings(tde_pipeline *p, float *track_ms, float *integrate_ms, float *raycast_ms,
+                               float *resize_ms, int capacity) {
     if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_timings: null");
     TDE_TRY(tde_pipeline_sync(p));
     int n = p->timing_n < capacity ? p->timing_n : capacity;
-    for (int i = 0; i < n; ++i) {
-        if (integrate_ms) TDE_CUDA(cudaEventElapsedTime(&integrate_ms[i], p->ev[4 * i], p->ev[4 * i + 1]), "elapsed");
-        if (raycast_ms) TDE_CUDA(cudaEventElapsedTime(&raycast_ms[i], p->ev[4 * i + 2], p->ev[4 * i + 3]), "elapsed");
-    }
+    float *out[4] = {track_ms, integrate_ms, raycast_ms, resize_ms};
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 4; ++k)
+            if (out[k])
+                TDE_CUDA(cudaEventElapsedTime(&out[k][i], p->ev[kEvents * i + k], p->ev[kEvents * i + k + 1]),
+                         "elapsed");
     return n;
 }
 
@@ -435,10 +448,11 @@ int tde_pipeline_integrate_stats(tde_pipeline *p, uint64_t *rw, int reset) {
     if (!p || !rw) return set_error(TDE_ERR_INVALID_ARG, "pipeline_integrate_stats: null");
     if (!p->stats) return set_error(TDE_ERR_UNSUPPORTED, "pipeline_integrate_stats: created without integrate_stats");
     TDE_TRY(tde_pipeline_sync(p));
-    unsigned long long h[2];
+    unsigned long long h[3];
     TDE_CUDA(cudaMemcpy(h, p->stats, sizeof(h), cudaMemcpyDeviceToHost), "stats");
     rw[0] = h[0];
     rw[1] = h[1];
+    rw[2] = h[2];
     if (reset) TDE_CUDA(cudaMemset(p->stats, 0, sizeof(h)), "stats reset");
     return TDE_OK;
 }
@@ -448,8 +462,8 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p) {
     int icp = 0;
     for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
     // bilateral, pyramid levels, normal maps, begin, ICP, finalize, scale,
-    // depth max, integrate, raycast, 2 resizes per coarser level
-    return 1 + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
+    // depth max, brick cull, integrate, raycast, 2 resizes per coarser level
+    return 1 + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
 }
 
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {

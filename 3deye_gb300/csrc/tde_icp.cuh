@@ -7,6 +7,7 @@ namespace tde {
 constexpr int kIcpTerms = 28;        // 27 system terms + inlier count
 constexpr int kIcpMinInliers = 6;    // fewer pairs cannot constrain 6 DoF
 constexpr int kIcpStatusSolveFailed = 1;
+constexpr int kIcpAccCopies = 8;
 
 // Float pose consumed by the association: current estimate (camera ->
 // global) and the previous frame's inverse (global -> previous camera).
@@ -25,6 +26,10 @@ struct IcpState {
     int status, inliers, iterations, pad0;
     unsigned counter;  // blocks done in the running launch (reset by the last block)
     unsigned pad1[3];
+    // Cross-block sums as 126-bit fixed point (2^-64 units) in three 42-bit
+    // limbs; integer atomics make the total independent of block order.
+    // Block b adds into copy b % kIcpAccCopies to spread atomic traffic.
+    unsigned long long acc[kIcpAccCopies][kIcpTerms][3];
 };
 
 struct IcpArgs {
@@ -55,7 +60,10 @@ __host__ __device__ inline void so3_exp(const double *x, double *R) {
 }
 
 size_t icp_gbuf_floats(int W, int H);
-int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, cudaStream_t stream);
+// overlap_previous: launch with a programmatic dependency on the previous
+// kernel in the stream (the kernel waits before reading anything it wrote).
+int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, bool overlap_previous,
+               cudaStream_t stream);
 int launch_icp_begin_frame(IcpState *st, cudaStream_t stream);
 
 }  // namespace tde

@@ -47,7 +47,10 @@ int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cu
 // neg_flags (may be null): per physical brick, set to 1 when a write leaves a
 // negative value there; a 0 therefore guarantees the brick holds no negative
 // TSDF value.
-int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P,
-                     const float *depth_max, uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream);
+// Scratch of one integration: the depth-max pyramid (filled by
+// launch_depth_max at its start) followed by the surviving-brick list.
+size_t integrate_scratch_bytes(int W, int H, const tde_round_buffer &rb);
+int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P, void *scratch,
+                     uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream);
 
 }  // namespace tde

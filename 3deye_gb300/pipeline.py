@@ -31,6 +31,7 @@ declare("tde_pipeline_frame_count", I, [P])
 declare("tde_pipeline_enable_timing", I, [P, I])
 declare("tde_pipeline_timings", I, [P, P, P, I])
 declare("tde_pipeline_integrate_stats", I, [P, P, I])
+declare("tde_pipeline_stage_timings", I, [P, P, P, P, P, I])
 declare("tde_pipeline_launches_per_frame", I, [P])
 declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
 declare("tde_pipeline_set_pose", I, [P, P])
@@ -130,9 +131,19 @@ class Pipeline:
             check(n)
         return a[:n], b[:n]
 
-    def integrate_stats(self, reset=False):
-        out = np.zeros(2, np.uint64)
+    def stage_timings(self, capacity: int):
+        """(track, integrate, raycast, resize) milliseconds per timed frame."""
+        a = [np.zeros(capacity, np.float32) for _ in range(4)]
+        n = lib.tde_pipeline_stage_timings(self._h, *[x.ctypes.data_as(P) for x in a], capacity)
+        if n < 0:
+            check(n)
+        return [x[:n] for x in a]
+
+    def integrate_stats(self, reset=False, bricks=False):
+        out = np.zeros(3, np.uint64)
         check(lib.tde_pipeline_integrate_stats(self._h, out.ctypes.data_as(P), int(reset)))
+        if bricks:
+            return int(out[0]), int(out[1]), int(out[2])
         return int(out[0]), int(out[1])
 
     def launches_per_frame(self) -> int:

@@ -242,8 +242,8 @@ def run_ours(args, ws, rank, local):
         p.sync()
     ms = e0.elapsed_time(e1)
     ms = max_over_ranks(ws, ms)
-    integ_ms, ray_ms = p.timings(K)
-    n_read, n_written = p.integrate_stats()
+    track_ms, integ_ms, ray_ms, resize_ms = p.stage_timings(K)
+    n_read, n_written, n_bricks = p.integrate_stats(bricks=True)
     pose_a = p.pose()
     p.close()
 
@@ -298,8 +298,10 @@ def run_ours(args, ws, rank, local):
                      "traffic": (traffic or {}).get("dram_bytes_per_launch"),
                      "alg_bytes_per_launch": int(alg_bytes), "avg_launch_ms": round(int_avg_ms, 5),
                      "voxels_read_per_launch": int(n_read / max(k_int, 1)),
-                     "voxels_written_per_launch": int(n_written / max(k_int, 1))},
-        "kernels_ms_per_frame": {"integrate": round(int_avg_ms, 5), "raycast": round(ray_avg_ms, 5)},
+                     "voxels_written_per_launch": int(n_written / max(k_int, 1)),
+                     "bricks_swept_per_launch": int(n_bricks / max(k_int, 1))},
+        "stages_ms_per_frame": {"track": round(float(np.mean(track_ms)), 5), "integrate": round(int_avg_ms, 5),
+                                "raycast": round(ray_avg_ms, 5), "model_pyramid": round(float(np.mean(resize_ms)), 5)},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches * K,

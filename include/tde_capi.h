@@ -200,14 +200,15 @@ int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, floa
                        void *stream);
 
 /* Integrate_Tsdf_Data with caller-provided memory: `scratch` (device,
- * tde_integrate_tsdf_scratch_bytes) holds the frame's per-tile maximum depth
- * used to skip 8^3 bricks that lie entirely more than trunc behind the
- * observed surface; tde_integrate_tsdf allocates it on the stream itself.
+ * 256-byte aligned, tde_integrate_tsdf_scratch_bytes) holds the frame's
+ * per-tile maximum depth, used to skip 8^3 bricks that lie entirely more than
+ * trunc behind the observed surface, and the list of surviving bricks;
+ * tde_integrate_tsdf allocates it on the stream itself.
  * `brick_flags` (device, tde_brick_flags_bytes, zero-initialised with the
  * volume; may be NULL) gets a 1 for every physical brick that receives a
  * negative value -- a 0 proves the brick has none, which the pipeline's
  * raycast uses to skip loads.  Same results as tde_integrate_tsdf. */
-size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows);
+size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows, const tde_round_buffer *rb);
 size_t tde_brick_flags_bytes(const tde_round_buffer *rb);
 int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, float trunc,
                           const tde_matrix3f *R_inv, const tde_point3f *t, const tde_intrinsics *intr,

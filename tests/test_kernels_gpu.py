@@ -123,13 +123,14 @@ def test_integrate_ex_brick_flags_are_sound(tde, orc, cuda, small, fmt):
     ti = tintr(tde, intr)
     L = tde.lib
     L.tde_integrate_tsdf_scratch_bytes.restype = C.c_size_t
+    L.tde_integrate_tsdf_scratch_bytes.argtypes = [C.c_int, C.c_int, C.POINTER(tde.RoundBuffer)]
     L.tde_brick_flags_bytes.restype = C.c_size_t
     L.tde_brick_flags_bytes.argtypes = [C.POINTER(tde.RoundBuffer)]
     L.tde_integrate_tsdf_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.POINTER(tde.Matrix3f),
                                         C.POINTER(tde.Point3f), C.POINTER(tde.Intrinsics), C.POINTER(tde.Point3f),
                                         C.POINTER(tde.RoundBuffer), C.c_int, C.c_void_p, C.c_size_t, C.c_void_p,
                                         C.c_void_p]
-    sb = L.tde_integrate_tsdf_scratch_bytes(intr.cols, intr.rows)
+    sb = L.tde_integrate_tsdf_scratch_bytes(intr.cols, intr.rows, C.byref(rb))
     scratch = torch.empty(sb, dtype=torch.uint8, device=cuda)
     nbr = L.tde_brick_flags_bytes(C.byref(rb))
     flags = torch.zeros(nbr, dtype=torch.uint8, device=cuda)
