@@ -303,7 +303,7 @@ size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows, const tde_round_buff
 
 size_t tde_brick_flags_bytes(const tde_round_buffer *rb) {
     if (!valid_round_buffer(rb)) return 0;
-    return brick_count(*rb);
+    return brick_flags_bytes(*rb);
 }
 
 int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
@@ -338,9 +338,9 @@ int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, floa
     return st;
 }
 
-int tde_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t, const tde_matrix3f *R,
-                float trunc, const tde_intrinsics *intr, const tde_round_buffer *rb, const tde_point3f *cell,
-                void *stream) {
+int tde_raycast_ex(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t,
+                   const tde_matrix3f *R, float trunc, const tde_intrinsics *intr, const tde_round_buffer *rb,
+                   const tde_point3f *cell, const uint8_t *brick_flags, void *stream) {
     TDE_REQUIRE(volume && vmap && nmap, "raycast: null buffer");
     TDE_REQUIRE(valid_format(format), "raycast: bad format %d", format);
     TDE_REQUIRE(t && R && cell, "raycast: null pose/cell");
@@ -348,7 +348,14 @@ int tde_raycast(const void *volume, int format, float *vmap, float *nmap, const 
     TDE_REQUIRE(valid_round_buffer(rb), "raycast: bad round_buffer");
     TDE_REQUIRE(trunc > 0.f && std::isfinite(trunc), "raycast: bad truncation distance");
     TDE_REQUIRE(cell->x > 0.f && cell->y > 0.f && cell->z > 0.f, "raycast: bad cell size");
-    return launch_raycast(volume, format, vmap, nmap, *t, *R, trunc, *intr, *rb, *cell, nullptr, as_stream(stream));
+    return launch_raycast(volume, format, vmap, nmap, *t, *R, trunc, *intr, *rb, *cell, nullptr, brick_flags,
+                          as_stream(stream));
+}
+
+int tde_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t, const tde_matrix3f *R,
+                float trunc, const tde_intrinsics *intr, const tde_round_buffer *rb, const tde_point3f *cell,
+                void *stream) {
+    return tde_raycast_ex(volume, format, vmap, nmap, t, R, trunc, intr, rb, cell, nullptr, stream);
 }
 
 int tde_resize_vertex_map(const float *src, float *dst, int src_cols, int src_rows, void *stream) {

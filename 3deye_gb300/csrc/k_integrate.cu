@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
     __syncthreads();
     const tde_point3i &Nv = P.rb.voxels_size;
     const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick;
+    const size_t nbricks_all = (size_t)nbx * nby * ((Nv.z + kBrick - 1) / kBrick);
     typedef TsdfStore<FMT> S;
     const float ntrunc = -P.trunc;
     const int W = P.intr.cols, H = P.intr.rows;
@@ -225,7 +226,10 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
                         float fs;
                         int ws;
                         S::decode(rn, fs, ws);
-                        if (fs < 0.f) neg_flags[physical_brick(x, yy[k], zz[k], P.rb)] = 1;
+                        if (fs < 0.f) {
+                            neg_flags[physical_brick(x, yy[k], zz[k], P.rb)] = 1;
+                            neg_flags[nbricks_all + physical_superbrick(x, yy[k], zz[k], P.rb)] = 1;
+                        }
                     }
                 }
             }
@@ -283,6 +287,10 @@ int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cu
 size_t brick_count(const tde_round_buffer &rb) {
     return (size_t)((rb.voxels_size.x + kBrick - 1) / kBrick) * ((rb.voxels_size.y + kBrick - 1) / kBrick) *
            ((rb.voxels_size.z + kBrick - 1) / kBrick);
+}
+
+size_t superbrick_count(const tde_round_buffer &rb) {
+    return (size_t)((rb.voxels_size.x + 31) / 32) * ((rb.voxels_size.y + 31) / 32) * ((rb.voxels_size.z + 31) / 32);
 }
 
 size_t integrate_scratch_bytes(int W, int H, const tde_round_buffer &rb) {

@@ -7,6 +7,7 @@
 // reference bit for bit on the same volume.
 #include "tde_common.cuh"
 #include "tde_launch.cuh"
+#include "tde_integrate.cuh"
 
 namespace tde {
 namespace {
@@ -21,6 +22,10 @@ struct RayParams {
     tde_point3f cell;
     size_t n;               // voxel count (F32 plane offset)
     const CamPose *dpose;   // when set, t and R are read from here
+    const uint8_t *neg_flags;  // per physical 8^3 brick: 0 = holds no negative value
+    const uint8_t *super_flags;  // per physical 32^3 super-brick (null: no sample skipping)
+    float inv_cell[3];
+    float skip_margin;           // time margin kept from a super-brick's exit
 };
 
 struct f3 { float x, y, z; };
@@ -46,6 +51,16 @@ __device__ __forceinline__ f3 along(const tde_point3f &o, f3 d, float t) {
 }
 
 __device__ __forceinline__ int floor_sat(float v) { return __float2int_rd(v); }  // convert_int_sat_rtn
+
+// floor(v / c) with the IEEE quotient's result: v * (1/c) is within 2.5 ulp of
+// v / c, so away from integer boundaries (and for |q| < 2048, where an ulp is
+// below 2.5e-4) both floors agree; near a boundary the division is done.
+__device__ __forceinline__ int floor_div(float v, float c, float inv_c) {
+    const float q = v * inv_c;
+    const float fr = q - floorf(q);
+    if (fabsf(q) < 2048.f && fr > 2e-3f && fr < 1.f - 2e-3f) return __float2int_rd(q);
+    return floor_sat(v / c);
+}
 
 template <int FMT>
 __device__ __forceinline__ float read_tsdf(const void *vol, const RayParams &p, int x, int y, int z) {
@@ -121,7 +136,7 @@ __device__ __noinline__ void refine_surface(const void *vol, const RayParams &p,
 // loop would.
 constexpr int kBatch = 4;
 
-template <int FMT>
+template <int FMT, bool SKIP>
 __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
                                                      float *__restrict__ nmap, RayParams p) {
     // 16x16 pixels per block; each warp takes an 8x4 tile so its rays start
@@ -148,6 +163,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
     const tde_point3i N = p.rb.voxels_size;
     const tde_point3f V = p.rb.volume_size;
     const float step = p.time_step;
+    const int nbx = (N.x + 7) >> 3, nby = (N.y + 7) >> 3;
 
     f3 rnu{((float)x - p.intr.cx) / p.intr.fx, ((float)y - p.intr.cy) / p.intr.fy, 1.f};
     f3 rn2 = mat_vec(p.R, rnu);
@@ -175,13 +191,54 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
         gx = max(0, min(gx, N.x - 1));
         gy = max(0, min(gy, N.y - 1));
         gz = max(0, min(gz, N.z - 1));
+        // prev sample: its value when `known`, else only "non-negative"; its
+        // sample time lets the value be fetched when it is needed after all
         float tsdf = read_tsdf<FMT>(vol, p, gx, gy, gz);
+        bool known = true;
+        float prev_ct = time_curr;
+        const int nsx = (N.x + 31) >> 5, nsy = (N.y + 31) >> 5;
 
         bool done = false;
         while (!done && time_curr < p.max_time) {
-            // Issue up to kBatch sample loads of the next steps.
+            if (SKIP && p.super_flags && !(known && tsdf < 0.f)) {
+                // Inside a 32^3 super-brick with no negative value and after a
+                // non-negative sample, no test of the loop can fire: advance
+                // time_curr by the same additions without evaluating samples,
+                // stopping while the next sample is still clear of the exit.
+                for (;;) {
+                    if (!(time_curr < p.max_time)) break;
+                    const float ct = time_curr + step;
+                    const f3 q = along(p.t, dir, ct);
+                    const int sx = floor_div(q.x, p.cell.x, p.inv_cell[0]);
+                    const int sy = floor_div(q.y, p.cell.y, p.inv_cell[1]);
+                    const int sz = floor_div(q.z, p.cell.z, p.inv_cell[2]);
+                    if (!(sx >= 0 && sy >= 0 && sz >= 0 && sx < N.x && sy < N.y && sz < N.z)) break;
+                    const int px = wrap_mod(sx + p.rb.origin_GRID.x, N.x);
+                    const int py = wrap_mod(sy + p.rb.origin_GRID.y, N.y);
+                    const int pz = wrap_mod(sz + p.rb.origin_GRID.z, N.z);
+                    if (__ldg(p.super_flags + ((px >> 5) + nsx * ((py >> 5) + nsy * (pz >> 5))))) break;
+                    // logical voxel box of this super-brick, in metres
+                    const float lox = (float)(sx - (px & 31)) * p.cell.x, loy = (float)(sy - (py & 31)) * p.cell.y,
+                                loz = (float)(sz - (pz & 31)) * p.cell.z;
+                    const float hix = lox + 32.f * p.cell.x, hiy = loy + 32.f * p.cell.y, hiz = loz + 32.f * p.cell.z;
+                    const float ex = ((dir.x > 0.f ? hix : lox) - p.t.x) / dir.x;
+                    const float ey = ((dir.y > 0.f ? hiy : loy) - p.t.y) / dir.y;
+                    const float ez = ((dir.z > 0.f ? hiz : loz) - p.t.z) / dir.z;
+                    const float lim = fminf(fminf(ex, ey), ez) - p.skip_margin;
+                    float tn = time_curr;
+                    int m = 0;
+                    while (tn < p.max_time && tn + step < lim) { tn = tn + step; ++m; }
+                    if (m == 0) break;  // next sample near the exit: evaluate it normally
+                    time_curr = tn;
+                    known = false;
+                    prev_ct = tn;
+                }
+                if (!(time_curr < p.max_time)) break;
+            }
             float ts[kBatch];
             float vals[kBatch];
+            size_t addr[kBatch];
+            bool have[kBatch];
             int nvalid = 0;  // samples in range, in order; the first out-of-range one ends the ray
             {
                 float tc = time_curr;
@@ -189,6 +246,8 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                 for (int k = 0; k < kBatch; ++k) {
                     ts[k] = tc;
                     vals[k] = 0.f;
+                    have[k] = false;
+                    addr[k] = 0;
                     tc = tc + step;
                 }
             }
@@ -198,11 +257,23 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                 if (nvalid == k && !stop_after) {
                     if (!(ts[k] < p.max_time)) { stop_after = true; }
                     else {
-                        float ct = ts[k] + step;
-                        f3 q = along(p.t, dir, ct);
-                        int sx = floor_sat(q.x / p.cell.x), sy = floor_sat(q.y / p.cell.y), sz = floor_sat(q.z / p.cell.z);
+                        const float ct = ts[k] + step;
+                        const f3 q = along(p.t, dir, ct);
+                        const int sx = floor_div(q.x, p.cell.x, p.inv_cell[0]);
+                        const int sy = floor_div(q.y, p.cell.y, p.inv_cell[1]);
+                        const int sz = floor_div(q.z, p.cell.z, p.inv_cell[2]);
                         if (sx >= 0 && sy >= 0 && sz >= 0 && sx < N.x && sy < N.y && sz < N.z) {
-                            vals[k] = read_tsdf<FMT>(vol, p, sx, sy, sz);
+                            const int px = wrap_mod(sx + p.rb.origin_GRID.x, N.x);
+                            const int py = wrap_mod(sy + p.rb.origin_GRID.y, N.y);
+                            const int pz = wrap_mod(sz + p.rb.origin_GRID.z, N.z);
+                            addr[k] = (size_t)px + (size_t)N.x * ((size_t)py + (size_t)N.y * (size_t)pz);
+                            bool load = true;
+                            if (SKIP)
+                                load = __ldg(p.neg_flags + ((px >> 3) + nbx * ((py >> 3) + nby * (pz >> 3)))) != 0;
+                            if (load) {
+                                vals[k] = TsdfStore<FMT>::value(vol, addr[k], p.n);
+                                have[k] = true;
+                            }
                             nvalid = k + 1;
                         } else {
                             stop_after = true;
@@ -210,14 +281,39 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                     }
                 }
             }
-            // Consume the samples in order.
+            // Consume the samples in order (raycast.cl:254-404).
             #pragma unroll
             for (int k = 0; k < kBatch; ++k) {
                 if (done) break;
                 if (k >= nvalid) { done = true; break; }  // out of volume or out of time
                 time_curr = ts[k];
-                float tsdf_prev = tsdf;
-                tsdf = vals[k];
+                if (SKIP && !have[k]) {
+                    if (!(known && tsdf < 0.f)) {
+                        // a non-negative sample after a non-negative one: no test can fire
+                        known = false;
+                        prev_ct = ts[k] + step;
+                        continue;
+                    }
+                    vals[k] = TsdfStore<FMT>::value(vol, addr[k], p.n);  // leaving a negative run
+                }
+                const float cur = vals[k];
+                if (SKIP && !known) {
+                    if (!(cur < 0.f)) {  // prev >= 0 and cur >= 0
+                        tsdf = cur;
+                        known = true;
+                        prev_ct = ts[k] + step;
+                        continue;
+                    }
+                    // the previous sample's sign decides a crossing: fetch it
+                    const f3 q = along(p.t, dir, prev_ct);
+                    tsdf = read_tsdf<FMT>(vol, p, floor_div(q.x, p.cell.x, p.inv_cell[0]),
+                                          floor_div(q.y, p.cell.y, p.inv_cell[1]),
+                                          floor_div(q.z, p.cell.z, p.inv_cell[2]));
+                }
+                const float tsdf_prev = tsdf;
+                tsdf = cur;
+                known = true;
+                prev_ct = ts[k] + step;
                 if (tsdf_prev < 0.f && tsdf > 0.f) { done = true; break; }
                 if (tsdf_prev > 0.f && tsdf < 0.f) {
                     done = true;
@@ -294,17 +390,24 @@ __global__ void transform_maps_kernel(const float *__restrict__ vs, const float 
 
 int launch_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f &t,
                    const tde_matrix3f &R, float trunc, const tde_intrinsics &intr, const tde_round_buffer &rb,
-                   const tde_point3f &cell, const CamPose *dpose, cudaStream_t stream) {
+                   const tde_point3f &cell, const CamPose *dpose, const uint8_t *neg_flags, cudaStream_t stream) {
     RayParams p;
     p.dpose = dpose;
+    p.neg_flags = neg_flags;
     p.t = t; p.R = R;
     p.time_step = (float)((double)trunc * 0.8);
     p.max_time = 3.f * ((rb.volume_size.x + rb.volume_size.y) + rb.volume_size.z);
     p.intr = intr; p.rb = rb; p.cell = cell; p.n = voxel_count(rb);
+    p.inv_cell[0] = 1.f / cell.x; p.inv_cell[1] = 1.f / cell.y; p.inv_cell[2] = 1.f / cell.z;
+    // super-brick sample skipping needs whole 32^3 super-bricks on every axis
+    const bool whole = rb.voxels_size.x % 32 == 0 && rb.voxels_size.y % 32 == 0 && rb.voxels_size.z % 32 == 0;
+    p.super_flags = (neg_flags && whole) ? neg_flags + brick_count(rb) : nullptr;
+    p.skip_margin = 1e-2f * fminf(fminf(cell.x, cell.y), cell.z);
     dim3 block(256);
     dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, 16));
     return dispatch_format(format, [&](auto F) {
-        raycast_kernel<decltype(F)::value><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+        if (neg_flags) raycast_kernel<decltype(F)::value, true><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+        else raycast_kernel<decltype(F)::value, false><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
         return check_launch("raycast");
     });
 }

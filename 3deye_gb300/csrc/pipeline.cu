@@ -169,7 +169,7 @@ int record_segment(tde_pipeline *p, Segment seg) {
         tde_point3f t0{0, 0, 0};
         tde_matrix3f R0{};
         return launch_raycast(p->volume, c.tsdf_format, p->vmod[0], p->nmod[0], t0, R0, c.trunc, p->intr[0], p->rb,
-                              p->cell, p->cam, s);
+                              p->cell, p->cam, p->negflags, s);
     }
     case SEG_RESIZE:
         for (int l = 1; l < p->levels; ++l) {
@@ -305,9 +305,9 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
         (st = dalloc(&p->stats, 3, "stats")) ||
         (st = dalloc(reinterpret_cast<char **>(&p->iscratch), integrate_scratch_bytes(c.intr.cols, c.intr.rows, p->rb),
                      "integration scratch")) ||
-        (st = dalloc(&p->negflags, brick_count(p->rb), "brick flags")))
+        (st = dalloc(&p->negflags, brick_flags_bytes(p->rb), "brick flags")))
         return fail(st);
-    e = cudaMemsetAsync(p->negflags, 0, brick_count(p->rb), p->stream);
+    e = cudaMemsetAsync(p->negflags, 0, brick_flags_bytes(p->rb), p->stream);
     if (e != cudaSuccess) return fail(cuda_fail(e, "brick flags"));
     e = cudaMemsetAsync(p->stats, 0, 3 * sizeof(unsigned long long), p->stream);
     if (e != cudaSuccess) return fail(cuda_fail(e, "stats"));

@@ -41,8 +41,22 @@ __host__ __device__ __forceinline__ size_t physical_brick(int x, int y, int z, c
     return (size_t)(px >> 3) + nbx * ((size_t)(py >> 3) + nby * (size_t)(pz >> 3));
 }
 
+// 32^3-voxel super-bricks (flag set together with the brick flag), stored
+// after the brick flags; only used when every volume dimension is a multiple
+// of 32.
+__host__ __device__ __forceinline__ size_t physical_superbrick(int x, int y, int z, const tde_round_buffer &rb) {
+    const int px = wrap_mod(x + rb.origin_GRID.x, rb.voxels_size.x);
+    const int py = wrap_mod(y + rb.origin_GRID.y, rb.voxels_size.y);
+    const int pz = wrap_mod(z + rb.origin_GRID.z, rb.voxels_size.z);
+    const size_t nsx = (size_t)(rb.voxels_size.x + 31) / 32, nsy = (size_t)(rb.voxels_size.y + 31) / 32;
+    return (size_t)(px >> 5) + nsx * ((size_t)(py >> 5) + nsy * (size_t)(pz >> 5));
+}
+
 size_t depth_max_floats(int W, int H);
 size_t brick_count(const tde_round_buffer &rb);
+size_t superbrick_count(const tde_round_buffer &rb);
+// bytes of the flag buffer: brick flags, then super-brick flags
+inline size_t brick_flags_bytes(const tde_round_buffer &rb) { return brick_count(rb) + superbrick_count(rb); }
 int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cudaStream_t stream);
 // neg_flags (may be null): per physical brick, set to 1 when a write leaves a
 // negative value there; a 0 therefore guarantees the brick holds no negative

@@ -205,9 +205,11 @@ int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, floa
  * trunc behind the observed surface, and the list of surviving bricks;
  * tde_integrate_tsdf allocates it on the stream itself.
  * `brick_flags` (device, tde_brick_flags_bytes, zero-initialised with the
- * volume; may be NULL) gets a 1 for every physical brick that receives a
- * negative value -- a 0 proves the brick has none, which the pipeline's
- * raycast uses to skip loads.  Same results as tde_integrate_tsdf. */
+ * volume; may be NULL) gets a 1 for every physical 8^3 brick, and every
+ * physical 32^3 super-brick (stored after the brick flags), that receives a
+ * negative value -- a 0 proves the brick has none, which tde_raycast_ex uses
+ * to skip loads and, across whole super-bricks, samples.  Same results as
+ * tde_integrate_tsdf. */
 size_t tde_integrate_tsdf_scratch_bytes(int cols, int rows, const tde_round_buffer *rb);
 size_t tde_brick_flags_bytes(const tde_round_buffer *rb);
 int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, float trunc,
@@ -225,6 +227,15 @@ int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, f
 int tde_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t,
                 const tde_matrix3f *R, float trunc, const tde_intrinsics *intr,
                 const tde_round_buffer *rb, const tde_point3f *cell_size, void *stream);
+
+/* Raycast with the brick flags kept by tde_integrate_tsdf_ex: samples in a
+ * brick flagged 0 are known to be >= 0, and the march only needs such a
+ * value when the previous sample was negative or the next one is; otherwise
+ * their loads are skipped.  Same output as tde_raycast. */
+int tde_raycast_ex(const void *volume, int format, float *vmap, float *nmap, const tde_point3f *t,
+                   const tde_matrix3f *R, float trunc, const tde_intrinsics *intr,
+                   const tde_round_buffer *rb, const tde_point3f *cell_size, const uint8_t *brick_flags,
+                   void *stream);
 
 /* Resize_Vertex_Map / Resize_Normal_Map: opencl_wrappers.cpp:97-146 (kernels
  * absent).  `src_cols` x `src_rows` is the source level; dst is half size.

@@ -110,13 +110,17 @@ def test_integrate_and_raycast_match_oracle(tde, orc, cuda, small, fmt, origin):
     assert bits_equal(N(vm), vmo) and bits_equal(N(nm), nmo)
 
 
-@pytest.mark.parametrize("fmt", [0, 1, 2])
-def test_integrate_ex_brick_flags_are_sound(tde, orc, cuda, small, fmt):
-    """tde_integrate_tsdf_ex with caller scratch gives the same volume, and a
-    zero brick flag proves the physical brick holds no negative value."""
+@pytest.mark.parametrize("fmt,voxels", [(0, 64), (1, 64), (2, 64), (1, 128)])
+def test_integrate_ex_brick_flags_are_sound(tde, orc, cuda, small, fmt, voxels):
+    """tde_integrate_tsdf_ex with caller scratch gives the same volume, a zero
+    brick / super-brick flag proves the physical (super-)brick holds no
+    negative value, and the raycast that skips on those flags is identical
+    to the full march."""
     import ctypes as C
+    import dataclasses
     import torch
     cfg, scene, traj, intr, depths = small
+    cfg = dataclasses.replace(cfg, voxels=voxels)
     origin = (5, 17, 60)
     vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt, origin, nframes=4)
     rb = trb(tde, rb_o)
@@ -153,11 +157,32 @@ def test_integrate_ex_brick_flags_are_sound(tde, orc, cuda, small, fmt):
     else:
         vals = vol_o[: 4 * n].view(np.float32)
     phys = vals.reshape(Nv, Nv, Nv)  # storage order: z, y, x
-    nb = Nv // 8
+    nb, ns = Nv // 8, Nv // 32
     neg = (phys < 0).reshape(nb, 8, nb, 8, nb, 8).any(axis=(1, 3, 5))  # [bz, by, bx]
-    f = N(flags).reshape(nb, nb, nb).astype(bool)
+    fl = N(flags)
+    assert fl.size == nb ** 3 + ns ** 3
+    f = fl[: nb ** 3].reshape(nb, nb, nb).astype(bool)
     assert neg.any()
     assert not (neg & ~f).any(), "a brick with a negative value has flag 0"
+    sneg = (phys < 0).reshape(ns, 32, ns, 32, ns, 32).any(axis=(1, 3, 5))
+    sf = fl[nb ** 3:].reshape(ns, ns, ns).astype(bool)
+    assert not (sneg & ~sf).any(), "a super-brick with a negative value has flag 0"
+    assert (~f).sum() > 0.5 * f.size  # most bricks are provably non-negative
+    # raycast skipping loads in flag-0 bricks: identical to the full march
+    L.tde_raycast_ex.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(tde.Point3f),
+                                 C.POINTER(tde.Matrix3f), C.c_float, C.POINTER(tde.Intrinsics),
+                                 C.POINTER(tde.RoundBuffer), C.POINTER(tde.Point3f), C.c_void_p, C.c_void_p]
+    for fi in (4, 5):
+        R, t = pose_parts(traj[fi])
+        vm = torch.empty((intr.rows, intr.cols, 3), dtype=torch.float32, device=cuda)
+        nm = torch.empty_like(vm)
+        Rm, tt, cs = tde.mat3(R), tde.vec3(t), tde.vec3(cell)
+        tde.check(L.tde_raycast_ex(vol.data_ptr(), fmt, vm.data_ptr(), nm.data_ptr(), C.byref(tt), C.byref(Rm),
+                                   cfg.trunc_m, C.byref(ti), C.byref(rb), C.byref(cs), flags.data_ptr(),
+                                   tde.stream_ptr()))
+        vmo, nmo = orc.raycast(vol_o, fmt, rb_o, intr, R, t, cfg.trunc_m, cell)
+        assert np.isfinite(vmo[..., 0]).sum() > 1000
+        assert bits_equal(N(vm), vmo) and bits_equal(N(nm), nmo), f"flagged raycast differs (frame {fi})"
 
 
 # ---------------------------------------------------------------------------
