@@ -25,7 +25,6 @@ struct RayParams {
     const uint8_t *neg_flags;  // per physical 8^3 brick: 0 = holds no negative value
     const uint8_t *super_flags;  // per physical 32^3 super-brick (null: no sample skipping)
     float inv_cell[3];
-    float skip_margin;           // time margin kept from a super-brick's exit
 };
 
 struct f3 { float x, y, z; };
@@ -52,26 +51,17 @@ __device__ __forceinline__ f3 along(const tde_point3f &o, f3 d, float t) {
 
 __device__ __forceinline__ int floor_sat(float v) { return __float2int_rd(v); }  // convert_int_sat_rtn
 
-// floor(v / c) with the IEEE quotient's result: v * (1/c) is within 2.5 ulp of
-// v / c, so away from integer boundaries (and for |q| < 2048, where an ulp is
-// below 2.5e-4) both floors agree; near a boundary the division is done.
-__device__ __forceinline__ int floor_div(float v, float c, float inv_c) {
-    const float q = v * inv_c;
-    const float fr = q - floorf(q);
-    if (fabsf(q) < 2048.f && fr > 2e-3f && fr < 1.f - 2e-3f) return __float2int_rd(q);
-    return floor_sat(v / c);
-}
-
 template <int FMT>
 __device__ __forceinline__ float read_tsdf(const void *vol, const RayParams &p, int x, int y, int z) {
     return TsdfStore<FMT>::value(vol, voxel_address(x, y, z, p.rb), p.n);
 }
 
-// interpolateTrilineary: raycast.cl:95-145.
+// interpolateTrilineary: raycast.cl:95-145, taking the quotients
+// point / Cell_Size (the reference computes each twice; the value is the same).
 template <int FMT>
-__device__ __noinline__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
+__device__ __noinline__ float trilinear_q(const void *vol, const RayParams &p, f3 pt, float qx, float qy, float qz) {
     const tde_point3i &N = p.rb.voxels_size;
-    int gx = floor_sat(pt.x / p.cell.x), gy = floor_sat(pt.y / p.cell.y), gz = floor_sat(pt.z / p.cell.z);
+    int gx = floor_sat(qx), gy = floor_sat(qy), gz = floor_sat(qz);
     if (gx <= 0 || gx >= N.x - 1) return __int_as_float(0x7fffffff);
     if (gy <= 0 || gy >= N.y - 1) return __int_as_float(0x7fffffff);
     if (gz <= 0 || gz >= N.z - 1) return __int_as_float(0x7fffffff);
@@ -81,17 +71,30 @@ __device__ __noinline__ float trilinear(const void *vol, const RayParams &p, f3 
     gx = (pt.x < vx) ? gx - 1 : gx;
     gy = (pt.y < vy) ? gy - 1 : gy;
     gz = (pt.z < vz) ? gz - 1 : gz;
-    float a = pt.x / p.cell.x - ((float)gx + 0.5f); if (a < 0) { gx--; a += 1.0f; }
-    float b = pt.y / p.cell.y - ((float)gy + 0.5f); if (b < 0) { gy--; b += 1.0f; }
-    float c = pt.z / p.cell.z - ((float)gz + 0.5f); if (c < 0) { gz--; c += 1.0f; }
-    float r000 = read_tsdf<FMT>(vol, p, gx, gy, gz), r001 = read_tsdf<FMT>(vol, p, gx, gy, gz + 1);
-    float r010 = read_tsdf<FMT>(vol, p, gx, gy + 1, gz), r011 = read_tsdf<FMT>(vol, p, gx, gy + 1, gz + 1);
-    float r100 = read_tsdf<FMT>(vol, p, gx + 1, gy, gz), r101 = read_tsdf<FMT>(vol, p, gx + 1, gy, gz + 1);
-    float r110 = read_tsdf<FMT>(vol, p, gx + 1, gy + 1, gz), r111 = read_tsdf<FMT>(vol, p, gx + 1, gy + 1, gz + 1);
+    float a = qx - ((float)gx + 0.5f); if (a < 0) { gx--; a += 1.0f; }
+    float b = qy - ((float)gy + 0.5f); if (b < 0) { gy--; b += 1.0f; }
+    float c = qz - ((float)gz + 0.5f); if (c < 0) { gz--; c += 1.0f; }
+    // the eight corners: gx..gx+1 etc. are inside [0, N) here
+    const int x0 = wrap_mod(gx + p.rb.origin_GRID.x, N.x), x1 = wrap_mod(gx + 1 + p.rb.origin_GRID.x, N.x);
+    const int y0 = wrap_mod(gy + p.rb.origin_GRID.y, N.y), y1 = wrap_mod(gy + 1 + p.rb.origin_GRID.y, N.y);
+    const int z0 = wrap_mod(gz + p.rb.origin_GRID.z, N.z), z1 = wrap_mod(gz + 1 + p.rb.origin_GRID.z, N.z);
+    const size_t sy = (size_t)N.x, sz = (size_t)N.x * (size_t)N.y;
+    const size_t r00 = (size_t)y0 * sy + (size_t)z0 * sz, r01 = (size_t)y0 * sy + (size_t)z1 * sz;
+    const size_t r10 = (size_t)y1 * sy + (size_t)z0 * sz, r11 = (size_t)y1 * sy + (size_t)z1 * sz;
+    typedef TsdfStore<FMT> S;
+    float v000 = S::value(vol, x0 + r00, p.n), v001 = S::value(vol, x0 + r01, p.n);
+    float v010 = S::value(vol, x0 + r10, p.n), v011 = S::value(vol, x0 + r11, p.n);
+    float v100 = S::value(vol, x1 + r00, p.n), v101 = S::value(vol, x1 + r01, p.n);
+    float v110 = S::value(vol, x1 + r10, p.n), v111 = S::value(vol, x1 + r11, p.n);
     float one_a = 1.f - a, one_b = 1.f - b, one_c = 1.f - c;
-    float x0 = one_b * (r000 * one_c + r001 * c) + b * (r010 * one_c + r011 * c);
-    float x1 = one_b * (r100 * one_c + r101 * c) + b * (r110 * one_c + r111 * c);
-    return one_a * x0 + a * x1;
+    float xa = one_b * (v000 * one_c + v001 * c) + b * (v010 * one_c + v011 * c);
+    float xb = one_b * (v100 * one_c + v101 * c) + b * (v110 * one_c + v111 * c);
+    return one_a * xa + a * xb;
+}
+
+template <int FMT>
+__device__ __forceinline__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
+    return trilinear_q<FMT>(vol, p, pt, pt.x / p.cell.x, pt.y / p.cell.y, pt.z / p.cell.z);
 }
 
 // Zero crossing between time_curr and time_curr + step: secant refinement of
@@ -115,26 +118,48 @@ __device__ __noinline__ void refine_surface(const void *vol, const RayParams &p,
     f3 p3 = along(p.t, dir, time_curr);
     int hx = floor_sat(p3.x / p.cell.x), hy = floor_sat(p3.y / p.cell.y), hz = floor_sat(p3.z / p.cell.z);
     if (hx > 1 && hy > 1 && hz > 1 && hx < N.x - 2 && hy < N.y - 2 && hz < N.z - 2) {
-        float F[6];
-        #pragma unroll 1
-        for (int k = 0; k < 6; ++k) {
-            f3 tt = vf;
-            const int axis = k >> 1;
-            const float d = axis == 0 ? p.cell.x : axis == 1 ? p.cell.y : p.cell.z;
-            float &c = axis == 0 ? tt.x : axis == 1 ? tt.y : tt.z;
-            c = (k & 1) ? c - d : c + d;
-            F[k] = trilinear<FMT>(vol, p, tt);
-        }
-        f3 n = normalized(f3{F[0] - F[1], F[2] - F[3], F[4] - F[5]});
+        // vf +- cell on one axis: the other two quotients are vf's
+        const float qx = vf.x / p.cell.x, qy = vf.y / p.cell.y, qz = vf.z / p.cell.z;
+        f3 t1 = vf, t2 = vf;
+        t1.x = t1.x + p.cell.x; t2.x = t2.x - p.cell.x;
+        const float Fx1 = trilinear_q<FMT>(vol, p, t1, t1.x / p.cell.x, qy, qz);
+        const float Fx2 = trilinear_q<FMT>(vol, p, t2, t2.x / p.cell.x, qy, qz);
+        t1 = vf; t2 = vf;
+        t1.y = t1.y + p.cell.y; t2.y = t2.y - p.cell.y;
+        const float Fy1 = trilinear_q<FMT>(vol, p, t1, qx, t1.y / p.cell.y, qz);
+        const float Fy2 = trilinear_q<FMT>(vol, p, t2, qx, t2.y / p.cell.y, qz);
+        t1 = vf; t2 = vf;
+        t1.z = t1.z + p.cell.z; t2.z = t2.z - p.cell.z;
+        const float Fz1 = trilinear_q<FMT>(vol, p, t1, qx, qy, t1.z / p.cell.z);
+        const float Fz2 = trilinear_q<FMT>(vol, p, t2, qx, qy, t2.z / p.cell.z);
+        f3 n = normalized(f3{Fx1 - Fx2, Fy1 - Fy2, Fz1 - Fz2});
         nx_out = n.x; ny_out = n.y; nz_out = n.z;
     }
 }
 
-// Number of march samples whose addresses are issued together.  The samples
-// are independent of each other's values, so their loads overlap; the
-// zero-crossing logic then consumes them in order exactly as a one-sample
-// loop would.
-constexpr int kBatch = 4;
+// Voxel of the sample at time ct: floor(pos / cell) with pos = t + dir * ct
+// evaluated exactly as the reference does whenever it matters.  The fast
+// estimate o/c + (d/c) ct is within ~4e-4 voxel of the exact quotient, so a
+// fractional part clear of 4e-3 from an integer settles the floor; otherwise
+// the position and the IEEE quotient are computed.
+constexpr float kSkipMargin = 1e-2f;  // voxels
+
+struct RayFast {
+    float o[3], d[3];  // t / cell, dir / cell
+};
+
+__device__ __forceinline__ int axis_floor(float q, float o, float d, float cell, float ct) {
+    const float fr = q - floorf(q);
+    if (fabsf(q) < 2048.f && fr > 4e-3f && fr < 1.f - 4e-3f) return __float2int_rd(q);
+    return floor_sat((o + d * ct) / cell);
+}
+
+__device__ __forceinline__ void sample_voxel(const RayParams &p, const f3 &dir, const RayFast &rf, float ct, int &sx,
+                                             int &sy, int &sz) {
+    sx = axis_floor(fmaf(rf.d[0], ct, rf.o[0]), p.t.x, dir.x, p.cell.x, ct);
+    sy = axis_floor(fmaf(rf.d[1], ct, rf.o[1]), p.t.y, dir.y, p.cell.y, ct);
+    sz = axis_floor(fmaf(rf.d[2], ct, rf.o[2]), p.t.z, dir.z, p.cell.z, ct);
+}
 
 template <int FMT, bool SKIP>
 __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
@@ -163,7 +188,6 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
     const tde_point3i N = p.rb.voxels_size;
     const tde_point3f V = p.rb.volume_size;
     const float step = p.time_step;
-    const int nbx = (N.x + 7) >> 3, nby = (N.y + 7) >> 3;
 
     f3 rnu{((float)x - p.intr.cx) / p.intr.fx, ((float)y - p.intr.cy) / p.intr.fy, 1.f};
     f3 rn2 = mat_vec(p.R, rnu);
@@ -191,140 +215,95 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
         gx = max(0, min(gx, N.x - 1));
         gy = max(0, min(gy, N.y - 1));
         gz = max(0, min(gz, N.z - 1));
-        // prev sample: its value when `known`, else only "non-negative"; its
-        // sample time lets the value be fetched when it is needed after all
+        RayFast rf;
+        rf.o[0] = p.t.x * p.inv_cell[0]; rf.o[1] = p.t.y * p.inv_cell[1]; rf.o[2] = p.t.z * p.inv_cell[2];
+        rf.d[0] = dir.x * p.inv_cell[0]; rf.d[1] = dir.y * p.inv_cell[1]; rf.d[2] = dir.z * p.inv_cell[2];
+        // previous sample: its value when `known`, else only "non-negative";
+        // its time lets the value be fetched when it turns out to matter
         float tsdf = read_tsdf<FMT>(vol, p, gx, gy, gz);
         bool known = true;
         float prev_ct = time_curr;
+        const int nbx = (N.x + 7) >> 3, nby = (N.y + 7) >> 3;
         const int nsx = (N.x + 31) >> 5, nsy = (N.y + 31) >> 5;
+        int last_super = -1;
 
-        bool done = false;
-        while (!done && time_curr < p.max_time) {
-            if (SKIP && p.super_flags && !(known && tsdf < 0.f)) {
-                // Inside a 32^3 super-brick with no negative value and after a
-                // non-negative sample, no test of the loop can fire: advance
-                // time_curr by the same additions without evaluating samples,
-                // stopping while the next sample is still clear of the exit.
-                for (;;) {
-                    if (!(time_curr < p.max_time)) break;
-                    const float ct = time_curr + step;
-                    const f3 q = along(p.t, dir, ct);
-                    const int sx = floor_div(q.x, p.cell.x, p.inv_cell[0]);
-                    const int sy = floor_div(q.y, p.cell.y, p.inv_cell[1]);
-                    const int sz = floor_div(q.z, p.cell.z, p.inv_cell[2]);
-                    if (!(sx >= 0 && sy >= 0 && sz >= 0 && sx < N.x && sy < N.y && sz < N.z)) break;
-                    const int px = wrap_mod(sx + p.rb.origin_GRID.x, N.x);
-                    const int py = wrap_mod(sy + p.rb.origin_GRID.y, N.y);
-                    const int pz = wrap_mod(sz + p.rb.origin_GRID.z, N.z);
-                    if (__ldg(p.super_flags + ((px >> 5) + nsx * ((py >> 5) + nsy * (pz >> 5))))) break;
-                    // logical voxel box of this super-brick, in metres
-                    const float lox = (float)(sx - (px & 31)) * p.cell.x, loy = (float)(sy - (py & 31)) * p.cell.y,
-                                loz = (float)(sz - (pz & 31)) * p.cell.z;
-                    const float hix = lox + 32.f * p.cell.x, hiy = loy + 32.f * p.cell.y, hiz = loz + 32.f * p.cell.z;
-                    const float ex = ((dir.x > 0.f ? hix : lox) - p.t.x) / dir.x;
-                    const float ey = ((dir.y > 0.f ? hiy : loy) - p.t.y) / dir.y;
-                    const float ez = ((dir.z > 0.f ? hiz : loz) - p.t.z) / dir.z;
-                    const float lim = fminf(fminf(ex, ey), ez) - p.skip_margin;
-                    float tn = time_curr;
-                    int m = 0;
-                    while (tn < p.max_time && tn + step < lim) { tn = tn + step; ++m; }
-                    if (m == 0) break;  // next sample near the exit: evaluate it normally
-                    time_curr = tn;
-                    known = false;
-                    prev_ct = tn;
-                }
-                if (!(time_curr < p.max_time)) break;
-            }
-            float ts[kBatch];
-            float vals[kBatch];
-            size_t addr[kBatch];
-            bool have[kBatch];
-            int nvalid = 0;  // samples in range, in order; the first out-of-range one ends the ray
-            {
-                float tc = time_curr;
-                #pragma unroll
-                for (int k = 0; k < kBatch; ++k) {
-                    ts[k] = tc;
-                    vals[k] = 0.f;
-                    have[k] = false;
-                    addr[k] = 0;
-                    tc = tc + step;
-                }
-            }
-            bool stop_after = false;
-            #pragma unroll
-            for (int k = 0; k < kBatch; ++k) {
-                if (nvalid == k && !stop_after) {
-                    if (!(ts[k] < p.max_time)) { stop_after = true; }
-                    else {
-                        const float ct = ts[k] + step;
-                        const f3 q = along(p.t, dir, ct);
-                        const int sx = floor_div(q.x, p.cell.x, p.inv_cell[0]);
-                        const int sy = floor_div(q.y, p.cell.y, p.inv_cell[1]);
-                        const int sz = floor_div(q.z, p.cell.z, p.inv_cell[2]);
-                        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < N.x && sy < N.y && sz < N.z) {
-                            const int px = wrap_mod(sx + p.rb.origin_GRID.x, N.x);
-                            const int py = wrap_mod(sy + p.rb.origin_GRID.y, N.y);
-                            const int pz = wrap_mod(sz + p.rb.origin_GRID.z, N.z);
-                            addr[k] = (size_t)px + (size_t)N.x * ((size_t)py + (size_t)N.y * (size_t)pz);
-                            bool load = true;
-                            if (SKIP)
-                                load = __ldg(p.neg_flags + ((px >> 3) + nbx * ((py >> 3) + nby * (pz >> 3)))) != 0;
-                            if (load) {
-                                vals[k] = TsdfStore<FMT>::value(vol, addr[k], p.n);
-                                have[k] = true;
+        // raycast.cl:254-404, one sample per iteration
+        while (time_curr < p.max_time) {
+            const float ct = time_curr + step;
+            int sx, sy, sz;
+            sample_voxel(p, dir, rf, ct, sx, sy, sz);
+            if (!((unsigned)sx < (unsigned)N.x && (unsigned)sy < (unsigned)N.y && (unsigned)sz < (unsigned)N.z)) break;
+            int px = sx + p.rb.origin_GRID.x; px -= px >= N.x ? N.x : 0;
+            int py = sy + p.rb.origin_GRID.y; py -= py >= N.y ? N.y : 0;
+            int pz = sz + p.rb.origin_GRID.z; pz -= pz >= N.z ? N.z : 0;
+            bool have = true;
+            if (SKIP) {
+                if (p.super_flags && !(known && tsdf < 0.f)) {
+                    const int sid = (px >> 5) + nsx * ((py >> 5) + nsy * (pz >> 5));
+                    if (sid != last_super) {
+                        last_super = sid;
+                        if (!__ldg(p.super_flags + sid)) {
+                            // A 32^3 super-brick with no negative value entered after a
+                            // non-negative sample: no test can fire inside it, so time
+                            // advances by the same additions without evaluating samples
+                            // until the next one nears the exit.
+                            // exit of the box shrunk by kSkipMargin voxels, in the fast
+                            // coordinates (their error is far below the margin)
+                            const float lox = (float)(sx - (px & 31)), loy = (float)(sy - (py & 31)),
+                                        loz = (float)(sz - (pz & 31));
+                            const float ex = ((rf.d[0] > 0.f ? lox + (32.f - kSkipMargin) : lox + kSkipMargin) - rf.o[0]) / rf.d[0];
+                            const float ey = ((rf.d[1] > 0.f ? loy + (32.f - kSkipMargin) : loy + kSkipMargin) - rf.o[1]) / rf.d[1];
+                            const float ez = ((rf.d[2] > 0.f ? loz + (32.f - kSkipMargin) : loz + kSkipMargin) - rf.o[2]) / rf.d[2];
+                            const float lim = fminf(fminf(ex, ey), ez);
+                            float tn = time_curr;
+                            int m = 0;
+                            while (tn < p.max_time && tn + step < lim) { tn = tn + step; ++m; }
+                            if (m > 0) {
+                                time_curr = tn;
+                                known = false;
+                                prev_ct = tn;
+                                continue;
                             }
-                            nvalid = k + 1;
-                        } else {
-                            stop_after = true;
                         }
                     }
                 }
+                have = __ldg(p.neg_flags + ((px >> 3) + nbx * ((py >> 3) + nby * (pz >> 3)))) != 0;
             }
-            // Consume the samples in order (raycast.cl:254-404).
-            #pragma unroll
-            for (int k = 0; k < kBatch; ++k) {
-                if (done) break;
-                if (k >= nvalid) { done = true; break; }  // out of volume or out of time
-                time_curr = ts[k];
-                if (SKIP && !have[k]) {
-                    if (!(known && tsdf < 0.f)) {
-                        // a non-negative sample after a non-negative one: no test can fire
-                        known = false;
-                        prev_ct = ts[k] + step;
-                        continue;
-                    }
-                    vals[k] = TsdfStore<FMT>::value(vol, addr[k], p.n);  // leaving a negative run
-                }
-                const float cur = vals[k];
-                if (SKIP && !known) {
-                    if (!(cur < 0.f)) {  // prev >= 0 and cur >= 0
-                        tsdf = cur;
-                        known = true;
-                        prev_ct = ts[k] + step;
-                        continue;
-                    }
-                    // the previous sample's sign decides a crossing: fetch it
-                    const f3 q = along(p.t, dir, prev_ct);
-                    tsdf = read_tsdf<FMT>(vol, p, floor_div(q.x, p.cell.x, p.inv_cell[0]),
-                                          floor_div(q.y, p.cell.y, p.inv_cell[1]),
-                                          floor_div(q.z, p.cell.z, p.inv_cell[2]));
-                }
-                const float tsdf_prev = tsdf;
-                tsdf = cur;
-                known = true;
-                prev_ct = ts[k] + step;
-                if (tsdf_prev < 0.f && tsdf > 0.f) { done = true; break; }
-                if (tsdf_prev > 0.f && tsdf < 0.f) {
-                    done = true;
-                    refine_surface<FMT>(vol, p, dir, time_curr, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
-                    break;
+            const size_t addr = (size_t)px + (size_t)N.x * ((size_t)py + (size_t)N.y * (size_t)pz);
+            float cur = 0.f;
+            if (SKIP && !have) {
+                if (!(known && tsdf < 0.f)) {
+                    // a non-negative sample after a non-negative one: no test can fire
+                    known = false;
+                    prev_ct = ct;
+                    time_curr = ct;
+                    continue;
                 }
             }
-            if (!done) {
-                // every sample of the batch was consumed without a decision
-                time_curr = ts[kBatch - 1] + step;
+            cur = TsdfStore<FMT>::value(vol, addr, p.n);
+            if (SKIP && !known) {
+                if (!(cur < 0.f)) {  // prev >= 0 and cur >= 0
+                    tsdf = cur;
+                    known = true;
+                    prev_ct = ct;
+                    time_curr = ct;
+                    continue;
+                }
+                // the previous sample's sign decides a crossing: fetch it
+                int qx, qy, qz;
+                sample_voxel(p, dir, rf, prev_ct, qx, qy, qz);
+                tsdf = read_tsdf<FMT>(vol, p, qx, qy, qz);
             }
+            const float tsdf_prev = tsdf;
+            tsdf = cur;
+            known = true;
+            prev_ct = ct;
+            if (tsdf_prev < 0.f && tsdf > 0.f) break;
+            if (tsdf_prev > 0.f && tsdf < 0.f) {
+                refine_surface<FMT>(vol, p, dir, time_curr, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
+                break;
+            }
+            time_curr = ct;
         }
     }
     vmap[3 * pix + 0] = vx_out; vmap[3 * pix + 1] = vy_out; vmap[3 * pix + 2] = vz_out;
@@ -402,7 +381,6 @@ int launch_raycast(const void *volume, int format, float *vmap, float *nmap, con
     // super-brick sample skipping needs whole 32^3 super-bricks on every axis
     const bool whole = rb.voxels_size.x % 32 == 0 && rb.voxels_size.y % 32 == 0 && rb.voxels_size.z % 32 == 0;
     p.super_flags = (neg_flags && whole) ? neg_flags + brick_count(rb) : nullptr;
-    p.skip_margin = 1e-2f * fminf(fminf(cell.x, cell.y), cell.z);
     dim3 block(256);
     dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, 16));
     return dispatch_format(format, [&](auto F) {
