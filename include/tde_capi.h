@@ -217,6 +217,25 @@ int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, f
                           const tde_point3f *cell_size, const tde_round_buffer *rb, int max_weight,
                           void *scratch, size_t scratch_bytes, uint8_t *brick_flags, void *stream);
 
+/* Integration that allocates nothing (no counterpart in the reference, whose
+ * host code allocates per call).  For callers that cannot call cudaMalloc --
+ * real-time loops with a memory footprint fixed at start-up, plug-in hosts
+ * whose allocator owns the device, interfaces with no way to pass a scratch
+ * buffer -- this takes its scratch from a fixed array in the library's static
+ * device memory (tde_integrate_tsdf_noalloc_max_scratch_bytes(): 1.5 MiB,
+ * enough for a 512^3 volume with a 640x480 frame; every GPU that loads the
+ * library holds it until exit).  Same results as tde_integrate_tsdf; a
+ * configuration needing more scratch is rejected with TDE_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address there
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls whose GPU work overlaps (other
+ * streams, other threads) race on it and must be serialised by the caller. */
+size_t tde_integrate_tsdf_noalloc_max_scratch_bytes(void);
+int tde_integrate_tsdf_noalloc(const float *depth_scaled, void *volume, int format, float trunc,
+                               const tde_matrix3f *R_inv, const tde_point3f *t, const tde_intrinsics *intr,
+                               const tde_point3f *cell_size, const tde_round_buffer *rb, int max_weight,
+                               void *stream);
+
 /* ======================================================================== */
 /* a8/a9: raycast and model maps                                             */
 /* ======================================================================== */
