@@ -62,10 +62,20 @@ __global__ void finalize_kernel(IcpState *st, const PrevPose *prev, CamPose *cam
     out->inliers = st->inliers;
 }
 
-enum Segment { SEG_TRACK_FIRST, SEG_TRACK, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE, SEG_COUNT };
-// Events per timed frame: before tracking, after tracking, after integration,
-// after raycast, after the model pyramid.
-constexpr int kEvents = 5;
+enum Segment {
+    SEG_PRE,         // bilateral filter, pyramid, vertex and normal maps, ICP setup
+    SEG_ICP,         // the ICP iterations
+    SEG_POST_FIRST,  // pose publication without tracking (first frame), scaled depth, depth tiles
+    SEG_POST,        // pose acceptance, scaled depth, depth tiles
+    SEG_INTEGRATE,
+    SEG_RAYCAST,
+    SEG_RESIZE,
+    SEG_COUNT
+};
+// Stages timed per frame, in order: SEG_PRE, SEG_ICP, SEG_POST(_FIRST),
+// SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE.
+constexpr int kStages = 6;
+constexpr int kEvents = kStages + 1;
 
 }  // namespace
 }  // namespace tde
@@ -131,8 +141,7 @@ int record_segment(tde_pipeline *p, Segment seg) {
     cudaStream_t s = p->stream;
     const int W = c.intr.cols, H = c.intr.rows;
     switch (seg) {
-    case SEG_TRACK_FIRST:
-    case SEG_TRACK: {
+    case SEG_PRE: {
         TDE_TRY(launch_bilateral(p->raw, p->depth[0], W, H, c.sigma_space, c.sigma_color, c.max_depth_mm, p->vcur[0],
                                  &p->intr[0], s));
         for (int l = 1; l < p->levels; ++l)
@@ -141,23 +150,25 @@ int record_segment(tde_pipeline *p, Segment seg) {
         for (int l = 0; l < p->levels; ++l)
             TDE_TRY(launch_normal_map(p->vcur[l], p->ncur[l], p->intr[l].cols, p->intr[l].rows, s));
         begin_frame_kernel<<<1, 1, 0, s>>>(p->st, p->prev);
-        TDE_TRY(check_launch("begin_frame"));
-        if (seg == SEG_TRACK) {
-            for (int l = p->levels - 1; l >= 0; --l) {
-                IcpArgs a;
-                a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
-                a.W = p->intr[l].cols; a.H = p->intr[l].rows;
-                a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
-                a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
-                for (int it = 0; it < c.icp_iters[l]; ++it)
-                    TDE_TRY(launch_icp(a, p->st, p->gbuf, nullptr, true, true, s));
-            }
+        return check_launch("begin_frame");
+    }
+    case SEG_ICP:
+        for (int l = p->levels - 1; l >= 0; --l) {
+            IcpArgs a;
+            a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
+            a.W = p->intr[l].cols; a.H = p->intr[l].rows;
+            a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
+            a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
+            for (int it = 0; it < c.icp_iters[l]; ++it)
+                TDE_TRY(launch_icp(a, p->st, p->gbuf, nullptr, true, true, s));
         }
-        finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_TRACK);
+        return TDE_OK;
+    case SEG_POST_FIRST:
+    case SEG_POST:
+        finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_POST);
         TDE_TRY(check_launch("finalize_pose"));
         TDE_TRY(launch_scale_depth(p->raw, p->scaled, p->intr[0], s));
         return launch_depth_max(p->scaled, W, H, static_cast<float *>(p->iscratch), s);
-    }
     case SEG_INTEGRATE: {
         IntegrateParams P;
         std::memset(&P, 0, sizeof(P));
@@ -213,17 +224,17 @@ int capture_all(tde_pipeline *p) {
         Segment sg = (Segment)sgi;
         TDE_TRY(capture(p, &sg, 1, &p->seg_exec[sgi]));
     }
-    const Segment first[] = {SEG_TRACK_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
-    const Segment track[] = {SEG_TRACK, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
-    TDE_TRY(capture(p, first, 4, &p->full_exec[0]));
-    TDE_TRY(capture(p, track, 4, &p->full_exec[1]));
+    const Segment first[] = {SEG_PRE, SEG_POST_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
+    const Segment track[] = {SEG_PRE, SEG_ICP, SEG_POST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
+    TDE_TRY(capture(p, first, 5, &p->full_exec[0]));
+    TDE_TRY(capture(p, track, 6, &p->full_exec[1]));
     p->captured = true;
     return TDE_OK;
 }
 
 int run_segment(tde_pipeline *p, Segment s) {
     if (p->cfg.use_graphs) {
-        TDE_CUDA(cudaGraphLaunch(p->seg_exec[s], p->stream), "graph launch");
+        if (p->seg_exec[s]) TDE_CUDA(cudaGraphLaunch(p->seg_exec[s], p->stream), "graph launch");
         return TDE_OK;
     }
     return record_segment(p, s);
@@ -343,15 +354,13 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
         TDE_CUDA(cudaGraphLaunch(p->full_exec[first ? 0 : 1], p->stream), "graph launch");
     } else {
         cudaEvent_t *ev = timed ? &p->ev[kEvents * p->timing_n] : nullptr;
+        const Segment order[kStages] = {SEG_PRE, SEG_ICP, first ? SEG_POST_FIRST : SEG_POST, SEG_INTEGRATE,
+                                        SEG_RAYCAST, SEG_RESIZE};
         if (ev) TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
-        TDE_TRY(run_segment(p, first ? SEG_TRACK_FIRST : SEG_TRACK));
-        if (ev) TDE_CUDA(cudaEventRecord(ev[1], p->stream), "event");
-        TDE_TRY(run_segment(p, SEG_INTEGRATE));
-        if (ev) TDE_CUDA(cudaEventRecord(ev[2], p->stream), "event");
-        TDE_TRY(run_segment(p, SEG_RAYCAST));
-        if (ev) TDE_CUDA(cudaEventRecord(ev[3], p->stream), "event");
-        TDE_TRY(run_segment(p, SEG_RESIZE));
-        if (ev) TDE_CUDA(cudaEventRecord(ev[4], p->stream), "event");
+        for (int k = 0; k < kStages; ++k) {
+            if (!(first && order[k] == SEG_ICP)) TDE_TRY(run_segment(p, order[k]));
+            if (ev) TDE_CUDA(cudaEventRecord(ev[k + 1], p->stream), "event");
+        }
         if (timed) p->timing_n++;
     }
     if (pose_out12)
@@ -427,20 +436,26 @@ int tde_pipeline_enable_timing(tde_pipeline *p, int capacity) {
 }
 
 int tde_pipeline_timings(tde_pipeline *p, float *integrate_ms, float *raycast_ms, int capacity) {
-    return tde_pipeline_stage_timings(p, nullptr, integrate_ms, raycast_ms, nullptr, capacity);
-}
-
-int tde_pipeline_stage_timings(tde_pipeline *p, float *track_ms, float *integrate_ms, float *raycast_ms,
-                               float *resize_ms, int capacity) {
-    if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_timings: null");
+    if (!p || capacity < 0) return set_error(TDE_ERR_INVALID_ARG, "pipeline_timings: bad argument");
     TDE_TRY(tde_pipeline_sync(p));
     int n = p->timing_n < capacity ? p->timing_n : capacity;
-    float *out[4] = {track_ms, integrate_ms, raycast_ms, resize_ms};
+    for (int i = 0; i < n; ++i) {
+        cudaEvent_t *ev = &p->ev[kEvents * i];
+        if (integrate_ms) TDE_CUDA(cudaEventElapsedTime(&integrate_ms[i], ev[3], ev[4]), "elapsed");
+        if (raycast_ms) TDE_CUDA(cudaEventElapsedTime(&raycast_ms[i], ev[4], ev[5]), "elapsed");
+    }
+    return n;
+}
+
+int tde_pipeline_stage_timings(tde_pipeline *p, float *ms, int capacity) {
+    if (!p || !ms || capacity < 0) return set_error(TDE_ERR_INVALID_ARG, "pipeline_stage_timings: bad argument");
+    TDE_TRY(tde_pipeline_sync(p));
+    int n = p->timing_n < capacity ? p->timing_n : capacity;
     for (int i = 0; i < n; ++i)
-        for (int k = 0; k < 4; ++k)
-            if (out[k])
-                TDE_CUDA(cudaEventElapsedTime(&out[k][i], p->ev[kEvents * i + k], p->ev[kEvents * i + k + 1]),
-                         "elapsed");
+        for (int k = 0; k < kStages; ++k)
+            TDE_CUDA(cudaEventElapsedTime(&ms[(size_t)i * kStages + k], p->ev[kEvents * i + k],
+                                          p->ev[kEvents * i + k + 1]),
+                     "elapsed");
     return n;
 }
 

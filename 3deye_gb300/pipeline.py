@@ -31,7 +31,7 @@ declare("tde_pipeline_frame_count", I, [P])
 declare("tde_pipeline_enable_timing", I, [P, I])
 declare("tde_pipeline_timings", I, [P, P, P, I])
 declare("tde_pipeline_integrate_stats", I, [P, P, I])
-declare("tde_pipeline_stage_timings", I, [P, P, P, P, P, I])
+declare("tde_pipeline_stage_timings", I, [P, P, I])
 declare("tde_pipeline_launches_per_frame", I, [P])
 declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
 declare("tde_pipeline_set_pose", I, [P, P])
@@ -131,13 +131,15 @@ class Pipeline:
             check(n)
         return a[:n], b[:n]
 
-    def stage_timings(self, capacity: int):
-        """(track, integrate, raycast, resize) milliseconds per timed frame."""
-        a = [np.zeros(capacity, np.float32) for _ in range(4)]
-        n = lib.tde_pipeline_stage_timings(self._h, *[x.ctypes.data_as(P) for x in a], capacity)
+    STAGES = ("preprocess", "icp", "pose_and_scaled_depth", "integrate", "raycast", "model_pyramid")
+
+    def stage_timings(self, capacity: int) -> dict:
+        """Milliseconds per timed frame of each stage (STAGES), as arrays."""
+        a = np.zeros((capacity, len(self.STAGES)), np.float32)
+        n = lib.tde_pipeline_stage_timings(self._h, a.ctypes.data_as(P), capacity)
         if n < 0:
             check(n)
-        return [x[:n] for x in a]
+        return {k: a[:n, i] for i, k in enumerate(self.STAGES)}
 
     def integrate_stats(self, reset=False, bricks=False):
         out = np.zeros(3, np.uint64)

@@ -84,10 +84,10 @@ int tde_pipeline_enable_timing(tde_pipeline *p, int capacity);
 /* Milliseconds of the integration and raycast launches of the timed frames
  * (synchronises); returns the number of frames written. */
 int tde_pipeline_timings(tde_pipeline *p, float *integrate_ms, float *raycast_ms, int capacity);
-/* Per-stage milliseconds of the timed frames: tracking (preprocessing + ICP
- * + pose), integration, raycast, model-map pyramid; any pointer may be NULL. */
-int tde_pipeline_stage_timings(tde_pipeline *p, float *track_ms, float *integrate_ms, float *raycast_ms,
-                               float *resize_ms, int capacity);
+/* Per-stage milliseconds of the timed frames, row-major [frame][6]: input
+ * preprocessing (bilateral, pyramid, vertex/normal maps), ICP iterations,
+ * pose publication + scaled depth, integration, raycast, model-map pyramid. */
+int tde_pipeline_stage_timings(tde_pipeline *p, float *ms, int capacity);
 /* Voxels read, voxels written and 8^3 bricks swept by integration since the
  * last reset, three counters (needs integrate_stats; synchronises). */
 int tde_pipeline_integrate_stats(tde_pipeline *p, uint64_t *read_written2, int reset);
