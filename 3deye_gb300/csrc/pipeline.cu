@@ -115,22 +115,6 @@ struct tde_pipeline {
 
 namespace {
 
-int cuda_fail(cudaError_t e, const char *what) {
-    return set_error(e == cudaErrorMemoryAllocation ? TDE_ERR_OOM : TDE_ERR_CUDA, "%s: %s", what,
-                     cudaGetErrorString(e));
-}
-
-#define TDE_CUDA(call, what)                           \
-    do {                                               \
-        cudaError_t e_ = (call);                       \
-        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-    } while (0)
-#define TDE_TRY(call)                                  \
-    do {                                               \
-        int s_ = (call);                               \
-        if (s_ != TDE_OK) return s_;                   \
-    } while (0)
-
 template <class T> int dalloc(T **p, size_t count, const char *what) {
     TDE_CUDA(cudaMalloc((void **)p, count * sizeof(T)), what);
     return TDE_OK;

@@ -35,6 +35,21 @@ int set_error(int code, const char *fmt, ...);
 // Maps the last CUDA launch error to a status code.
 int check_launch(const char *what);
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+inline int cuda_fail(cudaError_t e, const char *what) {
+    return set_error(e == cudaErrorMemoryAllocation ? TDE_ERR_OOM : TDE_ERR_CUDA, "%s: %s", what,
+                     cudaGetErrorString(e));
+}
+
+#define TDE_CUDA(call, what)                                    \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return ::tde::cuda_fail(e_, what); \
+    } while (0)
+#define TDE_TRY(call)                \
+    do {                             \
+        int s_ = (call);             \
+        if (s_ != TDE_OK) return s_; \
+    } while (0)
 
 // ---------------------------------------------------------------------------
 // OpenCL min/max for floats: max(x, y) = x < y ? y : x.
