@@ -15,12 +15,12 @@
 // copy.  The input gradient is the same kernel run on the output gradient
 // with the transposed, tap-flipped weights.
 //
-// Weight gradient (wgrad_tc_kernel): M = 128 rows of (tap, input channel),
-// N = output channels, K = pixels.  Both operands are transposed into
-// K-major core matrices in shared memory (K = 64 pixels per step); a row of
-// ones gives the bias gradient.  Each block accumulates its share of the
-// pixels for all row tiles in tensor memory and writes one partial; a
-// reduction kernel sums the partials in a fixed order (deterministic).
+// Weight gradient (wgrad_tc_kernel): M = 128 rows of (tap row, input
+// channel), N = output channels, K = pixels, with MN-major operands read from
+// the staged NHWC data; an all-ones operand gives the bias gradient.  Each
+// block accumulates its share of the pixels in tensor memory and writes one
+// partial; a reduction kernel sums the partials in a fixed order
+// (deterministic).
 #include <cuda_bf16.h>
 
 #include "tde_common.cuh"
@@ -72,13 +72,13 @@ __device__ __forceinline__ uint4 pack8(const float *f) {
 
 // Chunk c (channels 8c..8c+7) of the concatenated convolution input at
 // (img, y, x); zero outside the image.  ca and cb are multiples of 8.
-template <typename Args>
+template <int MODE, typename Args>
 __device__ __forceinline__ uint4 load_input_chunk(const Args &A, int img, int y, int x, int c) {
     if (y < 0 || y >= A.h || x < 0 || x >= A.w) return make_uint4(0u, 0u, 0u, 0u);
     const int cca = A.ca >> 3;
     if (c < cca) {
-        if (A.mode_a == SRC_DIRECT) return ldg16(A.a + (((size_t)img * A.h + y) * A.w + x) * A.ca + 8 * c);
-        if (A.mode_a == SRC_UP) {
+        if (MODE == SRC_DIRECT) return ldg16(A.a + (((size_t)img * A.h + y) * A.w + x) * A.ca + 8 * c);
+        if (MODE == SRC_UP) {
             const int hh = A.h >> 1, ww = A.w >> 1;
             return ldg16(A.a + (((size_t)img * hh + (y >> 1)) * ww + (x >> 1)) * A.ca + 8 * c);
         }
@@ -89,22 +89,120 @@ __device__ __forceinline__ uint4 load_input_chunk(const Args &A, int img, int y,
     }
     return ldg16(A.b + (((size_t)img * A.h + y) * A.w + x) * A.cb + 8 * (c - cca));
 }
+template <typename Args>
+__device__ __forceinline__ uint4 load_input_chunk(const Args &A, int img, int y, int x, int c) {
+    if (A.mode_a == SRC_POOL) return load_input_chunk<SRC_POOL>(A, img, y, x, c);
+    if (A.mode_a == SRC_UP) return load_input_chunk<SRC_UP>(A, img, y, x, c);
+    return load_input_chunk<SRC_DIRECT>(A, img, y, x, c);
+}
 
 // ---------------------------------------------------------------------------
 // Forward / input-gradient convolution
+//
+// A block owns a strip of R consecutive output rows of one 128-pixel column
+// tile.  Input rows live in a ring of 4 halo slots: tile row y reads slots
+// y-1, y, y+1 while row y+2 is loaded into the fourth, so each row is loaded
+// once per strip instead of three times.  Two TMEM accumulators let the MMAs
+// of row y run while the epilogue of row y-1 drains the other one.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs A) {
+constexpr int kSlots = 4;
+
+// Loads one input row (halo pixels x0-1 .. x0+128, every chunk) into a slot.
+// Loads are issued in groups before their stores so that several are in
+// flight per thread.
+template <int MODE>
+__device__ __forceinline__ void load_row(const ConvArgs &A, unsigned char *slot, int cc, int img, int y, int x0,
+                                         int tid) {
+    constexpr int G = MODE == SRC_POOL ? 4 : 8;
+    const int n = kHaloW * cc;
+    for (int base = tid; base < n; base += kConvThreads * G) {
+        uint4 v[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int i = base + g * kConvThreads;
+            v[g] = make_uint4(0u, 0u, 0u, 0u);
+            if (i < n) {
+                const int c = i % cc, px = i / cc;
+                v[g] = load_input_chunk<MODE>(A, img, y, x0 + px - 1, c);
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int i = base + g * kConvThreads;
+            if (i < n) {
+                const int c = i % cc, px = i / cc;
+                *reinterpret_cast<uint4 *>(slot + ((size_t)c * kHaloW + px) * 16) = v[g];
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, int warp, int lane, int img, int y,
+                                              int x0) {
+    const int m = warp * 32 + lane;
+    const int x = x0 + m;
+    const bool valid = x < A.w;
+    const size_t pix = ((size_t)img * A.h + y) * A.w + (valid ? x : 0);
+    float r = 0.f;
+    for (int j = 0; j < A.cout; j += 16) {
+        float v[16];
+        tc::tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + (uint32_t)j, v);
+        if (!valid) continue;
+        if (A.bias) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) v[k] += __ldg(A.bias + j + k);
+        }
+        if (A.relu) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) v[k] = v[k] > 0.f ? v[k] : 0.f;
+        }
+        if (A.mask) {
+            float mk[16];
+            unpack8(ldg16(A.mask + pix * A.cout + j), mk);
+            unpack8(ldg16(A.mask + pix * A.cout + j + 8), mk + 8);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) v[k] = mk[k] > 0.f ? v[k] : 0.f;
+        }
+        const uint4 q0 = pack8(v), q1 = pack8(v + 8);
+        uint4 *o = reinterpret_cast<uint4 *>(A.out + pix * A.cout + j);
+        o[0] = q0;
+        o[1] = q1;
+        if (A.head_w) {
+            float f[16];
+            unpack8(q0, f);
+            unpack8(q1, f + 8);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) r = fmaf(__ldg(A.head_w + j + k), f[k], r);
+        }
+    }
+    if (valid && A.head_w) {
+        const float d = A.depth_in[pix];
+        const float o = d > 0.f ? d + 0.01f * (r + __ldg(A.head_b)) : 0.f;  // residual in cm
+        if (A.depth_out) A.depth_out[pix] = o;
+        if (A.depth_mm) {
+            const float mm = fminf(fmaxf(rintf(o * 1000.f), 0.f), (float)TDE_MAX_DEPTH_VALUE);
+            A.depth_mm[pix] = (uint16_t)mm;
+        }
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs A, int rows_per_item) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     const int cin = A.ca + A.cb, cc = cin >> 3;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const size_t slot_bytes = (size_t)cc * kHaloW * 16;
     unsigned char *halo = smem;
-    unsigned char *wsm = smem + (size_t)3 * cc * kHaloW * 16;
+    unsigned char *wsm = smem + kSlots * slot_bytes;
     const uint32_t ncols = tmem_cols(A.cout);
 
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
-    if (tid == 0) tc::mbar_init(&mbar, 1);
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
     // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B
     const int nw = A.cout * 9 * cc;
     for (int i = tid; i < nw; i += kConvThreads) {
@@ -118,124 +216,120 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     const uint32_t halo_s = tc::smem_u32(halo), w_s = tc::smem_u32(wsm);
     const uint32_t idesc = tc::idesc_bf16(kTileM, A.cout);
     const int tiles_x = (A.w + kTileM - 1) / kTileM;
-    const int ntiles = A.n * A.h * tiles_x;
-    const int nh = 3 * kHaloW * cc;
-    uint32_t parity = 0;
+    const int chunks = (A.h + rows_per_item - 1) / rows_per_item;
+    const int items = A.n * tiles_x * chunks;
+    uint32_t g = 0;  // rows issued by this block: accumulator g & 1, its mbarrier phase (g >> 1) & 1
     bool failed = false;
 
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int xt = tile % tiles_x, rowi = tile / tiles_x;
-        const int y = rowi % A.h, img = rowi / A.h;
+    for (int item = blockIdx.x; item < items && !failed; item += gridDim.x) {
+        const int xt = item % tiles_x;
+        const int ch = (item / tiles_x) % chunks;
+        const int img = item / (tiles_x * chunks);
         const int x0 = xt * kTileM;
-        for (int i = tid; i < nh; i += kConvThreads) {
-            const int c = i % cc, px = (i / cc) % kHaloW, dy = i / (cc * kHaloW);
-            *reinterpret_cast<uint4 *>(halo + ((size_t)(dy * cc + c) * kHaloW + px) * 16) =
-                load_input_chunk(A, img, y + dy - 1, x0 + px - 1, c);
-        }
+        const int y0 = ch * rows_per_item;
+        const int y1 = min(A.h, y0 + rows_per_item);
+        for (int dy = -1; dy <= 1; ++dy)
+            load_row<MODE>(A, halo + (size_t)((y0 + dy + kSlots) % kSlots) * slot_bytes, cc, img, y0 + dy, x0, tid);
         tc::fence_proxy_async();
         __syncthreads();
-        if (tid == 0) {
-            tc::fence_after_sync();
-            uint32_t acc = 0;
-            for (int t = 0; t < 9; ++t) {
-                const int dy = t / 3, dx = t % 3;
-                for (int kc = 0; kc < cc; kc += 2) {
-                    const uint64_t ad = tc::desc(halo_s + (uint32_t)(((dy * cc + kc) * kHaloW + dx) * 16), kHaloW * 16, 128);
-                    const uint64_t bd = tc::desc(w_s + (uint32_t)((t * cc + kc) * A.cout * 16), A.cout * 16, 128);
-                    tc::mma_bf16(tmem, ad, bd, idesc, acc);
-                    acc = 1;
+        for (int y = y0; y < y1; ++y, ++g) {
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t dacc = tmem + (g & 1u) * ncols;
+                uint32_t acc = 0;
+                for (int t = 0; t < 9; ++t) {
+                    const int dy = t / 3, dx = t % 3;
+                    const uint32_t sbase = halo_s + (uint32_t)(((y + dy - 1 + kSlots) % kSlots) * slot_bytes);
+                    for (int kc = 0; kc < cc; kc += 2) {
+                        const uint64_t ad = tc::desc(sbase + (uint32_t)((kc * kHaloW + dx) * 16), kHaloW * 16, 128);
+                        const uint64_t bd = tc::desc(w_s + (uint32_t)((t * cc + kc) * A.cout * 16), A.cout * 16, 128);
+                        tc::mma_bf16(dacc, ad, bd, idesc, acc);
+                        acc = 1;
+                    }
                 }
+                tc::commit(&mbar[g & 1u]);
             }
-            tc::commit(&mbar);
+            if (y > y0) {
+                // row y-1: its MMAs are done, so its accumulator can be drained
+                // and the slot of row y-2 refilled
+                const uint32_t gp = g - 1;
+                const bool ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
+                if (__syncthreads_or(!ok)) {
+                    failed = true;
+                    break;
+                }
+                tc::fence_after_sync();
+                conv_epilogue(A, tmem + (gp & 1u) * ncols, warp, lane, img, y - 1, x0);
+            }
+            if (y + 1 < y1)
+                load_row<MODE>(A, halo + (size_t)((y + 2) % kSlots) * slot_bytes, cc, img, y + 2, x0, tid);
+            tc::fence_proxy_async();
+            tc::fence_before_sync();
+            __syncthreads();
         }
-        const bool done = tc::mbar_wait(&mbar, parity);
-        parity ^= 1u;
-        if (__syncthreads_or(!done)) {
+        if (failed) break;
+        // last row of the strip
+        const uint32_t gp = g - 1;
+        const bool ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
+        if (__syncthreads_or(!ok)) {
             failed = true;
             break;
         }
         tc::fence_after_sync();
-
-        // epilogue: warp w owns TMEM lanes (pixels) 32w..32w+31
-        const int m = warp * 32 + lane;
-        const int x = x0 + m;
-        const bool valid = x < A.w;
-        const size_t pix = ((size_t)img * A.h + y) * A.w + (valid ? x : 0);
-        float r = 0.f;
-        for (int j = 0; j < A.cout; j += 16) {
-            float v[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)j, v);
-            if (!valid) continue;
-            if (A.bias) {
-#pragma unroll
-                for (int k = 0; k < 16; ++k) v[k] += __ldg(A.bias + j + k);
-            }
-            if (A.relu) {
-#pragma unroll
-                for (int k = 0; k < 16; ++k) v[k] = v[k] > 0.f ? v[k] : 0.f;
-            }
-            if (A.mask) {
-                float mk[16];
-                unpack8(ldg16(A.mask + pix * A.cout + j), mk);
-                unpack8(ldg16(A.mask + pix * A.cout + j + 8), mk + 8);
-#pragma unroll
-                for (int k = 0; k < 16; ++k) v[k] = mk[k] > 0.f ? v[k] : 0.f;
-            }
-            const uint4 q0 = pack8(v), q1 = pack8(v + 8);
-            uint4 *o = reinterpret_cast<uint4 *>(A.out + pix * A.cout + j);
-            o[0] = q0;
-            o[1] = q1;
-            if (A.head_w) {
-                float f[16];
-                unpack8(q0, f);
-                unpack8(q1, f + 8);
-#pragma unroll
-                for (int k = 0; k < 16; ++k) r = fmaf(__ldg(A.head_w + j + k), f[k], r);
-            }
-        }
-        if (valid && A.head_w) {
-            const float d = A.depth_in[pix];
-            const float o = d > 0.f ? d + 0.01f * (r + __ldg(A.head_b)) : 0.f;  // residual in cm
-            if (A.depth_out) A.depth_out[pix] = o;
-            if (A.depth_mm) {
-                const float mm = fminf(fmaxf(rintf(o * 1000.f), 0.f), (float)TDE_MAX_DEPTH_VALUE);
-                A.depth_mm[pix] = (uint16_t)mm;
-            }
-        }
+        conv_epilogue(A, tmem + (gp & 1u) * ncols, warp, lane, img, y1 - 1, x0);
         tc::fence_before_sync();
         __syncthreads();
     }
     if (failed) {
         if (tid == 0) atomicExch(A.err, 1);
-        // give the MMAs in flight a second bounded chance to finish before
-        // the tensor memory they write is released
-        tc::mbar_wait(&mbar, parity ^ 1u);
+        // bounded second chance for MMAs still in flight before the TMEM is freed
+        tc::mbar_wait(&mbar[0], 0u);
+        tc::mbar_wait(&mbar[1], 0u);
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+    if (warp == 0) tc::tmem_dealloc(tmem, 2 * ncols);
 }
 
 // ---------------------------------------------------------------------------
 // Weight gradient
+//
+// dW[co][t][ci] = sum_p dZ[p][co] X[p + s_t][ci] as D = A B with K = pixels,
+// both operands MN-major: the tensor core reads the staged NHWC data as it
+// lies.  X is staged per 64-pixel step as planes of 8-channel chunks (3 rows
+// x 66 halo pixels, 16 B per pixel); for horizontal tap offset dx, the rows
+// (dy, ci) of A are the planes in order (a uniform chunk stride) and the
+// pixel window starts dx pixels later (16 * dx bytes).  dZ is staged the same
+// way (planes of 8 output channels).  The bias gradient is the same MMA with
+// a constant all-ones A.  Without swizzling, a descriptor's LBO is the stride
+// between 8-element groups along K and its SBO the stride along M (or N), for
+// MN-major operands as for K-major ones.
 // ---------------------------------------------------------------------------
+constexpr int kWgPlaneX = kWgHalo * 16;   // 1056 B: one 8-channel plane of X
+constexpr int kWgPlaneZ = kWgK * 16;      // 1024 B: one 8-channel plane of dZ
+
 struct WgLayout {
-    int cin, cc, rows, mtiles;
-    uint32_t x_off, z_off, bt_off, a_off, total;
+    int cin, cc, mtiles, xplanes, zplanes;
+    uint32_t x_bytes, z_bytes, ones_off, total, tcols;
 };
 __host__ __device__ inline WgLayout wg_layout(int cin, int cout) {
     WgLayout L;
     L.cin = cin;
     L.cc = cin / 8;
-    L.rows = 9 * cin + 1;
-    L.mtiles = (L.rows + 127) / 128;
-    L.x_off = 0;                                               // X halo, planes (row, chunk) x 66 px x 16 B
-    L.z_off = L.x_off + (uint32_t)(3 * L.cc * kWgHalo * 16);   // dZ rows [px][cout]
-    L.bt_off = L.z_off + (uint32_t)(kWgK * cout * 2);          // B: dZ^T core matrices
-    L.a_off = L.bt_off + (uint32_t)(kWgK * cout * 2);          // A: 2 buffers of 128 x 64 bf16
-    L.a_off = (L.a_off + 127u) & ~127u;
-    L.total = L.a_off + 2u * 128u * kWgK * 2u;
+    L.mtiles = (3 * cin + 127) / 128;                 // rows (dy, ci) per horizontal offset
+    L.xplanes = max(3 * L.cc, 16 * L.mtiles);         // MMAs read whole 16-chunk row tiles
+    L.zplanes = cout / 8;
+    L.x_bytes = (uint32_t)(L.xplanes * kWgPlaneX);
+    L.z_bytes = (uint32_t)(L.zplanes * kWgPlaneZ);
+    L.ones_off = 2u * (L.x_bytes + L.z_bytes);        // two staging buffers, then the ones tile
+    L.total = L.ones_off + 16u * 256u;                // 16 chunks x 16 pixels x 16 B
+    L.tcols = (uint32_t)(3 * L.mtiles * cout + cout);  // 3 dx x row tiles, + bias
     return L;
+}
+
+// MN-major kind::f16 instruction descriptor (bits 15, 16 = 1).
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) {
+    return tc::idesc_bf16(M, N) | (1u << 15) | (1u << 16);
 }
 
 __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs A) {
@@ -246,143 +340,130 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs A)
     const WgLayout L = wg_layout(cin, cout);
     const int cc = L.cc;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t ncols = tmem_cols(L.mtiles * cout);
-    unsigned char *xs = smem + L.x_off;
-    const bf16 *xsb = reinterpret_cast<const bf16 *>(xs);
-    bf16 *zs = reinterpret_cast<bf16 *>(smem + L.z_off);
-    unsigned char *bt = smem + L.bt_off;
-    unsigned char *as = smem + L.a_off;
+    const uint32_t ncols = tmem_cols((int)L.tcols);
+    unsigned char *ones = smem + L.ones_off;
 
     if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
     if (tid == 0) {
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
     }
+    {
+        const uint4 one8 = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);  // eight bf16 1.0
+        for (int i = tid; i < 256; i += kWgThreads) *reinterpret_cast<uint4 *>(ones + (size_t)i * 16) = one8;
+    }
+    tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
-    const uint32_t a_s = tc::smem_u32(as), b_s = tc::smem_u32(bt);
-    const uint32_t idesc = tc::idesc_bf16(128, cout);
+    const uint32_t s0 = tc::smem_u32(smem), ones_s = tc::smem_u32(ones);
+    const uint32_t idesc = idesc_bf16_mn(128, cout);
     const int tiles_x = (A.w + kWgK - 1) / kWgK;
     const int ntiles = A.n * A.h * tiles_x;
-    uint32_t issued[2] = {0u, 0u}, waited[2] = {0u, 0u};
-    bool first = true, failed = false;
+    const int zc = cout / 8;
+    uint32_t k = 0;  // K steps staged by this block: buffer k & 1, mbarrier phase (k >> 1) & 1
+    bool failed = false;
 
-    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
         const int xt = tile % tiles_x, rowi = tile / tiles_x;
         const int y = rowi % A.h, img = rowi / A.h;
         const int x0 = xt * kWgK;
-        // every MMA reading B (and the A buffers) must be done before restaging
-        bool ok = true;
-        for (int b = 0; b < 2; ++b)
-            if (issued[b] > waited[b]) {
-                ok &= tc::mbar_wait(&mbar[b], waited[b] & 1u);
-                waited[b]++;
-            }
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        // stage X halo (3 rows x 66 px x cin) and the dZ row segment (64 px x cout)
-        for (int i = tid; i < 3 * kWgHalo * cc; i += kWgThreads) {
-            const int c = i % cc, px = (i / cc) % kWgHalo, dy = i / (cc * kWgHalo);
-            *reinterpret_cast<uint4 *>(xs + ((size_t)(dy * cc + c) * kWgHalo + px) * 16) =
-                load_input_chunk(A, img, y + dy - 1, x0 + px - 1, c);
-        }
-        const int zc = cout / 8;
-        for (int i = tid; i < kWgK * zc; i += kWgThreads) {
-            const int c = i % zc, px = i / zc;
-            const int x = x0 + px;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (x < A.w) v = ldg16(A.dz + (((size_t)img * A.h + y) * A.w + x) * cout + 8 * c);
-            *reinterpret_cast<uint4 *>(zs + (size_t)px * cout + 8 * c) = v;
-        }
-        __syncthreads();
-        // B = dZ^T: row co, K = pixel; core matrix (k chunk g, row group co/8)
-        for (int i = tid; i < cout * (kWgK / 8); i += kWgThreads) {
-            const int co = i % cout, g = i / cout;
-            float f[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) f[j] = __bfloat162float(zs[(size_t)(8 * g + j) * cout + co]);
-            *reinterpret_cast<uint4 *>(bt + ((size_t)(g * (cout / 8) + co / 8) * 128 + (co % 8) * 16)) = pack8(f);
-        }
-        for (int mt = 0; mt < L.mtiles; ++mt) {
-            const int buf = (int)((issued[0] + issued[1]) & 1u);
-            ok = true;
-            if (issued[buf] > waited[buf]) {
-                ok = tc::mbar_wait(&mbar[buf], waited[buf] & 1u);
-                waited[buf]++;
-            }
+        const uint32_t buf = k & 1u;
+        // the MMAs that read this buffer two steps ago must be done
+        if (k >= 2) {
+            const uint32_t kp = k - 2;
+            const bool ok = tc::mbar_wait(&mbar[buf], (kp >> 1) & 1u);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
             }
-            unsigned char *ab = as + (size_t)buf * 128 * kWgK * 2;
-            // A rows r = mt*128 + i: (tap, channel) of the shifted input, or ones (bias), or zero
-            for (int it = tid; it < 128 * (kWgK / 8); it += kWgThreads) {
-                const int i = it % 128, g = it / 128;
-                const int r = mt * 128 + i;
-                float f[8];
-                if (r < 9 * cin) {
-                    const int t = r / cin, ci = r % cin;
-                    const int dy = t / 3, dx = t % 3;
-                    const bf16 *src = xsb + ((size_t)(dy * cc + ci / 8) * kWgHalo) * 8 + (ci % 8);
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) f[j] = __bfloat162float(src[(size_t)(8 * g + j + dx) * 8]);
-                } else {
-                    const float one = r == 9 * cin ? 1.f : 0.f;
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) f[j] = (x0 + 8 * g + j < A.w) ? one : 0.f;
-                }
-                *reinterpret_cast<uint4 *>(ab + ((size_t)g * 2048 + (i / 8) * 128 + (i % 8) * 16)) = pack8(f);
-            }
-            tc::fence_proxy_async();
-            __syncthreads();
-            if (tid == 0) {
-                tc::fence_after_sync();
-                const uint32_t abase = a_s + (uint32_t)buf * 128u * kWgK * 2u;
-                for (int kk = 0; kk < kWgK / 16; ++kk) {
-                    const uint64_t ad = tc::desc(abase + (uint32_t)(2 * kk * 2048), 2048, 128);
-                    const uint64_t bd = tc::desc(b_s + (uint32_t)(2 * kk * (cout / 8) * 128), cout * 16, 128);
-                    tc::mma_bf16(tmem + (uint32_t)(mt * cout), ad, bd, idesc, (first && kk == 0) ? 0u : 1u);
-                }
-                tc::commit(&mbar[buf]);
-            }
-            issued[buf]++;
         }
-        first = false;
+        unsigned char *xs = smem + buf * (L.x_bytes + L.z_bytes);
+        unsigned char *zs = xs + L.x_bytes;
+        // stage X (3 rows x 66 px x cin) and dZ (64 px x cout), loads grouped before stores
+        const int nx = 3 * kWgHalo * cc, nz = kWgK * zc;
+        for (int base = tid; base < nx + nz; base += kWgThreads * 4) {
+            uint4 v[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                const int i = base + g * kWgThreads;
+                v[g] = make_uint4(0u, 0u, 0u, 0u);
+                if (i < nx) {
+                    const int c = i % cc, px = (i / cc) % kWgHalo, dy = i / (cc * kWgHalo);
+                    v[g] = load_input_chunk(A, img, y + dy - 1, x0 + px - 1, c);
+                } else if (i < nx + nz) {
+                    const int j = i - nx, c = j % zc, px = j / zc;
+                    if (x0 + px < A.w) v[g] = ldg16(A.dz + (((size_t)img * A.h + y) * A.w + x0 + px) * cout + 8 * c);
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                const int i = base + g * kWgThreads;
+                if (i < nx) {
+                    const int c = i % cc, px = (i / cc) % kWgHalo, dy = i / (cc * kWgHalo);
+                    *reinterpret_cast<uint4 *>(xs + (size_t)(dy * cc + c) * kWgPlaneX + px * 16) = v[g];
+                } else if (i < nx + nz) {
+                    const int j = i - nx, c = j % zc, px = j / zc;
+                    *reinterpret_cast<uint4 *>(zs + (size_t)c * kWgPlaneZ + px * 16) = v[g];
+                }
+            }
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t xb = s0 + buf * (L.x_bytes + L.z_bytes), zb = xb + L.x_bytes;
+            for (int kk = 0; kk < kWgK / 16; ++kk) {
+                const uint32_t first = (k == 0 && kk == 0) ? 0u : 1u;
+                const uint64_t bd = tc::desc(zb + (uint32_t)(kk * 16 * 16), 128, kWgPlaneZ);
+                for (int dx = 0; dx < 3; ++dx)
+                    for (int mt = 0; mt < L.mtiles; ++mt) {
+                        const uint64_t ad =
+                            tc::desc(xb + (uint32_t)(16 * mt * kWgPlaneX + (kk * 16 + dx) * 16), 128, kWgPlaneX);
+                        tc::mma_bf16(tmem + (uint32_t)((dx * L.mtiles + mt) * cout), ad, bd, idesc, first);
+                    }
+                const uint64_t od = tc::desc(ones_s, 128, 256);
+                tc::mma_bf16(tmem + (uint32_t)(3 * L.mtiles * cout), od, bd, idesc, first);
+            }
+            tc::commit(&mbar[buf]);
+        }
     }
-    // drain
+    // drain: the last one or two steps
     bool ok = true;
-    for (int b = 0; b < 2; ++b)
-        if (issued[b] > waited[b]) {
-            ok &= tc::mbar_wait(&mbar[b], waited[b] & 1u);
-            waited[b]++;
-        }
+    if (!failed) {
+        for (uint32_t kp = (k >= 2 ? k - 2 : 0); kp < k; ++kp) ok &= tc::mbar_wait(&mbar[kp & 1u], (kp >> 1) & 1u);
+    }
     failed |= __syncthreads_or(!ok) != 0;
     tc::fence_after_sync();
     if (failed) {
         if (tid == 0) atomicExch(A.err, 1);
     } else {
-        // epilogue: warps w and w+4 share TMEM lane quarter w; they split the row tiles
+        // rows R = dx * mtiles * 128 + (dy * cin + ci), bias row R = 3 * mtiles * 128;
+        // warps w and w + 4 share TMEM lane quarter w and split the tiles
         const int q = warp & 3;
-        const size_t rows_pad = (size_t)L.mtiles * 128;
+        const size_t rows_pad = (size_t)3 * L.mtiles * 128 + 1;
         float *dst = A.partial + (size_t)blockIdx.x * rows_pad * cout;
-        for (int mt = 0; mt < L.mtiles; ++mt) {
-            const bool mine = ((mt & 1) == (warp >> 2));
+        const int ntile = 3 * L.mtiles + 1;
+        for (int tl = 0; tl < ntile; ++tl) {
+            if ((tl & 1) != (warp >> 2)) continue;
             for (int j = 0; j < cout; j += 16) {
                 float v[16];
-                if (mine) {
-                    tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(mt * cout + j), v);
-                    if (first) {  // this block visited no pixels
+                tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(tl * cout + j), v);
+                if (k == 0) {
 #pragma unroll
-                        for (int k = 0; k < 16; ++k) v[k] = 0.f;
-                    }
-                    const size_t r = (size_t)mt * 128 + q * 32 + lane;
+                    for (int e = 0; e < 16; ++e) v[e] = 0.f;
+                }
+                const int rr = q * 32 + lane;
+                if (tl < 3 * L.mtiles) {
+                    const size_t r = (size_t)tl * 128 + rr;
                     float4 *o = reinterpret_cast<float4 *>(dst + r * cout + j);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                    for (int e = 0; e < 4; ++e) o[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+                } else if (rr == 0) {
+                    float4 *o = reinterpret_cast<float4 *>(dst + (rows_pad - 1) * cout + j);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) o[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
                 }
             }
         }
@@ -392,16 +473,26 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs A)
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
-__global__ void wgrad_reduce_kernel(const float *__restrict__ partial, int blocks, int cin, int cout, size_t rows_pad,
+__global__ void wgrad_reduce_kernel(const float *__restrict__ partial, int blocks, int cin, int cout, int mtiles,
                                     float *__restrict__ dw, float *__restrict__ db) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = r * cout + co
-    const int nr = 9 * cin + 1;
-    if (i >= nr * cout) return;
-    const int r = i / cout, co = i % cout;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = ((co * 9 + t) * cin + ci), then cout biases
+    const int nw = cout * 9 * cin;
+    if (i >= nw + cout) return;
+    const size_t rows_pad = (size_t)3 * mtiles * 128 + 1;
+    size_t r;
+    int co;
+    if (i < nw) {
+        const int ci = i % cin, t = (i / cin) % 9;
+        co = i / (9 * cin);
+        r = (size_t)(t % 3) * mtiles * 128 + (size_t)(t / 3) * cin + ci;
+    } else {
+        co = i - nw;
+        r = rows_pad - 1;
+    }
     float s = 0.f;
     for (int b = 0; b < blocks; ++b) s += partial[((size_t)b * rows_pad + r) * cout + co];
-    if (r == 9 * cin) db[co] = s;
-    else dw[((size_t)co * 9 + r / cin) * cin + r % cin] = s;
+    if (i < nw) dw[i] = s;
+    else db[co] = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -463,8 +554,10 @@ constexpr int kInPartial = 16 * (kInK + 1);
 __global__ void __launch_bounds__(256) conv_in_wgrad_kernel(const float *__restrict__ depth_m,
                                                             const bf16 *__restrict__ dz1, int n, int h, int w,
                                                             float *__restrict__ partial) {
+    extern __shared__ float rows3[];  // depth rows y-1, y, y+1 with a zero column either side: 3 x (w + 2)
     __shared__ float red[16][16][kInK + 1];
     const int co = threadIdx.x & 15, pl = threadIdx.x >> 4;
+    const int W2 = w + 2;
     float s[kInK + 1];
 #pragma unroll
     for (int k = 0; k <= kInK; ++k) s[k] = 0.f;
@@ -473,16 +566,19 @@ __global__ void __launch_bounds__(256) conv_in_wgrad_kernel(const float *__restr
         const int rowi = row0 + rr;
         if (rowi >= n * h) break;
         const int y = rowi % h, img = rowi / h;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * W2; i += blockDim.x) {
+            const int r = i / W2, x = i % W2 - 1, yy = y + r - 1;
+            rows3[i] = (x >= 0 && x < w && yy >= 0 && yy < h) ? depth_m[((size_t)img * h + yy) * w + x] : 0.f;
+        }
+        __syncthreads();
         for (int x = pl; x < w; x += 16) {
             const size_t p = ((size_t)img * h + y) * w + x;
             const float g = __bfloat162float(dz1[p * 16 + co]);
             if (g == 0.f) continue;
             float d[9];
 #pragma unroll
-            for (int t = 0; t < 9; ++t) {
-                const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
-                d[t] = (yy >= 0 && yy < h && xx >= 0 && xx < w) ? depth_m[((size_t)img * h + yy) * w + xx] : 0.f;
-            }
+            for (int t = 0; t < 9; ++t) d[t] = rows3[(t / 3) * W2 + x + t % 3];
             float in[kInK];
             input_features(d, in);
 #pragma unroll
@@ -571,15 +667,24 @@ __global__ void __launch_bounds__(kLossThreads) loss_kernel(const float *__restr
     }
 }
 
+// One block per reduced quantity; a fixed-shape tree over the block partials.
 __global__ void loss_reduce_kernel(const float *__restrict__ partial, int blocks, float *__restrict__ dhead_w,
                                    float *__restrict__ dhead_b, double *__restrict__ loss2) {
-    const int k = threadIdx.x;
-    if (k >= 19) return;
+    __shared__ double red[256];
+    const int k = blockIdx.x;
     double t = 0.0;
-    for (int b = 0; b < blocks; ++b) t += (double)partial[(size_t)b * 19 + k];
-    if (k < 2) loss2[k] = t;
-    else if (k < 18) dhead_w[k - 2] = (float)t;
-    else dhead_b[0] = (float)t;
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) t += (double)partial[(size_t)b * 19 + k];
+    red[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (k < 2) loss2[k] = red[0];
+        else if (k < 18) dhead_w[k - 2] = (float)red[0];
+        else dhead_b[0] = (float)red[0];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -685,38 +790,70 @@ static uint32_t smem_floor_for_tmem(uint32_t ncols) {
     return kSmemPerSM / (kmax + 1) - 1024u + 16u;
 }
 
-// Raises the kernel's dynamic shared-memory limit to `bytes` when needed.
-static int allow_smem(const void *fn, size_t bytes, const char *what) {
-    cudaFuncAttributes fa;
-    TDE_CUDA(cudaFuncGetAttributes(&fa, fn), what);
-    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return TDE_OK;
-    if (bytes + fa.sharedSizeBytes > 227 * 1024)
-        return set_error(TDE_ERR_UNSUPPORTED, "%s: %zu B of shared memory", what, bytes);
-    TDE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), what);
+size_t conv_smem_bytes(int cin, int cout) {
+    const int cc = cin / 8;
+    const size_t s = (size_t)kSlots * cc * kHaloW * 16 + (size_t)9 * cc * cout * 16;
+    const size_t fl = smem_floor_for_tmem(2 * tmem_cols(cout));
+    return s > fl ? s : fl;
+}
+
+int prepare_kernels() {
+    // allow the largest dynamic shared memory a block may have, once, so that
+    // launches (also inside stream capture) make no other runtime call
+    const void *fns[4] = {(const void *)conv3x3_tc_kernel<SRC_DIRECT>, (const void *)conv3x3_tc_kernel<SRC_POOL>,
+                          (const void *)conv3x3_tc_kernel<SRC_UP>, (const void *)wgrad_tc_kernel};
+    for (const void *fn : fns) {
+        cudaFuncAttributes fa;
+        TDE_CUDA(cudaFuncGetAttributes(&fa, fn), "refiner: kernel attributes");
+        TDE_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(227 * 1024 - fa.sharedSizeBytes)),
+                 "refiner: shared memory limit");
+    }
     return TDE_OK;
 }
 
-size_t conv_smem_bytes(int cin, int cout) {
-    const int cc = cin / 8;
-    size_t s = (size_t)3 * cc * kHaloW * 16 + (size_t)9 * cc * cout * 16;
-    return s > smem_floor_for_tmem(tmem_cols(cout)) ? s : smem_floor_for_tmem(tmem_cols(cout));
+int conv_blocks_per_sm(int cin, int cout, int *out) {
+    // resident blocks per SM from the limits that apply: shared memory (with
+    // the 1 KB the SM reserves per block), registers, and the tensor memory
+    // each block allocates (2 accumulators)
+    cudaFuncAttributes fa;
+    TDE_CUDA(cudaFuncGetAttributes(&fa, (const void *)conv3x3_tc_kernel<SRC_DIRECT>), "refiner: kernel attributes");
+    int regs = 0;
+    for (const void *fn : {(const void *)conv3x3_tc_kernel<SRC_POOL>, (const void *)conv3x3_tc_kernel<SRC_UP>,
+                           (const void *)conv3x3_tc_kernel<SRC_DIRECT>}) {
+        cudaFuncAttributes f;
+        TDE_CUDA(cudaFuncGetAttributes(&f, fn), "refiner: kernel attributes");
+        regs = f.numRegs > regs ? f.numRegs : regs;
+    }
+    const size_t per_block = conv_smem_bytes(cin, cout) + fa.sharedSizeBytes + 1024;
+    int n = (int)(kSmemPerSM / per_block);
+    const int by_regs = 65536 / (((regs + 7) / 8) * 8 * kConvThreads);
+    const int by_tmem = (int)(512u / (2 * tmem_cols(cout)));
+    n = n < by_regs ? n : by_regs;
+    n = n < by_tmem ? n : by_tmem;
+    if (n < 1) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: cin=%d cout=%d does not fit an SM", cin, cout);
+    *out = n;
+    return TDE_OK;
 }
 
-int launch_conv(const ConvArgs &a, int num_sms, cudaStream_t s) {
+int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t s) {
     const int cin = a.ca + a.cb;
-    if (cin % 16 || a.ca % 8 || a.cout % 16 || a.cout < 16 || a.cout > 256 || a.w <= 0 || a.h <= 0 || a.n <= 0 ||
-        (a.head_w && a.cout != 16) || (a.mode_a == SRC_UP && (a.h % 2 || a.w % 2)))
+    if (cin % 16 || a.ca % 8 || a.cout % 16 || a.cout < 16 || a.cout > 128 || cin > 128 || a.w <= 0 || a.h <= 0 ||
+        a.n <= 0 || (a.head_w && a.cout != 16) || (a.mode_a == SRC_UP && (a.h % 2 || a.w % 2)))
         return set_error(TDE_ERR_INVALID_ARG, "refiner conv: unsupported shape cin=%d cout=%d", cin, a.cout);
     const size_t smem = conv_smem_bytes(cin, a.cout);
-    if (smem > 227 * 1024) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: %zu B of shared memory", smem);
-    TDE_TRY(allow_smem((const void *)conv3x3_tc_kernel, smem, "refiner conv"));
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3x3_tc_kernel, kConvThreads, smem);
-    if (per_sm < 1) per_sm = 1;
-    const int tiles = a.n * a.h * ((a.w + kTileM - 1) / kTileM);
-    int grid = num_sms * per_sm;
-    if (grid > tiles) grid = tiles;
-    conv3x3_tc_kernel<<<grid, kConvThreads, smem, s>>>(a);
+    if (smem > 227 * 1024 - 256) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: %zu B of shared memory", smem);
+    // rows per block: as many as keep every resident block busy
+    const int tiles_x = (a.w + kTileM - 1) / kTileM;
+    const long row_tiles = (long)a.n * a.h * tiles_x;
+    const long slots = (long)num_sms * blocks_per_sm;
+    int rows = (int)(row_tiles / slots);
+    rows = rows < 1 ? 1 : rows > 64 ? 64 : rows;
+    const long items = (long)a.n * tiles_x * ((a.h + rows - 1) / rows);
+    const int grid = (int)(items < slots ? items : slots);
+    if (a.mode_a == SRC_POOL) conv3x3_tc_kernel<SRC_POOL><<<grid, kConvThreads, smem, s>>>(a, rows);
+    else if (a.mode_a == SRC_UP) conv3x3_tc_kernel<SRC_UP><<<grid, kConvThreads, smem, s>>>(a, rows);
+    else conv3x3_tc_kernel<SRC_DIRECT><<<grid, kConvThreads, smem, s>>>(a, rows);
     return check_launch("refiner conv");
 }
 
@@ -728,27 +865,26 @@ int wgrad_blocks(int num_sms, int cin, int cout) {
 
 size_t wgrad_partial_floats(int blocks, int cin, int cout) {
     const WgLayout L = wg_layout(cin, cout);
-    return (size_t)blocks * L.mtiles * 128 * cout;
+    return (size_t)blocks * ((size_t)3 * L.mtiles * 128 + 1) * cout;
 }
 
 int launch_wgrad(const WgradArgs &a, int blocks, cudaStream_t s) {
     const int cin = a.ca + a.cb;
     const WgLayout L = wg_layout(cin, a.cout);
-    if (cin % 8 || a.cout % 16 || a.cout < 16 || L.mtiles * a.cout > 512)
+    if (cin % 8 || a.cout % 16 || a.cout < 16 || L.tcols > 512)
         return set_error(TDE_ERR_INVALID_ARG, "refiner wgrad: unsupported shape cin=%d cout=%d", cin, a.cout);
     size_t smem = L.total;
-    const size_t fl = smem_floor_for_tmem(tmem_cols(L.mtiles * a.cout));
+    const size_t fl = smem_floor_for_tmem(tmem_cols((int)L.tcols));
     if (smem < fl) smem = fl;
-    if (smem > 227 * 1024) return set_error(TDE_ERR_UNSUPPORTED, "refiner wgrad: %zu B of shared memory", smem);
-    TDE_TRY(allow_smem((const void *)wgrad_tc_kernel, smem, "refiner wgrad"));
+    if (smem > 227 * 1024 - 256) return set_error(TDE_ERR_UNSUPPORTED, "refiner wgrad: %zu B of shared memory", smem);
     wgrad_tc_kernel<<<blocks, kWgThreads, smem, s>>>(a);
     return check_launch("refiner wgrad");
 }
 
 int launch_wgrad_reduce(const float *partial, int blocks, int cin, int cout, float *dw, float *db, cudaStream_t s) {
     const WgLayout L = wg_layout(cin, cout);
-    const int n = (9 * cin + 1) * cout;
-    wgrad_reduce_kernel<<<div_up(n, 256), 256, 0, s>>>(partial, blocks, cin, cout, (size_t)L.mtiles * 128, dw, db);
+    const int n = cout * 9 * cin + cout;
+    wgrad_reduce_kernel<<<div_up(n, 256), 256, 0, s>>>(partial, blocks, cin, cout, L.mtiles, dw, db);
     return check_launch("refiner wgrad reduce");
 }
 
@@ -763,7 +899,10 @@ int conv_in_wgrad_blocks(int n, int h) { return div_up(n * h, kInRowsPerBlock); 
 
 int launch_conv_in_wgrad(const float *depth_m, const bf16 *dz1, int n, int h, int w, float *partial, int blocks,
                          float *dw1, float *db1, cudaStream_t s) {
-    conv_in_wgrad_kernel<<<blocks, 256, 0, s>>>(depth_m, dz1, n, h, w, partial);
+    const size_t rows_bytes = (size_t)3 * (w + 2) * sizeof(float);
+    if (rows_bytes + sizeof(float) * 16 * 16 * (kInK + 1) > 48 * 1024)
+        return set_error(TDE_ERR_UNSUPPORTED, "refiner: %d columns exceed the input-layer gradient kernel", w);
+    conv_in_wgrad_kernel<<<blocks, 256, rows_bytes, s>>>(depth_m, dz1, n, h, w, partial);
     TDE_TRY(check_launch("refiner conv_in wgrad"));
     conv_in_wgrad_reduce_kernel<<<div_up(kInPartial, 128), 128, 0, s>>>(partial, blocks, dw1, db1);
     return check_launch("refiner conv_in wgrad reduce");
@@ -782,7 +921,7 @@ int launch_loss(const float *out_m, const float *depth_m, const uint16_t *target
     loss_kernel<<<blocks, kLossThreads, 0, s>>>(out_m, depth_m, target, d0, head_w, np, 1.f / (float)np, dz11,
                                                 partial);
     TDE_TRY(check_launch("refiner loss"));
-    loss_reduce_kernel<<<1, 32, 0, s>>>(partial, blocks, dhead_w, dhead_b, loss2);
+    loss_reduce_kernel<<<19, 256, 0, s>>>(partial, blocks, dhead_w, dhead_b, loss2);
     return check_launch("refiner loss reduce");
 }
 

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/tde_pipeline.h"
+#include "../../include/tde_refiner.h"
 #include "tde_common.cuh"
 #include "tde_icp.cuh"
 #include "tde_integrate.cuh"
@@ -62,6 +63,18 @@ __global__ void finalize_kernel(IcpState *st, const PrevPose *prev, CamPose *cam
     out->inliers = st->inliers;
 }
 
+// Depth of the model surface along the camera axis, from the raycast
+// vertex map (volume frame) and the pose it was cast from; 0 where no hit.
+__global__ void model_depth_kernel(const float *__restrict__ vmap, const CamPose *__restrict__ cam, int n,
+                                   uint16_t *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float vx = vmap[3 * i], vy = vmap[3 * i + 1], vz = vmap[3 * i + 2];
+    float z = 0.f;
+    if (!isnan(vx)) z = cam->R[2] * (vx - cam->t[0]) + cam->R[5] * (vy - cam->t[1]) + cam->R[8] * (vz - cam->t[2]);
+    out[i] = z > 0.f ? (uint16_t)fminf(rintf(z * 1000.f), (float)TDE_MAX_DEPTH_VALUE) : (uint16_t)0;
+}
+
 enum Segment {
     SEG_PRE,         // bilateral filter, pyramid, vertex and normal maps, ICP setup
     SEG_ICP,         // the ICP iterations
@@ -103,6 +116,7 @@ struct tde_pipeline {
     void *iscratch = nullptr;     // integration: per-tile maximum depth + brick list
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     void *volume = nullptr;
+    tde_refiner *refiner = nullptr;  // replaces the bilateral filter when set
     // graphs: per segment and the whole frame
     cudaGraphExec_t seg_exec[SEG_COUNT] = {};
     cudaGraphExec_t full_exec[2] = {};  // [first frame, tracked frame]
@@ -126,8 +140,15 @@ int record_segment(tde_pipeline *p, Segment seg) {
     const int W = c.intr.cols, H = c.intr.rows;
     switch (seg) {
     case SEG_PRE: {
-        TDE_TRY(launch_bilateral(p->raw, p->depth[0], W, H, c.sigma_space, c.sigma_color, c.max_depth_mm, p->vcur[0],
-                                 &p->intr[0], s));
+        if (p->refiner) {
+            // learned refinement replaces the bilateral filter; ICP and
+            // integration both use the refined depth
+            TDE_TRY(tde_refiner_forward(p->refiner, p->raw, 1, p->depth[0], nullptr, s));
+            TDE_TRY(launch_vertex_map(p->depth[0], p->vcur[0], p->intr[0], s));
+        } else {
+            TDE_TRY(launch_bilateral(p->raw, p->depth[0], W, H, c.sigma_space, c.sigma_color, c.max_depth_mm,
+                                     p->vcur[0], &p->intr[0], s));
+        }
         for (int l = 1; l < p->levels; ++l)
             TDE_TRY(launch_pyramid(p->depth[l - 1], p->depth[l], p->intr[l - 1].cols, p->intr[l - 1].rows,
                                    c.sigma_color, p->vcur[l], &p->intr[l], s));
@@ -151,7 +172,7 @@ int record_segment(tde_pipeline *p, Segment seg) {
     case SEG_POST:
         finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_POST);
         TDE_TRY(check_launch("finalize_pose"));
-        TDE_TRY(launch_scale_depth(p->raw, p->scaled, p->intr[0], s));
+        TDE_TRY(launch_scale_depth(p->refiner ? p->depth[0] : p->raw, p->scaled, p->intr[0], s));
         return launch_depth_max(p->scaled, W, H, static_cast<float *>(p->iscratch), s);
     case SEG_INTEGRATE: {
         IntegrateParams P;
@@ -460,9 +481,11 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p) {
     if (!p) return 0;
     int icp = 0;
     for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
-    // bilateral, pyramid levels, normal maps, begin, ICP, finalize, scale,
-    // depth max, brick cull, integrate, raycast, 2 resizes per coarser level
-    return 1 + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
+    // bilateral (or the refiner's 11 convolutions + the level-0 vertex map),
+    // pyramid levels, normal maps, begin, ICP, finalize, scale, depth max,
+    // brick cull, integrate, raycast, 2 resizes per coarser level
+    const int pre = p->refiner ? 12 : 1;
+    return pre + (p->levels - 1) + p->levels + 1 + icp + 1 + 1 + 1 + 1 + 1 + 1 + 2 * (p->levels - 1);
 }
 
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {
@@ -472,6 +495,25 @@ int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {
         return set_error(TDE_ERR_INVALID_ARG, "pipeline_set_round_buffer: the volume resolution cannot change");
     TDE_TRY(tde_pipeline_sync(p));
     p->rb = *rb;
+    if (p->cfg.use_graphs) return capture_all(p);
+    return TDE_OK;
+}
+
+int tde_pipeline_model_depth(tde_pipeline *p, uint16_t *out) {
+    if (!p || !out) return set_error(TDE_ERR_INVALID_ARG, "pipeline_model_depth: null argument");
+    const int n = p->cfg.intr.cols * p->cfg.intr.rows;
+    model_depth_kernel<<<div_up(n, 256), 256, 0, p->stream>>>(p->vmod[0], p->cam, n, out);
+    return check_launch("pipeline_model_depth");
+}
+
+int tde_pipeline_set_refiner(tde_pipeline *p, tde_refiner *r) {
+    if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_set_refiner: null pipeline");
+    if (r) {
+        int st = tde_refiner_check_shape(r, p->cfg.intr.rows, p->cfg.intr.cols);
+        if (st != TDE_OK) return st;
+    }
+    TDE_TRY(tde_pipeline_sync(p));
+    p->refiner = r;
     if (p->cfg.use_graphs) return capture_all(p);
     return TDE_OK;
 }

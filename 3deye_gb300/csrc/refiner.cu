@@ -114,6 +114,7 @@ struct tde_refiner {
     bf16 *gr[GRAD_COUNT] = {};
     float *wpartial = nullptr;
     int wg_blocks = 0;
+    int fwd_per_sm[kConvs] = {}, bwd_per_sm[kConvs] = {};  // resident conv blocks per SM
     float *in_partial = nullptr;
     float *loss_partial = nullptr;
     double *loss2 = nullptr;
@@ -171,7 +172,7 @@ int forward(tde_refiner *r, const uint16_t *raw, int n, uint16_t *out_mm, cudaSt
             a.depth_out = r->out_m;
             a.depth_mm = out_mm;
         }
-        TDE_TRY(launch_conv(a, r->num_sms, s));
+        TDE_TRY(launch_conv(a, r->fwd_per_sm[i], r->num_sms, s));
     }
     r->last_batch = n;
     return TDE_OK;
@@ -204,7 +205,7 @@ int loss_grad(tde_refiner *r, const uint16_t *raw, const uint16_t *target, int n
         a.mask = k.mask >= 0 ? r->act[k.mask] : nullptr;
         a.n = n; a.h = h; a.w = w;
         a.err = r->err;
-        TDE_TRY(launch_conv(a, r->num_sms, s));
+        TDE_TRY(launch_conv(a, r->bwd_per_sm[i], r->num_sms, s));
         if (k.post == POST_UP)
             TDE_TRY(launch_up_back(r->gr[k.gx], cin, c.ca, r->act[c.a], r->gr[k.post_out], n, h, w, s));
         else if (k.post == POST_POOL)
@@ -236,6 +237,16 @@ int tde_refiner_create(int max_batch, int rows, int cols, uint64_t seed, tde_ref
         return set_error(TDE_ERR_CUDA, "refiner_create: no CUDA device");
     }
     r->wg_blocks = wgrad_blocks(r->num_sms, 0, 0);
+    st = prepare_kernels();
+    for (int i = 0; i < kConvs && !st; ++i) {
+        const int cin = kConv[i].ca + kConv[i].cb;
+        st = conv_blocks_per_sm(cin, kConv[i].cout, &r->fwd_per_sm[i]);
+        if (!st) st = conv_blocks_per_sm(kConv[i].cout, cin, &r->bwd_per_sm[i]);
+    }
+    if (st) {
+        delete r;
+        return st;
+    }
     size_t wpart = 0;
     for (int i = 0; i < kConvs; ++i) {
         const size_t f = wgrad_partial_floats(r->wg_blocks, kConv[i].ca + kConv[i].cb, kConv[i].cout);
@@ -394,6 +405,13 @@ int tde_refiner_get_tensor(tde_refiner *r, int id, void *host, size_t bytes) {
                                         : (const void *)r->gr[id - ACT_COUNT - 1];
     TDE_CUDA(cudaDeviceSynchronize(), "refiner_get_tensor");
     TDE_CUDA(cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost), "refiner_get_tensor");
+    return TDE_OK;
+}
+
+int tde_refiner_check_shape(tde_refiner *r, int rows, int cols) {
+    if (!r || r->rows != rows || r->cols != cols)
+        return set_error(TDE_ERR_INVALID_ARG, "refiner: created for %dx%d, used for %dx%d", r ? r->cols : 0,
+                         r ? r->rows : 0, cols, rows);
     return TDE_OK;
 }
 

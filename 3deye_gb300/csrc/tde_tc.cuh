@@ -3,9 +3,10 @@
 // an FP32 accumulator in tensor memory (TMEM), TMEM allocation and loads,
 // and bounded mbarrier waits.
 //
-// Operand layout used throughout (no swizzle, K-major): a "core matrix" is 8
-// rows of 16 contiguous bytes (8 bf16 along K), 128 bytes in all.  A
-// descriptor names the first core matrix and two strides:
+// Operand layouts used here have no swizzle.  A "core matrix" is 8 rows of 16
+// contiguous bytes, 128 bytes in all: for a K-major operand each row holds 8
+// bf16 along K, for an MN-major operand 8 bf16 along M (or N) of one k.  A
+// descriptor names the first core matrix and two strides, in both cases:
 //   LBO -- bytes between core matrices adjacent along K,
 //   SBO -- bytes between core matrices adjacent along M (or N).
 // One kind::f16 MMA consumes K = 16 (two core matrices along K).

@@ -35,6 +35,8 @@ declare("tde_pipeline_stage_timings", I, [P, P, I])
 declare("tde_pipeline_launches_per_frame", I, [P])
 declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
 declare("tde_pipeline_set_pose", I, [P, P])
+declare("tde_pipeline_set_refiner", I, [P, P])
+declare("tde_pipeline_model_depth", I, [P, P])
 
 
 def config_from(cfg, use_graphs=True, integrate_stats=False, levels=3) -> PipelineConfig:
@@ -157,6 +159,15 @@ class Pipeline:
     def set_pose(self, pose12):
         p = np.ascontiguousarray(pose12, np.float64)
         check(lib.tde_pipeline_set_pose(self._h, p.ctypes.data_as(P)))
+
+    def set_refiner(self, refiner):
+        """Learned refinement instead of the bilateral filter (None restores it)."""
+        self._refiner = refiner  # keeps it alive while the pipeline uses it
+        check(lib.tde_pipeline_set_refiner(self._h, refiner.handle if refiner is not None else None))
+
+    def model_depth(self, out_ptr: int):
+        """Enqueue: the last frame's model surface as depth in mm (device uint16)."""
+        check(lib.tde_pipeline_model_depth(self._h, out_ptr))
 
 
 def ate_rmse(est: np.ndarray, gt: np.ndarray, align: bool = False) -> float:

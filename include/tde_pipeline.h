@@ -23,6 +23,7 @@ extern "C" {
 #endif
 
 typedef struct tde_pipeline tde_pipeline;
+struct tde_refiner;
 
 typedef struct tde_pipeline_config {
     tde_intrinsics intr;         /* level-0 camera */
@@ -97,6 +98,18 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p);
 /* Replace the volume origin bookkeeping after a cyclic shift (the caller has
  * extracted and cleaned the outgoing slab); re-captures the graphs. */
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb);
+/* Enqueues on the pipeline's stream: the model surface of the last frame
+ * (its raycast, at the pose it was tracked to) as depth along the camera axis
+ * in mm, 0 where the ray found no surface -- the target of the learned
+ * refiner's training pairs.  `out` is device memory of rows x cols. */
+int tde_pipeline_model_depth(tde_pipeline *p, uint16_t *out);
+
+/* Replaces the bilateral stage with the learned refiner (include/tde_refiner.h)
+ * for the following frames; NULL restores the bilateral filter.  The refiner
+ * must have been created for the pipeline's rows x cols and must outlive its
+ * use here; refined depth feeds both ICP and integration. */
+int tde_pipeline_set_refiner(tde_pipeline *p, struct tde_refiner *r);
+
 /* Overwrite the current pose (e.g. after a shift of the volume frame). */
 int tde_pipeline_set_pose(tde_pipeline *p, const double *pose12);
 

@@ -71,7 +71,10 @@ int tde_refiner_last_loss(tde_refiner *r, double *loss, double *valid_pixels);
 int tde_refiner_get_tensor(tde_refiner *r, int id, void *host, size_t bytes);
 size_t tde_refiner_tensor_bytes(tde_refiner *r, int id);
 
-/* Device-side status: TDE_ERR_TIMEOUT once a tensor-core wait gave up. */
+/* TDE_OK when the refiner was created for rows x cols, else TDE_ERR_INVALID_ARG. */
+int tde_refiner_check_shape(tde_refiner *r, int rows, int cols);
+
+/* Device-side status: TDE_ERR_DEVICE_TIMEOUT once a tensor-core wait gave up. */
 int tde_refiner_status(tde_refiner *r);
 
 #ifdef __cplusplus

@@ -150,3 +150,44 @@ def test_training_reduces_error_against_ground_truth(cuda, rf):
     err_ref = np.abs(out_m[m] - gt[m] / 1000.0).mean()
     assert err_ref < 0.8 * err_raw, (err_ref, err_raw)
     R.close()
+
+
+def test_pipeline_with_identity_refiner(cuda, rf):
+    """The refiner in place of the bilateral stage: an untrained refiner (zero
+    head) is the identity on valid depth, so the pipeline's level-0 depth is
+    the raw frame, tracking still follows the ground truth, and the frame
+    runs 11 more kernels (the refiner's convolutions and the vertex map
+    instead of the fused bilateral kernel)."""
+    import ctypes as C
+    from oracle import oracle as orc
+    tde = importlib.import_module("3deye_gb300")
+    syn = importlib.import_module("3deye_gb300.synth")
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg = syn.small_config("c1", frames=10, cols=160, rows=120, voxels=96, fmt=1)
+    scene = syn.make_scene(cfg, 1000)
+    traj = syn.make_trajectory(cfg, 2000)
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    depths = [orc.apply_noise(orc.render_depth(scene, traj[i], intr), 3000, i) for i in range(cfg.frames)]
+    plain = pl.Pipeline(cfg, traj[0])
+    n_plain = plain.launches_per_frame()
+    plain.close()
+    R = rf.Refiner(1, cfg.rows, cfg.cols, seed=1)
+    p = pl.Pipeline(cfg, traj[0])
+    p.set_refiner(R)
+    assert p.launches_per_frame() == n_plain + 11
+    poses = []
+    for d in depths:
+        pose, st = p.process(d)
+        assert st == 0
+        poses.append(pose)
+        dptr, _, _ = p.frame_maps(0)
+        got = np.zeros((cfg.rows, cfg.cols), np.uint16)
+        tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        tde.check(tde.lib.tde_memcpy(got.ctypes.data_as(C.c_void_p), dptr, got.nbytes, 1))
+        assert np.array_equal(got, d)
+    assert pl.ate_rmse(np.array(poses), traj[:cfg.frames]) < 0.02
+    assert R.status() == 0
+    p.set_refiner(None)
+    assert p.launches_per_frame() == n_plain
+    p.close()
+    R.close()
