@@ -137,6 +137,41 @@ __device__ __forceinline__ void load_row(const ConvArgs &A, unsigned char *slot,
     }
 }
 
+// Address of chunk c of the concatenated input at (img, y, x) for a source
+// that needs no arithmetic (direct or nearest-upsampled A, or B); null
+// outside the image.
+template <int MODE>
+__device__ __forceinline__ const bf16 *chunk_ptr(const ConvArgs &A, int img, int y, int x, int c) {
+    if (y < 0 || y >= A.h || x < 0 || x >= A.w) return nullptr;
+    const int cca = A.ca >> 3;
+    if (c < cca) {
+        if (MODE == SRC_UP) {
+            const int hh = A.h >> 1, ww = A.w >> 1;
+            return A.a + (((size_t)img * hh + (y >> 1)) * ww + (x >> 1)) * A.ca + 8 * c;
+        }
+        return A.a + (((size_t)img * A.h + y) * A.w + x) * A.ca + 8 * c;
+    }
+    return A.b + (((size_t)img * A.h + y) * A.w + x) * A.cb + 8 * (c - cca);
+}
+
+// Starts the copies of one input row into a slot with cp.async (16 B each,
+// zero-filled outside the image); completed by cp.async.wait_all.
+template <int MODE>
+__device__ __forceinline__ void load_row_async(const ConvArgs &A, unsigned char *slot, int cc, int img, int y, int x0,
+                                               int tid) {
+    const int n = kHaloW * cc;
+    for (int i = tid; i < n; i += kConvThreads) {
+        const int c = i % cc, px = i / cc;
+        const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
+        const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
+        const int bytes = src ? 16 : 0;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src ? src : A.a), "r"(bytes)
+                     : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void wait_async_rows() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, int warp, int lane, int img, int y,
                                               int x0) {
     const int m = warp * 32 + lane;
@@ -198,11 +233,15 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     unsigned char *wsm = smem + kSlots * slot_bytes;
     const uint32_t ncols = tmem_cols(A.cout);
 
+    // the next layer may start its prologue; it waits for this grid before
+    // reading anything this one writes
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
     if (tid == 0) {
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
     }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B
     const int nw = A.cout * 9 * cc;
     for (int i = tid; i < nw; i += kConvThreads) {
@@ -228,8 +267,12 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         const int x0 = xt * kTileM;
         const int y0 = ch * rows_per_item;
         const int y1 = min(A.h, y0 + rows_per_item);
-        for (int dy = -1; dy <= 1; ++dy)
-            load_row<MODE>(A, halo + (size_t)((y0 + dy + kSlots) % kSlots) * slot_bytes, cc, img, y0 + dy, x0, tid);
+        for (int dy = -1; dy <= 1; ++dy) {
+            unsigned char *slot = halo + (size_t)((y0 + dy + kSlots) % kSlots) * slot_bytes;
+            if (MODE == SRC_POOL) load_row<MODE>(A, slot, cc, img, y0 + dy, x0, tid);
+            else load_row_async<MODE>(A, slot, cc, img, y0 + dy, x0, tid);
+        }
+        if (MODE != SRC_POOL) wait_async_rows();
         tc::fence_proxy_async();
         __syncthreads();
         for (int y = y0; y < y1; ++y, ++g) {
@@ -259,10 +302,15 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
                     break;
                 }
                 tc::fence_after_sync();
-                conv_epilogue(A, tmem + (gp & 1u) * ncols, warp, lane, img, y - 1, x0);
             }
-            if (y + 1 < y1)
-                load_row<MODE>(A, halo + (size_t)((y + 2) % kSlots) * slot_bytes, cc, img, y + 2, x0, tid);
+            unsigned char *next = halo + (size_t)((y + 2) % kSlots) * slot_bytes;
+            // the copies of row y+2 run while row y-1 is drained
+            if (MODE != SRC_POOL && y + 1 < y1) load_row_async<MODE>(A, next, cc, img, y + 2, x0, tid);
+            if (y > y0) conv_epilogue(A, tmem + ((g - 1) & 1u) * ncols, warp, lane, img, y - 1, x0);
+            if (y + 1 < y1) {
+                if (MODE == SRC_POOL) load_row<MODE>(A, next, cc, img, y + 2, x0, tid);
+                else wait_async_rows();
+            }
             tc::fence_proxy_async();
             tc::fence_before_sync();
             __syncthreads();
@@ -851,9 +899,21 @@ int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t 
     rows = rows < 1 ? 1 : rows > 64 ? 64 : rows;
     const long items = (long)a.n * tiles_x * ((a.h + rows - 1) / rows);
     const int grid = (int)(items < slots ? items : slots);
-    if (a.mode_a == SRC_POOL) conv3x3_tc_kernel<SRC_POOL><<<grid, kConvThreads, smem, s>>>(a, rows);
-    else if (a.mode_a == SRC_UP) conv3x3_tc_kernel<SRC_UP><<<grid, kConvThreads, smem, s>>>(a, rows);
-    else conv3x3_tc_kernel<SRC_DIRECT><<<grid, kConvThreads, smem, s>>>(a, rows);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kConvThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e;
+    if (a.mode_a == SRC_POOL) e = cudaLaunchKernelEx(&cfg, conv3x3_tc_kernel<SRC_POOL>, a, rows);
+    else if (a.mode_a == SRC_UP) e = cudaLaunchKernelEx(&cfg, conv3x3_tc_kernel<SRC_UP>, a, rows);
+    else e = cudaLaunchKernelEx(&cfg, conv3x3_tc_kernel<SRC_DIRECT>, a, rows);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "refiner conv: %s", cudaGetErrorString(e));
     return check_launch("refiner conv");
 }
 

@@ -117,6 +117,14 @@ struct tde_pipeline {
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     void *volume = nullptr;
     tde_refiner *refiner = nullptr;  // replaces the bilateral filter when set
+    int icp_blocks = 0;              // > 0: all ICP iterations of a frame in one cooperative launch
+    // volume shifts: extraction scratch and point buffers, grown on demand
+    void *slab_scratch = nullptr;
+    size_t slab_scratch_bytes = 0;
+    tde_xyzi *slab_points = nullptr;
+    float *slab_weights = nullptr;
+    uint32_t slab_capacity = 0;
+    uint32_t *slab_count = nullptr;
     // graphs: per segment and the whole frame
     cudaGraphExec_t seg_exec[SEG_COUNT] = {};
     cudaGraphExec_t full_exec[2] = {};  // [first frame, tracked frame]
@@ -158,6 +166,20 @@ int record_segment(tde_pipeline *p, Segment seg) {
         return check_launch("begin_frame");
     }
     case SEG_ICP:
+        if (p->icp_blocks > 0) {
+            IcpFrameArgs F;
+            std::memset(&F, 0, sizeof(F));
+            F.levels = p->levels;
+            for (int l = 0; l < p->levels; ++l) {
+                IcpArgs &a = F.lv[l];
+                a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
+                a.W = p->intr[l].cols; a.H = p->intr[l].rows;
+                a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
+                a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
+                F.iters[l] = c.icp_iters[l];
+            }
+            return launch_icp_frame(F, p->st, p->icp_blocks, s);
+        }
         for (int l = p->levels - 1; l >= 0; --l) {
             IcpArgs a;
             a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
@@ -268,6 +290,7 @@ void release(tde_pipeline *p) {
     }
     cudaFree(p->scaled); cudaFree(p->gbuf); cudaFree(p->st); cudaFree(p->prev); cudaFree(p->cam); cudaFree(p->out);
     cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->iscratch); cudaFree(p->negflags);
+    cudaFree(p->slab_scratch); cudaFree(p->slab_points); cudaFree(p->slab_weights); cudaFree(p->slab_count);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -294,6 +317,12 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     if (!p) return set_error(TDE_ERR_OOM, "pipeline_create: host allocation");
     p->cfg = c;
     p->levels = c.icp_levels;
+    {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            p->icp_blocks = icp_frame_blocks(c.intr.cols, c.intr.rows, sms);
+    }
     int st = tde_round_buffer_init(&p->rb, c.voxels, c.volume_size);
     if (st == TDE_OK && !valid_round_buffer(&p->rb)) st = set_error(TDE_ERR_INVALID_ARG, "pipeline_create: volume size");
     if (st != TDE_OK) { delete p; return st; }
@@ -481,6 +510,7 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p) {
     if (!p) return 0;
     int icp = 0;
     for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
+    if (p->icp_blocks > 0) icp = 1;  // one cooperative launch for every iteration
     // bilateral (or the refiner's 11 convolutions + the level-0 vertex map),
     // pyramid levels, normal maps, begin, ICP, finalize, scale, depth max,
     // brick cull, integrate, raycast, 2 resizes per coarser level
@@ -514,6 +544,110 @@ int tde_pipeline_set_refiner(tde_pipeline *p, tde_refiner *r) {
     }
     TDE_TRY(tde_pipeline_sync(p));
     p->refiner = r;
+    if (p->cfg.use_graphs) return capture_all(p);
+    return TDE_OK;
+}
+
+int tde_pipeline_shift_needed(tde_pipeline *p, float radius_m, int *delta3) {
+    if (!p || !delta3 || !(radius_m >= 0.f)) return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift_needed: bad argument");
+    double pose[12];
+    TDE_TRY(tde_pipeline_pose(p, pose));
+    const float *vs = &p->rb.volume_size.x;
+    const float *cs = &p->cell.x;
+    for (int a = 0; a < 3; ++a) {
+        const double off = pose[9 + a] - 0.5 * vs[a];
+        delta3[a] = std::fabs(off) > radius_m ? (int)std::lround(off / cs[a]) : 0;
+    }
+    return TDE_OK;
+}
+
+int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, uint32_t capacity,
+                       uint32_t *count) {
+    if (!p || !delta3 || !count || (capacity && !points))
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift: bad argument");
+    const int *N = &p->rb.voxels_size.x;
+    for (int a = 0; a < 3; ++a)
+        if (delta3[a] <= -N[a] || delta3[a] >= N[a])
+            return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift: |delta| must be below the volume size");
+    TDE_TRY(tde_pipeline_sync(p));
+    cudaStream_t s = p->stream;
+    // the slab leaving the volume, in the black-zone coordinates of
+    // scan_slice_of_both_volumes.cl:63-74 (logical voxel + origin_GRID); an
+    // axis without a shift gets an empty range
+    tde_point3i mn, mx;
+    int *pmn = &mn.x, *pmx = &mx.x;
+    const int *org = &p->rb.origin_GRID.x;
+    for (int a = 0; a < 3; ++a) {
+        if (delta3[a] > 0) { pmn[a] = org[a]; pmx[a] = org[a] + delta3[a] - 1; }
+        else if (delta3[a] < 0) { pmn[a] = org[a] + N[a] + delta3[a]; pmx[a] = org[a] + N[a] - 1; }
+        else { pmn[a] = 1 << 30; pmx[a] = -(1 << 30); }
+    }
+    const size_t need = tde_extract_slice_scratch_bytes(&p->rb);
+    if (need > p->slab_scratch_bytes) {
+        cudaFree(p->slab_scratch);
+        p->slab_scratch = nullptr;
+        TDE_CUDA(cudaMalloc(&p->slab_scratch, need), "pipeline_shift: scratch");
+        p->slab_scratch_bytes = need;
+    }
+    if (!p->slab_count) TDE_CUDA(cudaMalloc((void **)&p->slab_count, sizeof(uint32_t)), "pipeline_shift: count");
+    for (int pass = 0; pass < 2; ++pass) {
+        TDE_TRY(tde_extract_slice(p->volume, p->cfg.tsdf_format, nullptr, mn, mx, &p->rb, p->slab_scratch,
+                                  p->slab_scratch_bytes, p->slab_points, nullptr, p->slab_weights, p->slab_capacity,
+                                  p->slab_count, s));
+        uint32_t n = 0;
+        TDE_CUDA(cudaMemcpyAsync(&n, p->slab_count, sizeof(n), cudaMemcpyDeviceToHost, s), "pipeline_shift: count");
+        TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift: count");
+        if (n <= p->slab_capacity) {
+            *count = n;
+            break;
+        }
+        cudaFree(p->slab_points);
+        cudaFree(p->slab_weights);
+        p->slab_points = nullptr;
+        p->slab_weights = nullptr;
+        const uint32_t cap = n + n / 4 + 1024;
+        TDE_CUDA(cudaMalloc((void **)&p->slab_points, (size_t)cap * sizeof(tde_xyzi)), "pipeline_shift: points");
+        TDE_CUDA(cudaMalloc((void **)&p->slab_weights, (size_t)cap * sizeof(float)), "pipeline_shift: weights");
+        p->slab_capacity = cap;
+    }
+    const uint32_t ncopy = *count < capacity ? *count : capacity;
+    if (ncopy) {
+        TDE_CUDA(cudaMemcpy(points, p->slab_points, (size_t)ncopy * sizeof(tde_xyzi), cudaMemcpyDeviceToHost),
+                 "pipeline_shift: points");
+        if (weights)
+            TDE_CUDA(cudaMemcpy(weights, p->slab_weights, (size_t)ncopy * sizeof(float), cudaMemcpyDeviceToHost),
+                     "pipeline_shift: weights");
+    }
+    TDE_TRY(tde_clean_tsdf_slice(p->volume, p->cfg.tsdf_format, mn, mx, &p->rb, s));
+    // brick flags only ever over-approximate; after cleaning, the cleared
+    // voxels hold 0 >= 0 so stale flags stay conservative
+    // advance the round buffer (round_buffer.h:25-63 fields)
+    int *ogrid = &p->rb.origin_GRID.x;
+    float *oglob = &p->rb.origin_GRID_global.x, *ometric = &p->rb.origin_metric.x;
+    const float *cs = &p->cell.x;
+    for (int a = 0; a < 3; ++a) {
+        ogrid[a] = ((ogrid[a] + delta3[a]) % N[a] + N[a]) % N[a];
+        oglob[a] += (float)delta3[a];
+        ometric[a] += (float)delta3[a] * cs[a];
+    }
+    // the pose moves into the new volume frame; the model maps are cast again
+    double pose[12];
+    TDE_TRY(tde_pipeline_pose(p, pose));
+    for (int a = 0; a < 3; ++a) pose[9 + a] -= (double)delta3[a] * cs[a];
+    TDE_TRY(write_pose(p, pose));
+    CamPose cam;
+    std::memset(&cam, 0, sizeof(cam));
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            cam.R[3 * r + c] = (float)pose[3 * r + c];
+            cam.R_inv[3 * r + c] = (float)pose[3 * c + r];
+        }
+    for (int a = 0; a < 3; ++a) cam.t[a] = (float)pose[9 + a];
+    cam.tracking_ok = 1;
+    TDE_CUDA(cudaMemcpyAsync(p->cam, &cam, sizeof(cam), cudaMemcpyHostToDevice, s), "pipeline_shift: camera");
+    TDE_TRY(record_segment(p, SEG_RAYCAST));
+    TDE_TRY(record_segment(p, SEG_RESIZE));
+    TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift");
     if (p->cfg.use_graphs) return capture_all(p);
     return TDE_OK;
 }

@@ -2,20 +2,22 @@
 itself, training with the library's own kernels, and evaluation against the
 plain bilateral pipeline on held-out sequences.
 
-Pairs: every frame of a sequence run through the plain pipeline gives
-(raw noisy depth, model depth) -- the raycast of the fused volume at the pose
-the frame was tracked to (tde_pipeline_model_depth).  Evaluation: the same
+Pairs: every frame of a sequence run through the pipeline gives (raw noisy
+depth, model depth) -- the raycast of the fused volume (tde_pipeline_model_depth).
+Fusion and raycast run at the ground-truth poses of the synthetic sequence
+(tracking off), so the targets carry no tracking error.  Evaluation: the same
 held-out sequences through the plain and the learned pipeline; ATE against the
 ground-truth trajectory, and surface error of the final volume raycast at
 ground-truth poses against the noise-free rendered depth.
 
-    python -m 3deye_gb300.learned --scenes 40 --frames 500 --steps 3000 \\
+    python -m 3deye_gb300.learned --scenes 40 --frames 500 --steps 6000 \\
         --eval-seqs 5 --eval-frames 600 --out weights.f32 --report report.json
 """
 from __future__ import annotations
 
 import argparse
 import ctypes as C
+import dataclasses
 import importlib
 import json
 import time
@@ -60,31 +62,59 @@ def render_sequence(cfg, k, nframes, noise_free=False):
     return frames, traj, d_scene, clean
 
 
+SKIP_FRAMES = 50        # the model of a sequence's first frames is still thin: no pairs from them
+OUTLIER_MM = 30         # target pixels this far from the raw depth become the raw depth (edges, disocclusions)
+
+
 def generate_pairs(cfg, scenes, frames_per_scene, seed0=TRAIN_SEED0, log=print):
-    """Training pairs (raw, model depth) in mm as device int16 tensors [N,H,W]."""
+    """Training pairs (raw, model depth) in mm as device int16 tensors [N,H,W].
+    Each scene runs SKIP_FRAMES + frames_per_scene frames; target pixels with
+    no model surface or more than OUTLIER_MM from the raw depth take the raw
+    depth."""
     import torch
     n = scenes * frames_per_scene
     # int16 storage (values <= 32767): the same bits, and every torch op on it
     raw = torch.empty((n, cfg.rows, cfg.cols), dtype=torch.int16, device="cuda")
     tgt = torch.empty_like(raw)
     t0 = time.time()
+    total = SKIP_FRAMES + frames_per_scene
+    scratch = torch.empty((cfg.rows, cfg.cols), dtype=torch.int16, device="cuda")
+    # fusion and raycast at the ground-truth poses (tracking off: 0 ICP
+    # iterations), so that tracking error does not leak into the targets
+    fuse_cfg = dataclasses.replace(cfg, icp_iters=(0, 0, 0))
     for s in range(scenes):
-        frames, traj, _, _ = render_sequence(cfg, seed0 + s, frames_per_scene)
-        p = pl.Pipeline(cfg, traj[0], use_graphs=True)
+        frames, traj, _, _ = render_sequence(cfg, seed0 + s, total)
+        p = pl.Pipeline(fuse_cfg, traj[0], use_graphs=True)
         base = frames.data_ptr()
         fb = cfg.rows * cfg.cols * 2
-        for i in range(frames_per_scene):
-            j = s * frames_per_scene + i
+        for i in range(total):
+            p.set_pose(traj[i])
             p.enqueue(base + i * fb, True)
-            p.model_depth(tgt[j].data_ptr())
+            j = s * frames_per_scene + i - SKIP_FRAMES
+            p.model_depth(tgt[j].data_ptr() if j >= s * frames_per_scene else scratch.data_ptr())
         p.sync()
-        raw[s * frames_per_scene:(s + 1) * frames_per_scene].copy_(frames.view(torch.int16))
+        raw[s * frames_per_scene:(s + 1) * frames_per_scene].copy_(frames[SKIP_FRAMES:].view(torch.int16))
         p.close()
         del frames
         if log and (s + 1) % 10 == 0:
             log(f"pairs: {s + 1}/{scenes} scenes, {time.time() - t0:.1f} s")
+    # where the model has no surface, or one far from the raw depth (depth
+    # edges, disocclusions), the target is the raw depth itself: the refiner
+    # learns to leave such pixels alone
+    r32, t32 = raw.to(torch.int32), tgt.to(torch.int32)
+    keep = (r32 > 0) & ((t32 == 0) | ((t32 - r32).abs() > OUTLIER_MM))
+    tgt.copy_(torch.where(keep, raw, tgt))
+    del r32, t32, keep
     torch.cuda.synchronize()
     return raw, tgt
+
+
+def lr_at(step, steps, lr, warmup=100, floor=0.01):
+    """Linear warm-up, then cosine decay to floor * lr."""
+    if step < warmup:
+        return lr * (step + 1) / warmup
+    u = (step - warmup) / max(1, steps - warmup)
+    return lr * (floor + (1.0 - floor) * 0.5 * (1.0 + np.cos(np.pi * u)))
 
 
 def train(refiner, raw, tgt, steps, batch, lr, seed=0, log=print, log_every=250):
@@ -100,7 +130,7 @@ def train(refiner, raw, tgt, steps, batch, lr, seed=0, log=print, log_every=250)
         idx = torch.from_numpy(rng.integers(0, n, batch)).cuda()
         torch.index_select(raw, 0, idx, out=braw)
         torch.index_select(tgt, 0, idx, out=btgt)
-        refiner.train_step_ptr(braw.data_ptr(), btgt.data_ptr(), batch, lr,
+        refiner.train_step_ptr(braw.data_ptr(), btgt.data_ptr(), batch, lr_at(it, steps, lr),
                                torch.cuda.current_stream().cuda_stream)
         if (it + 1) % 50 == 0 or it == 0:
             loss, cnt = refiner.last_loss()
@@ -194,7 +224,7 @@ def main(argv=None):
     ap.add_argument("--config", default="c2")
     ap.add_argument("--scenes", type=int, default=40)
     ap.add_argument("--frames", type=int, default=500)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)

@@ -37,6 +37,8 @@ declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
 declare("tde_pipeline_set_pose", I, [P, P])
 declare("tde_pipeline_set_refiner", I, [P, P])
 declare("tde_pipeline_model_depth", I, [P, P])
+declare("tde_pipeline_shift_needed", I, [P, F, P])
+declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 
 
 def config_from(cfg, use_graphs=True, integrate_stats=False, levels=3) -> PipelineConfig:
@@ -164,6 +166,24 @@ class Pipeline:
         """Learned refinement instead of the bilateral filter (None restores it)."""
         self._refiner = refiner  # keeps it alive while the pipeline uses it
         check(lib.tde_pipeline_set_refiner(self._h, refiner.handle if refiner is not None else None))
+
+    def shift_needed(self, radius_m: float) -> np.ndarray:
+        """Voxel shift that re-centres the volume (zeros while the camera is within radius_m)."""
+        d = np.zeros(3, np.int32)
+        check(lib.tde_pipeline_shift_needed(self._h, radius_m, d.ctypes.data_as(P)))
+        return d
+
+    def shift(self, delta, capacity: int = 1 << 22):
+        """Shift the volume by delta voxels; returns the outgoing slab's points
+        [n,4] (logical voxel units before the shift) and their weights."""
+        d = np.ascontiguousarray(delta, np.int32)
+        pts = np.zeros((capacity, 4), np.float32)
+        w = np.zeros(capacity, np.float32)
+        n = C.c_uint32()
+        check(lib.tde_pipeline_shift(self._h, d.ctypes.data_as(P), pts.ctypes.data_as(P), w.ctypes.data_as(P),
+                                     capacity, C.byref(n)))
+        k = min(n.value, capacity)
+        return pts[:k], w[:k], n.value
 
     def model_depth(self, out_ptr: int):
         """Enqueue: the last frame's model surface as depth in mm (device uint16)."""

@@ -59,6 +59,9 @@ CONFIGS = {
     # 600 x 640x480, 512^3 FP16+u16 over 3 m
     "c2": Config("c2-640x480-512^3-fp16", 600, 640, 480, 525.0, 525.0, 319.5, 239.5, 512, 3.0, 1,
                  0.03, 4.5, 30.0, scene_cube_m=3.0),
+    # 600 x 640x480 along a 12 m corridor, 512^3 FP16+u16 over 3 m following the camera
+    "c3": Config("c3-640x480-512^3-corridor", 600, 640, 480, 525.0, 525.0, 319.5, 239.5, 512, 3.0, 1,
+                 0.03, 4.5, 30.0, scene_cube_m=3.0),
     # 300 x 640x480 of the c1 scene, 1024^3 over 4 m (precision study)
     "c4": Config("c4-640x480-1024^3", 300, 640, 480, 525.0, 525.0, 319.5, 239.5, 1024, 4.0, 1,
                  3 * 4.0 / 1024, 4.5, 30.0, scene_cube_m=2.0),
@@ -135,6 +138,64 @@ def make_trajectory(cfg: Config, seed: int, frames: int | None = None) -> np.nda
     for i in range(n):
         R = look_at(eye[i], tgt[i])
         out[i, :9] = R.ravel()
+        out[i, 9:] = eye[i]
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Corridor (cyclic-volume workload): the camera travels `length` metres along
+# +z through a tiled corridor while the volume follows it.
+# ---------------------------------------------------------------------------
+CORRIDOR_HALF_WIDTH = 1.1   # walls at x = V/2 +- this
+CORRIDOR_FLOOR = 1.2        # floor this far below the camera line (y down)
+CORRIDOR_CEILING = 1.0      # ceiling this far above it
+
+
+def make_corridor_scene(cfg: Config, seed: int, length: float = 12.0) -> np.ndarray:
+    """Floor, ceiling and two walls (planes) plus a random box every 0.5 m,
+    alternating walls, from behind the start to beyond the end of the walk."""
+    rng = np.random.default_rng(seed)
+    c = cfg.volume_m / 2.0
+    y_floor, y_ceil = c + CORRIDOR_FLOOR, c - CORRIDOR_CEILING
+    xl, xr = c - CORRIDOR_HALF_WIDTH, c + CORRIDOR_HALF_WIDTH
+    prims = [[0, 0.0, 1.0, 0.0, -y_floor, 0, 0, 0], [0, 0.0, 1.0, 0.0, -y_ceil, 0, 0, 0],
+             [0, 1.0, 0.0, 0.0, -xl, 0, 0, 0], [0, 1.0, 0.0, 0.0, -xr, 0, 0, 0]]
+    z = c - 1.5
+    side = 1
+    while z < c + length + 4.5:
+        w, h, d = rng.uniform(0.2, 0.5, size=3)
+        zz = z + rng.uniform(-0.1, 0.1)
+        if side > 0:
+            x0, x1 = xr - w, xr
+        else:
+            x0, x1 = xl, xl + w
+        if rng.uniform() < 0.6:      # on the floor
+            y0, y1 = y_floor - h, y_floor
+        else:                        # on the wall, at some height
+            ym = rng.uniform(y_ceil + 0.3, y_floor - 0.3)
+            y0, y1 = ym - h / 2, ym + h / 2
+        prims.append([2, x0, y0, zz - d / 2, x1, y1, zz + d / 2, 0])
+        side = -side
+        z += 0.5
+    return np.asarray(prims, dtype=np.float64)
+
+
+def make_corridor_trajectory(cfg: Config, seed: int, frames: int | None = None, length: float = 12.0) -> np.ndarray:
+    """Walk along +z from the volume centre over `length` metres (<= 2 cm per
+    frame for 600 frames), with slow lateral / vertical sway and a gently
+    wandering gaze ahead.  Returns (frames, 12) float64: R row-major, t."""
+    n = cfg.frames if frames is None else frames
+    rng = np.random.default_rng(seed)
+    c = cfg.volume_m / 2.0
+    k = np.arange(n, dtype=np.float64)
+    ph = rng.uniform(0, 2 * np.pi, size=6)
+    fr = rng.uniform(0.01, 0.03, size=6)
+    zc = c + length * k / max(n - 1, 1)
+    eye = np.stack([c + 0.15 * np.sin(fr[0] * k + ph[0]), c + 0.08 * np.sin(fr[1] * k + ph[1]), zc], axis=1)
+    tgt = np.stack([c + 0.4 * np.sin(fr[2] * k + ph[2]), c + 0.3 + 0.15 * np.sin(fr[3] * k + ph[3]), zc + 2.0], axis=1)
+    out = np.empty((n, 12), np.float64)
+    for i in range(n):
+        out[i, :9] = look_at(eye[i], tgt[i]).ravel()
         out[i, 9:] = eye[i]
     return out
 

@@ -98,6 +98,23 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p);
 /* Replace the volume origin bookkeeping after a cyclic shift (the caller has
  * extracted and cleaned the outgoing slab); re-captures the graphs. */
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb);
+/* Cyclic volume (config: a volume following the camera).  The shift, in
+ * voxels per axis, that re-centres the volume on the camera when the camera
+ * is more than radius_m from the volume centre along an axis, else 0. */
+int tde_pipeline_shift_needed(tde_pipeline *p, float radius_m, int *delta3);
+
+/* Shifts the volume by delta3 voxels (|delta| below the voxel count per
+ * axis), host-synchronous: the slab that leaves the volume is extracted as
+ * zero-crossing points (tde_extract_slice semantics and order: logical voxel
+ * units of the volume before the shift; `weights` the named voxels' weights,
+ * may be NULL) into host `points` up to `capacity` (the total goes to
+ * *count), the slab is cleaned, the round buffer's origins advance
+ * cyclically, the tracked pose moves into the new volume frame
+ * (t -= delta * cell) and the model maps are cast again from it.  World
+ * position of a point = origin_metric (before the shift) + point * cell. */
+int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, uint32_t capacity,
+                       uint32_t *count);
+
 /* Enqueues on the pipeline's stream: the model surface of the last frame
  * (its raycast, at the pose it was tracked to) as depth along the camera axis
  * in mm, 0 where the ray found no surface -- the target of the learned

@@ -1,0 +1,78 @@
+"""Cyclic volume following the camera along a corridor (the volume-shift
+path): the slab leaving the volume is extracted bit-exactly as the oracle
+extracts it from the same TSDF, the slab is cleaned, the round buffer's
+origins advance, and tracking continues in the shifted volume."""
+import ctypes as C
+import dataclasses
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+syn = importlib.import_module("3deye_gb300.synth")
+
+
+def v3(pt):
+    return np.array([pt.x, pt.y, pt.z])
+
+
+def download(tde, ptr, nbytes):
+    out = np.zeros(nbytes, np.uint8)
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    tde.check(tde.lib.tde_memcpy(out.ctypes.data_as(C.c_void_p), ptr, nbytes, 1))
+    return out
+
+
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_corridor_shifts_extract_bit_exact(cuda, orc, tde, fmt):
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    base = syn.small_config("c1", frames=150, cols=160, rows=120, voxels=128, fmt=fmt)
+    cfg = dataclasses.replace(base, volume_m=3.0, trunc_m=0.07, scene_cube_m=3.0)
+    length = 3.0
+    scene = syn.make_corridor_scene(cfg, 1003, length=length)
+    traj = syn.make_corridor_trajectory(cfg, 2003, cfg.frames, length=length)
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    p = pl.Pipeline(cfg, traj[0])
+    vol_bytes = tde.lib.tde_tsdf_volume_bytes(fmt, C.byref(p.volume()[1]))
+    shifts, offset = 0, np.zeros(3)
+    est = []
+    for i in range(cfg.frames):
+        d = orc.apply_noise(orc.render_depth(scene, traj[i], intr), 3003, i)
+        pose, st = p.process(d)
+        assert st == 0, i
+        est.append(np.concatenate([pose[:9], pose[9:] + offset]))
+        delta = p.shift_needed(0.75)
+        if not delta.any():
+            continue
+        vptr, rb = p.volume()
+        before = download(tde, vptr, vol_bytes)
+        pts, wts, n = p.shift(delta)
+        # the oracle on the same TSDF and the same black zone
+        N, org = v3(rb.voxels_size), v3(rb.origin_GRID)
+        orb = orc.RB.from_buffer_copy(bytes(rb))  # the same 72-byte round_buffer
+        mn, mx = np.full(3, 1 << 30), np.full(3, -(1 << 30))
+        for a in range(3):
+            if delta[a] > 0:
+                mn[a], mx[a] = org[a], org[a] + delta[a] - 1
+            elif delta[a] < 0:
+                mn[a], mx[a] = org[a] + N[a] + delta[a], org[a] + N[a] - 1
+        ref_pts, _, ref_w, ref_n = orc.extract_slice(before, fmt, None, mn, mx, orb, weights=True)
+        assert n == ref_n > 0
+        assert np.array_equal(pts, ref_pts) and np.array_equal(wts, ref_w)
+        # the slab is cleaned exactly as the oracle cleans it
+        orc.clean_tsdf_slice(before, fmt, mn, mx, orb)
+        assert np.array_equal(download(tde, vptr, vol_bytes), before)
+        # origins advance; the pose moves into the new volume frame
+        _, rb2 = p.volume()
+        assert np.array_equal(v3(rb2.origin_GRID), (org + delta) % N)
+        cell = cfg.volume_m / cfg.voxels
+        offset = offset + delta * cell
+        shifted = p.pose()
+        np.testing.assert_allclose(shifted[9:], pose[9:] - delta * cell, atol=1e-9)
+        shifts += 1
+    assert shifts >= 2
+    ate = pl.ate_rmse(np.array(est), traj[:cfg.frames])
+    assert ate < 0.03, ate
+    p.close()
