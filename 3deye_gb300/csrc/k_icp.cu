@@ -402,190 +402,6 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
     }
 }
 
-// ---------------------------------------------------------------------------
-// Every ICP iteration of a frame in one cooperative launch.
-//
-// One block per SM-sized share of the finest level (2048 pixels per block);
-// the blocks stay resident for all iterations and levels.  An iteration:
-// association and terms for the block's pixels, the block's exact
-// fixed-point totals added into the iteration's accumulator, a grid barrier,
-// then every block reads the same totals and runs the same FP64 solve, so
-// every block holds the same new pose without a second barrier.  Three
-// accumulators rotate: the one of iteration i-1 is zeroed by block 0 after
-// barrier i (every block read it before arriving there); the last block to
-// finish zeroes the final one and resets the barrier counters.
-// ---------------------------------------------------------------------------
-constexpr int kFrameThreads = 512;
-constexpr int kFramePix = kFrameThreads * kPixPerThread;  // pixels per block and level
-
-// Grid barrier: the `target`-th arrival releases; gives up after 1 s.
-__device__ bool grid_barrier(unsigned *counter, unsigned target) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(counter, 1u);
-        ok = 1;
-        unsigned v;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(counter) : "memory");
-        if (v < target) {
-            const uint64_t t0 = [] { uint64_t t; asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t)); return t; }();
-            while (true) {
-                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(counter) : "memory");
-                if (v >= target) break;
-                uint64_t t;
-                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-                if (t - t0 > 1000000000ull) {
-                    ok = 0;
-                    break;
-                }
-            }
-        }
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
-__global__ void __launch_bounds__(kFrameThreads, 1) icp_frame_kernel(const IcpFrameArgs F, IcpState *__restrict__ st) {
-    __shared__ IcpPose P;
-    __shared__ double sR[9], sT[3], sX[6];
-    __shared__ f2 red[kFrameThreads / 32][32];
-    __shared__ double s_sums[kIcpTerms];
-    __shared__ int s_status, s_iters;
-    const int tid = threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5;
-    if (tid < (int)(sizeof(IcpPose) / sizeof(float)))
-        reinterpret_cast<float *>(&P)[tid] = reinterpret_cast<const float *>(&st->pose)[tid];
-    if (tid < 9) sR[tid] = st->R[tid];
-    if (tid < 3) sT[tid] = st->t[tid];
-    if (tid == 0) {
-        s_status = 0;
-        s_iters = 0;
-    }
-    if (tid < kIcpTerms) s_sums[tid] = 0.0;
-    if (tid < 6) sX[tid] = 0.0;
-    __syncthreads();
-    const PoseRefs ref{sR, sT, P.R_cur, P.t_cur, sX};
-    unsigned arrivals = 0;
-    int iter = 0;
-    bool alive = true;
-    const float qnan = __int_as_float(0x7fffffff);
-
-    for (int l = F.levels - 1; l >= 0 && alive; --l) {
-        const IcpArgs &a = F.lv[l];
-        const int npix = a.W * a.H;
-        const int base = blockIdx.x * kFramePix + tid;
-        // this thread's current-frame maps stay in registers for the level
-        float3 nc[kPixPerThread], vc[kPixPerThread];
-#pragma unroll
-        for (int k = 0; k < kPixPerThread; ++k) {
-            const int p = base + k * kFrameThreads;
-            if (p < npix) { nc[k] = ld3(a.ncur, (size_t)p); vc[k] = ld3(a.vcur, (size_t)p); }
-            else { nc[k] = make_float3(qnan, qnan, qnan); vc[k] = nc[k]; }
-        }
-        for (int it = 0; it < F.iters[l]; ++it, ++iter) {
-            float s[32];
-#pragma unroll
-            for (int t = 0; t < 32; ++t) s[t] = 0.f;
-            Assoc as[kPixPerThread];
-#pragma unroll
-            for (int k = 0; k < kPixPerThread; ++k) as[k] = project(a, P, nc[k], vc[k]);
-            float3 np[kPixPerThread], vp[kPixPerThread];
-#pragma unroll
-            for (int k = 0; k < kPixPerThread; ++k)
-                if (as[k].j >= 0) { np[k] = ld3(a.nprev, (size_t)as[k].j); vp[k] = ld3(a.vprev, (size_t)as[k].j); }
-#pragma unroll
-            for (int k = 0; k < kPixPerThread; ++k) {
-                float row[7];
-                if (as[k].j >= 0 && pair_terms(a, as[k], np[k], vp[k], row)) {
-                    int t = 0;
-#pragma unroll
-                    for (int i = 0; i < 6; ++i)
-#pragma unroll
-                        for (int j = i; j < 7; ++j) { s[t] = s[t] + row[i] * row[j]; ++t; }
-                    s[27] = s[27] + 1.f;
-                }
-            }
-            const f2 wsum = warp_transpose_reduce(s, lane);
-            red[warp][lane] = wsum;
-            __syncthreads();
-            unsigned long long(*acc)[kIcpTerms][3] = st->acc3[iter % 3];
-            if (tid < kIcpTerms) {
-                f2 v = red[0][tid];
-#pragma unroll
-                for (int w = 1; w < kFrameThreads / 32; ++w) v = add_ff(v, red[w][tid]);
-                const unsigned __int128 q = (unsigned __int128)(to_fixed(v.hi) + to_fixed(v.lo));
-                const unsigned long long m42 = (1ull << 42) - 1ull;
-                unsigned long long *dst = acc[blockIdx.x % kIcpAccCopies][tid];
-                atomicAdd(dst + 0, (unsigned long long)q & m42);
-                atomicAdd(dst + 1, (unsigned long long)(q >> 42) & m42);
-                atomicAdd(dst + 2, (unsigned long long)(q >> 84) & m42);
-            }
-            arrivals += gridDim.x;
-            if (!grid_barrier(&st->barrier, arrivals)) {
-                alive = false;
-                break;
-            }
-            // every block: the exact totals, then the same solve
-            if (tid < kIcpTerms) {
-                unsigned long long a0 = 0, a1 = 0, a2 = 0;
-#pragma unroll
-                for (int c = 0; c < kIcpAccCopies; ++c) {
-                    a0 += __ldcg(&acc[c][tid][0]);
-                    a1 += __ldcg(&acc[c][tid][1]);
-                    a2 += __ldcg(&acc[c][tid][2]);
-                }
-                s_sums[tid] = from_fixed(a0, a1, a2);
-            }
-            if (blockIdx.x == 0 && iter > 0) {
-                // accumulator of iteration iter-1: every block read it before this barrier
-                unsigned long long *z = &st->acc3[(iter + 2) % 3][0][0][0];
-                for (int i = tid; i < kIcpAccCopies * kIcpTerms * 3; i += kFrameThreads) z[i] = 0ull;
-            }
-            __syncthreads();
-            if (warp == 0) {
-                const int inliers = (int)s_sums[27];
-                const bool ok = inliers >= kIcpMinInliers && warp_solve_update(ref, s_sums, lane);
-                if (lane == 0) {
-                    if (!ok) s_status |= kIcpStatusSolveFailed;
-                    s_iters += 1;
-                }
-            }
-            __syncthreads();
-        }
-    }
-    if (blockIdx.x == 0) {
-        if (tid < 9) st->R[tid] = sR[tid];
-        if (tid < 3) st->t[tid] = sT[tid];
-        if (tid < 6) st->x[tid] = sX[tid];
-        if (tid < 9) st->pose.R_cur[tid] = P.R_cur[tid];
-        if (tid < 3) st->pose.t_cur[tid] = P.t_cur[tid];
-        if (tid < kIcpTerms) st->sums[tid] = s_sums[tid];
-        if (tid == 0) {
-            st->inliers = (int)s_sums[27];
-            st->status |= s_status | (alive ? 0 : kIcpStatusTimeout);
-            st->iterations = s_iters;
-        }
-    }
-    // the last block out clears the final accumulator and the counters
-    __shared__ unsigned ticket;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) ticket = atomicAdd(&st->done, 1u);
-    __syncthreads();
-    if (ticket == gridDim.x - 1) {
-        __threadfence();
-        for (int b = 0; b < 3; ++b) {
-            unsigned long long *z = &st->acc3[b][0][0][0];
-            for (int i = tid; i < kIcpAccCopies * kIcpTerms * 3; i += kFrameThreads) z[i] = 0ull;
-        }
-        if (tid == 0) {
-            st->barrier = 0u;
-            st->done = 0u;
-        }
-    }
-}
-
 // transform_estimation.cl:4-53: group g sums its row of the partial buffer.
 __global__ void transform_estimation_kernel(const float *__restrict__ gbuf, float *__restrict__ out, int len,
                                             int stride) {
@@ -642,27 +458,6 @@ int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool so
                           : cudaLaunchKernelEx(&cfg, icp_kernel<false>, a, st, gbuf, mbuf);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "estimate_combined: %s", cudaGetErrorString(e));
     return check_launch("estimate_combined");
-}
-
-int icp_frame_blocks(int W0, int H0, int num_sms) {
-    const int nb = (int)div_up((unsigned)(W0 * H0), (unsigned)kFramePix);
-    return nb <= num_sms ? nb : 0;
-}
-
-int launch_icp_frame(const IcpFrameArgs &F, IcpState *st, int blocks, cudaStream_t stream) {
-    if (blocks < 1) return set_error(TDE_ERR_UNSUPPORTED, "icp_frame: image too large for one resident block per SM");
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(kFrameThreads);
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, icp_frame_kernel, F, st);
-    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "icp_frame: %s", cudaGetErrorString(e));
-    return check_launch("icp_frame");
 }
 
 int launch_icp_begin_frame(IcpState *st, cudaStream_t stream) {

@@ -242,12 +242,15 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         tc::mbar_init(&mbar[1], 1);
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B
+    // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B,
+    // as asynchronous copies (completed with the first rows' copies)
     const int nw = A.cout * 9 * cc;
     for (int i = tid; i < nw; i += kConvThreads) {
         const int c = i % cc, t = (i / cc) % 9, co = i / (9 * cc);
-        *reinterpret_cast<uint4 *>(wsm + ((size_t)(t * cc + c) * A.cout + co) * 16) = ldg16(A.wgt + (size_t)i * 8);
+        const uint32_t dst = tc::smem_u32(wsm + ((size_t)(t * cc + c) * A.cout + co) * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(A.wgt + (size_t)i * 8) : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -272,7 +275,7 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
             if (MODE == SRC_POOL) load_row<MODE>(A, slot, cc, img, y0 + dy, x0, tid);
             else load_row_async<MODE>(A, slot, cc, img, y0 + dy, x0, tid);
         }
-        if (MODE != SRC_POOL) wait_async_rows();
+        wait_async_rows();  // rows (and, the first time, the weights)
         tc::fence_proxy_async();
         __syncthreads();
         for (int y = y0; y < y1; ++y, ++g) {

@@ -117,7 +117,6 @@ struct tde_pipeline {
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     void *volume = nullptr;
     tde_refiner *refiner = nullptr;  // replaces the bilateral filter when set
-    int icp_blocks = 0;              // > 0: all ICP iterations of a frame in one cooperative launch
     // volume shifts: extraction scratch and point buffers, grown on demand
     void *slab_scratch = nullptr;
     size_t slab_scratch_bytes = 0;
@@ -166,20 +165,6 @@ int record_segment(tde_pipeline *p, Segment seg) {
         return check_launch("begin_frame");
     }
     case SEG_ICP:
-        if (p->icp_blocks > 0) {
-            IcpFrameArgs F;
-            std::memset(&F, 0, sizeof(F));
-            F.levels = p->levels;
-            for (int l = 0; l < p->levels; ++l) {
-                IcpArgs &a = F.lv[l];
-                a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
-                a.W = p->intr[l].cols; a.H = p->intr[l].rows;
-                a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
-                a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
-                F.iters[l] = c.icp_iters[l];
-            }
-            return launch_icp_frame(F, p->st, p->icp_blocks, s);
-        }
         for (int l = p->levels - 1; l >= 0; --l) {
             IcpArgs a;
             a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
@@ -317,12 +302,6 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     if (!p) return set_error(TDE_ERR_OOM, "pipeline_create: host allocation");
     p->cfg = c;
     p->levels = c.icp_levels;
-    {
-        int dev = 0, sms = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-            p->icp_blocks = icp_frame_blocks(c.intr.cols, c.intr.rows, sms);
-    }
     int st = tde_round_buffer_init(&p->rb, c.voxels, c.volume_size);
     if (st == TDE_OK && !valid_round_buffer(&p->rb)) st = set_error(TDE_ERR_INVALID_ARG, "pipeline_create: volume size");
     if (st != TDE_OK) { delete p; return st; }
@@ -510,7 +489,6 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p) {
     if (!p) return 0;
     int icp = 0;
     for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
-    if (p->icp_blocks > 0) icp = 1;  // one cooperative launch for every iteration
     // bilateral (or the refiner's 11 convolutions + the level-0 vertex map),
     // pyramid levels, normal maps, begin, ICP, finalize, scale, depth max,
     // brick cull, integrate, raycast, 2 resizes per coarser level
@@ -548,16 +526,21 @@ int tde_pipeline_set_refiner(tde_pipeline *p, tde_refiner *r) {
     return TDE_OK;
 }
 
-int tde_pipeline_shift_needed(tde_pipeline *p, float radius_m, int *delta3) {
-    if (!p || !delta3 || !(radius_m >= 0.f)) return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift_needed: bad argument");
+int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, int *delta3) {
+    if (!p || !delta3 || !(radius_m >= 0.f) || !(ahead_m >= 0.f))
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift_needed: bad argument");
     double pose[12];
     TDE_TRY(tde_pipeline_pose(p, pose));
     const float *vs = &p->rb.volume_size.x;
     const float *cs = &p->cell.x;
+    bool out = false;
+    double off[3];
     for (int a = 0; a < 3; ++a) {
-        const double off = pose[9 + a] - 0.5 * vs[a];
-        delta3[a] = std::fabs(off) > radius_m ? (int)std::lround(off / cs[a]) : 0;
+        // the point ahead_m along the optical axis (third column of R)
+        off[a] = pose[9 + a] + ahead_m * pose[3 * a + 2] - 0.5 * vs[a];
+        out |= std::fabs(off[a]) > radius_m;
     }
+    for (int a = 0; a < 3; ++a) delta3[a] = out ? (int)std::lround(off[a] / cs[a]) : 0;
     return TDE_OK;
 }
 

@@ -7,7 +7,6 @@ namespace tde {
 constexpr int kIcpTerms = 28;        // 27 system terms + inlier count
 constexpr int kIcpMinInliers = 6;    // fewer pairs cannot constrain 6 DoF
 constexpr int kIcpStatusSolveFailed = 1;
-constexpr int kIcpStatusTimeout = 2;  // a grid barrier of the per-frame kernel gave up
 constexpr int kIcpAccCopies = 8;
 
 // Float pose consumed by the association: current estimate (camera ->
@@ -26,16 +25,11 @@ struct IcpState {
     IcpPose pose;
     int status, inliers, iterations, pad0;
     unsigned counter;  // blocks done in the running launch (reset by the last block)
-    unsigned barrier;  // per-frame kernel: grid-barrier arrivals (reset by its last block)
-    unsigned done;     // per-frame kernel: blocks finished (reset by its last block)
-    unsigned pad1;
+    unsigned pad1[3];
     // Cross-block sums as 126-bit fixed point (2^-64 units) in three 42-bit
     // limbs; integer atomics make the total independent of block order.
     // Block b adds into copy b % kIcpAccCopies to spread atomic traffic.
     unsigned long long acc[kIcpAccCopies][kIcpTerms][3];
-    // per-frame kernel: one accumulator per iteration, three rotating; all
-    // zero between launches
-    unsigned long long acc3[3][kIcpAccCopies][kIcpTerms][3];
 };
 
 struct IcpArgs {
@@ -65,19 +59,8 @@ __host__ __device__ inline void so3_exp(const double *x, double *R) {
     R[6] = -A * wy + B * wx * wz;      R[7] = A * wx + B * wy * wz;       R[8] = 1.0 + B * (wz * wz - th2);
 }
 
-// All ICP iterations of a frame: levels coarse to fine, iters[l] each.
-struct IcpFrameArgs {
-    IcpArgs lv[3];
-    int iters[3];
-    int levels;
-};
-
 size_t icp_gbuf_floats(int W, int H);
-// Blocks of the per-frame kernel for a W0 x H0 finest level, 0 when it needs
-// more blocks than SMs (then the per-iteration kernel is used).
-int icp_frame_blocks(int W0, int H0, int num_sms);
-// Cooperative launch: every block resident for the whole frame.
-int launch_icp_frame(const IcpFrameArgs &F, IcpState *st, int blocks, cudaStream_t stream);
+
 // overlap_previous: launch with a programmatic dependency on the previous
 // kernel in the stream (the kernel waits before reading anything it wrote).
 int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, bool overlap_previous,

@@ -37,7 +37,7 @@ declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
 declare("tde_pipeline_set_pose", I, [P, P])
 declare("tde_pipeline_set_refiner", I, [P, P])
 declare("tde_pipeline_model_depth", I, [P, P])
-declare("tde_pipeline_shift_needed", I, [P, F, P])
+declare("tde_pipeline_shift_needed", I, [P, F, F, P])
 declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 
 
@@ -167,10 +167,13 @@ class Pipeline:
         self._refiner = refiner  # keeps it alive while the pipeline uses it
         check(lib.tde_pipeline_set_refiner(self._h, refiner.handle if refiner is not None else None))
 
-    def shift_needed(self, radius_m: float) -> np.ndarray:
-        """Voxel shift that re-centres the volume (zeros while the camera is within radius_m)."""
+    def shift_needed(self, radius_m: float, ahead_m: float | None = None) -> np.ndarray:
+        """Voxel shift re-centring the volume on the point ahead_m (default: half
+        the volume) in front of the camera; zeros while it is within radius_m."""
+        if ahead_m is None:
+            ahead_m = 0.5 * self.cfg.volume_m
         d = np.zeros(3, np.int32)
-        check(lib.tde_pipeline_shift_needed(self._h, radius_m, d.ctypes.data_as(P)))
+        check(lib.tde_pipeline_shift_needed(self._h, ahead_m, radius_m, d.ctypes.data_as(P)))
         return d
 
     def shift(self, delta, capacity: int = 1 << 22):

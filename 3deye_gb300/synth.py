@@ -153,16 +153,17 @@ CORRIDOR_CEILING = 1.0      # ceiling this far above it
 
 def make_corridor_scene(cfg: Config, seed: int, length: float = 12.0) -> np.ndarray:
     """Floor, ceiling and two walls (planes) plus a random box every 0.5 m,
-    alternating walls, from behind the start to beyond the end of the walk."""
+    alternating walls, from the start of the walk (the volume's rear face,
+    z = 0) to beyond its end."""
     rng = np.random.default_rng(seed)
     c = cfg.volume_m / 2.0
     y_floor, y_ceil = c + CORRIDOR_FLOOR, c - CORRIDOR_CEILING
     xl, xr = c - CORRIDOR_HALF_WIDTH, c + CORRIDOR_HALF_WIDTH
     prims = [[0, 0.0, 1.0, 0.0, -y_floor, 0, 0, 0], [0, 0.0, 1.0, 0.0, -y_ceil, 0, 0, 0],
              [0, 1.0, 0.0, 0.0, -xl, 0, 0, 0], [0, 1.0, 0.0, 0.0, -xr, 0, 0, 0]]
-    z = c - 1.5
+    z = 0.5
     side = 1
-    while z < c + length + 4.5:
+    while z < length + cfg.volume_m + 4.5:
         w, h, d = rng.uniform(0.2, 0.5, size=3)
         zz = z + rng.uniform(-0.1, 0.1)
         if side > 0:
@@ -181,16 +182,17 @@ def make_corridor_scene(cfg: Config, seed: int, length: float = 12.0) -> np.ndar
 
 
 def make_corridor_trajectory(cfg: Config, seed: int, frames: int | None = None, length: float = 12.0) -> np.ndarray:
-    """Walk along +z from the volume centre over `length` metres (<= 2 cm per
-    frame for 600 frames), with slow lateral / vertical sway and a gently
-    wandering gaze ahead.  Returns (frames, 12) float64: R row-major, t."""
+    """Walk along +z from the volume's rear face (z = 0, the volume ahead of
+    the camera) over `length` metres (2 cm per frame for 600 frames), with
+    slow lateral / vertical sway and a gently wandering gaze ahead.  Returns
+    (frames, 12) float64: R row-major, t."""
     n = cfg.frames if frames is None else frames
     rng = np.random.default_rng(seed)
     c = cfg.volume_m / 2.0
     k = np.arange(n, dtype=np.float64)
     ph = rng.uniform(0, 2 * np.pi, size=6)
     fr = rng.uniform(0.01, 0.03, size=6)
-    zc = c + length * k / max(n - 1, 1)
+    zc = length * k / max(n - 1, 1)
     eye = np.stack([c + 0.15 * np.sin(fr[0] * k + ph[0]), c + 0.08 * np.sin(fr[1] * k + ph[1]), zc], axis=1)
     tgt = np.stack([c + 0.4 * np.sin(fr[2] * k + ph[2]), c + 0.3 + 0.15 * np.sin(fr[3] * k + ph[3]), zc + 2.0], axis=1)
     out = np.empty((n, 12), np.float64)

@@ -98,10 +98,12 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p);
 /* Replace the volume origin bookkeeping after a cyclic shift (the caller has
  * extracted and cleaned the outgoing slab); re-captures the graphs. */
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb);
-/* Cyclic volume (config: a volume following the camera).  The shift, in
- * voxels per axis, that re-centres the volume on the camera when the camera
- * is more than radius_m from the volume centre along an axis, else 0. */
-int tde_pipeline_shift_needed(tde_pipeline *p, float radius_m, int *delta3);
+/* Cyclic volume following the camera: the point ahead_m in front of the
+ * camera (along its optical axis; half the volume keeps the volume on what
+ * the camera sees) is compared with the volume centre; when it is more than
+ * radius_m away along some axis, delta3 receives the shift in voxels that
+ * re-centres the volume on it, else zeros. */
+int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, int *delta3);
 
 /* Shifts the volume by delta3 voxels (|delta| below the voxel count per
  * axis), host-synchronous: the slab that leaves the volume is extracted as

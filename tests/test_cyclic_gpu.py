@@ -28,22 +28,23 @@ def download(tde, ptr, nbytes):
 @pytest.mark.parametrize("fmt", [0, 1])
 def test_corridor_shifts_extract_bit_exact(cuda, orc, tde, fmt):
     pl = importlib.import_module("3deye_gb300.pipeline")
-    base = syn.small_config("c1", frames=150, cols=160, rows=120, voxels=128, fmt=fmt)
+    # 320x240: at 160x120 this corridor is too coarse to track even without shifts
+    base = syn.small_config("c1", frames=200, cols=320, rows=240, voxels=128, fmt=fmt)
     cfg = dataclasses.replace(base, volume_m=3.0, trunc_m=0.07, scene_cube_m=3.0)
-    length = 3.0
+    length = 4.0
     scene = syn.make_corridor_scene(cfg, 1003, length=length)
     traj = syn.make_corridor_trajectory(cfg, 2003, cfg.frames, length=length)
     intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
     p = pl.Pipeline(cfg, traj[0])
     vol_bytes = tde.lib.tde_tsdf_volume_bytes(fmt, C.byref(p.volume()[1]))
-    shifts, offset = 0, np.zeros(3)
+    shifts, points, offset = 0, 0, np.zeros(3)
     est = []
     for i in range(cfg.frames):
         d = orc.apply_noise(orc.render_depth(scene, traj[i], intr), 3003, i)
         pose, st = p.process(d)
         assert st == 0, i
         est.append(np.concatenate([pose[:9], pose[9:] + offset]))
-        delta = p.shift_needed(0.75)
+        delta = p.shift_needed(0.4)
         if not delta.any():
             continue
         vptr, rb = p.volume()
@@ -59,8 +60,9 @@ def test_corridor_shifts_extract_bit_exact(cuda, orc, tde, fmt):
             elif delta[a] < 0:
                 mn[a], mx[a] = org[a] + N[a] + delta[a], org[a] + N[a] - 1
         ref_pts, _, ref_w, ref_n = orc.extract_slice(before, fmt, None, mn, mx, orb, weights=True)
-        assert n == ref_n > 0
+        assert n == ref_n
         assert np.array_equal(pts, ref_pts) and np.array_equal(wts, ref_w)
+        points += n
         # the slab is cleaned exactly as the oracle cleans it
         orc.clean_tsdf_slice(before, fmt, mn, mx, orb)
         assert np.array_equal(download(tde, vptr, vol_bytes), before)
@@ -72,7 +74,7 @@ def test_corridor_shifts_extract_bit_exact(cuda, orc, tde, fmt):
         shifted = p.pose()
         np.testing.assert_allclose(shifted[9:], pose[9:] - delta * cell, atol=1e-9)
         shifts += 1
-    assert shifts >= 2
+    assert shifts >= 3 and points > 0
     ate = pl.ate_rmse(np.array(est), traj[:cfg.frames])
-    assert ate < 0.03, ate
+    assert ate < 0.03, ate  # about 1 cm measured (4 m walk, a shift every ~20 frames)
     p.close()

@@ -76,8 +76,7 @@ def test_async_enqueue_matches_blocking(cuda, seq):
     assert len(ti) == len(depths) and (ti > 0).all() and (tr > 0).all()
     r, w = p.integrate_stats()
     assert r > 0 and 0 < w <= r
-    # 160x120: every ICP iteration of a frame runs in one cooperative launch
-    assert p.launches_per_frame() == 18
+    assert p.launches_per_frame() == 36
     p.close()
 
 
