@@ -102,18 +102,11 @@ __device__ __forceinline__ bool pair_terms(const IcpArgs &a, const Assoc &s, flo
 //
 // GB300 executes FP64 at a small fraction of the FP32 rate (a dependent DFMA
 // takes ~64 cycles, a double reciprocal ~430, sqrt ~670, sincos ~1600), so the
-// solve is arranged for latency: LDL^T instead of Cholesky (no square roots),
-// one row per lane so the row updates of a column issue as one instruction,
-// reciprocals from an FP32 seed and two Newton steps, and the SO(3)
-// exponential from its Taylor series when the rotation step is small.
+// solve is arranged for latency: 3x3 blocks with adjugate inverses (two
+// divisions, no square roots, short chains of 3-term dot products spread
+// over lanes), and the SO(3) exponential from its Taylor series when the
+// rotation step is small.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double rcp64(double d) {
-    double y = (double)__frcp_rn((float)d);
-    y = y * fma(-d, y, 2.0);
-    y = y * fma(-d, y, 2.0);
-    return y;
-}
-
 // A(theta) = sin(theta)/theta, B(theta) = (1 - cos(theta))/theta^2.
 __device__ __forceinline__ void rodrigues_coeffs(double th2, double &A, double &B) {
     if (th2 < 1e-2) {  // theta < 0.1: truncation below 1e-17
@@ -127,62 +120,74 @@ __device__ __forceinline__ void rodrigues_coeffs(double th2, double &A, double &
     }
 }
 
-// Loads the unpacked system into shared memory (lanes 0..5, one row each).
-__device__ __forceinline__ void unpack_system(const double *sums, int lane, double (&A)[6][6], double (&b)[6]) {
-    if (lane < 6) {
-        int s = 0;
-        for (int k = 0; k < 6; ++k)
-            for (int j = k; j < 7; ++j, ++s) {
-                if (k == lane) { if (j == 6) b[lane] = sums[s]; else A[lane][j] = sums[s]; }
-                else if (j == lane) A[lane][k] = sums[s];
-            }
-    }
-    __syncwarp();
+// Term index of entry (r, c) of [A | b] in the 27-term upper-triangular
+// order of opencl_wrappers.cpp:426-437 (row k holds columns k..6).
+__device__ __forceinline__ int term_index(int r, int c) {
+    const int k = r < c ? r : c, j = r < c ? c : r;  // A is symmetric
+    return k * 7 - (k * (k - 1)) / 2 + (j - k);
 }
 
-// FP64 LDL^T solve, one row per lane.  False when A is not positive definite.
-__device__ bool fp64_ldlt_solve(const double (&A)[6][6], const double (&b)[6], int lane, double (&xo)[6]) {
-    // E_jk = L_jk D_k is kept beside L so each column costs one FMA chain
-    __shared__ double L[6][6], E[6][6], D[6], z[6];
+// Cofactor (r, c) of a symmetric 3x3 matrix held row-major in M; the cyclic
+// index form gives the sign.  adj(M) = cofactors (symmetric M).
+__device__ __forceinline__ double cofactor3(const double *M, int r, int c) {
+    const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    return fma(M[3 * r1 + c1], M[3 * r2 + c2], -M[3 * r1 + c2] * M[3 * r2 + c1]);
+}
+
+// FP64 solve of the 6x6 system by 3x3 blocks: with A = [[P, Q], [Q^T, R]],
+// S = R - Q^T P^-1 Q, x2 = S^-1 (b2 - Q^T P^-1 b1), x1 = P^-1 b1 - P^-1 Q x2,
+// each 3x3 inverse as adjugate / determinant.  Two reciprocals and chains of
+// 3-term dot products keep the dependent FP64 latency short.  False when A is
+// not positive definite (a pivot of P or S at or below 1e-30, tested through
+// the leading minors).  Lanes 0..11 work; the result is in xo.
+__device__ bool fp64_block_solve(const double *sums, int lane, double (&xo)[6]) {
+    __shared__ double P[9], Q[9], R[9], b[6], CP[9], iP[9], T[9], S[9], CS[9], iS[9], u[3], w[3];
     __shared__ int ok;
+    const int r = lane / 3, c = lane % 3;
+    if (lane < 9) {
+        P[lane] = sums[term_index(r, c)];
+        Q[lane] = sums[term_index(r, 3 + c)];
+        R[lane] = sums[term_index(3 + r, 3 + c)];
+    } else if (lane < 15) {
+        b[lane - 9] = sums[term_index(lane - 9, 6)];
+    }
     if (lane == 0) ok = 1;
     __syncwarp();
-    #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        // t_i = A_ij - sum_k L_ik E_jk
-        double t = lane < 6 ? A[lane][j] : 0.0;
-        #pragma unroll
-        for (int k = 0; k < j; ++k)
-            if (lane > k && lane < 6) t = fma(-L[lane][k], E[j][k], t);
-        if (lane == j) {
-            D[j] = t;
-            if (!(t > 1e-30)) ok = 0;
-        }
-        __syncwarp();
-        const double inv = rcp64(D[j]);
-        if (lane > j && lane < 6) { L[lane][j] = t * inv; E[lane][j] = t; }
-        if (lane == j) L[j][j] = 1.0;
-        __syncwarp();
-    }
-    if (!ok) return false;
-    // L z = b (lane i accumulates as z_k arrive), then y = z / D, L^T x = y
-    double acc = lane < 6 ? b[lane] : 0.0;
-    #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        if (lane == k) z[k] = acc;
-        __syncwarp();
-        if (lane > k && lane < 6) acc = fma(-L[lane][k], z[k], acc);
+    if (lane < 9) CP[lane] = cofactor3(P, r, c);
+    __syncwarp();
+    // det P through the first row; leading minors P00, P00 P11 - P01^2 (= CP[8]), det P
+    const double detP = fma(P[0], CP[0], fma(P[1], CP[1], P[2] * CP[2]));
+    if (lane == 0 && !(P[0] > 1e-30 && CP[8] > 1e-30 * P[0] && detP > 1e-30 * CP[8])) ok = 0;
+    const double invP = 1.0 / detP;
+    if (lane < 9) iP[lane] = CP[lane] * invP;
+    __syncwarp();
+    // T = Q^T P^-1 (3x3), w = P^-1 b1
+    if (lane < 9) T[lane] = fma(Q[r], iP[c], fma(Q[3 + r], iP[3 + c], Q[6 + r] * iP[6 + c]));
+    else if (lane < 12) {
+        const int i = lane - 9;
+        w[i] = fma(iP[3 * i], b[0], fma(iP[3 * i + 1], b[1], iP[3 * i + 2] * b[2]));
     }
     __syncwarp();
-    acc = lane < 6 ? z[lane] * rcp64(D[lane]) : 0.0;
-    #pragma unroll
-    for (int k = 5; k >= 0; --k) {
-        if (lane == k) xo[k] = acc;
-        __syncwarp();
-        if (lane < k) acc = fma(-L[k][lane], xo[k], acc);
+    // S = R - T Q, u = b2 - T b1
+    if (lane < 9) S[lane] = R[lane] - fma(T[3 * r], Q[c], fma(T[3 * r + 1], Q[3 + c], T[3 * r + 2] * Q[6 + c]));
+    else if (lane < 12) {
+        const int i = lane - 9;
+        u[i] = b[3 + i] - fma(T[3 * i], b[0], fma(T[3 * i + 1], b[1], T[3 * i + 2] * b[2]));
     }
     __syncwarp();
-    return true;
+    if (lane < 9) CS[lane] = cofactor3(S, r, c);
+    __syncwarp();
+    const double detS = fma(S[0], CS[0], fma(S[1], CS[1], S[2] * CS[2]));
+    if (lane == 0 && !(S[0] > 1e-30 && CS[8] > 1e-30 * S[0] && detS > 1e-30 * CS[8])) ok = 0;
+    const double invS = 1.0 / detS;
+    if (lane < 9) iS[lane] = CS[lane] * invS;
+    __syncwarp();
+    // x2 = S^-1 u; x1 = w - T^T x2
+    if (lane < 3) xo[3 + lane] = fma(iS[3 * lane], u[0], fma(iS[3 * lane + 1], u[1], iS[3 * lane + 2] * u[2]));
+    __syncwarp();
+    if (lane < 3) xo[lane] = w[lane] - fma(T[lane], xo[3], fma(T[3 + lane], xo[4], T[6 + lane] * xo[5]));
+    __syncwarp();
+    return ok != 0;
 }
 
 // The pose a solve updates: FP64 estimate, its float mirror, the last step.
@@ -195,10 +200,9 @@ struct PoseRefs {
 // Solve and apply the update to the pose; false (pose unchanged) when A is
 // not positive definite.
 __device__ bool warp_solve_update(const PoseRefs &P, const double *sums, int lane) {
-    __shared__ double A[6][6], b[6], Rinc[9];
-    unpack_system(sums, lane, A, b);
+    __shared__ double Rinc[9];
     __shared__ double x[6];
-    if (!fp64_ldlt_solve(A, b, lane, x)) return false;
+    if (!fp64_block_solve(sums, lane, x)) return false;
     // Rinc = I + A [w]x + B (w w^T - th2 I), lanes 0..8 one entry each
     const double wx = x[0], wy = x[1], wz = x[2];
     const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
