@@ -34,7 +34,7 @@ NO_FMAD = {"k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu"}
 CUDA_UNITS = ["capi.cu", "k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_slab.cu",
               "pipeline.cu", "k_synth.cu", "noalloc.cu", "k_refiner.cu", "refiner.cu"]
 CXX_UNITS = ["wrappers.cpp"]
-ORACLE_SOURCES = ["oracle.c", "oracle_scene.c"]
+ORACLE_SOURCES = ["oracle.c", "oracle_scene.c", "oracle_f64.c"]
 
 
 def _nvcc() -> str:

@@ -62,4 +62,17 @@ int or_apply_noise(const float *depth_m, uint16_t *depth_mm, int W, int H, uint3
 #ifdef __cplusplus
 }
 #endif
+
+/* Full-FP64 model stages for the storage precision study (oracle_f64.c):
+ * FP64 TSDF values with int32 weights, FP64 raycast maps, FP64 ICP terms. */
+int or_scale_depth_f64(const uint16_t *depth, double *scaled, const tde_intrinsics *in);
+int or_integrate_f64(const double *depth, double *tsdf, int32_t *weight, double trunc, const double *Ri,
+                     const double *t, const tde_intrinsics *in, const double *cell, const tde_round_buffer *rb,
+                     int max_weight);
+int or_raycast_f64(const double *tsdf, double *vmap, double *nmap, const double *t, const double *R, double trunc,
+                   const tde_intrinsics *intr, const tde_round_buffer *rb, const double *cell);
+int or_icp_terms_f64(const float *vcur, const float *ncur, const double *vprev, const double *nprev,
+                     const double *Rc, const double *tc, const double *Rpi, const double *tp,
+                     const tde_intrinsics *in, double dist_thresh, double angle_thresh, double *sums);
+
 #endif

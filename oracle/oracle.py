@@ -76,6 +76,10 @@ _sigs = {
     "or_clean_tsdf_slice": (I, [P, I, P, P, pRB]),
     "or_clean_color_slice": (I, [P, P, P, pRB]),
     "or_set_threads": (I, [I]),
+    "or_scale_depth_f64": (I, [P, P, pI]),
+    "or_integrate_f64": (I, [P, P, P, C.c_double, P, P, pI, P, pRB, I]),
+    "or_raycast_f64": (I, [P, P, P, P, P, C.c_double, pI, pRB, P]),
+    "or_icp_terms_f64": (I, [P, P, P, P, P, P, P, P, pI, C.c_double, C.c_double, P]),
     "or_render_depth": (I, [P, I, P, pI, P]),
     "or_apply_noise": (I, [P, P, I, I, C.c_uint32, C.c_uint32, F, F]),
 }
@@ -244,3 +248,37 @@ def ref(name: str) -> C.CDLL:
     if name not in _ref_cache:
         _ref_cache[name] = C.CDLL(str(REF_DIR / f"ref_{name}.so"))
     return _ref_cache[name]
+
+
+# ---------------------------------------------------------------------------
+# full-FP64 model stages (precision study)
+# ---------------------------------------------------------------------------
+def f64(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+def scale_depth_f64(depth, intr):
+    out = np.empty(depth.shape, np.float64)
+    lib.or_scale_depth_f64(_p(np.ascontiguousarray(depth)), _p(out), C.byref(intr))
+    return out
+
+
+def integrate_f64(depth_scaled, tsdf, weight, trunc, R_inv, t, intr, cell, rb, max_weight):
+    lib.or_integrate_f64(_p(f64(depth_scaled)), _p(tsdf), _p(weight), float(trunc), _p(f64(R_inv)), _p(f64(t)),
+                         C.byref(intr), _p(f64(cell)), C.byref(rb), int(max_weight))
+
+
+def raycast_f64(tsdf, rb, intr, R, t, trunc, cell):
+    vm = np.empty((intr.rows, intr.cols, 3), np.float64)
+    nm = np.empty_like(vm)
+    lib.or_raycast_f64(_p(tsdf), _p(vm), _p(nm), _p(f64(t)), _p(f64(R)), float(trunc), C.byref(intr), C.byref(rb),
+                       _p(f64(cell)))
+    return vm, nm
+
+
+def icp_terms_f64(vcur, ncur, vprev, nprev, R, t, R_prev_inv, t_prev, intr, dist_thresh, angle_thresh):
+    sums = np.zeros(28, np.float64)
+    lib.or_icp_terms_f64(_p(f32(vcur)), _p(f32(ncur)), _p(f64(vprev)), _p(f64(nprev)), _p(f64(R)), _p(f64(t)),
+                         _p(f64(R_prev_inv)), _p(f64(t_prev)), C.byref(intr), float(dist_thresh), float(angle_thresh),
+                         _p(sums))
+    return sums

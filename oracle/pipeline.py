@@ -82,3 +82,71 @@ class OraclePipeline:
             self.nmod[l] = orc.resize_map(self.nmod[l - 1], True)
         self.frames += 1
         return np.concatenate([self.R.ravel(), self.t])
+
+
+class OraclePipelineF64(OraclePipeline):
+    """The same loop with a full-FP64 model: FP64 TSDF values (int32 weights,
+    no storage rounding), FP64 integration and raycast, FP64 ICP terms, sums
+    and solve.  The reference point of the storage precision study."""
+
+    def __init__(self, cfg, pose12, levels=3):
+        super().__init__(cfg, pose12, levels)
+        n = cfg.voxels ** 3
+        self.vol = None
+        self.tsdf = np.zeros(n, np.float64)
+        self.weight = np.zeros(n, np.int32)
+        self.cell64 = np.full(3, cfg.volume_m / cfg.voxels, np.float64)
+
+    def track(self, vs, ns):
+        c = self.cfg
+        R_prev, t_prev = self.R.copy(), self.t.copy()
+        R, t = self.R.copy(), self.t.copy()
+        ok = True
+        for l in range(self.levels - 1, -1, -1):
+            il = self.intr.level(l)
+            for _ in range(c.icp_iters[l]):
+                sums = orc.icp_terms_f64(vs[l], ns[l], self.vmod[l], self.nmod[l], R, t, R_prev.T, t_prev, il,
+                                         c.dist_thresh, c.angle_thresh)
+                if sums[27] < 6:
+                    ok = False
+                    continue
+                st, R2, t2, _ = orc.icp_solve(sums, R.ravel(), t)
+                if st != 0:
+                    ok = False
+                    continue
+                R, t = R2.reshape(3, 3), t2
+        if ok:
+            self.R, self.t = R, t
+        return ok
+
+    def process(self, depth):
+        c = self.cfg
+        ds, vs, ns = self.frame_maps(depth)
+        ok = True
+        if self.frames > 0:
+            ok = self.track(vs, ns)
+        self.lost.append(not ok)
+        sd = orc.scale_depth_f64(depth, self.intr)
+        orc.integrate_f64(sd, self.tsdf, self.weight, c.trunc_m, self.R.T, self.t, self.intr, self.cell64, self.rb,
+                          c.max_weight)
+        vm, nm = orc.raycast_f64(self.tsdf, self.rb, self.intr, self.R, self.t, c.trunc_m, self.cell64)
+        self.vmod[0], self.nmod[0] = vm, nm
+        for l in range(1, self.levels):
+            # 2x2 means as the model pyramid, in FP64
+            self.vmod[l] = _resize64(self.vmod[l - 1], False)
+            self.nmod[l] = _resize64(self.nmod[l - 1], True)
+        self.frames += 1
+        return np.concatenate([self.R.ravel(), self.t])
+
+
+def _resize64(m, normal):
+    h, w, _ = m.shape
+    b = m[: h // 2 * 2, : w // 2 * 2].reshape(h // 2, 2, w // 2, 2, 3)
+    s = b.sum(axis=(1, 3))
+    bad = np.isnan(b).any(axis=(1, 3, 4))
+    if normal:
+        s = s / np.linalg.norm(s, axis=-1, keepdims=True)
+    else:
+        s = s * 0.25
+    s[bad] = np.nan
+    return np.ascontiguousarray(s)
