@@ -23,6 +23,8 @@
 // (deterministic).
 #include <cuda_bf16.h>
 
+#include <vector>
+
 #include "tde_common.cuh"
 #include "tde_refiner.cuh"
 #include "tde_tc.cuh"
@@ -33,7 +35,8 @@ namespace {
 
 constexpr int kTileM = 128;             // output pixels per MMA tile
 constexpr int kHaloW = kTileM + 2;      // halo pixels per row
-constexpr int kConvThreads = 128;       // 4 warps: one TMEM lane quarter each
+constexpr int kConvWorkers = 128;       // warps 0-3: loads and epilogue, one TMEM lane quarter each
+constexpr int kConvThreads = 160;       // + warp 4: issues the MMAs
 constexpr int kWgK = 64;                // pixels per weight-gradient K step
 constexpr int kWgHalo = kWgK + 2;
 constexpr int kWgThreads = 256;
@@ -110,29 +113,22 @@ constexpr int kSlots = 4;
 // Loads one input row (halo pixels x0-1 .. x0+128, every chunk) into a slot.
 // Loads are issued in groups before their stores so that several are in
 // flight per thread.
-template <int MODE>
-__device__ __forceinline__ void load_row(const ConvArgs &A, unsigned char *slot, int cc, int img, int y, int x0,
-                                         int tid) {
+template <int MODE, int CC>
+__device__ __forceinline__ void load_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int tid) {
     constexpr int G = MODE == SRC_POOL ? 4 : 8;
-    const int n = kHaloW * cc;
-    for (int base = tid; base < n; base += kConvThreads * G) {
+    constexpr int n = kHaloW * CC;
+    for (int base = tid; base < n; base += kConvWorkers * G) {
         uint4 v[G];
 #pragma unroll
         for (int g = 0; g < G; ++g) {
-            const int i = base + g * kConvThreads;
+            const int i = base + g * kConvWorkers;
             v[g] = make_uint4(0u, 0u, 0u, 0u);
-            if (i < n) {
-                const int c = i % cc, px = i / cc;
-                v[g] = load_input_chunk<MODE>(A, img, y, x0 + px - 1, c);
-            }
+            if (i < n) v[g] = load_input_chunk<MODE>(A, img, y, x0 + i / CC - 1, i % CC);
         }
 #pragma unroll
         for (int g = 0; g < G; ++g) {
-            const int i = base + g * kConvThreads;
-            if (i < n) {
-                const int c = i % cc, px = i / cc;
-                *reinterpret_cast<uint4 *>(slot + ((size_t)c * kHaloW + px) * 16) = v[g];
-            }
+            const int i = base + g * kConvWorkers;
+            if (i < n) *reinterpret_cast<uint4 *>(slot + ((size_t)(i % CC) * kHaloW + i / CC) * 16) = v[g];
         }
     }
 }
@@ -156,12 +152,12 @@ __device__ __forceinline__ const bf16 *chunk_ptr(const ConvArgs &A, int img, int
 
 // Starts the copies of one input row into a slot with cp.async (16 B each,
 // zero-filled outside the image); completed by cp.async.wait_all.
-template <int MODE>
-__device__ __forceinline__ void load_row_async(const ConvArgs &A, unsigned char *slot, int cc, int img, int y, int x0,
+template <int MODE, int CC>
+__device__ __forceinline__ void load_row_async(const ConvArgs &A, unsigned char *slot, int img, int y, int x0,
                                                int tid) {
-    const int n = kHaloW * cc;
-    for (int i = tid; i < n; i += kConvThreads) {
-        const int c = i % cc, px = i / cc;
+    constexpr int n = kHaloW * CC;
+    for (int i = tid; i < n; i += kConvWorkers) {
+        const int c = i % CC, px = i / CC;
         const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
         const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
         const int bytes = src ? 16 : 0;
@@ -221,14 +217,14 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
     }
 }
 
-template <int MODE>
+template <int MODE, int CC>
 __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs A, int rows_per_item) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
-    const int cin = A.ca + A.cb, cc = cin >> 3;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const size_t slot_bytes = (size_t)cc * kHaloW * 16;
+    const bool worker = warp < 4;
+    constexpr uint32_t slot_bytes = (uint32_t)CC * kHaloW * 16;
     unsigned char *halo = smem;
     unsigned char *wsm = smem + kSlots * slot_bytes;
     const uint32_t ncols = tmem_cols(A.cout);
@@ -244,19 +240,26 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B,
     // as asynchronous copies (completed with the first rows' copies)
-    const int nw = A.cout * 9 * cc;
-    for (int i = tid; i < nw; i += kConvThreads) {
-        const int c = i % cc, t = (i / cc) % 9, co = i / (9 * cc);
-        const uint32_t dst = tc::smem_u32(wsm + ((size_t)(t * cc + c) * A.cout + co) * 16);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(A.wgt + (size_t)i * 8) : "memory");
+    if (worker) {
+        const int nw = A.cout * 9 * CC;
+        for (int i = tid; i < nw; i += kConvWorkers) {
+            const int c = i % CC, t = (i / CC) % 9, co = i / (9 * CC);
+            const uint32_t dst = tc::smem_u32(wsm + ((size_t)(t * CC + c) * A.cout + co) * 16);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(A.wgt + (size_t)i * 8) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    asm volatile("cp.async.commit_group;" ::: "memory");
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
     const uint32_t halo_s = tc::smem_u32(halo), w_s = tc::smem_u32(wsm);
     const uint32_t idesc = tc::idesc_bf16(kTileM, A.cout);
+    // descriptor bases: A at a slot's first plane (LBO = plane stride), B at
+    // the first weight plane; an MMA adds its byte offset >> 4
+    const uint64_t a_desc0 = tc::desc(halo_s, kHaloW * 16, 128);
+    const uint64_t b_desc0 = tc::desc(w_s, A.cout * 16, 128);
+    const uint32_t b_plane = (uint32_t)A.cout * 16;
     const int tiles_x = (A.w + kTileM - 1) / kTileM;
     const int chunks = (A.h + rows_per_item - 1) / rows_per_item;
     const int items = A.n * tiles_x * chunks;
@@ -270,49 +273,59 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         const int x0 = xt * kTileM;
         const int y0 = ch * rows_per_item;
         const int y1 = min(A.h, y0 + rows_per_item);
-        for (int dy = -1; dy <= 1; ++dy) {
-            unsigned char *slot = halo + (size_t)((y0 + dy + kSlots) % kSlots) * slot_bytes;
-            if (MODE == SRC_POOL) load_row<MODE>(A, slot, cc, img, y0 + dy, x0, tid);
-            else load_row_async<MODE>(A, slot, cc, img, y0 + dy, x0, tid);
+        if (worker) {
+            for (int dy = -1; dy <= 1; ++dy) {
+                unsigned char *slot = halo + (size_t)((y0 + dy + kSlots) % kSlots) * slot_bytes;
+                if (MODE == SRC_POOL) load_row<MODE, CC>(A, slot, img, y0 + dy, x0, tid);
+                else load_row_async<MODE, CC>(A, slot, img, y0 + dy, x0, tid);
+            }
+            wait_async_rows();  // rows (and, the first time, the weights)
         }
-        wait_async_rows();  // rows (and, the first time, the weights)
         tc::fence_proxy_async();
         __syncthreads();
         for (int y = y0; y < y1; ++y, ++g) {
-            if (tid == 0) {
-                tc::fence_after_sync();
-                const uint32_t dacc = tmem + (g & 1u) * ncols;
-                uint32_t acc = 0;
-                for (int t = 0; t < 9; ++t) {
-                    const int dy = t / 3, dx = t % 3;
-                    const uint32_t sbase = halo_s + (uint32_t)(((y + dy - 1 + kSlots) % kSlots) * slot_bytes);
-                    for (int kc = 0; kc < cc; kc += 2) {
-                        const uint64_t ad = tc::desc(sbase + (uint32_t)((kc * kHaloW + dx) * 16), kHaloW * 16, 128);
-                        const uint64_t bd = tc::desc(w_s + (uint32_t)((t * cc + kc) * A.cout * 16), A.cout * 16, 128);
-                        tc::mma_bf16(dacc, ad, bd, idesc, acc);
-                        acc = 1;
+            if (warp == 4) {
+                if (lane == 0) {
+                    tc::fence_after_sync();
+                    const uint32_t dacc = tmem + (g & 1u) * ncols;
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) {
+                        const int dy = t / 3, dx = t % 3;
+                        const uint32_t a_off = (uint32_t)((y + dy - 1 + kSlots) % kSlots) * slot_bytes + dx * 16;
+#pragma unroll
+                        for (int kc = 0; kc < CC; kc += 2) {
+                            const uint64_t ad = a_desc0 + ((a_off + (uint32_t)kc * kHaloW * 16) >> 4);
+                            const uint64_t bd = b_desc0 + (((uint32_t)(t * CC + kc) * b_plane) >> 4);
+                            tc::mma_bf16(dacc, ad, bd, idesc, (t | kc) ? 1u : 0u);
+                        }
                     }
+                    tc::commit(&mbar[g & 1u]);
                 }
-                tc::commit(&mbar[g & 1u]);
+                __syncwarp();
             }
             if (y > y0) {
                 // row y-1: its MMAs are done, so its accumulator can be drained
                 // and the slot of row y-2 refilled
-                const uint32_t gp = g - 1;
-                const bool ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
+                bool ok = true;
+                if (worker) {
+                    const uint32_t gp = g - 1;
+                    ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
+                }
                 if (__syncthreads_or(!ok)) {
                     failed = true;
                     break;
                 }
                 tc::fence_after_sync();
             }
-            unsigned char *next = halo + (size_t)((y + 2) % kSlots) * slot_bytes;
-            // the copies of row y+2 run while row y-1 is drained
-            if (MODE != SRC_POOL && y + 1 < y1) load_row_async<MODE>(A, next, cc, img, y + 2, x0, tid);
-            if (y > y0) conv_epilogue(A, tmem + ((g - 1) & 1u) * ncols, warp, lane, img, y - 1, x0);
-            if (y + 1 < y1) {
-                if (MODE == SRC_POOL) load_row<MODE>(A, next, cc, img, y + 2, x0, tid);
-                else wait_async_rows();
+            if (worker) {
+                unsigned char *next = halo + (size_t)((y + 2) % kSlots) * slot_bytes;
+                // the copies of row y+2 run while row y-1 is drained
+                if (MODE != SRC_POOL && y + 1 < y1) load_row_async<MODE, CC>(A, next, img, y + 2, x0, tid);
+                if (y > y0) conv_epilogue(A, tmem + ((g - 1) & 1u) * ncols, warp, lane, img, y - 1, x0);
+                if (y + 1 < y1) {
+                    if (MODE == SRC_POOL) load_row<MODE, CC>(A, next, img, y + 2, x0, tid);
+                    else wait_async_rows();
+                }
             }
             tc::fence_proxy_async();
             tc::fence_before_sync();
@@ -320,14 +333,17 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         }
         if (failed) break;
         // last row of the strip
-        const uint32_t gp = g - 1;
-        const bool ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
+        bool ok = true;
+        if (worker) {
+            const uint32_t gp = g - 1;
+            ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
+        }
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
         }
         tc::fence_after_sync();
-        conv_epilogue(A, tmem + (gp & 1u) * ncols, warp, lane, img, y1 - 1, x0);
+        if (worker) conv_epilogue(A, tmem + ((g - 1) & 1u) * ncols, warp, lane, img, y1 - 1, x0);
         tc::fence_before_sync();
         __syncthreads();
     }
@@ -340,6 +356,21 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 2 * ncols);
+}
+
+// (mode, input chunks) pairs the network uses: forward c2..c11 and the input
+// gradients of c2..c11 (direct sources with cout/8 chunks)
+#define TDE_CONV_VARIANTS(X) \
+    X(SRC_DIRECT, 2) X(SRC_DIRECT, 4) X(SRC_DIRECT, 6) X(SRC_DIRECT, 8) \
+    X(SRC_POOL, 2) X(SRC_POOL, 4) X(SRC_POOL, 6) \
+    X(SRC_UP, 6) X(SRC_UP, 10) X(SRC_UP, 14)
+
+const void *conv_kernel_fn(int mode, int cc) {
+#define TDE_CONV_FN(M, C) \
+    if (mode == M && cc == C) return (const void *)conv3x3_tc_kernel<M, C>;
+    TDE_CONV_VARIANTS(TDE_CONV_FN)
+#undef TDE_CONV_FN
+    return nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -851,8 +882,10 @@ size_t conv_smem_bytes(int cin, int cout) {
 int prepare_kernels() {
     // allow the largest dynamic shared memory a block may have, once, so that
     // launches (also inside stream capture) make no other runtime call
-    const void *fns[4] = {(const void *)conv3x3_tc_kernel<SRC_DIRECT>, (const void *)conv3x3_tc_kernel<SRC_POOL>,
-                          (const void *)conv3x3_tc_kernel<SRC_UP>, (const void *)wgrad_tc_kernel};
+    std::vector<const void *> fns = {(const void *)wgrad_tc_kernel};
+#define TDE_CONV_FN(M, C) fns.push_back((const void *)conv3x3_tc_kernel<M, C>);
+    TDE_CONV_VARIANTS(TDE_CONV_FN)
+#undef TDE_CONV_FN
     for (const void *fn : fns) {
         cudaFuncAttributes fa;
         TDE_CUDA(cudaFuncGetAttributes(&fa, fn), "refiner: kernel attributes");
@@ -863,22 +896,17 @@ int prepare_kernels() {
     return TDE_OK;
 }
 
-int conv_blocks_per_sm(int cin, int cout, int *out) {
+int conv_blocks_per_sm(int mode, int cin, int cout, int *out) {
     // resident blocks per SM from the limits that apply: shared memory (with
     // the 1 KB the SM reserves per block), registers, and the tensor memory
     // each block allocates (2 accumulators)
+    const void *fn = conv_kernel_fn(mode, cin / 8);
+    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d input channels", mode, cin);
     cudaFuncAttributes fa;
-    TDE_CUDA(cudaFuncGetAttributes(&fa, (const void *)conv3x3_tc_kernel<SRC_DIRECT>), "refiner: kernel attributes");
-    int regs = 0;
-    for (const void *fn : {(const void *)conv3x3_tc_kernel<SRC_POOL>, (const void *)conv3x3_tc_kernel<SRC_UP>,
-                           (const void *)conv3x3_tc_kernel<SRC_DIRECT>}) {
-        cudaFuncAttributes f;
-        TDE_CUDA(cudaFuncGetAttributes(&f, fn), "refiner: kernel attributes");
-        regs = f.numRegs > regs ? f.numRegs : regs;
-    }
+    TDE_CUDA(cudaFuncGetAttributes(&fa, fn), "refiner: kernel attributes");
     const size_t per_block = conv_smem_bytes(cin, cout) + fa.sharedSizeBytes + 1024;
     int n = (int)(kSmemPerSM / per_block);
-    const int by_regs = 65536 / (((regs + 7) / 8) * 8 * kConvThreads);
+    const int by_regs = 65536 / (((fa.numRegs + 7) / 8) * 8 * kConvThreads);
     const int by_tmem = (int)(512u / (2 * tmem_cols(cout)));
     n = n < by_regs ? n : by_regs;
     n = n < by_tmem ? n : by_tmem;
@@ -912,10 +940,10 @@ int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t 
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e;
-    if (a.mode_a == SRC_POOL) e = cudaLaunchKernelEx(&cfg, conv3x3_tc_kernel<SRC_POOL>, a, rows);
-    else if (a.mode_a == SRC_UP) e = cudaLaunchKernelEx(&cfg, conv3x3_tc_kernel<SRC_UP>, a, rows);
-    else e = cudaLaunchKernelEx(&cfg, conv3x3_tc_kernel<SRC_DIRECT>, a, rows);
+    const void *fn = conv_kernel_fn(a.mode_a, cin / 8);
+    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d input channels", a.mode_a, cin);
+    void *args[] = {(void *)&a, (void *)&rows};
+    cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "refiner conv: %s", cudaGetErrorString(e));
     return check_launch("refiner conv");
 }

@@ -240,8 +240,8 @@ int tde_refiner_create(int max_batch, int rows, int cols, uint64_t seed, tde_ref
     st = prepare_kernels();
     for (int i = 0; i < kConvs && !st; ++i) {
         const int cin = kConv[i].ca + kConv[i].cb;
-        st = conv_blocks_per_sm(cin, kConv[i].cout, &r->fwd_per_sm[i]);
-        if (!st) st = conv_blocks_per_sm(kConv[i].cout, cin, &r->bwd_per_sm[i]);
+        st = conv_blocks_per_sm(kConv[i].mode, cin, kConv[i].cout, &r->fwd_per_sm[i]);
+        if (!st) st = conv_blocks_per_sm(SRC_DIRECT, kConv[i].cout, cin, &r->bwd_per_sm[i]);
     }
     if (st) {
         delete r;

@@ -56,7 +56,7 @@ struct WgradArgs {
 // Once per process and device, before any launch: shared-memory limits.
 int prepare_kernels();
 size_t conv_smem_bytes(int cin, int cout);
-int conv_blocks_per_sm(int cin, int cout, int *out);
+int conv_blocks_per_sm(int mode, int cin, int cout, int *out);
 // Launches only (no other runtime call), so it may be stream-captured.
 int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t s);
 int wgrad_blocks(int num_sms, int cin, int cout);
