@@ -25,6 +25,7 @@ struct RayParams {
     const uint8_t *neg_flags;  // per physical 8^3 brick: 0 = holds no negative value
     const uint8_t *super_flags;  // per physical 32^3 super-brick (null: no sample skipping)
     float inv_cell[3];
+    unsigned *touched;      // measurement runs: one bit per voxel record read
 };
 
 struct f3 { float x, y, z; };
@@ -51,14 +52,21 @@ __device__ __forceinline__ f3 along(const tde_point3f &o, f3 d, float t) {
 
 __device__ __forceinline__ int floor_sat(float v) { return __float2int_rd(v); }  // convert_int_sat_rtn
 
-template <int FMT>
+// A voxel record's value; measurement instantiations also mark the record.
+template <int FMT, bool STATS>
+__device__ __forceinline__ float load_rec(const void *vol, const RayParams &p, size_t addr) {
+    if (STATS) atomicOr(p.touched + (addr >> 5), 1u << (addr & 31));
+    return TsdfStore<FMT>::value(vol, addr, p.n);
+}
+
+template <int FMT, bool STATS>
 __device__ __forceinline__ float read_tsdf(const void *vol, const RayParams &p, int x, int y, int z) {
-    return TsdfStore<FMT>::value(vol, voxel_address(x, y, z, p.rb), p.n);
+    return load_rec<FMT, STATS>(vol, p, voxel_address(x, y, z, p.rb));
 }
 
 // interpolateTrilineary: raycast.cl:95-145, taking the quotients
 // point / Cell_Size (the reference computes each twice; the value is the same).
-template <int FMT>
+template <int FMT, bool STATS>
 __device__ __noinline__ float trilinear_q(const void *vol, const RayParams &p, f3 pt, float qx, float qy, float qz) {
     const tde_point3i &N = p.rb.voxels_size;
     int gx = floor_sat(qx), gy = floor_sat(qy), gz = floor_sat(qz);
@@ -81,36 +89,35 @@ __device__ __noinline__ float trilinear_q(const void *vol, const RayParams &p, f
     const size_t sy = (size_t)N.x, sz = (size_t)N.x * (size_t)N.y;
     const size_t r00 = (size_t)y0 * sy + (size_t)z0 * sz, r01 = (size_t)y0 * sy + (size_t)z1 * sz;
     const size_t r10 = (size_t)y1 * sy + (size_t)z0 * sz, r11 = (size_t)y1 * sy + (size_t)z1 * sz;
-    typedef TsdfStore<FMT> S;
-    float v000 = S::value(vol, x0 + r00, p.n), v001 = S::value(vol, x0 + r01, p.n);
-    float v010 = S::value(vol, x0 + r10, p.n), v011 = S::value(vol, x0 + r11, p.n);
-    float v100 = S::value(vol, x1 + r00, p.n), v101 = S::value(vol, x1 + r01, p.n);
-    float v110 = S::value(vol, x1 + r10, p.n), v111 = S::value(vol, x1 + r11, p.n);
+    float v000 = load_rec<FMT, STATS>(vol, p, x0 + r00), v001 = load_rec<FMT, STATS>(vol, p, x0 + r01);
+    float v010 = load_rec<FMT, STATS>(vol, p, x0 + r10), v011 = load_rec<FMT, STATS>(vol, p, x0 + r11);
+    float v100 = load_rec<FMT, STATS>(vol, p, x1 + r00), v101 = load_rec<FMT, STATS>(vol, p, x1 + r01);
+    float v110 = load_rec<FMT, STATS>(vol, p, x1 + r10), v111 = load_rec<FMT, STATS>(vol, p, x1 + r11);
     float one_a = 1.f - a, one_b = 1.f - b, one_c = 1.f - c;
     float xa = one_b * (v000 * one_c + v001 * c) + b * (v010 * one_c + v011 * c);
     float xb = one_b * (v100 * one_c + v101 * c) + b * (v110 * one_c + v111 * c);
     return one_a * xa + a * xb;
 }
 
-template <int FMT>
+template <int FMT, bool STATS>
 __device__ __forceinline__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
-    return trilinear_q<FMT>(vol, p, pt, pt.x / p.cell.x, pt.y / p.cell.y, pt.z / p.cell.z);
+    return trilinear_q<FMT, STATS>(vol, p, pt, pt.x / p.cell.x, pt.y / p.cell.y, pt.z / p.cell.z);
 }
 
 // Zero crossing between time_curr and time_curr + step: secant refinement of
 // the hit and central-difference normal (raycast.cl:280-401).  Kept out of
 // line: it runs once per ray, and inlining it would bloat the march loop past
 // the instruction cache.
-template <int FMT>
+template <int FMT, bool STATS>
 __device__ __noinline__ void refine_surface(const void *vol, const RayParams &p, f3 dir, float time_curr,
                                             float &vx_out, float &vy_out, float &vz_out, float &nx_out,
                                             float &ny_out, float &nz_out) {
     const tde_point3i N = p.rb.voxels_size;
     const float step = p.time_step;
     float ct = time_curr + step;
-    float Ftdt = trilinear<FMT>(vol, p, along(p.t, dir, ct));
+    float Ftdt = trilinear<FMT, STATS>(vol, p, along(p.t, dir, ct));
     if (isnan(Ftdt)) return;
-    float Ft = trilinear<FMT>(vol, p, along(p.t, dir, time_curr));
+    float Ft = trilinear<FMT, STATS>(vol, p, along(p.t, dir, time_curr));
     if (isnan(Ft)) return;
     float Ts = time_curr - step * Ft / (Ftdt - Ft);
     f3 vf = along(p.t, dir, Ts);
@@ -122,16 +129,16 @@ __device__ __noinline__ void refine_surface(const void *vol, const RayParams &p,
         const float qx = vf.x / p.cell.x, qy = vf.y / p.cell.y, qz = vf.z / p.cell.z;
         f3 t1 = vf, t2 = vf;
         t1.x = t1.x + p.cell.x; t2.x = t2.x - p.cell.x;
-        const float Fx1 = trilinear_q<FMT>(vol, p, t1, t1.x / p.cell.x, qy, qz);
-        const float Fx2 = trilinear_q<FMT>(vol, p, t2, t2.x / p.cell.x, qy, qz);
+        const float Fx1 = trilinear_q<FMT, STATS>(vol, p, t1, t1.x / p.cell.x, qy, qz);
+        const float Fx2 = trilinear_q<FMT, STATS>(vol, p, t2, t2.x / p.cell.x, qy, qz);
         t1 = vf; t2 = vf;
         t1.y = t1.y + p.cell.y; t2.y = t2.y - p.cell.y;
-        const float Fy1 = trilinear_q<FMT>(vol, p, t1, qx, t1.y / p.cell.y, qz);
-        const float Fy2 = trilinear_q<FMT>(vol, p, t2, qx, t2.y / p.cell.y, qz);
+        const float Fy1 = trilinear_q<FMT, STATS>(vol, p, t1, qx, t1.y / p.cell.y, qz);
+        const float Fy2 = trilinear_q<FMT, STATS>(vol, p, t2, qx, t2.y / p.cell.y, qz);
         t1 = vf; t2 = vf;
         t1.z = t1.z + p.cell.z; t2.z = t2.z - p.cell.z;
-        const float Fz1 = trilinear_q<FMT>(vol, p, t1, qx, qy, t1.z / p.cell.z);
-        const float Fz2 = trilinear_q<FMT>(vol, p, t2, qx, qy, t2.z / p.cell.z);
+        const float Fz1 = trilinear_q<FMT, STATS>(vol, p, t1, qx, qy, t1.z / p.cell.z);
+        const float Fz2 = trilinear_q<FMT, STATS>(vol, p, t2, qx, qy, t2.z / p.cell.z);
         f3 n = normalized(f3{Fx1 - Fx2, Fy1 - Fy2, Fz1 - Fz2});
         nx_out = n.x; ny_out = n.y; nz_out = n.z;
     }
@@ -161,7 +168,7 @@ __device__ __forceinline__ void sample_voxel(const RayParams &p, const f3 &dir, 
     sz = axis_floor(fmaf(rf.d[2], ct, rf.o[2]), p.t.z, dir.z, p.cell.z, ct);
 }
 
-template <int FMT, bool SKIP>
+template <int FMT, bool SKIP, bool STATS>
 __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
                                                      float *__restrict__ nmap, RayParams p) {
     // 16x16 pixels per block; each warp takes an 8x4 tile so its rays start
@@ -220,7 +227,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
         rf.d[0] = dir.x * p.inv_cell[0]; rf.d[1] = dir.y * p.inv_cell[1]; rf.d[2] = dir.z * p.inv_cell[2];
         // previous sample: its value when `known`, else only "non-negative";
         // its time lets the value be fetched when it turns out to matter
-        float tsdf = read_tsdf<FMT>(vol, p, gx, gy, gz);
+        float tsdf = read_tsdf<FMT, STATS>(vol, p, gx, gy, gz);
         bool known = true;
         float prev_ct = time_curr;
         const int nbx = (N.x + 7) >> 3, nby = (N.y + 7) >> 3;
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                     continue;
                 }
             }
-            cur = TsdfStore<FMT>::value(vol, addr, p.n);
+            cur = load_rec<FMT, STATS>(vol, p, addr);
             if (SKIP && !known) {
                 if (!(cur < 0.f)) {  // prev >= 0 and cur >= 0
                     tsdf = cur;
@@ -292,7 +299,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                 // the previous sample's sign decides a crossing: fetch it
                 int qx, qy, qz;
                 sample_voxel(p, dir, rf, prev_ct, qx, qy, qz);
-                tsdf = read_tsdf<FMT>(vol, p, qx, qy, qz);
+                tsdf = read_tsdf<FMT, STATS>(vol, p, qx, qy, qz);
             }
             const float tsdf_prev = tsdf;
             tsdf = cur;
@@ -300,7 +307,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
             prev_ct = ct;
             if (tsdf_prev < 0.f && tsdf > 0.f) break;
             if (tsdf_prev > 0.f && tsdf < 0.f) {
-                refine_surface<FMT>(vol, p, dir, time_curr, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
+                refine_surface<FMT, STATS>(vol, p, dir, time_curr, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
                 break;
             }
             time_curr = ct;
@@ -369,7 +376,8 @@ __global__ void transform_maps_kernel(const float *__restrict__ vs, const float 
 
 int launch_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f &t,
                    const tde_matrix3f &R, float trunc, const tde_intrinsics &intr, const tde_round_buffer &rb,
-                   const tde_point3f &cell, const CamPose *dpose, const uint8_t *neg_flags, cudaStream_t stream) {
+                   const tde_point3f &cell, const CamPose *dpose, const uint8_t *neg_flags, cudaStream_t stream,
+                   unsigned *touched) {
     RayParams p;
     p.dpose = dpose;
     p.neg_flags = neg_flags;
@@ -383,9 +391,16 @@ int launch_raycast(const void *volume, int format, float *vmap, float *nmap, con
     p.super_flags = (neg_flags && whole) ? neg_flags + brick_count(rb) : nullptr;
     dim3 block(256);
     dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, 16));
+    p.touched = touched;
     return dispatch_format(format, [&](auto F) {
-        if (neg_flags) raycast_kernel<decltype(F)::value, true><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
-        else raycast_kernel<decltype(F)::value, false><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+        constexpr int FM = decltype(F)::value;
+        if (touched) {
+            if (neg_flags) raycast_kernel<FM, true, true><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+            else raycast_kernel<FM, false, true><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+        } else {
+            if (neg_flags) raycast_kernel<FM, true, false><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+            else raycast_kernel<FM, false, false><<<grid, block, 0, stream>>>(volume, vmap, nmap, p);
+        }
         return check_launch("raycast");
     });
 }

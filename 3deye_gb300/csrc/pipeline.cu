@@ -507,6 +507,47 @@ int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {
     return TDE_OK;
 }
 
+__global__ void popcount_kernel(const unsigned *__restrict__ bits, size_t words, unsigned long long *count) {
+    unsigned long long c = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+        c += __popc(bits[i]);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(count, c);
+}
+
+int tde_pipeline_raycast_records(tde_pipeline *p, int skip_empty, uint64_t *records) {
+    if (!p || !records) return set_error(TDE_ERR_INVALID_ARG, "pipeline_raycast_records: null argument");
+    TDE_TRY(tde_pipeline_sync(p));
+    const size_t n = voxel_count(p->rb), words = (n + 31) / 32;
+    const int W = p->cfg.intr.cols, H = p->cfg.intr.rows;
+    unsigned *bits = nullptr;
+    unsigned long long *cnt = nullptr;
+    float *vm = nullptr, *nm = nullptr;
+    int st = TDE_OK;
+    if (cudaMalloc((void **)&bits, words * 4) != cudaSuccess || cudaMalloc((void **)&cnt, 8) != cudaSuccess ||
+        cudaMalloc((void **)&vm, (size_t)W * H * 12) != cudaSuccess ||
+        cudaMalloc((void **)&nm, (size_t)W * H * 12) != cudaSuccess)
+        st = set_error(TDE_ERR_OOM, "pipeline_raycast_records: allocation");
+    if (st == TDE_OK) {
+        cudaMemsetAsync(bits, 0, words * 4, p->stream);
+        cudaMemsetAsync(cnt, 0, 8, p->stream);
+        tde_point3f t0{0, 0, 0};
+        tde_matrix3f R0{};
+        st = launch_raycast(p->volume, p->cfg.tsdf_format, vm, nm, t0, R0, p->cfg.trunc, p->intr[0], p->rb, p->cell,
+                            p->cam, skip_empty ? p->negflags : nullptr, p->stream, bits);
+        if (st == TDE_OK) {
+            popcount_kernel<<<1024, 256, 0, p->stream>>>(bits, words, cnt);
+            unsigned long long h = 0;
+            if (cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, p->stream) != cudaSuccess ||
+                cudaStreamSynchronize(p->stream) != cudaSuccess)
+                st = set_error(TDE_ERR_CUDA, "pipeline_raycast_records: %s", cudaGetErrorString(cudaGetLastError()));
+            *records = h;
+        }
+    }
+    cudaFree(bits); cudaFree(cnt); cudaFree(vm); cudaFree(nm);
+    return st;
+}
+
 int tde_pipeline_model_depth(tde_pipeline *p, uint16_t *out) {
     if (!p || !out) return set_error(TDE_ERR_INVALID_ARG, "pipeline_model_depth: null argument");
     const int n = p->cfg.intr.cols * p->cfg.intr.rows;

@@ -15,7 +15,8 @@ int launch_normal_map(const float *vmap, float *nmap, int W, int H, cudaStream_t
 
 int launch_raycast(const void *volume, int format, float *vmap, float *nmap, const tde_point3f &t,
                    const tde_matrix3f &R, float trunc, const tde_intrinsics &intr, const tde_round_buffer &rb,
-                   const tde_point3f &cell, const CamPose *dpose, const uint8_t *neg_flags, cudaStream_t stream);
+                   const tde_point3f &cell, const CamPose *dpose, const uint8_t *neg_flags, cudaStream_t stream,
+                   unsigned *touched = nullptr);  // touched: measurement bitmap of records read, or null
 int launch_resize_map(const float *src, float *dst, int sc, int sr, bool normal, cudaStream_t stream);
 int launch_transform_maps(const float *vs, const float *ns, float *vd, float *nd, const tde_matrix3f &R,
                           const tde_point3f &t, int W, int H, cudaStream_t stream);

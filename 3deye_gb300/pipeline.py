@@ -37,6 +37,7 @@ declare("tde_pipeline_set_round_buffer", I, [P, C.POINTER(RoundBuffer)])
 declare("tde_pipeline_set_pose", I, [P, P])
 declare("tde_pipeline_set_refiner", I, [P, P])
 declare("tde_pipeline_model_depth", I, [P, P])
+declare("tde_pipeline_raycast_records", I, [P, I, C.POINTER(C.c_uint64)])
 declare("tde_pipeline_shift_needed", I, [P, F, F, P])
 declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 
@@ -187,6 +188,12 @@ class Pipeline:
                                      capacity, C.byref(n)))
         k = min(n.value, capacity)
         return pts[:k], w[:k], n.value
+
+    def raycast_records(self, skip_empty: bool = True) -> int:
+        """Distinct voxel records a raycast of the current model reads."""
+        n = C.c_uint64()
+        check(lib.tde_pipeline_raycast_records(self._h, int(skip_empty), C.byref(n)))
+        return n.value
 
     def model_depth(self, out_ptr: int):
         """Enqueue: the last frame's model surface as depth in mm (device uint16)."""

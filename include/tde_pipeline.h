@@ -117,6 +117,13 @@ int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, in
 int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, uint32_t capacity,
                        uint32_t *count);
 
+/* Measurement: casts the current model again from the last frame's pose
+ * (into scratch maps) and counts the distinct voxel records the raycast
+ * reads -- with skip_empty, as the pipeline's raycast does (skipping bricks
+ * that hold no negative value), else as the reference algorithm does (every
+ * sample read).  Host-synchronous; allocates scratch. */
+int tde_pipeline_raycast_records(tde_pipeline *p, int skip_empty, uint64_t *records);
+
 /* Enqueues on the pipeline's stream: the model surface of the last frame
  * (its raycast, at the pose it was tracked to) as depth along the camera axis
  * in mm, 0 where the ray found no surface -- the target of the learned

@@ -159,9 +159,11 @@ static v3 along(const float *o, v3 d, float t) {
     v3 r = {o[0] + d.x * t, o[1] + d.y * t, o[2] + d.z * t};
     return r;
 }
-typedef struct { const void *vol; vol_t v; const tde_round_buffer *rb; const float *cell; } rc_ctx;
+typedef struct { const void *vol; vol_t v; const tde_round_buffer *rb; const float *cell; uint32_t *touched; } rc_ctx;
 static float rc_read(const rc_ctx *c, int x, int y, int z) {
-    return rec_value(c->vol, c->v, or_voxel_address(x, y, z, c->rb));
+    const size_t a = or_voxel_address(x, y, z, c->rb);
+    if (c->touched) __atomic_fetch_or(c->touched + (a >> 5), 1u << (a & 31), __ATOMIC_RELAXED);
+    return rec_value(c->vol, c->v, a);
 }
 /* interpolateTrilineary: raycast.cl:95-145 */
 static float rc_trilinear(const rc_ctx *c, v3 p) {
@@ -188,9 +190,29 @@ static float rc_trilinear(const rc_ctx *c, v3 p) {
     return oa * x0 + a * x1;
 }
 
+static int raycast_impl(const void *vol, int fmt, float *vmap, float *nmap, const float *t, const float *R, float trunc,
+                        const tde_intrinsics *intr, const tde_round_buffer *rb, const float *cell, uint32_t *touched);
+
 int or_raycast(const void *vol, int fmt, float *vmap, float *nmap, const float *t, const float *R, float trunc,
                const tde_intrinsics *intr, const tde_round_buffer *rb, const float *cell) {
-    rc_ctx c = {vol, {fmt, vox_count(rb)}, rb, cell};
+    return raycast_impl(vol, fmt, vmap, nmap, t, R, trunc, intr, rb, cell, NULL);
+}
+
+/* The raycast of or_raycast, also marking every voxel record it reads in
+ * `touched` (one bit per record); returns the number of distinct records. */
+int64_t or_raycast_records(const void *vol, int fmt, float *vmap, float *nmap, const float *t, const float *R,
+                           float trunc, const tde_intrinsics *intr, const tde_round_buffer *rb, const float *cell,
+                           uint32_t *touched) {
+    raycast_impl(vol, fmt, vmap, nmap, t, R, trunc, intr, rb, cell, touched);
+    int64_t n = 0;
+    const size_t words = (vox_count(rb) + 31) / 32;
+    for (size_t i = 0; i < words; ++i) n += __builtin_popcount(touched[i]);
+    return n;
+}
+
+static int raycast_impl(const void *vol, int fmt, float *vmap, float *nmap, const float *t, const float *R, float trunc,
+                        const tde_intrinsics *intr, const tde_round_buffer *rb, const float *cell, uint32_t *touched) {
+    rc_ctx c = {vol, {fmt, vox_count(rb)}, rb, cell, touched};
     const int W = intr->cols, H = intr->rows;
     const float step = (float)((double)trunc * 0.8);
     const tde_point3f V = rb->volume_size;

@@ -29,6 +29,9 @@ float or_half_to_float(uint16_t h);
 
 int or_raycast(const void *vol, int fmt, float *vmap, float *nmap, const float *t, const float *R, float trunc,
                const tde_intrinsics *intr, const tde_round_buffer *rb, const float *cell);
+int64_t or_raycast_records(const void *vol, int fmt, float *vmap, float *nmap, const float *t, const float *R,
+                           float trunc, const tde_intrinsics *intr, const tde_round_buffer *rb, const float *cell,
+                           uint32_t *touched);
 int or_bilateral(const uint16_t *src, uint16_t *dst, int W, int H, float ss, float sc, uint32_t max_mm,
                  float *ratio_out);
 int or_pyramid(const uint16_t *src, uint16_t *dst, int sW, int sH, float sigma_color);

@@ -76,6 +76,7 @@ _sigs = {
     "or_clean_tsdf_slice": (I, [P, I, P, P, pRB]),
     "or_clean_color_slice": (I, [P, P, P, pRB]),
     "or_set_threads": (I, [I]),
+    "or_raycast_records": (C.c_int64, [P, I, P, P, P, P, F, pI, pRB, P, P]),
     "or_scale_depth_f64": (I, [P, P, pI]),
     "or_integrate_f64": (I, [P, P, P, C.c_double, P, P, pI, P, pRB, I]),
     "or_raycast_f64": (I, [P, P, P, P, P, C.c_double, pI, pRB, P]),
@@ -97,6 +98,17 @@ def f32(a):
 def volume_bytes(fmt, rb: RB) -> int:
     n = rb.voxels_size[0] * rb.voxels_size[1] * rb.voxels_size[2]
     return n * (6 if fmt == 2 else 4)
+
+
+def raycast_records(vol, fmt, rb, intr, R, t, trunc, cell):
+    """Distinct voxel records the reference raycast reads (and its maps)."""
+    vm = np.empty((intr.rows, intr.cols, 3), F32)
+    nm = np.empty_like(vm)
+    n = int(rb.voxels_size[0]) * int(rb.voxels_size[1]) * int(rb.voxels_size[2])
+    bits = np.zeros((n + 31) // 32, np.uint32)
+    cnt = lib.or_raycast_records(_p(vol), fmt, _p(vm), _p(nm), _p(f32(t)), _p(f32(R)), trunc, C.byref(intr),
+                                 C.byref(rb), _p(f32(cell)), _p(bits))
+    return int(cnt), vm, nm
 
 
 def set_threads(n: int) -> int:

@@ -96,3 +96,30 @@ def test_tracking_loss_keeps_previous_pose(cuda, seq):
     pose3, st3 = p.process(depths[4])
     assert st3 == 0
     p.close()
+
+
+def test_raycast_record_count_matches_oracle(cuda, orc, tde, seq):
+    """The raycast's distinct voxel records (the numerator of its roofline):
+    the reference march counted on the GPU equals the oracle's count on the
+    same volume and pose; skipping empty bricks reads fewer."""
+    import ctypes as C
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    p = pl.Pipeline(cfg, traj[0])
+    for d in depths[:6]:
+        p.process(d)
+    full = p.raycast_records(skip_empty=False)
+    skipped = p.raycast_records(skip_empty=True)
+    vptr, rb = p.volume()
+    nbytes = int(tde.lib.tde_tsdf_volume_bytes(cfg.tsdf_format, C.byref(rb)))
+    vol = np.zeros(nbytes, np.uint8)
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    tde.check(tde.lib.tde_memcpy(vol.ctypes.data_as(C.c_void_p), vptr, nbytes, 1))
+    pose = p.pose()
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    orb = orc.RB.from_buffer_copy(bytes(rb))
+    cnt, _, _ = orc.raycast_records(vol, cfg.tsdf_format, orb, intr, pose[:9].astype(np.float32).reshape(3, 3),
+                                    pose[9:].astype(np.float32), cfg.trunc_m, np.full(3, cfg.cell, np.float32))
+    assert cnt == full > 0
+    assert 0 < skipped <= full
+    p.close()
