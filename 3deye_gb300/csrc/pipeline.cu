@@ -1,5 +1,12 @@
 // pipeline.cu -- the per-frame loop (tde_pipeline.h): buffers, the launch
 // sequence of one frame, its CUDA-graph capture, live timing.
+//
+// A frame's preprocessing (filter or refiner, pyramid, vertex and normal
+// maps) reads only that frame's depth, so it runs on a second stream into one
+// of two input sets while the previous frame is still tracked, integrated and
+// raycast on the main stream.  Per frame f, set f & 1:
+//   pre stream:  wait set_free[set]; upload depth; preprocessing; record pre_done[set]
+//   main stream: wait pre_done[set]; ICP, pose, integration, raycast; record set_free[set]
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -76,8 +83,8 @@ __global__ void model_depth_kernel(const float *__restrict__ vmap, const CamPose
 }
 
 enum Segment {
-    SEG_PRE,         // bilateral filter, pyramid, vertex and normal maps, ICP setup
-    SEG_ICP,         // the ICP iterations
+    SEG_PRE,         // bilateral filter, pyramid, vertex and normal maps
+    SEG_ICP,         // ICP setup and iterations
     SEG_POST_FIRST,  // pose publication without tracking (first frame), scaled depth, depth tiles
     SEG_POST,        // pose acceptance, scaled depth, depth tiles
     SEG_INTEGRATE,
@@ -99,14 +106,17 @@ struct tde_pipeline {
     tde_pipeline_config cfg;
     tde_round_buffer rb;
     tde_point3f cell;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // tracking and fusion
+    cudaStream_t pre_stream = nullptr;  // preprocessing of the next frame
+    cudaEvent_t pre_done[2] = {}, set_free[2] = {};
     int levels = 3;
     tde_intrinsics intr[3];
-    // device buffers
-    uint16_t *raw = nullptr;
-    uint16_t *depth[3] = {};
+    // device buffers; raw depth and the current-frame maps come in two sets
+    uint16_t *raw[2] = {};
+    uint16_t *depth[2][3] = {};
+    float *vcur[2][3] = {}, *ncur[2][3] = {};
     float *scaled = nullptr;
-    float *vcur[3] = {}, *ncur[3] = {}, *vmod[3] = {}, *nmod[3] = {};
+    float *vmod[3] = {}, *nmod[3] = {};
     float *gbuf = nullptr;
     IcpState *st = nullptr;
     PrevPose *prev = nullptr;
@@ -124,9 +134,9 @@ struct tde_pipeline {
     float *slab_weights = nullptr;
     uint32_t slab_capacity = 0;
     uint32_t *slab_count = nullptr;
-    // graphs: per segment and the whole frame
-    cudaGraphExec_t seg_exec[SEG_COUNT] = {};
-    cudaGraphExec_t full_exec[2] = {};  // [first frame, tracked frame]
+    // graphs per input set: each segment, and the main-stream part of a frame
+    cudaGraphExec_t seg_exec[2][SEG_COUNT] = {};
+    cudaGraphExec_t main_exec[2][2] = {};  // [set][first frame, tracked frame]
     bool captured = false;
     int frames = 0;
     // timing
@@ -141,33 +151,36 @@ template <class T> int dalloc(T **p, size_t count, const char *what) {
     return TDE_OK;
 }
 
-int record_segment(tde_pipeline *p, Segment seg) {
+// Records one segment for input set `set` onto stream s.
+int record_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
     const tde_pipeline_config &c = p->cfg;
-    cudaStream_t s = p->stream;
     const int W = c.intr.cols, H = c.intr.rows;
+    uint16_t *raw = p->raw[set], *const *depth = p->depth[set];
+    float *const *vcur = p->vcur[set], *const *ncur = p->ncur[set];
     switch (seg) {
     case SEG_PRE: {
         if (p->refiner) {
             // learned refinement replaces the bilateral filter; ICP and
             // integration both use the refined depth
-            TDE_TRY(tde_refiner_forward(p->refiner, p->raw, 1, p->depth[0], nullptr, s));
-            TDE_TRY(launch_vertex_map(p->depth[0], p->vcur[0], p->intr[0], s));
+            TDE_TRY(tde_refiner_forward(p->refiner, raw, 1, depth[0], nullptr, s));
+            TDE_TRY(launch_vertex_map(depth[0], vcur[0], p->intr[0], s));
         } else {
-            TDE_TRY(launch_bilateral(p->raw, p->depth[0], W, H, c.sigma_space, c.sigma_color, c.max_depth_mm,
-                                     p->vcur[0], &p->intr[0], s));
+            TDE_TRY(launch_bilateral(raw, depth[0], W, H, c.sigma_space, c.sigma_color, c.max_depth_mm, vcur[0],
+                                     &p->intr[0], s));
         }
         for (int l = 1; l < p->levels; ++l)
-            TDE_TRY(launch_pyramid(p->depth[l - 1], p->depth[l], p->intr[l - 1].cols, p->intr[l - 1].rows,
-                                   c.sigma_color, p->vcur[l], &p->intr[l], s));
+            TDE_TRY(launch_pyramid(depth[l - 1], depth[l], p->intr[l - 1].cols, p->intr[l - 1].rows, c.sigma_color,
+                                   vcur[l], &p->intr[l], s));
         for (int l = 0; l < p->levels; ++l)
-            TDE_TRY(launch_normal_map(p->vcur[l], p->ncur[l], p->intr[l].cols, p->intr[l].rows, s));
-        begin_frame_kernel<<<1, 1, 0, s>>>(p->st, p->prev);
-        return check_launch("begin_frame");
+            TDE_TRY(launch_normal_map(vcur[l], ncur[l], p->intr[l].cols, p->intr[l].rows, s));
+        return TDE_OK;
     }
     case SEG_ICP:
+        begin_frame_kernel<<<1, 1, 0, s>>>(p->st, p->prev);
+        TDE_TRY(check_launch("begin_frame"));
         for (int l = p->levels - 1; l >= 0; --l) {
             IcpArgs a;
-            a.vcur = p->vcur[l]; a.ncur = p->ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
+            a.vcur = vcur[l]; a.ncur = ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
             a.W = p->intr[l].cols; a.H = p->intr[l].rows;
             a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
             a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
@@ -179,7 +192,7 @@ int record_segment(tde_pipeline *p, Segment seg) {
     case SEG_POST:
         finalize_kernel<<<1, 1, 0, s>>>(p->st, p->prev, p->cam, p->out, seg == SEG_POST);
         TDE_TRY(check_launch("finalize_pose"));
-        TDE_TRY(launch_scale_depth(p->refiner ? p->depth[0] : p->raw, p->scaled, p->intr[0], s));
+        TDE_TRY(launch_scale_depth(p->refiner ? depth[0] : raw, p->scaled, p->intr[0], s));
         return launch_depth_max(p->scaled, W, H, static_cast<float *>(p->iscratch), s);
     case SEG_INTEGRATE: {
         IntegrateParams P;
@@ -205,11 +218,11 @@ int record_segment(tde_pipeline *p, Segment seg) {
     }
 }
 
-int capture(tde_pipeline *p, const Segment *segs, int n, cudaGraphExec_t *exec) {
+int capture(tde_pipeline *p, const Segment *segs, int n, int set, cudaGraphExec_t *exec) {
     cudaGraph_t g = nullptr;
     TDE_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     int st = TDE_OK;
-    for (int i = 0; i < n && st == TDE_OK; ++i) st = record_segment(p, segs[i]);
+    for (int i = 0; i < n && st == TDE_OK; ++i) st = record_segment(p, segs[i], set, p->stream);
     cudaError_t e = cudaStreamEndCapture(p->stream, &g);
     if (st != TDE_OK) {
         if (g) cudaGraphDestroy(g);
@@ -223,33 +236,45 @@ int capture(tde_pipeline *p, const Segment *segs, int n, cudaGraphExec_t *exec) 
 }
 
 void drop_graphs(tde_pipeline *p) {
-    for (auto &x : p->seg_exec)
-        if (x) { cudaGraphExecDestroy(x); x = nullptr; }
-    for (auto &x : p->full_exec)
-        if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    for (auto &row : p->seg_exec)
+        for (auto &x : row)
+            if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+    for (auto &row : p->main_exec)
+        for (auto &x : row)
+            if (x) { cudaGraphExecDestroy(x); x = nullptr; }
     p->captured = false;
 }
 
+// Main-stream segments of a frame, after its preprocessing.
+const Segment kMainFirst[] = {SEG_POST_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
+const Segment kMainTracked[] = {SEG_ICP, SEG_POST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
+
 int capture_all(tde_pipeline *p) {
     drop_graphs(p);
-    for (int sgi = 0; sgi < SEG_COUNT; ++sgi) {
-        Segment sg = (Segment)sgi;
-        TDE_TRY(capture(p, &sg, 1, &p->seg_exec[sgi]));
+    for (int set = 0; set < 2; ++set) {
+        for (int sgi = 0; sgi < SEG_COUNT; ++sgi) {
+            Segment sg = (Segment)sgi;
+            TDE_TRY(capture(p, &sg, 1, set, &p->seg_exec[set][sgi]));
+        }
+        TDE_TRY(capture(p, kMainFirst, 4, set, &p->main_exec[set][0]));
+        TDE_TRY(capture(p, kMainTracked, 5, set, &p->main_exec[set][1]));
     }
-    const Segment first[] = {SEG_PRE, SEG_POST_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
-    const Segment track[] = {SEG_PRE, SEG_ICP, SEG_POST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
-    TDE_TRY(capture(p, first, 5, &p->full_exec[0]));
-    TDE_TRY(capture(p, track, 6, &p->full_exec[1]));
     p->captured = true;
     return TDE_OK;
 }
 
-int run_segment(tde_pipeline *p, Segment s) {
+int run_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
     if (p->cfg.use_graphs) {
-        if (p->seg_exec[s]) TDE_CUDA(cudaGraphLaunch(p->seg_exec[s], p->stream), "graph launch");
+        TDE_CUDA(cudaGraphLaunch(p->seg_exec[set][seg], s), "graph launch");
         return TDE_OK;
     }
-    return record_segment(p, s);
+    return record_segment(p, seg, set, s);
+}
+
+int sync_streams(tde_pipeline *p) {
+    if (p->pre_stream) TDE_CUDA(cudaStreamSynchronize(p->pre_stream), "pipeline sync");
+    TDE_CUDA(cudaStreamSynchronize(p->stream), "pipeline sync");
+    return TDE_OK;
 }
 
 int write_pose(tde_pipeline *p, const double *pose12) {
@@ -266,16 +291,23 @@ int write_pose(tde_pipeline *p, const double *pose12) {
 
 void release(tde_pipeline *p) {
     if (!p) return;
+    if (p->pre_stream) cudaStreamSynchronize(p->pre_stream);
     if (p->stream) cudaStreamSynchronize(p->stream);
     drop_graphs(p);
     for (auto e : p->ev) cudaEventDestroy(e);
-    cudaFree(p->raw);
-    for (int l = 0; l < 3; ++l) {
-        cudaFree(p->depth[l]); cudaFree(p->vcur[l]); cudaFree(p->ncur[l]); cudaFree(p->vmod[l]); cudaFree(p->nmod[l]);
+    for (int set = 0; set < 2; ++set) {
+        cudaFree(p->raw[set]);
+        for (int l = 0; l < 3; ++l) {
+            cudaFree(p->depth[set][l]); cudaFree(p->vcur[set][l]); cudaFree(p->ncur[set][l]);
+        }
+        if (p->pre_done[set]) cudaEventDestroy(p->pre_done[set]);
+        if (p->set_free[set]) cudaEventDestroy(p->set_free[set]);
     }
+    for (int l = 0; l < 3; ++l) { cudaFree(p->vmod[l]); cudaFree(p->nmod[l]); }
     cudaFree(p->scaled); cudaFree(p->gbuf); cudaFree(p->st); cudaFree(p->prev); cudaFree(p->cam); cudaFree(p->out);
     cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->iscratch); cudaFree(p->negflags);
     cudaFree(p->slab_scratch); cudaFree(p->slab_points); cudaFree(p->slab_weights); cudaFree(p->slab_count);
+    if (p->pre_stream) cudaStreamDestroy(p->pre_stream);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -314,13 +346,28 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     auto fail = [&](int code) { release(p); return code; };
     cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(cuda_fail(e, "stream"));
+    e = cudaStreamCreateWithFlags(&p->pre_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "stream"));
+    for (int set = 0; set < 2; ++set) {
+        if ((e = cudaEventCreateWithFlags(&p->pre_done[set], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&p->set_free[set], cudaEventDisableTiming)) != cudaSuccess)
+            return fail(cuda_fail(e, "event"));
+    }
     const size_t npx = (size_t)c.intr.cols * c.intr.rows;
-    if ((st = dalloc(&p->raw, npx, "raw depth")) || (st = dalloc(&p->scaled, npx, "scaled depth"))) return fail(st);
+    if ((st = dalloc(&p->scaled, npx, "scaled depth"))) return fail(st);
+    for (int set = 0; set < 2; ++set) {
+        if ((st = dalloc(&p->raw[set], npx, "raw depth"))) return fail(st);
+        for (int l = 0; l < p->levels; ++l) {
+            size_t n = (size_t)p->intr[l].cols * p->intr[l].rows;
+            if ((st = dalloc(&p->depth[set][l], n, "depth pyramid")) ||
+                (st = dalloc(&p->vcur[set][l], 3 * n, "vertex map")) ||
+                (st = dalloc(&p->ncur[set][l], 3 * n, "normal map")))
+                return fail(st);
+        }
+    }
     for (int l = 0; l < p->levels; ++l) {
         size_t n = (size_t)p->intr[l].cols * p->intr[l].rows;
-        if ((st = dalloc(&p->depth[l], n, "depth pyramid")) || (st = dalloc(&p->vcur[l], 3 * n, "vertex map")) ||
-            (st = dalloc(&p->ncur[l], 3 * n, "normal map")) || (st = dalloc(&p->vmod[l], 3 * n, "model vertices")) ||
-            (st = dalloc(&p->nmod[l], 3 * n, "model normals")))
+        if ((st = dalloc(&p->vmod[l], 3 * n, "model vertices")) || (st = dalloc(&p->nmod[l], 3 * n, "model normals")))
             return fail(st);
     }
     if ((st = dalloc(&p->gbuf, icp_gbuf_floats(c.intr.cols, c.intr.rows), "icp partials")) ||
@@ -358,24 +405,40 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
                          int *status_out) {
     if (!p || !depth) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enqueue: null argument");
     const size_t bytes = (size_t)p->cfg.intr.cols * p->cfg.intr.rows * sizeof(uint16_t);
-    TDE_CUDA(cudaMemcpyAsync(p->raw, depth, bytes, depth_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                             p->stream),
-             "depth upload");
+    const cudaMemcpyKind kind = depth_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const int set = p->frames & 1;
     const bool first = p->frames == 0;
     const bool timed = p->timing_n < p->timing_cap;
-    if (p->cfg.use_graphs && !timed) {
-        TDE_CUDA(cudaGraphLaunch(p->full_exec[first ? 0 : 1], p->stream), "graph launch");
-    } else {
-        cudaEvent_t *ev = timed ? &p->ev[kEvents * p->timing_n] : nullptr;
+    if (timed) {
+        // timed frames run serially on the main stream, so that each pair of
+        // events brackets one stage alone
+        cudaEvent_t *ev = &p->ev[kEvents * p->timing_n];
+        TDE_CUDA(cudaMemcpyAsync(p->raw[set], depth, bytes, kind, p->stream), "depth upload");
         const Segment order[kStages] = {SEG_PRE, SEG_ICP, first ? SEG_POST_FIRST : SEG_POST, SEG_INTEGRATE,
                                         SEG_RAYCAST, SEG_RESIZE};
-        if (ev) TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
+        TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
         for (int k = 0; k < kStages; ++k) {
-            if (!(first && order[k] == SEG_ICP)) TDE_TRY(run_segment(p, order[k]));
-            if (ev) TDE_CUDA(cudaEventRecord(ev[k + 1], p->stream), "event");
+            if (!(first && order[k] == SEG_ICP)) TDE_TRY(run_segment(p, order[k], set, p->stream));
+            TDE_CUDA(cudaEventRecord(ev[k + 1], p->stream), "event");
         }
-        if (timed) p->timing_n++;
+        p->timing_n++;
+    } else {
+        // preprocessing on the second stream, once the frame two back no
+        // longer reads this input set
+        TDE_CUDA(cudaStreamWaitEvent(p->pre_stream, p->set_free[set], 0), "wait");
+        TDE_CUDA(cudaMemcpyAsync(p->raw[set], depth, bytes, kind, p->pre_stream), "depth upload");
+        TDE_TRY(run_segment(p, SEG_PRE, set, p->pre_stream));
+        TDE_CUDA(cudaEventRecord(p->pre_done[set], p->pre_stream), "event");
+        TDE_CUDA(cudaStreamWaitEvent(p->stream, p->pre_done[set], 0), "wait");
+        if (p->cfg.use_graphs) {
+            TDE_CUDA(cudaGraphLaunch(p->main_exec[set][first ? 0 : 1], p->stream), "graph launch");
+        } else {
+            const Segment *segs = first ? kMainFirst : kMainTracked;
+            const int n = first ? 4 : 5;
+            for (int k = 0; k < n; ++k) TDE_TRY(record_segment(p, segs[k], set, p->stream));
+        }
     }
+    TDE_CUDA(cudaEventRecord(p->set_free[set], p->stream), "event");
     if (pose_out12)
         TDE_CUDA(cudaMemcpyAsync(pose_out12, p->out->pose, sizeof(p->out->pose), cudaMemcpyDeviceToHost, p->stream),
                  "pose download");
@@ -388,8 +451,7 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
 
 int tde_pipeline_sync(tde_pipeline *p) {
     if (!p) return set_error(TDE_ERR_INVALID_ARG, "pipeline_sync: null");
-    TDE_CUDA(cudaStreamSynchronize(p->stream), "pipeline sync");
-    return TDE_OK;
+    return sync_streams(p);
 }
 
 int tde_pipeline_process(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose12, int *status) {
@@ -429,9 +491,10 @@ int tde_pipeline_model_maps(tde_pipeline *p, int level, const float **vmap, cons
 int tde_pipeline_frame_maps(tde_pipeline *p, int level, const uint16_t **depth, const float **vmap,
                             const float **nmap) {
     if (!p || level < 0 || level >= p->levels) return set_error(TDE_ERR_INVALID_ARG, "pipeline_frame_maps: level");
-    if (depth) *depth = p->depth[level];
-    if (vmap) *vmap = p->vcur[level];
-    if (nmap) *nmap = p->ncur[level];
+    const int set = p->frames > 0 ? (p->frames - 1) & 1 : 0;  // the last enqueued frame's set
+    if (depth) *depth = p->depth[set][level];
+    if (vmap) *vmap = p->vcur[set][level];
+    if (nmap) *nmap = p->ncur[set][level];
     return TDE_OK;
 }
 
@@ -669,8 +732,8 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
     for (int a = 0; a < 3; ++a) cam.t[a] = (float)pose[9 + a];
     cam.tracking_ok = 1;
     TDE_CUDA(cudaMemcpyAsync(p->cam, &cam, sizeof(cam), cudaMemcpyHostToDevice, s), "pipeline_shift: camera");
-    TDE_TRY(record_segment(p, SEG_RAYCAST));
-    TDE_TRY(record_segment(p, SEG_RESIZE));
+    TDE_TRY(record_segment(p, SEG_RAYCAST, 0, s));
+    TDE_TRY(record_segment(p, SEG_RESIZE, 0, s));
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift");
     if (p->cfg.use_graphs) return capture_all(p);
     return TDE_OK;

@@ -50,7 +50,11 @@ typedef struct tde_pipeline_config {
  * row-major R (camera -> volume frame) then t (camera centre), FP64. */
 int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, tde_pipeline **out);
 int tde_pipeline_destroy(tde_pipeline *p);
-/* The stream all of the pipeline's work runs on. */
+/* The pipeline's main stream (tracking, fusion, pose downloads, and every
+ * call other than tde_pipeline_enqueue).  A frame's upload and preprocessing
+ * run on a second, internal stream that overlaps the previous frame's
+ * tracking; the main stream waits for them before the frame's tracking, so
+ * work ordered after the main stream sees every enqueued frame complete. */
 void *tde_pipeline_stream(tde_pipeline *p);
 
 /* Enqueue one frame.  `depth` is cols x rows uint16 millimetres, on the host

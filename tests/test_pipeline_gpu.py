@@ -1,6 +1,7 @@
 """The per-frame pipeline (include/tde_pipeline.h) on the GPU against the CPU
 oracle pipeline (FP64 ICP sums and solve) and against itself (graph replay
 vs eager launches, asynchronous vs blocking API)."""
+import ctypes as C
 import importlib
 
 import numpy as np
@@ -77,6 +78,39 @@ def test_async_enqueue_matches_blocking(cuda, seq):
     r, w = p.integrate_stats()
     assert r > 0 and 0 < w <= r
     assert p.launches_per_frame() == 36
+    p.close()
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_overlapped_preprocessing_matches_blocking(cuda, tde, seq, use_graphs):
+    """Frames enqueued back to back: each frame's upload and preprocessing run
+    on the second stream into alternating input sets while the previous frame
+    is tracked; the poses equal the one-frame-at-a-time run bit for bit, and
+    the last frame's maps are those of the last frame."""
+    import torch
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    ref, _ = run_gpu(cfg, traj, depths)
+    host = torch.from_numpy(np.stack(depths)).pin_memory()
+    poses = torch.zeros((len(depths), 12), dtype=torch.float64).pin_memory()
+    status = torch.zeros(len(depths), dtype=torch.int32).pin_memory()
+    p = pl.Pipeline(cfg, traj[0], use_graphs=use_graphs)
+    fb = cfg.rows * cfg.cols * 2
+    for i in range(len(depths)):
+        p.enqueue(host.data_ptr() + i * fb, False, poses.data_ptr() + 96 * i, status.data_ptr() + 4 * i)
+    p.sync()
+    assert np.array_equal(poses.numpy(), ref)
+    assert not status.numpy().any()
+    nbytes = cfg.rows * cfg.cols * 2
+    q = pl.Pipeline(cfg, traj[0], use_graphs=use_graphs)
+    q.process(depths[-1])
+    last = [np.zeros(nbytes, np.uint8) for _ in range(2)]
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    for buf, pipe in zip(last, (p, q)):
+        ptr = pipe.frame_maps(0)[0]
+        tde.check(tde.lib.tde_memcpy(buf.ctypes.data_as(C.c_void_p), C.c_void_p(ptr), nbytes, 1))
+    assert np.array_equal(last[0], last[1]) and last[0].any()
+    q.close()
     p.close()
 
 
