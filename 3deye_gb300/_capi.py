@@ -100,6 +100,7 @@ _SIGS = {
     "tde_transform_estimation": (I, [P, P, I, I, P]),
     "tde_clean_buff": (I, [P, I, P]),
     "tde_icp_solve_update_host": (I, [P, P, P, P]),
+    "tde_icp_solve_device": (I, [P, I, P, P, P, P]),
     "tde_scale_depth": (I, [P, P, pI, P]),
     "tde_integrate_tsdf": (I, [P, P, I, F, pM, pV, pI, pV, pRB, I, P]),
     "tde_raycast": (I, [P, I, P, P, pV, pM, F, pI, pRB, pV, P]),

@@ -200,7 +200,7 @@ int tde_estimate_combined(const float *vmap_cur, const float *nmap_cur, const fl
     a.W = intr->cols; a.H = intr->rows;
     a.fx = intr->fx; a.fy = intr->fy; a.cx = intr->cx; a.cy = intr->cy;
     a.dist_thresh = dist_thresh; a.angle_thresh = angle_thresh;
-    int st_code = launch_icp(a, st, gbuf, mbuf, false, false, s);
+    int st_code = launch_icp(a, st, mbuf, s);
     if (st_code) return st_code;
     // the host copy of h must outlive the async copy above
     e = cudaStreamSynchronize(s);
@@ -217,6 +217,12 @@ int tde_transform_estimation(const float *gbuf, float *out, int buf_length, int 
 int tde_clean_buff(float *gbuf, int width, void *stream) {
     TDE_REQUIRE(gbuf && width > 0, "clean_buff: bad arguments");
     return launch_clean_buff(gbuf, width, as_stream(stream));
+}
+
+int tde_icp_solve_device(const double *sums28, int n, double *pose12, double *x6, int *ok, void *stream) {
+    TDE_REQUIRE(n >= 0, "icp_solve_device: n < 0");
+    TDE_REQUIRE(n == 0 || (sums28 && pose12 && x6 && ok), "icp_solve_device: null argument");
+    return launch_icp_solve(sums28, n, pose12, x6, ok, as_stream(stream));
 }
 
 int tde_icp_solve_update_host(const float *mbuf27, double *R9, double *t3, double *x6) {

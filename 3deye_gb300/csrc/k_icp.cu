@@ -6,20 +6,27 @@
 // each block's totals as float-float values; each block adds them, converted
 // exactly to 126-bit fixed point, into integer accumulators with atomics --
 // integer addition is associative, so the grid total is the same bits in any
-// block order; the last block to finish reads the totals and, in the pipeline
-// form, solves the 6x6 system to FP64 accuracy and updates the device pose.
+// block order.
+//
+// Pipeline form: launch i's blocks, once the programmatic dependency on
+// launch i - 1 has resolved (its atomics complete and visible), read its
+// exact totals and solve the 6x6 system in FP64 themselves -- every block the
+// same operations on the same bits, so the same pose -- instead of a last
+// block of launch i - 1 solving after a grid-wide ticket.  That takes the
+// ticket, its fence and one dependent read off every iteration; only the
+// frame's last launch keeps the ticket, to solve its own totals.
 //
 // Built with -fmad=false so the per-pixel association and terms are the same
 // IEEE float operations as the CPU oracle: inlier sets match exactly.
 #include "tde_common.cuh"
 #include "tde_icp.cuh"
+#include "tde_integrate.cuh"
 
 namespace tde {
 namespace {
 
 constexpr int kThreads = 256;
 constexpr int kPixPerThread = 4;
-constexpr int kTailSlices = 9;  // 9 x 28 = 252 threads of the last block
 
 struct f2 { float hi, lo; };
 
@@ -98,13 +105,13 @@ __device__ __forceinline__ bool pair_terms(const IcpArgs &a, const Assoc &s, flo
 }
 
 // ---------------------------------------------------------------------------
-// FP64 solve and pose update, run by one warp of the last block.
+// FP64 solve and pose update, run by one warp per block.
 //
 // GB300 executes FP64 at a small fraction of the FP32 rate (a dependent DFMA
-// takes ~64 cycles, a double reciprocal ~430, sqrt ~670, sincos ~1600), so the
-// solve is arranged for latency: 3x3 blocks with adjugate inverses (two
-// divisions, no square roots, short chains of 3-term dot products spread
-// over lanes), and the SO(3) exponential from its Taylor series when the
+// takes ~64 cycles, sqrt ~670, sincos ~1600), so the solve is arranged for
+// latency: 3x3 blocks with adjugate inverses, lanes exchanging values by
+// shuffles only, reciprocals from the hardware approximation refined by
+// Newton steps, and the SO(3) exponential from its Taylor series when the
 // rotation step is small.
 // ---------------------------------------------------------------------------
 // A(theta) = sin(theta)/theta, B(theta) = (1 - cos(theta))/theta^2.
@@ -122,123 +129,103 @@ __device__ __forceinline__ void rodrigues_coeffs(double th2, double &A, double &
 
 // Term index of entry (r, c) of [A | b] in the 27-term upper-triangular
 // order of opencl_wrappers.cpp:426-437 (row k holds columns k..6).
-__device__ __forceinline__ int term_index(int r, int c) {
+__host__ __device__ __forceinline__ int term_index(int r, int c) {
     const int k = r < c ? r : c, j = r < c ? c : r;  // A is symmetric
     return k * 7 - (k * (k - 1)) / 2 + (j - k);
 }
 
-// Cofactor (r, c) of a symmetric 3x3 matrix held row-major in M; the cyclic
-// index form gives the sign.  adj(M) = cofactors (symmetric M).
-__device__ __forceinline__ double cofactor3(const double *M, int r, int c) {
+// 1/d for a positive normal d: the hardware approximation, then Newton-
+// Raphson x <- x + x (1 - d x), each step squaring the relative error
+// (three steps from the approximation's ~2^-20 leave rounding error only).
+__device__ __forceinline__ double rcp_nr(double d) {
+    double x;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) x = fma(x, fma(-d, x, 1.0), x);
+    return x;
+}
+
+__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double pick3(int i, double a, double b, double c) { return i == 0 ? a : (i == 1 ? b : c); }
+
+// One Gauss-Newton step, executed by all 32 lanes of a warp.  Lane l < 28
+// holds term l of [A | b] (27 terms, then the inlier count).  With
+// A = [[P, Q], [Q^T, R]]: S = R - Q^T P^-1 Q, x2 = S^-1 (b2 - Q^T P^-1 b1),
+// x1 = P^-1 (b1 - Q x2), each 3x3 inverse as adjugate / determinant.  The
+// pose (R_old, t_old: shared, FP64) moves by exp([x1]x), x2:
+//   R <- R + A (w x R) + B (w (w . R) - th2 R)   column by column, and
+//   t <- t + A (w x t) + B (w (w . t) - th2 t) + x2,   w = x1.
+// Lane l < 9 returns entry l of the new R (row-major) in `out`, lanes 9..11
+// entry l - 9 of the new t; lane l < 6 returns x[l] in `xl`.  False (out =
+// the old entry) when A is not positive definite (a pivot of P or S at or
+// below 1e-30, tested through the leading minors).
+__device__ bool warp_solve_step(double term, const double *R_old, const double *t_old, int lane, double &out,
+                                double &xl) {
+    const bool vec = lane >= 9;                       // lanes 9..11: vector entries
+    const int vi = (lane >= 9 && lane < 12) ? lane - 9 : 0;
+    const int l9 = lane < 9 ? lane : 0;
+    const int r = l9 / 3, c = l9 % 3;
     const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-    return fma(M[3 * r1 + c1], M[3 * r2 + c2], -M[3 * r1 + c2] * M[3 * r2 + c1]);
-}
-
-// FP64 solve of the 6x6 system by 3x3 blocks: with A = [[P, Q], [Q^T, R]],
-// S = R - Q^T P^-1 Q, x2 = S^-1 (b2 - Q^T P^-1 b1), x1 = P^-1 b1 - P^-1 Q x2,
-// each 3x3 inverse as adjugate / determinant.  Two reciprocals and chains of
-// 3-term dot products keep the dependent FP64 latency short.  False when A is
-// not positive definite (a pivot of P or S at or below 1e-30, tested through
-// the leading minors).  Lanes 0..11 work; the result is in xo.
-__device__ bool fp64_block_solve(const double *sums, int lane, double (&xo)[6]) {
-    __shared__ double P[9], Q[9], R[9], b[6], CP[9], iP[9], T[9], S[9], CS[9], iS[9], u[3], w[3];
-    __shared__ int ok;
-    const int r = lane / 3, c = lane % 3;
-    if (lane < 9) {
-        P[lane] = sums[term_index(r, c)];
-        Q[lane] = sums[term_index(r, 3 + c)];
-        R[lane] = sums[term_index(3 + r, 3 + c)];
-    } else if (lane < 15) {
-        b[lane - 9] = sums[term_index(lane - 9, 6)];
+    // P^-1: cofactors (lane r, c), determinant through the first row
+    const double CP = fma(shfl(term, term_index(r1, c1)), shfl(term, term_index(r2, c2)),
+                          -(shfl(term, term_index(r1, c2)) * shfl(term, term_index(r2, c1))));
+    const double P0 = shfl(term, 0), P1 = shfl(term, 1), P2 = shfl(term, 2);
+    const double detP = fma(P0, shfl(CP, 0), fma(P1, shfl(CP, 1), P2 * shfl(CP, 2)));
+    const double CP8 = shfl(CP, 8);  // P00 P11 - P01^2
+    bool ok = P0 > 1e-30 && CP8 > 1e-30 * P0 && detP > 1e-30 * CP8;
+    const double iP = CP * rcp_nr(detP);
+    // T = Q^T P^-1 (lane r, c: sum_k Q(k, r) iP(k, c)); w = P^-1 b1 (lane 9 + i)
+    const int col = vec ? vi : c;
+    double TW = 0.0;
+    {
+        double a[3], g[3];
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            a[k] = shfl(term, vec ? term_index(k, 6) : term_index(k, 3 + r));
+            g[k] = shfl(iP, 3 * k + col);
+        }
+        TW = fma(a[0], g[0], fma(a[1], g[1], a[2] * g[2]));
     }
-    if (lane == 0) ok = 1;
-    __syncwarp();
-    if (lane < 9) CP[lane] = cofactor3(P, r, c);
-    __syncwarp();
-    // det P through the first row; leading minors P00, P00 P11 - P01^2 (= CP[8]), det P
-    const double detP = fma(P[0], CP[0], fma(P[1], CP[1], P[2] * CP[2]));
-    if (lane == 0 && !(P[0] > 1e-30 && CP[8] > 1e-30 * P[0] && detP > 1e-30 * CP[8])) ok = 0;
-    const double invP = 1.0 / detP;
-    if (lane < 9) iP[lane] = CP[lane] * invP;
-    __syncwarp();
-    // T = Q^T P^-1 (3x3), w = P^-1 b1
-    if (lane < 9) T[lane] = fma(Q[r], iP[c], fma(Q[3 + r], iP[3 + c], Q[6 + r] * iP[6 + c]));
-    else if (lane < 12) {
-        const int i = lane - 9;
-        w[i] = fma(iP[3 * i], b[0], fma(iP[3 * i + 1], b[1], iP[3 * i + 2] * b[2]));
+    // S = R - T Q (lane r, c); u = b2 - T b1 (lane 9 + i)
+    const int row = vec ? vi : r;
+    double SU;
+    {
+        const double base = shfl(term, vec ? term_index(3 + vi, 6) : term_index(3 + r, 3 + c));
+        double t[3], y[3];
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            t[k] = shfl(TW, 3 * row + k);
+            y[k] = shfl(term, vec ? term_index(k, 6) : term_index(k, 3 + c));
+        }
+        SU = fma(-t[0], y[0], fma(-t[1], y[1], fma(-t[2], y[2], base)));
     }
-    __syncwarp();
-    // S = R - T Q, u = b2 - T b1
-    if (lane < 9) S[lane] = R[lane] - fma(T[3 * r], Q[c], fma(T[3 * r + 1], Q[3 + c], T[3 * r + 2] * Q[6 + c]));
-    else if (lane < 12) {
-        const int i = lane - 9;
-        u[i] = b[3 + i] - fma(T[3 * i], b[0], fma(T[3 * i + 1], b[1], T[3 * i + 2] * b[2]));
-    }
-    __syncwarp();
-    if (lane < 9) CS[lane] = cofactor3(S, r, c);
-    __syncwarp();
-    const double detS = fma(S[0], CS[0], fma(S[1], CS[1], S[2] * CS[2]));
-    if (lane == 0 && !(S[0] > 1e-30 && CS[8] > 1e-30 * S[0] && detS > 1e-30 * CS[8])) ok = 0;
-    const double invS = 1.0 / detS;
-    if (lane < 9) iS[lane] = CS[lane] * invS;
-    __syncwarp();
-    // x2 = S^-1 u; x1 = w - T^T x2
-    if (lane < 3) xo[3 + lane] = fma(iS[3 * lane], u[0], fma(iS[3 * lane + 1], u[1], iS[3 * lane + 2] * u[2]));
-    __syncwarp();
-    if (lane < 3) xo[lane] = w[lane] - fma(T[lane], xo[3], fma(T[3 + lane], xo[4], T[6 + lane] * xo[5]));
-    __syncwarp();
-    return ok != 0;
-}
-
-// The pose a solve updates: FP64 estimate, its float mirror, the last step.
-struct PoseRefs {
-    double *R, *t;
-    float *Rf, *tf;
-    double *x;
-};
-
-// Solve and apply the update to the pose; false (pose unchanged) when A is
-// not positive definite.
-__device__ bool warp_solve_update(const PoseRefs &P, const double *sums, int lane) {
-    __shared__ double Rinc[9];
-    __shared__ double x[6];
-    if (!fp64_block_solve(sums, lane, x)) return false;
-    // Rinc = I + A [w]x + B (w w^T - th2 I), lanes 0..8 one entry each
-    const double wx = x[0], wy = x[1], wz = x[2];
+    // S^-1
+    const double CS = fma(shfl(SU, 3 * r1 + c1), shfl(SU, 3 * r2 + c2), -(shfl(SU, 3 * r1 + c2) * shfl(SU, 3 * r2 + c1)));
+    const double S0 = shfl(SU, 0);
+    const double detS = fma(S0, shfl(CS, 0), fma(shfl(SU, 1), shfl(CS, 1), shfl(SU, 2) * shfl(CS, 2)));
+    const double CS8 = shfl(CS, 8);
+    ok = ok && S0 > 1e-30 && CS8 > 1e-30 * S0 && detS > 1e-30 * CS8;
+    const double iS = CS * rcp_nr(detS);
+    // x2 = S^-1 u (lane 9 + i)
+    const double X2 = fma(shfl(iS, 3 * vi), shfl(SU, 9), fma(shfl(iS, 3 * vi + 1), shfl(SU, 10), shfl(iS, 3 * vi + 2) * shfl(SU, 11)));
+    // x1 = w - T^T x2 (lane 9 + i)
+    const double x20 = shfl(X2, 9), x21 = shfl(X2, 10), x22 = shfl(X2, 11);
+    const double X1 = fma(-shfl(TW, vi), x20, fma(-shfl(TW, 3 + vi), x21, fma(-shfl(TW, 6 + vi), x22, TW)));
+    const double wx = shfl(X1, 9), wy = shfl(X1, 10), wz = shfl(X1, 11);
+    xl = lane < 3 ? pick3(lane, wx, wy, wz) : pick3(lane - 3, x20, x21, x22);
+    // the pose update: this lane's column (of R, or t) and row
     const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
-    double Ac, Bc;
-    rodrigues_coeffs(th2, Ac, Bc);
-    if (lane < 9) {
-        const int r = lane / 3, c = lane % 3;
-        const double w[3] = {wx, wy, wz};
-        double e = Bc * w[r] * w[c];
-        if (r == c) e += fma(-Bc, th2, 1.0);
-        // skew part: [w]x = [[0,-wz,wy],[wz,0,-wx],[-wy,wx,0]]
-        const double sk = (r == 0 && c == 1) ? -wz : (r == 0 && c == 2) ? wy : (r == 1 && c == 0) ? wz
-                        : (r == 1 && c == 2) ? -wx : (r == 2 && c == 0) ? -wy : (r == 2 && c == 1) ? wx : 0.0;
-        Rinc[lane] = fma(Ac, sk, e);
-    }
-    __syncwarp();
-    // R <- Rinc R, t <- Rinc t + v (lanes 0..8 rotation, 9..11 translation)
-    double out = 0.0;
-    if (lane < 9) {
-        const int r = lane / 3, c = lane % 3;
-        out = fma(Rinc[3 * r], P.R[c], fma(Rinc[3 * r + 1], P.R[3 + c], Rinc[3 * r + 2] * P.R[6 + c]));
-    } else if (lane < 12) {
-        const int r = lane - 9;
-        out = fma(Rinc[3 * r], P.t[0], fma(Rinc[3 * r + 1], P.t[1], fma(Rinc[3 * r + 2], P.t[2], x[3 + r])));
-    }
-    __syncwarp();
-    if (lane < 9) { P.R[lane] = out; P.Rf[lane] = (float)out; }
-    else if (lane < 12) { P.t[lane - 9] = out; P.tf[lane - 9] = (float)out; }
-    if (lane < 6) P.x[lane] = x[lane];
-    __syncwarp();
-    return true;
-}
-
-__device__ bool warp_solve_and_update(IcpState *st, const double *sums, int lane) {
-    const PoseRefs P{st->R, st->t, st->pose.R_cur, st->pose.t_cur, st->x};
-    return warp_solve_update(P, sums, lane);
+    double A, B;
+    rodrigues_coeffs(th2, A, B);
+    const double k0 = vec ? t_old[0] : R_old[c], k1 = vec ? t_old[1] : R_old[3 + c], k2 = vec ? t_old[2] : R_old[6 + c];
+    const double cr = pick3(row, fma(wy, k2, -(wz * k1)), fma(wz, k0, -(wx * k2)), fma(wx, k1, -(wy * k0)));
+    const double dt = fma(wx, k0, fma(wy, k1, wz * k2));
+    const double kr = pick3(row, k0, k1, k2);
+    const double M = fma(pick3(row, wx, wy, wz), dt, -(th2 * kr));
+    double o = fma(A, cr, fma(B, M, kr));
+    if (vec) o += pick3(vi, x20, x21, x22);
+    out = ok ? o : kr;
+    return ok;
 }
 
 // ---------------------------------------------------------------------------
@@ -298,37 +285,12 @@ __device__ __forceinline__ f2 warp_transpose_reduce(const float (&s)[32], int la
     return v[0];
 }
 
-template <bool SOLVE>
-__global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState *__restrict__ st,
-                                                       float *__restrict__ gbuf, float *__restrict__ mbuf) {
-    __shared__ IcpPose P;
-    __shared__ f2 red[kThreads / 32][32];
-    __shared__ unsigned ticket;
-    const int tid = threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5;
-    // Let the next ICP launch start: it only reads this launch's results
-    // (pose, accumulators, counter) after its own griddepcontrol.wait.
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-
-    const int npix = a.W * a.H;
-    const int base = blockIdx.x * kThreads * kPixPerThread + tid;
-    // this thread's current-frame maps do not depend on the pose: load them
-    // before waiting for the previous iteration
-    float3 nc[kPixPerThread], vc[kPixPerThread];
-    const float qnan = __int_as_float(0x7fffffff);
-    #pragma unroll
-    for (int k = 0; k < kPixPerThread; ++k) {
-        const int p = base + k * kThreads;
-        if (p < npix) { nc[k] = ld3(a.ncur, (size_t)p); vc[k] = ld3(a.vcur, (size_t)p); }
-        else { nc[k] = make_float3(qnan, qnan, qnan); vc[k] = nc[k]; }
-    }
-    // wait for the previous launch in the stream (a no-op without a
-    // programmatic dependency)
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    if (tid < (int)(sizeof(IcpPose) / sizeof(float)))
-        reinterpret_cast<float *>(&P)[tid] = reinterpret_cast<const float *>(&st->pose)[tid];
-    __syncthreads();
-
+// Association, the per-block sums, and their exact addition into
+// accumulator buffer `acc` (copy blockIdx % kIcpAccCopies).
+__device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose &P, const float3 (&nc)[kPixPerThread],
+                                                 const float3 (&vc)[kPixPerThread], f2 (*red)[32],
+                                                 unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3]) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float s[32];
     #pragma unroll
     for (int t = 0; t < 32; ++t) s[t] = 0.f;
@@ -360,50 +322,232 @@ __global__ void __launch_bounds__(kThreads) icp_kernel(const IcpArgs a, IcpState
         for (int w = 1; w < kThreads / 32; ++w) v = add_ff(v, red[w][tid]);
         const unsigned __int128 q = (unsigned __int128)(to_fixed(v.hi) + to_fixed(v.lo));
         const unsigned long long m42 = (1ull << 42) - 1ull;
-        unsigned long long *acc = st->acc[blockIdx.x % kIcpAccCopies][tid];
-        atomicAdd(acc + 0, (unsigned long long)q & m42);
-        atomicAdd(acc + 1, (unsigned long long)(q >> 42) & m42);
-        atomicAdd(acc + 2, (unsigned long long)(q >> 84) & m42);
+        unsigned long long *dst = (*acc)[blockIdx.x % kIcpAccCopies][tid];
+        atomicAdd(dst + 0, (unsigned long long)q & m42);
+        atomicAdd(dst + 1, (unsigned long long)(q >> 42) & m42);
+        atomicAdd(dst + 2, (unsigned long long)(q >> 84) & m42);
     }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) ticket = atomicAdd(&st->counter, 1u);
-    __syncthreads();
-    if (ticket != (unsigned)gridDim.x - 1) return;
+}
 
-    // ---- last block: read the exact integer totals, reset them, solve ----
-    __shared__ double s_sums[kIcpTerms];
+// Exact total of term `term` in accumulator buffer `acc` (all copies).
+__device__ __forceinline__ double read_total(const unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3], int term) {
+    unsigned long long v[kIcpAccCopies][3];
+    #pragma unroll
+    for (int c = 0; c < kIcpAccCopies; ++c)
+        #pragma unroll
+        for (int l = 0; l < 3; ++l) v[c][l] = __ldcg(&(*acc)[c][term][l]);
+    unsigned long long a0 = 0, a1 = 0, a2 = 0;
+    #pragma unroll
+    for (int c = 0; c < kIcpAccCopies; ++c) { a0 += v[c][0]; a1 += v[c][1]; a2 += v[c][2]; }
+    return from_fixed(a0, a1, a2);
+}
+
+// Last block of a launch: true for exactly one block, after every block's
+// atomics are complete.
+__device__ __forceinline__ bool last_block(IcpState *st, unsigned *ticket) {
     __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) *ticket = atomicAdd(&st->counter, 1u);
+    __syncthreads();
+    if (*ticket != gridDim.x - 1) return false;
+    __threadfence();
+    return true;
+}
+
+// Loads this thread's current-frame maps (independent of the pose).
+__device__ __forceinline__ void load_current(const IcpArgs &a, float3 (&nc)[kPixPerThread], float3 (&vc)[kPixPerThread]) {
+    const int npix = a.W * a.H;
+    const int base = blockIdx.x * kThreads * kPixPerThread + threadIdx.x;
+    const float qnan = __int_as_float(0x7fffffff);
+    #pragma unroll
+    for (int k = 0; k < kPixPerThread; ++k) {
+        const int p = base + k * kThreads;
+        if (p < npix) { nc[k] = ld3(a.ncur, (size_t)p); vc[k] = ld3(a.vcur, (size_t)p); }
+        else { nc[k] = make_float3(qnan, qnan, qnan); vc[k] = nc[k]; }
+    }
+}
+
+// One-shot sums for the pose in st->pose (the Estimate_Combined drop-in):
+// the last block writes the exact totals to st->sums / mbuf and resets the
+// accumulators.
+__global__ void __launch_bounds__(kThreads) icp_sums_kernel(const IcpArgs a, IcpState *__restrict__ st,
+                                                            float *__restrict__ mbuf) {
+    __shared__ IcpPose P;
+    __shared__ f2 red[kThreads / 32][32];
+    __shared__ unsigned ticket;
+    const int tid = threadIdx.x;
+    float3 nc[kPixPerThread], vc[kPixPerThread];
+    load_current(a, nc, vc);
+    if (tid < (int)(sizeof(IcpPose) / sizeof(float)))
+        reinterpret_cast<float *>(&P)[tid] = reinterpret_cast<const float *>(&st->pose)[tid];
+    __syncthreads();
+    accumulate_block(a, P, nc, vc, red, &st->acc[0]);
+    if (!last_block(st, &ticket)) return;
     if (tid < kIcpTerms) {
-        unsigned long long a[kIcpAccCopies][3];
+        const double d = read_total(&st->acc[0], tid);
         #pragma unroll
         for (int c = 0; c < kIcpAccCopies; ++c)
             #pragma unroll
-            for (int l = 0; l < 3; ++l) a[c][l] = __ldcg(&st->acc[c][tid][l]);
-        unsigned long long a0 = 0, a1 = 0, a2 = 0;
-        #pragma unroll
-        for (int c = 0; c < kIcpAccCopies; ++c) {
-            a0 += a[c][0]; a1 += a[c][1]; a2 += a[c][2];
-            st->acc[c][tid][0] = 0ull; st->acc[c][tid][1] = 0ull; st->acc[c][tid][2] = 0ull;
+            for (int l = 0; l < 3; ++l) st->acc[0][c][tid][l] = 0ull;
+        st->sums[tid] = d;
+        if (tid < 27) mbuf[tid] = (float)d;
+        if (tid == 27) st->inliers = (int)d;
+    }
+    if (tid == 0) st->counter = 0u;
+}
+
+// Pipeline form, launch `iter` of the frame (see the file comment).
+template <bool LAST>
+__global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, IcpState *__restrict__ st, int iter,
+                                                            const IcpPublish pub) {
+    __shared__ IcpPose P;
+    __shared__ f2 red[kThreads / 32][32];
+    __shared__ double Rs[9], ts[3];  // this launch's FP64 pose
+    __shared__ unsigned ticket;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    // Let the next launch start: it reads this launch's accumulators and
+    // pose slot only after its own griddepcontrol.wait.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    float3 nc[kPixPerThread], vc[kPixPerThread];
+    load_current(a, nc, vc);
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+
+    // ---- the pose this launch associates with ----
+    if (warp == 0) {
+        const double *R0 = iter == 0 ? st->R : st->R_it[(iter - 1) & 1];
+        const double *t0 = iter == 0 ? st->t : st->t_it[(iter - 1) & 1];
+        // the previous pose and the previous launch's totals, loads in flight together
+        double pv = 0.0, term = 0.0;
+        if (lane < 12) pv = __ldcg(lane < 9 ? R0 + lane : t0 + (lane - 9));
+        if (iter > 0 && lane < kIcpTerms) term = read_total(&st->acc[(iter - 1) % kIcpAccBuffers], lane);
+        if (lane < 9) Rs[lane] = pv;
+        else if (lane < 12) ts[lane - 9] = pv;
+        __syncwarp();
+        bool ok = true;
+        int inliers = 0;
+        double xl = 0.0;
+        if (iter > 0) {
+            inliers = (int)shfl(term, 27);
+            double o;
+            ok = warp_solve_step(term, Rs, ts, lane, o, xl) && inliers >= kIcpMinInliers;
+            if (ok) pv = o;
+            __syncwarp();
+            if (lane < 9) Rs[lane] = pv;
+            else if (lane < 12) ts[lane - 9] = pv;
         }
-        const double d = from_fixed(a0, a1, a2);
-        s_sums[tid] = d;
-        if (mbuf && tid < 27) mbuf[tid] = (float)d;
+        if (lane < 9) P.R_cur[lane] = (float)pv;
+        else if (lane < 12) P.t_cur[lane - 9] = (float)pv;
+        if (iter == 0) {
+            // the frame's start pose is the association reference: R^T, t
+            if (lane < 9) P.R_prev_inv[3 * (lane % 3) + lane / 3] = (float)pv;
+            else if (lane < 12) P.t_prev[lane - 9] = (float)pv;
+        }
+        if (blockIdx.x == 0) {
+            // publish the pose for the next launch, and the bookkeeping of the solve
+            if (lane < 9) st->R_it[iter & 1][lane] = pv;
+            else if (lane < 12) st->t_it[iter & 1][lane - 9] = pv;
+            if (iter == 0) {
+                if (lane < 9) {
+                    st->R_start[lane] = pv;
+                    st->pose.R_prev_inv[3 * (lane % 3) + lane / 3] = (float)pv;
+                } else if (lane < 12) {
+                    st->t_start[lane - 9] = pv;
+                    st->pose.t_prev[lane - 9] = (float)pv;
+                }
+                if (lane == 0) { st->status = 0; st->iterations = 0; }
+            }
+            if (iter > 0) {
+                if (lane < kIcpTerms) st->sums[lane] = term;
+                if (ok && lane < 6) st->x[lane] = xl;
+                if (lane == 0) {
+                    st->inliers = inliers;
+                    if (!ok) st->status |= kIcpStatusSolveFailed;
+                    st->iterations += 1;
+                }
+            }
+        }
+    } else if (iter > 0 && tid < 32 + 12) {
+        // the frame's start pose (launch 0 wrote it)
+        const int k = tid - 32;
+        if (k < 9) P.R_prev_inv[k] = st->pose.R_prev_inv[k];
+        else P.t_prev[k - 9] = st->pose.t_prev[k - 9];
+    }
+    if (blockIdx.x == 0) {
+        // the buffer launch iter + 1 adds into; launch iter - 1 read its
+        // previous contents, and it has completed
+        unsigned long long *z = &st->acc[(iter + 1) % kIcpAccBuffers][0][0][0];
+        for (int i = tid; i < kIcpAccCopies * kIcpTerms * 3; i += kThreads) z[i] = 0ull;
     }
     __syncthreads();
+
+    accumulate_block(a, P, nc, vc, red, &st->acc[iter % kIcpAccBuffers]);
+    if (!LAST) return;
+
+    // ---- the frame's last launch: its last block solves its own totals ----
+    if (!last_block(st, &ticket)) return;
+    double term = 0.0;
+    if (warp == 0 && lane < kIcpTerms) term = read_total(&st->acc[iter % kIcpAccBuffers], lane);
+    __syncthreads();
+    // every launch of the frame has read what it needed: clear all buffers
+    // so that the next frame's first launch adds into zeros
+    {
+        unsigned long long *z = &st->acc[0][0][0][0];
+        for (int i = tid; i < kIcpAccBuffers * kIcpAccCopies * kIcpTerms * 3; i += kThreads) z[i] = 0ull;
+    }
     if (warp != 0) return;
-    if (lane < kIcpTerms) st->sums[lane] = s_sums[lane];
-    const int inliers = (int)s_sums[27];
-    bool ok = true;
-    if (SOLVE) ok = inliers >= kIcpMinInliers && warp_solve_and_update(st, s_sums, lane);
+    const int inliers = (int)shfl(term, 27);
+    double o, xl;
+    const bool ok = warp_solve_step(term, Rs, ts, lane, o, xl) && inliers >= kIcpMinInliers;
+    // accept the estimate, or keep the start pose when any solve failed
+    const bool lost = !ok || (*(volatile int *)&st->status & kIcpStatusSolveFailed);
+    double nv = 0.0;
+    if (lane < 9) nv = lost ? st->R_start[lane] : (ok ? o : Rs[lane]);
+    else if (lane < 12) nv = lost ? st->t_start[lane - 9] : (ok ? o : ts[lane - 9]);
+    if (lane < 9) {
+        st->R[lane] = nv;
+        st->pose.R_cur[lane] = (float)nv;
+        pub.cam->R[lane] = (float)nv;
+        pub.cam->R_inv[3 * (lane % 3) + lane / 3] = (float)nv;
+        pub.pose12[lane] = nv;
+    } else if (lane < 12) {
+        st->t[lane - 9] = nv;
+        st->pose.t_cur[lane - 9] = (float)nv;
+        pub.cam->t[lane - 9] = (float)nv;
+        pub.pose12[lane] = nv;
+    }
+    if (lane < kIcpTerms) st->sums[lane] = term;
+    if (ok && lane < 6) st->x[lane] = xl;
     if (lane == 0) {
         st->counter = 0u;
         st->inliers = inliers;
-        if (SOLVE) {
-            if (!ok) st->status |= kIcpStatusSolveFailed;
-            st->iterations += 1;
-        }
+        if (!ok) st->status |= kIcpStatusSolveFailed;
+        st->iterations += 1;
+        pub.cam->tracking_ok = !lost;
+        *pub.status = lost ? pub.lost_status : 0;
+        *pub.inliers = inliers;
     }
+}
+
+// Solve-and-update steps for `n` systems, one warp each (the device solve
+// on its own, for tests): sums[28 n] (27 terms + inlier count), pose[12 n]
+// updated in place, x[6 n], ok[n].
+__global__ void icp_solve_kernel(const double *__restrict__ sums, int n, double *__restrict__ pose,
+                                 double *__restrict__ x, int *__restrict__ okv) {
+    __shared__ double Rs[4][9], ts[4][3];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 4 + warp;
+    if (i >= n) return;  // whole warps leave together
+    const double term = lane < kIcpTerms ? sums[(size_t)28 * i + lane] : 0.0;
+    const double pv = lane < 12 ? pose[(size_t)12 * i + lane] : 0.0;
+    if (lane < 9) Rs[warp][lane] = pv;
+    else if (lane < 12) ts[warp][lane - 9] = pv;
+    __syncwarp();
+    double o, xl;
+    const bool ok = warp_solve_step(term, Rs[warp], ts[warp], lane, o, xl);
+    if (lane < 12) pose[(size_t)12 * i + lane] = ok ? o : pv;
+    if (ok && lane < 6) x[(size_t)6 * i + lane] = xl;
+    if (lane == 0) okv[i] = ok;
 }
 
 // transform_estimation.cl:4-53: group g sums its row of the partial buffer.
@@ -429,14 +573,6 @@ __global__ void clean_buff_kernel(float *__restrict__ g, int width) {
     for (int i = 0; i < 27; ++i) g[(size_t)i * width + id] = 0.f;
 }
 
-__global__ void icp_begin_frame_kernel(IcpState *st) {
-    // the previous frame's pose becomes the association reference
-    for (int k = 0; k < 9; ++k) st->pose.R_prev_inv[k] = (float)st->R[3 * (k % 3) + k / 3];
-    for (int k = 0; k < 3; ++k) st->pose.t_prev[k] = (float)st->t[k];
-    st->status = 0;
-    st->iterations = 0;
-}
-
 }  // namespace
 
 size_t icp_gbuf_floats(int W, int H) {
@@ -446,8 +582,13 @@ size_t icp_gbuf_floats(int W, int H) {
     return 64;
 }
 
-int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, bool overlap_previous,
-               cudaStream_t stream) {
+int launch_icp(const IcpArgs &a, IcpState *st, float *mbuf, cudaStream_t stream) {
+    const unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * kPixPerThread));
+    icp_sums_kernel<<<nb, kThreads, 0, stream>>>(a, st, mbuf);
+    return check_launch("estimate_combined");
+}
+
+int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const IcpPublish &pub, cudaStream_t stream) {
     const unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * kPixPerThread));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
@@ -457,16 +598,17 @@ int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool so
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = overlap_previous ? 1 : 0;
-    cudaError_t e = solve ? cudaLaunchKernelEx(&cfg, icp_kernel<true>, a, st, gbuf, mbuf)
-                          : cudaLaunchKernelEx(&cfg, icp_kernel<false>, a, st, gbuf, mbuf);
-    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "estimate_combined: %s", cudaGetErrorString(e));
-    return check_launch("estimate_combined");
+    cfg.numAttrs = 1;
+    cudaError_t e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<true>, a, st, iter, pub)
+                         : cudaLaunchKernelEx(&cfg, icp_step_kernel<false>, a, st, iter, pub);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "icp_step: %s", cudaGetErrorString(e));
+    return check_launch("icp_step");
 }
 
-int launch_icp_begin_frame(IcpState *st, cudaStream_t stream) {
-    icp_begin_frame_kernel<<<1, 1, 0, stream>>>(st);
-    return check_launch("icp_begin_frame");
+int launch_icp_solve(const double *sums, int n, double *pose, double *x, int *ok, cudaStream_t stream) {
+    if (n <= 0) return TDE_OK;
+    icp_solve_kernel<<<div_up(n, 4), 128, 0, stream>>>(sums, n, pose, x, ok);
+    return check_launch("icp_solve");
 }
 
 int launch_transform_estimation(const float *gbuf, float *out, int len, int stride, cudaStream_t stream) {

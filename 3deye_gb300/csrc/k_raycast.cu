@@ -46,7 +46,7 @@ __device__ __forceinline__ f3 normalized(f3 v) {
 }
 
 // ray_start + ray_dir * t, component-wise (add_3f after the scale).
-__device__ __forceinline__ f3 along(const tde_point3f &o, f3 d, float t) {
+__device__ __forceinline__ f3 along(f3 o, f3 d, float t) {
     return f3{o.x + d.x * t, o.y + d.y * t, o.z + d.z * t};
 }
 
@@ -109,20 +109,20 @@ __device__ __forceinline__ float trilinear(const void *vol, const RayParams &p, 
 // line: it runs once per ray, and inlining it would bloat the march loop past
 // the instruction cache.
 template <int FMT, bool STATS>
-__device__ __noinline__ void refine_surface(const void *vol, const RayParams &p, f3 dir, float time_curr,
+__device__ __noinline__ void refine_surface(const void *vol, const RayParams &p, f3 org, f3 dir, float time_curr,
                                             float &vx_out, float &vy_out, float &vz_out, float &nx_out,
                                             float &ny_out, float &nz_out) {
     const tde_point3i N = p.rb.voxels_size;
     const float step = p.time_step;
     float ct = time_curr + step;
-    float Ftdt = trilinear<FMT, STATS>(vol, p, along(p.t, dir, ct));
+    float Ftdt = trilinear<FMT, STATS>(vol, p, along(org, dir, ct));
     if (isnan(Ftdt)) return;
-    float Ft = trilinear<FMT, STATS>(vol, p, along(p.t, dir, time_curr));
+    float Ft = trilinear<FMT, STATS>(vol, p, along(org, dir, time_curr));
     if (isnan(Ft)) return;
     float Ts = time_curr - step * Ft / (Ftdt - Ft);
-    f3 vf = along(p.t, dir, Ts);
+    f3 vf = along(org, dir, Ts);
     vx_out = vf.x; vy_out = vf.y; vz_out = vf.z;
-    f3 p3 = along(p.t, dir, time_curr);
+    f3 p3 = along(org, dir, time_curr);
     int hx = floor_sat(p3.x / p.cell.x), hy = floor_sat(p3.y / p.cell.y), hz = floor_sat(p3.z / p.cell.z);
     if (hx > 1 && hy > 1 && hz > 1 && hx < N.x - 2 && hy < N.y - 2 && hz < N.z - 2) {
         // vf +- cell on one axis: the other two quotients are vf's
@@ -161,16 +161,16 @@ __device__ __forceinline__ int axis_floor(float q, float o, float d, float cell,
     return floor_sat((o + d * ct) / cell);
 }
 
-__device__ __forceinline__ void sample_voxel(const RayParams &p, const f3 &dir, const RayFast &rf, float ct, int &sx,
-                                             int &sy, int &sz) {
-    sx = axis_floor(fmaf(rf.d[0], ct, rf.o[0]), p.t.x, dir.x, p.cell.x, ct);
-    sy = axis_floor(fmaf(rf.d[1], ct, rf.o[1]), p.t.y, dir.y, p.cell.y, ct);
-    sz = axis_floor(fmaf(rf.d[2], ct, rf.o[2]), p.t.z, dir.z, p.cell.z, ct);
+__device__ __forceinline__ void sample_voxel(const RayParams &p, const f3 &org, const f3 &dir, const RayFast &rf,
+                                             float ct, int &sx, int &sy, int &sz) {
+    sx = axis_floor(fmaf(rf.d[0], ct, rf.o[0]), org.x, dir.x, p.cell.x, ct);
+    sy = axis_floor(fmaf(rf.d[1], ct, rf.o[1]), org.y, dir.y, p.cell.y, ct);
+    sz = axis_floor(fmaf(rf.d[2], ct, rf.o[2]), org.z, dir.z, p.cell.z, ct);
 }
 
 template <int FMT, bool SKIP, bool STATS>
 __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
-                                                     float *__restrict__ nmap, RayParams p) {
+                                                     float *__restrict__ nmap, const __grid_constant__ RayParams p) {
     // 16x16 pixels per block; each warp takes an 8x4 tile so its rays start
     // close together and sample neighbouring voxels.
     const int tid = threadIdx.x;
@@ -178,13 +178,16 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
     const int W = p.intr.cols, H = p.intr.rows;
+    // the pose: from the parameters, or read on the device
+    tde_matrix3f R = p.R;
+    f3 org{p.t.x, p.t.y, p.t.z};
     if (p.dpose) {
         __shared__ float s_pose[12];
         if (tid < 12) s_pose[tid] = tid < 9 ? p.dpose->R[tid] : p.dpose->t[tid - 9];
         __syncthreads();
-        p.R = tde_matrix3f{{{s_pose[0], s_pose[1], s_pose[2]}, {s_pose[3], s_pose[4], s_pose[5]},
-                            {s_pose[6], s_pose[7], s_pose[8]}}};
-        p.t = tde_point3f{s_pose[9], s_pose[10], s_pose[11]};
+        R = tde_matrix3f{{{s_pose[0], s_pose[1], s_pose[2]}, {s_pose[3], s_pose[4], s_pose[5]},
+                          {s_pose[6], s_pose[7], s_pose[8]}}};
+        org = f3{s_pose[9], s_pose[10], s_pose[11]};
     }
     if (x >= W || y >= H) return;
     const size_t pix = (size_t)W * y + x;
@@ -197,33 +200,38 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
     const float step = p.time_step;
 
     f3 rnu{((float)x - p.intr.cx) / p.intr.fx, ((float)y - p.intr.cy) / p.intr.fy, 1.f};
-    f3 rn2 = mat_vec(p.R, rnu);
-    f3 ray_next{rn2.x + p.t.x, rn2.y + p.t.y, rn2.z + p.t.z};
-    f3 dir = normalized(f3{ray_next.x - p.t.x, ray_next.y - p.t.y, ray_next.z - p.t.z});
+    f3 rn2 = mat_vec(R, rnu);
+    f3 ray_next{rn2.x + org.x, rn2.y + org.y, rn2.z + org.z};
+    f3 dir = normalized(f3{ray_next.x - org.x, ray_next.y - org.y, ray_next.z - org.z});
     dir.x = (dir.x == 0.f) ? 1e-15f : dir.x;
     dir.y = (dir.y == 0.f) ? 1e-15f : dir.y;
     dir.z = (dir.z == 0.f) ? 1e-15f : dir.z;
 
     // getMinTime / getMaxTime: raycast.cl:153-171
-    float txmin = ((dir.x > 0 ? 0.f : V.x) - p.t.x) / dir.x;
-    float tymin = ((dir.y > 0 ? 0.f : V.y) - p.t.y) / dir.y;
-    float tzmin = ((dir.z > 0 ? 0.f : V.z) - p.t.z) / dir.z;
+    float txmin = ((dir.x > 0 ? 0.f : V.x) - org.x) / dir.x;
+    float tymin = ((dir.y > 0 ? 0.f : V.y) - org.y) / dir.y;
+    float tzmin = ((dir.z > 0 ? 0.f : V.z) - org.z) / dir.z;
     float t_start = cl_fmax(cl_fmax(txmin, tymin), tzmin);
-    float txmax = ((dir.x > 0 ? V.x : 0.f) - p.t.x) / dir.x;
-    float tymax = ((dir.y > 0 ? V.y : 0.f) - p.t.y) / dir.y;
-    float tzmax = ((dir.z > 0 ? V.z : 0.f) - p.t.z) / dir.z;
+    float txmax = ((dir.x > 0 ? V.x : 0.f) - org.x) / dir.x;
+    float tymax = ((dir.y > 0 ? V.y : 0.f) - org.y) / dir.y;
+    float tzmax = ((dir.z > 0 ? V.z : 0.f) - org.z) / dir.z;
     float t_exit = cl_fmin(cl_fmin(txmax, tymax), tzmax);
     t_start = cl_fmax(t_start, 0.f);
 
+    // the march finds the zero crossing; the secant refinement and the normal
+    // run after it, once per warp for all lanes that hit (lanes reaching the
+    // crossing at different samples would otherwise refine one by one)
+    bool hit = false;
+    float hit_time = 0.f;
     if (!(t_start >= t_exit)) {
         float time_curr = t_start;
-        f3 pu = along(p.t, dir, time_curr);
+        f3 pu = along(org, dir, time_curr);
         int gx = floor_sat(pu.x / p.cell.x), gy = floor_sat(pu.y / p.cell.y), gz = floor_sat(pu.z / p.cell.z);
         gx = max(0, min(gx, N.x - 1));
         gy = max(0, min(gy, N.y - 1));
         gz = max(0, min(gz, N.z - 1));
         RayFast rf;
-        rf.o[0] = p.t.x * p.inv_cell[0]; rf.o[1] = p.t.y * p.inv_cell[1]; rf.o[2] = p.t.z * p.inv_cell[2];
+        rf.o[0] = org.x * p.inv_cell[0]; rf.o[1] = org.y * p.inv_cell[1]; rf.o[2] = org.z * p.inv_cell[2];
         rf.d[0] = dir.x * p.inv_cell[0]; rf.d[1] = dir.y * p.inv_cell[1]; rf.d[2] = dir.z * p.inv_cell[2];
         // previous sample: its value when `known`, else only "non-negative";
         // its time lets the value be fetched when it turns out to matter
@@ -238,7 +246,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
         while (time_curr < p.max_time) {
             const float ct = time_curr + step;
             int sx, sy, sz;
-            sample_voxel(p, dir, rf, ct, sx, sy, sz);
+            sample_voxel(p, org, dir, rf, ct, sx, sy, sz);
             if (!((unsigned)sx < (unsigned)N.x && (unsigned)sy < (unsigned)N.y && (unsigned)sz < (unsigned)N.z)) break;
             int px = sx + p.rb.origin_GRID.x; px -= px >= N.x ? N.x : 0;
             int py = sy + p.rb.origin_GRID.y; py -= py >= N.y ? N.y : 0;
@@ -298,7 +306,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                 }
                 // the previous sample's sign decides a crossing: fetch it
                 int qx, qy, qz;
-                sample_voxel(p, dir, rf, prev_ct, qx, qy, qz);
+                sample_voxel(p, org, dir, rf, prev_ct, qx, qy, qz);
                 tsdf = read_tsdf<FMT, STATS>(vol, p, qx, qy, qz);
             }
             const float tsdf_prev = tsdf;
@@ -307,12 +315,14 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
             prev_ct = ct;
             if (tsdf_prev < 0.f && tsdf > 0.f) break;
             if (tsdf_prev > 0.f && tsdf < 0.f) {
-                refine_surface<FMT, STATS>(vol, p, dir, time_curr, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
+                hit = true;
+                hit_time = time_curr;
                 break;
             }
             time_curr = ct;
         }
     }
+    if (hit) refine_surface<FMT, STATS>(vol, p, org, dir, hit_time, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
     vmap[3 * pix + 0] = vx_out; vmap[3 * pix + 1] = vy_out; vmap[3 * pix + 2] = vz_out;
     nmap[3 * pix + 0] = nx_out; nmap[3 * pix + 1] = ny_out; nmap[3 * pix + 2] = nz_out;
 }
@@ -349,6 +359,82 @@ __global__ void resize_map_kernel(const float *__restrict__ src, float *__restri
     }
     size_t o = 3 * ((size_t)y * dc + x);
     dst[o] = ox; dst[o + 1] = oy; dst[o + 2] = oz;
+}
+
+// 2x2 mean of a vertex (NORMAL false) or normal map at destination pixel
+// (x, y): the same IEEE operations as resize_map_kernel.
+template <bool NORMAL>
+__device__ __forceinline__ f3 resize_px(const float *__restrict__ src, int sc, int x, int y) {
+    const float qnan = __int_as_float(0x7fffffff);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    bool ok = true;
+    #pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+        #pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+            size_t i = 3 * ((size_t)(2 * y + dy) * sc + (2 * x + dx));
+            float a = src[i], b = src[i + 1], c = src[i + 2];
+            ok = ok && !isnan(a);
+            sx = sx + a; sy = sy + b; sz = sz + c;
+        }
+    if (!ok) return f3{qnan, qnan, qnan};
+    if (NORMAL) {
+        float d = 0.f; d += sx * sx; d += sy * sy; d += sz * sz;
+        float rs = 1.f / sqrtf(d);
+        return f3{sx * rs, sy * rs, sz * rs};
+    }
+    return f3{sx * 0.25f, sy * 0.25f, sz * 0.25f};
+}
+
+// The same mean over four values already in registers (level 1 -> 2).
+template <bool NORMAL>
+__device__ __forceinline__ f3 mean4(const f3 (&q)[4]) {
+    const float qnan = __int_as_float(0x7fffffff);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    bool ok = true;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ok = ok && !isnan(q[k].x);
+        sx = sx + q[k].x; sy = sy + q[k].y; sz = sz + q[k].z;
+    }
+    if (!ok) return f3{qnan, qnan, qnan};
+    if (NORMAL) {
+        float d = 0.f; d += sx * sx; d += sy * sy; d += sz * sz;
+        float rs = 1.f / sqrtf(d);
+        return f3{sx * rs, sy * rs, sz * rs};
+    }
+    return f3{sx * 0.25f, sy * 0.25f, sz * 0.25f};
+}
+
+__device__ __forceinline__ void put3(float *dst, size_t i, f3 v) {
+    dst[3 * i] = v.x; dst[3 * i + 1] = v.y; dst[3 * i + 2] = v.z;
+}
+
+// Model-map pyramid in one launch: thread (X, Y) makes level-1 pixels
+// (2X..2X+1, 2Y..2Y+1) of the vertex and normal maps and, from those four
+// values, level-2 pixel (X, Y) -- the values resize_map_kernel gives level
+// by level.  v2/n2 null: level 1 only.
+__global__ void resize_model_maps_kernel(const float *__restrict__ v0, const float *__restrict__ n0,
+                                         float *__restrict__ v1, float *__restrict__ n1, float *__restrict__ v2,
+                                         float *__restrict__ n2, int c0, int r0) {
+    const int c1 = c0 >> 1, r1 = r0 >> 1, c2 = c1 >> 1, r2 = r1 >> 1;
+    const int X = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (2 * X >= c1 || 2 * Y >= r1) return;
+    f3 qv[4], qn[4];
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = 2 * X + (k & 1), y = 2 * Y + (k >> 1);
+        if (x >= c1 || y >= r1) { qv[k] = qn[k] = f3{0.f, 0.f, 0.f}; continue; }
+        qv[k] = resize_px<false>(v0, c0, x, y);
+        qn[k] = resize_px<true>(n0, c0, x, y);
+        put3(v1, (size_t)y * c1 + x, qv[k]);
+        put3(n1, (size_t)y * c1 + x, qn[k]);
+    }
+    if (v2 && X < c2 && Y < r2) {
+        put3(v2, (size_t)Y * c2 + X, mean4<false>(qv));
+        put3(n2, (size_t)Y * c2 + X, mean4<true>(qn));
+    }
 }
 
 // transform_map.cl:6-65
@@ -411,6 +497,14 @@ int launch_resize_map(const float *src, float *dst, int sc, int sr, bool normal,
     if (normal) resize_map_kernel<true><<<grid, block, 0, stream>>>(src, dst, sc, sr);
     else resize_map_kernel<false><<<grid, block, 0, stream>>>(src, dst, sc, sr);
     return check_launch("resize_map");
+}
+
+int launch_resize_model_maps(const float *v0, const float *n0, float *v1, float *n1, float *v2, float *n2, int c0,
+                             int r0, cudaStream_t stream) {
+    dim3 block(32, 8);
+    dim3 grid(div_up(div_up(c0 >> 1, 2), 32), div_up(div_up(r0 >> 1, 2), 8));
+    resize_model_maps_kernel<<<grid, block, 0, stream>>>(v0, n0, v1, n1, v2, n2, c0, r0);
+    return check_launch("resize_model_maps");
 }
 
 int launch_transform_maps(const float *vs, const float *ns, float *vd, float *nd, const tde_matrix3f &R,

@@ -8,6 +8,7 @@ constexpr int kIcpTerms = 28;        // 27 system terms + inlier count
 constexpr int kIcpMinInliers = 6;    // fewer pairs cannot constrain 6 DoF
 constexpr int kIcpStatusSolveFailed = 1;
 constexpr int kIcpAccCopies = 8;
+constexpr int kIcpAccBuffers = 3;  // pipeline launches rotate through these
 
 // Float pose consumed by the association: current estimate (camera ->
 // global) and the previous frame's inverse (global -> previous camera).
@@ -26,10 +27,27 @@ struct IcpState {
     int status, inliers, iterations, pad0;
     unsigned counter;  // blocks done in the running launch (reset by the last block)
     unsigned pad1[3];
+    // Pipeline form: the FP64 pose launch i associated with, in slot i & 1,
+    // and the pose the frame started from (kept when a solve fails).
+    double R_it[2][9], t_it[2][3];
+    double R_start[9], t_start[3];
     // Cross-block sums as 126-bit fixed point (2^-64 units) in three 42-bit
     // limbs; integer atomics make the total independent of block order.
     // Block b adds into copy b % kIcpAccCopies to spread atomic traffic.
-    unsigned long long acc[kIcpAccCopies][kIcpTerms][3];
+    // Pipeline launch i of a frame adds into buffer i % kIcpAccBuffers; the
+    // one-shot form uses buffer 0.
+    unsigned long long acc[kIcpAccBuffers][kIcpAccCopies][kIcpTerms][3];
+};
+
+struct CamPose;
+
+// Where the frame's last ICP launch publishes the pose it accepts.
+struct IcpPublish {
+    CamPose *cam;      // float pose and inverse for integration and raycast
+    double *pose12;    // row-major R, then t
+    int *status;       // 0, or lost_status when a solve failed (the start pose is kept)
+    int *inliers;
+    int lost_status;
 };
 
 struct IcpArgs {
@@ -61,10 +79,20 @@ __host__ __device__ inline void so3_exp(const double *x, double *R) {
 
 size_t icp_gbuf_floats(int W, int H);
 
-// overlap_previous: launch with a programmatic dependency on the previous
-// kernel in the stream (the kernel waits before reading anything it wrote).
-int launch_icp(const IcpArgs &a, IcpState *st, float *gbuf, float *mbuf, bool solve, bool overlap_previous,
-               cudaStream_t stream);
-int launch_icp_begin_frame(IcpState *st, cudaStream_t stream);
+// One-shot form: the 27 sums (and the inlier count) for the pose in
+// st->pose, exact totals to mbuf[0..26]; no solve.
+int launch_icp(const IcpArgs &a, IcpState *st, float *mbuf, cudaStream_t stream);
+// Pipeline form: launch `iter` of a frame's ICP (iterations of all levels
+// counted together), with a programmatic dependency on the previous kernel in
+// the stream.  Launch 0 starts from st->R / st->t (and records it as the
+// frame's start and association reference); launch i > 0 first solves the
+// totals of launch i - 1 and updates the pose (every block, identically); the
+// frame's last launch (`last`) also solves its own totals, accepts the pose
+// (or returns to the start pose when a solve failed), commits it to st->R /
+// st->t and publishes it through `pub`.
+int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const IcpPublish &pub, cudaStream_t stream);
+// The pipeline's FP64 solve-and-update step alone, on n systems (device
+// arrays: sums[28 n], pose[12 n] in place, x[6 n], ok[n]).
+int launch_icp_solve(const double *sums, int n, double *pose, double *x, int *ok, cudaStream_t stream);
 
 }  // namespace tde

@@ -18,6 +18,10 @@ int launch_raycast(const void *volume, int format, float *vmap, float *nmap, con
                    const tde_point3f &cell, const CamPose *dpose, const uint8_t *neg_flags, cudaStream_t stream,
                    unsigned *touched = nullptr);  // touched: measurement bitmap of records read, or null
 int launch_resize_map(const float *src, float *dst, int sc, int sr, bool normal, cudaStream_t stream);
+// Vertex and normal maps of level 0 (c0 x r0) -> levels 1 and (v2, n2 not
+// null) 2, bit-identical to two rounds of launch_resize_map.
+int launch_resize_model_maps(const float *v0, const float *n0, float *v1, float *n1, float *v2, float *n2, int c0,
+                             int r0, cudaStream_t stream);
 int launch_transform_maps(const float *vs, const float *ns, float *vd, float *nd, const tde_matrix3f &R,
                           const tde_point3f &t, int W, int H, cudaStream_t stream);
 int launch_transform_estimation(const float *gbuf, float *out, int len, int stride, cudaStream_t stream);

@@ -136,7 +136,7 @@ class Pipeline:
             check(n)
         return a[:n], b[:n]
 
-    STAGES = ("preprocess", "icp", "pose_and_scaled_depth", "integrate", "raycast", "model_pyramid")
+    STAGES = ("preprocess", "icp", "integrate", "raycast", "model_pyramid")
 
     def stage_timings(self, capacity: int) -> dict:
         """Milliseconds per timed frame of each stage (STAGES), as arrays."""

@@ -178,6 +178,14 @@ int tde_clean_buff(float *gbuf, int width, void *stream);
  * x = (w, v).  Returns TDE_ERR_INVALID_ARG if A is not positive definite. */
 int tde_icp_solve_update_host(const float *mbuf27, double *R9, double *t3, double *x6);
 
+/* The pipeline's on-device FP64 solve-and-update step on n independent
+ * systems (one warp each; device pointers): sums28[28 n] = the 27 terms in
+ * the order above and an inlier count (not read), pose12[12 n] = row-major R
+ * then t, updated in place, x6[6 n] = the step (w, v), ok[n] = 1 when A is
+ * positive definite (else the pose is left unchanged).  Enqueued on
+ * `stream`; nothing blocks. */
+int tde_icp_solve_device(const double *sums28, int n, double *pose12, double *x6, int *ok, void *stream);
+
 /* ======================================================================== */
 /* a7: TSDF integration                                                      */
 /* ======================================================================== */

@@ -89,9 +89,11 @@ int tde_pipeline_enable_timing(tde_pipeline *p, int capacity);
 /* Milliseconds of the integration and raycast launches of the timed frames
  * (synchronises); returns the number of frames written. */
 int tde_pipeline_timings(tde_pipeline *p, float *integrate_ms, float *raycast_ms, int capacity);
-/* Per-stage milliseconds of the timed frames, row-major [frame][6]: input
- * preprocessing (bilateral, pyramid, vertex/normal maps), ICP iterations,
- * pose publication + scaled depth, integration, raycast, model-map pyramid. */
+/* Per-stage milliseconds of the timed frames, row-major [frame][5]: input
+ * preprocessing (bilateral or refiner, pyramid, vertex/normal maps, scaled
+ * depth, depth tiles), ICP iterations with pose acceptance and publication
+ * (pose publication alone on the first frame), integration, raycast,
+ * model-map pyramid. */
 int tde_pipeline_stage_timings(tde_pipeline *p, float *ms, int capacity);
 /* Voxels read, voxels written and 8^3 bricks swept by integration since the
  * last reset, three counters (needs integrate_stats; synchronises). */

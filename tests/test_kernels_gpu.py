@@ -350,3 +350,71 @@ def test_clean_color_slice_golden(tde, cuda):
         tde.clean_color_slice(c, g[f"c{ci}_mn"], g[f"c{ci}_mx"], rb)
         torch.cuda.synchronize()
         assert np.array_equal(N(c), g[f"c{ci}_color_cleaned"])
+
+
+# ---------------------------------------------------------------------------
+# FP64 solve-and-update step (the one every ICP launch runs)
+# ---------------------------------------------------------------------------
+def terms_of(A, b):
+    out = []
+    for k in range(6):
+        for j in range(k, 7):
+            out.append(b[k] if j == 6 else A[k, j])
+    return out
+
+
+def test_device_icp_solve_matches_fp64_oracle(tde, orc, cuda):
+    """The device solve (3x3 blocks, adjugates, Newton-refined reciprocals,
+    Taylor / Rodrigues update) against the oracle's FP64 Cholesky solve and
+    exponential, over systems with entries from 1e-3 to 1e7, rotation steps
+    from 1e-5 to 0.5 rad (both branches of the exponential), and systems that
+    are not positive definite (rejected, pose unchanged)."""
+    import ctypes as C
+    import torch
+    rng = np.random.default_rng(11)
+    n = 384
+    sums = np.zeros((n, 28))
+    pose = np.zeros((n, 12))
+    want_ok = np.ones(n, bool)
+    for i in range(n):
+        J = rng.normal(0, 1, (60, 6)) * rng.uniform(0.3, 3.0, 6)
+        A = J.T @ J * 10.0 ** rng.uniform(-3, 7)
+        step = rng.normal(0, 1, 6)
+        step[:3] *= 10.0 ** rng.uniform(-5, np.log10(0.5)) / np.linalg.norm(step[:3])
+        step[3:] *= 0.05
+        b = A @ step
+        if i % 16 == 5:
+            A[:, 4] = A[4, :] = 0.0  # singular: S has a zero pivot
+        if i % 16 == 9:
+            A = -A  # negative definite
+        want_ok[i] = i % 16 not in (5, 9)
+        sums[i, :27] = terms_of(A, b)
+        sums[i, 27] = 1000
+        q = rng.normal(0, 1, 4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        pose[i] = np.concatenate([R.ravel(), rng.uniform(-2, 2, 3)])
+    d_sums = torch.from_numpy(sums).to(cuda)
+    d_pose = torch.from_numpy(pose).to(cuda)
+    d_x = torch.zeros((n, 6), dtype=torch.float64, device=cuda)
+    d_ok = torch.zeros(n, dtype=torch.int32, device=cuda)
+    tde.check(tde.lib.tde_icp_solve_device(C.c_void_p(d_sums.data_ptr()), n, C.c_void_p(d_pose.data_ptr()),
+                                           C.c_void_p(d_x.data_ptr()), C.c_void_p(d_ok.data_ptr()), None))
+    torch.cuda.synchronize()
+    got_pose, got_x, got_ok = N(d_pose), N(d_x), N(d_ok).astype(bool)
+    assert np.array_equal(got_ok, want_ok)
+    for i in range(n):
+        if not want_ok[i]:
+            assert np.array_equal(got_pose[i], pose[i])
+            continue
+        st, R2, t2, x2 = orc.icp_solve(sums[i, :27], pose[i, :9], pose[i, 9:])
+        assert st == 0
+        # both solves are backward-stable FP64: agreement to ~cond(A) x 1e-16
+        np.testing.assert_allclose(got_x[i], x2, rtol=1e-10, atol=1e-12 * np.abs(x2).max())
+        np.testing.assert_allclose(got_pose[i, :9], R2.ravel(), rtol=0, atol=1e-12)
+        np.testing.assert_allclose(got_pose[i, 9:], t2, rtol=0, atol=1e-11)
+        Rm = got_pose[i, :9].reshape(3, 3)
+        np.testing.assert_allclose(Rm @ Rm.T, np.eye(3), atol=1e-13)

@@ -77,7 +77,7 @@ def test_async_enqueue_matches_blocking(cuda, seq):
     assert len(ti) == len(depths) and (ti > 0).all() and (tr > 0).all()
     r, w = p.integrate_stats()
     assert r > 0 and 0 < w <= r
-    assert p.launches_per_frame() == 36
+    assert p.launches_per_frame() == 31
     p.close()
 
 
@@ -156,4 +156,37 @@ def test_raycast_record_count_matches_oracle(cuda, orc, tde, seq):
                                     pose[9:].astype(np.float32), cfg.trunc_m, np.full(3, cfg.cell, np.float32))
     assert cnt == full > 0
     assert 0 < skipped <= full
+    p.close()
+
+
+def test_model_pyramid_matches_oracle_resize(cuda, orc, tde, seq):
+    """The fused model-map pyramid (levels 1 and 2 in one launch) equals the
+    oracle's 2x2 resize applied level by level, bit for bit."""
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    p = pl.Pipeline(cfg, traj[0])
+    for d in depths[:5]:
+        p.process(d)
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+
+    def maps(level):
+        out = []
+        for ptr in p.model_maps(level):
+            a = np.zeros(((cfg.rows >> level), (cfg.cols >> level), 3), np.float32)
+            tde.check(tde.lib.tde_memcpy(a.ctypes.data_as(C.c_void_p), C.c_void_p(ptr), a.nbytes, 1))
+            out.append(a)
+        return out
+
+    v0, n0 = maps(0)
+    assert np.isfinite(v0).any()
+    v1, n1 = maps(1)
+    v2, n2 = maps(2)
+
+    def same(a, b):
+        na, nb = np.isnan(a[..., 0]), np.isnan(b[..., 0])
+        return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32))
+
+    rv1, rn1 = orc.resize_map(v0, False), orc.resize_map(n0, True)
+    assert same(v1, rv1) and same(n1, rn1)
+    assert same(v2, orc.resize_map(rv1, False)) and same(n2, orc.resize_map(rn1, True))
     p.close()
