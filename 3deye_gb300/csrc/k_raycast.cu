@@ -56,7 +56,7 @@ __device__ __forceinline__ int floor_sat(float v) { return __float2int_rd(v); } 
 template <int FMT, bool STATS>
 __device__ __forceinline__ float load_rec(const void *vol, const RayParams &p, size_t addr) {
     if (STATS) atomicOr(p.touched + (addr >> 5), 1u << (addr & 31));
-    return TsdfStore<FMT>::value(vol, addr, p.n);
+    return TsdfStore<FMT>::value_ro(vol, addr, p.n);
 }
 
 template <int FMT, bool STATS>
@@ -189,15 +189,15 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                           {s_pose[6], s_pose[7], s_pose[8]}}};
         org = f3{s_pose[9], s_pose[10], s_pose[11]};
     }
-    if (x >= W || y >= H) return;
-    const size_t pix = (size_t)W * y + x;
     const float qnan = __int_as_float(0x7fffffff);
-    float vx_out = qnan, vy_out = qnan, vz_out = qnan;
-    float nx_out = qnan, ny_out = qnan, nz_out = qnan;
-
     const tde_point3i N = p.rb.voxels_size;
     const tde_point3f V = p.rb.volume_size;
     const float step = p.time_step;
+    // lanes outside the image stay (no early return): the warp reconverges
+    // before the refinement
+    const bool inside = x < W && y < H;
+    float vx_out = qnan, vy_out = qnan, vz_out = qnan;
+    float nx_out = qnan, ny_out = qnan, nz_out = qnan;
 
     f3 rnu{((float)x - p.intr.cx) / p.intr.fx, ((float)y - p.intr.cy) / p.intr.fy, 1.f};
     f3 rn2 = mat_vec(R, rnu);
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
     // crossing at different samples would otherwise refine one by one)
     bool hit = false;
     float hit_time = 0.f;
-    if (!(t_start >= t_exit)) {
+    if (inside && !(t_start >= t_exit)) {
         float time_curr = t_start;
         f3 pu = along(org, dir, time_curr);
         int gx = floor_sat(pu.x / p.cell.x), gy = floor_sat(pu.y / p.cell.y), gz = floor_sat(pu.z / p.cell.z);
@@ -322,9 +322,13 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
             time_curr = ct;
         }
     }
+    __syncwarp();
     if (hit) refine_surface<FMT, STATS>(vol, p, org, dir, hit_time, vx_out, vy_out, vz_out, nx_out, ny_out, nz_out);
-    vmap[3 * pix + 0] = vx_out; vmap[3 * pix + 1] = vy_out; vmap[3 * pix + 2] = vz_out;
-    nmap[3 * pix + 0] = nx_out; nmap[3 * pix + 1] = ny_out; nmap[3 * pix + 2] = nz_out;
+    if (inside) {
+        const size_t pix = (size_t)W * y + x;
+        vmap[3 * pix + 0] = vx_out; vmap[3 * pix + 1] = vy_out; vmap[3 * pix + 2] = vz_out;
+        nmap[3 * pix + 0] = nx_out; nmap[3 * pix + 1] = ny_out; nmap[3 * pix + 2] = nz_out;
+    }
 }
 
 // resize_vertex_map / resize_normal_map (absent from the reference; named at
@@ -475,9 +479,9 @@ int launch_raycast(const void *volume, int format, float *vmap, float *nmap, con
     // super-brick sample skipping needs whole 32^3 super-bricks on every axis
     const bool whole = rb.voxels_size.x % 32 == 0 && rb.voxels_size.y % 32 == 0 && rb.voxels_size.z % 32 == 0;
     p.super_flags = (neg_flags && whole) ? neg_flags + brick_count(rb) : nullptr;
+    p.touched = touched;
     dim3 block(256);
     dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, 16));
-    p.touched = touched;
     return dispatch_format(format, [&](auto F) {
         constexpr int FM = decltype(F)::value;
         if (touched) {

@@ -98,6 +98,11 @@ template <> struct TsdfStore<TDE_TSDF_I16> {
         int v = reinterpret_cast<const tde_tsdf_i16 *>(base)[i].value;
         return (float)v / (float)TDE_MAX_DEPTH_VALUE;
     }
+    // value() through the read-only path (the volume must not change during the kernel)
+    __device__ __forceinline__ static float value_ro(const void *base, size_t i, size_t) {
+        int v = __ldg(reinterpret_cast<const short *>(base) + 2 * i);
+        return (float)v / (float)TDE_MAX_DEPTH_VALUE;
+    }
     __device__ __forceinline__ static Raw load_raw(const void *base, size_t i, size_t) {
         return __ldg(reinterpret_cast<const uint32_t *>(base) + i);
     }
@@ -127,6 +132,9 @@ template <> struct TsdfStore<TDE_TSDF_F16> {
     __device__ __forceinline__ static float value(const void *base, size_t i, size_t) {
         return __half2float(reinterpret_cast<const __half *>(base)[2 * i]);
     }
+    __device__ __forceinline__ static float value_ro(const void *base, size_t i, size_t) {
+        return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short *>(base) + 2 * i)));
+    }
     __device__ __forceinline__ static Raw load_raw(const void *base, size_t i, size_t) {
         return __ldg(reinterpret_cast<const uint32_t *>(base) + i);
     }
@@ -153,6 +161,9 @@ template <> struct TsdfStore<TDE_TSDF_F32> {
     typedef TsdfRawF32 Raw;
     __device__ __forceinline__ static float value(const void *base, size_t i, size_t) {
         return reinterpret_cast<const float *>(base)[i];
+    }
+    __device__ __forceinline__ static float value_ro(const void *base, size_t i, size_t) {
+        return __ldg(reinterpret_cast<const float *>(base) + i);
     }
     __device__ __forceinline__ static const unsigned short *wplane(const void *base, size_t n) {
         return reinterpret_cast<const unsigned short *>(reinterpret_cast<const float *>(base) + n);
