@@ -127,7 +127,7 @@ __global__ void vertex_map_kernel(const uint16_t *__restrict__ depth, float *__r
 
 // ---------------------------------------------------------------------------
 // PCA normals.  The 7x7 window's vertices are staged in shared memory; each
-// thread forms the centred covariance and takes the eigenvector of its
+// thread forms the window's covariance and takes the eigenvector of its
 // smallest eigenvalue (closed-form eigenvalues, Smith 1961; eigenvector from
 // the largest cross product of two rows of C - l I).
 // ---------------------------------------------------------------------------
@@ -195,31 +195,31 @@ __global__ void __launch_bounds__(kBX *kBY) normal_map_kernel(const float *__res
     float nx = qnan, ny = qnan, nz = qnan;
     const float px = sx[ly][lx], py = sy[ly][lx], pz = sz[ly][lx];
     if (!isnan(px)) {
-        // two passes: centroid, then centred covariance
-        float mx = 0.f, my = 0.f, mz = 0.f;
+        // one pass over the window: first and second moments of the offsets
+        // from the centre vertex (a window of a smooth surface is centred on
+        // it, so the moments carry no large common part to cancel), then
+        // C = S2 - S1 S1^T / n
+        float s1x = 0.f, s1y = 0.f, s1z = 0.f;
+        float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f;
         int cnt = 0;
         #pragma unroll
         for (int dy = -kNR; dy <= kNR; ++dy)
             #pragma unroll
             for (int dx = -kNR; dx <= kNR; ++dx) {
-                float a = sx[ly + dy][lx + dx];
-                if (!isnan(a)) { mx += a - px; my += sy[ly + dy][lx + dx] - py; mz += sz[ly + dy][lx + dx] - pz; ++cnt; }
+                const float a = sx[ly + dy][lx + dx];
+                if (!isnan(a)) {
+                    const float ux = a - px, uy = sy[ly + dy][lx + dx] - py, uz = sz[ly + dy][lx + dx] - pz;
+                    s1x += ux; s1y += uy; s1z += uz;
+                    c00 = fmaf(ux, ux, c00); c01 = fmaf(ux, uy, c01); c02 = fmaf(ux, uz, c02);
+                    c11 = fmaf(uy, uy, c11); c12 = fmaf(uy, uz, c12); c22 = fmaf(uz, uz, c22);
+                    ++cnt;
+                }
             }
         if (cnt >= kNMin) {
-            float ic = 1.f / (float)cnt;
-            mx *= ic; my *= ic; mz *= ic;
-            float c00 = 0, c01 = 0, c02 = 0, c11 = 0, c12 = 0, c22 = 0;
-            #pragma unroll
-            for (int dy = -kNR; dy <= kNR; ++dy)
-                #pragma unroll
-                for (int dx = -kNR; dx <= kNR; ++dx) {
-                    float a = sx[ly + dy][lx + dx];
-                    if (!isnan(a)) {
-                        float ux = a - px - mx, uy = sy[ly + dy][lx + dx] - py - my, uz = sz[ly + dy][lx + dx] - pz - mz;
-                        c00 += ux * ux; c01 += ux * uy; c02 += ux * uz;
-                        c11 += uy * uy; c12 += uy * uz; c22 += uz * uz;
-                    }
-                }
+            const float ic = 1.f / (float)cnt;
+            const float mx = s1x * ic, my = s1y * ic, mz = s1z * ic;
+            c00 = fmaf(-mx, s1x, c00); c01 = fmaf(-mx, s1y, c01); c02 = fmaf(-mx, s1z, c02);
+            c11 = fmaf(-my, s1y, c11); c12 = fmaf(-my, s1z, c12); c22 = fmaf(-mz, s1z, c22);
             smallest_eigvec(c00, c01, c02, c11, c12, c22, nx, ny, nz);
             if (nx * px + ny * py + nz * pz > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
         }

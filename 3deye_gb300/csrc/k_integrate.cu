@@ -166,11 +166,31 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
     const int n_list = *count;
     const int gwarp = (blockIdx.x * blockDim.x + tid) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned n_read = 0, n_written = 0;
+    const int NxNy = Nv.x * Nv.y;
     for (int i = gwarp; i < n_list; i += nwarps) {
         const int b = list[i];
         const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
         const int x = bx * kBrick + (lane & 7);
         const float gx = ((float)x + 0.5f) * P.cell.x - q.t[0];
+        // A lane's 16 voxels share x and take two y values: the x and y parts
+        // of the projection sums, of the squared distance and of the address
+        // are formed once, as the leading terms of the same left-to-right
+        // sums (identical bits).
+        float pvx[2], pvy[2], pvz[2], pn2[2];
+        int pxy[2], py_[2];
+        const int px = wrap_mod(x + P.rb.origin_GRID.x, Nv.x);
+        #pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int y = by * kBrick + (lane >> 3) + 4 * h;
+            const float gy = ((float)y + 0.5f) * P.cell.y - q.t[1];
+            float vx = 0.f; vx += q.Ri[0] * gx; vx += q.Ri[1] * gy;
+            float vy = 0.f; vy += q.Ri[3] * gx; vy += q.Ri[4] * gy;
+            float vz = 0.f; vz += q.Ri[6] * gx; vz += q.Ri[7] * gy;
+            float n2 = 0.f; n2 += gx * gx; n2 += gy * gy;
+            pvx[h] = vx; pvy[h] = vy; pvz[h] = vz; pn2[h] = n2;
+            py_[h] = y;
+            pxy[h] = Nv.x * wrap_mod(y + P.rb.origin_GRID.y, Nv.y) + px;
+        }
         #pragma unroll 1
         for (int j0 = 0; j0 < 16; j0 += 4) {
             size_t idx[4];
@@ -180,28 +200,32 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
             #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int j = j0 + k;
-                const int y = by * kBrick + (lane >> 3) + 4 * (j & 1);
+                const int h = j & 1;
+                const int y = py_[h];
                 const int z = bz * kBrick + (j >> 1);
                 yy[k] = y; zz[k] = z;
                 take[k] = false; sdfv[k] = 0.f; idx[k] = 0;
                 if (x >= Nv.x || y >= Nv.y || z >= Nv.z) continue;
-                const float gy = ((float)y + 0.5f) * P.cell.y - q.t[1];
                 const float gz = ((float)z + 0.5f) * P.cell.z - q.t[2];
-                float vx = 0.f; vx += q.Ri[0] * gx; vx += q.Ri[1] * gy; vx += q.Ri[2] * gz;
-                float vy = 0.f; vy += q.Ri[3] * gx; vy += q.Ri[4] * gy; vy += q.Ri[5] * gz;
-                float vz = 0.f; vz += q.Ri[6] * gx; vz += q.Ri[7] * gy; vz += q.Ri[8] * gz;
+                float vx = pvx[h]; vx += q.Ri[2] * gz;
+                float vy = pvy[h]; vy += q.Ri[5] * gz;
+                float vz = pvz[h]; vz += q.Ri[8] * gz;
                 if (!(vz > 0.f)) continue;
                 const int u = __float2int_rn(vx * fx / vz + ccx);
                 const int v = __float2int_rn(vy * fy / vz + ccy);
                 if (u < 0 || u >= W || v < 0 || v >= H) continue;
                 const float Dp = __ldg(depth + (size_t)v * W + u);
                 if (Dp == 0.f) continue;
-                float n2 = 0.f; n2 += gx * gx; n2 += gy * gy; n2 += gz * gz;
+                float n2 = pn2[h]; n2 += gz * gz;
                 const float sdf = Dp - sqrtf(n2);
                 if (!(sdf >= ntrunc)) continue;
                 take[k] = true;
                 sdfv[k] = sdf;
-                idx[k] = voxel_address(x, y, z, P.rb);
+                // voxel_address with the x and y parts above
+                size_t a = (size_t)(long)(NxNy * wrap_mod(z + P.rb.origin_GRID.z, Nv.z) + pxy[h]);
+                a += (size_t)(long)P.rb.start_index;
+                if (a > (size_t)(long)P.rb.buffer_length) a %= (size_t)(long)P.rb.buffer_length;
+                idx[k] = a;
             }
             typename S::Raw raw[4];
             #pragma unroll
