@@ -13,8 +13,12 @@
 // visits every voxel.  Culling only removes voxels the exact test rejects, so
 // volumes are bit-identical.
 //
-// The maximum observed depth per screen tile comes from a 5-level pyramid
-// (16..256-pixel tiles) built by depth_max_kernel each frame.
+// The maximum (and smallest non-zero) observed depth per screen tile comes
+// from a 5-level pyramid (16..256-pixel tiles) built by depth_max_kernel each
+// frame.  With saturation flags, a brick whose every voxel already holds f = 1
+// at the maximum weight, and which lies entirely more than the truncation
+// distance in front of the smallest depth it projects to, is not swept either:
+// each of its voxels would get tsdf = 1 and keep f = 1, w = max, bit for bit.
 //
 // Built with -fmad=false so every voxel decision and value equals the oracle's.
 #include "tde_common.cuh"
@@ -26,6 +30,7 @@ namespace tde {
 namespace {
 
 constexpr int kBrick = 8;
+constexpr float kNoDepth = 3.3961514e38f;  // bytes 0x7f7f7f7f: "no non-zero depth in the tile"
 
 // ---------------------------------------------------------------------------
 // Max scaled depth per 16x16 tile (level 0) and per 32..256 tiles (levels 1-4,
@@ -33,20 +38,32 @@ constexpr int kBrick = 8;
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) depth_max_kernel(const float *__restrict__ depth, int W, int H,
                                                         DepthMaxPyramid pyr) {
-    __shared__ float red[8];
+    __shared__ float red[8], red_min[8];
     const int tx = blockIdx.x, ty = blockIdx.y;
     const int x = tx * 16 + (threadIdx.x & 15), y = ty * 16 + (threadIdx.x >> 4);
-    float m = 0.f;
-    if (x < W && y < H) m = fmaxf(0.f, depth[(size_t)y * W + x]);
+    float m = 0.f, mn = kNoDepth;
+    if (x < W && y < H) {
+        const float d = depth[(size_t)y * W + x];
+        m = fmaxf(0.f, d);
+        if (d > 0.f) mn = d;
+    }
     #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    for (int o = 16; o > 0; o >>= 1) {
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = m; red_min[threadIdx.x >> 5] = mn; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int i = 1; i < 8; ++i) m = fmaxf(m, red[i]);
+        for (int i = 1; i < 8; ++i) { m = fmaxf(m, red[i]); mn = fminf(mn, red_min[i]); }
         pyr.level[0][ty * pyr.tiles_x[0] + tx] = m;
-        for (int l = 1; l < kDepthMaxLevels; ++l)
-            atomicMax(reinterpret_cast<int *>(&pyr.level[l][(ty >> l) * pyr.tiles_x[l] + (tx >> l)]), __float_as_int(m));
+        pyr.level_min[0][ty * pyr.tiles_x[0] + tx] = mn;
+        // non-negative floats order like their bit patterns
+        for (int l = 1; l < kDepthMaxLevels; ++l) {
+            const int i = (ty >> l) * pyr.tiles_x[l] + (tx >> l);
+            atomicMax(reinterpret_cast<int *>(&pyr.level[l][i]), __float_as_int(m));
+            atomicMin(reinterpret_cast<int *>(&pyr.level_min[l][i]), __float_as_int(mn));
+        }
     }
 }
 
@@ -64,14 +81,30 @@ __device__ __forceinline__ float rect_max_depth(const DepthMaxPyramid &pyr, int 
     return m;
 }
 
+// Smallest non-zero observed depth over the same rectangle; 0 (nothing
+// provable) when the rectangle is larger than the coarsest tile.
+__device__ __forceinline__ float rect_min_depth(const DepthMaxPyramid &pyr, int u0, int v0, int u1, int v1) {
+    const int ext = max(u1 - u0, v1 - v0) + 1;
+    int l = 0;
+    while (l < kDepthMaxLevels - 1 && (16 << l) < ext) ++l;
+    if ((16 << l) < ext) return 0.f;
+    const int s = 4 + l;
+    float m = kNoDepth;
+    for (int ty = v0 >> s; ty <= (v1 >> s); ++ty)
+        for (int tx = u0 >> s; tx <= (u1 >> s); ++tx) m = fminf(m, pyr.level_min[l][ty * pyr.tiles_x[l] + tx]);
+    return m;
+}
+
 struct Pose {
     float Ri[9];
     float t[3];
 };
 
-// True when no voxel of brick (bx,by,bz) can pass the per-voxel test.
-__device__ bool brick_culled(const IntegrateParams &P, const Pose &q, const DepthMaxPyramid &pyr, int bx, int by,
-                             int bz) {
+// True when no voxel of brick (bx,by,bz) can pass the per-voxel test, or
+// (saturated: every voxel holds f = 1 at the maximum weight) when every voxel
+// that passes would get tsdf = 1 and so stay as it is.
+__device__ __forceinline__ bool brick_culled(const IntegrateParams &P, const Pose &q, const DepthMaxPyramid &pyr, int bx,
+                                             int by, int bz, bool saturated) {
     const tde_point3i &Nv = P.rb.voxels_size;
     const int x0 = bx * kBrick, y0 = by * kBrick, z0 = bz * kBrick;
     const int x1 = min(x0 + kBrick, Nv.x) - 1, y1 = min(y0 + kBrick, Nv.y) - 1, z1 = min(z0 + kBrick, Nv.z) - 1;
@@ -110,14 +143,31 @@ __device__ bool brick_culled(const IntegrateParams &P, const Pose &q, const Dept
         const float d = fmaxf(0.f, fmaxf(lo[a], -hi[a]));
         d2 += d * d;
     }
-    return sqrtf(d2) > dmax + P.trunc + 1e-3f + 1e-4f * dmax;
+    if (sqrtf(d2) > dmax + P.trunc + 1e-3f + 1e-4f * dmax) return true;
+    if (!saturated) return false;
+    // farthest voxel centre: every voxel that projects onto a non-zero depth
+    // Dp >= dmin has sdf = Dp - dist > trunc (margins far above float error)
+    float dmin;
+    if ((u1 >> 4) - (u0 >> 4) < 8 && (v1 >> 4) - (v0 >> 4) < 8) {
+        dmin = kNoDepth;  // the 16-pixel tiles over the footprint
+        for (int ty = v0 >> 4; ty <= (v1 >> 4); ++ty)
+            for (int tx = u0 >> 4; tx <= (u1 >> 4); ++tx) dmin = fminf(dmin, pyr.level_min[0][ty * pyr.tiles_x[0] + tx]);
+    } else {
+        dmin = rect_min_depth(pyr, u0, v0, u1, v1);
+    }
+    float f2 = 0.f;
+    #pragma unroll
+    for (int a = 0; a < 3; ++a) f2 += fmaxf(lo[a] * lo[a], hi[a] * hi[a]);
+    return dmin - sqrtf(f2) > P.trunc + 1e-3f + 1e-4f * dmin;
 }
 
 // One thread per brick: surviving bricks are appended to a global list (its
 // order varies run to run; every brick owns disjoint voxels, so the result
 // does not depend on it).
-__global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams P, const DepthMaxPyramid pyr,
-                                                          int *__restrict__ list, int *__restrict__ count) {
+__global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams P,
+                                                          const __grid_constant__ DepthMaxPyramid pyr,
+                                                          int *__restrict__ list, int *__restrict__ count,
+                                                          const uint8_t *__restrict__ sat) {
     __shared__ Pose q;
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid < 12) {
@@ -131,7 +181,8 @@ __global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams 
     const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick, nbz = (Nv.z + kBrick - 1) / kBrick;
     const int b = blockIdx.x * blockDim.x + tid;
     bool keep = false;
-    if (b < nbx * nby * nbz) keep = !brick_culled(P, q, pyr, b % nbx, (b / nbx) % nby, b / (nbx * nby));
+    if (b < nbx * nby * nbz)
+        keep = !brick_culled(P, q, pyr, b % nbx, (b / nbx) % nby, b / (nbx * nby), sat && sat[b] != 0);
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     int base = 0;
     if (lane == 0 && m) base = atomicAdd(count, __popc(m));
@@ -142,11 +193,12 @@ __global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams 
 // One warp per surviving brick (16 voxels per lane), grid-strided over the
 // list so the work spreads over every SM whatever the scene's layout.
 template <int FMT>
-__global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
+__global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
                                                                const IntegrateParams P, const int *__restrict__ list,
                                                                const int *__restrict__ count,
                                                                uint8_t *__restrict__ neg_flags,
-                                                               unsigned long long *__restrict__ stats) {
+                                                               unsigned long long *__restrict__ stats,
+                                                               uint8_t *__restrict__ sat) {
     __shared__ Pose q;
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid < 12) {
@@ -167,6 +219,7 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
     const int gwarp = (blockIdx.x * blockDim.x + tid) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned n_read = 0, n_written = 0;
     const int NxNy = Nv.x * Nv.y;
+    const typename S::Raw sat_raw = S::encode(1.f, P.max_weight);  // f = 1 at the maximum weight
     for (int i = gwarp; i < n_list; i += nwarps) {
         const int b = list[i];
         const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
@@ -191,6 +244,8 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
             py_[h] = y;
             pxy[h] = Nv.x * wrap_mod(y + P.rb.origin_GRID.y, Nv.y) + px;
         }
+        bool all_sat = true;    // every voxel this lane updated was left saturated
+        unsigned taken = 0u;    // bit j: voxel j of this lane was updated
         #pragma unroll 1
         for (int j0 = 0; j0 < 16; j0 += 4) {
             size_t idx[4];
@@ -234,6 +289,7 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
             #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (!take[k]) continue;
+                taken |= 1u << (j0 + k);
                 ++n_read;
                 float fo;
                 int wo;
@@ -243,6 +299,7 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
                 const float fnew = (fo * fw + tsdf) / (fw + 1.f);
                 const int wnew = min(wo + 1, P.max_weight);
                 const typename S::Raw rn = S::encode(fnew, wnew);
+                all_sat = all_sat && S::same(rn, sat_raw);
                 if (!S::same(rn, raw[k])) {
                     S::store_raw(vol, idx[k], P.n, rn);
                     ++n_written;
@@ -257,6 +314,27 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(const float *__re
                     }
                 }
             }
+        }
+        if (sat) {
+            // Saturated brick: every voxel at f = 1, maximum weight.  Only when
+            // all updated voxels are, the others (depth dropouts, outside the
+            // image) are read to check them too.
+            bool brick_sat = __all_sync(0xffffffffu, all_sat);
+            if (brick_sat) {
+                bool rest = true;
+                #pragma unroll 1
+                for (int j = 0; j < 16; ++j) {
+                    if (taken & (1u << j)) continue;
+                    const int h = j & 1, z = bz * kBrick + (j >> 1);
+                    if (x >= Nv.x || py_[h] >= Nv.y || z >= Nv.z) { rest = false; break; }
+                    size_t a = (size_t)(long)(NxNy * wrap_mod(z + P.rb.origin_GRID.z, Nv.z) + pxy[h]);
+                    a += (size_t)(long)P.rb.start_index;
+                    if (a > (size_t)(long)P.rb.buffer_length) a %= (size_t)(long)P.rb.buffer_length;
+                    if (!S::same(S::load_raw(vol, a, P.n), sat_raw)) { rest = false; break; }
+                }
+                brick_sat = __all_sync(0xffffffffu, rest);
+            }
+            if (lane == 0) sat[b] = brick_sat ? 1 : 0;
         }
     }
     if (stats) {
@@ -285,13 +363,16 @@ size_t depth_max_floats(int W, int H) {
     return n;
 }
 
+// The max pyramid, then the min pyramid (same layout).
 DepthMaxPyramid depth_max_layout(float *base, int W, int H) {
     DepthMaxPyramid p;
+    const size_t n = depth_max_floats(W, H);
     size_t off = 0;
     for (int l = 0; l < kDepthMaxLevels; ++l) {
         const int t = 16 << l;
         p.tiles_x[l] = (W + t - 1) / t;
         p.level[l] = base + off;
+        p.level_min[l] = base + n + off;
         off += (size_t)p.tiles_x[l] * ((H + t - 1) / t);
     }
     return p;
@@ -299,9 +380,10 @@ DepthMaxPyramid depth_max_layout(float *base, int W, int H) {
 
 int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cudaStream_t stream) {
     DepthMaxPyramid pyr = depth_max_layout(scratch, W, H);
-    // levels >= 1 are atomicMax targets: start them at +0
-    const size_t l0 = (size_t)pyr.tiles_x[0] * ((H + 15) / 16);
-    cudaError_t e = cudaMemsetAsync(scratch + l0, 0, (depth_max_floats(W, H) - l0) * sizeof(float), stream);
+    // levels >= 1 are atomicMax / atomicMin targets: start them at +0 / kNoDepth
+    const size_t l0 = (size_t)pyr.tiles_x[0] * ((H + 15) / 16), n = depth_max_floats(W, H);
+    cudaError_t e = cudaMemsetAsync(scratch + l0, 0, (n - l0) * sizeof(float), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch + n + l0, 0x7f, (n - l0) * sizeof(float), stream);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "depth_max: %s", cudaGetErrorString(e));
     dim3 grid(div_up(W, 16), div_up(H, 16));
     depth_max_kernel<<<grid, 256, 0, stream>>>(depth_scaled, W, H, pyr);
@@ -318,23 +400,23 @@ size_t superbrick_count(const tde_round_buffer &rb) {
 }
 
 size_t integrate_scratch_bytes(int W, int H, const tde_round_buffer &rb) {
-    // depth-max pyramid, then (aligned) the brick counter and the brick list
-    const size_t dm = ((depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
+    // depth max and min pyramids, then (aligned) the brick counter and the brick list
+    const size_t dm = ((2 * depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
     return dm + 256 + brick_count(rb) * sizeof(int);
 }
 
 int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P, void *scratch,
-                     uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream) {
+                     uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream, uint8_t *sat_flags) {
     const int W = P.intr.cols, H = P.intr.rows;
     float *dmax = static_cast<float *>(scratch);
-    const size_t dm = ((depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
+    const size_t dm = ((2 * depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
     int *count = reinterpret_cast<int *>(static_cast<char *>(scratch) + dm);
     int *list = reinterpret_cast<int *>(static_cast<char *>(scratch) + dm + 256);
     const DepthMaxPyramid pyr = depth_max_layout(dmax, W, H);
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), stream);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "integrate: %s", cudaGetErrorString(e));
     const unsigned nb = (unsigned)brick_count(P.rb);
-    cull_bricks_kernel<<<div_up(nb, 256u), 256, 0, stream>>>(P, pyr, list, count);
+    cull_bricks_kernel<<<div_up(nb, 256u), 256, 0, stream>>>(P, pyr, list, count, sat_flags);
     int st = check_launch("integrate/cull");
     if (st) return st;
     int dev = 0, sms = 152;
@@ -343,7 +425,7 @@ int launch_integrate(const float *depth_scaled, void *volume, int format, const 
     const unsigned blocks = std::min(div_up(nb, 8u), (unsigned)sms * 8u);
     return dispatch_format(format, [&](auto F) {
         integrate_bricks_kernel<decltype(F)::value><<<blocks, 256, 0, stream>>>(depth_scaled, volume, P, list, count,
-                                                                               neg_flags, stats);
+                                                                               neg_flags, stats, sat_flags);
         return check_launch("integrate_tsdf");
     });
 }

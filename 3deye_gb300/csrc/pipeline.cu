@@ -96,6 +96,7 @@ struct tde_pipeline {
     FrameOut *out = nullptr;
     unsigned long long *stats = nullptr;
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
+    uint8_t *satflags = nullptr;  // per logical brick: every voxel at f = 1, maximum weight
     void *volume = nullptr;
     tde_refiner *refiner = nullptr;  // replaces the bilateral filter when set
     // volume shifts: extraction scratch and point buffers, grown on demand
@@ -176,7 +177,8 @@ int record_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
         std::memset(&P, 0, sizeof(P));
         P.trunc = c.trunc; P.max_weight = c.max_weight; P.intr = p->intr[0]; P.rb = p->rb; P.cell = p->cell;
         P.n = voxel_count(p->rb); P.dpose = p->cam;
-        return launch_integrate(p->scaled[set], p->volume, c.tsdf_format, P, p->iscratch[set], p->negflags, p->stats, s);
+        return launch_integrate(p->scaled[set], p->volume, c.tsdf_format, P, p->iscratch[set], p->negflags, p->stats, s,
+                                p->satflags);
     }
     case SEG_RAYCAST: {
         tde_point3f t0{0, 0, 0};
@@ -300,7 +302,7 @@ void release(tde_pipeline *p) {
     }
     for (int l = 0; l < 3; ++l) { cudaFree(p->vmod[l]); cudaFree(p->nmod[l]); }
     cudaFree(p->st); cudaFree(p->cam); cudaFree(p->out);
-    cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->negflags);
+    cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->negflags); cudaFree(p->satflags);
     cudaFree(p->slab_scratch); cudaFree(p->slab_points); cudaFree(p->slab_weights); cudaFree(p->slab_count);
     if (p->pre_stream) cudaStreamDestroy(p->pre_stream);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -370,8 +372,11 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     }
     if ((st = dalloc(&p->st, 1, "icp state")) || (st = dalloc(&p->cam, 1, "camera pose")) ||
         (st = dalloc(&p->out, 1, "frame out")) || (st = dalloc(&p->stats, 3, "stats")) ||
-        (st = dalloc(&p->negflags, brick_flags_bytes(p->rb), "brick flags")))
+        (st = dalloc(&p->negflags, brick_flags_bytes(p->rb), "brick flags")) ||
+        (st = dalloc(&p->satflags, brick_count(p->rb), "saturation flags")))
         return fail(st);
+    e = cudaMemsetAsync(p->satflags, 0, brick_count(p->rb), p->stream);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "saturation flags"));
     e = cudaMemsetAsync(p->negflags, 0, brick_flags_bytes(p->rb), p->stream);
     if (e != cudaSuccess) return fail(cuda_fail(e, "brick flags"));
     e = cudaMemsetAsync(p->stats, 0, 3 * sizeof(unsigned long long), p->stream);
@@ -560,6 +565,8 @@ int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {
         return set_error(TDE_ERR_INVALID_ARG, "pipeline_set_round_buffer: the volume resolution cannot change");
     TDE_TRY(tde_pipeline_sync(p));
     p->rb = *rb;
+    // logical bricks now name other voxels
+    TDE_CUDA(cudaMemsetAsync(p->satflags, 0, brick_count(p->rb), p->stream), "saturation flags");
     if (p->cfg.use_graphs) return capture_all(p);
     return TDE_OK;
 }
@@ -701,6 +708,8 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
                      "pipeline_shift: weights");
     }
     TDE_TRY(tde_clean_tsdf_slice(p->volume, p->cfg.tsdf_format, mn, mx, &p->rb, s));
+    // logical bricks name other voxels after the shift (and the slab was cleaned)
+    TDE_CUDA(cudaMemsetAsync(p->satflags, 0, brick_count(p->rb), s), "pipeline_shift: saturation flags");
     // brick flags only ever over-approximate; after cleaning, the cleared
     // voxels hold 0 >= 0 so stale flags stay conservative
     // advance the round buffer (round_buffer.h:25-63 fields)

@@ -27,8 +27,11 @@ struct IntegrateParams {
 
 // Max observed depth per screen tile: level l has (16 << l)-pixel tiles.
 constexpr int kDepthMaxLevels = 5;
+// Per screen tile: the largest scaled depth (level) and the smallest
+// non-zero one (level_min, kNoDepth where the tile has none).
 struct DepthMaxPyramid {
     float *level[kDepthMaxLevels];
+    float *level_min[kDepthMaxLevels];
     int tiles_x[kDepthMaxLevels];
 };
 
@@ -61,10 +64,16 @@ int launch_depth_max(const float *depth_scaled, int W, int H, float *scratch, cu
 // neg_flags (may be null): per physical brick, set to 1 when a write leaves a
 // negative value there; a 0 therefore guarantees the brick holds no negative
 // TSDF value.
-// Scratch of one integration: the depth-max pyramid (filled by
+// Scratch of one integration: the depth max / min pyramids (filled by
 // launch_depth_max at its start) followed by the surviving-brick list.
 size_t integrate_scratch_bytes(int W, int H, const tde_round_buffer &rb);
+// sat_flags (may be null): per logical brick (brick_count bytes, zero when a
+// pipeline starts or the round buffer moves), 1 when the last integration
+// that swept the brick left every voxel at f = 1 with the maximum weight.
+// Such a brick lying entirely more than the truncation distance in front of
+// every observed depth it projects to would be left unchanged voxel by voxel,
+// so it is not swept.
 int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P, void *scratch,
-                     uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream);
+                     uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream, uint8_t *sat_flags = nullptr);
 
 }  // namespace tde

@@ -190,3 +190,43 @@ def test_model_pyramid_matches_oracle_resize(cuda, orc, tde, seq):
     assert same(v1, rv1) and same(n1, rn1)
     assert same(v2, orc.resize_map(rv1, False)) and same(n2, orc.resize_map(rn1, True))
     p.close()
+
+
+def test_saturated_brick_skip_is_exact(cuda, tde, seq):
+    """Bricks whose voxels all hold f = 1 at the maximum weight and lie more
+    than the truncation distance in front of the observed surface are not
+    swept.  With max_weight 4 many bricks saturate within a few frames; the
+    pipeline's volume still equals, bit for bit, a replay of the same frames
+    and poses through the C-ABI integration (which sweeps every brick), and
+    the pipeline swept fewer bricks than with a weight that never saturates."""
+    import dataclasses
+    import torch
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg0, traj, depths = seq
+    swept = {}
+    for mw in (4, 128):
+        cfg = dataclasses.replace(cfg0, max_weight=mw)
+        p = pl.Pipeline(cfg, traj[0], integrate_stats=True)
+        poses = [p.process(d)[0] for d in depths]
+        swept[mw] = p.integrate_stats(bricks=True)[2]
+        if mw != 4:
+            p.close()
+            continue
+        vptr, rb = p.volume()
+        nbytes = int(tde.lib.tde_tsdf_volume_bytes(cfg.tsdf_format, C.byref(rb)))
+        got = np.zeros(nbytes, np.uint8)
+        tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        tde.check(tde.lib.tde_memcpy(got.ctypes.data_as(C.c_void_p), C.c_void_p(vptr), nbytes, 1))
+        p.close()
+        intr = tde.Intrinsics(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+        cell = float(np.float32(np.float32(cfg.volume_m) / np.float32(cfg.voxels)))
+        vol = tde.new_volume(cfg.tsdf_format, rb)
+        for d, pose in zip(depths, poses):
+            R = pose[:9].reshape(3, 3)
+            scaled = tde.scale_depth(torch.from_numpy(np.ascontiguousarray(d)).to(cuda), intr)
+            tde.integrate_tsdf(scaled, vol, cfg.tsdf_format, cfg.trunc_m, np.ascontiguousarray(R.T), pose[9:], intr,
+                               [cell] * 3, rb, max_weight=mw)
+        torch.cuda.synchronize()
+        ref = vol.cpu().numpy()
+        assert np.array_equal(got, ref)
+    assert swept[4] < swept[128], swept
