@@ -64,44 +64,64 @@ __device__ __forceinline__ float read_tsdf(const void *vol, const RayParams &p, 
     return load_rec<FMT, STATS>(vol, p, voxel_address(x, y, z, p.rb));
 }
 
-// interpolateTrilineary: raycast.cl:95-145, taking the quotients
-// point / Cell_Size (the reference computes each twice; the value is the same).
+// interpolateTrilineary (raycast.cl:95-145), split by axis: the lower corner
+// along one axis, the upper corner's weight, and both corners' physical
+// indices times the axis stride.  False when the base voxel lies on the
+// volume border (the interpolation is then NaN).  The six normal samples of a
+// hit share two of their three axes with the refined point, so those are
+// formed once.
+struct Axis {
+    size_t i0, i1;
+    float w;
+};
+
+__device__ __forceinline__ bool tri_axis(float pt, float q, float cell, int N, int origin, size_t stride, Axis &ax) {
+    int g = floor_sat(q);
+    if (g <= 0 || g >= N - 1) return false;
+    const float v = ((float)g + 0.5f) * cell;
+    g = (pt < v) ? g - 1 : g;
+    float a = q - ((float)g + 0.5f);
+    if (a < 0) { g--; a += 1.0f; }
+    // the two corners g, g + 1 are inside [0, N) here
+    ax.i0 = (size_t)wrap_mod(g + origin, N) * stride;
+    ax.i1 = (size_t)wrap_mod(g + 1 + origin, N) * stride;
+    ax.w = a;
+    return true;
+}
+
 template <int FMT, bool STATS>
-__device__ __noinline__ float trilinear_q(const void *vol, const RayParams &p, f3 pt, float qx, float qy, float qz) {
-    const tde_point3i &N = p.rb.voxels_size;
-    int gx = floor_sat(qx), gy = floor_sat(qy), gz = floor_sat(qz);
-    if (gx <= 0 || gx >= N.x - 1) return __int_as_float(0x7fffffff);
-    if (gy <= 0 || gy >= N.y - 1) return __int_as_float(0x7fffffff);
-    if (gz <= 0 || gz >= N.z - 1) return __int_as_float(0x7fffffff);
-    float vx = ((float)gx + 0.5f) * p.cell.x;
-    float vy = ((float)gy + 0.5f) * p.cell.y;
-    float vz = ((float)gz + 0.5f) * p.cell.z;
-    gx = (pt.x < vx) ? gx - 1 : gx;
-    gy = (pt.y < vy) ? gy - 1 : gy;
-    gz = (pt.z < vz) ? gz - 1 : gz;
-    float a = qx - ((float)gx + 0.5f); if (a < 0) { gx--; a += 1.0f; }
-    float b = qy - ((float)gy + 0.5f); if (b < 0) { gy--; b += 1.0f; }
-    float c = qz - ((float)gz + 0.5f); if (c < 0) { gz--; c += 1.0f; }
-    // the eight corners: gx..gx+1 etc. are inside [0, N) here
-    const int x0 = wrap_mod(gx + p.rb.origin_GRID.x, N.x), x1 = wrap_mod(gx + 1 + p.rb.origin_GRID.x, N.x);
-    const int y0 = wrap_mod(gy + p.rb.origin_GRID.y, N.y), y1 = wrap_mod(gy + 1 + p.rb.origin_GRID.y, N.y);
-    const int z0 = wrap_mod(gz + p.rb.origin_GRID.z, N.z), z1 = wrap_mod(gz + 1 + p.rb.origin_GRID.z, N.z);
-    const size_t sy = (size_t)N.x, sz = (size_t)N.x * (size_t)N.y;
-    const size_t r00 = (size_t)y0 * sy + (size_t)z0 * sz, r01 = (size_t)y0 * sy + (size_t)z1 * sz;
-    const size_t r10 = (size_t)y1 * sy + (size_t)z0 * sz, r11 = (size_t)y1 * sy + (size_t)z1 * sz;
-    float v000 = load_rec<FMT, STATS>(vol, p, x0 + r00), v001 = load_rec<FMT, STATS>(vol, p, x0 + r01);
-    float v010 = load_rec<FMT, STATS>(vol, p, x0 + r10), v011 = load_rec<FMT, STATS>(vol, p, x0 + r11);
-    float v100 = load_rec<FMT, STATS>(vol, p, x1 + r00), v101 = load_rec<FMT, STATS>(vol, p, x1 + r01);
-    float v110 = load_rec<FMT, STATS>(vol, p, x1 + r10), v111 = load_rec<FMT, STATS>(vol, p, x1 + r11);
+__device__ __forceinline__ float tri_corners(const void *vol, const RayParams &p, const Axis &X, const Axis &Y,
+                                             const Axis &Z) {
+    const size_t r00 = Y.i0 + Z.i0, r01 = Y.i0 + Z.i1, r10 = Y.i1 + Z.i0, r11 = Y.i1 + Z.i1;
+    float v000 = load_rec<FMT, STATS>(vol, p, X.i0 + r00), v001 = load_rec<FMT, STATS>(vol, p, X.i0 + r01);
+    float v010 = load_rec<FMT, STATS>(vol, p, X.i0 + r10), v011 = load_rec<FMT, STATS>(vol, p, X.i0 + r11);
+    float v100 = load_rec<FMT, STATS>(vol, p, X.i1 + r00), v101 = load_rec<FMT, STATS>(vol, p, X.i1 + r01);
+    float v110 = load_rec<FMT, STATS>(vol, p, X.i1 + r10), v111 = load_rec<FMT, STATS>(vol, p, X.i1 + r11);
+    const float a = X.w, b = Y.w, c = Z.w;
     float one_a = 1.f - a, one_b = 1.f - b, one_c = 1.f - c;
     float xa = one_b * (v000 * one_c + v001 * c) + b * (v010 * one_c + v011 * c);
     float xb = one_b * (v100 * one_c + v101 * c) + b * (v110 * one_c + v111 * c);
     return one_a * xa + a * xb;
 }
 
+__device__ __forceinline__ bool axis_x(const RayParams &p, float pt, float q, Axis &ax) {
+    return tri_axis(pt, q, p.cell.x, p.rb.voxels_size.x, p.rb.origin_GRID.x, 1, ax);
+}
+__device__ __forceinline__ bool axis_y(const RayParams &p, float pt, float q, Axis &ax) {
+    return tri_axis(pt, q, p.cell.y, p.rb.voxels_size.y, p.rb.origin_GRID.y, (size_t)p.rb.voxels_size.x, ax);
+}
+__device__ __forceinline__ bool axis_z(const RayParams &p, float pt, float q, Axis &ax) {
+    return tri_axis(pt, q, p.cell.z, p.rb.voxels_size.z, p.rb.origin_GRID.z,
+                    (size_t)p.rb.voxels_size.x * (size_t)p.rb.voxels_size.y, ax);
+}
+
 template <int FMT, bool STATS>
 __device__ __forceinline__ float trilinear(const void *vol, const RayParams &p, f3 pt) {
-    return trilinear_q<FMT, STATS>(vol, p, pt, pt.x / p.cell.x, pt.y / p.cell.y, pt.z / p.cell.z);
+    Axis X, Y, Z;
+    if (!axis_x(p, pt.x, pt.x / p.cell.x, X) || !axis_y(p, pt.y, pt.y / p.cell.y, Y) ||
+        !axis_z(p, pt.z, pt.z / p.cell.z, Z))
+        return __int_as_float(0x7fffffff);
+    return tri_corners<FMT, STATS>(vol, p, X, Y, Z);
 }
 
 // Zero crossing between time_curr and time_curr + step: secant refinement of
@@ -125,20 +145,24 @@ __device__ __noinline__ void refine_surface(const void *vol, const RayParams &p,
     f3 p3 = along(org, dir, time_curr);
     int hx = floor_sat(p3.x / p.cell.x), hy = floor_sat(p3.y / p.cell.y), hz = floor_sat(p3.z / p.cell.z);
     if (hx > 1 && hy > 1 && hz > 1 && hx < N.x - 2 && hy < N.y - 2 && hz < N.z - 2) {
-        // vf +- cell on one axis: the other two quotients are vf's
-        const float qx = vf.x / p.cell.x, qy = vf.y / p.cell.y, qz = vf.z / p.cell.z;
-        f3 t1 = vf, t2 = vf;
-        t1.x = t1.x + p.cell.x; t2.x = t2.x - p.cell.x;
-        const float Fx1 = trilinear_q<FMT, STATS>(vol, p, t1, t1.x / p.cell.x, qy, qz);
-        const float Fx2 = trilinear_q<FMT, STATS>(vol, p, t2, t2.x / p.cell.x, qy, qz);
-        t1 = vf; t2 = vf;
-        t1.y = t1.y + p.cell.y; t2.y = t2.y - p.cell.y;
-        const float Fy1 = trilinear_q<FMT, STATS>(vol, p, t1, qx, t1.y / p.cell.y, qz);
-        const float Fy2 = trilinear_q<FMT, STATS>(vol, p, t2, qx, t2.y / p.cell.y, qz);
-        t1 = vf; t2 = vf;
-        t1.z = t1.z + p.cell.z; t2.z = t2.z - p.cell.z;
-        const float Fz1 = trilinear_q<FMT, STATS>(vol, p, t1, qx, qy, t1.z / p.cell.z);
-        const float Fz2 = trilinear_q<FMT, STATS>(vol, p, t2, qx, qy, t2.z / p.cell.z);
+        // vf +- cell on one axis: the other two axes are vf's
+        const float qnan = __int_as_float(0x7fffffff);
+        Axis X, Y, Z, A1, A2;
+        const bool okx = axis_x(p, vf.x, vf.x / p.cell.x, X);
+        const bool oky = axis_y(p, vf.y, vf.y / p.cell.y, Y);
+        const bool okz = axis_z(p, vf.z, vf.z / p.cell.z, Z);
+        float t1 = vf.x + p.cell.x, t2 = vf.x - p.cell.x;
+        const bool x1 = axis_x(p, t1, t1 / p.cell.x, A1), x2 = axis_x(p, t2, t2 / p.cell.x, A2);
+        const float Fx1 = (x1 && oky && okz) ? tri_corners<FMT, STATS>(vol, p, A1, Y, Z) : qnan;
+        const float Fx2 = (x2 && oky && okz) ? tri_corners<FMT, STATS>(vol, p, A2, Y, Z) : qnan;
+        t1 = vf.y + p.cell.y; t2 = vf.y - p.cell.y;
+        const bool y1 = axis_y(p, t1, t1 / p.cell.y, A1), y2 = axis_y(p, t2, t2 / p.cell.y, A2);
+        const float Fy1 = (okx && y1 && okz) ? tri_corners<FMT, STATS>(vol, p, X, A1, Z) : qnan;
+        const float Fy2 = (okx && y2 && okz) ? tri_corners<FMT, STATS>(vol, p, X, A2, Z) : qnan;
+        t1 = vf.z + p.cell.z; t2 = vf.z - p.cell.z;
+        const bool z1 = axis_z(p, t1, t1 / p.cell.z, A1), z2 = axis_z(p, t2, t2 / p.cell.z, A2);
+        const float Fz1 = (okx && oky && z1) ? tri_corners<FMT, STATS>(vol, p, X, Y, A1) : qnan;
+        const float Fz2 = (okx && oky && z2) ? tri_corners<FMT, STATS>(vol, p, X, Y, A2) : qnan;
         f3 n = normalized(f3{Fx1 - Fx2, Fy1 - Fy2, Fz1 - Fz2});
         nx_out = n.x; ny_out = n.y; nz_out = n.z;
     }
@@ -153,7 +177,19 @@ constexpr float kSkipMargin = 1e-2f;  // voxels
 
 struct RayFast {
     float o[3], d[3];  // t / cell, dir / cell
+    float inv_d[3];    // 1 / d
 };
+
+// Time at which the ray (fast coordinates) leaves the box [lo, lo + size)^3
+// shrunk by kSkipMargin voxels on every side: the last time a sample may take
+// and still lie inside the box (the fast coordinates' error is far below the
+// margin).
+__device__ __forceinline__ float box_exit(const RayFast &rf, float lox, float loy, float loz, float size) {
+    const float ex = ((rf.d[0] > 0.f ? lox + (size - kSkipMargin) : lox + kSkipMargin) - rf.o[0]) * rf.inv_d[0];
+    const float ey = ((rf.d[1] > 0.f ? loy + (size - kSkipMargin) : loy + kSkipMargin) - rf.o[1]) * rf.inv_d[1];
+    const float ez = ((rf.d[2] > 0.f ? loz + (size - kSkipMargin) : loz + kSkipMargin) - rf.o[2]) * rf.inv_d[2];
+    return fminf(fminf(ex, ey), ez);
+}
 
 __device__ __forceinline__ int axis_floor(float q, float o, float d, float cell, float ct) {
     const float fr = q - floorf(q);
@@ -233,6 +269,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
         RayFast rf;
         rf.o[0] = org.x * p.inv_cell[0]; rf.o[1] = org.y * p.inv_cell[1]; rf.o[2] = org.z * p.inv_cell[2];
         rf.d[0] = dir.x * p.inv_cell[0]; rf.d[1] = dir.y * p.inv_cell[1]; rf.d[2] = dir.z * p.inv_cell[2];
+        rf.inv_d[0] = 1.f / rf.d[0]; rf.inv_d[1] = 1.f / rf.d[1]; rf.inv_d[2] = 1.f / rf.d[2];
         // previous sample: its value when `known`, else only "non-negative";
         // its time lets the value be fetched when it turns out to matter
         float tsdf = read_tsdf<FMT, STATS>(vol, p, gx, gy, gz);
@@ -262,14 +299,8 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
                             // non-negative sample: no test can fire inside it, so time
                             // advances by the same additions without evaluating samples
                             // until the next one nears the exit.
-                            // exit of the box shrunk by kSkipMargin voxels, in the fast
-                            // coordinates (their error is far below the margin)
-                            const float lox = (float)(sx - (px & 31)), loy = (float)(sy - (py & 31)),
-                                        loz = (float)(sz - (pz & 31));
-                            const float ex = ((rf.d[0] > 0.f ? lox + (32.f - kSkipMargin) : lox + kSkipMargin) - rf.o[0]) / rf.d[0];
-                            const float ey = ((rf.d[1] > 0.f ? loy + (32.f - kSkipMargin) : loy + kSkipMargin) - rf.o[1]) / rf.d[1];
-                            const float ez = ((rf.d[2] > 0.f ? loz + (32.f - kSkipMargin) : loz + kSkipMargin) - rf.o[2]) / rf.d[2];
-                            const float lim = fminf(fminf(ex, ey), ez);
+                            const float lim = box_exit(rf, (float)(sx - (px & 31)), (float)(sy - (py & 31)),
+                                                       (float)(sz - (pz & 31)), 32.f);
                             float tn = time_curr;
                             int m = 0;
                             while (tn < p.max_time && tn + step < lim) { tn = tn + step; ++m; }
@@ -288,10 +319,16 @@ __global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ v
             float cur = 0.f;
             if (SKIP && !have) {
                 if (!(known && tsdf < 0.f)) {
-                    // a non-negative sample after a non-negative one: no test can fire
+                    // a non-negative sample after a non-negative one: no test can
+                    // fire, nor at the following samples inside this 8^3 brick,
+                    // which advance by the same additions
+                    const float lim = box_exit(rf, (float)(sx - (px & 7)), (float)(sy - (py & 7)),
+                                               (float)(sz - (pz & 7)), 8.f);
+                    float tn = ct;
+                    while (tn < p.max_time && tn + step < lim) tn = tn + step;
                     known = false;
-                    prev_ct = ct;
-                    time_curr = ct;
+                    prev_ct = tn;
+                    time_curr = tn;
                     continue;
                 }
             }
