@@ -237,9 +237,10 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
     }
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B,
-    // as asynchronous copies (completed with the first rows' copies)
+    // as asynchronous copies (completed with the first rows' copies).  No
+    // kernel launched right before a convolution writes weights, so they are
+    // fetched before waiting for the previous grid, overlapping its tail.
     if (worker) {
         const int nw = A.cout * 9 * CC;
         for (int i = tid; i < nw; i += kConvWorkers) {
@@ -249,6 +250,7 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
