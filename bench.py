@@ -367,7 +367,7 @@ def run_ours(args, ws, rank, local):
                    "parallelism": "replicas" if ws > 1 else "single"},
         "e2e": {"value": round(ws * K / (e2e_ms * 1e-3), 2), "unit": "frames/s", "h2d_bytes_per_step": fbytes,
                 "d2h_bytes_per_step": 96 + 4},
-        "roofline": {"kernel": "icp_kernel (dominant: largest share of the frame)", "bound": "hbm",
+        "roofline": {"kernel": "icp_step_kernel (dominant: largest share of the frame)", "bound": "hbm",
                      "achieved": round(icp_achieved, 1), "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(icp_achieved / hbm, 4), "traffic": None,
                      "alg_bytes_per_launch": int(icp_bytes / icp_launches), "avg_launch_ms": round(icp_launch_ms, 5),
