@@ -151,14 +151,15 @@ __host__ __device__ __forceinline__ int term_index(int r, int c) {
     return k * 7 - (k * (k - 1)) / 2 + (j - k);
 }
 
-// 1/d for a positive normal d: the hardware approximation, then Newton-
-// Raphson x <- x + x (1 - d x), each step squaring the relative error
-// (three steps from the approximation's ~2^-20 leave rounding error only).
+// 1/d for a positive normal d: the hardware approximation (relative error
+// below 2^-20, measured), then two Newton-Raphson steps x <- x + x (1 - d x),
+// each squaring the relative error (measured on 2^20 inputs from 2^-200 to
+// 2^199: equal to the IEEE quotient 1.0 / d for every one).
 __device__ __forceinline__ double rcp_nr(double d) {
     double x;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
     #pragma unroll
-    for (int k = 0; k < 3; ++k) x = fma(x, fma(-d, x, 1.0), x);
+    for (int k = 0; k < 2; ++k) x = fma(x, fma(-d, x, 1.0), x);
     return x;
 }
 
@@ -273,15 +274,31 @@ __device__ __forceinline__ __int128 to_fixed(float f) {
     return (u >> 31) ? -q : q;
 }
 
-// Sum of the three 42-bit limbs modulo 2^126, read as a signed value.
-__device__ __forceinline__ double from_fixed(unsigned long long a0, unsigned long long a1, unsigned long long a2) {
+// Sum of the three 42-bit limbs modulo 2^126, read as a signed value v:
+// v * 2^-64 rounded to the nearest double (ties to even), built with integer
+// operations only (the FP64 pipe carries the solve), and the integer part
+// floor(v / 2^64) in *whole.
+__device__ __forceinline__ double from_fixed(unsigned long long a0, unsigned long long a1, unsigned long long a2,
+                                             long long *whole) {
     unsigned __int128 S = (unsigned __int128)a0 + ((unsigned __int128)a1 << 42) + ((unsigned __int128)a2 << 84);
     S &= ((unsigned __int128)1 << 126) - 1;
+    const bool neg = (S >> 125) & 1;
     __int128 v = (__int128)S;
-    if ((S >> 125) & 1) v -= (__int128)1 << 126;
-    const long long hi = (long long)(v >> 64);  // floor(v / 2^64)
-    const unsigned long long lo = (unsigned long long)v;
-    return (double)hi + (double)lo * 0x1p-64;
+    if (neg) v -= (__int128)1 << 126;
+    *whole = (long long)(v >> 64);
+    const unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;  // |v| < 2^125
+    const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+    if ((mh | ml) == 0ull) return 0.0;
+    const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+    const unsigned __int128 norm = m << lz;                    // leading one at bit 127
+    const unsigned long long top = (unsigned long long)(norm >> 64), rest = (unsigned long long)norm;
+    unsigned long long mant = (top >> 11) & ((1ull << 52) - 1ull);  // the 52 bits after the leading one
+    const bool round = (top >> 10) & 1ull, sticky = (top & 0x3ffull) != 0ull || rest != 0ull;
+    unsigned long long bexp = (unsigned long long)(127 - lz - 64 + 1023);  // value = 2^(msb - 64) * 1.mant
+    if (round && (sticky || (mant & 1ull))) {
+        if (++mant == (1ull << 52)) { mant = 0ull; ++bexp; }
+    }
+    return __longlong_as_double((long long)(((unsigned long long)neg << 63) | (bexp << 52) | mant));
 }
 
 // Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
@@ -357,8 +374,10 @@ __device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose
     }
 }
 
-// Exact total of term `term` in accumulator buffer `acc` (all copies).
-__device__ __forceinline__ double read_total(const unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3], int term) {
+// Exact total of term `term` in accumulator buffer `acc` (all copies), and
+// its integer part in *whole (the inlier count for the last term).
+__device__ __forceinline__ double read_total(const unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3], int term,
+                                            long long *whole) {
     unsigned long long v[kIcpAccCopies][3];
     #pragma unroll
     for (int c = 0; c < kIcpAccCopies; ++c)
@@ -367,7 +386,7 @@ __device__ __forceinline__ double read_total(const unsigned long long (*acc)[kIc
     unsigned long long a0 = 0, a1 = 0, a2 = 0;
     #pragma unroll
     for (int c = 0; c < kIcpAccCopies; ++c) { a0 += v[c][0]; a1 += v[c][1]; a2 += v[c][2]; }
-    return from_fixed(a0, a1, a2);
+    return from_fixed(a0, a1, a2, whole);
 }
 
 // Last block of a launch: true for exactly one block, after every block's
@@ -412,14 +431,15 @@ __global__ void __launch_bounds__(kThreads) icp_sums_kernel(const IcpArgs a, Icp
     accumulate_block(a, P, nc, vc, red, &st->acc[0]);
     if (!last_block(st, &ticket)) return;
     if (tid < kIcpTerms) {
-        const double d = read_total(&st->acc[0], tid);
+        long long whole;
+        const double d = read_total(&st->acc[0], tid, &whole);
         #pragma unroll
         for (int c = 0; c < kIcpAccCopies; ++c)
             #pragma unroll
             for (int l = 0; l < 3; ++l) st->acc[0][c][tid][l] = 0ull;
         st->sums[tid] = d;
         if (tid < 27) mbuf[tid] = (float)d;
-        if (tid == 27) st->inliers = (int)d;
+        if (tid == 27) st->inliers = (int)whole;
     }
     if (tid == 0) st->counter = 0u;
 }
@@ -447,8 +467,9 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
         const double *t0 = iter == 0 ? st->t : st->t_it[(iter - 1) & 1];
         // the previous pose and the previous launch's totals, loads in flight together
         double pv = 0.0, term = 0.0;
+        long long whole = 0;
         if (lane < 12) pv = __ldcg(lane < 9 ? R0 + lane : t0 + (lane - 9));
-        if (iter > 0 && lane < kIcpTerms) term = read_total(&st->acc[(iter - 1) % kIcpAccBuffers], lane);
+        if (iter > 0 && lane < kIcpTerms) term = read_total(&st->acc[(iter - 1) % kIcpAccBuffers], lane, &whole);
         if (lane < 9) Rs[lane] = pv;
         else if (lane < 12) ts[lane - 9] = pv;
         __syncwarp();
@@ -456,7 +477,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
         int inliers = 0;
         double xl = 0.0;
         if (iter > 0) {
-            inliers = (int)shfl(term, 27);
+            inliers = __shfl_sync(0xffffffffu, (int)whole, 27);
             double o;
             ok = warp_solve_step(term, Rs, ts, lane, o, xl) && inliers >= kIcpMinInliers;
             if (ok) pv = o;
@@ -515,7 +536,8 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     // ---- the frame's last launch: its last block solves its own totals ----
     if (!last_block(st, &ticket)) return;
     double term = 0.0;
-    if (warp == 0 && lane < kIcpTerms) term = read_total(&st->acc[iter % kIcpAccBuffers], lane);
+    long long whole = 0;
+    if (warp == 0 && lane < kIcpTerms) term = read_total(&st->acc[iter % kIcpAccBuffers], lane, &whole);
     __syncthreads();
     // every launch of the frame has read what it needed: clear all buffers
     // so that the next frame's first launch adds into zeros
@@ -524,7 +546,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
         for (int i = tid; i < kIcpAccBuffers * kIcpAccCopies * kIcpTerms * 3; i += kThreads) z[i] = 0ull;
     }
     if (warp != 0) return;
-    const int inliers = (int)shfl(term, 27);
+    const int inliers = __shfl_sync(0xffffffffu, (int)whole, 27);
     double o, xl;
     const bool ok = warp_solve_step(term, Rs, ts, lane, o, xl) && inliers >= kIcpMinInliers;
     // accept the estimate, or keep the start pose when any solve failed
