@@ -138,6 +138,16 @@ def integrate_tsdf(depth_scaled, volume, fmt, trunc, R_inv, t, intr: Intrinsics,
     return volume
 
 
+def integrate_colors(color_volume, rgb, vertex_map, intr: Intrinsics, R_inv, t, trunc, cell, rb: RoundBuffer,
+                     max_weight=255, stream=None):
+    """Integrate_Colors (opencl_wrappers.cpp:181-214): color_volume uint8 [n, 4] (r, g, b, w) on the device,
+    rgb uint8 [rows, cols, 3], vertex_map float32 [rows, cols, 3] (the model raycast from the same pose)."""
+    Ri, tt, cs = mat3(R_inv), vec3(t), vec3(cell)
+    check(lib.tde_integrate_colors(ptr(color_volume), ptr(rgb), ptr(vertex_map), C.byref(intr), C.byref(Ri),
+                                   C.byref(tt), trunc, max_weight, C.byref(cs), C.byref(rb), stream_ptr(stream)))
+    return color_volume
+
+
 def raycast(volume, fmt, rb: RoundBuffer, intr: Intrinsics, R, t, trunc, cell, vmap=None, nmap=None, stream=None):
     """Raycast (opencl_wrappers.cpp:66-95)."""
     torch = _torch()

@@ -101,6 +101,11 @@ _SIGS = {
     "tde_clean_buff": (I, [P, I, P]),
     "tde_icp_solve_update_host": (I, [P, P, P, P]),
     "tde_icp_solve_device": (I, [P, I, P, P, P, P]),
+    "tde_integrate_colors_scratch_bytes": (C.c_size_t, [I, I, C.POINTER(RoundBuffer)]),
+    "tde_integrate_colors": (I, [P, P, P, C.POINTER(Intrinsics), C.POINTER(Matrix3f), C.POINTER(Point3f), C.c_float, I,
+                                 C.POINTER(Point3f), C.POINTER(RoundBuffer), P]),
+    "tde_integrate_colors_ex": (I, [P, P, P, C.POINTER(Intrinsics), C.POINTER(Matrix3f), C.POINTER(Point3f),
+                                    C.c_float, I, C.POINTER(Point3f), C.POINTER(RoundBuffer), P, C.c_size_t, P, P]),
     "tde_scale_depth": (I, [P, P, pI, P]),
     "tde_integrate_tsdf": (I, [P, P, I, F, pM, pV, pI, pV, pRB, I, P]),
     "tde_raycast": (I, [P, I, P, P, pV, pM, F, pI, pRB, pV, P]),

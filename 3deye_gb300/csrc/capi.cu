@@ -327,6 +327,45 @@ int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, f
     return launch_integrate(depth_scaled, volume, format, P, scratch, brick_flags, nullptr, s);
 }
 
+size_t tde_integrate_colors_scratch_bytes(int cols, int rows, const tde_round_buffer *rb) {
+    if (cols <= 0 || rows <= 0 || !valid_round_buffer(rb)) return 0;
+    return integrate_colors_scratch_bytes(cols, rows, *rb);
+}
+
+int tde_integrate_colors_ex(tde_color *color_volume, const uint8_t *rgb, const float *vertex_map,
+                            const tde_intrinsics *intr, const tde_matrix3f *R_inv, const tde_point3f *t, float trunc,
+                            int max_weight, const tde_point3f *cell, const tde_round_buffer *rb, void *scratch,
+                            size_t scratch_bytes, uint64_t *updated, void *stream) {
+    TDE_REQUIRE(color_volume && rgb && vertex_map && R_inv && t && cell, "integrate_colors: null argument");
+    TDE_REQUIRE(valid_intr(intr), "integrate_colors: bad intrinsics");
+    TDE_REQUIRE(valid_round_buffer(rb), "integrate_colors: bad round_buffer");
+    TDE_REQUIRE(trunc > 0.f && std::isfinite(trunc), "integrate_colors: truncation must be positive");
+    TDE_REQUIRE(max_weight >= 1, "integrate_colors: max_weight must be >= 1");
+    TDE_REQUIRE(cell->x > 0.f && cell->y > 0.f && cell->z > 0.f, "integrate_colors: bad cell size");
+    TDE_REQUIRE(scratch && scratch_bytes >= tde_integrate_colors_scratch_bytes(intr->cols, intr->rows, rb),
+                "integrate_colors: scratch smaller than tde_integrate_colors_scratch_bytes()");
+    TDE_REQUIRE((reinterpret_cast<uintptr_t>(scratch) & 255) == 0, "integrate_colors: scratch must be 256-byte aligned");
+    IntegrateParams P = integrate_params(trunc, R_inv, t, intr, cell, rb, max_weight);
+    return launch_integrate_colors(color_volume, rgb, vertex_map, P, scratch,
+                                   reinterpret_cast<unsigned long long *>(updated), as_stream(stream));
+}
+
+int tde_integrate_colors(tde_color *color_volume, const uint8_t *rgb, const float *vertex_map,
+                         const tde_intrinsics *intr, const tde_matrix3f *R_inv, const tde_point3f *t, float trunc,
+                         int max_weight, const tde_point3f *cell, const tde_round_buffer *rb, void *stream) {
+    TDE_REQUIRE(valid_intr(intr) && valid_round_buffer(rb), "integrate_colors: bad intrinsics or round_buffer");
+    cudaStream_t s = as_stream(stream);
+    const size_t sb = tde_integrate_colors_scratch_bytes(intr->cols, intr->rows, rb);
+    void *scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    if (e != cudaSuccess) return set_error(TDE_ERR_OOM, "integrate_colors: scratch: %s", cudaGetErrorString(e));
+    int st = tde_integrate_colors_ex(color_volume, rgb, vertex_map, intr, R_inv, t, trunc, max_weight, cell, rb, scratch,
+                                     sb, nullptr, stream);
+    e = cudaFreeAsync(scratch, s);
+    if (st == TDE_OK && e != cudaSuccess) return set_error(TDE_ERR_CUDA, "integrate_colors: %s", cudaGetErrorString(e));
+    return st;
+}
+
 int tde_integrate_tsdf(const float *depth_scaled, void *volume, int format, float trunc, const tde_matrix3f *R_inv,
                        const tde_point3f *t, const tde_intrinsics *intr, const tde_point3f *cell,
                        const tde_round_buffer *rb, int max_weight, void *stream) {

@@ -103,6 +103,11 @@ struct Pose {
 // True when no voxel of brick (bx,by,bz) can pass the per-voxel test, or
 // (saturated: every voxel holds f = 1 at the maximum weight) when every voxel
 // that passes would get tsdf = 1 and so stay as it is.
+// COLOR: the pyramid holds the model surface's distances from the camera
+// instead, and a voxel can only be updated within the truncation distance of
+// the model point at its pixel, so the brick must also reach past the
+// smallest of those distances minus the truncation (triangle inequality).
+template <bool COLOR = false>
 __device__ __forceinline__ bool brick_culled(const IntegrateParams &P, const Pose &q, const DepthMaxPyramid &pyr, int bx,
                                              int by, int bz, bool saturated) {
     const tde_point3i &Nv = P.rb.voxels_size;
@@ -144,7 +149,7 @@ __device__ __forceinline__ bool brick_culled(const IntegrateParams &P, const Pos
         d2 += d * d;
     }
     if (sqrtf(d2) > dmax + P.trunc + 1e-3f + 1e-4f * dmax) return true;
-    if (!saturated) return false;
+    if (!saturated && !COLOR) return false;
     // farthest voxel centre: every voxel that projects onto a non-zero depth
     // Dp >= dmin has sdf = Dp - dist > trunc (margins far above float error)
     float dmin;
@@ -158,12 +163,13 @@ __device__ __forceinline__ bool brick_culled(const IntegrateParams &P, const Pos
     float f2 = 0.f;
     #pragma unroll
     for (int a = 0; a < 3; ++a) f2 += fmaxf(lo[a] * lo[a], hi[a] * hi[a]);
-    return dmin - sqrtf(f2) > P.trunc + 1e-3f + 1e-4f * dmin;
+    return dmin - sqrtf(f2) > P.trunc + 1e-3f + 1e-4f * dmin;  // COLOR: every voxel closer than every model point - trunc
 }
 
 // One thread per brick: surviving bricks are appended to a global list (its
 // order varies run to run; every brick owns disjoint voxels, so the result
 // does not depend on it).
+template <bool COLOR = false>
 __global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams P,
                                                           const __grid_constant__ DepthMaxPyramid pyr,
                                                           int *__restrict__ list, int *__restrict__ count,
@@ -182,7 +188,7 @@ __global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams 
     const int b = blockIdx.x * blockDim.x + tid;
     bool keep = false;
     if (b < nbx * nby * nbz)
-        keep = !brick_culled(P, q, pyr, b % nbx, (b / nbx) % nby, b / (nbx * nby), sat && sat[b] != 0);
+        keep = !brick_culled<COLOR>(P, q, pyr, b % nbx, (b / nbx) % nby, b / (nbx * nby), sat && sat[b] != 0);
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     int base = 0;
     if (lane == 0 && m) base = atomicAdd(count, __popc(m));
@@ -352,6 +358,89 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
     }
 }
 
+// Distance of each model surface point (raycast vertex map, volume frame)
+// from the camera centre; 0 where the map holds no point.
+__global__ void model_dist_kernel(const float *__restrict__ vmap, int n, const IntegrateParams P,
+                                  float *__restrict__ dist) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float tx = P.dpose ? P.dpose->t[0] : P.t[0], ty = P.dpose ? P.dpose->t[1] : P.t[1],
+                tz = P.dpose ? P.dpose->t[2] : P.t[2];
+    const float x = vmap[3 * i], y = vmap[3 * i + 1], z = vmap[3 * i + 2];
+    float d = 0.f;
+    if (!isnan(x)) d = sqrtf((x - tx) * (x - tx) + (y - ty) * (y - ty) + (z - tz) * (z - tz));
+    dist[i] = d;
+}
+
+// Colour integration of the surviving bricks, one warp per brick: the same
+// voxel test and running mean, in the same IEEE operations, as the oracle.
+__global__ void __launch_bounds__(256) integrate_colors_kernel(const uint8_t *__restrict__ rgb,
+                                                               const float *__restrict__ vmap,
+                                                               tde_color *__restrict__ col, const IntegrateParams P,
+                                                               const int *__restrict__ list,
+                                                               const int *__restrict__ count,
+                                                               unsigned long long *__restrict__ updated) {
+    __shared__ Pose q;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < 12) {
+        float v;
+        if (P.dpose) v = tid < 9 ? P.dpose->R_inv[tid] : P.dpose->t[tid - 9];
+        else v = tid < 9 ? P.R_inv[tid] : P.t[tid - 9];
+        if (tid < 9) q.Ri[tid] = v; else q.t[tid - 9] = v;
+    }
+    __syncthreads();
+    const tde_point3i &Nv = P.rb.voxels_size;
+    const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick;
+    const int W = P.intr.cols, H = P.intr.rows;
+    const int mw = min(P.max_weight, 255);
+    const int n_list = *count;
+    const int gwarp = (blockIdx.x * blockDim.x + tid) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned n_up = 0;
+    for (int i = gwarp; i < n_list; i += nwarps) {
+        const int b = list[i];
+        const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+        const int x = bx * kBrick + (lane & 7);
+        const float ax = ((float)x + 0.5f) * P.cell.x;
+        const float gx = ax - q.t[0];
+        #pragma unroll 2
+        for (int j = 0; j < 16; ++j) {
+            const int y = by * kBrick + (lane >> 3) + 4 * (j & 1);
+            const int z = bz * kBrick + (j >> 1);
+            if (x >= Nv.x || y >= Nv.y || z >= Nv.z) continue;
+            const float ay = ((float)y + 0.5f) * P.cell.y, az = ((float)z + 0.5f) * P.cell.z;
+            const float gy = ay - q.t[1], gz = az - q.t[2];
+            float vx = 0.f; vx += q.Ri[0] * gx; vx += q.Ri[1] * gy; vx += q.Ri[2] * gz;
+            float vy = 0.f; vy += q.Ri[3] * gx; vy += q.Ri[4] * gy; vy += q.Ri[5] * gz;
+            float vz = 0.f; vz += q.Ri[6] * gx; vz += q.Ri[7] * gy; vz += q.Ri[8] * gz;
+            if (!(vz > 0.f)) continue;
+            const int u = __float2int_rn(vx * P.intr.fx / vz + P.intr.cx);
+            const int v = __float2int_rn(vy * P.intr.fy / vz + P.intr.cy);
+            if (u < 0 || u >= W || v < 0 || v >= H) continue;
+            const size_t pix = (size_t)v * W + u;
+            const float px = __ldg(vmap + 3 * pix);
+            if (isnan(px)) continue;
+            const float dx = px - ax, dy = __ldg(vmap + 3 * pix + 1) - ay, dz = __ldg(vmap + 3 * pix + 2) - az;
+            float d2 = 0.f; d2 += dx * dx; d2 += dy * dy; d2 += dz * dz;
+            if (!(sqrtf(d2) < P.trunc)) continue;
+            tde_color *c = col + voxel_address(x, y, z, P.rb);
+            const tde_color o = *c;
+            const uint8_t *src = rgb + 3 * pix;
+            const float fw = (float)o.w, fw1 = fw + 1.f;
+            tde_color nc;
+            nc.r = (uint8_t)max(0, min(255, __float2int_rn(((float)o.r * fw + (float)__ldg(src)) / fw1)));
+            nc.g = (uint8_t)max(0, min(255, __float2int_rn(((float)o.g * fw + (float)__ldg(src + 1)) / fw1)));
+            nc.b = (uint8_t)max(0, min(255, __float2int_rn(((float)o.b * fw + (float)__ldg(src + 2)) / fw1)));
+            nc.w = (uint8_t)min((int)o.w + 1, mw);
+            *c = nc;
+            ++n_up;
+        }
+    }
+    if (updated) {
+        for (int off = 16; off > 0; off >>= 1) n_up += __shfl_down_sync(0xffffffffu, n_up, off);
+        if (lane == 0 && n_up) atomicAdd(updated, (unsigned long long)n_up);
+    }
+}
+
 }  // namespace
 
 size_t depth_max_floats(int W, int H) {
@@ -428,6 +517,36 @@ int launch_integrate(const float *depth_scaled, void *volume, int format, const 
                                                                                neg_flags, stats, sat_flags);
         return check_launch("integrate_tsdf");
     });
+}
+
+size_t integrate_colors_scratch_bytes(int W, int H, const tde_round_buffer &rb) {
+    return (((size_t)W * H * sizeof(float) + 255) & ~size_t(255)) + integrate_scratch_bytes(W, H, rb);
+}
+
+int launch_integrate_colors(tde_color *col, const uint8_t *rgb, const float *vmap, const IntegrateParams &P,
+                            void *scratch, unsigned long long *updated, cudaStream_t stream) {
+    const int W = P.intr.cols, H = P.intr.rows, n = W * H;
+    float *dist = static_cast<float *>(scratch);
+    char *iscratch = static_cast<char *>(scratch) + (((size_t)n * sizeof(float) + 255) & ~size_t(255));
+    model_dist_kernel<<<div_up(n, 256), 256, 0, stream>>>(vmap, n, P, dist);
+    int st = check_launch("integrate_colors/model distances");
+    if (st) return st;
+    if ((st = launch_depth_max(dist, W, H, reinterpret_cast<float *>(iscratch), stream))) return st;
+    const size_t dm = ((2 * depth_max_floats(W, H) * sizeof(float)) + 255) & ~size_t(255);
+    int *count = reinterpret_cast<int *>(iscratch + dm);
+    int *list = reinterpret_cast<int *>(iscratch + dm + 256);
+    const DepthMaxPyramid pyr = depth_max_layout(reinterpret_cast<float *>(iscratch), W, H);
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "integrate_colors: %s", cudaGetErrorString(e));
+    const unsigned nb = (unsigned)brick_count(P.rb);
+    cull_bricks_kernel<true><<<div_up(nb, 256u), 256, 0, stream>>>(P, pyr, list, count, nullptr);
+    if ((st = check_launch("integrate_colors/cull"))) return st;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned blocks = std::min(div_up(nb, 8u), (unsigned)sms * 8u);
+    integrate_colors_kernel<<<blocks, 256, 0, stream>>>(rgb, vmap, col, P, list, count, updated);
+    return check_launch("integrate_colors");
 }
 
 }  // namespace tde

@@ -75,5 +75,10 @@ size_t integrate_scratch_bytes(int W, int H, const tde_round_buffer &rb);
 // so it is not swept.
 int launch_integrate(const float *depth_scaled, void *volume, int format, const IntegrateParams &P, void *scratch,
                      uint8_t *neg_flags, unsigned long long *stats, cudaStream_t stream, uint8_t *sat_flags = nullptr);
+// Colour integration (Integrate_Colors): scratch of integrate_colors_scratch_bytes (256-byte aligned);
+// `updated` (may be null) accumulates the count of voxels updated.
+size_t integrate_colors_scratch_bytes(int W, int H, const tde_round_buffer &rb);
+int launch_integrate_colors(tde_color *col, const uint8_t *rgb, const float *vmap, const IntegrateParams &P,
+                            void *scratch, unsigned long long *updated, cudaStream_t stream);
 
 }  // namespace tde

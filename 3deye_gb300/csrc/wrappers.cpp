@@ -42,7 +42,7 @@ const char *const kKnown[] = {
     "estimate_combined", "transform_estimation", "clean_buff", "scale_depth", "integrate_tsdf_volume", "raycast",
     "resize_vertex_map", "resize_normal_map", "transform_map", "scan_slice_of_both_volumes", "extract_slice_as_cloud",
     "scan_slice_of_tsdf_volume", "extract_tsdf_slice_as_cloud", "scan_pow2", "scan_subarrays", "clean_tsdf_slice",
-    "clean_color_slice", "init_tsdf"};
+    "clean_color_slice", "init_tsdf", "integrate_color_volume"};
 
 string base_name(const string &n) {
     if (n.size() > 3 && n.compare(n.size() - 3, 3, ".cl") == 0) return n.substr(0, n.size() - 3);
@@ -271,9 +271,18 @@ void Transform_Maps(gpu_array_base *vs, gpu_array_base *ns, gpu_array_base *vd, 
     sync("Transform_Maps");
 }
 
-void Integrate_Colors(gpu_array_base *, gpu_array_base *, gpu_array_base *, intrinsics &, matrix_3f &, vector_3f &,
-                      float, int, point_3f, round_buffer *, opencl_kernel *) {
-    throw std::runtime_error("Integrate_Colors: colour integration is not available in this build");
+// opencl_wrappers.cpp:181-214.  gRGB_Frame: cols x rows pixels of 3 bytes (r, g, b);
+// Vertex_Map: the model surface raycast from the same pose.
+void Integrate_Colors(gpu_array_base *gTsdf_Color_Volume, gpu_array_base *gRGB_Frame, gpu_array_base *Vertex_Map,
+                      intrinsics &Intr, matrix_3f &Rotation_Inverse, vector_3f &Translation, float Truncation_Distance,
+                      int Max_Weight, point_3f Cell_Size, round_buffer *Round_Buffer, opencl_kernel *) {
+    check(tde_integrate_colors(static_cast<tde_color *>(dev(gTsdf_Color_Volume, "Integrate_Colors")),
+                               static_cast<const uint8_t *>(dev(gRGB_Frame, "Integrate_Colors")),
+                               static_cast<const float *>(dev(Vertex_Map, "Integrate_Colors")), I(Intr),
+                               M(Rotation_Inverse), V(Translation), Truncation_Distance, Max_Weight, V(Cell_Size),
+                               RB(Round_Buffer), nullptr),
+          "Integrate_Colors");
+    sync("Integrate_Colors");
 }
 
 // opencl_wrappers.cpp:216-235; Trunc_Dist is the maximum depth in millimetres.

@@ -10,9 +10,9 @@
  * accepted and not needed.  Failures throw std::runtime_error.
  *
  * Stages whose kernels the reference does not ship either follow the
- * KinectFusion method (documented in tde_capi.h) or, outside this path
- * (colour integration, whole-volume export, shading, RGBD odometry), throw
- * std::runtime_error("... not available").
+ * KinectFusion method (documented in tde_capi.h: colour integration among
+ * them) or, outside this path (whole-volume export, shading, RGBD odometry),
+ * throw std::runtime_error("... not available").
  */
 #ifndef TDE_3DEYE_OPENCL_WRAPPERS_H
 #define TDE_3DEYE_OPENCL_WRAPPERS_H

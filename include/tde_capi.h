@@ -244,6 +244,30 @@ int tde_integrate_tsdf_noalloc(const float *depth_scaled, void *volume, int form
                                const tde_point3f *cell_size, const tde_round_buffer *rb, int max_weight,
                                void *stream);
 
+/* Colour integration: Integrate_Colors (opencl_wrappers.cpp:181-214, declared at
+ * opencl_wrappers.h:59-70; its kernel integrate_color_volume is absent from the
+ * reference and is restated from KinectFusion's colour averaging).  color_volume holds
+ * one tde_color {r, g, b, w} per voxel at the TSDF's cyclic addresses; rgb is the
+ * frame, cols x rows pixels of 3 bytes (r, g, b); vertex_map is the model surface
+ * raycast from the same pose (volume frame, 3 floats per pixel, NaN where empty).
+ * Each voxel whose centre projects into the frame, where the model point lies
+ * closer than `trunc` to that centre, takes the weighted running mean of its
+ * colour and the pixel's (each channel rounded to nearest, ties to even) and its
+ * weight grows by one up to min(max_weight, 255).  Bricks no update can reach are
+ * skipped (the model's distances from the camera bound the voxels that can
+ * change); results equal a sweep of every voxel.  R_inv, t: volume -> camera
+ * rotation and the camera centre, as for tde_integrate_tsdf.  The _ex form takes
+ * 256-byte aligned device scratch of tde_integrate_colors_scratch_bytes() and, in
+ * `updated` (device, may be NULL), adds the count of voxels updated. */
+size_t tde_integrate_colors_scratch_bytes(int cols, int rows, const tde_round_buffer *rb);
+int tde_integrate_colors(tde_color *color_volume, const uint8_t *rgb, const float *vertex_map,
+                         const tde_intrinsics *intr, const tde_matrix3f *R_inv, const tde_point3f *t, float trunc,
+                         int max_weight, const tde_point3f *cell_size, const tde_round_buffer *rb, void *stream);
+int tde_integrate_colors_ex(tde_color *color_volume, const uint8_t *rgb, const float *vertex_map,
+                            const tde_intrinsics *intr, const tde_matrix3f *R_inv, const tde_point3f *t, float trunc,
+                            int max_weight, const tde_point3f *cell_size, const tde_round_buffer *rb, void *scratch,
+                            size_t scratch_bytes, uint64_t *updated, void *stream);
+
 /* ======================================================================== */
 /* a8/a9: raycast and model maps                                             */
 /* ======================================================================== */

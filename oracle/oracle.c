@@ -706,6 +706,53 @@ int or_clean_tsdf_slice(void *vol, int fmt, const int *mn, const int *mx, const 
 }
 
 /* clean_color_slice.cl:41-67 */
+/* ---------------- colour integration (Integrate_Colors, opencl_wrappers.cpp:181-214; the kernel
+ * integrate_color_volume is absent and is restated from KinectFusion's colour averaging).  Every
+ * voxel is visited: its centre is projected into the frame; where the model surface point at that
+ * pixel (the raycast vertex map, volume frame) lies closer than the truncation distance to the centre,
+ * the voxel's colour becomes the weighted running mean of its colour and the pixel's, each channel
+ * rounded to nearest (ties to even), and its weight grows by one up to max_weight. */
+int or_integrate_colors(tde_color *col, const uint8_t *rgb, const float *vmap, float trunc, const float *Ri,
+                        const float *t, const tde_intrinsics *in, const float *cell, const tde_round_buffer *rb,
+                        int max_weight, uint64_t *updated) {
+    const int W = in->cols, H = in->rows, Nx = rb->voxels_size.x, Ny = rb->voxels_size.y, Nz = rb->voxels_size.z;
+    const int mw = imin(max_weight, 255);
+    uint64_t n_up = 0;
+#pragma omp parallel for schedule(static) reduction(+ : n_up)
+    for (int y = 0; y < Ny; ++y)
+        for (int x = 0; x < Nx; ++x) {
+            const float ax = ((float)x + 0.5f) * cell[0], ay = ((float)y + 0.5f) * cell[1];
+            const float gx = ax - t[0], gy = ay - t[1];
+            for (int z = 0; z < Nz; ++z) {
+                const float az = ((float)z + 0.5f) * cell[2];
+                const float gz = az - t[2];
+                float vx = 0.f; vx += Ri[0] * gx; vx += Ri[1] * gy; vx += Ri[2] * gz;
+                float vy = 0.f; vy += Ri[3] * gx; vy += Ri[4] * gy; vy += Ri[5] * gz;
+                float vz = 0.f; vz += Ri[6] * gx; vz += Ri[7] * gy; vz += Ri[8] * gz;
+                if (!(vz > 0.f)) continue;
+                int u = rint_sat(vx * in->fx / vz + in->cx);
+                int w = rint_sat(vy * in->fy / vz + in->cy);
+                if (u < 0 || u >= W || w < 0 || w >= H) continue;
+                const float *pv = vmap + 3 * ((size_t)w * W + u);
+                if (isnan(pv[0])) continue;
+                const float dx = pv[0] - ax, dy = pv[1] - ay, dz = pv[2] - az;
+                float d2 = 0.f; d2 += dx * dx; d2 += dy * dy; d2 += dz * dz;
+                if (!(sqrtf(d2) < trunc)) continue;
+                tde_color *c = &col[or_voxel_address(x, y, z, rb)];
+                const uint8_t *src = rgb + 3 * ((size_t)w * W + u);
+                const float fw = (float)c->w, fw1 = fw + 1.f;
+                const int r = imax(0, imin(255, rint_sat(((float)c->r * fw + (float)src[0]) / fw1)));
+                const int g = imax(0, imin(255, rint_sat(((float)c->g * fw + (float)src[1]) / fw1)));
+                const int b = imax(0, imin(255, rint_sat(((float)c->b * fw + (float)src[2]) / fw1)));
+                c->r = (uint8_t)r; c->g = (uint8_t)g; c->b = (uint8_t)b;
+                c->w = (uint8_t)imin((int)c->w + 1, mw);
+                ++n_up;
+            }
+        }
+    if (updated) *updated = n_up;
+    return 0;
+}
+
 int or_clean_color_slice(tde_color *col, const int *mn, const int *mx, const tde_round_buffer *rb) {
     for (int z = 0; z < rb->voxels_size.z; ++z)
         for (int y = 0; y < rb->voxels_size.y; ++y)

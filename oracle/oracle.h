@@ -54,6 +54,9 @@ int64_t or_extract_slice(const void *vol, int fmt, const tde_color *color, const
                          int64_t capacity);
 int or_clean_tsdf_slice(void *vol, int fmt, const int *mn, const int *mx, const tde_round_buffer *rb);
 int or_clean_color_slice(tde_color *col, const int *mn, const int *mx, const tde_round_buffer *rb);
+int or_integrate_colors(tde_color *col, const uint8_t *rgb, const float *vmap, float trunc, const float *Ri,
+                        const float *t, const tde_intrinsics *in, const float *cell, const tde_round_buffer *rb,
+                        int max_weight, uint64_t *updated);
 int or_set_threads(int n);
 
 /* synthetic scenes (oracle_scene.c) */

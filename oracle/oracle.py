@@ -75,6 +75,7 @@ _sigs = {
     "or_extract_slice": (C.c_int64, [P, I, P, P, P, pRB, I, P, P, P, C.c_int64]),
     "or_clean_tsdf_slice": (I, [P, I, P, P, pRB]),
     "or_clean_color_slice": (I, [P, P, P, pRB]),
+    "or_integrate_colors": (I, [P, P, P, F, P, P, pI, P, pRB, I, P]),
     "or_set_threads": (I, [I]),
     "or_raycast_records": (C.c_int64, [P, I, P, P, P, P, F, pI, pRB, P, P]),
     "or_scale_depth_f64": (I, [P, P, pI]),
@@ -225,6 +226,15 @@ def extract_slice(vol, fmt, color, mn, mx, rb, capacity=None, weights=False):
 
 def clean_tsdf_slice(vol, fmt, mn, mx, rb):
     lib.or_clean_tsdf_slice(_p(vol), fmt, _p(np.array(mn, np.int32)), _p(np.array(mx, np.int32)), C.byref(rb))
+
+
+def integrate_colors(color, rgb, vmap, trunc, R_inv, t, intr, cell, rb, max_weight=255):
+    """Colour integration in place on `color` (uint8 [n, 4] records r, g, b, w); returns the count of
+    voxels updated."""
+    n = np.zeros(1, np.uint64)
+    lib.or_integrate_colors(_p(color), _p(np.ascontiguousarray(rgb, np.uint8)), _p(f32(vmap)), trunc, _p(f32(R_inv)),
+                            _p(f32(t)), C.byref(intr), _p(f32(cell)), C.byref(rb), max_weight, _p(n))
+    return int(n[0])
 
 
 def clean_color_slice(color, mn, mx, rb):

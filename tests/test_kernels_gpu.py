@@ -418,3 +418,35 @@ def test_device_icp_solve_matches_fp64_oracle(tde, orc, cuda):
         np.testing.assert_allclose(got_pose[i, 9:], t2, rtol=0, atol=1e-11)
         Rm = got_pose[i, :9].reshape(3, 3)
         np.testing.assert_allclose(Rm @ Rm.T, np.eye(3), atol=1e-13)
+
+
+# ---------------------------------------------------------------------------
+# colour integration (Integrate_Colors)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("origin,max_weight", [((0, 0, 0), 255), ((5, 17, 3), 2)])
+def test_integrate_colors_matches_oracle(tde, orc, cuda, small, origin, max_weight):
+    """Three colour integrations into one volume (weights growing, capped at
+    max_weight) from the model surface raycast at each pose: the GPU's brick-
+    culled update equals the oracle's sweep of every voxel, byte for byte."""
+    import torch
+    cfg, scene, traj, intr, depths = small
+    fmt = 1
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt, origin, nframes=4)
+    rb = trb(tde, rb_o)
+    ti = tintr(tde, intr)
+    n = cfg.voxels ** 3
+    col_o = np.zeros((n, 4), np.uint8)
+    col = torch.zeros((n, 4), dtype=torch.uint8, device=cuda)
+    rng = np.random.default_rng(7)
+    updated = 0
+    for k in (1, 2, 3):
+        R, t = pose_parts(traj[k])
+        vmo, _ = orc.raycast(vol_o, fmt, rb_o, intr, R, t, cfg.trunc_m, cell)
+        rgb = rng.integers(0, 256, (cfg.rows, cfg.cols, 3), dtype=np.uint8)
+        updated += orc.integrate_colors(col_o, rgb, vmo, cfg.trunc_m, R.T.copy(), t, intr, cell, rb_o, max_weight)
+        tde.integrate_colors(col, T(rgb, cuda), T(vmo, cuda), ti, R.T.copy(), t, cfg.trunc_m, cell, rb, max_weight)
+    torch.cuda.synchronize()
+    assert updated > 1000
+    got = N(col)
+    assert np.array_equal(got, col_o)
+    assert got[:, 3].max() == min(3, max_weight)
