@@ -97,6 +97,11 @@ struct tde_pipeline {
     unsigned long long *stats = nullptr;
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     uint8_t *satflags = nullptr;  // per logical brick: every voxel at f = 1, maximum weight
+    // colour volume (tde_pipeline_enable_color): RGB frames per input set
+    tde_color *colvol = nullptr;
+    uint8_t *rgb[2] = {};
+    void *cscratch = nullptr;
+    int color_max_weight = 0;
     void *volume = nullptr;
     tde_refiner *refiner = nullptr;  // replaces the bilateral filter when set
     // volume shifts: extraction scratch and point buffers, grown on demand
@@ -104,6 +109,7 @@ struct tde_pipeline {
     size_t slab_scratch_bytes = 0;
     tde_xyzi *slab_points = nullptr;
     float *slab_weights = nullptr;
+    tde_color *slab_colors = nullptr;
     uint32_t slab_capacity = 0;
     uint32_t *slab_count = nullptr;
     // graphs per input set: each segment, and the main-stream part of a frame
@@ -121,6 +127,15 @@ namespace {
 template <class T> int dalloc(T **p, size_t count, const char *what) {
     TDE_CUDA(cudaMalloc((void **)p, count * sizeof(T)), what);
     return TDE_OK;
+}
+
+// The model maps (level 0) cast from the published camera pose.
+int cast_model(tde_pipeline *p, cudaStream_t s) {
+    const tde_pipeline_config &c = p->cfg;
+    tde_point3f t0{0, 0, 0};
+    tde_matrix3f R0{};
+    return launch_raycast(p->volume, c.tsdf_format, p->vmod[0], p->nmod[0], t0, R0, c.trunc, p->intr[0], p->rb, p->cell,
+                          p->cam, p->negflags, s);
 }
 
 // Records one segment for input set `set` onto stream s.
@@ -181,10 +196,14 @@ int record_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
                                 p->satflags);
     }
     case SEG_RAYCAST: {
-        tde_point3f t0{0, 0, 0};
-        tde_matrix3f R0{};
-        return launch_raycast(p->volume, c.tsdf_format, p->vmod[0], p->nmod[0], t0, R0, c.trunc, p->intr[0], p->rb,
-                              p->cell, p->cam, p->negflags, s);
+        TDE_TRY(cast_model(p, s));
+        if (!p->colvol) return TDE_OK;
+        // colour at the model surface just cast from this frame's pose
+        IntegrateParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.trunc = c.trunc; P.max_weight = p->color_max_weight; P.intr = p->intr[0]; P.rb = p->rb; P.cell = p->cell;
+        P.n = voxel_count(p->rb); P.dpose = p->cam;
+        return launch_integrate_colors(p->colvol, p->rgb[set], p->vmod[0], P, p->cscratch, nullptr, s);
     }
     case SEG_RESIZE:
         if (p->levels < 2) return TDE_OK;
@@ -304,6 +323,7 @@ void release(tde_pipeline *p) {
     cudaFree(p->st); cudaFree(p->cam); cudaFree(p->out);
     cudaFree(p->stats); cudaFree(p->volume); cudaFree(p->negflags); cudaFree(p->satflags);
     cudaFree(p->slab_scratch); cudaFree(p->slab_points); cudaFree(p->slab_weights); cudaFree(p->slab_count);
+    cudaFree(p->slab_colors); cudaFree(p->colvol); cudaFree(p->rgb[0]); cudaFree(p->rgb[1]); cudaFree(p->cscratch);
     if (p->pre_stream) cudaStreamDestroy(p->pre_stream);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -400,9 +420,14 @@ int tde_pipeline_destroy(tde_pipeline *p) {
 
 void *tde_pipeline_stream(tde_pipeline *p) { return p ? (void *)p->stream : nullptr; }
 
-int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose_out12,
-                         int *status_out) {
+int tde_pipeline_enqueue_rgbd(tde_pipeline *p, const uint16_t *depth, const uint8_t *rgb, int on_device,
+                              double *pose_out12, int *status_out) {
     if (!p || !depth) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enqueue: null argument");
+    if ((p->colvol != nullptr) != (rgb != nullptr))
+        return set_error(TDE_ERR_INVALID_ARG, p->colvol ? "pipeline_enqueue: the colour volume needs an RGB frame"
+                                                        : "pipeline_enqueue: an RGB frame needs tde_pipeline_enable_color");
+    const int depth_on_device = on_device;
+    const size_t rgb_bytes = (size_t)p->cfg.intr.cols * p->cfg.intr.rows * 3;
     const size_t bytes = (size_t)p->cfg.intr.cols * p->cfg.intr.rows * sizeof(uint16_t);
     const cudaMemcpyKind kind = depth_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const int set = p->frames & 1;
@@ -413,6 +438,7 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
         // events brackets one stage alone
         cudaEvent_t *ev = &p->ev[kEvents * p->timing_n];
         TDE_CUDA(cudaMemcpyAsync(p->raw[set], depth, bytes, kind, p->stream), "depth upload");
+        if (rgb) TDE_CUDA(cudaMemcpyAsync(p->rgb[set], rgb, rgb_bytes, kind, p->stream), "rgb upload");
         const Segment order[kStages] = {SEG_PRE, first ? SEG_POST_FIRST : SEG_ICP, SEG_INTEGRATE, SEG_RAYCAST,
                                         SEG_RESIZE};
         TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
@@ -426,6 +452,7 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
         // longer reads this input set
         TDE_CUDA(cudaStreamWaitEvent(p->pre_stream, p->set_free[set], 0), "wait");
         TDE_CUDA(cudaMemcpyAsync(p->raw[set], depth, bytes, kind, p->pre_stream), "depth upload");
+        if (rgb) TDE_CUDA(cudaMemcpyAsync(p->rgb[set], rgb, rgb_bytes, kind, p->pre_stream), "rgb upload");
         TDE_TRY(run_segment(p, SEG_PRE, set, p->pre_stream));
         TDE_CUDA(cudaEventRecord(p->pre_done[set], p->pre_stream), "event");
         TDE_CUDA(cudaStreamWaitEvent(p->stream, p->pre_done[set], 0), "wait");
@@ -445,6 +472,36 @@ int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_de
         TDE_CUDA(cudaMemcpyAsync(status_out, &p->out->status, sizeof(int), cudaMemcpyDeviceToHost, p->stream),
                  "status download");
     p->frames++;
+    return TDE_OK;
+}
+
+int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose_out12,
+                         int *status_out) {
+    return tde_pipeline_enqueue_rgbd(p, depth, nullptr, depth_on_device, pose_out12, status_out);
+}
+
+int tde_pipeline_enable_color(tde_pipeline *p, int max_weight) {
+    if (!p || max_weight < 1) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enable_color: bad argument");
+    TDE_TRY(tde_pipeline_sync(p));
+    if (!p->colvol) {
+        const size_t n = voxel_count(p->rb), px = (size_t)p->cfg.intr.cols * p->cfg.intr.rows;
+        int st;
+        if ((st = dalloc(&p->colvol, n, "colour volume")) || (st = dalloc(&p->rgb[0], 3 * px, "rgb frame")) ||
+            (st = dalloc(&p->rgb[1], 3 * px, "rgb frame")) ||
+            (st = dalloc(reinterpret_cast<char **>(&p->cscratch),
+                         integrate_colors_scratch_bytes(p->cfg.intr.cols, p->cfg.intr.rows, p->rb), "colour scratch")))
+            return st;
+        TDE_CUDA(cudaMemsetAsync(p->colvol, 0, n * sizeof(tde_color), p->stream), "colour volume");
+    }
+    p->color_max_weight = max_weight;
+    TDE_TRY(tde_pipeline_sync(p));
+    if (p->cfg.use_graphs) return capture_all(p);
+    return TDE_OK;
+}
+
+int tde_pipeline_color_volume(tde_pipeline *p, tde_color **color_volume) {
+    if (!p || !color_volume) return set_error(TDE_ERR_INVALID_ARG, "pipeline_color_volume: null");
+    *color_volume = p->colvol;
     return TDE_OK;
 }
 
@@ -553,9 +610,10 @@ int tde_pipeline_launches_per_frame(tde_pipeline *p) {
     for (int l = 0; l < p->levels; ++l) icp += p->cfg.icp_iters[l];
     // bilateral (or the refiner's 11 convolutions + the level-0 vertex map),
     // pyramid levels, normal maps, scaled depth, depth tiles; ICP, brick
-    // cull, integrate, raycast, the model-map pyramid
+    // cull, integrate, raycast, the model-map pyramid; with colour, model
+    // distances, their tiles, the colour brick cull and the colour update
     const int pre = p->refiner ? 12 : 1;
-    return pre + (p->levels - 1) + p->levels + 2 + icp + 1 + 1 + 1 + (p->levels > 1 ? 1 : 0);
+    return pre + (p->levels - 1) + p->levels + 2 + icp + 1 + 1 + 1 + (p->levels > 1 ? 1 : 0) + (p->colvol ? 4 : 0);
 }
 
 int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb) {
@@ -652,6 +710,11 @@ int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, in
 
 int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, uint32_t capacity,
                        uint32_t *count) {
+    return tde_pipeline_shift_ex(p, delta3, points, weights, nullptr, capacity, count);
+}
+
+int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, tde_color *colors,
+                          uint32_t capacity, uint32_t *count) {
     if (!p || !delta3 || !count || (capacity && !points))
         return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift: bad argument");
     const int *N = &p->rb.voxels_size.x;
@@ -680,9 +743,9 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
     }
     if (!p->slab_count) TDE_CUDA(cudaMalloc((void **)&p->slab_count, sizeof(uint32_t)), "pipeline_shift: count");
     for (int pass = 0; pass < 2; ++pass) {
-        TDE_TRY(tde_extract_slice(p->volume, p->cfg.tsdf_format, nullptr, mn, mx, &p->rb, p->slab_scratch,
-                                  p->slab_scratch_bytes, p->slab_points, nullptr, p->slab_weights, p->slab_capacity,
-                                  p->slab_count, s));
+        TDE_TRY(tde_extract_slice(p->volume, p->cfg.tsdf_format, p->colvol, mn, mx, &p->rb, p->slab_scratch,
+                                  p->slab_scratch_bytes, p->slab_points, p->colvol ? p->slab_colors : nullptr,
+                                  p->slab_weights, p->slab_capacity, p->slab_count, s));
         uint32_t n = 0;
         TDE_CUDA(cudaMemcpyAsync(&n, p->slab_count, sizeof(n), cudaMemcpyDeviceToHost, s), "pipeline_shift: count");
         TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift: count");
@@ -692,11 +755,14 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
         }
         cudaFree(p->slab_points);
         cudaFree(p->slab_weights);
+        cudaFree(p->slab_colors);
         p->slab_points = nullptr;
         p->slab_weights = nullptr;
+        p->slab_colors = nullptr;
         const uint32_t cap = n + n / 4 + 1024;
         TDE_CUDA(cudaMalloc((void **)&p->slab_points, (size_t)cap * sizeof(tde_xyzi)), "pipeline_shift: points");
         TDE_CUDA(cudaMalloc((void **)&p->slab_weights, (size_t)cap * sizeof(float)), "pipeline_shift: weights");
+        TDE_CUDA(cudaMalloc((void **)&p->slab_colors, (size_t)cap * sizeof(tde_color)), "pipeline_shift: colours");
         p->slab_capacity = cap;
     }
     const uint32_t ncopy = *count < capacity ? *count : capacity;
@@ -706,8 +772,12 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
         if (weights)
             TDE_CUDA(cudaMemcpy(weights, p->slab_weights, (size_t)ncopy * sizeof(float), cudaMemcpyDeviceToHost),
                      "pipeline_shift: weights");
+        if (colors && p->colvol)
+            TDE_CUDA(cudaMemcpy(colors, p->slab_colors, (size_t)ncopy * sizeof(tde_color), cudaMemcpyDeviceToHost),
+                     "pipeline_shift: colours");
     }
     TDE_TRY(tde_clean_tsdf_slice(p->volume, p->cfg.tsdf_format, mn, mx, &p->rb, s));
+    if (p->colvol) TDE_TRY(tde_clean_color_slice(p->colvol, mn, mx, &p->rb, s));
     // logical bricks name other voxels after the shift (and the slab was cleaned)
     TDE_CUDA(cudaMemsetAsync(p->satflags, 0, brick_count(p->rb), s), "pipeline_shift: saturation flags");
     // brick flags only ever over-approximate; after cleaning, the cleared
@@ -736,7 +806,7 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
     for (int a = 0; a < 3; ++a) cam.t[a] = (float)pose[9 + a];
     cam.tracking_ok = 1;
     TDE_CUDA(cudaMemcpyAsync(p->cam, &cam, sizeof(cam), cudaMemcpyHostToDevice, s), "pipeline_shift: camera");
-    TDE_TRY(record_segment(p, SEG_RAYCAST, 0, s));
+    TDE_TRY(cast_model(p, s));
     TDE_TRY(record_segment(p, SEG_RESIZE, 0, s));
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift");
     if (p->cfg.use_graphs) return capture_all(p);

@@ -40,6 +40,10 @@ declare("tde_pipeline_model_depth", I, [P, P])
 declare("tde_pipeline_raycast_records", I, [P, I, C.POINTER(C.c_uint64)])
 declare("tde_pipeline_shift_needed", I, [P, F, F, P])
 declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
+declare("tde_pipeline_shift_ex", I, [P, P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
+declare("tde_pipeline_enqueue_rgbd", I, [P, P, P, I, P, P])
+declare("tde_pipeline_enable_color", I, [P, I])
+declare("tde_pipeline_color_volume", I, [P, C.POINTER(P)])
 
 
 def config_from(cfg, use_graphs=True, integrate_stats=False, levels=3) -> PipelineConfig:
@@ -101,6 +105,29 @@ class Pipeline:
         else:
             check(lib.tde_pipeline_process(self._h, depth.data_ptr(), 1, pose.ctypes.data_as(P), C.byref(st)))
         return pose, st.value
+
+    def enable_color(self, max_weight: int = 255):
+        """Adds a colour volume; every frame then needs an RGB image (enqueue_rgbd / process_rgbd)."""
+        check(lib.tde_pipeline_enable_color(self._h, max_weight))
+
+    def enqueue_rgbd(self, depth_ptr: int, rgb_ptr: int, on_device: bool, pose_out_ptr=None, status_out_ptr=None):
+        check(lib.tde_pipeline_enqueue_rgbd(self._h, depth_ptr, rgb_ptr, int(on_device), pose_out_ptr, status_out_ptr))
+
+    def process_rgbd(self, depth: np.ndarray, rgb: np.ndarray) -> tuple[np.ndarray, int]:
+        """Blocking RGB-D frame from host arrays: depth uint16 [rows, cols], rgb uint8 [rows, cols, 3]."""
+        d = np.ascontiguousarray(depth, np.uint16)
+        c = np.ascontiguousarray(rgb, np.uint8)
+        pose = np.zeros(12, np.float64)
+        st = np.zeros(1, np.int32)
+        check(lib.tde_pipeline_enqueue_rgbd(self._h, d.ctypes.data_as(P), c.ctypes.data_as(P), 0,
+                                            pose.ctypes.data_as(P), st.ctypes.data_as(P)))
+        self.sync()
+        return pose, int(st[0])
+
+    def color_volume(self) -> int:
+        v = P()
+        check(lib.tde_pipeline_color_volume(self._h, C.byref(v)))
+        return v.value
 
     def sync(self):
         check(lib.tde_pipeline_sync(self._h))
@@ -180,14 +207,20 @@ class Pipeline:
     def shift(self, delta, capacity: int = 1 << 22):
         """Shift the volume by delta voxels; returns the outgoing slab's points
         [n,4] (logical voxel units before the shift) and their weights."""
+        pts, w, _, n = self.shift_colors(delta, capacity)
+        return pts, w, n
+
+    def shift_colors(self, delta, capacity: int = 1 << 22):
+        """As shift, and the points' colours uint8 [n, 4] (zeros without a colour volume)."""
         d = np.ascontiguousarray(delta, np.int32)
         pts = np.zeros((capacity, 4), np.float32)
         w = np.zeros(capacity, np.float32)
+        col = np.zeros((capacity, 4), np.uint8)
         n = C.c_uint32()
-        check(lib.tde_pipeline_shift(self._h, d.ctypes.data_as(P), pts.ctypes.data_as(P), w.ctypes.data_as(P),
-                                     capacity, C.byref(n)))
+        check(lib.tde_pipeline_shift_ex(self._h, d.ctypes.data_as(P), pts.ctypes.data_as(P), w.ctypes.data_as(P),
+                                        col.ctypes.data_as(P), capacity, C.byref(n)))
         k = min(n.value, capacity)
-        return pts[:k], w[:k], n.value
+        return pts[:k], w[:k], col[:k], n.value
 
     def raycast_records(self, skip_empty: bool = True) -> int:
         """Distinct voxel records a raycast of the current model reads."""

@@ -65,6 +65,18 @@ void *tde_pipeline_stream(tde_pipeline *p);
  * reading.  Nothing blocks. */
 int tde_pipeline_enqueue(tde_pipeline *p, const uint16_t *depth, int depth_on_device, double *pose_out12,
                          int *status_out);
+/* RGB-D frame: as tde_pipeline_enqueue, with rgb = cols x rows pixels of 3
+ * bytes (r, g, b) registered to the depth frame (host or device as the
+ * depth); required once tde_pipeline_enable_color was called, refused before.
+ * The colour volume is updated right after the frame's raycast, at the model
+ * surface cast from the frame's pose (tde_integrate_colors semantics). */
+int tde_pipeline_enqueue_rgbd(tde_pipeline *p, const uint16_t *depth, const uint8_t *rgb, int on_device,
+                              double *pose_out12, int *status_out);
+/* Adds a colour volume (one tde_color per voxel, zeroed; synchronises) whose
+ * weights cap at max_weight (<= 255 effective). */
+int tde_pipeline_enable_color(tde_pipeline *p, int max_weight);
+/* The colour volume (device; NULL without tde_pipeline_enable_color). */
+int tde_pipeline_color_volume(tde_pipeline *p, tde_color **color_volume);
 /* Block until all enqueued work is done. */
 int tde_pipeline_sync(tde_pipeline *p);
 /* Blocking convenience: enqueue, wait, return the pose (any host memory). */
@@ -122,6 +134,10 @@ int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, in
  * position of a point = origin_metric (before the shift) + point * cell. */
 int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, uint32_t capacity,
                        uint32_t *count);
+/* As tde_pipeline_shift; with a colour volume, `colors` (host, may be NULL)
+ * receives the points' colours and the colour slab is cleaned as well. */
+int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, tde_color *colors,
+                          uint32_t capacity, uint32_t *count);
 
 /* Measurement: casts the current model again from the last frame's pose
  * (into scratch maps) and counts the distinct voxel records the raycast

@@ -230,3 +230,40 @@ def test_saturated_brick_skip_is_exact(cuda, tde, seq):
         ref = vol.cpu().numpy()
         assert np.array_equal(got, ref)
     assert swept[4] < swept[128], swept
+
+
+def test_color_pipeline_matches_c_abi_replay(cuda, tde, seq):
+    """RGB-D frames: the pipeline updates its colour volume right after each
+    frame's raycast; replaying each frame's model map, pose and RGB image
+    through the C-ABI colour integration gives the same volume, byte for byte.
+    Plain enqueue is refused once colour is on."""
+    import torch
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    p = pl.Pipeline(cfg, traj[0])
+    p.enable_color(max_weight=4)
+    with pytest.raises(RuntimeError):
+        p.process(depths[0])
+    rng = np.random.default_rng(3)
+    n = cfg.voxels ** 3
+    ref = torch.zeros((n, 4), dtype=torch.uint8, device=cuda)
+    intr = tde.Intrinsics(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    cell = float(np.float32(np.float32(cfg.volume_m) / np.float32(cfg.voxels)))
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    for d in depths:
+        rgb = rng.integers(0, 256, (cfg.rows, cfg.cols, 3), dtype=np.uint8)
+        pose, st = p.process_rgbd(d, rgb)
+        assert st == 0
+        vptr, _ = p.model_maps(0)
+        vm = torch.empty((cfg.rows, cfg.cols, 3), dtype=torch.float32, device=cuda)
+        tde.check(tde.lib.tde_memcpy(C.c_void_p(vm.data_ptr()), C.c_void_p(vptr), vm.numel() * 4, 2))
+        _, rb = p.volume()
+        R = pose[:9].reshape(3, 3)
+        tde.integrate_colors(ref, torch.from_numpy(rgb).to(cuda), vm, intr, np.ascontiguousarray(R.T), pose[9:],
+                             cfg.trunc_m, [cell] * 3, rb, max_weight=4)
+    torch.cuda.synchronize()
+    got = np.zeros((n, 4), np.uint8)
+    tde.check(tde.lib.tde_memcpy(got.ctypes.data_as(C.c_void_p), C.c_void_p(p.color_volume()), got.nbytes, 1))
+    assert np.array_equal(got, ref.cpu().numpy())
+    assert (got[:, 3] > 0).sum() > 1000 and got[:, 3].max() == 4
+    p.close()
