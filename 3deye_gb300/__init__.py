@@ -21,8 +21,8 @@ __all__ = [
     "TdeError", "lib", "check", "last_error", "mat3", "vec3", "round_buffer", "ptr", "stream_ptr",
     "tsdf_volume_bytes", "tsdf_init", "bilateral_filter", "depth_pyramid_level", "vertex_map", "normal_map",
     "estimate_combined", "transform_estimation", "clean_buff", "scale_depth", "integrate_tsdf", "raycast",
-    "resize_vertex_map", "resize_normal_map", "transform_maps", "extract_slice", "clean_tsdf_slice",
-    "clean_color_slice",
+    "resize_vertex_map", "resize_normal_map", "transform_maps", "extract_slice", "extract_tsdf_volume",
+    "extract_color_volume", "clean_tsdf_slice", "clean_color_slice",
 ]
 
 
@@ -209,6 +209,41 @@ def extract_slice(volume, fmt, color, min_bounds, max_bounds, rb: RoundBuffer, c
             return pts[:k], cols[:k], (wts[:k] if wts is not None else None), n
         cap = n
     raise TdeError(-5, "extract_slice: capacity retry failed")
+
+
+def extract_tsdf_volume(volume, fmt, rb: RoundBuffer, cell_size, capacity=None, weights=False, stream=None):
+    """Extract_Tsdf_Volume (opencl_wrappers.cpp:440-543): every zero crossing
+    of the volume as the metric centre {(i + 0.5) * cell, 1} of the voxel it
+    names.  Returns (points [n, 4], weights-or-None, total count); grows the
+    output once if it was too small."""
+    torch = _torch()
+    dev = volume.device
+    scratch = torch.empty(lib.tde_extract_tsdf_volume_scratch_bytes(C.byref(rb)), dtype=torch.uint8, device=dev)
+    count = torch.zeros(1, dtype=torch.int32, device=dev)
+    cap = 1 << 20 if capacity is None else int(capacity)
+    for _ in range(2):
+        pts = torch.empty((max(cap, 1), 4), dtype=torch.float32, device=dev)
+        wts = torch.empty(max(cap, 1), dtype=torch.float32, device=dev) if weights else None
+        check(lib.tde_extract_tsdf_volume(ptr(volume), fmt, C.byref(rb), Point3f(*cell_size), ptr(scratch),
+                                          scratch.numel(), ptr(pts), ptr(wts) if wts is not None else None, cap,
+                                          ptr(count), stream_ptr(stream)))
+        n = int(count.item())
+        if n <= cap or capacity is not None:
+            k = min(n, cap)
+            return pts[:k], (wts[:k] if wts is not None else None), n
+        cap = n
+    raise TdeError(-5, "extract_tsdf_volume: capacity retry failed")
+
+
+def extract_color_volume(color, rb: RoundBuffer, points, cell_size, stream=None):
+    """Extract_Color_Volume (opencl_wrappers.cpp:545-581): the colour of the
+    voxel floor(p / cell) holding each point; uint8 [n, 4]."""
+    torch = _torch()
+    pts = points.contiguous()
+    out = torch.zeros((pts.shape[0], 4), dtype=torch.uint8, device=pts.device)
+    check(lib.tde_extract_color_volume(ptr(color), C.byref(rb), ptr(pts), pts.shape[0], Point3f(*cell_size),
+                                       ptr(out), stream_ptr(stream)))
+    return out
 
 
 def clean_tsdf_slice(volume, fmt, min_bounds, max_bounds, rb: RoundBuffer, stream=None):

@@ -1,5 +1,6 @@
 // capi.cu -- extern "C" entry points of tde_capi.h: argument validation,
 // error reporting and dispatch to the kernel launchers.
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -437,7 +438,40 @@ int tde_extract_slice(const void *volume, int format, const tde_color *color_vol
     TDE_REQUIRE(valid_format(format), "extract_slice: bad format %d", format);
     TDE_REQUIRE(valid_round_buffer(rb), "extract_slice: bad round_buffer");
     return launch_extract_slice(volume, format, color_volume, min_bounds, max_bounds, *rb, scratch, scratch_bytes,
-                                points, colors, weights, capacity, count_device, as_stream(stream));
+                                points, colors, weights, capacity, count_device, 0, nullptr, as_stream(stream));
+}
+
+size_t tde_extract_tsdf_volume_scratch_bytes(const tde_round_buffer *rb) {
+    if (!valid_round_buffer(rb)) return 0;
+    return slab_scratch_bytes(*rb);
+}
+
+static bool valid_cell(tde_point3f c) {
+    return std::isfinite(c.x) && std::isfinite(c.y) && std::isfinite(c.z) && c.x > 0.f && c.y > 0.f && c.z > 0.f;
+}
+
+int tde_extract_tsdf_volume(const void *volume, int format, const tde_round_buffer *rb, tde_point3f cell_size,
+                            void *scratch, size_t scratch_bytes, tde_xyzi *points, float *weights, uint32_t capacity,
+                            uint32_t *count_device, void *stream) {
+    TDE_REQUIRE(volume && scratch && count_device, "extract_tsdf_volume: null buffer");
+    TDE_REQUIRE(points || capacity == 0, "extract_tsdf_volume: null points with capacity %u", capacity);
+    TDE_REQUIRE(valid_format(format), "extract_tsdf_volume: bad format %d", format);
+    TDE_REQUIRE(valid_round_buffer(rb), "extract_tsdf_volume: bad round_buffer");
+    TDE_REQUIRE(valid_cell(cell_size), "extract_tsdf_volume: cell size must be finite and positive");
+    // every voxel is in the zone: the slab scan over the whole volume, in
+    // chunks of determine_extract_step(depth, divisor 2)
+    const tde_point3i lo = {INT_MIN, INT_MIN, INT_MIN}, hi = {INT_MAX, INT_MAX, INT_MAX};
+    return launch_extract_slice(volume, format, nullptr, lo, hi, *rb, scratch, scratch_bytes, points, nullptr,
+                                weights, capacity, count_device, slab_chunk_depth(rb->voxels_size.z, 2), &cell_size,
+                                as_stream(stream));
+}
+
+int tde_extract_color_volume(const tde_color *color_volume, const tde_round_buffer *rb, const tde_xyzi *points,
+                             uint32_t num_points, tde_point3f cell_size, tde_color *colors, void *stream) {
+    TDE_REQUIRE(color_volume && (num_points == 0 || (points && colors)), "extract_color_volume: null buffer");
+    TDE_REQUIRE(valid_round_buffer(rb), "extract_color_volume: bad round_buffer");
+    TDE_REQUIRE(valid_cell(cell_size), "extract_color_volume: cell size must be finite and positive");
+    return launch_gather_colors(color_volume, *rb, points, num_points, cell_size, colors, as_stream(stream));
 }
 
 int tde_clean_tsdf_slice(void *volume, int format, tde_point3i min_bounds, tde_point3i max_bounds,

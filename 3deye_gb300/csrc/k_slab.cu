@@ -32,6 +32,8 @@ struct SlabParams {
     int ty;              // rows per tile
     int tiles_per_z;     // ceil(H / ty)
     int tiles_per_chunk; // step * tiles_per_z
+    int metric;          // points as metric voxel centres (x + 0.5) * cell
+    tde_point3f cell;
 };
 
 __device__ __forceinline__ bool color_set(tde_color c) { return (c.r | c.g | c.b | c.w) != 0; }
@@ -199,7 +201,13 @@ __global__ void __launch_bounds__(kSlabThreads) slab_scatter_kernel(const SlabPa
             if (slot >= capacity) continue;
             const int dx = q == 0, dy = q == 1, dz = q == 2;
             const int nx = x + dx, ny = y + dy, nz = z + dz;
-            pts[slot] = tde_xyzi{(float)nx, (float)ny, (float)nz, 1.0f};
+            float px = (float)nx, py = (float)ny, pz = (float)nz;
+            if (p.metric) {
+                px = __fmul_rn(__fadd_rn(px, 0.5f), p.cell.x);
+                py = __fmul_rn(__fadd_rn(py, 0.5f), p.cell.y);
+                pz = __fmul_rn(__fadd_rn(pz, 0.5f), p.cell.z);
+            }
+            pts[slot] = tde_xyzi{px, py, pz, 1.0f};
             const size_t a = voxel_address(nx, ny, nz, p.rb);
             if (cols) cols[slot] = p.color ? p.color[a] : tde_color{0, 0, 0, 0};
             if (wts) {
@@ -242,6 +250,25 @@ __global__ void clean_color_kernel(tde_color *__restrict__ col, const tde_point3
     for (int z = z0; z <= z1; ++z) col[voxel_address(x, y, z, rb)] = tde_color{0, 0, 0, 0};
 }
 
+// Extract_Color_Volume (opencl_wrappers.cpp:545-581, kernel extract_colors
+// absent): the voxel holding a metric point is floor(p / cell) per axis
+// (correctly rounded division); points outside the volume get zero colour.
+__global__ void gather_colors_kernel(const tde_color *__restrict__ color, const tde_round_buffer rb,
+                                     const tde_xyzi *__restrict__ pts, uint32_t n, tde_point3f cell,
+                                     tde_color *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const tde_xyzi q = pts[i];
+    const float fx = floorf(__fdiv_rn(q.x, cell.x)), fy = floorf(__fdiv_rn(q.y, cell.y)),
+                fz = floorf(__fdiv_rn(q.z, cell.z));
+    tde_color c = {0, 0, 0, 0};
+    // NaN fails every comparison
+    if (fx >= 0.f && fy >= 0.f && fz >= 0.f && fx < (float)rb.voxels_size.x && fy < (float)rb.voxels_size.y &&
+        fz < (float)rb.voxels_size.z)
+        c = color[voxel_address((int)fx, (int)fy, (int)fz, rb)];
+    out[i] = c;
+}
+
 void slab_geometry(const tde_round_buffer &rb, SlabParams &p) {
     const int W = rb.voxels_size.x, H = rb.voxels_size.y;
     p.ty = max(1, min(H, 8192 / max(1, W)));
@@ -251,17 +278,19 @@ void slab_geometry(const tde_round_buffer &rb, SlabParams &p) {
 
 }  // namespace
 
-int slab_chunk_depth(int depth) {
+int slab_chunk_depth(int depth, int divisor) {
     unsigned step = 0, n = 0;
-    if (tde_determine_extract_step((unsigned)depth, 4, &step, &n) == TDE_OK) return (int)step;
+    if (tde_determine_extract_step((unsigned)depth, divisor, &step, &n) == TDE_OK) return (int)step;
     // depths outside the reference's table: 64-voxel chunks when they divide it
     if (depth % 64 == 0) return 64;
     return depth;
 }
 
+// chunks * 4 planes * (step * tiles_per_z) counts = 4 * depth * tiles_per_z:
+// the same for every chunk depth that divides the volume depth.
 size_t slab_scratch_bytes(const tde_round_buffer &rb) {
     SlabParams p;
-    p.step = slab_chunk_depth(rb.voxels_size.z);
+    p.step = slab_chunk_depth(rb.voxels_size.z, 4);
     slab_geometry(rb, p);
     const size_t chunks = (size_t)rb.voxels_size.z / p.step;
     return (chunks * 4 * (size_t)p.tiles_per_chunk + 64) * sizeof(uint32_t);
@@ -269,10 +298,16 @@ size_t slab_scratch_bytes(const tde_round_buffer &rb) {
 
 int launch_extract_slice(const void *vol, int fmt, const tde_color *color, tde_point3i mn, tde_point3i mx,
                          const tde_round_buffer &rb, void *scratch, size_t scratch_bytes, tde_xyzi *pts,
-                         tde_color *cols, float *wts, uint32_t capacity, uint32_t *count, cudaStream_t stream) {
+                         tde_color *cols, float *wts, uint32_t capacity, uint32_t *count, int step,
+                         const tde_point3f *cell, cudaStream_t stream) {
     SlabParams p;
     p.vol = vol; p.color = color; p.rb = rb; p.mn = mn; p.mx = mx; p.n = voxel_count(rb);
-    p.step = slab_chunk_depth(rb.voxels_size.z);
+    p.metric = cell != nullptr;
+    p.cell = cell ? *cell : tde_point3f{1.f, 1.f, 1.f};
+    p.step = step > 0 ? step : slab_chunk_depth(rb.voxels_size.z, 4);
+    if (rb.voxels_size.z % p.step)
+        return set_error(TDE_ERR_INVALID_ARG, "extract_slice: chunk depth %d does not divide %d", p.step,
+                         rb.voxels_size.z);
     slab_geometry(rb, p);
     const int chunks = rb.voxels_size.z / p.step;
     const int ntiles = chunks * p.tiles_per_chunk;
@@ -292,6 +327,13 @@ int launch_extract_slice(const void *vol, int fmt, const tde_color *color, tde_p
         slab_scatter_kernel<FMT><<<ntiles, kSlabThreads, 0, stream>>>(p, counts, pts, cols, wts, capacity);
         return check_launch("extract_slice/scatter");
     });
+}
+
+int launch_gather_colors(const tde_color *color, const tde_round_buffer &rb, const tde_xyzi *pts, uint32_t n,
+                         tde_point3f cell, tde_color *out, cudaStream_t stream) {
+    if (!n) return TDE_OK;
+    gather_colors_kernel<<<div_up(n, 256u), 256, 0, stream>>>(color, rb, pts, n, cell, out);
+    return check_launch("extract_color_volume");
 }
 
 int launch_clean_tsdf_slice(void *vol, int fmt, tde_point3i mn, tde_point3i mx, const tde_round_buffer &rb,

@@ -331,6 +331,61 @@ void release(tde_pipeline *p) {
 
 }  // namespace
 
+// Count pass and scatter into the pipeline's point buffers (grown once when
+// short); the total goes to *count.  `launch(capacity)` enqueues one
+// extraction on the pipeline stream.
+template <class Launch>
+static int extract_points(tde_pipeline *p, const char *what, uint32_t *count, Launch launch) {
+    cudaStream_t s = p->stream;
+    const size_t need = tde_extract_slice_scratch_bytes(&p->rb);
+    if (need > p->slab_scratch_bytes) {
+        cudaFree(p->slab_scratch);
+        p->slab_scratch = nullptr;
+        p->slab_scratch_bytes = 0;
+        TDE_CUDA(cudaMalloc(&p->slab_scratch, need), what);
+        p->slab_scratch_bytes = need;
+    }
+    if (!p->slab_count) TDE_CUDA(cudaMalloc((void **)&p->slab_count, sizeof(uint32_t)), what);
+    for (int pass = 0; pass < 2; ++pass) {
+        TDE_TRY(launch(p->slab_capacity));
+        uint32_t n = 0;
+        TDE_CUDA(cudaMemcpyAsync(&n, p->slab_count, sizeof(n), cudaMemcpyDeviceToHost, s), what);
+        TDE_CUDA(cudaStreamSynchronize(s), what);
+        if (n <= p->slab_capacity) {
+            *count = n;
+            return TDE_OK;
+        }
+        cudaFree(p->slab_points);
+        cudaFree(p->slab_weights);
+        cudaFree(p->slab_colors);
+        p->slab_points = nullptr;
+        p->slab_weights = nullptr;
+        p->slab_colors = nullptr;
+        p->slab_capacity = 0;
+        const uint32_t cap = n + n / 4 + 1024;
+        TDE_CUDA(cudaMalloc((void **)&p->slab_points, (size_t)cap * sizeof(tde_xyzi)), what);
+        TDE_CUDA(cudaMalloc((void **)&p->slab_weights, (size_t)cap * sizeof(float)), what);
+        TDE_CUDA(cudaMalloc((void **)&p->slab_colors, (size_t)cap * sizeof(tde_color)), what);
+        p->slab_capacity = cap;
+    }
+    return set_error(TDE_ERR_CAPACITY, "%s: point count changed between passes", what);
+}
+
+// Up to `capacity` of the n extracted points (and weights / colours when
+// asked) to host memory.
+static int points_to_host(tde_pipeline *p, const char *what, uint32_t n, tde_xyzi *points, float *weights,
+                          tde_color *colors, uint32_t capacity) {
+    const uint32_t ncopy = n < capacity ? n : capacity;
+    if (!ncopy) return TDE_OK;
+    TDE_CUDA(cudaMemcpy(points, p->slab_points, (size_t)ncopy * sizeof(tde_xyzi), cudaMemcpyDeviceToHost), what);
+    if (weights)
+        TDE_CUDA(cudaMemcpy(weights, p->slab_weights, (size_t)ncopy * sizeof(float), cudaMemcpyDeviceToHost), what);
+    if (colors)
+        TDE_CUDA(cudaMemcpy(colors, p->slab_colors, (size_t)ncopy * sizeof(tde_color), cudaMemcpyDeviceToHost),
+                 what);
+    return TDE_OK;
+}
+
 extern "C" {
 
 int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, tde_pipeline **out) {
@@ -734,48 +789,12 @@ int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, 
         else if (delta3[a] < 0) { pmn[a] = org[a] + N[a] + delta3[a]; pmx[a] = org[a] + N[a] - 1; }
         else { pmn[a] = 1 << 30; pmx[a] = -(1 << 30); }
     }
-    const size_t need = tde_extract_slice_scratch_bytes(&p->rb);
-    if (need > p->slab_scratch_bytes) {
-        cudaFree(p->slab_scratch);
-        p->slab_scratch = nullptr;
-        TDE_CUDA(cudaMalloc(&p->slab_scratch, need), "pipeline_shift: scratch");
-        p->slab_scratch_bytes = need;
-    }
-    if (!p->slab_count) TDE_CUDA(cudaMalloc((void **)&p->slab_count, sizeof(uint32_t)), "pipeline_shift: count");
-    for (int pass = 0; pass < 2; ++pass) {
-        TDE_TRY(tde_extract_slice(p->volume, p->cfg.tsdf_format, p->colvol, mn, mx, &p->rb, p->slab_scratch,
-                                  p->slab_scratch_bytes, p->slab_points, p->colvol ? p->slab_colors : nullptr,
-                                  p->slab_weights, p->slab_capacity, p->slab_count, s));
-        uint32_t n = 0;
-        TDE_CUDA(cudaMemcpyAsync(&n, p->slab_count, sizeof(n), cudaMemcpyDeviceToHost, s), "pipeline_shift: count");
-        TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift: count");
-        if (n <= p->slab_capacity) {
-            *count = n;
-            break;
-        }
-        cudaFree(p->slab_points);
-        cudaFree(p->slab_weights);
-        cudaFree(p->slab_colors);
-        p->slab_points = nullptr;
-        p->slab_weights = nullptr;
-        p->slab_colors = nullptr;
-        const uint32_t cap = n + n / 4 + 1024;
-        TDE_CUDA(cudaMalloc((void **)&p->slab_points, (size_t)cap * sizeof(tde_xyzi)), "pipeline_shift: points");
-        TDE_CUDA(cudaMalloc((void **)&p->slab_weights, (size_t)cap * sizeof(float)), "pipeline_shift: weights");
-        TDE_CUDA(cudaMalloc((void **)&p->slab_colors, (size_t)cap * sizeof(tde_color)), "pipeline_shift: colours");
-        p->slab_capacity = cap;
-    }
-    const uint32_t ncopy = *count < capacity ? *count : capacity;
-    if (ncopy) {
-        TDE_CUDA(cudaMemcpy(points, p->slab_points, (size_t)ncopy * sizeof(tde_xyzi), cudaMemcpyDeviceToHost),
-                 "pipeline_shift: points");
-        if (weights)
-            TDE_CUDA(cudaMemcpy(weights, p->slab_weights, (size_t)ncopy * sizeof(float), cudaMemcpyDeviceToHost),
-                     "pipeline_shift: weights");
-        if (colors && p->colvol)
-            TDE_CUDA(cudaMemcpy(colors, p->slab_colors, (size_t)ncopy * sizeof(tde_color), cudaMemcpyDeviceToHost),
-                     "pipeline_shift: colours");
-    }
+    TDE_TRY(extract_points(p, "pipeline_shift", count, [&](uint32_t cap) {
+        return tde_extract_slice(p->volume, p->cfg.tsdf_format, p->colvol, mn, mx, &p->rb, p->slab_scratch,
+                                 p->slab_scratch_bytes, p->slab_points, p->colvol ? p->slab_colors : nullptr,
+                                 p->slab_weights, cap, p->slab_count, s);
+    }));
+    TDE_TRY(points_to_host(p, "pipeline_shift", *count, points, weights, p->colvol ? colors : nullptr, capacity));
     TDE_TRY(tde_clean_tsdf_slice(p->volume, p->cfg.tsdf_format, mn, mx, &p->rb, s));
     if (p->colvol) TDE_TRY(tde_clean_color_slice(p->colvol, mn, mx, &p->rb, s));
     // logical bricks name other voxels after the shift (and the slab was cleaned)
@@ -811,6 +830,24 @@ int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, 
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift");
     if (p->cfg.use_graphs) return capture_all(p);
     return TDE_OK;
+}
+
+int tde_pipeline_extract_volume(tde_pipeline *p, tde_xyzi *points, float *weights, tde_color *colors,
+                                uint32_t capacity, uint32_t *count) {
+    if (!p || !count || (capacity && !points))
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_extract_volume: bad argument");
+    TDE_TRY(tde_pipeline_sync(p));
+    cudaStream_t s = p->stream;
+    TDE_TRY(extract_points(p, "pipeline_extract_volume", count, [&](uint32_t cap) {
+        return tde_extract_tsdf_volume(p->volume, p->cfg.tsdf_format, &p->rb, p->cell, p->slab_scratch,
+                                       p->slab_scratch_bytes, p->slab_points, p->slab_weights, cap, p->slab_count,
+                                       s);
+    }));
+    if (p->colvol && colors)
+        TDE_TRY(tde_extract_color_volume(p->colvol, &p->rb, p->slab_points, *count, p->cell, p->slab_colors, s));
+    TDE_CUDA(cudaStreamSynchronize(s), "pipeline_extract_volume");
+    return points_to_host(p, "pipeline_extract_volume", *count, points, weights, p->colvol ? colors : nullptr,
+                          capacity);
 }
 
 int tde_pipeline_set_pose(tde_pipeline *p, const double *pose12) {

@@ -51,10 +51,14 @@ string base_name(const string &n) {
 
 // Slab extraction through the C-ABI: count, size, extract (the reference
 // counts, scans and extracts per chunk, opencl_wrappers.cpp:885-955).
+// Count pass (capacity 0), then the scatter into a buffer of that size.
+// `whole_cell` set: every voxel, no colour plane, metric points
+// (Extract_Tsdf_Volume).
 void extract(point_3i mn, point_3i mx, round_buffer *rb, gpu_array_base *vol, gpu_array_base *color,
-             matrix<Point_XYZI> &pts_out, matrix<Point_Color> *cols_out) {
+             matrix<Point_XYZI> &pts_out, matrix<Point_Color> *cols_out, const point_3f *whole_cell = nullptr) {
+    const bool whole = whole_cell != nullptr;
     const tde_round_buffer *r = RB(rb);
-    size_t sb = tde_extract_slice_scratch_bytes(r);
+    size_t sb = whole ? tde_extract_tsdf_volume_scratch_bytes(r) : tde_extract_slice_scratch_bytes(r);
     if (!sb) throw std::runtime_error("Extract_Slice: bad round_buffer");
     void *scratch = nullptr, *cnt = nullptr, *pts = nullptr, *cols = nullptr;
     check(tde_device_malloc(&scratch, sb), "Extract_Slice");
@@ -64,18 +68,23 @@ void extract(point_3i mn, point_3i mx, round_buffer *rb, gpu_array_base *vol, gp
     try {
         check(tde_device_malloc(&cnt, sizeof(uint32_t)), "Extract_Slice");
         const tde_color *cv = color ? static_cast<const tde_color *>(dev(color, "Extract_Slice colour")) : nullptr;
-        check(tde_extract_slice(dev(vol, "Extract_Slice"), g_tsdf_format, cv, P3(mn), P3(mx), r, scratch, sb, nullptr,
-                                nullptr, nullptr, 0, static_cast<uint32_t *>(cnt), nullptr),
-              "Extract_Slice");
+        auto run = [&](tde_xyzi *p, tde_color *c, uint32_t cap) {
+            if (whole)
+                check(tde_extract_tsdf_volume(dev(vol, "Extract_Tsdf_Volume"), g_tsdf_format, r, *V(*whole_cell),
+                                              scratch, sb, p, nullptr, cap, static_cast<uint32_t *>(cnt), nullptr),
+                      "Extract_Tsdf_Volume");
+            else
+                check(tde_extract_slice(dev(vol, "Extract_Slice"), g_tsdf_format, cv, P3(mn), P3(mx), r, scratch, sb,
+                                        p, c, nullptr, cap, static_cast<uint32_t *>(cnt), nullptr),
+                      "Extract_Slice");
+        };
+        run(nullptr, nullptr, 0);
         uint32_t n = 0;
         check(tde_memcpy(&n, cnt, sizeof(n), 1), "Extract_Slice");
         if (n) {
             check(tde_device_malloc(&pts, (size_t)n * sizeof(tde_xyzi)), "Extract_Slice");
             if (cols_out) check(tde_device_malloc(&cols, (size_t)n * sizeof(tde_color)), "Extract_Slice");
-            check(tde_extract_slice(dev(vol, "Extract_Slice"), g_tsdf_format, cv, P3(mn), P3(mx), r, scratch, sb,
-                                    static_cast<tde_xyzi *>(pts), static_cast<tde_color *>(cols), nullptr, n,
-                                    static_cast<uint32_t *>(cnt), nullptr),
-                  "Extract_Slice");
+            run(static_cast<tde_xyzi *>(pts), static_cast<tde_color *>(cols), n);
             matrix<Point_XYZI> part(n);
             check(tde_memcpy(part.data, pts, (size_t)n * sizeof(tde_xyzi), 1), "Extract_Slice");
             pts_out.extend_from(part);
@@ -360,8 +369,41 @@ void Estimate_Combined(matrix_3f &Rotation_Current, vector_3f &Translation_Curre
         }
 }
 
-void Extract_Tsdf_Volume(round_buffer *, const point_3f &, gpu_array_base *, kernel_manager *, matrix<Point_XYZI> &) {
-    throw std::runtime_error("Extract_Tsdf_Volume: whole-volume export is not available in this build");
+// opencl_wrappers.cpp:440-543: every zero crossing as the metric centre of
+// the voxel it names; appends to the cloud, as extend_from does there.
+void Extract_Tsdf_Volume(round_buffer *Round_Buffer, const point_3f &Cell_Size, gpu_array_base *gTsdf_Volume,
+                         kernel_manager *, matrix<Point_XYZI> &Resulting_Cloud_Parallel) {
+    extract(point_3i{}, point_3i{}, Round_Buffer, gTsdf_Volume, nullptr, Resulting_Cloud_Parallel, nullptr,
+            &Cell_Size);
+}
+
+// opencl_wrappers.cpp:545-581: the colour of the voxel holding each point of
+// Vertex_Point_Cloud, into Resulting_Color_Point_Cloud (sized like the cloud
+// by the caller, as there).
+void Extract_Color_Volume(gpu_array_base *gColor_Volume, round_buffer *Round_Buffer,
+                          matrix<Point_XYZI> &Vertex_Point_Cloud, point_3f Cell_Size, opencl_kernel *,
+                          matrix<Point_Color> &Resulting_Color_Point_Cloud) {
+    const uint32_t n = Vertex_Point_Cloud.Get_Num_Of_Elem();
+    if (Resulting_Color_Point_Cloud.Get_Num_Of_Elem() < n)
+        throw std::runtime_error("Extract_Color_Volume: colour cloud smaller than the vertex cloud");
+    if (!n) return;
+    void *pts = nullptr, *cols = nullptr;
+    auto release = [&] { tde_device_free(pts); tde_device_free(cols); };
+    try {
+        check(tde_device_malloc(&pts, (size_t)n * sizeof(tde_xyzi)), "Extract_Color_Volume");
+        check(tde_device_malloc(&cols, (size_t)n * sizeof(tde_color)), "Extract_Color_Volume");
+        check(tde_memcpy(pts, Vertex_Point_Cloud.data, (size_t)n * sizeof(tde_xyzi), 0), "Extract_Color_Volume");
+        check(tde_extract_color_volume(static_cast<const tde_color *>(dev(gColor_Volume, "Extract_Color_Volume")),
+                                       RB(Round_Buffer), static_cast<const tde_xyzi *>(pts), n, *V(Cell_Size),
+                                       static_cast<tde_color *>(cols), nullptr),
+              "Extract_Color_Volume");
+        check(tde_memcpy(Resulting_Color_Point_Cloud.data, cols, (size_t)n * sizeof(tde_color), 1),
+              "Extract_Color_Volume");
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
 }
 
 // opencl_wrappers.cpp:583-683 (three planes: +x, +y, +z)

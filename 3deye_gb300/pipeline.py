@@ -41,6 +41,7 @@ declare("tde_pipeline_raycast_records", I, [P, I, C.POINTER(C.c_uint64)])
 declare("tde_pipeline_shift_needed", I, [P, F, F, P])
 declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_shift_ex", I, [P, P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
+declare("tde_pipeline_extract_volume", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_enqueue_rgbd", I, [P, P, P, I, P, P])
 declare("tde_pipeline_enable_color", I, [P, I])
 declare("tde_pipeline_color_volume", I, [P, C.POINTER(P)])
@@ -221,6 +222,31 @@ class Pipeline:
                                         col.ctypes.data_as(P), capacity, C.byref(n)))
         k = min(n.value, capacity)
         return pts[:k], w[:k], col[:k], n.value
+
+    def extract_volume(self, capacity: int | None = None):
+        """The whole model as zero-crossing points (Extract_Tsdf_Volume):
+        metric voxel centres [n, 4] in the volume frame, their weights and,
+        with a colour volume, colours uint8 [n, 4] (zeros without one).
+        Without `capacity` the buffers are sized from a count pass."""
+        n = C.c_uint32()
+        if capacity is None:
+            check(lib.tde_pipeline_extract_volume(self._h, None, None, None, 0, C.byref(n)))
+            capacity = n.value
+        pts = np.zeros((max(capacity, 1), 4), np.float32)
+        w = np.zeros(max(capacity, 1), np.float32)
+        col = np.zeros((max(capacity, 1), 4), np.uint8)
+        check(lib.tde_pipeline_extract_volume(self._h, pts.ctypes.data_as(P), w.ctypes.data_as(P),
+                                              col.ctypes.data_as(P), capacity, C.byref(n)))
+        k = min(n.value, capacity)
+        return pts[:k], w[:k], col[:k], n.value
+
+    def world_cloud(self, points):
+        """Volume-frame points (as extract_volume returns them) in the world
+        frame: plus the round buffer's origin_metric."""
+        _, rb = self.volume()
+        out = np.array(points, np.float32, copy=True)
+        out[:, :3] += np.array([rb.origin_metric.x, rb.origin_metric.y, rb.origin_metric.z], np.float32)
+        return out
 
     def raycast_records(self, skip_empty: bool = True) -> int:
         """Distinct voxel records a raycast of the current model reads."""

@@ -76,6 +76,10 @@ void Estimate_Combined(matrix_3f &Rotation_Current, vector_3f &Translation_Curre
 void Extract_Tsdf_Volume(round_buffer *Round_Buffer, const point_3f &Cell_Size, gpu_array_base *gTsdf_Volume,
                          kernel_manager *Gpu_Methods, matrix<Point_XYZI> &Resulting_Cloud_Parallel);
 
+void Extract_Color_Volume(gpu_array_base *gColor_Volume, round_buffer *Round_Buffer,
+                          matrix<Point_XYZI> &Vertex_Point_Cloud, point_3f Cell_Size, opencl_kernel *extract_color,
+                          matrix<Point_Color> &Resulting_Color_Point_Cloud);
+
 void Extract_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer, point_3f &Cell_Size,
                         gpu_array_base *gTsdf_Volume, kernel_manager *Gpu_Methods,
                         matrix<Point_XYZI> &Resulting_Tsdf_Cloud);

@@ -325,6 +325,33 @@ int tde_extract_slice(const void *volume, int format, const tde_color *color_vol
                       void *scratch, size_t scratch_bytes, tde_xyzi *points, tde_color *colors,
                       float *weights, uint32_t capacity, uint32_t *count_device, void *stream);
 
+/* Scratch bytes tde_extract_tsdf_volume needs (the same as the slab's). */
+size_t tde_extract_tsdf_volume_scratch_bytes(const tde_round_buffer *rb);
+
+/* Extract_Tsdf_Volume: opencl_wrappers.cpp:440-543.  Its kernels
+ * (scan_the_whole_array, extract_tsdf_cloud) are not in the reference's
+ * sources; the wrapper shows the shape: z chunks of
+ * determine_extract_step(depth, divisor 2), three predicate planes per chunk
+ * (3 * width * height * step), an in-place prefix scan, and a scatter that
+ * is given Cell_Size.  Restated as the slab extraction above with every voxel
+ * in the zone and no colour plane: the same +x/+y/+z predicates (the +z test
+ * stops at the chunk end) in the same per-chunk plane/raster order.  A point
+ * is the metric centre of the voxel it names, {(x+dx+0.5f)*cell.x,
+ * (y+dy+0.5f)*cell.y, (z+dz+0.5f)*cell.z, 1.0f} in logical (origin-relative)
+ * coordinates -- the V of extract_slice_as_cloud.cl:99-112 -- each step
+ * rounded to float.  `weights` (the named voxel's weight) may be NULL.
+ * Reads the volume twice (count, then scatter): HBM-bound. */
+int tde_extract_tsdf_volume(const void *volume, int format, const tde_round_buffer *rb, tde_point3f cell_size,
+                            void *scratch, size_t scratch_bytes, tde_xyzi *points, float *weights, uint32_t capacity,
+                            uint32_t *count_device, void *stream);
+
+/* Extract_Color_Volume: opencl_wrappers.cpp:545-581 (kernel extract_colors,
+ * absent).  colors[i] = colour of the voxel floor(points[i] / cell) (per
+ * axis, correctly rounded float division) of the logical volume; zero for a
+ * point outside it.  Inverts tde_extract_tsdf_volume's voxel centres. */
+int tde_extract_color_volume(const tde_color *color_volume, const tde_round_buffer *rb, const tde_xyzi *points,
+                             uint32_t num_points, tde_point3f cell_size, tde_color *colors, void *stream);
+
 /* Clean_Tsdf_Slice: opencl_wrappers.cpp:835-854 (kernel clean_tsdf_slice,
  * absent): black-zone voxels get f = 0, w = 0. */
 int tde_clean_tsdf_slice(void *volume, int format, tde_point3i min_bounds, tde_point3i max_bounds,

@@ -139,6 +139,16 @@ int tde_pipeline_shift(tde_pipeline *p, const int *delta3, tde_xyzi *points, flo
 int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, float *weights, tde_color *colors,
                           uint32_t capacity, uint32_t *count);
 
+/* Extract_Tsdf_Volume over the pipeline's volume, host-synchronous: every
+ * zero crossing (tde_extract_tsdf_volume semantics and order: metric voxel
+ * centres in the volume frame; world position = origin_metric + point) into
+ * host `points` up to `capacity`, the total to *count.  `weights` (may be
+ * NULL) receives the named voxels' weights; with a colour volume, `colors`
+ * (may be NULL) the colours of the voxels holding the points
+ * (tde_extract_color_volume).  The volume is not changed. */
+int tde_pipeline_extract_volume(tde_pipeline *p, tde_xyzi *points, float *weights, tde_color *colors,
+                                uint32_t capacity, uint32_t *count);
+
 /* Measurement: casts the current model again from the last frame's pose
  * (into scratch maps) and counts the distinct voxel records the raycast
  * reads -- with skip_empty, as the pipeline's raycast does (skipping bricks

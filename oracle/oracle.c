@@ -7,6 +7,7 @@
  */
 #include "oracle.h"
 
+#include <limits.h>
 #include <math.h>
 #include <omp.h>
 #include <stdlib.h>
@@ -694,6 +695,41 @@ int64_t or_extract_slice(const void *vol, int fmt, const tde_color *color, const
     }
     free(bits);
     return count;
+}
+
+/* Extract_Tsdf_Volume (common/src/opencl_wrappers.cpp:440-543; its kernels
+ * scan_the_whole_array / extract_tsdf_cloud are not in the reference): the
+ * slab scan above with every voxel in the zone and no colour plane, chunks of
+ * `step`, and each point moved to the metric centre (i + 0.5f) * cell of the
+ * voxel it names (the V of extract_slice_as_cloud.cl:99-112), each operation
+ * rounded to float. */
+int64_t or_extract_tsdf_volume(const void *vol, int fmt, const tde_round_buffer *rb, int step, const float *cell,
+                               tde_xyzi *pts, float *wts, int64_t capacity) {
+    const int lo[3] = {INT_MIN, INT_MIN, INT_MIN}, hi[3] = {INT_MAX, INT_MAX, INT_MAX};
+    int64_t n = or_extract_slice(vol, fmt, NULL, lo, hi, rb, step, pts, NULL, wts, capacity);
+    int64_t k = n < capacity ? n : capacity;
+    for (int64_t i = 0; i < k; ++i) {
+        float x = pts[i].x + 0.5f, y = pts[i].y + 0.5f, z = pts[i].z + 0.5f;
+        pts[i].x = x * cell[0];
+        pts[i].y = y * cell[1];
+        pts[i].z = z * cell[2];
+    }
+    return n;
+}
+
+/* Extract_Color_Volume (common/src/opencl_wrappers.cpp:545-581; kernel
+ * extract_colors not in the reference): the colour of voxel floor(p / cell)
+ * per axis, zero outside the volume. */
+void or_extract_color_volume(const tde_color *color, const tde_round_buffer *rb, const tde_xyzi *pts, int64_t n,
+                             const float *cell, tde_color *out) {
+    for (int64_t i = 0; i < n; ++i) {
+        float fx = floorf(pts[i].x / cell[0]), fy = floorf(pts[i].y / cell[1]), fz = floorf(pts[i].z / cell[2]);
+        tde_color c = {0, 0, 0, 0};
+        if (fx >= 0.f && fy >= 0.f && fz >= 0.f && fx < (float)rb->voxels_size.x && fy < (float)rb->voxels_size.y &&
+            fz < (float)rb->voxels_size.z)
+            c = color[or_voxel_address((int)fx, (int)fy, (int)fz, rb)];
+        out[i] = c;
+    }
 }
 
 int or_clean_tsdf_slice(void *vol, int fmt, const int *mn, const int *mx, const tde_round_buffer *rb) {

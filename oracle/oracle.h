@@ -52,6 +52,10 @@ int or_transform_estimation(const float *gbuf, float *out, int len, int stride);
 int64_t or_extract_slice(const void *vol, int fmt, const tde_color *color, const int *mn, const int *mx,
                          const tde_round_buffer *rb, int chunk_depth, tde_xyzi *pts, tde_color *cols, float *wts,
                          int64_t capacity);
+int64_t or_extract_tsdf_volume(const void *vol, int fmt, const tde_round_buffer *rb, int step, const float *cell,
+                               tde_xyzi *pts, float *wts, int64_t capacity);
+void or_extract_color_volume(const tde_color *color, const tde_round_buffer *rb, const tde_xyzi *pts, int64_t n,
+                             const float *cell, tde_color *out);
 int or_clean_tsdf_slice(void *vol, int fmt, const int *mn, const int *mx, const tde_round_buffer *rb);
 int or_clean_color_slice(tde_color *col, const int *mn, const int *mx, const tde_round_buffer *rb);
 int or_integrate_colors(tde_color *col, const uint8_t *rgb, const float *vmap, float trunc, const float *Ri,

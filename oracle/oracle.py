@@ -73,6 +73,8 @@ _sigs = {
     "or_transform_maps": (I, [P, P, P, P, P, P, I, I]),
     "or_transform_estimation": (I, [P, P, I, I]),
     "or_extract_slice": (C.c_int64, [P, I, P, P, P, pRB, I, P, P, P, C.c_int64]),
+    "or_extract_tsdf_volume": (C.c_int64, [P, I, pRB, I, P, P, P, C.c_int64]),
+    "or_extract_color_volume": (None, [P, pRB, P, C.c_int64, P, P]),
     "or_clean_tsdf_slice": (I, [P, I, P, P, pRB]),
     "or_clean_color_slice": (I, [P, P, P, pRB]),
     "or_integrate_colors": (I, [P, P, P, F, P, P, pI, P, pRB, I, P]),
@@ -201,12 +203,13 @@ def transform_estimation(gbuf, length, stride=1200):
     return out
 
 
-def chunk_depth(depth: int) -> int:
-    """determine_extract_step(depth, divisor 4) of common/src/mem_utils.cpp:43-85;
-    64-voxel chunks for other depths divisible by 64, else one chunk."""
-    table = {512: 64, 256: 32, 128: 16}
+def chunk_depth(depth: int, divisor: int = 4) -> int:
+    """determine_extract_step(depth, divisor) of common/src/mem_utils.cpp:43-85
+    (step = {512: 256, 256: 128, 128: 64}[depth] / divisor); 64-voxel chunks
+    for other depths divisible by 64, else one chunk."""
+    table = {512: 256, 256: 128, 128: 64}
     if depth in table:
-        return table[depth]
+        return table[depth] // divisor
     return 64 if depth % 64 == 0 else depth
 
 
@@ -222,6 +225,34 @@ def extract_slice(vol, fmt, color, mn, mx, rb, capacity=None, weights=False):
     lib.or_extract_slice(_p(vol), fmt, cp, _p(mn_a), _p(mx_a), C.byref(rb), step, _p(pts), _p(cols), _p(wts), cap)
     k = min(n, cap)
     return pts[:k], cols[:k], (wts[:k] if weights else None), n
+
+
+def extract_tsdf_volume(vol, fmt, rb, cell, capacity=None, weights=False):
+    """Extract_Tsdf_Volume (common/src/opencl_wrappers.cpp:440-543): the slab
+    scan with every voxel in the zone, no colour plane, z chunks of
+    determine_extract_step(depth, divisor 2), and points at the metric centre
+    (i + 0.5) * cell of the voxel they name.  Its kernels are not in the
+    reference's sources; this follows the shipped slab kernels
+    (scan_slice_of_both_volumes.cl:76-208, extract_slice_as_cloud.cl:72-201)."""
+    step = chunk_depth(rb.voxels_size[2], 2)
+    c = np.asarray(cell, F32)
+    n = lib.or_extract_tsdf_volume(_p(vol), fmt, C.byref(rb), step, _p(c), None, None, 0)
+    cap = n if capacity is None else capacity
+    pts = np.zeros((max(cap, 1), 4), F32)
+    wts = np.zeros(max(cap, 1), F32) if weights else None
+    lib.or_extract_tsdf_volume(_p(vol), fmt, C.byref(rb), step, _p(c), _p(pts), _p(wts), cap)
+    k = min(n, cap)
+    return pts[:k], (wts[:k] if weights else None), n
+
+
+def extract_color_volume(color, rb, points, cell):
+    """Extract_Color_Volume (common/src/opencl_wrappers.cpp:545-581): colour of
+    voxel floor(p / cell) for each point; zero outside the volume."""
+    pts = np.ascontiguousarray(points, F32)
+    out = np.zeros((len(pts), 4), np.uint8)
+    lib.or_extract_color_volume(_p(np.ascontiguousarray(color)), C.byref(rb), _p(pts), len(pts),
+                                _p(np.asarray(cell, F32)), _p(out))
+    return out
 
 
 def clean_tsdf_slice(vol, fmt, mn, mx, rb):

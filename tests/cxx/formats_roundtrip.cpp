@@ -1,0 +1,51 @@
+// Text formats of include/3deye/ (header-only: no library, no GPU).
+// argv[1] = a directory holding input.bin:
+//   int32 n_poses, n_points; float R[n_poses][9], t[n_poses][3];
+//   float points[n_points][4]; uint8 colors[n_points][4]
+// Writes trajectory.txt, cloud.txt, colors.txt there with the C++ writers,
+// reads both clouds back with Fill_From_File and writes readback.bin
+// (int32 status pair, then the points and colours read).
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "matrix.h"
+#include "string_utils.h"
+
+int main(int argc, char **argv) {
+    if (argc < 2) return 2;
+    const std::string dir = argv[1];
+    FILE *f = std::fopen((dir + "/input.bin").c_str(), "rb");
+    if (!f) return 3;
+    int32_t np = 0, nq = 0;
+    if (std::fread(&np, 4, 1, f) != 1 || std::fread(&nq, 4, 1, f) != 1) return 4;
+    std::vector<matrix_3f> R(np);
+    std::vector<vector_3f> t(np);
+    for (int i = 0; i < np; ++i)
+        if (std::fread(&R[i], sizeof(float), 9, f) != 9) return 5;
+    for (int i = 0; i < np; ++i)
+        if (std::fread(&t[i], sizeof(float), 3, f) != 3) return 5;
+    matrix<Point_XYZI> cloud(nq);
+    matrix<Point_Color> colors(nq);
+    if (nq && std::fread(cloud.data, sizeof(Point_XYZI), nq, f) != (size_t)nq) return 6;
+    if (nq && std::fread(colors.data, sizeof(Point_Color), nq, f) != (size_t)nq) return 6;
+    std::fclose(f);
+
+    write_isometry_to_file((dir + "/trajectory.txt").c_str(), R.data(), t.data(), R.size());
+    cloud.Save_To_File(dir + "/cloud.txt");
+    colors.Save_To_File(dir + "/colors.txt");
+
+    matrix<Point_XYZI> cloud_in;
+    matrix<Point_Color> colors_in;
+    int32_t st[2] = {cloud_in.Fill_From_File(dir + "/cloud.txt"), colors_in.Fill_From_File(dir + "/colors.txt")};
+    FILE *o = std::fopen((dir + "/readback.bin").c_str(), "wb");
+    if (!o) return 7;
+    std::fwrite(st, 4, 2, o);
+    int32_t n_in[2] = {(int32_t)cloud_in.Get_Num_Of_Elem(), (int32_t)colors_in.Get_Num_Of_Elem()};
+    std::fwrite(n_in, 4, 2, o);
+    if (n_in[0]) std::fwrite(cloud_in.data, sizeof(Point_XYZI), n_in[0], o);
+    if (n_in[1]) std::fwrite(colors_in.data, sizeof(Point_Color), n_in[1], o);
+    std::fclose(o);
+    return 0;
+}

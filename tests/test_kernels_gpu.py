@@ -342,6 +342,67 @@ def test_extract_and_clean_formats_match_oracle(tde, orc, cuda, small, fmt):
     assert np.array_equal(N(vol), vol_o)
 
 
+# ---------------------------------------------------------------------------
+# whole-volume export (Extract_Tsdf_Volume) and colour lookup (Extract_Color_Volume)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("fmt,vox,origin", [(0, 64, (0, 0, 0)), (1, 128, (5, 70, 17)), (2, 128, (0, 0, 100))])
+def test_extract_tsdf_volume_matches_oracle(tde, orc, cuda, small, fmt, vox, origin):
+    import dataclasses
+    cfg, scene, traj, intr, depths = small
+    cfg = dataclasses.replace(cfg, voxels=vox)
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, fmt, origin=origin)
+    po, wo, no = orc.extract_tsdf_volume(vol_o, fmt, rb_o, cell, weights=True)
+    assert no > 1000
+    vol, rb = T(vol_o, cuda), trb(tde, rb_o)
+    pts, w, n = tde.extract_tsdf_volume(vol, fmt, rb, tuple(cell), weights=True)
+    assert n == no
+    assert bits_equal(N(pts), po) and np.array_equal(N(w), wo)
+    # a short buffer keeps the prefix and still reports the total
+    pts2, _, n2 = tde.extract_tsdf_volume(vol, fmt, rb, tuple(cell), capacity=100)
+    assert n2 == no and bits_equal(N(pts2), po[:100])
+    # every point is a voxel centre of the volume, inside it
+    idx = N(pts)[:, :3] / cell - 0.5
+    assert np.abs(idx - np.round(idx)).max() < 1e-3 and idx.min() > -0.01 and idx.max() < vox - 0.99
+    # the slab extraction over a zone covering the whole volume uses finer z
+    # chunks (divisor 4): it loses +z crossings at the extra chunk ends only,
+    # so its points are a subset of these
+    sp, _, _, sn = orc.extract_slice(vol_o, fmt, None, (-10**6,) * 3, (10**6,) * 3, rb_o)
+    key = lambda a: a[:, 0] + vox * (a[:, 1] + vox * a[:, 2])
+    vox_pts = np.round(N(pts)[:, :3] / cell - 0.5).astype(np.int64)
+    assert set(key(sp[:, :3].astype(np.int64))) <= set(key(vox_pts))
+    extra_ends = vox // orc.chunk_depth(vox, 4) - vox // orc.chunk_depth(vox, 2)
+    assert 0 <= n - sn <= extra_ends * vox * vox
+
+
+def test_extract_tsdf_volume_empty_and_rejects(tde, cuda):
+    import torch
+    rb = tde.round_buffer((64, 64, 64), (2.0, 2.0, 2.0))
+    vol = torch.zeros(tde.tsdf_volume_bytes(0, rb), dtype=torch.uint8, device=cuda)
+    pts, _, n = tde.extract_tsdf_volume(vol, 0, rb, (0.03125,) * 3)
+    assert n == 0 and len(pts) == 0
+    with pytest.raises(tde.TdeError):
+        tde.extract_tsdf_volume(vol, 0, rb, (0.0, 1.0, 1.0))
+
+
+def test_extract_color_volume_matches_oracle(tde, orc, cuda, small):
+    cfg, scene, traj, intr, depths = small
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, 0, origin=(9, 0, 33))
+    po, _, no = orc.extract_tsdf_volume(vol_o, 0, rb_o, cell)
+    rng = np.random.default_rng(21)
+    nvox = cfg.voxels ** 3
+    color = rng.integers(0, 256, size=(nvox, 4), dtype=np.uint8)
+    color[rng.random(nvox) < 0.3] = 0
+    # the exported points, then points outside the volume, on its faces and NaN
+    extra = np.array([[-0.01, 0.5, 0.5, 1], [0.5, 0.5, cfg.volume_m, 1], [0, 0, 0, 1],
+                      [cfg.volume_m - 1e-4, cfg.volume_m - 1e-4, cfg.volume_m - 1e-4, 1],
+                      [np.nan, 0.5, 0.5, 1], [0.5, np.inf, 0.5, 1]], np.float32)
+    pts = np.concatenate([po, extra, rng.uniform(-0.2, cfg.volume_m + 0.2, size=(5000, 4)).astype(np.float32)])
+    ref = orc.extract_color_volume(color, rb_o, pts, cell)
+    out = tde.extract_color_volume(T(color, cuda), trb(tde, rb_o), T(pts, cuda), tuple(cell))
+    assert np.array_equal(N(out), ref)
+    assert not ref[no:no + 2].any() and not ref[no + 4:no + 6].any() and ref[:no].any()
+
+
 def test_clean_color_slice_golden(tde, cuda):
     import torch
     g, rb = slice_golden(tde)

@@ -267,3 +267,41 @@ def test_color_pipeline_matches_c_abi_replay(cuda, tde, seq):
     assert np.array_equal(got, ref.cpu().numpy())
     assert (got[:, 3] > 0).sum() > 1000 and got[:, 3].max() == 4
     p.close()
+
+
+def test_pipeline_extract_volume_matches_oracle(cuda, tde, orc, seq, tmp_path):
+    """Whole-model export after tracking: the pipeline's points, weights and
+    colours equal the oracle's Extract_Tsdf_Volume / Extract_Color_Volume on
+    the downloaded volumes, and survive the on-disk cloud format."""
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    fmt = importlib.import_module("3deye_gb300.formats")
+    cfg, traj, depths = seq
+    p = pl.Pipeline(cfg, traj[0])
+    p.enable_color(max_weight=8)
+    rng = np.random.default_rng(4)
+    for d in depths:
+        pose, st = p.process_rgbd(d, rng.integers(0, 256, (cfg.rows, cfg.cols, 3), dtype=np.uint8))
+        assert st == 0
+    pts, w, col, n = p.extract_volume()
+    assert n > 1000 and len(pts) == n
+    vptr, rb = p.volume()
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    vol = np.zeros(tde.lib.tde_tsdf_volume_bytes(cfg.tsdf_format, C.byref(rb)), np.uint8)
+    tde.check(tde.lib.tde_memcpy(vol.ctypes.data_as(C.c_void_p), C.c_void_p(vptr), vol.nbytes, 1))
+    colv = np.zeros((cfg.voxels ** 3, 4), np.uint8)
+    tde.check(tde.lib.tde_memcpy(colv.ctypes.data_as(C.c_void_p), C.c_void_p(p.color_volume()), colv.nbytes, 1))
+    orb = orc.RB.from_buffer_copy(bytes(rb))
+    cell = np.full(3, np.float32(np.float32(cfg.volume_m) / np.float32(cfg.voxels)), np.float32)
+    po, wo, no = orc.extract_tsdf_volume(vol, cfg.tsdf_format, orb, cell, weights=True)
+    assert n == no and np.array_equal(pts.view(np.uint32), po.view(np.uint32)) and np.array_equal(w, wo)
+    assert np.array_equal(col, orc.extract_color_volume(colv, orb, pts, cell))
+    assert (col[:, 3] > 0).mean() > 0.5  # the surface was coloured
+    # a short buffer: the prefix, and the total
+    p2, _, _, n2 = p.extract_volume(capacity=10)
+    assert n2 == n and np.array_equal(p2, pts[:10])
+    # the cloud file round trip (6 significant digits)
+    path = tmp_path / "model.txt"
+    fmt.write_cloud(path, points=p.world_cloud(pts))
+    back = fmt.read_cloud(path)
+    np.testing.assert_allclose(back, p.world_cloud(pts), rtol=1e-5, atol=1e-6)
+    p.close()
