@@ -301,9 +301,14 @@ def run_ours(args, ws, rank, local):
     # resident in HBM beside the depth frames
     cp = pl.Pipeline(cfg, traj[0], use_graphs=True)
     cp.enable_color(max_weight=128)
-    yy, xx = torch.meshgrid(torch.arange(cfg.rows, device=dev), torch.arange(cfg.cols, device=dev), indexing="ij")
-    kk = torch.arange(n, device=dev).view(n, 1, 1)
-    rgb_frames = torch.stack([(xx + 3 * kk) % 256, (yy + 5 * kk) % 256, (xx + yy) % 256], dim=-1).to(torch.uint8)
+    i32 = torch.int32
+    yy, xx = torch.meshgrid(torch.arange(cfg.rows, device=dev, dtype=i32), torch.arange(cfg.cols, device=dev, dtype=i32),
+                            indexing="ij")
+    kk = torch.arange(n, device=dev, dtype=i32).view(n, 1, 1)
+    rgb_frames = torch.empty((n, cfg.rows, cfg.cols, 3), dtype=torch.uint8, device=dev)
+    rgb_frames[..., 0] = (xx + 3 * kk) % 256
+    rgb_frames[..., 1] = (yy + 5 * kk) % 256
+    rgb_frames[..., 2] = ((xx + yy) % 256).expand(n, -1, -1)
     cbase, cfb = rgb_frames.data_ptr(), cfg.rows * cfg.cols * 3
     for i in range(W):
         cp.enqueue_rgbd(base + i * fbytes, cbase + i * cfb, True)
