@@ -13,8 +13,8 @@ from __future__ import annotations
 
 import ctypes as C
 
-from ._capi import (TSDF_F16, TSDF_F32, TSDF_I16, Color, Intrinsics, Matrix3f, Point3f, Point3i, RoundBuffer,
-                    TdeError, check, last_error, lib, mat3, round_buffer, vec3)
+from ._capi import (TSDF_F16, TSDF_F32, TSDF_I16, Color, Intrinsics, LightSource, Matrix3f, Point3f, Point3i,
+                    RoundBuffer, TdeError, check, last_error, lib, mat3, round_buffer, vec3)
 
 __all__ = [
     "TSDF_I16", "TSDF_F16", "TSDF_F32", "Intrinsics", "RoundBuffer", "Point3f", "Point3i", "Matrix3f", "Color",
@@ -22,7 +22,7 @@ __all__ = [
     "tsdf_volume_bytes", "tsdf_init", "bilateral_filter", "depth_pyramid_level", "vertex_map", "normal_map",
     "estimate_combined", "transform_estimation", "clean_buff", "scale_depth", "integrate_tsdf", "raycast",
     "resize_vertex_map", "resize_normal_map", "transform_maps", "extract_slice", "extract_tsdf_volume",
-    "extract_color_volume", "clean_tsdf_slice", "clean_color_slice",
+    "extract_color_volume", "clean_tsdf_slice", "clean_color_slice", "generate_image", "LightSource",
 ]
 
 
@@ -209,6 +209,18 @@ def extract_slice(volume, fmt, color, min_bounds, max_bounds, rb: RoundBuffer, c
             return pts[:k], cols[:k], (wts[:k] if wts is not None else None), n
         cap = n
     raise TdeError(-5, "extract_slice: capacity retry failed")
+
+
+def generate_image(vmap, nmap, light_pos=(0.0, 0.0, 0.0), light_number=1, image=None, stream=None):
+    """Generate_Image (opencl_wrappers.cpp:967-992): grey shading of [rows,
+    cols, 3] vertex and normal maps into a uint8 [rows, cols, 3] image."""
+    torch = _torch()
+    rows, cols = vmap.shape[0], vmap.shape[1]
+    if image is None:
+        image = torch.empty((rows, cols, 3), dtype=torch.uint8, device=vmap.device)
+    light = LightSource(Point3f(*light_pos), int(light_number))
+    check(lib.tde_generate_image(ptr(vmap), ptr(nmap), cols, rows, C.byref(light), ptr(image), stream_ptr(stream)))
+    return image
 
 
 def extract_tsdf_volume(volume, fmt, rb: RoundBuffer, cell_size, capacity=None, weights=False, stream=None):

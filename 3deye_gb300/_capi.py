@@ -55,7 +55,13 @@ class Color(C.Structure):
     _fields_ = [("r", C.c_uint8), ("g", C.c_uint8), ("b", C.c_uint8), ("w", C.c_uint8)]
 
 
+class LightSource(C.Structure):
+    """light_source {point_3f pos; int number;} (types/light_source.h:4-8)."""
+    _fields_ = [("pos", Point3f), ("number", C.c_int)]
+
+
 assert C.sizeof(RoundBuffer) == 72 and C.sizeof(Intrinsics) == 24 and C.sizeof(Matrix3f) == 36
+assert C.sizeof(LightSource) == 16
 
 
 class TdeError(RuntimeError):
@@ -117,6 +123,7 @@ _SIGS = {
     "tde_extract_tsdf_volume_scratch_bytes": (SZ, [pRB]),
     "tde_extract_tsdf_volume": (I, [P, I, pRB, Point3f, P, SZ, P, P, U32, P, P]),
     "tde_extract_color_volume": (I, [P, pRB, P, U32, Point3f, P, P]),
+    "tde_generate_image": (I, [P, P, I, I, C.POINTER(LightSource), P, P]),
     "tde_clean_tsdf_slice": (I, [P, I, Point3i, Point3i, pRB, P]),
     "tde_clean_color_slice": (I, [P, Point3i, Point3i, pRB, P]),
 }

@@ -474,6 +474,16 @@ int tde_extract_color_volume(const tde_color *color_volume, const tde_round_buff
     return launch_gather_colors(color_volume, *rb, points, num_points, cell_size, colors, as_stream(stream));
 }
 
+int tde_generate_image(const float *vmap, const float *nmap, int cols, int rows, const tde_light_source *light,
+                       uint8_t *image, void *stream) {
+    TDE_REQUIRE(vmap && nmap && image && light, "generate_image: null buffer");
+    TDE_REQUIRE(cols > 0 && rows > 0, "generate_image: bad size %dx%d", cols, rows);
+    TDE_REQUIRE(light->number == 0 || light->number == 1, "generate_image: light.number %d (0 or 1)",
+                light->number);
+    return launch_generate_image(vmap, nmap, cols, rows, light->pos, light->number, nullptr, image,
+                                 as_stream(stream));
+}
+
 int tde_clean_tsdf_slice(void *volume, int format, tde_point3i min_bounds, tde_point3i max_bounds,
                          const tde_round_buffer *rb, void *stream) {
     TDE_REQUIRE(volume, "clean_tsdf_slice: null volume");

@@ -8,6 +8,7 @@
 //   pre stream:  wait set_free[set]; upload depth; preprocessing; record pre_done[set]
 //   main stream: wait pre_done[set]; ICP, pose, integration, raycast; record set_free[set]
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -597,6 +598,20 @@ int tde_pipeline_model_maps(tde_pipeline *p, int level, const float **vmap, cons
     if (vmap) *vmap = p->vmod[level];
     if (nmap) *nmap = p->nmod[level];
     return TDE_OK;
+}
+
+int tde_pipeline_render(tde_pipeline *p, const tde_light_source *light, uint8_t *image) {
+    if (!p || !image) return set_error(TDE_ERR_INVALID_ARG, "pipeline_render: null argument");
+    if (light && light->number != 0 && light->number != 1)
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_render: light.number %d (0 or 1)", light->number);
+    // no light given: one light at the camera centre, read on the device
+    // after the last enqueued frame published its pose
+    const float *at_camera =
+        light ? nullptr
+              : reinterpret_cast<const float *>(reinterpret_cast<const char *>(p->cam) + offsetof(CamPose, t));
+    return launch_generate_image(p->vmod[0], p->nmod[0], p->intr[0].cols, p->intr[0].rows,
+                                 light ? light->pos : tde_point3f{0.f, 0.f, 0.f}, light ? light->number : 1,
+                                 at_camera, image, p->stream);
 }
 
 int tde_pipeline_frame_maps(tde_pipeline *p, int level, const uint16_t **depth, const float **vmap,

@@ -27,5 +27,9 @@ int launch_transform_maps(const float *vs, const float *ns, float *vd, float *nd
 int launch_transform_estimation(const float *gbuf, float *out, int len, int stride, cudaStream_t stream);
 int launch_clean_buff(float *g, int width, cudaStream_t stream);
 int launch_tsdf_init(void *vol, int fmt, size_t n, cudaStream_t stream);
+// Generate_Image shading; light_dev (3 floats on the device) replaces
+// `light` when not null.
+int launch_generate_image(const float *vmap, const float *nmap, int W, int H, const tde_point3f &light, int nlights,
+                          const float *light_dev, uint8_t *image, cudaStream_t stream);
 
 }  // namespace tde

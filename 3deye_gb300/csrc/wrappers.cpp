@@ -419,6 +419,19 @@ void Extract_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round
     extract(Min_Bounds, Max_Bounds, Round_Buffer, gTsdf_Volume, gColor_Volume, Vertex_Slice, &Color_Slice);
 }
 
+// opencl_wrappers.cpp:967-992: Image_Out holds cols*rows RGB8 pixels.
+void Generate_Image(gpu_array_base *Vertex_Map, gpu_array_base *Normal_Map, intrinsics &Intr, light_source &light,
+                    gpu_array_base *Image_Out, opencl_kernel *) {
+    if (!Image_Out || Image_Out->bytes() < (size_t)Intr.cols * Intr.rows * 3)
+        throw std::runtime_error("Generate_Image: Image_Out smaller than cols*rows*3 bytes");
+    check(tde_generate_image(static_cast<const float *>(dev(Vertex_Map, "Generate_Image")),
+                             static_cast<const float *>(dev(Normal_Map, "Generate_Image")), Intr.cols, Intr.rows,
+                             reinterpret_cast<const tde_light_source *>(&light),
+                             static_cast<uint8_t *>(dev(Image_Out, "Generate_Image")), nullptr),
+          "Generate_Image");
+    sync("Generate_Image");
+}
+
 // opencl_wrappers.cpp:835-854
 void Clean_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
                       gpu_array_base *gTsdf_Volume, opencl_kernel *) {

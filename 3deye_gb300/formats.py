@@ -8,6 +8,9 @@
   components joined by "x" and then one space
   (common/inc/types/elementary_point_template.h:182-194).
 
+* Image -- binary PPM (P6) of an RGB8 image, the headless output of
+  Generate_Image (the reference draws it in a window).
+
 * Cloud -- matrix<T>::Save_To_File (common/inc/impl/matrix.hpp:413-476): a
   header line "width height depth typename", then one line per row of
   elements, each element followed by a space.  A cloud is one row
@@ -127,3 +130,23 @@ def read_cloud(path):
     if "." in toks[0] and "x" not in toks[0]:
         return np.array([[int(v) for v in t.split(".")] for t in toks], np.uint8).reshape(-1, 4)
     return np.array([[float(v) for v in t.split("x")] for t in toks], np.float32).reshape(-1, 4)
+
+
+def write_ppm(path, image) -> None:
+    """RGB8 image uint8 [rows, cols, 3] as binary PPM (P6, maxval 255)."""
+    a = np.ascontiguousarray(image, np.uint8)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError(f"image must be [rows, cols, 3], got {a.shape}")
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (a.shape[1], a.shape[0]))
+        f.write(a.tobytes())
+
+
+def read_ppm(path) -> np.ndarray:
+    """Inverse of write_ppm."""
+    raw = open(path, "rb").read()
+    parts = raw.split(b"\n", 3)
+    if parts[0] != b"P6" or parts[2] != b"255":
+        raise ValueError("read_ppm: not a binary 8-bit PPM")
+    cols, rows = (int(v) for v in parts[1].split())
+    return np.frombuffer(parts[3], np.uint8, rows * cols * 3).reshape(rows, cols, 3)

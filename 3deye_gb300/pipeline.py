@@ -5,7 +5,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import Intrinsics, Point3f, Point3i, RoundBuffer, check, declare, lib
+from ._capi import Intrinsics, LightSource, Point3f, Point3i, RoundBuffer, check, declare, lib
 
 P, I, F = C.c_void_p, C.c_int, C.c_float
 
@@ -42,6 +42,7 @@ declare("tde_pipeline_shift_needed", I, [P, F, F, P])
 declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_shift_ex", I, [P, P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_extract_volume", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
+declare("tde_pipeline_render", I, [P, P, P])
 declare("tde_pipeline_enqueue_rgbd", I, [P, P, P, I, P, P])
 declare("tde_pipeline_enable_color", I, [P, I])
 declare("tde_pipeline_color_volume", I, [P, C.POINTER(P)])
@@ -239,6 +240,12 @@ class Pipeline:
                                               col.ctypes.data_as(P), capacity, C.byref(n)))
         k = min(n.value, capacity)
         return pts[:k], w[:k], col[:k], n.value
+
+    def render(self, image_ptr: int, light_pos=None):
+        """Enqueue Generate_Image of the current model into a device buffer
+        of cols*rows*3 bytes; light at the camera centre unless light_pos."""
+        light = None if light_pos is None else C.byref(LightSource(Point3f(*light_pos), 1))
+        check(lib.tde_pipeline_render(self._h, light, image_ptr))
 
     def world_cloud(self, points):
         """Volume-frame points (as extract_volume returns them) in the world

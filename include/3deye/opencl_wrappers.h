@@ -94,6 +94,9 @@ void Clean_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Ro
 void Clean_Color_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
                        gpu_array_base *gColor_Volume, opencl_kernel *clean_color_kernel);
 
+void Generate_Image(gpu_array_base *Vertex_Map, gpu_array_base *Normal_Map, intrinsics &Intr, light_source &light,
+                    gpu_array_base *Image_Out, opencl_kernel *generate_image_kernel);
+
 void Clean_Buff(gpu_array_base *gPtr, opencl_kernel *clean_buff_kernel);
 
 #endif

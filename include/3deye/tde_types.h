@@ -101,6 +101,12 @@ typedef Point<XYZ> Point_XYZ;
 typedef Point<NXYZ> Point_NXYZ;
 typedef Point<XYZI> Point_XYZI;
 
+/* ---- light_source: common/inc/types/light_source.h:4-8 ----------------- */
+typedef struct light_source {
+    point_3f pos;
+    int number;
+} light_source;
+
 /* ---- constants: common/inc/common_defines.h / constants.h -------------- */
 #ifndef DEFAULT_STRIDE
 #define DEFAULT_STRIDE 256
@@ -123,5 +129,6 @@ static_assert(sizeof(Point_Tsdf) == 4 && sizeof(Point_Color) == 4 && sizeof(Poin
                   sizeof(Point_XYZI) == 16 && sizeof(Point_Depth) == 2,
               "point record layouts");
 static_assert(sizeof(round_buffer) == sizeof(tde_round_buffer), "round_buffer is the C-ABI record");
+static_assert(sizeof(light_source) == sizeof(tde_light_source), "light_source is the C-ABI record");
 
 #endif

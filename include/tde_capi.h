@@ -362,6 +362,23 @@ int tde_clean_color_slice(tde_color *color_volume, tde_point3i min_bounds, tde_p
                           const tde_round_buffer *rb, void *stream);
 
 /* ======================================================================== */
+/* Shaded model image                                                        */
+/* ======================================================================== */
+/* light_source: common/inc/types/light_source.h:4-8 */
+typedef struct tde_light_source { tde_point3f pos; int number; } tde_light_source;
+
+/* Generate_Image: opencl_wrappers.cpp:967-992 (kernel generate_image, absent;
+ * restated from the published KinectFusion image generator).  For a pixel
+ * whose vertex and normal are valid: w = |dot(normalize(light.pos - v), n)|
+ * (w = 1 when light.number is 0; 0 when the light sits on v), grey level
+ * clamp(trunc(205 w) + 50, 0, 255) in all three channels; invalid pixels
+ * are 0.  `image` is cols*rows*3 bytes (RGB8, row-major) on the device.
+ * light.number must be 0 or 1 (light_source holds one position).  Every
+ * float operation is correctly rounded: the image is exact. */
+int tde_generate_image(const float *vmap, const float *nmap, int cols, int rows, const tde_light_source *light,
+                       uint8_t *image, void *stream);
+
+/* ======================================================================== */
 /* Device memory helpers for hosts that do not include the CUDA headers      */
 /* (the C++ layer of include/3deye/ replaces gpu_array_base's cl_mem          */
 /* allocation, common/src/opencl_helper.cpp:344-420, with these).            */

@@ -149,6 +149,13 @@ int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, 
 int tde_pipeline_extract_volume(tde_pipeline *p, tde_xyzi *points, float *weights, tde_color *colors,
                                 uint32_t capacity, uint32_t *count);
 
+/* Generate_Image of the current model (the level-0 model maps the last
+ * enqueued frame raycast) into `image` (device, cols*rows*3 bytes RGB8),
+ * enqueued on the pipeline stream (tde_pipeline_sync waits for it).  `light`
+ * NULL: one light at the camera centre of that frame.  Shading as
+ * tde_generate_image. */
+int tde_pipeline_render(tde_pipeline *p, const tde_light_source *light, uint8_t *image);
+
 /* Measurement: casts the current model again from the last frame's pose
  * (into scratch maps) and counts the distinct voxel records the raycast
  * reads -- with skip_empty, as the pipeline's raycast does (skipping bricks

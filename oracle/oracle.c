@@ -799,3 +799,35 @@ int or_clean_color_slice(tde_color *col, const int *mn, const int *mx, const tde
                 }
     return 0;
 }
+
+/* Generate_Image (common/src/opencl_wrappers.cpp:967-992; kernel
+ * generate_image not in the reference): the published KinectFusion image
+ * generator -- w = |dot(normalize(light - v), n)| (1 without a light, 0 with
+ * the light on v), grey = clamp(trunc(205 w) + 50, 0, 255), black where the
+ * vertex or normal is invalid.  Float operations in the kernel's order. */
+void or_generate_image(const float *vmap, const float *nmap, int64_t npix, const float *light, int nlights,
+                       uint8_t *image) {
+    for (int64_t i = 0; i < npix; ++i) {
+        const float *v = vmap + 3 * i, *n = nmap + 3 * i;
+        int br = 0;
+        if (!isnan(v[0]) && !isnan(n[0])) {
+            float w = 1.f;
+            if (nlights > 0) {
+                float dx = light[0] - v[0], dy = light[1] - v[1], dz = light[2] - v[2];
+                float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 > 0.f) {
+                    float inv = 1.f / sqrtf(d2);
+                    dx *= inv; dy *= inv; dz *= inv;
+                    w = fabsf(dx * n[0] + dy * n[1] + dz * n[2]);
+                } else {
+                    w = 0.f;
+                }
+            }
+            if (isnan(w)) w = 0.f;  /* a NaN in y or z of an otherwise valid pixel */
+            else if (w > 2.f) w = 2.f;  /* non-unit normals: 255 either way, no int overflow */
+            br = (int)(205.f * w) + 50;
+            br = br < 0 ? 0 : (br > 255 ? 255 : br);
+        }
+        image[3 * i] = image[3 * i + 1] = image[3 * i + 2] = (uint8_t)br;
+    }
+}

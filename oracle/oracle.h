@@ -56,6 +56,8 @@ int64_t or_extract_tsdf_volume(const void *vol, int fmt, const tde_round_buffer 
                                tde_xyzi *pts, float *wts, int64_t capacity);
 void or_extract_color_volume(const tde_color *color, const tde_round_buffer *rb, const tde_xyzi *pts, int64_t n,
                              const float *cell, tde_color *out);
+void or_generate_image(const float *vmap, const float *nmap, int64_t npix, const float *light, int nlights,
+                       uint8_t *image);
 int or_clean_tsdf_slice(void *vol, int fmt, const int *mn, const int *mx, const tde_round_buffer *rb);
 int or_clean_color_slice(tde_color *col, const int *mn, const int *mx, const tde_round_buffer *rb);
 int or_integrate_colors(tde_color *col, const uint8_t *rgb, const float *vmap, float trunc, const float *Ri,

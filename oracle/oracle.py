@@ -75,6 +75,7 @@ _sigs = {
     "or_extract_slice": (C.c_int64, [P, I, P, P, P, pRB, I, P, P, P, C.c_int64]),
     "or_extract_tsdf_volume": (C.c_int64, [P, I, pRB, I, P, P, P, C.c_int64]),
     "or_extract_color_volume": (None, [P, pRB, P, C.c_int64, P, P]),
+    "or_generate_image": (None, [P, P, C.c_int64, P, I, P]),
     "or_clean_tsdf_slice": (I, [P, I, P, P, pRB]),
     "or_clean_color_slice": (I, [P, P, P, pRB]),
     "or_integrate_colors": (I, [P, P, P, F, P, P, pI, P, pRB, I, P]),
@@ -252,6 +253,16 @@ def extract_color_volume(color, rb, points, cell):
     out = np.zeros((len(pts), 4), np.uint8)
     lib.or_extract_color_volume(_p(np.ascontiguousarray(color)), C.byref(rb), _p(pts), len(pts),
                                 _p(np.asarray(cell, F32)), _p(out))
+    return out
+
+
+def generate_image(vmap, nmap, light, nlights=1):
+    """Generate_Image (common/src/opencl_wrappers.cpp:967-992): grey shading,
+    uint8 [rows, cols, 3] for [rows, cols, 3] vertex and normal maps."""
+    v = np.ascontiguousarray(vmap, F32)
+    nm = np.ascontiguousarray(nmap, F32)
+    out = np.zeros(v.shape[:-1] + (3,), np.uint8)
+    lib.or_generate_image(_p(v), _p(nm), v.size // 3, _p(np.asarray(light, F32)), nlights, _p(out))
     return out
 
 

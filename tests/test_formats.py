@@ -97,3 +97,17 @@ def test_cxx_writers_match_python_and_round_trip(tmp_path, n_pts):
     if n_pts:
         np.testing.assert_array_equal(fmt.read_cloud(tmp_path / "colors.txt"), cols)
     np.testing.assert_allclose(fmt.read_trajectory(tmp_path / "trajectory.txt"), m, rtol=5e-6, atol=0)
+
+
+def test_ppm_known_answer_and_round_trip(tmp_path):
+    img = np.zeros((2, 3, 3), np.uint8)
+    img[0, 1] = (50, 50, 50)
+    img[1, 2] = (255, 255, 255)
+    p = tmp_path / "a.ppm"
+    fmt.write_ppm(p, img)
+    raw = p.read_bytes()
+    assert raw[:11] == b"P6\n3 2\n255\n" and len(raw) == 11 + 18
+    assert raw[11 + 3:11 + 6] == b"\x32\x32\x32"
+    np.testing.assert_array_equal(fmt.read_ppm(p), img)
+    with pytest.raises(ValueError):
+        fmt.write_ppm(p, np.zeros((2, 3), np.uint8))

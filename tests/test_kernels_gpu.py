@@ -403,6 +403,55 @@ def test_extract_color_volume_matches_oracle(tde, orc, cuda, small):
     assert not ref[no:no + 2].any() and not ref[no + 4:no + 6].any() and ref[:no].any()
 
 
+# ---------------------------------------------------------------------------
+# Generate_Image (grey shading of vertex/normal maps)
+# ---------------------------------------------------------------------------
+def shading_maps(rows=96, cols=128, seed=31):
+    rng = np.random.default_rng(seed)
+    v = rng.uniform(-1.0, 3.0, size=(rows, cols, 3)).astype(np.float32)
+    n = rng.normal(size=(rows, cols, 3)).astype(np.float32)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    v[rng.random((rows, cols)) < 0.1] = np.nan  # no surface
+    n[rng.random((rows, cols)) < 0.05] = np.nan
+    n[0, 0] = (3.0, 4.0, 0.0)        # non-unit normal: saturates
+    n[0, 1, 1] = np.nan              # NaN only in y: weight 0
+    v[0, 2] = (0.5, -0.25, 1.0)      # the light on the vertex: weight 0
+    n[0, 2] = (0.0, 0.0, 1.0)
+    v[0, 3] = (1e30, 1e30, 1e30)     # overflowing distance
+    n[0, 3] = (0.0, 0.0, 1.0)
+    return v, n
+
+
+@pytest.mark.parametrize("number", [1, 0])
+def test_generate_image_matches_oracle(tde, orc, cuda, number):
+    v, n = shading_maps()
+    light = (0.5, -0.25, 1.0)
+    ref = orc.generate_image(v, n, light, number)
+    img = tde.generate_image(T(v, cuda), T(n, cuda), light, number)
+    assert np.array_equal(N(img), ref)
+    valid = ~np.isnan(v[..., 0]) & ~np.isnan(n[..., 0])
+    assert not ref[~valid].any() and (ref[valid] >= 50).all()
+    if number:
+        assert ref[0, 0, 0] == 255 and ref[0, 1, 0] == 50 and ref[0, 2, 0] == 50 and ref[0, 3, 0] == 50
+        assert len(np.unique(ref[valid])) > 100
+    else:
+        assert (ref[valid] == 255).all()
+    with pytest.raises(tde.TdeError):
+        tde.generate_image(T(v, cuda), T(n, cuda), light, 2)
+
+
+def test_generate_image_of_raycast_model(tde, orc, cuda, small):
+    """Shading the oracle's raycast of an integrated volume, light at the camera."""
+    cfg, scene, traj, intr, depths = small
+    vol_o, rb_o, cell = oracle_volume(orc, cfg, intr, depths, traj, 0)
+    R, t = pose_parts(traj[2])
+    vo, no_ = orc.raycast(vol_o, 0, rb_o, intr, R, t, cfg.trunc_m, cell)
+    ref = orc.generate_image(vo, no_, t)
+    img = tde.generate_image(T(vo, cuda), T(no_, cuda), tuple(t))
+    assert np.array_equal(N(img), ref)
+    assert (ref[..., 0] > 0).mean() > 0.3
+
+
 def test_clean_color_slice_golden(tde, cuda):
     import torch
     g, rb = slice_golden(tde)

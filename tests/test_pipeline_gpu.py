@@ -305,3 +305,35 @@ def test_pipeline_extract_volume_matches_oracle(cuda, tde, orc, seq, tmp_path):
     back = fmt.read_cloud(path)
     np.testing.assert_allclose(back, p.world_cloud(pts), rtol=1e-5, atol=1e-6)
     p.close()
+
+
+def test_pipeline_render_matches_oracle(cuda, tde, orc, seq, tmp_path):
+    """Generate_Image of the tracked model: light at the camera by default or
+    given; equal to the oracle's shading of the downloaded model maps."""
+    import torch
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    fmt = importlib.import_module("3deye_gb300.formats")
+    cfg, traj, depths = seq
+    p = pl.Pipeline(cfg, traj[0])
+    for d in depths:
+        pose, st = p.process(d)
+        assert st == 0
+    img = torch.empty((cfg.rows, cfg.cols, 3), dtype=torch.uint8, device=cuda)
+    p.render(img.data_ptr())
+    p.sync()
+    vptr, nptr = p.model_maps(0)
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    vm = np.zeros((cfg.rows, cfg.cols, 3), np.float32)
+    nm = np.zeros_like(vm)
+    tde.check(tde.lib.tde_memcpy(vm.ctypes.data_as(C.c_void_p), C.c_void_p(vptr), vm.nbytes, 1))
+    tde.check(tde.lib.tde_memcpy(nm.ctypes.data_as(C.c_void_p), C.c_void_p(nptr), nm.nbytes, 1))
+    ref = orc.generate_image(vm, nm, pose[9:].astype(np.float32))
+    got = img.cpu().numpy()
+    assert np.array_equal(got, ref)
+    assert (got[..., 0] > 0).mean() > 0.3
+    p.render(img.data_ptr(), light_pos=(0.0, 0.0, 0.0))
+    p.sync()
+    assert np.array_equal(img.cpu().numpy(), orc.generate_image(vm, nm, (0.0, 0.0, 0.0)))
+    fmt.write_ppm(tmp_path / "model.ppm", got)
+    assert np.array_equal(fmt.read_ppm(tmp_path / "model.ppm"), got)
+    p.close()
