@@ -283,6 +283,25 @@ template <int FMT> __device__ __forceinline__ void load4(const void *vol, uint32
     decode4<FMT>(load_raw4<FMT>(vol, a, n), c);
 }
 
+// 4-bit mask of the group's voxels with w != 0 and f != 1, read from the
+// record bits: I16 f == 1 only for v == 32767 (v / 32767 is correctly
+// rounded), F16 only for the half 0x3c00; F32 compares the float.
+template <int FMT> __device__ __forceinline__ unsigned live_mask(const Raw4<FMT> &r, uint32_t one) {
+    const uint32_t u[4] = {r.v.x, r.v.y, r.v.z, r.v.w};
+    unsigned m = 0;
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) m |= (unsigned)((u[i] >> 16) != 0u && (u[i] & 0xffffu) != one) << i;
+    return m;
+}
+template <>
+__device__ __forceinline__ unsigned live_mask<TDE_TSDF_F32>(const Raw4<TDE_TSDF_F32> &r, uint32_t) {
+    return (unsigned)(r.w.x != 0 && r.f.x != 1.f) | ((unsigned)(r.w.y != 0 && r.f.y != 1.f) << 1) |
+           ((unsigned)(r.w.z != 0 && r.f.z != 1.f) << 2) | ((unsigned)(r.w.w != 0 && r.f.w != 1.f) << 3);
+}
+template <int FMT> struct OneBits { static constexpr uint32_t value = 0x7fffu; };  // I16: v = 32767
+template <> struct OneBits<TDE_TSDF_F16> { static constexpr uint32_t value = 0x3c00u; };  // half 1.0
+template <> struct OneBits<TDE_TSDF_F32> { static constexpr uint32_t value = 0u; };       // unused
+
 // Per-launch constants of the row kernels.
 struct RowGeom {
     uint32_t g_magic;  // ceil(2^32 / G): g / G = umulhi(g, g_magic) for g < 2^16
@@ -317,7 +336,7 @@ __device__ __forceinline__ unsigned plane_count(unsigned bits, int q) { return _
 // x' = 4k + i) and plane q.  ZONE = false: every voxel is in the zone.
 template <int FMT, bool ZONE, bool COLOR>
 __device__ __forceinline__ unsigned group_bits(const SlabParams &p, const RowGeom &rg, const GroupAt &at, int y, int z,
-                                               int z_end, const Raw4<FMT> &raw, const uint4 &colour) {
+                                               int z_end, const Raw4<FMT> &raw, const uint4 &colour, unsigned lmask) {
     const int W = p.rb.voxels_size.x, H = p.rb.voxels_size.y, D = p.rb.voxels_size.z;
     const int x0 = 4 * at.k;
     bool zone[4] = {true, true, true, true};
@@ -333,16 +352,16 @@ __device__ __forceinline__ unsigned group_bits(const SlabParams &p, const RowGeo
             zone[i] = yz || (ix >= p.mn.x && ix <= p.mx.x);
         }
     }
-    Rec4 c;
-    decode4<FMT>(raw, c);
     bool live[4], any = false;
     #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        live[i] = zone[i] && c.w[i] != 0 && c.f[i] != 1.f;
+        live[i] = zone[i] && ((lmask >> i) & 1u);
         any |= live[i];
     }
     unsigned bits = 0;
     if (any) {
+        Rec4 c;
+        decode4<FMT>(raw, c);
         Rec4 ny, nz;
         const bool has_y = y + 1 < H, has_z = z + 1 < z_end;
         const uint32_t row = at.a - (uint32_t)x0;
@@ -398,9 +417,16 @@ __device__ __forceinline__ void tile_bits(const SlabParams &p, const RowGeom &rg
         const int g = g0 + stride * j;
         bits[j] = 0;
         if (g < ngroups) {
-            const GroupAt at = group_at(p, rg, g, y0, z);
-            bits[j] = group_bits<FMT, ZONE, COLOR>(p, rg, at, y0 + at.r, z, z_end, raw[j],
-                                                   COLOR ? colour[COLOR ? j : 0] : make_uint4(0u, 0u, 0u, 0u));
+            // most groups hold nothing that can emit: no coordinates, no decode
+            const unsigned lmask = live_mask<FMT>(raw[j], OneBits<FMT>::value);
+            const bool colour_any = COLOR && (colour[COLOR ? j : 0].x | colour[COLOR ? j : 0].y |
+                                              colour[COLOR ? j : 0].z | colour[COLOR ? j : 0].w) != 0u;
+            if (lmask || colour_any) {
+                const GroupAt at = group_at(p, rg, g, y0, z);
+                bits[j] = group_bits<FMT, ZONE, COLOR>(p, rg, at, y0 + at.r, z, z_end, raw[j],
+                                                       COLOR ? colour[COLOR ? j : 0] : make_uint4(0u, 0u, 0u, 0u),
+                                                       lmask);
+            }
         }
     }
 }
