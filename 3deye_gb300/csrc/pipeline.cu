@@ -63,6 +63,7 @@ enum Segment {
     SEG_INTEGRATE,
     SEG_RAYCAST,
     SEG_RESIZE,
+    SEG_COLOR,       // colour volume update (side stream; reads this frame's snapshot of the model map and pose)
     SEG_COUNT
 };
 // Stages timed per frame, in order: SEG_PRE, SEG_ICP (SEG_POST_FIRST on the
@@ -81,8 +82,10 @@ struct tde_pipeline {
     tde_point3f cell;
     cudaStream_t stream = nullptr;      // tracking and fusion
     cudaStream_t pre_stream = nullptr;  // preprocessing of the next frame
+    cudaStream_t col_stream = nullptr;  // colour volume update, beside the next frame's tracking
     int prio_low = 0, prio_high = 0;
     cudaEvent_t pre_done[2] = {}, set_free[2] = {};
+    cudaEvent_t col_ready[2] = {}, col_done[2] = {};
     int levels = 3;
     tde_intrinsics intr[3];
     // device buffers; raw depth and the current-frame maps come in two sets
@@ -98,9 +101,13 @@ struct tde_pipeline {
     unsigned long long *stats = nullptr;
     uint8_t *negflags = nullptr;  // per physical brick: may hold a negative value
     uint8_t *satflags = nullptr;  // per logical brick: every voxel at f = 1, maximum weight
-    // colour volume (tde_pipeline_enable_color): RGB frames per input set
+    // colour volume (tde_pipeline_enable_color): RGB frames per input set, and
+    // per set the level-0 model vertex map and camera pose the update reads
+    // (the next frame's raycast and pose publication overwrite the live ones)
     tde_color *colvol = nullptr;
     uint8_t *rgb[2] = {};
+    float *vcol[2] = {};
+    CamPose *cam_col[2] = {};
     void *cscratch = nullptr;
     int color_max_weight = 0;
     void *volume = nullptr;
@@ -199,12 +206,21 @@ int record_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
     case SEG_RAYCAST: {
         TDE_TRY(cast_model(p, s));
         if (!p->colvol) return TDE_OK;
-        // colour at the model surface just cast from this frame's pose
+        // snapshot of the model map and pose for this frame's colour update
+        TDE_CUDA(cudaMemcpyAsync(p->vcol[set], p->vmod[0], (size_t)W * H * 3 * sizeof(float), cudaMemcpyDeviceToDevice,
+                                 s), "colour snapshot");
+        TDE_CUDA(cudaMemcpyAsync(p->cam_col[set], p->cam, sizeof(CamPose), cudaMemcpyDeviceToDevice, s),
+                 "colour snapshot");
+        return TDE_OK;
+    }
+    case SEG_COLOR: {
+        if (!p->colvol) return TDE_OK;
+        // colour at the model surface cast from this frame's pose
         IntegrateParams P;
         std::memset(&P, 0, sizeof(P));
         P.trunc = c.trunc; P.max_weight = p->color_max_weight; P.intr = p->intr[0]; P.rb = p->rb; P.cell = p->cell;
-        P.n = voxel_count(p->rb); P.dpose = p->cam;
-        return launch_integrate_colors(p->colvol, p->rgb[set], p->vmod[0], P, p->cscratch, nullptr, s);
+        P.n = voxel_count(p->rb); P.dpose = p->cam_col[set];
+        return launch_integrate_colors(p->colvol, p->rgb[set], p->vcol[set], P, p->cscratch, nullptr, s);
     }
     case SEG_RESIZE:
         if (p->levels < 2) return TDE_OK;
@@ -252,6 +268,7 @@ int capture_all(tde_pipeline *p) {
     for (int set = 0; set < 2; ++set) {
         for (int sgi = 0; sgi < SEG_COUNT; ++sgi) {
             Segment sg = (Segment)sgi;
+            if (sg == SEG_COLOR && !p->colvol) continue;  // nothing to capture
             TDE_TRY(capture(p, &sg, 1, set, &p->seg_exec[set][sgi]));
         }
         TDE_TRY(capture(p, kMainFirst, 4, set, &p->main_exec[set][0]));
@@ -289,6 +306,7 @@ int make_pre_stream(tde_pipeline *p) {
 int sync_streams(tde_pipeline *p) {
     if (p->pre_stream) TDE_CUDA(cudaStreamSynchronize(p->pre_stream), "pipeline sync");
     TDE_CUDA(cudaStreamSynchronize(p->stream), "pipeline sync");
+    if (p->col_stream) TDE_CUDA(cudaStreamSynchronize(p->col_stream), "pipeline sync");
     return TDE_OK;
 }
 
@@ -308,6 +326,7 @@ void release(tde_pipeline *p) {
     if (!p) return;
     if (p->pre_stream) cudaStreamSynchronize(p->pre_stream);
     if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->col_stream) cudaStreamSynchronize(p->col_stream);
     drop_graphs(p);
     for (auto e : p->ev) cudaEventDestroy(e);
     for (int set = 0; set < 2; ++set) {
@@ -319,6 +338,10 @@ void release(tde_pipeline *p) {
         }
         if (p->pre_done[set]) cudaEventDestroy(p->pre_done[set]);
         if (p->set_free[set]) cudaEventDestroy(p->set_free[set]);
+        if (p->col_ready[set]) cudaEventDestroy(p->col_ready[set]);
+        if (p->col_done[set]) cudaEventDestroy(p->col_done[set]);
+        cudaFree(p->vcol[set]);
+        cudaFree(p->cam_col[set]);
     }
     for (int l = 0; l < 3; ++l) { cudaFree(p->vmod[l]); cudaFree(p->nmod[l]); }
     cudaFree(p->st); cudaFree(p->cam); cudaFree(p->out);
@@ -326,6 +349,7 @@ void release(tde_pipeline *p) {
     cudaFree(p->slab_scratch); cudaFree(p->slab_points); cudaFree(p->slab_weights); cudaFree(p->slab_count);
     cudaFree(p->slab_colors); cudaFree(p->colvol); cudaFree(p->rgb[0]); cudaFree(p->rgb[1]); cudaFree(p->cscratch);
     if (p->pre_stream) cudaStreamDestroy(p->pre_stream);
+    if (p->col_stream) cudaStreamDestroy(p->col_stream);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -500,6 +524,8 @@ int tde_pipeline_enqueue_rgbd(tde_pipeline *p, const uint16_t *depth, const uint
         TDE_CUDA(cudaEventRecord(ev[0], p->stream), "event");
         for (int k = 0; k < kStages; ++k) {
             TDE_TRY(run_segment(p, order[k], set, p->stream));
+            // timed frames count the colour update with the raycast
+            if (order[k] == SEG_RAYCAST && p->colvol) TDE_TRY(run_segment(p, SEG_COLOR, set, p->stream));
             TDE_CUDA(cudaEventRecord(ev[k + 1], p->stream), "event");
         }
         p->timing_n++;
@@ -507,17 +533,29 @@ int tde_pipeline_enqueue_rgbd(tde_pipeline *p, const uint16_t *depth, const uint
         // preprocessing on the second stream, once the frame two back no
         // longer reads this input set
         TDE_CUDA(cudaStreamWaitEvent(p->pre_stream, p->set_free[set], 0), "wait");
+        // the colour update of the frame two back reads this set's RGB frame
+        if (rgb) TDE_CUDA(cudaStreamWaitEvent(p->pre_stream, p->col_done[set], 0), "wait");
         TDE_CUDA(cudaMemcpyAsync(p->raw[set], depth, bytes, kind, p->pre_stream), "depth upload");
         if (rgb) TDE_CUDA(cudaMemcpyAsync(p->rgb[set], rgb, rgb_bytes, kind, p->pre_stream), "rgb upload");
         TDE_TRY(run_segment(p, SEG_PRE, set, p->pre_stream));
         TDE_CUDA(cudaEventRecord(p->pre_done[set], p->pre_stream), "event");
         TDE_CUDA(cudaStreamWaitEvent(p->stream, p->pre_done[set], 0), "wait");
+        // ... and this set's model-map and pose snapshots, which the raycast rewrites
+        if (p->colvol) TDE_CUDA(cudaStreamWaitEvent(p->stream, p->col_done[set], 0), "wait");
         if (p->cfg.use_graphs) {
             TDE_CUDA(cudaGraphLaunch(p->main_exec[set][first ? 0 : 1], p->stream), "graph launch");
         } else {
             const Segment *segs = first ? kMainFirst : kMainTracked;
             const int n = 4;
             for (int k = 0; k < n; ++k) TDE_TRY(record_segment(p, segs[k], set, p->stream));
+        }
+        if (p->colvol) {
+            // the colour update runs beside the next frame's tracking; only the
+            // frame after next waits for it
+            TDE_CUDA(cudaEventRecord(p->col_ready[set], p->stream), "event");
+            TDE_CUDA(cudaStreamWaitEvent(p->col_stream, p->col_ready[set], 0), "wait");
+            TDE_TRY(run_segment(p, SEG_COLOR, set, p->col_stream));
+            TDE_CUDA(cudaEventRecord(p->col_done[set], p->col_stream), "event");
         }
     }
     TDE_CUDA(cudaEventRecord(p->set_free[set], p->stream), "event");
@@ -543,10 +581,17 @@ int tde_pipeline_enable_color(tde_pipeline *p, int max_weight) {
         const size_t n = voxel_count(p->rb), px = (size_t)p->cfg.intr.cols * p->cfg.intr.rows;
         int st;
         if ((st = dalloc(&p->colvol, n, "colour volume")) || (st = dalloc(&p->rgb[0], 3 * px, "rgb frame")) ||
-            (st = dalloc(&p->rgb[1], 3 * px, "rgb frame")) ||
+            (st = dalloc(&p->rgb[1], 3 * px, "rgb frame")) || (st = dalloc(&p->vcol[0], 3 * px, "colour snapshot")) ||
+            (st = dalloc(&p->vcol[1], 3 * px, "colour snapshot")) ||
+            (st = dalloc(&p->cam_col[0], 1, "colour snapshot")) || (st = dalloc(&p->cam_col[1], 1, "colour snapshot")) ||
             (st = dalloc(reinterpret_cast<char **>(&p->cscratch),
                          integrate_colors_scratch_bytes(p->cfg.intr.cols, p->cfg.intr.rows, p->rb), "colour scratch")))
             return st;
+        TDE_CUDA(cudaStreamCreateWithPriority(&p->col_stream, cudaStreamNonBlocking, p->prio_low), "colour stream");
+        for (int set = 0; set < 2; ++set) {
+            TDE_CUDA(cudaEventCreateWithFlags(&p->col_ready[set], cudaEventDisableTiming), "event");
+            TDE_CUDA(cudaEventCreateWithFlags(&p->col_done[set], cudaEventDisableTiming), "event");
+        }
         TDE_CUDA(cudaMemsetAsync(p->colvol, 0, n * sizeof(tde_color), p->stream), "colour volume");
     }
     p->color_max_weight = max_weight;

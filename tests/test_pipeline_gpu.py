@@ -269,6 +269,45 @@ def test_color_pipeline_matches_c_abi_replay(cuda, tde, seq):
     p.close()
 
 
+def test_color_update_overlapped_equals_serial(cuda, tde, seq):
+    """The colour update runs on its own stream beside the next frame's
+    tracking, reading per-set snapshots of the model map and pose: frames
+    enqueued back to back (device-resident inputs, one sync at the end) give
+    the same colour volume, TSDF and pose as frames synchronised one by one."""
+    import torch
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    rng = np.random.default_rng(8)
+    rgbs = [rng.integers(0, 256, (cfg.rows, cfg.cols, 3), dtype=np.uint8) for _ in depths]
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+
+    def volumes(p):
+        vptr, rb = p.volume()
+        vol = np.zeros(tde.lib.tde_tsdf_volume_bytes(cfg.tsdf_format, C.byref(rb)), np.uint8)
+        tde.check(tde.lib.tde_memcpy(vol.ctypes.data_as(C.c_void_p), C.c_void_p(vptr), vol.nbytes, 1))
+        col = np.zeros((cfg.voxels ** 3, 4), np.uint8)
+        tde.check(tde.lib.tde_memcpy(col.ctypes.data_as(C.c_void_p), C.c_void_p(p.color_volume()), col.nbytes, 1))
+        return vol, col, p.pose()
+
+    serial = pl.Pipeline(cfg, traj[0])
+    serial.enable_color(max_weight=16)
+    for d, c in zip(depths, rgbs):
+        assert serial.process_rgbd(d, c)[1] == 0
+    ref = volumes(serial)
+    serial.close()
+    over = pl.Pipeline(cfg, traj[0])
+    over.enable_color(max_weight=16)
+    dd = torch.from_numpy(np.stack(depths)).to(cuda)
+    cc = torch.from_numpy(np.stack(rgbs)).to(cuda)
+    for i in range(len(depths)):
+        over.enqueue_rgbd(dd[i].data_ptr(), cc[i].data_ptr(), True)
+    over.sync()
+    got = volumes(over)
+    over.close()
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    assert (ref[1][:, 3] > 0).sum() > 1000
+
+
 def test_pipeline_extract_volume_matches_oracle(cuda, tde, orc, seq, tmp_path):
     """Whole-model export after tracking: the pipeline's points, weights and
     colours equal the oracle's Extract_Tsdf_Volume / Extract_Color_Volume on
