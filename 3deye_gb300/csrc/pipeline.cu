@@ -243,6 +243,18 @@ int capture(tde_pipeline *p, const Segment *segs, int n, int set, cudaGraphExec_
         return st;
     }
     if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    if (*exec) {
+        // same topology, new parameters (a volume shift moves the round
+        // buffer's origins): update in place, far cheaper than instantiating
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(*exec, g, &info) == cudaSuccess) {
+            cudaGraphDestroy(g);
+            return TDE_OK;
+        }
+        (void)cudaGetLastError();  // a topology change: instantiate afresh
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+    }
     e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
@@ -263,8 +275,9 @@ void drop_graphs(tde_pipeline *p) {
 const Segment kMainFirst[] = {SEG_POST_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
 const Segment kMainTracked[] = {SEG_ICP, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
 
+// (Re)captures every graph; existing executables are updated in place.
 int capture_all(tde_pipeline *p) {
-    drop_graphs(p);
+    p->captured = false;
     for (int set = 0; set < 2; ++set) {
         for (int sgi = 0; sgi < SEG_COUNT; ++sgi) {
             Segment sg = (Segment)sgi;
