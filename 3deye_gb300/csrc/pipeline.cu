@@ -823,6 +823,12 @@ int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, in
         return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift_needed: bad argument");
     double pose[12];
     TDE_TRY(tde_pipeline_pose(p, pose));
+    return tde_pipeline_shift_needed_pose(p, pose, ahead_m, radius_m, delta3);
+}
+
+int tde_pipeline_shift_needed_pose(tde_pipeline *p, const double *pose, float ahead_m, float radius_m, int *delta3) {
+    if (!p || !pose || !delta3 || !(radius_m >= 0.f) || !(ahead_m >= 0.f))
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_shift_needed: bad argument");
     const float *vs = &p->rb.volume_size.x;
     const float *cs = &p->cell.x;
     bool out = false;

@@ -43,6 +43,7 @@ declare("tde_pipeline_shift", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)]
 declare("tde_pipeline_shift_ex", I, [P, P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_extract_volume", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_render", I, [P, P, P])
+declare("tde_pipeline_shift_needed_pose", I, [P, P, C.c_float, C.c_float, P])
 declare("tde_pipeline_enqueue_rgbd", I, [P, P, P, I, P, P])
 declare("tde_pipeline_enable_color", I, [P, I])
 declare("tde_pipeline_color_volume", I, [P, C.POINTER(P)])
@@ -204,6 +205,16 @@ class Pipeline:
             ahead_m = 0.5 * self.cfg.volume_m
         d = np.zeros(3, np.int32)
         check(lib.tde_pipeline_shift_needed(self._h, ahead_m, radius_m, d.ctypes.data_as(P)))
+        return d
+
+    def shift_needed_for(self, pose12, radius_m: float, ahead_m: float | None = None) -> np.ndarray:
+        """shift_needed for a given pose (current volume frame), without waiting for the GPU."""
+        if ahead_m is None:
+            ahead_m = 0.5 * self.cfg.volume_m
+        pose = np.ascontiguousarray(pose12, np.float64)
+        d = np.zeros(3, np.int32)
+        check(lib.tde_pipeline_shift_needed_pose(self._h, pose.ctypes.data_as(P), ahead_m, radius_m,
+                                                 d.ctypes.data_as(P)))
         return d
 
     def shift(self, delta, capacity: int = 1 << 22):

@@ -122,6 +122,11 @@ int tde_pipeline_set_round_buffer(tde_pipeline *p, const tde_round_buffer *rb);
  * radius_m away along some axis, delta3 receives the shift in voxels that
  * re-centres the volume on it, else zeros. */
 int tde_pipeline_shift_needed(tde_pipeline *p, float ahead_m, float radius_m, int *delta3);
+/* As tde_pipeline_shift_needed for a given pose (row-major R, then t, in the
+ * current volume frame) instead of the tracked one: no synchronisation, so a
+ * host can decide on a shift from an earlier frame's pose (downloaded by
+ * tde_pipeline_enqueue) while later frames run. */
+int tde_pipeline_shift_needed_pose(tde_pipeline *p, const double *pose12, float ahead_m, float radius_m, int *delta3);
 
 /* Shifts the volume by delta3 voxels (|delta| below the voxel count per
  * axis), host-synchronous: the slab that leaves the volume is extracted as

@@ -45,6 +45,7 @@ def test_corridor_shifts_extract_bit_exact(cuda, orc, tde, fmt):
         assert st == 0, i
         est.append(np.concatenate([pose[:9], pose[9:] + offset]))
         delta = p.shift_needed(0.4)
+        assert np.array_equal(p.shift_needed_for(pose, 0.4), delta)  # the same decision from a given pose
         if not delta.any():
             continue
         vptr, rb = p.volume()
@@ -121,6 +122,7 @@ def test_corridor_full_size_extract_bit_exact(cuda, orc, tde):
         assert st == 0, i
         est.append(np.concatenate([pose[:9], pose[9:] + offset]))
         delta = p.shift_needed(0.4)
+        assert np.array_equal(p.shift_needed_for(pose, 0.4), delta)  # the same decision from a given pose
         if not delta.any():
             continue
         vptr, rb = p.volume()
