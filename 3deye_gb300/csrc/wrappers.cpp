@@ -42,7 +42,8 @@ const char *const kKnown[] = {
     "estimate_combined", "transform_estimation", "clean_buff", "scale_depth", "integrate_tsdf_volume", "raycast",
     "resize_vertex_map", "resize_normal_map", "transform_map", "scan_slice_of_both_volumes", "extract_slice_as_cloud",
     "scan_slice_of_tsdf_volume", "extract_tsdf_slice_as_cloud", "scan_pow2", "scan_subarrays", "clean_tsdf_slice",
-    "clean_color_slice", "init_tsdf", "integrate_color_volume"};
+    "clean_color_slice", "init_tsdf", "integrate_color_volume", "scan_the_whole_array", "extract_tsdf_cloud",
+    "extract_colors", "generate_image"};
 
 string base_name(const string &n) {
     if (n.size() > 3 && n.compare(n.size() - 3, 3, ".cl") == 0) return n.substr(0, n.size() - 3);

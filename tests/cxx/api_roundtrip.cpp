@@ -2,6 +2,7 @@
 // and friends), built only with -I include/3deye and linked to
 // lib3deye_gb300.so.  Reads a depth frame and a pose from argv[1]/input.bin,
 // runs Integrate_Tsdf_Data -> Raycast -> Resize maps -> Extract_Slice ->
+// Extract_Tsdf_Volume -> Extract_Color_Volume -> Generate_Image ->
 // Clean_Tsdf_Slice -> Estimate_Combined, and writes every result to
 // argv[1]/output.bin for the Python test to compare with the CPU oracle.
 #include <cstdio>
@@ -99,6 +100,27 @@ int main(int argc, char **argv) {
     point_3i mx = make_point_3i(bounds[3], bounds[4], bounds[5]);
     matrix<Point_XYZI> cloud;
     Extract_Tsdf_Slice(mn, mx, &rb, cell, &vol, &gm, cloud);
+    // whole-model export, colour lookup and the shaded image, before cleaning
+    matrix<Point_XYZI> whole;
+    Extract_Tsdf_Volume(&rb, cell, &vol, &gm, whole);
+    const size_t nvox = (size_t)N * N * N;
+    std::vector<Point_Color> hcol(nvox);
+    for (size_t i = 0; i < nvox; ++i) {
+        hcol[i].data.r = (unsigned char)(i * 7);
+        hcol[i].data.g = (unsigned char)(i * 13);
+        hcol[i].data.b = (unsigned char)(i * 29);
+        hcol[i].data.w = (unsigned char)(i % 5 == 0 ? 0 : 200);
+    }
+    gpu_array<Point_Color> gcol(hcol.data(), dim3((unsigned)nvox), TO_GPU);
+    matrix<Point_Color> wcols(whole.Get_Num_Of_Elem());
+    Extract_Color_Volume(&gcol, &rb, whole, cell, gm.Get_Kernel("extract_colors"), wcols);
+    light_source light;
+    light.pos = t;
+    light.number = 1;
+    gpu_array<unsigned char> img(dim3((unsigned)(W * H * 3)));
+    Generate_Image(&vmap, &nmap, intr, light, &img, gm.Get_Kernel("generate_image"));
+    std::vector<unsigned char> himg((size_t)W * H * 3);
+    img.memcpy_to_host(himg.data());
     Clean_Tsdf_Slice(mn, mx, &rb, &vol, gm.Get_Kernel("clean_tsdf_slice"));
 
     std::vector<float> hv((size_t)W * H * 3), hn((size_t)W * H * 3), hv1((size_t)W * H * 3 / 4), hn1(hv1.size());
@@ -125,6 +147,11 @@ int main(int argc, char **argv) {
     wr(out, hvol.data(), hvol.size());
     wr(out, hvc.data(), hvc.size());
     wr(out, hnc.data(), hnc.size());
+    unsigned nw = whole.Get_Num_Of_Elem();
+    wr(out, &nw, 1);
+    if (nw) wr(out, (const float *)whole.data, (size_t)nw * 4);
+    if (nw) wr(out, (const unsigned char *)wcols.data, (size_t)nw * 4);
+    wr(out, himg.data(), himg.size());
     fclose(out);
     printf("ok points=%u\n", n);
     return 0;

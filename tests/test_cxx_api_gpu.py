@@ -69,6 +69,10 @@ def test_cxx_api_roundtrip_matches_oracle(cuda, orc, tmp_path, fmt):
     vol_bytes = orc.volume_bytes(fmt, rb)
     vol_after = take(np.uint8, vol_bytes)
     vc, nc = take(np.float32, W * H * 3).reshape(H, W, 3), take(np.float32, W * H * 3).reshape(H, W, 3)
+    nw = int(take(np.uint32, 1)[0])
+    whole = take(np.float32, 4 * nw).reshape(nw, 4)
+    wcols = take(np.uint8, 4 * nw).reshape(nw, 4)
+    img = take(np.uint8, W * H * 3).reshape(H, W, 3)
 
     # oracle
     R = traj[0, :9].reshape(3, 3).astype(np.float32)
@@ -81,6 +85,14 @@ def test_cxx_api_roundtrip_matches_oracle(cuda, orc, tmp_path, fmt):
     assert bits_equal(vm1, orc.resize_map(vmo, False)) and bits_equal(nm1, orc.resize_map(nmo, True))
     po, _, _, no = orc.extract_slice(vol, fmt, None, bounds[:3], bounds[3:], rb)
     assert n == no and n > 0 and np.array_equal(pts, po)
+    # Extract_Tsdf_Volume, Extract_Color_Volume (the caller's colour pattern), Generate_Image
+    wo, _, nwo = orc.extract_tsdf_volume(vol, fmt, rb, cell)
+    assert nw == nwo and nw > 100 and bits_equal(whole, wo)
+    i = np.arange(N ** 3, dtype=np.uint64)
+    colour = np.stack([(i * 7) % 256, (i * 13) % 256, (i * 29) % 256, np.where(i % 5 == 0, 0, 200)],
+                      axis=1).astype(np.uint8)
+    assert np.array_equal(wcols, orc.extract_color_volume(colour, rb, wo, cell))
+    assert np.array_equal(img, orc.generate_image(vmo, nmo, t))
     orc.clean_tsdf_slice(vol, fmt, bounds[:3], bounds[3:], rb)
     assert np.array_equal(vol_after, vol)
     # Estimate_Combined: the oracle's FP64 sums on the caller's own maps
