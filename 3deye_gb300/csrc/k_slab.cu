@@ -9,11 +9,15 @@
 // of one z slice, contiguous in raster order:
 //   1. count:   per tile and plane, the number of set predicates;
 //   2. scan:    one exclusive scan over counts laid out (chunk, plane, tile);
-//   3. scatter: predicates recomputed, ranked inside the tile with warp
-//               ballots, and written at offset + rank.
-// Tiles that cannot intersect the black zone exit at once, so the cost
-// follows the slab, not the volume.  All indexing is integer: the output is
-// bit-identical to the reference on the scan's predicate set.
+//   3. scatter: points ranked inside the tile and written at offset + rank.
+// Two forms: the row kernels (rows of whole 4-voxel groups: 16-byte loads,
+// the count pass stores each group's predicate bits for the scatter, ranks
+// from one block scan) and the scalar kernels (any row length: predicates
+// recomputed in the scatter, ranked with warp ballots).  Tiles that cannot
+// intersect the black zone exit at once, so the cost follows the slab, not
+// the volume; Extract_Tsdf_Volume is the same scan with the whole volume as
+// the zone.  All indexing is integer: the output is bit-identical to the
+// reference on the scan's predicate set.
 #include "tde_common.cuh"
 #include "tde_slab.cuh"
 
