@@ -42,7 +42,8 @@ int main(int argc, char **argv) {
     vector<string> names = {"scale_depth.cl", "integrate_tsdf_volume.cl", "raycast.cl", "resize_vertex_map.cl",
                             "resize_normal_map.cl", "estimate_combined.cl", "transform_estimation.cl",
                             "compute_bilateral_filtering.cl", "compute_vertex_map.cl", "compute_normal_map_eigen.cl",
-                            "clean_tsdf_slice.cl"};
+                            "clean_tsdf_slice.cl", "scan_the_whole_array.cl", "extract_tsdf_cloud.cl",
+                            "extract_colors.cl", "generate_image.cl"};
     kernel_manager gm("ignored/path", names);
     bool threw = false;
     try { gm.Get_Kernel("no_such_kernel.cl"); } catch (const std::exception &) { threw = true; }
