@@ -317,6 +317,29 @@ def test_extract_slice_capacity_and_no_color(tde, orc, cuda):
     assert not N(cols).any()
 
 
+def test_extract_scalar_path_matches_golden_and_oracle(tde, orc, cuda):
+    """A volume that is not 16-byte aligned takes the scalar count/scatter
+    kernels: the same golden slabs and the same whole-volume export."""
+    import torch
+    g, rb = slice_golden(tde)
+    raw = np.ascontiguousarray(g["tsdf"]).view(np.uint8).ravel()
+    buf = torch.zeros(raw.size + 16, dtype=torch.uint8, device=cuda)
+    buf[4:4 + raw.size] = torch.from_numpy(raw).to(cuda)
+    tsdf = buf[4:4 + raw.size]
+    assert tsdf.data_ptr() % 16 == 4
+    color = T(g["color"], cuda)
+    for ci in range(int(g["ncases"])):
+        pts, cols, _, n = tde.extract_slice(tsdf, tde.TSDF_I16, color, g[f"c{ci}_mn"], g[f"c{ci}_mx"], rb)
+        assert n == int(g[f"c{ci}_count"])
+        assert np.array_equal(N(pts).view(np.uint32), g[f"c{ci}_points"].view(np.uint32))
+        assert np.array_equal(N(cols), g[f"c{ci}_colors"])
+    ob = orc.make_rb(tuple(int(v) for v in g["dims"]), (2.0, 2.0, 2.0), tuple(int(v) for v in g["origin"]))
+    cell = (np.float32(2.0) / np.asarray(g["dims"], np.float32)).astype(np.float32)
+    po, wo, no = orc.extract_tsdf_volume(np.ascontiguousarray(g["tsdf"]), 0, ob, cell, weights=True)
+    pts, w, n = tde.extract_tsdf_volume(tsdf, tde.TSDF_I16, rb, tuple(cell), weights=True)
+    assert n == no and bits_equal(N(pts), po) and np.array_equal(N(w), wo)
+
+
 def test_extract_slice_empty_zone(tde, cuda):
     g, rb = slice_golden(tde)
     pts, cols, _, n = tde.extract_slice(T(g["tsdf"], cuda), 0, T(g["color"], cuda), (-50, -50, -50),
