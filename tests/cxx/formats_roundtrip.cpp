@@ -4,7 +4,8 @@
 //   float points[n_points][4]; uint8 colors[n_points][4]
 // Writes trajectory.txt, cloud.txt, colors.txt there with the C++ writers,
 // reads both clouds back with Fill_From_File and writes readback.bin
-// (int32 status pair, then the points and colours read).
+// (int32 status pair, counts, then the points and colours read); with two
+// more arguments, reads those text clouds into golden.bin likewise.
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -47,5 +48,20 @@ int main(int argc, char **argv) {
     if (n_in[0]) std::fwrite(cloud_in.data, sizeof(Point_XYZI), n_in[0], o);
     if (n_in[1]) std::fwrite(colors_in.data, sizeof(Point_Color), n_in[1], o);
     std::fclose(o);
+    // argv[2], argv[3] (optional): a point cloud and a colour cloud in the
+    // reference's text format, read with Fill_From_File into golden.bin
+    if (argc >= 4) {
+        matrix<Point_XYZI> gp;
+        matrix<Point_Color> gc;
+        int32_t gs[2] = {gp.Fill_From_File(argv[2]), gc.Fill_From_File(argv[3])};
+        FILE *g = std::fopen((dir + "/golden.bin").c_str(), "wb");
+        if (!g) return 8;
+        int32_t gn[2] = {(int32_t)gp.Get_Num_Of_Elem(), (int32_t)gc.Get_Num_Of_Elem()};
+        std::fwrite(gs, 4, 2, g);
+        std::fwrite(gn, 4, 2, g);
+        if (gn[0]) std::fwrite(gp.data, sizeof(Point_XYZI), gn[0], g);
+        if (gn[1]) std::fwrite(gc.data, sizeof(Point_Color), gn[1], g);
+        std::fclose(g);
+    }
     return 0;
 }

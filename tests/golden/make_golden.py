@@ -5,6 +5,8 @@ the reference tree).  Run here, where the reference tree exists:
     python tests/golden/make_golden.py
 
 Inputs are seeded; every fixture stores its inputs and the reference outputs.
+The slab clouds are also written in the reference's text format
+(slices_c*_points.txt, slices_c*_colors.txt).
 The reference ships no golden vectors or tests of its own, so these fixtures
 are what pins the oracle (tests/test_oracle_golden.py) and, through it, the
 CUDA kernels.
@@ -234,6 +236,18 @@ def gen_slices():
     return {ci: int(out[f"c{ci}_count"]) for ci in range(len(cases))}
 
 
+def gen_text_fixtures():
+    """The slab clouds of slices.npz again in the reference's own text format
+    (matrix<Point_XYZI> / matrix<Point_Color>::Save_To_File,
+    common/inc/impl/matrix.hpp:413-476), as a reference caller would save them."""
+    import importlib
+    fmt = importlib.import_module("3deye_gb300.formats")
+    g = np.load(OUT / "slices.npz")
+    for ci in range(int(g["ncases"])):
+        fmt.write_cloud(OUT / f"slices_c{ci}_points.txt", points=g[f"c{ci}_points"])
+        fmt.write_cloud(OUT / f"slices_c{ci}_colors.txt", colors=g[f"c{ci}_colors"])
+
+
 def main():
     if not orc.ref_available():
         sys.exit("oracle/_ref is not built: run oracle/build_ref.sh (needs the reference tree)")
@@ -242,6 +256,7 @@ def main():
     gen_transform_map()
     gen_transform_estimation()
     print("slice counts", gen_slices())
+    gen_text_fixtures()
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -111,3 +111,42 @@ def test_ppm_known_answer_and_round_trip(tmp_path):
     np.testing.assert_array_equal(fmt.read_ppm(p), img)
     with pytest.raises(ValueError):
         fmt.write_ppm(p, np.zeros((2, 3), np.uint8))
+
+
+def test_golden_slab_clouds_in_reference_text_format():
+    """tests/golden/slices_c*_{points,colors}.txt hold the reference kernels'
+    slab clouds as matrix<T>::Save_To_File writes them; read back they equal
+    the binary fixtures exactly (voxel-unit points print without rounding)."""
+    golden = ROOT / "tests" / "golden"
+    g = np.load(golden / "slices.npz")
+    for ci in range(int(g["ncases"])):
+        pts = fmt.read_cloud(golden / f"slices_c{ci}_points.txt")
+        np.testing.assert_array_equal(pts.reshape(-1, 4), g[f"c{ci}_points"])
+        cols = fmt.read_cloud(golden / f"slices_c{ci}_colors.txt")
+        if len(cols):
+            np.testing.assert_array_equal(cols, g[f"c{ci}_colors"])
+        text = (golden / f"slices_c{ci}_points.txt").read_text()
+        assert text == fmt.format_cloud(points=g[f"c{ci}_points"])
+
+
+def test_golden_text_clouds_read_by_cxx_fill_from_file(tmp_path):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    exe = tmp_path / "formats_roundtrip"
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", str(ROOT / "include" / "3deye"), "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cxx" / "formats_roundtrip.cpp"), "-o", str(exe)], check=True)
+    with open(tmp_path / "input.bin", "wb") as f:
+        np.array([0, 0], np.int32).tofile(f)
+    golden = ROOT / "tests" / "golden"
+    g = np.load(golden / "slices.npz")
+    ci = 1
+    r = subprocess.run([str(exe), str(tmp_path), str(golden / f"slices_c{ci}_points.txt"),
+                        str(golden / f"slices_c{ci}_colors.txt")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = (tmp_path / "golden.bin").read_bytes()
+    st = np.frombuffer(raw, np.int32, 4)
+    n = len(g[f"c{ci}_points"])
+    assert st[0] == 0 and st[1] == 0 and st[2] == n and st[3] == n
+    np.testing.assert_array_equal(np.frombuffer(raw, np.float32, 4 * n, 16).reshape(-1, 4), g[f"c{ci}_points"])
+    np.testing.assert_array_equal(np.frombuffer(raw, np.uint8, 4 * n, 16 + 16 * n).reshape(-1, 4), g[f"c{ci}_colors"])
