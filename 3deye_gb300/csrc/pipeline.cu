@@ -275,13 +275,21 @@ void drop_graphs(tde_pipeline *p) {
 const Segment kMainFirst[] = {SEG_POST_FIRST, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
 const Segment kMainTracked[] = {SEG_ICP, SEG_INTEGRATE, SEG_RAYCAST, SEG_RESIZE};
 
-// (Re)captures every graph; existing executables are updated in place.
-int capture_all(tde_pipeline *p) {
+// Segments whose kernels take the round buffer by value (a volume shift
+// changes it); the others -- preprocessing, ICP, pose publication, model
+// pyramid -- read only frame and model maps.
+bool reads_round_buffer(Segment sg) { return sg == SEG_INTEGRATE || sg == SEG_RAYCAST || sg == SEG_COLOR; }
+
+// (Re)captures the graphs; existing executables are updated in place.  After
+// a volume shift (`shift_only`) the segments that do not read the round
+// buffer keep their graphs.
+int capture_all(tde_pipeline *p, bool shift_only = false) {
     p->captured = false;
     for (int set = 0; set < 2; ++set) {
         for (int sgi = 0; sgi < SEG_COUNT; ++sgi) {
             Segment sg = (Segment)sgi;
             if (sg == SEG_COLOR && !p->colvol) continue;  // nothing to capture
+            if (shift_only && p->seg_exec[set][sgi] && !reads_round_buffer(sg)) continue;
             TDE_TRY(capture(p, &sg, 1, set, &p->seg_exec[set][sgi]));
         }
         TDE_TRY(capture(p, kMainFirst, 4, set, &p->main_exec[set][0]));
@@ -907,7 +915,7 @@ int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, 
     TDE_TRY(cast_model(p, s));
     TDE_TRY(record_segment(p, SEG_RESIZE, 0, s));
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift");
-    if (p->cfg.use_graphs) return capture_all(p);
+    if (p->cfg.use_graphs) return capture_all(p, true);
     return TDE_OK;
 }
 
