@@ -377,6 +377,55 @@ void release(tde_pipeline *p) {
 
 }  // namespace
 
+// The float camera pose (and its inverse) the raycast and integration read,
+// from an FP64 pose.
+static int upload_camera(tde_pipeline *p, const double *pose, cudaStream_t s) {
+    CamPose cam;
+    std::memset(&cam, 0, sizeof(cam));
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            cam.R[3 * r + c] = (float)pose[3 * r + c];
+            cam.R_inv[3 * r + c] = (float)pose[3 * c + r];
+        }
+    for (int a = 0; a < 3; ++a) cam.t[a] = (float)pose[9 + a];
+    cam.tracking_ok = 1;
+    TDE_CUDA(cudaMemcpyAsync(p->cam, &cam, sizeof(cam), cudaMemcpyHostToDevice, s), "camera upload");
+    return TDE_OK;
+}
+
+// Checkpoint layout: this header, then the TSDF volume, the brick flags
+// (negative ever written, per brick and super-brick), the saturation flags
+// and, with a colour volume, the colour volume.
+struct CheckpointHeader {
+    char magic[8];  // "TDECKPT1"
+    int32_t tsdf_format, has_color;
+    int32_t cols, rows, levels, pad;
+    int64_t frames;
+    tde_round_buffer rb;
+    double pose12[12];
+    uint64_t volume_bytes, negflags_bytes, satflags_bytes, color_bytes;
+};
+static_assert(sizeof(CheckpointHeader) == 240, "checkpoint header layout");
+static const char kCheckpointMagic[8] = {'T', 'D', 'E', 'C', 'K', 'P', 'T', '1'};
+
+static CheckpointHeader checkpoint_layout(const tde_pipeline *p) {
+    CheckpointHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kCheckpointMagic, 8);
+    h.tsdf_format = p->cfg.tsdf_format;
+    h.has_color = p->colvol != nullptr;
+    h.cols = p->cfg.intr.cols;
+    h.rows = p->cfg.intr.rows;
+    h.levels = p->levels;
+    h.frames = p->frames;
+    h.rb = p->rb;
+    h.volume_bytes = tde_tsdf_volume_bytes(p->cfg.tsdf_format, &p->rb);
+    h.negflags_bytes = brick_flags_bytes(p->rb);
+    h.satflags_bytes = brick_count(p->rb);
+    h.color_bytes = p->colvol ? voxel_count(p->rb) * sizeof(tde_color) : 0;
+    return h;
+}
+
 // Count pass and scatter into the pipeline's point buffers (grown once when
 // short); the total goes to *count.  `launch(capacity)` enqueues one
 // extraction on the pipeline stream.
@@ -902,16 +951,7 @@ int tde_pipeline_shift_ex(tde_pipeline *p, const int *delta3, tde_xyzi *points, 
     TDE_TRY(tde_pipeline_pose(p, pose));
     for (int a = 0; a < 3; ++a) pose[9 + a] -= (double)delta3[a] * cs[a];
     TDE_TRY(write_pose(p, pose));
-    CamPose cam;
-    std::memset(&cam, 0, sizeof(cam));
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) {
-            cam.R[3 * r + c] = (float)pose[3 * r + c];
-            cam.R_inv[3 * r + c] = (float)pose[3 * c + r];
-        }
-    for (int a = 0; a < 3; ++a) cam.t[a] = (float)pose[9 + a];
-    cam.tracking_ok = 1;
-    TDE_CUDA(cudaMemcpyAsync(p->cam, &cam, sizeof(cam), cudaMemcpyHostToDevice, s), "pipeline_shift: camera");
+    TDE_TRY(upload_camera(p, pose, s));
     TDE_TRY(cast_model(p, s));
     TDE_TRY(record_segment(p, SEG_RESIZE, 0, s));
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_shift");
@@ -935,6 +975,78 @@ int tde_pipeline_extract_volume(tde_pipeline *p, tde_xyzi *points, float *weight
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_extract_volume");
     return points_to_host(p, "pipeline_extract_volume", *count, points, weights, p->colvol ? colors : nullptr,
                           capacity);
+}
+
+size_t tde_pipeline_checkpoint_bytes(tde_pipeline *p) {
+    if (!p) return 0;
+    const CheckpointHeader h = checkpoint_layout(p);
+    return sizeof(h) + h.volume_bytes + h.negflags_bytes + h.satflags_bytes + h.color_bytes;
+}
+
+int tde_pipeline_checkpoint(tde_pipeline *p, void *buffer, size_t bytes) {
+    if (!p || !buffer) return set_error(TDE_ERR_INVALID_ARG, "pipeline_checkpoint: null argument");
+    if (bytes < tde_pipeline_checkpoint_bytes(p))
+        return set_error(TDE_ERR_CAPACITY, "pipeline_checkpoint: %zu < %zu bytes", bytes,
+                         tde_pipeline_checkpoint_bytes(p));
+    TDE_TRY(tde_pipeline_sync(p));
+    CheckpointHeader h = checkpoint_layout(p);
+    TDE_TRY(tde_pipeline_pose(p, h.pose12));
+    char *o = static_cast<char *>(buffer);
+    std::memcpy(o, &h, sizeof(h));
+    o += sizeof(h);
+    TDE_CUDA(cudaMemcpy(o, p->volume, h.volume_bytes, cudaMemcpyDeviceToHost), "pipeline_checkpoint: volume");
+    o += h.volume_bytes;
+    TDE_CUDA(cudaMemcpy(o, p->negflags, h.negflags_bytes, cudaMemcpyDeviceToHost), "pipeline_checkpoint: flags");
+    o += h.negflags_bytes;
+    TDE_CUDA(cudaMemcpy(o, p->satflags, h.satflags_bytes, cudaMemcpyDeviceToHost), "pipeline_checkpoint: flags");
+    o += h.satflags_bytes;
+    if (h.color_bytes)
+        TDE_CUDA(cudaMemcpy(o, p->colvol, h.color_bytes, cudaMemcpyDeviceToHost), "pipeline_checkpoint: colour");
+    return TDE_OK;
+}
+
+int tde_pipeline_restore(tde_pipeline *p, const void *buffer, size_t bytes) {
+    if (!p || !buffer) return set_error(TDE_ERR_INVALID_ARG, "pipeline_restore: null argument");
+    CheckpointHeader h;
+    if (bytes < sizeof(h)) return set_error(TDE_ERR_INVALID_ARG, "pipeline_restore: %zu bytes, no header", bytes);
+    std::memcpy(&h, buffer, sizeof(h));
+    if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0)
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_restore: not a pipeline checkpoint");
+    if (!valid_round_buffer(&h.rb)) return set_error(TDE_ERR_INVALID_ARG, "pipeline_restore: bad round buffer");
+    // the checkpoint must describe this pipeline's shapes and storage
+    const CheckpointHeader mine = checkpoint_layout(p);
+    if (h.tsdf_format != mine.tsdf_format || h.cols != mine.cols || h.rows != mine.rows || h.levels != mine.levels ||
+        h.rb.voxels_size.x != mine.rb.voxels_size.x || h.rb.voxels_size.y != mine.rb.voxels_size.y ||
+        h.rb.voxels_size.z != mine.rb.voxels_size.z || h.has_color != mine.has_color ||
+        h.volume_bytes != mine.volume_bytes || h.negflags_bytes != mine.negflags_bytes ||
+        h.satflags_bytes != mine.satflags_bytes || h.color_bytes != mine.color_bytes || h.frames < 0)
+        return set_error(TDE_ERR_INVALID_ARG,
+                         "pipeline_restore: the checkpoint's format, frame size, volume size or colour volume "
+                         "differs from this pipeline's");
+    const size_t need = sizeof(h) + h.volume_bytes + h.negflags_bytes + h.satflags_bytes + h.color_bytes;
+    if (bytes < need) return set_error(TDE_ERR_INVALID_ARG, "pipeline_restore: %zu < %zu bytes", bytes, need);
+    TDE_TRY(tde_pipeline_sync(p));
+    const char *i = static_cast<const char *>(buffer) + sizeof(h);
+    TDE_CUDA(cudaMemcpy(p->volume, i, h.volume_bytes, cudaMemcpyHostToDevice), "pipeline_restore: volume");
+    i += h.volume_bytes;
+    TDE_CUDA(cudaMemcpy(p->negflags, i, h.negflags_bytes, cudaMemcpyHostToDevice), "pipeline_restore: flags");
+    i += h.negflags_bytes;
+    TDE_CUDA(cudaMemcpy(p->satflags, i, h.satflags_bytes, cudaMemcpyHostToDevice), "pipeline_restore: flags");
+    i += h.satflags_bytes;
+    if (h.color_bytes)
+        TDE_CUDA(cudaMemcpy(p->colvol, i, h.color_bytes, cudaMemcpyHostToDevice), "pipeline_restore: colour");
+    p->rb = h.rb;
+    p->frames = (int)h.frames;
+    TDE_TRY(write_pose(p, h.pose12));
+    // the model maps the next frame tracks against: cast from the restored
+    // volume and pose, as the checkpointed frame cast them
+    cudaStream_t s = p->stream;
+    TDE_TRY(upload_camera(p, h.pose12, s));
+    TDE_TRY(cast_model(p, s));
+    TDE_TRY(record_segment(p, SEG_RESIZE, 0, s));
+    TDE_CUDA(cudaStreamSynchronize(s), "pipeline_restore");
+    if (p->cfg.use_graphs) return capture_all(p, true);
+    return TDE_OK;
 }
 
 int tde_pipeline_set_pose(tde_pipeline *p, const double *pose12) {

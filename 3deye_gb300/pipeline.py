@@ -44,6 +44,9 @@ declare("tde_pipeline_shift_ex", I, [P, P, P, P, P, C.c_uint32, C.POINTER(C.c_ui
 declare("tde_pipeline_extract_volume", I, [P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)])
 declare("tde_pipeline_render", I, [P, P, P])
 declare("tde_pipeline_shift_needed_pose", I, [P, P, C.c_float, C.c_float, P])
+declare("tde_pipeline_checkpoint_bytes", C.c_size_t, [P])
+declare("tde_pipeline_checkpoint", I, [P, P, C.c_size_t])
+declare("tde_pipeline_restore", I, [P, P, C.c_size_t])
 declare("tde_pipeline_enqueue_rgbd", I, [P, P, P, I, P, P])
 declare("tde_pipeline_enable_color", I, [P, I])
 declare("tde_pipeline_color_volume", I, [P, C.POINTER(P)])
@@ -257,6 +260,24 @@ class Pipeline:
         of cols*rows*3 bytes; light at the camera centre unless light_pos."""
         light = None if light_pos is None else C.byref(LightSource(Point3f(*light_pos), 1))
         check(lib.tde_pipeline_render(self._h, light, image_ptr))
+
+    def checkpoint(self) -> np.ndarray:
+        """The state the next frame depends on, as bytes (see tde_pipeline_checkpoint)."""
+        n = lib.tde_pipeline_checkpoint_bytes(self._h)
+        buf = np.empty(n, np.uint8)
+        check(lib.tde_pipeline_checkpoint(self._h, buf.ctypes.data_as(P), n))
+        return buf
+
+    def restore(self, buf) -> None:
+        """Continue from a checkpoint of a pipeline with the same configuration."""
+        b = np.ascontiguousarray(buf, np.uint8)
+        check(lib.tde_pipeline_restore(self._h, b.ctypes.data_as(P), b.size))
+
+    def save(self, path) -> None:
+        self.checkpoint().tofile(path)
+
+    def load(self, path) -> None:
+        self.restore(np.fromfile(path, np.uint8))
 
     def world_cloud(self, points):
         """Volume-frame points (as extract_volume returns them) in the world

@@ -161,6 +161,19 @@ int tde_pipeline_extract_volume(tde_pipeline *p, tde_xyzi *points, float *weight
  * tde_generate_image. */
 int tde_pipeline_render(tde_pipeline *p, const tde_light_source *light, uint8_t *image);
 
+/* Checkpoint / resume.  A checkpoint holds what the next frame depends on:
+ * the TSDF volume, the per-brick flags, the round buffer, the FP64 pose,
+ * the frame count and, with one, the colour volume (a 240-byte header, then
+ * those buffers).  tde_pipeline_restore loads one into a pipeline created
+ * with the same configuration (and tde_pipeline_enable_color when the
+ * checkpoint has colour), casts the model maps again from the restored
+ * volume and pose, and the frames that follow produce the same bits as
+ * they would have after the checkpointed frame.  Both are host-synchronous;
+ * `buffer` is host memory of tde_pipeline_checkpoint_bytes bytes. */
+size_t tde_pipeline_checkpoint_bytes(tde_pipeline *p);
+int tde_pipeline_checkpoint(tde_pipeline *p, void *buffer, size_t bytes);
+int tde_pipeline_restore(tde_pipeline *p, const void *buffer, size_t bytes);
+
 /* Measurement: casts the current model again from the last frame's pose
  * (into scratch maps) and counts the distinct voxel records the raycast
  * reads -- with skip_empty, as the pipeline's raycast does (skipping bricks

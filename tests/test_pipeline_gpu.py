@@ -2,6 +2,7 @@
 oracle pipeline (FP64 ICP sums and solve) and against itself (graph replay
 vs eager launches, asynchronous vs blocking API)."""
 import ctypes as C
+import dataclasses
 import importlib
 
 import numpy as np
@@ -199,7 +200,6 @@ def test_saturated_brick_skip_is_exact(cuda, tde, seq):
     pipeline's volume still equals, bit for bit, a replay of the same frames
     and poses through the C-ABI integration (which sweeps every brick), and
     the pipeline swept fewer bricks than with a weight that never saturates."""
-    import dataclasses
     import torch
     pl = importlib.import_module("3deye_gb300.pipeline")
     cfg0, traj, depths = seq
@@ -376,3 +376,68 @@ def test_pipeline_render_matches_oracle(cuda, tde, orc, seq, tmp_path):
     fmt.write_ppm(tmp_path / "model.ppm", got)
     assert np.array_equal(fmt.read_ppm(tmp_path / "model.ppm"), got)
     p.close()
+
+
+@pytest.mark.parametrize("color", [False, True])
+def test_checkpoint_resume_bit_identical(cuda, tde, seq, tmp_path, color):
+    """A pipeline restored from a checkpoint (here one that started from
+    another pose) continues exactly as the checkpointed one: the same poses,
+    TSDF and colour volume, bit for bit.  Checkpoints of another
+    configuration are refused."""
+    pl = importlib.import_module("3deye_gb300.pipeline")
+    cfg, traj, depths = seq
+    rng = np.random.default_rng(12)
+    rgbs = [rng.integers(0, 256, (cfg.rows, cfg.cols, 3), dtype=np.uint8) for _ in depths]
+    tde.lib.tde_memcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+
+    def make(pose):
+        p = pl.Pipeline(cfg, pose)
+        if color:
+            p.enable_color(max_weight=16)
+        return p
+
+    def step(p, i):
+        return p.process_rgbd(depths[i], rgbs[i]) if color else p.process(depths[i])
+
+    def state(p):
+        vptr, rb = p.volume()
+        vol = np.zeros(tde.lib.tde_tsdf_volume_bytes(cfg.tsdf_format, C.byref(rb)), np.uint8)
+        tde.check(tde.lib.tde_memcpy(vol.ctypes.data_as(C.c_void_p), C.c_void_p(vptr), vol.nbytes, 1))
+        col = None
+        if color:
+            col = np.zeros((cfg.voxels ** 3, 4), np.uint8)
+            tde.check(tde.lib.tde_memcpy(col.ctypes.data_as(C.c_void_p), C.c_void_p(p.color_volume()), col.nbytes, 1))
+        return vol, col
+
+    k = 6
+    a = make(traj[0])
+    for i in range(k):
+        assert step(a, i)[1] == 0
+    ck = a.checkpoint()
+    a.save(tmp_path / "ck.bin")
+    ref = [step(a, i)[0] for i in range(k, len(depths))]
+    ref_vol, ref_col = state(a)
+    a.close()
+    for via_file in (False, True):
+        b = make(traj[3])
+        if via_file:
+            b.load(tmp_path / "ck.bin")
+        else:
+            b.restore(ck)
+        got = [step(b, i)[0] for i in range(k, len(depths))]
+        vol, col = state(b)
+        b.close()
+        assert all(np.array_equal(x, y) for x, y in zip(got, ref))
+        assert np.array_equal(vol, ref_vol)
+        if color:
+            assert np.array_equal(col, ref_col) and (col[:, 3] > 0).sum() > 1000
+    # another storage format, or colour on one side only, is refused
+    other = pl.Pipeline(dataclasses.replace(cfg, tsdf_format=1), traj[0])
+    with pytest.raises(tde.TdeError):
+        other.restore(ck)
+    other.close()
+    if color:
+        plain = pl.Pipeline(cfg, traj[0])
+        with pytest.raises(tde.TdeError):
+            plain.restore(ck)
+        plain.close()
