@@ -2,6 +2,7 @@
 declare, and its host-only logic and argument validation behave (no kernel
 launches here)."""
 import ctypes as C
+import importlib
 import re
 import subprocess
 
@@ -68,6 +69,20 @@ def test_round_buffer_init_and_volume_bytes(tde):
     assert tde.tsdf_volume_bytes(0, bad) == 0  # beyond int32 voxel addressing
 
 
+_DUMMY = C.c_void_p(256)  # never dereferenced: each call below fails validation first
+
+
+def _p3f(v):
+    from importlib import import_module
+    return import_module("3deye_gb300").Point3f(v, v, v)
+
+
+def _light(number):
+    from importlib import import_module
+    t = import_module("3deye_gb300")
+    return t.LightSource(t.Point3f(0.0, 0.0, 0.0), number)
+
+
 @pytest.mark.parametrize("call", [
     lambda L, rb: L.tde_integrate_tsdf(None, None, 0, 0.03, None, None, None, None, C.byref(rb), 128, None),
     lambda L, rb: L.tde_tsdf_init(None, 0, C.byref(rb), None),
@@ -77,10 +92,31 @@ def test_round_buffer_init_and_volume_bytes(tde):
                                       None, None),
     lambda L, rb: L.tde_clean_tsdf_slice(None, 0, _p3(0), _p3(0), C.byref(rb), None),
     lambda L, rb: L.tde_raycast(None, 5, None, None, None, None, 0.1, None, C.byref(rb), None, None),
+    # whole-volume export, colour lookup, shading: refused before any device work
+    lambda L, rb: L.tde_extract_tsdf_volume(None, 0, C.byref(rb), _p3f(0.1), None, 0, None, None, 0, None, None),
+    lambda L, rb: L.tde_extract_tsdf_volume(_DUMMY, 0, C.byref(rb), _p3f(0.0), _DUMMY, 64, None, None, 0, _DUMMY,
+                                            None),
+    lambda L, rb: L.tde_extract_tsdf_volume(_DUMMY, 9, C.byref(rb), _p3f(0.1), _DUMMY, 64, None, None, 0, _DUMMY,
+                                            None),
+    lambda L, rb: L.tde_extract_color_volume(None, C.byref(rb), None, 0, _p3f(0.1), None, None),
+    lambda L, rb: L.tde_extract_color_volume(_DUMMY, C.byref(rb), _DUMMY, 4, _p3f(float("nan")), _DUMMY, None),
+    lambda L, rb: L.tde_generate_image(_DUMMY, _DUMMY, 4, 4, C.byref(_light(2)), _DUMMY, None),
+    lambda L, rb: L.tde_generate_image(_DUMMY, _DUMMY, 0, 4, C.byref(_light(1)), _DUMMY, None),
+    lambda L, rb: L.tde_generate_image(None, _DUMMY, 4, 4, C.byref(_light(1)), _DUMMY, None),
+    # pipeline checkpoint / resume and pose-driven shifts without a pipeline
+    lambda L, rb: L.tde_pipeline_checkpoint(None, None, 0),
+    lambda L, rb: L.tde_pipeline_restore(None, None, 0),
+    lambda L, rb: L.tde_pipeline_shift_needed_pose(None, None, 1.5, 0.4, None),
 ])
 def test_invalid_arguments_are_reported(tde, call):
+    importlib.import_module("3deye_gb300.pipeline")  # declares the pipeline entry points
     rb = tde.round_buffer((8, 8, 8), (1.0, 1.0, 1.0))
     assert call(tde.lib, rb) == -1
+
+
+def test_checkpoint_size_without_pipeline(tde):
+    importlib.import_module("3deye_gb300.pipeline")
+    assert tde.lib.tde_pipeline_checkpoint_bytes(None) == 0
 
 
 def test_host_icp_solve_matches_oracle(tde, orc):
