@@ -11,11 +11,16 @@ Reported (one JSON line, rank 0):
   e2e        frames/s through the C-ABI pipeline with depth in pinned host
              memory: every step copies its frame host->device and the frame's
              pose device->host inside the timed region;
-  roofline   integration kernel (the HBM-bound sweep): algorithmic bytes per
-             launch (4 B/voxel read + 4 B/voxel written for the voxels the
-             update touches, counted live, + the scaled depth map) over its
-             CUDA-event launch time, against MEASURED_PEAKS.json hbm_gbs;
-  cpu_baseline  the CPU oracle of the same pipeline on this host's cores.
+  roofline   the dominant kernel, the ICP iteration: 48 B per pixel of
+             algorithmic traffic over its time per iteration, against
+             MEASURED_PEAKS.json hbm_gbs; `kernels` adds the integration
+             sweep (4 B/voxel read + 4 B/voxel written for the voxels the
+             update touches, counted live) and the raycast;
+  cpu_baseline  the CPU oracle of the same pipeline on this host's cores;
+  learned_refine, color_volume, model_export, cyclic_volume
+             the refiner in place of the bilateral filter, RGB-D frames with
+             the colour volume, the whole-model export and shading, and the
+             640x480 / 512^3 corridor with the volume following the camera.
 N > 1 runs independent replicas (sequence seed = rank): scaling "weak".
 
 --impl reference runs the CPU implementation of the path (the oracle port:
