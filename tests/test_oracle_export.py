@@ -79,3 +79,43 @@ def test_shading_known_answers(orc):
     flat = orc.generate_image(v, n, (0.0, 0.0, 0.0), 0)
     valid = ~np.isnan(v[..., 0]) & ~np.isnan(n[..., 0])
     assert (flat[valid] == 255).all() and not flat[~valid].any()
+
+
+def test_color_integration_known_answers(orc):
+    """Integrate_Colors as restated (KinectFusion colour averaging): a camera
+    looking along +z at a model plane through the centres of voxel slice
+    z = 8; only that slice is within the truncation distance of the model
+    surface.  Colours are running means rounded half to even; the weight
+    stops at max_weight."""
+    N, cellv, trunc = 16, 0.1, 0.06
+    rb = orc.make_rb((N, N, N), (N * cellv,) * 3, (0, 0, 0))
+    cell = np.full(3, cellv, np.float32)
+    W = H = 16
+    intr = orc.Intr(20.0, 20.0, 7.5, 7.5, W, H)
+    t = np.array([0.8, 0.8, -1.0], np.float32)
+    Ri = np.eye(3, dtype=np.float32)
+    plane_z = np.float32(8.5 * cellv)
+    vs, us = np.mgrid[0:H, 0:W].astype(np.float32)
+    depth = plane_z - t[2]
+    vmap = np.stack([(us - 7.5) / 20.0 * depth + t[0], (vs - 7.5) / 20.0 * depth + t[1],
+                     np.full_like(us, plane_z)], axis=-1).astype(np.float32)
+    color = np.zeros((N ** 3, 4), np.uint8)
+    z_of = np.arange(N ** 3) // (N * N)
+
+    def rgb(r, g, b):
+        return np.broadcast_to(np.array([r, g, b], np.uint8), (H, W, 3)).copy()
+
+    n1 = orc.integrate_colors(color, rgb(10, 200, 253), vmap, trunc, Ri, t, intr, cell, rb, max_weight=2)
+    hit = color[:, 3] > 0
+    assert n1 == hit.sum() > 50 and (z_of[hit] == 8).all()
+    assert (color[hit] == [10, 200, 253, 1]).all() and not color[~hit].any()
+    # a second frame: means (10+20)/2 = 15, (200+100)/2 = 150, (253+0)/2 = 126.5 -> 126 (ties to even)
+    orc.integrate_colors(color, rgb(20, 100, 0), vmap, trunc, Ri, t, intr, cell, rb, max_weight=2)
+    assert (color[hit] == [15, 150, 126, 2]).all()
+    # at max_weight the mean keeps weight 2: (15*2 + 30)/3 = 20, (150*2 + 0)/3 = 100, (126*2 + 3)/3 = 85
+    orc.integrate_colors(color, rgb(30, 0, 3), vmap, trunc, Ri, t, intr, cell, rb, max_weight=2)
+    assert (color[hit] == [20, 100, 85, 2]).all()
+    # no model surface: nothing changes
+    before = color.copy()
+    assert orc.integrate_colors(color, rgb(1, 2, 3), np.full_like(vmap, np.nan), trunc, Ri, t, intr, cell, rb) == 0
+    assert np.array_equal(color, before)
