@@ -150,3 +150,12 @@ def read_ppm(path) -> np.ndarray:
         raise ValueError("read_ppm: not a binary 8-bit PPM")
     cols, rows = (int(v) for v in parts[1].split())
     return np.frombuffer(parts[3], np.uint8, rows * cols * 3).reshape(rows, cols, 3)
+
+
+def format_round_buffer(origin_grid, origin_grid_global, origin_metric, volume_size, voxels_size, start_index,
+                        buffer_length) -> str:
+    """round_buffer's text record (common/src/round_buffer.cpp:99-113): the five
+    points "axbxc " each followed by "r", then start_index and buffer_length
+    each followed by "r", then a space."""
+    pts = (origin_grid, origin_grid_global, origin_metric, volume_size, voxels_size)
+    return "".join(format_point(p) + "r" for p in pts) + f"{int(start_index)}r{int(buffer_length)}r "

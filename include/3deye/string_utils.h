@@ -7,6 +7,7 @@
  *   XYZI                  "xxyxzxw"  common/src/base_points.cpp:571-574 (reader :550-568)
  *   Color                 "r.g.b.w " common/src/base_points.cpp:279-282 (reader :251-276)
  *   Point<T>              as T       common/inc/types/base_point_interface.hpp:46-62
+ *   round_buffer          "<p>r" x5, "start r length r "  common/src/round_buffer.cpp:99-113
  *   write_isometry_to_file           common/src/string_utils.cpp:26-74
  * Floats print with the stream's defaults (6 significant digits).  The
  * Python twin (3deye_gb300/formats.py) writes the same bytes.
@@ -66,6 +67,31 @@ inline std::istream &operator>>(std::istream &in, Color &c) {
     return in;
 }
 template <class T> std::istream &operator>>(std::istream &in, Point<T> &p) { return in >> p.data; }
+
+/* round_buffer as common/src/round_buffer.cpp:99-113 writes it: origin_GRID,
+ * origin_GRID_global, origin_metric, volume_size and voxels_size (points,
+ * "axbxc "), start_index and buffer_length, each followed by "r", then a
+ * space. */
+inline std::ostream &operator<<(std::ostream &out, const round_buffer &rb) {
+    return out << rb.origin_GRID << 'r' << rb.origin_GRID_global << 'r' << rb.origin_metric << 'r' << rb.volume_size
+               << 'r' << rb.voxels_size << 'r' << rb.start_index << 'r' << rb.buffer_length << 'r' << ' ';
+}
+/* Reads the whole record back (six whitespace-separated tokens; the
+ * reference's reader, round_buffer.cpp:76-97, takes one token, which ends
+ * after the first point). */
+inline std::istream &operator>>(std::istream &in, round_buffer &rb) {
+    std::string rec, tok;
+    for (int k = 0; k < 6 && in >> tok; ++k) rec += tok + " ";
+    replaceAll(rec, "x", " ");
+    replaceAll(rec, "r", " ");
+    std::istringstream t(rec);
+    t >> rb.origin_GRID.x >> rb.origin_GRID.y >> rb.origin_GRID.z >> rb.origin_GRID_global.x >>
+        rb.origin_GRID_global.y >> rb.origin_GRID_global.z >> rb.origin_metric.x >> rb.origin_metric.y >>
+        rb.origin_metric.z >> rb.volume_size.x >> rb.volume_size.y >> rb.volume_size.z >> rb.voxels_size.x >>
+        rb.voxels_size.y >> rb.voxels_size.z >> rb.start_index >> rb.buffer_length;
+    if (!t) in.setstate(std::ios::failbit);
+    return in;
+}
 
 /* write_isometry_to_file: per pose its index, R (matrix_3f) and t
  * (vector_3f), each followed by a newline.  A null name throws (the

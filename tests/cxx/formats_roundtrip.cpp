@@ -8,6 +8,7 @@
 // more arguments, reads those text clouds into golden.bin likewise.
 #include <cstdint>
 #include <cstdio>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -48,6 +49,32 @@ int main(int argc, char **argv) {
     if (n_in[0]) std::fwrite(cloud_in.data, sizeof(Point_XYZI), n_in[0], o);
     if (n_in[1]) std::fwrite(colors_in.data, sizeof(Point_Color), n_in[1], o);
     std::fclose(o);
+    // a round buffer record, written and read back into rb.bin
+    {
+        // the record's fields only (round_buffer's constructors live in the library)
+        alignas(round_buffer) unsigned char store[2][sizeof(round_buffer)] = {};
+        round_buffer &rb = *reinterpret_cast<round_buffer *>(store[0]);
+        round_buffer &back = *reinterpret_cast<round_buffer *>(store[1]);
+        rb.origin_GRID = make_point_3i(3, 500, 7);
+        rb.origin_GRID_global = make_point_3f(3.f, -12.f, 7.f);
+        rb.origin_metric = make_point_3f(0.0175781f, -0.0703125f, 0.0410156f);
+        rb.volume_size = make_point_3f(3.f, 3.f, 3.f);
+        rb.voxels_size = make_point_3i(512, 512, 512);
+        rb.start_index = 0;
+        rb.buffer_length = 512 * 512 * 512;
+        {
+            std::ofstream f((dir + "/rb.txt").c_str());
+            f << rb;
+        }
+        std::ifstream f((dir + "/rb.txt").c_str());
+        f >> back;
+        FILE *b = std::fopen((dir + "/rb.bin").c_str(), "wb");
+        if (!b) return 9;
+        int32_t ok = f ? 1 : 0;
+        std::fwrite(&ok, 4, 1, b);
+        std::fwrite(&back, sizeof(back), 1, b);
+        std::fclose(b);
+    }
     // argv[2], argv[3] (optional): a point cloud and a colour cloud in the
     // reference's text format, read with Fill_From_File into golden.bin
     if (argc >= 4) {

@@ -150,3 +150,32 @@ def test_golden_text_clouds_read_by_cxx_fill_from_file(tmp_path):
     assert st[0] == 0 and st[1] == 0 and st[2] == n and st[3] == n
     np.testing.assert_array_equal(np.frombuffer(raw, np.float32, 4 * n, 16).reshape(-1, 4), g[f"c{ci}_points"])
     np.testing.assert_array_equal(np.frombuffer(raw, np.uint8, 4 * n, 16 + 16 * n).reshape(-1, 4), g[f"c{ci}_colors"])
+
+
+def test_round_buffer_text_record(tmp_path):
+    """C++ operator<< writes round_buffer.cpp's record byte for byte as the
+    Python formatter does, and operator>> reads every field back."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    exe = tmp_path / "formats_roundtrip"
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", str(ROOT / "include" / "3deye"), "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cxx" / "formats_roundtrip.cpp"), "-o", str(exe)], check=True)
+    with open(tmp_path / "input.bin", "wb") as f:
+        np.array([0, 0], np.int32).tofile(f)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f32 = np.float32
+    expect = fmt.format_round_buffer((3, 500, 7), (f32(3), f32(-12), f32(7)),
+                                     (f32(0.0175781), f32(-0.0703125), f32(0.0410156)), (f32(3),) * 3, (512,) * 3,
+                                     0, 512 ** 3)
+    assert (tmp_path / "rb.txt").read_text() == expect
+    assert expect.startswith("3x500x7 r3x-12x7 r0.0175781x-0.0703125x0.0410156 r3x3x3 r512x512x512 r0r134217728r")
+    raw = (tmp_path / "rb.bin").read_bytes()
+    assert np.frombuffer(raw, np.int32, 1)[0] == 1
+    ints = np.frombuffer(raw, np.int32, 18, 4)
+    floats = np.frombuffer(raw, np.float32, 18, 4)
+    assert list(ints[0:3]) == [0, 0, 512 ** 3]          # start_index, end_index (unset), buffer_length
+    assert list(ints[3:6]) == [3, 500, 7] and list(ints[15:18]) == [512, 512, 512]
+    np.testing.assert_array_equal(floats[6:9], [3, -12, 7])
+    np.testing.assert_allclose(floats[9:12], [0.0175781, -0.0703125, 0.0410156], rtol=1e-6)
