@@ -73,7 +73,8 @@ def parse(argv=None):
     ap.add_argument("--out", type=Path, required=True)
     ap.add_argument("--frames", type=int, default=None, help="frames to fuse (default: all)")
     ap.add_argument("--seed", type=int, default=0, help="synthetic sequence seed index")
-    ap.add_argument("--corridor", action="store_true", help="synthetic corridor walk (the cyclic-volume workload)")
+    ap.add_argument("--corridor", action="store_true",
+                    help="synthetic corridor walk (the cyclic-volume workload; implied by --config c3)")
     ap.add_argument("--fx", type=float), ap.add_argument("--fy", type=float)
     ap.add_argument("--cx", type=float), ap.add_argument("--cy", type=float)
     ap.add_argument("--voxels", type=int, default=512)
@@ -94,7 +95,7 @@ def run(args) -> dict:
         cfg = synth.CONFIGS[args.config]
         n = cfg.frames if args.frames is None else args.frames
         s_scene, s_traj, s_noise = synth.seeds(args.seed)
-        if args.corridor:
+        if args.corridor or args.config == "c3":  # c3 is the corridor workload
             scene, gt = synth.make_corridor_scene(cfg, s_scene), synth.make_corridor_trajectory(cfg, s_traj, n)
         else:
             scene, gt = synth.make_scene(cfg, s_scene), synth.make_trajectory(cfg, s_traj, n)
