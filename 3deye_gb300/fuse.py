@@ -40,19 +40,26 @@ def read_depth(path: Path) -> np.ndarray:
     raw = path.read_bytes()
     fields, pos = [], 0
     while len(fields) < 4:  # magic, width, height, maxval, skipping comments
-        while raw[pos:pos + 1].isspace():
+        while pos < len(raw) and raw[pos:pos + 1].isspace():
             pos += 1
         if raw[pos:pos + 1] == b"#":
-            pos = raw.index(b"\n", pos) + 1
+            nl = raw.find(b"\n", pos)
+            if nl < 0:
+                break
+            pos = nl + 1
             continue
         end = pos
-        while not raw[end:end + 1].isspace():
+        while end < len(raw) and not raw[end:end + 1].isspace():
             end += 1
+        if end == pos or end >= len(raw):
+            break  # the header ends early
         fields.append(raw[pos:end])
         pos = end
-    if fields[0] != b"P5" or int(fields[3]) <= 255:
+    if len(fields) < 4 or fields[0] != b"P5" or not fields[3].isdigit() or int(fields[3]) <= 255:
         raise ValueError(f"{path}: not a 16-bit binary PGM")
     w, h = int(fields[1]), int(fields[2])
+    if len(raw) < pos + 1 + 2 * w * h:
+        raise ValueError(f"{path}: {w}x{h} samples do not fit in the file")
     data = np.frombuffer(raw, ">u2", w * h, pos + 1)
     return data.reshape(h, w).astype(np.uint16)
 

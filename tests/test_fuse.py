@@ -24,6 +24,11 @@ def test_pgm_depth_round_trip(tmp_path):
     (tmp_path / "d.pgm").write_bytes(b"P5\n3 2\n255\n" + bytes(6))
     with pytest.raises(ValueError):
         fuse.read_depth(tmp_path / "d.pgm")
+    # headers cut short, and too few samples, are refused (not read past the end)
+    for bad in (b"P5\n3 2", b"P5\n3", b"P5\n# comment without end", b"P5\n3 2\n65535\n" + bytes(5)):
+        (tmp_path / "e.pgm").write_bytes(bad)
+        with pytest.raises(ValueError):
+            fuse.read_depth(tmp_path / "e.pgm")
 
 
 @pytest.mark.gpu
