@@ -146,9 +146,11 @@ def read_ppm(path) -> np.ndarray:
     """Inverse of write_ppm."""
     raw = open(path, "rb").read()
     parts = raw.split(b"\n", 3)
-    if parts[0] != b"P6" or parts[2] != b"255":
-        raise ValueError("read_ppm: not a binary 8-bit PPM")
+    if len(parts) < 4 or parts[0] != b"P6" or parts[2] != b"255" or len(parts[1].split()) != 2:
+        raise ValueError("read_ppm: not a binary 8-bit PPM as write_ppm writes it")
     cols, rows = (int(v) for v in parts[1].split())
+    if len(parts[3]) < rows * cols * 3:
+        raise ValueError(f"read_ppm: {cols}x{rows} pixels do not fit in the file")
     return np.frombuffer(parts[3], np.uint8, rows * cols * 3).reshape(rows, cols, 3)
 
 

@@ -111,6 +111,10 @@ def test_ppm_known_answer_and_round_trip(tmp_path):
     np.testing.assert_array_equal(fmt.read_ppm(p), img)
     with pytest.raises(ValueError):
         fmt.write_ppm(p, np.zeros((2, 3), np.uint8))
+    for bad in (b"P6\n3 2\n", b"P6\n3 2\n255\n" + bytes(5), b"P5\n3 2\n255\n" + bytes(18)):
+        (tmp_path / "bad.ppm").write_bytes(bad)
+        with pytest.raises(ValueError):
+            fmt.read_ppm(tmp_path / "bad.ppm")
 
 
 def test_golden_slab_clouds_in_reference_text_format():
