@@ -1035,7 +1035,8 @@ int tde_pipeline_restore(tde_pipeline *p, const void *buffer, size_t bytes) {
         h.rb.voxels_size.x != mine.rb.voxels_size.x || h.rb.voxels_size.y != mine.rb.voxels_size.y ||
         h.rb.voxels_size.z != mine.rb.voxels_size.z || h.has_color != mine.has_color ||
         h.volume_bytes != mine.volume_bytes || h.negflags_bytes != mine.negflags_bytes ||
-        h.satflags_bytes != mine.satflags_bytes || h.color_bytes != mine.color_bytes || h.frames < 0)
+        h.satflags_bytes != mine.satflags_bytes || h.color_bytes != mine.color_bytes || h.frames < 0 ||
+        h.frames > 0x7fffffff)
         return set_error(TDE_ERR_INVALID_ARG,
                          "pipeline_restore: the checkpoint's format, frame size, volume size or colour volume "
                          "differs from this pipeline's");
