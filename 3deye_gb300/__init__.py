@@ -22,7 +22,7 @@ __all__ = [
     "tsdf_volume_bytes", "tsdf_init", "bilateral_filter", "depth_pyramid_level", "vertex_map", "normal_map",
     "estimate_combined", "transform_estimation", "clean_buff", "scale_depth", "integrate_tsdf", "raycast",
     "resize_vertex_map", "resize_normal_map", "transform_maps", "extract_slice", "extract_tsdf_volume",
-    "extract_color_volume", "clean_tsdf_slice", "clean_color_slice", "generate_image", "LightSource",
+    "extract_color_volume", "extract_color_slice", "clean_tsdf_slice", "clean_color_slice", "generate_image", "LightSource",
 ]
 
 
@@ -209,6 +209,27 @@ def extract_slice(volume, fmt, color, min_bounds, max_bounds, rb: RoundBuffer, c
             return pts[:k], cols[:k], (wts[:k] if wts is not None else None), n
         cap = n
     raise TdeError(-5, "extract_slice: capacity retry failed")
+
+
+def extract_color_slice(color, min_bounds, max_bounds, rb: RoundBuffer, capacity=None, stream=None):
+    """Extract_Color_Slice (opencl_wrappers.cpp:687-782): the colours of the
+    set voxels of the black zone in raster order.  Returns (colors, total
+    count); grows the output once if it was too small."""
+    torch = _torch()
+    dev = color.device
+    scratch = torch.empty(lib.tde_extract_slice_scratch_bytes(C.byref(rb)), dtype=torch.uint8, device=dev)
+    count = torch.zeros(1, dtype=torch.int32, device=dev)
+    cap = 1 << 16 if capacity is None else int(capacity)
+    for _ in range(2):
+        cols = torch.empty((max(cap, 1), 4), dtype=torch.uint8, device=dev)
+        check(lib.tde_extract_color_slice(ptr(color), Point3i(*min_bounds), Point3i(*max_bounds), C.byref(rb),
+                                          ptr(scratch), scratch.numel(), ptr(cols), cap, ptr(count),
+                                          stream_ptr(stream)))
+        n = int(count.item())
+        if n <= cap or capacity is not None:
+            return cols[:min(n, cap)], n
+        cap = n
+    raise TdeError(-5, "extract_color_slice: capacity retry failed")
 
 
 def generate_image(vmap, nmap, light_pos=(0.0, 0.0, 0.0), light_number=1, image=None, stream=None):

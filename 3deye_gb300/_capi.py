@@ -120,6 +120,7 @@ _SIGS = {
     "tde_transform_maps": (I, [P, P, P, P, pM, pV, I, I, P]),
     "tde_extract_slice_scratch_bytes": (SZ, [pRB]),
     "tde_extract_slice": (I, [P, I, P, Point3i, Point3i, pRB, P, SZ, P, P, P, U32, P, P]),
+    "tde_extract_color_slice": (I, [P, Point3i, Point3i, pRB, P, SZ, P, U32, P, P]),
     "tde_extract_tsdf_volume_scratch_bytes": (SZ, [pRB]),
     "tde_extract_tsdf_volume": (I, [P, I, pRB, Point3f, P, SZ, P, P, U32, P, P]),
     "tde_extract_color_volume": (I, [P, pRB, P, U32, Point3f, P, P]),

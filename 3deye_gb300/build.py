@@ -4,8 +4,8 @@
   ``include/tde_capi.h`` (sm_103a only), plus the C++ reference API of
   ``include/3deye/``.
 * ``oracle/liboracle.so`` -- the CPU oracle (test infrastructure).
-* ``oracle/_ref/*.so`` -- the reference kernels compiled as C, only when the
-  reference tree is present (test infrastructure).
+* ``oracle/_ref/*.so`` -- the reference kernels compiled as C, only when
+  TDE_REFERENCE names a checkout of the reference (test infrastructure).
 
 Translation units compile in parallel; each one is rebuilt only when a source
 or header it may include is newer than its object.
@@ -30,7 +30,7 @@ ORACLE_LIB = ORACLE / "liboracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Kernels whose float arithmetic must equal the CPU oracle's operation by
 # operation are compiled without FMA contraction.
-NO_FMAD = {"k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_render.cu"}
+NO_FMAD = {"k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_render.cu", "k_synth.cu"}
 CUDA_UNITS = ["capi.cu", "k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_slab.cu",
               "pipeline.cu", "k_synth.cu", "noalloc.cu", "k_refiner.cu", "refiner.cu", "k_render.cu"]
 CXX_UNITS = ["wrappers.cpp"]
@@ -105,11 +105,13 @@ def build_oracle(verbose: bool = False) -> Path:
 
 
 def build_reference_kernels(verbose: bool = False) -> None:
+    """The reference's kernels compiled as C, when TDE_REFERENCE names a
+    checkout of the reference (test infrastructure; skipped otherwise)."""
     script = ORACLE / "build_ref.sh"
-    ref = Path(os.environ.get("TDE_REFERENCE", "/root/reference"))
-    if not (ref / "GPU" / "opencl").is_dir():
+    ref = os.environ.get("TDE_REFERENCE")
+    if not ref or not (Path(ref) / "GPU" / "opencl").is_dir():
         return
-    r = subprocess.run(["bash", str(script)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    r = subprocess.run(["bash", str(script), ref], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError("reference kernel build failed:\n" + r.stdout)
     if verbose:

@@ -441,6 +441,16 @@ int tde_extract_slice(const void *volume, int format, const tde_color *color_vol
                                 points, colors, weights, capacity, count_device, 0, nullptr, as_stream(stream));
 }
 
+int tde_extract_color_slice(const tde_color *color_volume, tde_point3i min_bounds, tde_point3i max_bounds,
+                            const tde_round_buffer *rb, void *scratch, size_t scratch_bytes, tde_color *colors,
+                            uint32_t capacity, uint32_t *count_device, void *stream) {
+    TDE_REQUIRE(color_volume && scratch && count_device, "extract_color_slice: null buffer");
+    TDE_REQUIRE(colors || capacity == 0, "extract_color_slice: null colours with capacity %u", capacity);
+    TDE_REQUIRE(valid_round_buffer(rb), "extract_color_slice: bad round_buffer");
+    return launch_extract_color_slice(color_volume, min_bounds, max_bounds, *rb, scratch, scratch_bytes, colors,
+                                      capacity, count_device, as_stream(stream));
+}
+
 size_t tde_extract_tsdf_volume_scratch_bytes(const tde_round_buffer *rb) {
     if (!valid_round_buffer(rb)) return 0;
     return slab_scratch_bytes(*rb);

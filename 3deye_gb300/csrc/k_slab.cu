@@ -632,6 +632,75 @@ __global__ void gather_colors_kernel(const tde_color *__restrict__ color, const 
     out[i] = c;
 }
 
+// Extract_Color_Slice (opencl_wrappers.cpp:687-782; its kernels
+// scan_slice_of_color_volume and extract_color_slice_as_cloud are absent):
+// the colour plane alone -- voxels of the black zone whose colour is set
+// (Color_Point_Is_Set, scan_slice_of_both_volumes.cl:53-58), in (z, y, x)
+// raster order of logical voxels (the order chunking in z keeps for one
+// plane).  Tiles as above, one count per tile.
+__global__ void __launch_bounds__(kSlabThreads) color_count_kernel(const SlabParams p, uint32_t *__restrict__ counts) {
+    __shared__ unsigned s_cnt;
+    const int tile = blockIdx.x;
+    int chunk, z, y0, y1;
+    const bool live = tile_coords(p, tile, chunk, z, y0, y1);
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    unsigned c = 0;
+    if (live) {
+        const int W = p.rb.voxels_size.x, nvox = (y1 - y0) * W;
+        for (int r = threadIdx.x; r < nvox; r += kSlabThreads) {
+            const int y = y0 + r / W, x = r - (r / W) * W;
+            c += in_black_zone(x, y, z, p.mn, p.mx, p.rb) && color_set(p.color[voxel_address(x, y, z, p.rb)]);
+        }
+    }
+    #pragma unroll
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_cnt, c);
+    __syncthreads();
+    if (threadIdx.x == 0) counts[tile] = s_cnt;
+}
+
+__global__ void __launch_bounds__(kSlabThreads) color_scatter_kernel(const SlabParams p, const uint32_t *__restrict__ offs,
+                                                                    tde_color *__restrict__ cols, uint32_t capacity) {
+    __shared__ unsigned s_warp[kSlabThreads / 32];
+    __shared__ unsigned s_base;
+    const int tile = blockIdx.x;
+    int chunk, z, y0, y1;
+    if (!tile_coords(p, tile, chunk, z, y0, y1)) return;
+    const int W = p.rb.voxels_size.x, nvox = (y1 - y0) * W;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_base = offs[tile];
+    __syncthreads();
+    for (int r0 = 0; r0 < nvox; r0 += kSlabThreads) {
+        const int r = r0 + threadIdx.x;
+        bool set = false;
+        tde_color c = {0, 0, 0, 0};
+        if (r < nvox) {
+            const int y = y0 + r / W, x = r - (r / W) * W;
+            if (in_black_zone(x, y, z, p.mn, p.mx, p.rb)) {
+                c = p.color[voxel_address(x, y, z, p.rb)];
+                set = color_set(c);
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, set);
+        if (lane == 0) s_warp[warp] = __popc(m);
+        __syncthreads();
+        if (set) {
+            unsigned before = 0;
+            for (int w2 = 0; w2 < warp; ++w2) before += s_warp[w2];
+            const uint32_t slot = s_base + before + __popc(m & ((1u << lane) - 1u));
+            if (slot < capacity) cols[slot] = c;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int w2 = 0; w2 < kSlabThreads / 32; ++w2) tot += s_warp[w2];
+            s_base += tot;
+        }
+        __syncthreads();
+    }
+}
+
 void slab_geometry(const tde_round_buffer &rb, SlabParams &p) {
     const int W = rb.voxels_size.x, H = rb.voxels_size.y;
     p.ty = max(1, min(H, 8192 / max(1, W)));
@@ -727,6 +796,29 @@ int launch_extract_slice(const void *vol, int fmt, const tde_color *color, tde_p
                 <<<ntiles, kSlabThreads, 0, stream>>>(p, rg, counts, pts, cols, wts, capacity);
         return check_launch("extract_slice/scatter");
     });
+}
+
+int launch_extract_color_slice(const tde_color *color, tde_point3i mn, tde_point3i mx, const tde_round_buffer &rb,
+                               void *scratch, size_t scratch_bytes, tde_color *cols, uint32_t capacity,
+                               uint32_t *count, cudaStream_t stream) {
+    SlabParams p;
+    p.vol = nullptr; p.color = color; p.rb = rb; p.mn = mn; p.mx = mx; p.n = voxel_count(rb);
+    p.metric = 0; p.cell = tde_point3f{1.f, 1.f, 1.f}; p.gbits = nullptr;
+    // one plane: the whole depth as one chunk gives the same raster order
+    p.step = rb.voxels_size.z;
+    slab_geometry(rb, p);
+    const int ntiles = p.tiles_per_chunk;
+    if (scratch_bytes < slab_scratch_bytes(rb) || (size_t)ntiles * sizeof(uint32_t) > scratch_bytes)
+        return set_error(TDE_ERR_INVALID_ARG, "extract_color_slice: scratch %zu < %zu bytes", scratch_bytes,
+                         slab_scratch_bytes(rb));
+    uint32_t *counts = reinterpret_cast<uint32_t *>(scratch);
+    color_count_kernel<<<ntiles, kSlabThreads, 0, stream>>>(p, counts);
+    int st = check_launch("extract_color_slice/count");
+    if (st) return st;
+    exclusive_scan_kernel<<<1, 1024, 0, stream>>>(counts, ntiles, count);
+    if ((st = check_launch("extract_color_slice/scan"))) return st;
+    color_scatter_kernel<<<ntiles, kSlabThreads, 0, stream>>>(p, counts, cols, capacity);
+    return check_launch("extract_color_slice/scatter");
 }
 
 int launch_gather_colors(const tde_color *color, const tde_round_buffer &rb, const tde_xyzi *pts, uint32_t n,

@@ -1,7 +1,9 @@
 // k_synth.cu -- synthetic depth sensor: ray-casts the seeded procedural scene
 // (plane / sphere / axis-aligned box primitives) and applies the Kinect noise
 // model.  It produces benchmark and test inputs; it is not part of the
-// per-frame pipeline.
+// per-frame pipeline.  Every operation is IEEE exact or correctly rounded and
+// the unit is compiled without contraction, so its frames equal the CPU
+// sensor's bit for bit (the CPU arm of the benchmark renders the same ones).
 #include "tde_common.cuh"
 
 namespace tde {
@@ -59,6 +61,21 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
 }
 __device__ __forceinline__ float u01(uint32_t h) { return ((float)(h >> 8) + 0.5f) * (1.0f / 16777216.0f); }
 
+// Standard normal deviate as the Irwin-Hall sum of 12 uniforms minus 6 (mean
+// 0, variance 1): twelve 16-bit uniforms from six hashes; the numerator is an
+// integer below 2^19 and the scale a power of two, so the result is exact and
+// equal to the CPU sensor's.
+__device__ __forceinline__ float gauss12(uint32_t key) {
+    const uint32_t salt[6] = {0x02e5be93U, 0x967a889bU, 0x1b873593U, 0xcc9e2d51U, 0x85ebca6bU, 0xc2b2ae35U};
+    int32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const uint32_t h = hash32(key ^ salt[k]);
+        sum += (int32_t)(h & 0xFFFFu) + (int32_t)(h >> 16);
+    }
+    return (float)(sum + 6 - 6 * 65536) * (1.0f / 65536.0f);
+}
+
 struct SynthParams {
     double R[9], t[3];
     tde_intrinsics intr;
@@ -84,10 +101,9 @@ __global__ void synth_kernel(const double *__restrict__ scene, const SynthParams
     if (out_mm) {
         uint32_t key = hash32(p.seed ^ hash32(p.frame * 0x9e3779b9U ^ hash32((uint32_t)i)));
         float ud = u01(hash32(key ^ 0x68bc21ebU));
-        float u1 = u01(hash32(key ^ 0x02e5be93U)), u2 = u01(hash32(key ^ 0x967a889bU));
         uint16_t o = 0;
         if (z > 0.f && z <= p.max_range && ud >= p.dropout) {
-            float g = sqrtf(-2.f * logf(u1)) * cosf(6.2831853071795865f * u2);
+            float g = gauss12(key);
             float s = 0.0012f + 0.0019f * (z - 0.4f) * (z - 0.4f);
             float mm = nearbyintf((z + s * g) * 1000.f);
             if (mm > 0.f && mm <= p.max_range * 1000.f && mm < 65535.f) o = (uint16_t)mm;

@@ -26,25 +26,67 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
+struct ScratchSlot {
+    unsigned long long ctx_id;  // the context the address belongs to
+    void *addr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 
-// Device address of the array on the current device.  In host code the
-// array's name is only a host-side stand-in, so the address is looked up with
-// cudaGetSymbolAddress, once per device, with that device current.
+// Two driver entry points, fetched through the runtime so the library needs
+// no link against the driver library: the current context and its id, which
+// stays unique for the life of the process (a context created after
+// cudaDeviceReset gets a new one even where its handle value repeats).
+typedef int (*CtxGetCurrentFn)(void **ctx);
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+int current_context_id(unsigned long long *id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return set_error(TDE_ERR_CUDA, "integrate_noalloc: driver entry points cuCtxGetCurrent/cuCtxGetId");
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    void *ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0 || !ctx || g_ctx_get_id(ctx, id) != 0)
+        return set_error(TDE_ERR_CUDA, "integrate_noalloc: no current CUDA context");
+    return TDE_OK;
+}
+
+// Device address of the array in the current device's context.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// with cudaGetSymbolAddress, once per device and context, with that device
+// current; a later context on the device (after cudaDeviceReset) loads the
+// module again and gets its own lookup.
 int scratch_address(void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "integrate_noalloc: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return set_error(TDE_ERR_UNSUPPORTED, "integrate_noalloc: device %d", dev);
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return set_error(TDE_ERR_CUDA, "integrate_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-        g_scratch_addr[dev] = p;
+    unsigned long long id = 0;
+    void *p = nullptr;
+    if (g_scratch[dev].addr) {
+        TDE_TRY(current_context_id(&id));
+        if (g_scratch[dev].ctx_id == id) {
+            *out = g_scratch[dev].addr;
+            return TDE_OK;
+        }
     }
-    *out = g_scratch_addr[dev];
+    // set-up: also makes the device's primary context current when nothing
+    // has used the device yet
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return set_error(TDE_ERR_CUDA, "integrate_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    TDE_TRY(current_context_id(&id));
+    g_scratch[dev] = ScratchSlot{id, p};
+    *out = p;
     return TDE_OK;
 }
 

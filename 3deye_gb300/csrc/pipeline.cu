@@ -126,6 +126,7 @@ struct tde_pipeline {
     cudaGraphExec_t seg_exec[2][SEG_COUNT] = {};
     cudaGraphExec_t main_exec[2][2] = {};  // [set][first frame, tracked frame]
     bool captured = false;
+    bool inconsistent = false;  // a restore failed part-way: frames are refused
     int frames = 0;
     // timing
     int timing_cap = 0, timing_n = 0;
@@ -407,17 +408,23 @@ static int upload_camera(tde_pipeline *p, const double *pose, cudaStream_t s) {
 // Checkpoint layout: this header, then the TSDF volume, the brick flags
 // (negative ever written, per brick and super-brick), the saturation flags
 // and, with a colour volume, the colour volume.
+// The geometry fields (intrinsics, truncation, weight cap, colour weight cap)
+// are the ones the stored volume was fused with: a pipeline whose values differ
+// would read the volume at other positions or scales, so restore refuses it.
 struct CheckpointHeader {
-    char magic[8];  // "TDECKPT1"
+    char magic[8];  // "TDECKPT2"
     int32_t tsdf_format, has_color;
-    int32_t cols, rows, levels, pad;
+    int32_t cols, rows, levels, max_weight;
     int64_t frames;
     tde_round_buffer rb;
     double pose12[12];
     uint64_t volume_bytes, negflags_bytes, satflags_bytes, color_bytes;
+    tde_intrinsics intr;
+    float trunc;
+    int32_t color_max_weight;
 };
-static_assert(sizeof(CheckpointHeader) == 240, "checkpoint header layout");
-static const char kCheckpointMagic[8] = {'T', 'D', 'E', 'C', 'K', 'P', 'T', '1'};
+static_assert(sizeof(CheckpointHeader) == 272, "checkpoint header layout");
+static const char kCheckpointMagic[8] = {'T', 'D', 'E', 'C', 'K', 'P', 'T', '2'};
 
 static CheckpointHeader checkpoint_layout(const tde_pipeline *p) {
     CheckpointHeader h;
@@ -428,6 +435,10 @@ static CheckpointHeader checkpoint_layout(const tde_pipeline *p) {
     h.cols = p->cfg.intr.cols;
     h.rows = p->cfg.intr.rows;
     h.levels = p->levels;
+    h.max_weight = p->cfg.max_weight;
+    h.intr = p->cfg.intr;
+    h.trunc = p->cfg.trunc;
+    h.color_max_weight = p->colvol ? p->color_max_weight : 0;
     h.frames = p->frames;
     h.rb = p->rb;
     h.volume_bytes = tde_tsdf_volume_bytes(p->cfg.tsdf_format, &p->rb);
@@ -585,6 +596,8 @@ int tde_pipeline_enqueue_rgbd(tde_pipeline *p, const uint16_t *depth, const uint
                               double *pose_out12, int *status_out) {
     NvtxRange range("tde_pipeline_enqueue");
     if (!p || !depth) return set_error(TDE_ERR_INVALID_ARG, "pipeline_enqueue: null argument");
+    if (p->inconsistent)
+        return set_error(TDE_ERR_INVALID_ARG, "pipeline_enqueue: a restore failed part-way; restore a checkpoint first");
     if ((p->colvol != nullptr) != (rgb != nullptr))
         return set_error(TDE_ERR_INVALID_ARG, p->colvol ? "pipeline_enqueue: the colour volume needs an RGB frame"
                                                         : "pipeline_enqueue: an RGB frame needs tde_pipeline_enable_color");
@@ -1040,9 +1053,21 @@ int tde_pipeline_restore(tde_pipeline *p, const void *buffer, size_t bytes) {
         return set_error(TDE_ERR_INVALID_ARG,
                          "pipeline_restore: the checkpoint's format, frame size, volume size or colour volume "
                          "differs from this pipeline's");
+    // the metric geometry the volume was fused with: the volume edge (metres),
+    // camera, truncation and weight caps, compared bit for bit
+    if (std::memcmp(&h.rb.volume_size, &mine.rb.volume_size, sizeof(h.rb.volume_size)) != 0 ||
+        std::memcmp(&h.intr, &mine.intr, sizeof(h.intr)) != 0 ||
+        std::memcmp(&h.trunc, &mine.trunc, sizeof(h.trunc)) != 0 || h.max_weight != mine.max_weight ||
+        h.color_max_weight != mine.color_max_weight)
+        return set_error(TDE_ERR_INVALID_ARG,
+                         "pipeline_restore: the checkpoint's volume edge, intrinsics, truncation or weight cap "
+                         "differs from this pipeline's");
     const size_t need = sizeof(h) + h.volume_bytes + h.negflags_bytes + h.satflags_bytes + h.color_bytes;
     if (bytes < need) return set_error(TDE_ERR_INVALID_ARG, "pipeline_restore: %zu < %zu bytes", bytes, need);
     TDE_TRY(tde_pipeline_sync(p));
+    // from here on a failure leaves the device state half replaced: the
+    // pipeline refuses frames until a restore succeeds
+    p->inconsistent = true;
     const char *i = static_cast<const char *>(buffer) + sizeof(h);
     TDE_CUDA(cudaMemcpy(p->volume, i, h.volume_bytes, cudaMemcpyHostToDevice), "pipeline_restore: volume");
     i += h.volume_bytes;
@@ -1062,7 +1087,8 @@ int tde_pipeline_restore(tde_pipeline *p, const void *buffer, size_t bytes) {
     TDE_TRY(cast_model(p, s));
     TDE_TRY(record_segment(p, SEG_RESIZE, 0, s));
     TDE_CUDA(cudaStreamSynchronize(s), "pipeline_restore");
-    if (p->cfg.use_graphs) return capture_all(p, true);
+    if (p->cfg.use_graphs) TDE_TRY(capture_all(p, true));
+    p->inconsistent = false;
     return TDE_OK;
 }
 

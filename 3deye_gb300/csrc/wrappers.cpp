@@ -43,7 +43,7 @@ const char *const kKnown[] = {
     "resize_vertex_map", "resize_normal_map", "transform_map", "scan_slice_of_both_volumes", "extract_slice_as_cloud",
     "scan_slice_of_tsdf_volume", "extract_tsdf_slice_as_cloud", "scan_pow2", "scan_subarrays", "clean_tsdf_slice",
     "clean_color_slice", "init_tsdf", "integrate_color_volume", "scan_the_whole_array", "extract_tsdf_cloud",
-    "extract_colors", "generate_image"};
+    "extract_colors", "generate_image", "scan_slice_of_color_volume", "extract_color_slice_as_cloud"};
 
 string base_name(const string &n) {
     if (n.size() > 3 && n.compare(n.size() - 3, 3, ".cl") == 0) return n.substr(0, n.size() - 3);
@@ -418,6 +418,39 @@ void Extract_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round
                    gpu_array_base *gColor_Volume, point_3f, kernel_manager *, matrix<Point_XYZI> &Vertex_Slice,
                    matrix<Point_Color> &Color_Slice) {
     extract(Min_Bounds, Max_Bounds, Round_Buffer, gTsdf_Volume, gColor_Volume, Vertex_Slice, &Color_Slice);
+}
+
+// opencl_wrappers.cpp:687-782: count, then the colours, appended to the cloud
+void Extract_Color_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
+                         gpu_array_base *gColor_Volume, kernel_manager *, matrix<Point_Color> &cloud) {
+    const tde_round_buffer *r = RB(Round_Buffer);
+    const size_t sb = tde_extract_slice_scratch_bytes(r);
+    if (!sb) throw std::runtime_error("Extract_Color_Slice: bad round_buffer");
+    const tde_color *cv = static_cast<const tde_color *>(dev(gColor_Volume, "Extract_Color_Slice"));
+    void *scratch = nullptr, *cnt = nullptr, *cols = nullptr;
+    auto release = [&] { tde_device_free(scratch); tde_device_free(cnt); tde_device_free(cols); };
+    try {
+        check(tde_device_malloc(&scratch, sb), "Extract_Color_Slice");
+        check(tde_device_malloc(&cnt, sizeof(uint32_t)), "Extract_Color_Slice");
+        check(tde_extract_color_slice(cv, P3(Min_Bounds), P3(Max_Bounds), r, scratch, sb, nullptr, 0,
+                                      static_cast<uint32_t *>(cnt), nullptr),
+              "Extract_Color_Slice");
+        uint32_t n = 0;
+        check(tde_memcpy(&n, cnt, sizeof(n), 1), "Extract_Color_Slice");
+        if (n) {
+            check(tde_device_malloc(&cols, (size_t)n * sizeof(tde_color)), "Extract_Color_Slice");
+            check(tde_extract_color_slice(cv, P3(Min_Bounds), P3(Max_Bounds), r, scratch, sb,
+                                          static_cast<tde_color *>(cols), n, static_cast<uint32_t *>(cnt), nullptr),
+                  "Extract_Color_Slice");
+            matrix<Point_Color> part(n);
+            check(tde_memcpy(part.data, cols, (size_t)n * sizeof(tde_color), 1), "Extract_Color_Slice");
+            cloud.extend_from(part);
+        }
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
 }
 
 // opencl_wrappers.cpp:967-992: Image_Out holds cols*rows RGB8 pixels.

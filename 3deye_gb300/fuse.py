@@ -84,14 +84,24 @@ def parse(argv=None):
                     help="synthetic corridor walk (the cyclic-volume workload; implied by --config c3)")
     ap.add_argument("--fx", type=float), ap.add_argument("--fy", type=float)
     ap.add_argument("--cx", type=float), ap.add_argument("--cy", type=float)
-    ap.add_argument("--voxels", type=int, default=512)
-    ap.add_argument("--volume", type=float, default=3.0, help="volume edge (m)")
-    ap.add_argument("--format", choices=sorted(FORMATS), default="fp16")
-    ap.add_argument("--trunc", type=float, default=0.03, help="truncation distance (m)")
+    # volume settings of --depth-dir input; a --config fixes its own
+    ap.add_argument("--voxels", type=int, default=None, help="voxels per axis (default 512)")
+    ap.add_argument("--volume", type=float, default=None, help="volume edge in m (default 3.0)")
+    ap.add_argument("--format", choices=sorted(FORMATS), default=None, help="TSDF storage (default fp16)")
+    ap.add_argument("--trunc", type=float, default=None, help="truncation distance in m (default 0.03)")
     ap.add_argument("--shift-radius", type=float, default=0.4,
                     help="re-centre the volume when the point half a volume ahead leaves this radius (m); "
                          "0 disables shifts")
-    return ap.parse_args(argv)
+    args = ap.parse_args(argv)
+    fixed = [f"--{k}" for k in ("voxels", "volume", "format", "trunc", "fx", "fy", "cx", "cy")
+             if getattr(args, k) is not None]
+    if args.config and fixed:
+        ap.error(f"{', '.join(fixed)} cannot be combined with --config (the configuration fixes them)")
+    args.voxels = 512 if args.voxels is None else args.voxels
+    args.volume = 3.0 if args.volume is None else args.volume
+    args.format = "fp16" if args.format is None else args.format
+    args.trunc = 0.03 if args.trunc is None else args.trunc
+    return args
 
 
 def run(args) -> dict:

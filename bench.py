@@ -17,10 +17,13 @@ Reported (one JSON line, rank 0):
              sweep (4 B/voxel read + 4 B/voxel written for the voxels the
              update touches, counted live) and the raycast;
   cpu_baseline  the CPU oracle of the same pipeline on this host's cores;
-  learned_refine, color_volume, model_export, cyclic_volume
+  learned_refine, color_volume, model_export, cyclic_volume, config1
              the refiner in place of the bilateral filter, RGB-D frames with
-             the colour volume, the whole-model export and shading, and the
-             640x480 / 512^3 corridor with the volume following the camera.
+             the colour volume, the whole-model export and shading, the
+             640x480 / 512^3 corridor with the volume following the camera,
+             and the 100-frame 320x240 / 128^3 FP32 sequence (GPU and CPU);
+  ate_m      against the ground truth and, over the first --f64-frames
+             frames, against the full-FP64 oracle pipeline run on the host.
 N > 1 runs independent replicas (sequence seed = rank): scaling "weak".
 
 --impl reference runs the CPU implementation of the path (the oracle port:
@@ -46,6 +49,27 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "frames/s 640x480 @512³ TSDF (plain vs learned-refine, equal ATE); kernel GB/s vs HBM"
 WORKLOAD = "c2"
+WORKLOAD_DESC = "640x480 depth, 512^3 TSDF over 3 m (fp16+u16), ICP 3 levels 10/5/4"
+DATA = "synthetic (seeded procedural scene, orbit, Kinect noise; sequence seed 0 + rank)"
+
+
+def bench_config(ws: int, nframes: int) -> dict:
+    """The `config` object both arms print (the same workload, frames and seed)."""
+    return {"workload": WORKLOAD_DESC, "global_batch": 1, "frames": nframes, "sequence_seed": 0,
+            "l2": "inputs larger than L2 (512 MiB TSDF volume swept every frame)",
+            "parallelism": "replicas" if ws > 1 else "single"}
+
+
+def load_synth():
+    """synth.py (the seeded scene, trajectory and seed rules) loaded by file
+    path, so that the CPU arm never imports the package (which maps the CUDA
+    library)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("tde_synth_standalone", ROOT / "3deye_gb300" / "synth.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod  # dataclasses resolve their module by name
+    spec.loader.exec_module(mod)
+    return mod
 
 
 def parse():
@@ -57,6 +81,9 @@ def parse():
     ap.add_argument("--cpu-frames", type=int, default=40,
                     help="frames of the CPU baseline sample (about 11 s on 16 cores; capped by the sequence length)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--f64-frames", type=int, default=30,
+                    help="leading frames of the sequence the full-FP64 oracle also runs (ATE of the GPU trajectory "
+                         "against it)")
     ap.add_argument("--refiner-weights", default=str(ROOT / "3deye_gb300" / "weights" / "refiner_640x480.f32"),
                     help="trained refiner for the learned-refine line (skipped when the file is absent)")
     return ap.parse_args()
@@ -76,59 +103,105 @@ def dist_init(args):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """SM clocks and clock-event (throttle) reasons of the benchmark's GPU,
+    read through NVML (libnvidia-ml, by ctypes) in a polling thread every
+    ~0.5 ms, so that even a timed region of a few milliseconds holds samples;
+    nvidia-smi at 50 ms where NVML cannot be loaded.  `window()` brackets a
+    timed region: summary(window=True) covers only the samples inside it."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, gpu_index: int):
-        self.idx = gpu_index
-        self.proc = None
-        self.lines = []
+    def __init__(self, torch_device):
+        self.dev = torch_device
+        self.samples = []  # (perf_counter, sm_mhz, reasons mask)
+        self.max_mhz = None
+        self.windows = []
+        self._stop = threading.Event()
+        self._nvml = None
+        self._h = None
+        self.source = None
+
+    def _open_nvml(self):
+        import torch
+        nv = C.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = C.c_void_p()
+        uuid = getattr(torch.cuda.get_device_properties(self.dev), "uuid", None)
+        ok = False
+        if uuid is not None:
+            ok = nv.nvmlDeviceGetHandleByUUID(f"GPU-{uuid}".encode(), C.byref(h)) == 0
+        if not ok and nv.nvmlDeviceGetHandleByIndex_v2(self.dev.index or 0, C.byref(h)) != 0:
+            raise OSError("no NVML handle")
+        self.reason_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = C.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        self._nvml, self._h = nv, h
+
+    def _poll_nvml(self):
+        nv, h = self._nvml, self._h
+        mhz, mask = C.c_uint(), C.c_ulonglong()
+        while not self._stop.is_set():
+            if nv.nvmlDeviceGetClockInfo(h, 1, C.byref(mhz)) == 0 and self.reason_fn(h, C.byref(mask)) == 0:
+                self.samples.append((time.perf_counter(), float(mhz.value), int(mask.value)))
+            time.sleep(0.0005)
+
+    def _poll_smi(self):
+        q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active"
+        proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev.index or 0), f"--query-gpu={q}",
+                                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
+                                stderr=subprocess.DEVNULL, text=True)
+        self._proc = proc
+        for line in proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            try:
+                self.samples.append((time.perf_counter(), float(f[0]), int(f[2], 16)))
+                self.max_mhz = float(f[1])
+            except (ValueError, IndexError):
+                continue
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
-                                         stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except OSError:
-            self.proc = None
+            self._open_nvml()
+            self.source = "nvml"
+            target = self._poll_nvml
+        except (OSError, AttributeError):
+            self.source = "nvidia-smi"
+            target = self._poll_smi
+        self._thread = threading.Thread(target=target, daemon=True)
+        self._thread.start()
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
     def __exit__(self, *exc):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+        self._stop.set()
+        if getattr(self, "_proc", None):
+            self._proc.terminate()
+        self._thread.join(timeout=5)
 
-    def summary(self):
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
-            f = [x.strip() for x in l.split(",")]
-            if len(f) < 8:
-                continue
-            try:
-                sm.append(float(f[0]))
-                smax.append(float(f[1]))
-            except ValueError:
-                continue
-            for n, v in zip(names, f[4:8]):
-                if v.lower().startswith("active"):
-                    reasons.add(n)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+    def window(self):
+        sampler = self
+
+        class _W:
+            def __enter__(self):
+                self.t0 = time.perf_counter()
+                return self
+
+            def __exit__(self, *exc):
+                sampler.windows.append((self.t0, time.perf_counter()))
+        return _W()
+
+    def summary(self, window=True):
+        pts = list(self.samples)
+        if window and self.windows:
+            pts = [p for p in pts if any(a <= p[0] <= b for a, b in self.windows)]
+        if not pts:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0, "source": self.source}
+        reasons = sorted({name for _, _, m in pts for bit, name in self.REASONS.items() if m & bit})
+        return {"sm_mhz": statistics.median(p[1] for p in pts), "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(pts), "source": self.source}
 
 
 def load_peaks():
@@ -197,18 +270,57 @@ def max_over_ranks(ws, x):
     return float(t.item())
 
 
-def cpu_baseline_run(cfg, frames_np, traj, nframes):
-    """Oracle pipeline on the host's cores over the first frames."""
+def cpu_baseline_run(cfg, frames_np, traj, nframes, threads=None):
+    """Oracle pipeline on the host's cores (or `threads` of them) over the
+    first frames; frame 0 (model initialisation) is untimed."""
     from oracle import oracle as orc
     from oracle.pipeline import OraclePipeline
-    cores = orc.set_threads(os.cpu_count() or 1)
+    cores = orc.set_threads(threads or os.cpu_count() or 1)
     op = OraclePipeline(cfg, traj[0])
-    op.process(frames_np[0])  # model initialisation, untimed
+    op.process(frames_np[0])
     t0 = time.perf_counter()
     for i in range(1, nframes + 1):
         op.process(frames_np[i])
     dt = time.perf_counter() - t0
+    orc.set_threads(os.cpu_count() or 1)
     return nframes / dt, cores, dt
+
+
+def fp64_oracle_poses(cfg, frames_np, traj):
+    """Poses of the full-FP64 oracle pipeline (FP64 TSDF, integration,
+    raycast, ICP terms and solve) on the given frames, all host cores."""
+    from oracle import oracle as orc
+    from oracle.pipeline import OraclePipelineF64
+    orc.set_threads(os.cpu_count() or 1)
+    op = OraclePipelineF64(cfg, traj[0])
+    poses = [op.process(f) for f in frames_np]
+    return __import__("numpy").array(poses), int(sum(op.lost))
+
+
+def cpu_legs(cfg, frames, traj, n_all, n_one, n_f64, label):
+    """The CPU side of one workload, on rank 0: the oracle pipeline timed on
+    every host core and on one core, and the FP64 oracle's poses of the first
+    n_f64 frames (for the GPU trajectory's ATE against it)."""
+    fnp = frames[: max(n_all, n_one, n_f64 - 1) + 1].cpu().numpy()
+    v, cores, dt = cpu_baseline_run(cfg, fnp, traj, n_all)
+    v1, _, dt1 = cpu_baseline_run(cfg, fnp, traj, n_one, threads=1)
+    t0 = time.perf_counter()
+    f64, f64_lost = fp64_oracle_poses(cfg, fnp[:n_f64], traj)
+    cpu = {"value": round(v, 4), "unit": "frames/s", "cores": cores, "kind": "port",
+           "sample": f"frames 1-{n_all} of the same sequence through the CPU oracle pipeline ({label}, {cores} "
+                     f"OpenMP threads, {dt:.1f} s)",
+           "one_core": {"value": round(v1, 4), "unit": "frames/s", "cores": 1,
+                        "sample": f"frames 1-{n_one}, 1 thread, {dt1:.1f} s"}}
+    return cpu, {"poses": f64, "lost": f64_lost, "frames": n_f64, "s": time.perf_counter() - t0}
+
+
+def ate_vs_fp64(pl, est, f64):
+    if not f64:
+        return {}
+    m = f64["frames"]
+    return {"vs_fp64_oracle": round(pl.ate_rmse(est[:m], f64["poses"]), 9),
+            "vs_fp64_oracle_frames": f"0-{m - 1} (the full-FP64 oracle pipeline on the same frames, "
+                                     f"{f64['s']:.1f} s on the host; tracking lost there on {f64['lost']} frames)"}
 
 
 def model_export(tde, torch, cp, cfg, dev, reps=5):
@@ -330,6 +442,46 @@ def cyclic_run(tde, syn, pl, torch, dev, rank):
                     "re-casts the model and updates the frame graphs; wall clock"}
 
 
+def config1_run(tde, syn, pl, torch, dev, rank, ws, with_cpu):
+    """The small configuration (100 frames of 320x240, 128^3 FP32 over 2 m,
+    ICP 10/5/4): GPU frames/s over frames 10-99 resident in HBM, the
+    trajectory's ATE against the ground truth and against the full-FP64
+    oracle over all 100 frames, and the CPU oracle pipeline on every host core
+    and on one core."""
+    cfg = syn.CONFIGS["c1"]
+    n, W = cfg.frames, 10
+    frames, traj, _ = make_frames(tde, syn, cfg, n, rank, dev)
+    cpu, f64 = (None, None)
+    if with_cpu:
+        cpu, f64 = cpu_legs(cfg, frames, traj, n - 1, 10, n, "320x240, 128^3 FP32")
+    p = pl.Pipeline(cfg, traj[0], use_graphs=True)
+    poses = torch.zeros((n, 12), dtype=torch.float64, pin_memory=True)
+    stat = torch.zeros(n, dtype=torch.int32, pin_memory=True)
+    base, fb = frames.data_ptr(), cfg.rows * cfg.cols * 2
+    for i in range(W):
+        p.enqueue(base + i * fb, True, poses[i].data_ptr(), stat[i].data_ptr())
+    p.sync()
+    st = torch.cuda.ExternalStream(p.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier_sync(ws)
+    e0.record(st)
+    for i in range(W, n):
+        p.enqueue(base + i * fb, True, poses[i].data_ptr(), stat[i].data_ptr())
+    e1.record(st)
+    p.sync()
+    ms = max_over_ranks(ws, e0.elapsed_time(e1))
+    p.close()
+    est = poses.numpy().copy()
+    out = {"workload": "320x240 depth, 128^3 TSDF over 2 m (fp32+u16), ICP 3 levels 10/5/4, 100 frames",
+           "value": round(ws * (n - W) / (ms * 1e-3), 2), "unit": "frames/s", "timed_frames": f"{W}-{n - 1}",
+           "ms_per_step": round(ms / (n - W), 5),
+           "ate_m": {"vs_ground_truth": round(pl.ate_rmse(est, traj), 6),
+                     "frames_tracking_lost": int((stat.numpy() != 0).sum()), **ate_vs_fp64(pl, est, f64)},
+           "cpu_baseline": cpu}
+    del frames
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -343,15 +495,11 @@ def run_ours(args, ws, rank, local):
     n = W + K
     frames, traj, _ = make_frames(tde, syn, cfg, n, rank, dev)
 
-    # CPU baseline (rank 0, N = 1 only), before the timed GPU passes
-    cpu = None
+    # CPU baseline and FP64 oracle poses (rank 0, N = 1 only), before the timed GPU passes
+    cpu, f64 = None, None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu_n = max(1, min(args.cpu_frames, n - 1))
-        fnp = frames[: cpu_n + 1].cpu().numpy()
-        v, cores, dt = cpu_baseline_run(cfg, fnp, traj, cpu_n)
-        cpu = {"value": round(v, 4), "unit": "frames/s", "cores": cores, "kind": "port",
-               "sample": f"frames 1-{cpu_n} of the same sequence through the CPU oracle pipeline "
-                         f"(640x480, 512^3, {cores} OpenMP threads, {dt:.1f} s)"}
+        cpu, f64 = cpu_legs(cfg, frames, traj, max(1, min(args.cpu_frames, n - 1)), min(3, n - 1),
+                            min(args.f64_frames, n), "640x480, 512^3")
 
     # ---- pass A: frames resident in HBM -----------------------------------
     # (each frame's preprocessing overlaps the previous frame's tracking on a
@@ -367,7 +515,9 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.ExternalStream(p.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier_sync(ws)
-    with ClockSampler(local) as clk:
+    clk = ClockSampler(dev).__enter__()  # runs through every GPU pass below
+    time.sleep(0.05)
+    with clk.window():
         e0.record(stream)
         for i in range(W, n):
             p.enqueue(base + i * fbytes, True)
@@ -455,6 +605,7 @@ def run_ours(args, ws, rank, local):
     export = model_export(tde, torch, cp, cfg, dev)
     cp.close()
     cyclic = cyclic_run(tde, syn, pl, torch, dev, rank)
+    config1 = config1_run(tde, syn, pl, torch, dev, rank, ws, rank == 0 and ws == 1 and not args.no_cpu_baseline)
     del rgb_frames
     color = {"value": round(ws * K / (c_ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(c_ms / K, 5),
              "gpu_launches": c_launches * K, "same_trajectory_as_plain": bool(np.array_equal(pose_c, pose_a)),
@@ -498,6 +649,7 @@ def run_ours(args, ws, rank, local):
                    "note": "bf16 U-Net (tcgen05 implicit-GEMM convolutions) replaces the bilateral filter; "
                            "frames resident in HBM, same sequence as the plain line"}
 
+    clk.__exit__(None, None, None)
     if rank != 0:
         return None
     hbm, peak_kind = load_peaks()
@@ -525,11 +677,8 @@ def run_ours(args, ws, rank, local):
     line = {
         "metric": METRIC, "value": round(fps, 2), "unit": "frames/s", "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": round(ms / K, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (TSDF stored f16+u16)", "data": "synthetic (seeded procedural scene, orbit, Kinect noise)",
-        "config": {"workload": "640x480 depth, 512^3 TSDF over 3 m (fp16+u16), ICP 3 levels 10/5/4, "
-                               f"frames {W}+{K} of one sequence", "global_batch": 1, "frames": n,
-                   "l2": "inputs larger than L2 (512 MiB TSDF volume swept every frame)",
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "dtype": "f32 (TSDF stored f16+u16)", "data": DATA,
+        "config": bench_config(ws, n),
         "e2e": {"value": round(ws * K / (e2e_ms * 1e-3), 2), "unit": "frames/s", "h2d_bytes_per_step": fbytes,
                 "d2h_bytes_per_step": 96 + 4},
         "roofline": {"kernel": "icp_step_kernel (dominant: largest share of the frame)", "bound": "hbm",
@@ -557,40 +706,47 @@ def run_ours(args, ws, rank, local):
         "stages_note": "stage times from a serial replay with per-stage events; the headline overlaps each "
                        "frame's preprocessing with the previous frame's tracking and fusion",
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
+        "clocks": {**clk.summary(window=True),
+                   "all_gpu_passes": clk.summary(window=False),
+                   "note": "sampled inside the headline's timed region (window), and over every GPU pass of the run"},
         "gpu_launches": launches * K,
-        "ate_m": {"vs_ground_truth": round(ate, 6), "frames_tracking_lost": lost, "deterministic": deterministic},
+        "ate_m": {"vs_ground_truth": round(ate, 6), "frames_tracking_lost": lost, "deterministic": deterministic,
+                  **ate_vs_fp64(pl, est, f64)},
         "learned_refine": learned,
         "color_volume": color,
         "model_export": export,
         "cyclic_volume": cyclic,
+        "config1": config1,
     }
     return line
 
 
 def run_reference(args, ws, rank, local):
-    """CPU implementation of the path on the host cores (rank 0 only)."""
+    """CPU implementation of the path on the host cores (rank 0 only): the
+    oracle pipeline over the same sequence as the GPU arm (the CPU sensor
+    renders the GPU sensor's frames bit for bit), W warm-up frames, then K
+    timed frames or as many as fit the time budget.  Imports neither the
+    package nor its CUDA library."""
     if rank != 0:
         return None
-    import numpy as np
-    syn = importlib.import_module("3deye_gb300.synth")
+    syn = load_synth()
     from oracle import oracle as orc
     from oracle.pipeline import OraclePipeline
     cfg = syn.CONFIGS[WORKLOAD]
     cores = orc.set_threads(os.cpu_count() or 1)
     W, K = args.warmup, args.steps
+    n = W + K
     s_scene, s_traj, s_noise = syn.seeds(0)
     scene = syn.make_scene(cfg, s_scene)
     budget_s = float(os.environ.get("TDE_REF_BUDGET_S", "150"))
     intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
-    traj = syn.make_trajectory(cfg, s_traj, W + K)
+    traj = syn.make_trajectory(cfg, s_traj, n)
     frames = lambda i: orc.apply_noise(orc.render_depth(scene, traj[i], intr), s_noise, i)
     op = OraclePipeline(cfg, traj[0])
-    warm = min(W, 2)
-    for i in range(warm):
+    for i in range(W):
         op.process(frames(i))
     done, t_total = 0, 0.0
-    for i in range(warm, warm + K):
+    for i in range(W, n):
         d = frames(i)
         t0 = time.perf_counter()
         op.process(d)
@@ -599,14 +755,13 @@ def run_reference(args, ws, rank, local):
         if t_total > budget_s:
             break
     fps = done / t_total
-    sample = (f"{done} of {K} frames (after {warm} warm-up) of the 640x480 / 512^3 sequence through the CPU oracle "
-              f"pipeline, {cores} OpenMP threads, {t_total:.1f} s; the reference's OpenCL kernels need a CPU OpenCL "
-              "runtime absent from this host")
+    sample = (f"frames {W}-{W + done - 1} ({done} of the {K} timed frames, after {W} warm-up) of the 640x480 / 512^3 "
+              f"sequence through the CPU oracle pipeline, {cores} OpenMP threads, {t_total:.1f} s; the reference's "
+              "OpenCL kernels need a CPU OpenCL runtime absent from this host")
     return {"metric": METRIC, "value": round(fps, 4), "unit": "frames/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": round(1e3 * t_total / done, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, orbit, Kinect noise)",
-            "config": {"workload": "640x480 depth, 512^3 TSDF over 3 m (fp16+u16), ICP 3 levels 10/5/4",
-                       "global_batch": 1, "parallelism": "cpu"},
+            "vs_baseline": None, "dtype": "f32 (TSDF stored f16+u16)", "data": DATA,
+            "config": bench_config(ws, n),
             "impl": "reference",
             "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": cores, "kind": "port",
                              "sample": sample},

@@ -9,10 +9,10 @@
  * the host on return.  `opencl_kernel *` / `kernel_manager *` arguments are
  * accepted and not needed.  Failures throw std::runtime_error.
  *
- * Stages whose kernels the reference does not ship either follow the
- * KinectFusion method (documented in tde_capi.h: colour integration among
- * them) or, outside this path (whole-volume export, shading, RGBD odometry),
- * throw std::runtime_error("... not available").
+ * Stages whose kernels the reference does not ship follow the KinectFusion
+ * method or the reference wrapper's own shape, documented per function in
+ * tde_capi.h (colour integration, whole-volume export, colour lookup and
+ * colour-slab extraction, shading among them).
  */
 #ifndef TDE_3DEYE_OPENCL_WRAPPERS_H
 #define TDE_3DEYE_OPENCL_WRAPPERS_H
@@ -87,6 +87,12 @@ void Extract_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *
 void Extract_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer, gpu_array_base *gTsdf_Volume,
                    gpu_array_base *gColor_Volume, point_3f Cell_Size, kernel_manager *Gpu_Methods,
                    matrix<Point_XYZI> &Vertex_Slice, matrix<Point_Color> &Color_Slice);
+
+/* opencl_wrappers.cpp:687-782: appends the colours of the set voxels of the
+ * black zone to Resulting_Cloud_Parallel (tde_extract_color_slice). */
+void Extract_Color_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
+                         gpu_array_base *gColor_Volume, kernel_manager *Gpu_Methods,
+                         matrix<Point_Color> &Resulting_Cloud_Parallel);
 
 void Clean_Tsdf_Slice(point_3i Min_Bounds, point_3i Max_Bounds, round_buffer *Round_Buffer,
                       gpu_array_base *gTsdf_Volume, opencl_kernel *clean_tsdf_kernel);

@@ -236,6 +236,8 @@ int tde_integrate_tsdf_ex(const float *depth_scaled, void *volume, int format, f
  * configuration needing more scratch is rejected with TDE_ERR_CAPACITY.
  * The first call on a device looks up the array's device address there
  * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is kept per device and CUDA context: after cudaDeviceReset the
+ * next call looks it up again in the new context (again outside capture).
  * All calls share the one array: calls whose GPU work overlaps (other
  * streams, other threads) race on it and must be serialised by the caller. */
 size_t tde_integrate_tsdf_noalloc_max_scratch_bytes(void);
@@ -324,6 +326,20 @@ int tde_extract_slice(const void *volume, int format, const tde_color *color_vol
                       tde_point3i min_bounds, tde_point3i max_bounds, const tde_round_buffer *rb,
                       void *scratch, size_t scratch_bytes, tde_xyzi *points, tde_color *colors,
                       float *weights, uint32_t capacity, uint32_t *count_device, void *stream);
+
+/* Extract_Color_Slice: opencl_wrappers.cpp:687-782 (declared at
+ * opencl_wrappers.h:149-156 and :193-199); its kernels
+ * scan_slice_of_color_volume and extract_color_slice_as_cloud are not in the
+ * reference's sources.  The colour plane of Extract_Slice on its own: every
+ * voxel of the black zone whose colour is set (any of r, g, b, w non-zero,
+ * Color_Point_Is_Set, scan_slice_of_both_volumes.cl:53-58) gives its colour,
+ * in (z, y, x) raster order of logical voxels -- the order the reference's z
+ * chunks of determine_extract_step(depth, divisor 2) give for a single plane.
+ * Scratch: tde_extract_slice_scratch_bytes().  The count goes to
+ * *count_device; colours past `capacity` are not written. */
+int tde_extract_color_slice(const tde_color *color_volume, tde_point3i min_bounds, tde_point3i max_bounds,
+                            const tde_round_buffer *rb, void *scratch, size_t scratch_bytes, tde_color *colors,
+                            uint32_t capacity, uint32_t *count_device, void *stream);
 
 /* Scratch bytes tde_extract_tsdf_volume needs (the same as the slab's). */
 size_t tde_extract_tsdf_volume_scratch_bytes(const tde_round_buffer *rb);

@@ -163,13 +163,18 @@ int tde_pipeline_render(tde_pipeline *p, const tde_light_source *light, uint8_t 
 
 /* Checkpoint / resume.  A checkpoint holds what the next frame depends on:
  * the TSDF volume, the per-brick flags, the round buffer, the FP64 pose,
- * the frame count and, with one, the colour volume (a 240-byte header, then
- * those buffers).  tde_pipeline_restore loads one into a pipeline created
- * with the same configuration (and tde_pipeline_enable_color when the
- * checkpoint has colour), casts the model maps again from the restored
- * volume and pose, and the frames that follow produce the same bits as
- * they would have after the checkpointed frame.  Both are host-synchronous;
- * `buffer` is host memory of tde_pipeline_checkpoint_bytes bytes. */
+ * the frame count and, with one, the colour volume (a 272-byte header that
+ * also records the intrinsics, volume edge, truncation and weight caps the
+ * volume was fused with, then those buffers).  tde_pipeline_restore loads one
+ * into a pipeline created with the same configuration (and
+ * tde_pipeline_enable_color with the same weight cap when the checkpoint has
+ * colour) and refuses any other (TDE_ERR_INVALID_ARG, nothing changed); it
+ * casts the model maps again from the restored volume and pose, and the
+ * frames that follow produce the same bits as they would have after the
+ * checkpointed frame.  If a restore fails after its checks (a device copy
+ * failed), the pipeline holds a mix of old and new state and refuses frames
+ * until a later restore succeeds.  Both are host-synchronous; `buffer` is
+ * host memory of tde_pipeline_checkpoint_bytes bytes. */
 size_t tde_pipeline_checkpoint_bytes(tde_pipeline *p);
 int tde_pipeline_checkpoint(tde_pipeline *p, void *buffer, size_t bytes);
 int tde_pipeline_restore(tde_pipeline *p, const void *buffer, size_t bytes);

@@ -1,18 +1,19 @@
 #!/usr/bin/env bash
 # Compile the reference's OpenCL kernels as C (test infrastructure only).
 #
-# Reads the read-only reference tree (default /root/reference, or $TDE_REFERENCE)
-# and writes one shared object per kernel into oracle/_ref/.  Nothing is copied
-# out of the reference tree: gcc reads the .cl files where they lie.  The
-# outputs are git-ignored.  Exit status 0 with a message when the reference is
-# absent (the GPU machine has no reference tree; tests there use committed golden
-# vectors instead).
+# Usage: TDE_REFERENCE=<reference checkout> bash oracle/build_ref.sh
+#    or: bash oracle/build_ref.sh <reference checkout>
+# Reads the read-only reference tree and writes one shared object per kernel
+# into oracle/_ref/.  Nothing is copied out of the reference tree: gcc reads
+# the .cl files where they lie.  The outputs are git-ignored.  Exit status 0
+# with a message when no reference tree is given or found (machines without
+# one run the tests on the committed golden vectors instead).
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${TDE_REFERENCE:-/root/reference}"
+REF="${1:-${TDE_REFERENCE:-}}"
 OUT="$HERE/_ref"
-if [ ! -d "$REF/GPU/opencl" ]; then
-    echo "build_ref: reference tree not found at $REF; skipping" >&2
+if [ -z "$REF" ] || [ ! -d "$REF/GPU/opencl" ]; then
+    echo "build_ref: no reference tree (set TDE_REFERENCE or pass its path); skipping" >&2
     exit 0
 fi
 mkdir -p "$OUT"

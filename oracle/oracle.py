@@ -228,6 +228,34 @@ def extract_slice(vol, fmt, color, mn, mx, rb, capacity=None, weights=False):
     return pts[:k], cols[:k], (wts[:k] if weights else None), n
 
 
+def voxel_addresses(rb, x, y, z):
+    """calculate_address (scan_slice_of_both_volumes.cl:17-35): physical index
+    of logical voxels, the start_index shift with its `>` wrap test."""
+    N = [int(v) for v in rb.voxels_size]
+    o = [int(v) for v in rb.origin_GRID]
+    px, py, pz = ((np.asarray(c, np.int64) + o[k]) % N[k] for k, c in enumerate((x, y, z)))
+    a = N[0] * N[1] * pz + N[0] * py + px + int(rb.start_index)
+    L = int(rb.buffer_length)
+    return np.where(a > L, a % L, a)
+
+
+def extract_color_slice(color, mn, mx, rb):
+    """Extract_Color_Slice (common/src/opencl_wrappers.cpp:687-782; its scan
+    and extract kernels are absent): for logical voxels in (z, y, x) raster
+    order -- what the wrapper's z chunks of determine_extract_step(depth, 2)
+    give for one plane -- those in the black zone
+    (check_whether_it_within_the_black_zone, scan_slice_of_both_volumes.cl:63-74)
+    whose colour is set (Color_Point_Is_Set, :53-58) contribute their colour."""
+    W, H, D = (int(v) for v in rb.voxels_size)
+    z, y, x = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
+    o = [int(v) for v in rb.origin_GRID]
+    zone = (((x + o[0] >= mn[0]) & (x + o[0] <= mx[0])) | ((y + o[1] >= mn[1]) & (y + o[1] <= mx[1])) |
+            ((z + o[2] >= mn[2]) & (z + o[2] <= mx[2])))
+    c = np.asarray(color, np.uint8).reshape(-1, 4)[voxel_addresses(rb, x, y, z).ravel()]
+    keep = zone.ravel() & (c != 0).any(axis=1)
+    return np.ascontiguousarray(c[keep])
+
+
 def extract_tsdf_volume(vol, fmt, rb, cell, capacity=None, weights=False):
     """Extract_Tsdf_Volume (common/src/opencl_wrappers.cpp:440-543): the slab
     scan with every voxel in the zone, no colour plane, z chunks of

@@ -1,8 +1,9 @@
 /*
  * oracle_scene.c -- CPU renderer of the seeded procedural scenes and the
  * Kinect-style depth noise model.  TEST INFRASTRUCTURE ONLY (synthetic
- * sensor for CPU tests; the GPU sensor in 3deye_gb300/csrc/k_synth.cu uses
- * the same scene encoding, counter-based hash and noise model).
+ * sensor for CPU tests and the CPU baseline; the GPU sensor in
+ * 3deye_gb300/csrc/k_synth.cu uses the same scene encoding, counter-based
+ * hash and noise model, operation for operation, and renders the same bits).
  *
  * Scene: nprim primitives of 8 doubles each, [type, a0..a6]:
  *   type 0  plane   n . p + d = 0          a = (nx, ny, nz, d)
@@ -86,19 +87,34 @@ static uint32_t hash32(uint32_t x) {
 }
 static float u01(uint32_t h) { return ((float)(h >> 8) + 0.5f) * (1.0f / 16777216.0f); }
 
+/* Standard normal deviate as the Irwin-Hall sum of 12 uniforms minus 6
+ * (mean 0, variance 1, support [-6, 6]): twelve 16-bit uniforms u_k from six
+ * hashes, U_k = (u_k + 1/2) / 2^16, g = (sum u_k + 6 - 6 * 2^16) / 2^16.  The
+ * numerator is an integer below 2^19 and the scale a power of two, so g is
+ * exact in float and the GPU sensor (k_synth.cu) produces the same bits. */
+static float gauss12(uint32_t key) {
+    static const uint32_t salt[6] = {0x02e5be93U, 0x967a889bU, 0x1b873593U, 0xcc9e2d51U, 0x85ebca6bU, 0xc2b2ae35U};
+    int32_t sum = 0;
+    for (int k = 0; k < 6; ++k) {
+        uint32_t h = hash32(key ^ salt[k]);
+        sum += (int32_t)(h & 0xFFFFu) + (int32_t)(h >> 16);
+    }
+    return (float)(sum + 6 - 6 * 65536) * (1.0f / 65536.0f);
+}
+
 /* Kinect noise: axial sigma = 0.0012 + 0.0019 (z - 0.4)^2 m (Nguyen et al.
  * 2012), 1 mm quantisation, `dropout` fraction of holes, invalid beyond
- * max_range.  Gaussian by Box-Muller on two hashed uniforms. */
+ * max_range.  Every operation is exact or correctly rounded, in the same
+ * order as the GPU sensor (compiled without contraction there and here). */
 int or_apply_noise(const float *depth_m, uint16_t *depth_mm, int W, int H, uint32_t seed, uint32_t frame,
                    float max_range, float dropout) {
     for (int i = 0; i < W * H; ++i) {
         float z = depth_m[i];
         uint32_t key = hash32(seed ^ hash32(frame * 0x9e3779b9U ^ hash32((uint32_t)i)));
         float ud = u01(hash32(key ^ 0x68bc21ebU));
-        float u1 = u01(hash32(key ^ 0x02e5be93U)), u2 = u01(hash32(key ^ 0x967a889bU));
         uint16_t out = 0;
         if (z > 0.f && z <= max_range && ud >= dropout) {
-            float g = sqrtf(-2.f * logf(u1)) * cosf(6.2831853071795865f * u2);
+            float g = gauss12(key);
             float s = 0.0012f + 0.0019f * (z - 0.4f) * (z - 0.4f);
             float zn = z + s * g;
             float mm = nearbyintf(zn * 1000.f);

@@ -2,7 +2,7 @@
 // and friends), built only with -I include/3deye and linked to
 // lib3deye_gb300.so.  Reads a depth frame and a pose from argv[1]/input.bin,
 // runs Integrate_Tsdf_Data -> Raycast -> Resize maps -> Extract_Slice ->
-// Extract_Tsdf_Volume -> Extract_Color_Volume -> Generate_Image ->
+// Extract_Tsdf_Volume -> Extract_Color_Volume -> Extract_Color_Slice -> Generate_Image ->
 // Clean_Tsdf_Slice -> Estimate_Combined, and writes every result to
 // argv[1]/output.bin for the Python test to compare with the CPU oracle.
 #include <cstdio>
@@ -43,7 +43,8 @@ int main(int argc, char **argv) {
                             "resize_normal_map.cl", "estimate_combined.cl", "transform_estimation.cl",
                             "compute_bilateral_filtering.cl", "compute_vertex_map.cl", "compute_normal_map_eigen.cl",
                             "clean_tsdf_slice.cl", "scan_the_whole_array.cl", "extract_tsdf_cloud.cl",
-                            "extract_colors.cl", "generate_image.cl"};
+                            "extract_colors.cl", "generate_image.cl", "scan_slice_of_color_volume.cl",
+                            "extract_color_slice_as_cloud.cl"};
     kernel_manager gm("ignored/path", names);
     bool threw = false;
     try { gm.Get_Kernel("no_such_kernel.cl"); } catch (const std::exception &) { threw = true; }
@@ -115,6 +116,10 @@ int main(int argc, char **argv) {
     gpu_array<Point_Color> gcol(hcol.data(), dim3((unsigned)nvox), TO_GPU);
     matrix<Point_Color> wcols(whole.Get_Num_Of_Elem());
     Extract_Color_Volume(&gcol, &rb, whole, cell, gm.Get_Kernel("extract_colors"), wcols);
+    // colour slab of the same bounds, appended to a cloud that holds one entry
+    matrix<Point_Color> cslab(1);
+    cslab.data[0].data.r = 1; cslab.data[0].data.g = 2; cslab.data[0].data.b = 3; cslab.data[0].data.w = 4;
+    Extract_Color_Slice(mn, mx, &rb, &gcol, &gm, cslab);
     light_source light;
     light.pos = t;
     light.number = 1;
@@ -153,6 +158,9 @@ int main(int argc, char **argv) {
     if (nw) wr(out, (const float *)whole.data, (size_t)nw * 4);
     if (nw) wr(out, (const unsigned char *)wcols.data, (size_t)nw * 4);
     wr(out, himg.data(), himg.size());
+    unsigned nc_slab = cslab.Get_Num_Of_Elem();
+    wr(out, &nc_slab, 1);
+    wr(out, (const unsigned char *)cslab.data, (size_t)nc_slab * 4);
     fclose(out);
     printf("ok points=%u\n", n);
     return 0;

@@ -1,7 +1,8 @@
 """Generate the golden vectors under tests/golden/ from the reference's own
 OpenCL kernels compiled as C (oracle/_ref, built by oracle/build_ref.sh from
-the reference tree).  Run here, where the reference tree exists:
+a checkout of the reference).  Run where a reference checkout exists:
 
+    TDE_REFERENCE=<reference checkout> bash oracle/build_ref.sh
     python tests/golden/make_golden.py
 
 Inputs are seeded; every fixture stores its inputs and the reference outputs.
@@ -250,7 +251,7 @@ def gen_text_fixtures():
 
 def main():
     if not orc.ref_available():
-        sys.exit("oracle/_ref is not built: run oracle/build_ref.sh (needs the reference tree)")
+        sys.exit("oracle/_ref is not built: run TDE_REFERENCE=<reference checkout> bash oracle/build_ref.sh")
     print("raycast hits", gen_raycast())
     gen_bilateral()
     gen_transform_map()

@@ -73,6 +73,8 @@ def test_cxx_api_roundtrip_matches_oracle(cuda, orc, tmp_path, fmt):
     whole = take(np.float32, 4 * nw).reshape(nw, 4)
     wcols = take(np.uint8, 4 * nw).reshape(nw, 4)
     img = take(np.uint8, W * H * 3).reshape(H, W, 3)
+    ncs = int(take(np.uint32, 1)[0])
+    cslab = take(np.uint8, 4 * ncs).reshape(ncs, 4)
 
     # oracle
     R = traj[0, :9].reshape(3, 3).astype(np.float32)
@@ -92,6 +94,10 @@ def test_cxx_api_roundtrip_matches_oracle(cuda, orc, tmp_path, fmt):
     colour = np.stack([(i * 7) % 256, (i * 13) % 256, (i * 29) % 256, np.where(i % 5 == 0, 0, 200)],
                       axis=1).astype(np.uint8)
     assert np.array_equal(wcols, orc.extract_color_volume(colour, rb, wo, cell))
+    # Extract_Color_Slice appends to the caller's one-entry cloud
+    cso = orc.extract_color_slice(colour, bounds[:3], bounds[3:], rb)
+    assert ncs == 1 + len(cso) and len(cso) > 100
+    assert np.array_equal(cslab[0], [1, 2, 3, 4]) and np.array_equal(cslab[1:], cso)
     assert np.array_equal(img, orc.generate_image(vmo, nmo, t))
     orc.clean_tsdf_slice(vol, fmt, bounds[:3], bounds[3:], rb)
     assert np.array_equal(vol_after, vol)

@@ -60,3 +60,15 @@ def test_fuse_synthetic_and_depth_dir(tmp_path, cuda, orc):
                               "--format", "int16", "--out", str(out2), "--shift-radius", "0"]))
     assert s2["frames"] == 6 and s2["model_points"] > 100
     assert len(fmt.read_trajectory(out2 / "trajectory.txt")) == 6
+
+
+def test_config_refuses_volume_overrides(capsys):
+    """A synthetic --config fixes its own volume and camera: explicit volume or
+    camera options beside it are an error, not silently ignored."""
+    for extra in (["--voxels", "256"], ["--volume", "4"], ["--format", "int16"], ["--trunc", "0.05"],
+                  ["--fx", "500"]):
+        with pytest.raises(SystemExit):
+            fuse.parse(["--config", "c2", "--out", "x", *extra])
+        assert "cannot be combined with --config" in capsys.readouterr().err
+    a = fuse.parse(["--config", "c2", "--out", "x"])
+    assert (a.voxels, a.volume, a.format, a.trunc) == (512, 3.0, "fp16", 0.03)

@@ -340,6 +340,25 @@ def test_extract_scalar_path_matches_golden_and_oracle(tde, orc, cuda):
     assert n == no and bits_equal(N(pts), po) and np.array_equal(N(w), wo)
 
 
+def test_extract_color_slice_matches_oracle(tde, orc, cuda):
+    """Extract_Color_Slice on the golden slab cases (and the whole volume,
+    an empty zone and a short capacity) against the oracle restatement, which
+    is pinned to the reference's slab scan."""
+    g, rb = slice_golden(tde)
+    color = T(g["color"], cuda)
+    ob = orc.make_rb((32, 32, 128), (2.0, 2.0, 2.0), tuple(int(v) for v in g["origin"]))
+    cases = [(g[f"c{ci}_mn"], g[f"c{ci}_mx"]) for ci in range(int(g["ncases"]))]
+    cases += [((-10**6,) * 3, (10**6,) * 3), ((-50, -50, -50), (-60, -60, -60))]
+    for mn, mx in cases:
+        ref = orc.extract_color_slice(g["color"], mn, mx, ob)
+        cols, n = tde.extract_color_slice(color, mn, mx, rb)
+        assert n == len(ref) and np.array_equal(N(cols), ref)
+    mn, mx = cases[1]
+    ref = orc.extract_color_slice(g["color"], mn, mx, ob)
+    cols, n = tde.extract_color_slice(color, mn, mx, rb, capacity=50)
+    assert n == len(ref) > 50 and np.array_equal(N(cols), ref[:50])
+
+
 def test_extract_slice_empty_zone(tde, cuda):
     g, rb = slice_golden(tde)
     pts, cols, _, n = tde.extract_slice(T(g["tsdf"], cuda), 0, T(g["color"], cuda), (-50, -50, -50),

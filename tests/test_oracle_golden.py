@@ -95,6 +95,25 @@ def test_extract_slice_oracle_bit_exact(orc):
         assert np.array_equal(cols, g[f"c{ci}_colors"])
 
 
+def test_extract_color_slice_is_the_colour_plane_of_the_pinned_slab_scan(orc):
+    """Extract_Color_Slice's restatement equals the colour plane of the
+    golden-pinned slab scan: with every TSDF weight zero the scan's +x/+y/+z
+    predicates never fire (scan_slice_of_both_volumes.cl:108-135 need w != 0),
+    so its output is the colour plane alone, chunk after chunk."""
+    g, rb = slice_inputs(orc)
+    tsdf = np.ascontiguousarray(g["tsdf"]).copy()
+    tsdf[:, 1] = 0
+    color = np.ascontiguousarray(g["color"])
+    total = 0
+    for ci in range(int(g["ncases"])):
+        mn, mx = g[f"c{ci}_mn"], g[f"c{ci}_mx"]
+        _, cols, _, n = orc.extract_slice(tsdf, 0, color, mn, mx, rb)
+        got = orc.extract_color_slice(color, mn, mx, rb)
+        assert len(got) == n and np.array_equal(got, cols)
+        total += n
+    assert total > 1000
+
+
 def test_extract_slice_reference_boundary_writes_documented(orc):
     """The reference's extract kernel writes +z points at chunk ends that its
     scan never counted (extract_slice_as_cloud.cl:369 vs

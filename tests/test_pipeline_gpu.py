@@ -431,11 +431,23 @@ def test_checkpoint_resume_bit_identical(cuda, tde, seq, tmp_path, color):
         assert np.array_equal(vol, ref_vol)
         if color:
             assert np.array_equal(col, ref_col) and (col[:, 3] > 0).sum() > 1000
-    # another storage format, or colour on one side only, is refused
-    other = pl.Pipeline(dataclasses.replace(cfg, tsdf_format=1), traj[0])
-    with pytest.raises(tde.TdeError):
-        other.restore(ck)
-    other.close()
+    # another storage format, volume edge (same voxel count), truncation or
+    # camera, or colour on one side only, is refused and changes nothing
+    for change in (dict(tsdf_format=1), dict(volume_m=cfg.volume_m * 1.25), dict(trunc_m=cfg.trunc_m * 1.5),
+                   dict(fx=cfg.fx * 1.01)):
+        other = pl.Pipeline(dataclasses.replace(cfg, **change), traj[0])
+        if color:
+            other.enable_color(max_weight=16)
+        with pytest.raises(tde.TdeError):
+            other.restore(ck)
+        assert step(other, 0)[1] == 0  # still usable
+        other.close()
+    if color:
+        other = make(traj[0])
+        other.enable_color(max_weight=17)
+        with pytest.raises(tde.TdeError):
+            other.restore(ck)
+        other.close()
     if color:
         plain = pl.Pipeline(cfg, traj[0])
         with pytest.raises(tde.TdeError):
