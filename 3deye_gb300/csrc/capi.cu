@@ -200,7 +200,7 @@ int tde_estimate_combined(const float *vmap_cur, const float *nmap_cur, const fl
     a.vcur = vmap_cur; a.ncur = nmap_cur; a.vprev = vmap_prev_g; a.nprev = nmap_prev_g;
     a.W = intr->cols; a.H = intr->rows;
     a.fx = intr->fx; a.fy = intr->fy; a.cx = intr->cx; a.cy = intr->cy;
-    a.dist_thresh = dist_thresh; a.angle_thresh = angle_thresh;
+    icp_set_thresholds(a, dist_thresh, angle_thresh);
     int st_code = launch_icp(a, st, mbuf, s);
     if (st_code) return st_code;
     // the host copy of h must outlive the async copy above

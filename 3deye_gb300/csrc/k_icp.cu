@@ -49,17 +49,20 @@ __device__ __forceinline__ f2 add_f(f2 a, float b) {
     return two_sum(s.hi, s.lo);
 }
 
+// The association's float operations, written as explicit fused
+// multiply-adds (one rounding each, as C's fmaf in the CPU oracle); the unit
+// is compiled without contraction, so nothing else fuses.
 __device__ __forceinline__ float3 mv(const float *M, float3 v) {
-    float a = 0.f; a += M[0] * v.x; a += M[1] * v.y; a += M[2] * v.z;
-    float b = 0.f; b += M[3] * v.x; b += M[4] * v.y; b += M[5] * v.z;
-    float c = 0.f; c += M[6] * v.x; c += M[7] * v.y; c += M[8] * v.z;
-    return make_float3(a, b, c);
+    return make_float3(__fmaf_rn(M[2], v.z, __fmaf_rn(M[1], v.y, __fmul_rn(M[0], v.x))),
+                       __fmaf_rn(M[5], v.z, __fmaf_rn(M[4], v.y, __fmul_rn(M[3], v.x))),
+                       __fmaf_rn(M[8], v.z, __fmaf_rn(M[7], v.y, __fmul_rn(M[6], v.x))));
 }
 __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
-    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    return make_float3(__fmaf_rn(a.y, b.z, -__fmul_rn(a.z, b.y)), __fmaf_rn(a.z, b.x, -__fmul_rn(a.x, b.z)),
+                       __fmaf_rn(a.x, b.y, -__fmul_rn(a.y, b.x)));
 }
 __device__ __forceinline__ float dot3(float3 a, float3 b) {
-    float d = 0.f; d += a.x * b.x; d += a.y * b.y; d += a.z * b.z; return d;
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
 }
 __device__ __forceinline__ float3 ld3(const float *p, size_t i) {
     return make_float3(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2));
@@ -81,8 +84,9 @@ __device__ __forceinline__ Assoc project(const IcpArgs &a, const IcpPose &P, flo
     r.vg = make_float3(rv.x + P.t_cur[0], rv.y + P.t_cur[1], rv.z + P.t_cur[2]);
     const float3 vcp = mv(P.R_prev_inv, make_float3(r.vg.x - P.t_prev[0], r.vg.y - P.t_prev[1], r.vg.z - P.t_prev[2]));
     if (!(vcp.z > 0.f)) return r;
-    const int u = __float2int_rn(vcp.x * a.fx / vcp.z + a.cx);
-    const int w = __float2int_rn(vcp.y * a.fy / vcp.z + a.cy);
+    const float iz = __frcp_rn(vcp.z);
+    const int u = __float2int_rn(__fmaf_rn(vcp.x, __fmul_rn(a.fx, iz), a.cx));
+    const int w = __float2int_rn(__fmaf_rn(vcp.y, __fmul_rn(a.fy, iz), a.cy));
     if (u < 0 || w < 0 || u >= a.W || w >= a.H) return r;
     r.ng = mv(P.R_cur, n);
     r.j = w * a.W + u;
@@ -94,9 +98,9 @@ __device__ __forceinline__ Assoc project(const IcpArgs &a, const IcpPose &P, flo
 __device__ __forceinline__ bool pair_terms(const IcpArgs &a, const Assoc &s, float3 np, float3 vp, float row[7]) {
     if (isnan(np.x)) return false;
     const float3 dv = make_float3(vp.x - s.vg.x, vp.y - s.vg.y, vp.z - s.vg.z);
-    if (sqrtf(dot3(dv, dv)) > a.dist_thresh) return false;
+    if (dot3(dv, dv) > a.dist2) return false;
     const float3 cr = cross3(s.ng, np);
-    if (sqrtf(dot3(cr, cr)) >= a.angle_thresh) return false;
+    if (dot3(cr, cr) >= a.angle2) return false;
     const float3 c = cross3(s.vg, np);
     row[0] = c.x; row[1] = c.y; row[2] = c.z;
     row[3] = np.x; row[4] = np.y; row[5] = np.z;
@@ -354,7 +358,7 @@ __device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose
             #pragma unroll
             for (int i = 0; i < 6; ++i)
                 #pragma unroll
-                for (int j = i; j < 7; ++j) { s[t] = s[t] + row[i] * row[j]; ++t; }
+                for (int j = i; j < 7; ++j) { s[t] = __fmaf_rn(row[i], row[j], s[t]); ++t; }
             s[27] = s[27] + 1.f;
         }
     }
@@ -462,7 +466,12 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     // ---- the pose this launch associates with ----
-    if (warp == 0) {
+    // Solver warp: 0, or 2 for every other wave of blocks, so that two blocks
+    // resident on one SM (blocks b and b + SM count) solve on different
+    // sub-partitions and their FP64 instruction streams do not queue on one
+    // FP64 pipe.  Warp 1 loads the frame's start pose meanwhile.
+    const int solver = ((blockIdx.x / a.sm_count) & 1) * 2;
+    if (warp == solver) {
         const double *R0 = iter == 0 ? st->R : st->R_it[(iter - 1) & 1];
         const double *t0 = iter == 0 ? st->t : st->t_it[(iter - 1) & 1];
         // the previous pose and the previous launch's totals, loads in flight together
@@ -516,7 +525,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
                 }
             }
         }
-    } else if (iter > 0 && tid < 32 + 12) {
+    } else if (iter > 0 && warp == 1 && lane < 12) {
         // the frame's start pose (launch 0 wrote it)
         const int k = tid - 32;
         if (k < 9) P.R_prev_inv[k] = st->pose.R_prev_inv[k];

@@ -10,7 +10,8 @@
 // test, so the brick is dropped.  A second kernel sweeps the surviving bricks,
 // one warp per brick, and applies the per-voxel update --
 // the same IEEE float operations, in the same order, as the CPU oracle, which
-// visits every voxel.  Culling only removes voxels the exact test rejects, so
+// visits every voxel (fused multiply-adds and correctly rounded reciprocals
+// written out on both sides, no divisions).  Culling only removes voxels the exact test rejects, so
 // volumes are bit-identical.
 //
 // The maximum (and smallest non-zero) observed depth per screen tile comes
@@ -20,7 +21,8 @@
 // distance in front of the smallest depth it projects to, is not swept either:
 // each of its voxels would get tsdf = 1 and keep f = 1, w = max, bit for bit.
 //
-// Built with -fmad=false so every voxel decision and value equals the oracle's.
+// Built with -fmad=false (no contraction beyond the explicit __fmaf_rn) so every
+// voxel decision and value equals the oracle's.
 #include "tde_common.cuh"
 #include "tde_integrate.cuh"
 
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
     const int nbx = (Nv.x + kBrick - 1) / kBrick, nby = (Nv.y + kBrick - 1) / kBrick;
     const size_t nbricks_all = (size_t)nbx * nby * ((Nv.z + kBrick - 1) / kBrick);
     typedef TsdfStore<FMT> S;
-    const float ntrunc = -P.trunc;
+    const float ntrunc = -P.trunc, itrunc = __frcp_rn(P.trunc);
     const int W = P.intr.cols, H = P.intr.rows;
     const float fx = P.intr.fx, fy = P.intr.fy, ccx = P.intr.cx, ccy = P.intr.cy;
     const int n_list = *count;
@@ -242,11 +244,10 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
         for (int h = 0; h < 2; ++h) {
             const int y = by * kBrick + (lane >> 3) + 4 * h;
             const float gy = ((float)y + 0.5f) * P.cell.y - q.t[1];
-            float vx = 0.f; vx += q.Ri[0] * gx; vx += q.Ri[1] * gy;
-            float vy = 0.f; vy += q.Ri[3] * gx; vy += q.Ri[4] * gy;
-            float vz = 0.f; vz += q.Ri[6] * gx; vz += q.Ri[7] * gy;
-            float n2 = 0.f; n2 += gx * gx; n2 += gy * gy;
-            pvx[h] = vx; pvy[h] = vy; pvz[h] = vz; pn2[h] = n2;
+            pvx[h] = __fmaf_rn(q.Ri[1], gy, __fmul_rn(q.Ri[0], gx));
+            pvy[h] = __fmaf_rn(q.Ri[4], gy, __fmul_rn(q.Ri[3], gx));
+            pvz[h] = __fmaf_rn(q.Ri[7], gy, __fmul_rn(q.Ri[6], gx));
+            pn2[h] = __fmaf_rn(gy, gy, __fmul_rn(gx, gx));
             py_[h] = y;
             pxy[h] = Nv.x * wrap_mod(y + P.rb.origin_GRID.y, Nv.y) + px;
         }
@@ -268,17 +269,17 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
                 take[k] = false; sdfv[k] = 0.f; idx[k] = 0;
                 if (x >= Nv.x || y >= Nv.y || z >= Nv.z) continue;
                 const float gz = ((float)z + 0.5f) * P.cell.z - q.t[2];
-                float vx = pvx[h]; vx += q.Ri[2] * gz;
-                float vy = pvy[h]; vy += q.Ri[5] * gz;
-                float vz = pvz[h]; vz += q.Ri[8] * gz;
+                const float vx = __fmaf_rn(q.Ri[2], gz, pvx[h]);
+                const float vy = __fmaf_rn(q.Ri[5], gz, pvy[h]);
+                const float vz = __fmaf_rn(q.Ri[8], gz, pvz[h]);
                 if (!(vz > 0.f)) continue;
-                const int u = __float2int_rn(vx * fx / vz + ccx);
-                const int v = __float2int_rn(vy * fy / vz + ccy);
+                const float iz = __frcp_rn(vz);
+                const int u = __float2int_rn(__fmaf_rn(vx, __fmul_rn(fx, iz), ccx));
+                const int v = __float2int_rn(__fmaf_rn(vy, __fmul_rn(fy, iz), ccy));
                 if (u < 0 || u >= W || v < 0 || v >= H) continue;
                 const float Dp = __ldg(depth + (size_t)v * W + u);
                 if (Dp == 0.f) continue;
-                float n2 = pn2[h]; n2 += gz * gz;
-                const float sdf = Dp - sqrtf(n2);
+                const float sdf = Dp - __fsqrt_rn(__fmaf_rn(gz, gz, pn2[h]));
                 if (!(sdf >= ntrunc)) continue;
                 take[k] = true;
                 sdfv[k] = sdf;
@@ -300,9 +301,10 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
                 float fo;
                 int wo;
                 S::decode(raw[k], fo, wo);
-                const float tsdf = fminf(1.f, sdfv[k] / P.trunc);
+                const float tsdf = fminf(1.f, __fmul_rn(sdfv[k], itrunc));
                 const float fw = (float)wo;
-                const float fnew = (fo * fw + tsdf) / (fw + 1.f);
+                // running mean as an increment: f = tsdf (free space at 1) is a fixed point
+                const float fnew = __fmaf_rn(tsdf - fo, __frcp_rn(fw + 1.f), fo);
                 const int wnew = min(wo + 1, P.max_weight);
                 const typename S::Raw rn = S::encode(fnew, wnew);
                 all_sat = all_sat && S::same(rn, sat_raw);

@@ -89,6 +89,7 @@ struct tde_pipeline {
     cudaEvent_t pre_done[2] = {}, set_free[2] = {};
     cudaEvent_t col_ready[2] = {}, col_done[2] = {};
     int levels = 3;
+    int sm_count = 1;  // multiprocessors of the pipeline's device
     tde_intrinsics intr[3];
     // device buffers; raw depth and the current-frame maps come in two sets
     uint16_t *raw[2] = {};
@@ -189,7 +190,8 @@ int record_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
             a.vcur = vcur[l]; a.ncur = ncur[l]; a.vprev = p->vmod[l]; a.nprev = p->nmod[l];
             a.W = p->intr[l].cols; a.H = p->intr[l].rows;
             a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
-            a.dist_thresh = c.dist_thresh; a.angle_thresh = c.angle_thresh;
+            icp_set_thresholds(a, c.dist_thresh, c.angle_thresh);
+            a.sm_count = p->sm_count;
             for (int it = 0; it < c.icp_iters[l]; ++it, ++iter)
                 TDE_TRY(launch_icp_step(a, p->st, iter, iter == total - 1, pub, s));
         }
@@ -535,6 +537,10 @@ int tde_pipeline_create(const tde_pipeline_config *cfg, const double *pose12, td
     auto fail = [&](int code) { release(p); return code; };
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&p->prio_low, &p->prio_high);
     if (e != cudaSuccess) return fail(cuda_fail(e, "stream priorities"));
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || p->sm_count < 1) return fail(cuda_fail(e, "multiprocessor count"));
     e = cudaStreamCreateWithPriority(&p->stream, cudaStreamNonBlocking, p->prio_high);
     if (e != cudaSuccess) return fail(cuda_fail(e, "stream"));
     if ((st = make_pre_stream(p))) return fail(st);

@@ -54,8 +54,16 @@ struct IcpArgs {
     const float *vcur, *ncur, *vprev, *nprev;
     int W, H;
     float fx, fy, cx, cy;
-    float dist_thresh, angle_thresh;
+    // squared thresholds (float products, as the oracle forms them): a pair is
+    // kept when |dv|^2 <= dist2 and |n x n_model|^2 < angle2
+    float dist2, angle2;
+    int sm_count;  // multiprocessors of the device (spreads the per-block solves)
 };
+inline void icp_set_thresholds(IcpArgs &a, float dist_thresh, float angle_thresh) {
+    a.dist2 = dist_thresh * dist_thresh;
+    a.angle2 = angle_thresh * angle_thresh;
+    a.sm_count = 1;
+}
 
 // exp of the rotation part x[0..2] (Rodrigues), row-major 3x3.
 __host__ __device__ inline void so3_exp(const double *x, double *R) {

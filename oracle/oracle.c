@@ -448,10 +448,22 @@ int or_normal_map(const float *vmap, float *nmap, int W, int H) {
 
 /* ---------------- ICP association (estimate_combined absent;
  * opencl_wrappers.cpp:386-437 fixes the argument order and the 27-term
- * [A | b] layout) ---------------------------------------------------------- */
-static float dot3(v3 a, v3 b) { float d = 0.f; d += a.x * b.x; d += a.y * b.y; d += a.z * b.z; return d; }
-static v3 cross3(v3 a, v3 b) {
-    v3 r = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+ * [A | b] layout) ----------------------------------------------------------
+ * Float operations are written out with fused multiply-adds (fmaf: one
+ * rounding, the same result as CUDA's __fmaf_rn), one correctly rounded
+ * reciprocal per projection, and the distance and angle thresholds compared
+ * on squares, so that the GPU association (k_icp.cu) performs exactly these
+ * operations with fewer instructions and selects the same pairs. */
+static v3 mat_vec_fma(const float *M, v3 v) {
+    v3 r;
+    r.x = fmaf(M[2], v.z, fmaf(M[1], v.y, M[0] * v.x));
+    r.y = fmaf(M[5], v.z, fmaf(M[4], v.y, M[3] * v.x));
+    r.z = fmaf(M[8], v.z, fmaf(M[7], v.y, M[6] * v.x));
+    return r;
+}
+static float dot3_fma(v3 a, v3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+static v3 cross3_fma(v3 a, v3 b) {
+    v3 r = {fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x))};
     return r;
 }
 
@@ -459,6 +471,7 @@ int or_icp_terms(const float *vcur, const float *ncur, const float *vprev, const
                  const tde_intrinsics *in, float dist_thresh, float angle_thresh, double *sums, uint8_t *mask) {
     const int W = in->cols, H = in->rows;
     const float *Rc = P, *tc = P + 9, *Rpi = P + 12, *tp = P + 21;
+    const float dist2 = dist_thresh * dist_thresh, angle2 = angle_thresh * angle_thresh;
     for (int k = 0; k < 28; ++k) sums[k] = 0.0;
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {
@@ -467,28 +480,29 @@ int or_icp_terms(const float *vcur, const float *ncur, const float *vprev, const
             v3 n = {ncur[3 * i], ncur[3 * i + 1], ncur[3 * i + 2]};
             if (isnan(n.x)) continue;
             v3 v = {vcur[3 * i], vcur[3 * i + 1], vcur[3 * i + 2]};
-            v3 rv = mat_vec(Rc, v);
+            v3 rv = mat_vec_fma(Rc, v);
             v3 vg = {rv.x + tc[0], rv.y + tc[1], rv.z + tc[2]};
             v3 dd = {vg.x - tp[0], vg.y - tp[1], vg.z - tp[2]};
-            v3 vcp = mat_vec(Rpi, dd);
+            v3 vcp = mat_vec_fma(Rpi, dd);
             if (!(vcp.z > 0.f)) continue;
-            int u = rint_sat(vcp.x * in->fx / vcp.z + in->cx);
-            int w = rint_sat(vcp.y * in->fy / vcp.z + in->cy);
+            const float iz = 1.f / vcp.z;
+            int u = rint_sat(fmaf(vcp.x, in->fx * iz, in->cx));
+            int w = rint_sat(fmaf(vcp.y, in->fy * iz, in->cy));
             if (u < 0 || w < 0 || u >= W || w >= H) continue;
             size_t j = (size_t)w * W + u;
             v3 np = {nprev[3 * j], nprev[3 * j + 1], nprev[3 * j + 2]};
             if (isnan(np.x)) continue;
             v3 vp = {vprev[3 * j], vprev[3 * j + 1], vprev[3 * j + 2]};
             v3 dv = {vp.x - vg.x, vp.y - vg.y, vp.z - vg.z};
-            if (sqrtf(dot3(dv, dv)) > dist_thresh) continue;
-            v3 ng = mat_vec(Rc, n);
-            v3 cr = cross3(ng, np);
-            if (sqrtf(dot3(cr, cr)) >= angle_thresh) continue;
-            v3 c = cross3(vg, np);
-            float row[7] = {c.x, c.y, c.z, np.x, np.y, np.z, dot3(np, dv)};
+            if (dot3_fma(dv, dv) > dist2) continue;
+            v3 ng = mat_vec_fma(Rc, n);
+            v3 cr = cross3_fma(ng, np);
+            if (dot3_fma(cr, cr) >= angle2) continue;
+            v3 c = cross3_fma(vg, np);
+            float row[7] = {c.x, c.y, c.z, np.x, np.y, np.z, dot3_fma(np, dv)};
             int s = 0;
             for (int a = 0; a < 6; ++a)
-                for (int b = a; b < 7; ++b) sums[s++] += (double)(row[a] * row[b]);
+                for (int b = a; b < 7; ++b) sums[s++] += (double)row[a] * (double)row[b];
             sums[27] += 1.0;
             if (mask) mask[i] = 1;
         }
@@ -544,8 +558,11 @@ int or_integrate(const float *depth, void *vol, int fmt, float trunc, const floa
                  uint64_t *stats) {
     vol_t v = {fmt, vox_count(rb)};
     const int W = in->cols, H = in->rows, Nx = rb->voxels_size.x, Ny = rb->voxels_size.y, Nz = rb->voxels_size.z;
-    const float ntrunc = -trunc;
+    const float ntrunc = -trunc, itrunc = 1.f / trunc;
     uint64_t n_read = 0, n_written = 0;
+    /* Written with fused multiply-adds (fmaf) and correctly rounded
+     * reciprocals in place of divisions, operation for operation as the GPU
+     * sweep (k_integrate.cu), which is compiled without contraction. */
 #pragma omp parallel for schedule(static) reduction(+ : n_read, n_written)
     for (int y = 0; y < Ny; ++y)
         for (int x = 0; x < Nx; ++x) {
@@ -553,25 +570,28 @@ int or_integrate(const float *depth, void *vol, int fmt, float trunc, const floa
             const float gy = ((float)y + 0.5f) * cell[1] - t[1];
             for (int z = 0; z < Nz; ++z) {
                 const float gz = ((float)z + 0.5f) * cell[2] - t[2];
-                float vx = 0.f; vx += Ri[0] * gx; vx += Ri[1] * gy; vx += Ri[2] * gz;
-                float vy = 0.f; vy += Ri[3] * gx; vy += Ri[4] * gy; vy += Ri[5] * gz;
-                float vz = 0.f; vz += Ri[6] * gx; vz += Ri[7] * gy; vz += Ri[8] * gz;
+                const float vx = fmaf(Ri[2], gz, fmaf(Ri[1], gy, Ri[0] * gx));
+                const float vy = fmaf(Ri[5], gz, fmaf(Ri[4], gy, Ri[3] * gx));
+                const float vz = fmaf(Ri[8], gz, fmaf(Ri[7], gy, Ri[6] * gx));
                 if (!(vz > 0.f)) continue;
-                int u = rint_sat(vx * in->fx / vz + in->cx);
-                int w = rint_sat(vy * in->fy / vz + in->cy);
+                const float iz = 1.f / vz;
+                int u = rint_sat(fmaf(vx, in->fx * iz, in->cx));
+                int w = rint_sat(fmaf(vy, in->fy * iz, in->cy));
                 if (u < 0 || u >= W || w < 0 || w >= H) continue;
                 float Dp = depth[(size_t)w * W + u];
                 if (Dp == 0.f) continue;
-                float n2 = 0.f; n2 += gx * gx; n2 += gy * gy; n2 += gz * gz;
+                const float n2 = fmaf(gz, gz, fmaf(gy, gy, gx * gx));
                 float sdf = Dp - sqrtf(n2);
                 if (!(sdf >= ntrunc)) continue;
                 size_t idx = or_voxel_address(x, y, z, rb);
                 float fo; int wo; uint32_t raw;
                 rec_load(vol, v, idx, &fo, &wo, &raw);
                 ++n_read;
-                float tsdf = fminf(1.f, sdf / trunc);
+                float tsdf = fminf(1.f, sdf * itrunc);
                 float fw = (float)wo;
-                float fnew = (fo * fw + tsdf) / (fw + 1.f);
+                /* the running mean as an increment: f + (tsdf - f) / (w + 1), so
+                 * that a voxel at f = tsdf (free space at 1) keeps its bits */
+                float fnew = fmaf(tsdf - fo, 1.f / (fw + 1.f), fo);
                 int wnew = imin(wo + 1, max_weight);
                 n_written += (uint64_t)rec_store(vol, v, idx, fnew, wnew);
             }
