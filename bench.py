@@ -81,6 +81,8 @@ def parse():
     ap.add_argument("--cpu-frames", type=int, default=40,
                     help="frames of the CPU baseline sample (about 11 s on 16 cores; capped by the sequence length)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip", default="", help="comma list of further passes to leave out (color, learned, cyclic, "
+                                               "config1), e.g. for a short profiling run")
     ap.add_argument("--f64-frames", type=int, default=30,
                     help="leading frames of the sequence the full-FP64 oracle also runs (ATE of the GPU trajectory "
                          "against it)")
@@ -482,6 +484,48 @@ def config1_run(tde, syn, pl, torch, dev, rank, ws, with_cpu):
     return out
 
 
+def color_pass(tde, pl, torch, cfg, traj, frames, W, n, ws, dev, pose_a):
+    """Pass D: RGB-D frames with the colour volume on (Integrate_Colors), then
+    the whole-model export.  Synthetic colour: a deterministic pattern of the
+    pixel and frame index, resident in HBM beside the depth frames."""
+    import numpy as np
+    K = n - W
+    base, fbytes = frames.data_ptr(), cfg.rows * cfg.cols * 2
+    cp = pl.Pipeline(cfg, traj[0], use_graphs=True)
+    cp.enable_color(max_weight=128)
+    i32 = torch.int32
+    yy, xx = torch.meshgrid(torch.arange(cfg.rows, device=dev, dtype=i32), torch.arange(cfg.cols, device=dev, dtype=i32),
+                            indexing="ij")
+    kk = torch.arange(n, device=dev, dtype=i32).view(n, 1, 1)
+    rgb_frames = torch.empty((n, cfg.rows, cfg.cols, 3), dtype=torch.uint8, device=dev)
+    rgb_frames[..., 0] = (xx + 3 * kk) % 256
+    rgb_frames[..., 1] = (yy + 5 * kk) % 256
+    rgb_frames[..., 2] = ((xx + yy) % 256).expand(n, -1, -1)
+    cbase, cfb = rgb_frames.data_ptr(), cfg.rows * cfg.cols * 3
+    for i in range(W):
+        cp.enqueue_rgbd(base + i * fbytes, cbase + i * cfb, True)
+    cp.sync()
+    cstream = torch.cuda.ExternalStream(cp.stream)
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier_sync(ws)
+    h0.record(cstream)
+    for i in range(W, n):
+        cp.enqueue_rgbd(base + i * fbytes, cbase + i * cfb, True)
+    h1.record(cstream)
+    cp.sync()
+    c_ms = max_over_ranks(ws, h0.elapsed_time(h1))
+    c_launches = cp.launches_per_frame()
+    pose_c = cp.pose()
+    export = model_export(tde, torch, cp, cfg, dev)
+    cp.close()
+    del rgb_frames
+    color = {"value": round(ws * K / (c_ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(c_ms / K, 5),
+             "gpu_launches": c_launches * K, "same_trajectory_as_plain": bool(np.array_equal(pose_c, pose_a)),
+             "note": "RGB-D frames (synthetic colour pattern, resident in HBM): the plain pipeline plus the colour "
+                     "volume update at the model surface after each raycast (brick-culled, 4 B per voxel)"}
+    return color, export
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -574,48 +618,19 @@ def run_ours(args, ws, rank, local):
     deterministic = bool(np.array_equal(est[-1], pose_a) and np.array_equal(pose_s, pose_a))
     ate = pl.ate_rmse(est, traj)
 
-    # ---- pass D: RGB-D frames, colour volume on (Integrate_Colors) ---------
-    # synthetic colour: a deterministic pattern of the pixel and frame index,
-    # resident in HBM beside the depth frames
-    cp = pl.Pipeline(cfg, traj[0], use_graphs=True)
-    cp.enable_color(max_weight=128)
-    i32 = torch.int32
-    yy, xx = torch.meshgrid(torch.arange(cfg.rows, device=dev, dtype=i32), torch.arange(cfg.cols, device=dev, dtype=i32),
-                            indexing="ij")
-    kk = torch.arange(n, device=dev, dtype=i32).view(n, 1, 1)
-    rgb_frames = torch.empty((n, cfg.rows, cfg.cols, 3), dtype=torch.uint8, device=dev)
-    rgb_frames[..., 0] = (xx + 3 * kk) % 256
-    rgb_frames[..., 1] = (yy + 5 * kk) % 256
-    rgb_frames[..., 2] = ((xx + yy) % 256).expand(n, -1, -1)
-    cbase, cfb = rgb_frames.data_ptr(), cfg.rows * cfg.cols * 3
-    for i in range(W):
-        cp.enqueue_rgbd(base + i * fbytes, cbase + i * cfb, True)
-    cp.sync()
-    cstream = torch.cuda.ExternalStream(cp.stream)
-    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier_sync(ws)
-    h0.record(cstream)
-    for i in range(W, n):
-        cp.enqueue_rgbd(base + i * fbytes, cbase + i * cfb, True)
-    h1.record(cstream)
-    cp.sync()
-    c_ms = max_over_ranks(ws, h0.elapsed_time(h1))
-    c_launches = cp.launches_per_frame()
-    pose_c = cp.pose()
-    export = model_export(tde, torch, cp, cfg, dev)
-    cp.close()
-    cyclic = cyclic_run(tde, syn, pl, torch, dev, rank)
-    config1 = config1_run(tde, syn, pl, torch, dev, rank, ws, rank == 0 and ws == 1 and not args.no_cpu_baseline)
-    del rgb_frames
-    color = {"value": round(ws * K / (c_ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(c_ms / K, 5),
-             "gpu_launches": c_launches * K, "same_trajectory_as_plain": bool(np.array_equal(pose_c, pose_a)),
-             "note": "RGB-D frames (synthetic colour pattern, resident in HBM): the plain pipeline plus the colour "
-                     "volume update at the model surface after each raycast (brick-culled, 4 B per voxel)"}
+    skip = set(x for x in args.skip.split(",") if x)
+    color = export = cyclic = config1 = None
+    if "color" not in skip:
+        color, export = color_pass(tde, pl, torch, cfg, traj, frames, W, n, ws, dev, pose_a)
+    if "cyclic" not in skip:
+        cyclic = cyclic_run(tde, syn, pl, torch, dev, rank)
+    if "config1" not in skip:
+        config1 = config1_run(tde, syn, pl, torch, dev, rank, ws, rank == 0 and ws == 1 and not args.no_cpu_baseline)
 
     # ---- pass C: the learned refiner in place of the bilateral filter -------
     learned = None
     wpath = Path(args.refiner_weights)
-    if wpath.exists():
+    if wpath.exists() and "learned" not in skip:
         rf = importlib.import_module("3deye_gb300.refiner")
         R = rf.Refiner(1, cfg.rows, cfg.cols)
         R.set_params(np.fromfile(wpath, dtype=np.float32))
