@@ -35,8 +35,6 @@ namespace {
 
 constexpr int kTileM = 128;             // output pixels per MMA tile
 constexpr int kHaloW = kTileM + 2;      // halo pixels per row
-constexpr int kConvWorkers = 128;       // warps 0-3: loads and epilogue, one TMEM lane quarter each
-constexpr int kConvThreads = 160;       // + warp 4: issues the MMAs
 constexpr int kWgK = 64;                // pixels per weight-gradient K step
 constexpr int kWgHalo = kWgK + 2;
 constexpr int kWgThreads = 256;
@@ -100,37 +98,74 @@ __device__ __forceinline__ uint4 load_input_chunk(const Args &A, int img, int y,
 }
 
 // ---------------------------------------------------------------------------
-// Forward / input-gradient convolution
+// Forward / input-gradient convolution: a warp-specialised pipeline.
 //
-// A block owns a strip of R consecutive output rows of one 128-pixel column
-// tile.  Input rows live in a ring of 4 halo slots: tile row y reads slots
-// y-1, y, y+1 while row y+2 is loaded into the fourth, so each row is loaded
-// once per strip instead of three times.  Two TMEM accumulators let the MMAs
-// of row y run while the epilogue of row y-1 drains the other one.
+// A block owns strips of consecutive output rows of one 128-pixel column
+// tile.  Its warps have fixed roles, connected by mbarriers (no block-wide
+// barrier in the steady state):
+//   warps 4-7 (producers): input row j goes to warp 4 + (j & 3), which loads
+//     the halo row (pixels x0-1 .. x0+128, every 8-channel chunk, as planes)
+//     into ring slot j % S once the tensor core has released that slot, and
+//     marks it full -- four rows in flight, one per warp;
+//   warp 8, one lane (MMA issuer): output row r waits for its three input
+//     rows and for a free accumulator (one of kConvAcc in tensor memory),
+//     issues 9 taps x CC/2 MMAs (M = 128 pixels, N = cout, K = 16), and
+//     commits them to the accumulator's "full" barrier and to the "empty"
+//     barrier of the input row no later output row reads;
+//   warps 0-3 (epilogue): TMEM lane quarter q of warp q, one pixel per
+//     thread -- wait for the accumulator, read it (tcgen05.ld), apply bias,
+//     ReLU, mask or the fused head, store bf16 NHWC, release the accumulator.
+// Input rows are loaded once per strip; loads, MMAs and epilogues of
+// different rows overlap.  Every wait is bounded: on a timeout the block
+// raises A.err, all roles leave their loops, the issuer waits (bounded) for
+// its MMAs in flight, and the tensor memory is freed.
 // ---------------------------------------------------------------------------
-constexpr int kSlots = 4;
+constexpr int kConvEpiWarps = 4, kConvProdWarps = 4;
+constexpr int kConvThreads = 32 * (kConvEpiWarps + kConvProdWarps + 1);  // + the MMA warp
+constexpr int kConvMmaWarp = kConvEpiWarps + kConvProdWarps;
+constexpr int kConvAcc = 4;       // accumulators in tensor memory
+constexpr int kConvMaxSlots = 8;  // input-row ring
+constexpr int kConvMinSlots = 4;
+constexpr uint64_t kConvWaitNs = 2000000000ull;
 
-// Loads one input row (halo pixels x0-1 .. x0+128, every chunk) into a slot.
-// Loads are issued in groups before their stores so that several are in
-// flight per thread.
-template <int MODE, int CC>
-__device__ __forceinline__ void load_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int tid) {
-    constexpr int G = MODE == SRC_POOL ? 4 : 8;
-    constexpr int n = kHaloW * CC;
-    for (int base = tid; base < n; base += kConvWorkers * G) {
-        uint4 v[G];
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-            const int i = base + g * kConvWorkers;
-            v[g] = make_uint4(0u, 0u, 0u, 0u);
-            if (i < n) v[g] = load_input_chunk<MODE>(A, img, y, x0 + i / CC - 1, i % CC);
-        }
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-            const int i = base + g * kConvWorkers;
-            if (i < n) *reinterpret_cast<uint4 *>(slot + ((size_t)(i % CC) * kHaloW + i / CC) * 16) = v[g];
+struct ConvPipe {
+    uint64_t full[kConvMaxSlots], empty[kConvMaxSlots];
+    uint64_t acc_full[kConvAcc], acc_empty[kConvAcc];
+    uint64_t drain;
+    uint32_t tmem;
+    int abort;
+};
+
+// Bounded wait on an mbarrier phase; false when the block aborted (here or
+// in another role).
+__device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort, int *err) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = tc::globaltimer_ns();
+    while (!tc::mbar_try_wait(bar, parity)) {
+        if (*abort) return false;
+        if (tc::globaltimer_ns() - t0 > kConvWaitNs) {
+            *abort = 1;
+            atomicExch(err, 1);
+            return false;
         }
     }
+    return true;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+// Strip `item` of the block's sequence: image, column start, rows [y0, y1).
+struct Strip { int img, x0, y0, y1; };
+__device__ __forceinline__ Strip strip_of(const ConvArgs &A, int item, int rows_per_item) {
+    const int tiles_x = (A.w + kTileM - 1) / kTileM;
+    const int chunks = (A.h + rows_per_item - 1) / rows_per_item;
+    Strip s;
+    s.x0 = (item % tiles_x) * kTileM;
+    s.y0 = ((item / tiles_x) % chunks) * rows_per_item;
+    s.img = item / (tiles_x * chunks);
+    s.y1 = min(A.h, s.y0 + rows_per_item);
+    return s;
 }
 
 // Address of chunk c of the concatenated input at (img, y, x) for a source
@@ -150,34 +185,55 @@ __device__ __forceinline__ const bf16 *chunk_ptr(const ConvArgs &A, int img, int
     return A.b + (((size_t)img * A.h + y) * A.w + x) * A.cb + 8 * (c - cca);
 }
 
-// Starts the copies of one input row into a slot with cp.async (16 B each,
-// zero-filled outside the image); completed by cp.async.wait_all.
+// One warp loads input row y (halo pixels x0-1 .. x0+128, CC chunks) into a
+// slot as planes: 16-byte copies, zero outside the image; complete (and made
+// visible to the tensor core) when it returns.
 template <int MODE, int CC>
-__device__ __forceinline__ void load_row_async(const ConvArgs &A, unsigned char *slot, int img, int y, int x0,
-                                               int tid) {
+__device__ __forceinline__ void warp_load_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int lane) {
     constexpr int n = kHaloW * CC;
-    for (int i = tid; i < n; i += kConvWorkers) {
-        const int c = i % CC, px = i / CC;
-        const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
-        const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
-        const int bytes = src ? 16 : 0;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src ? src : A.a), "r"(bytes)
-                     : "memory");
+    if (MODE == SRC_POOL) {
+        constexpr int G = 4;
+        for (int base = lane; base < n; base += 32 * G) {
+            uint4 v[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int i = base + 32 * g;
+                v[g] = make_uint4(0u, 0u, 0u, 0u);
+                if (i < n) v[g] = load_input_chunk<MODE>(A, img, y, x0 + i / CC - 1, i % CC);
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int i = base + 32 * g;
+                if (i < n) *reinterpret_cast<uint4 *>(slot + ((size_t)(i % CC) * kHaloW + i / CC) * 16) = v[g];
+            }
+        }
+    } else {
+        for (int i = lane; i < n; i += 32) {
+            const int c = i % CC, px = i / CC;
+            const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
+            const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
+            const int bytes = src ? 16 : 0;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src ? src : A.a),
+                         "r"(bytes)
+                         : "memory");
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
-    asm volatile("cp.async.commit_group;" ::: "memory");
+    tc::fence_proxy_async();
+    __syncwarp();
 }
-__device__ __forceinline__ void wait_async_rows() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-__device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, int warp, int lane, int img, int y,
-                                              int x0) {
-    const int m = warp * 32 + lane;
+// Epilogue of one output row for one pixel (TMEM lane quarter of this warp).
+__device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, int quarter, int lane, int img, int y,
+                                              int x0, float depth_in) {
+    const int m = quarter * 32 + lane;
     const int x = x0 + m;
     const bool valid = x < A.w;
     const size_t pix = ((size_t)img * A.h + y) * A.w + (valid ? x : 0);
     float r = 0.f;
     for (int j = 0; j < A.cout; j += 16) {
         float v[16];
-        tc::tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + (uint32_t)j, v);
+        tc::tmem_ld16(tacc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)j, v);
         if (!valid) continue;
         if (A.bias) {
 #pragma unroll
@@ -207,8 +263,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
         }
     }
     if (valid && A.head_w) {
-        const float d = A.depth_in[pix];
-        const float o = d > 0.f ? d + 0.01f * (r + __ldg(A.head_b)) : 0.f;  // residual in cm
+        const float o = depth_in > 0.f ? depth_in + 0.01f * (r + __ldg(A.head_b)) : 0.f;  // residual in cm
         if (A.depth_out) A.depth_out[pix] = o;
         if (A.depth_mm) {
             const float mm = fminf(fmaxf(rintf(o * 1000.f), 0.f), (float)TDE_MAX_DEPTH_VALUE);
@@ -218,82 +273,98 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
 }
 
 template <int MODE, int CC>
-__global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs A, int rows_per_item) {
+__global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs A, int rows_per_item, int S) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ uint32_t tmem_slot;
+    __shared__ ConvPipe pp;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const bool worker = warp < 4;
     constexpr uint32_t slot_bytes = (uint32_t)CC * kHaloW * 16;
     unsigned char *halo = smem;
-    unsigned char *wsm = smem + kSlots * slot_bytes;
+    unsigned char *wsm = smem + (size_t)S * slot_bytes;
     const uint32_t ncols = tmem_cols(A.cout);
+    const uint32_t tcols = kConvAcc * ncols;
+    volatile int *abort = &pp.abort;
 
     // the next layer may start its prologue; it waits for this grid before
     // reading anything this one writes
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
+    if (warp == kConvMmaWarp) tc::tmem_alloc(&pp.tmem, tcols);
     if (tid == 0) {
-        tc::mbar_init(&mbar[0], 1);
-        tc::mbar_init(&mbar[1], 1);
+        for (int s = 0; s < kConvMaxSlots; ++s) {
+            tc::mbar_init(&pp.full[s], 1);
+            tc::mbar_init(&pp.empty[s], 1);
+        }
+        for (int a = 0; a < kConvAcc; ++a) {
+            tc::mbar_init(&pp.acc_full[a], 1);
+            tc::mbar_init(&pp.acc_empty[a], kConvEpiWarps);
+        }
+        tc::mbar_init(&pp.drain, 1);
+        pp.abort = 0;
     }
-    // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B,
-    // as asynchronous copies (completed with the first rows' copies).  No
-    // kernel launched right before a convolution writes weights, so they are
-    // fetched before waiting for the previous grid, overlapping its tail.
-    if (worker) {
+    // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B.
+    // No kernel launched right before a convolution writes weights, so they
+    // are fetched before waiting for the previous grid.
+    {
         const int nw = A.cout * 9 * CC;
-        for (int i = tid; i < nw; i += kConvWorkers) {
+        for (int i = tid; i < nw; i += kConvThreads) {
             const int c = i % CC, t = (i / CC) % 9, co = i / (9 * CC);
             const uint32_t dst = tc::smem_u32(wsm + ((size_t)(t * CC + c) * A.cout + co) * 16);
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(A.wgt + (size_t)i * 8) : "memory");
         }
-        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t halo_s = tc::smem_u32(halo), w_s = tc::smem_u32(wsm);
-    const uint32_t idesc = tc::idesc_bf16(kTileM, A.cout);
-    // descriptor bases: A at a slot's first plane (LBO = plane stride), B at
-    // the first weight plane; an MMA adds its byte offset >> 4
-    const uint64_t a_desc0 = tc::desc(halo_s, kHaloW * 16, 128);
-    const uint64_t b_desc0 = tc::desc(w_s, A.cout * 16, 128);
-    const uint32_t b_plane = (uint32_t)A.cout * 16;
+    const uint32_t tmem = pp.tmem;
     const int tiles_x = (A.w + kTileM - 1) / kTileM;
-    const int chunks = (A.h + rows_per_item - 1) / rows_per_item;
-    const int items = A.n * tiles_x * chunks;
-    uint32_t g = 0;  // rows issued by this block: accumulator g & 1, its mbarrier phase (g >> 1) & 1
-    bool failed = false;
+    const int items = A.n * tiles_x * ((A.h + rows_per_item - 1) / rows_per_item);
 
-    for (int item = blockIdx.x; item < items && !failed; item += gridDim.x) {
-        const int xt = item % tiles_x;
-        const int ch = (item / tiles_x) % chunks;
-        const int img = item / (tiles_x * chunks);
-        const int x0 = xt * kTileM;
-        const int y0 = ch * rows_per_item;
-        const int y1 = min(A.h, y0 + rows_per_item);
-        if (worker) {
-            for (int dy = -1; dy <= 1; ++dy) {
-                unsigned char *slot = halo + (size_t)((y0 + dy + kSlots) % kSlots) * slot_bytes;
-                if (MODE == SRC_POOL) load_row<MODE, CC>(A, slot, img, y0 + dy, x0, tid);
-                else load_row_async<MODE, CC>(A, slot, img, y0 + dy, x0, tid);
+    if (warp >= kConvEpiWarps && warp < kConvMmaWarp) {
+        // ---- producers ----
+        const int pw = warp - kConvEpiWarps;
+        uint32_t j = 0;  // this block's input-row sequence
+        for (int item = blockIdx.x; item < items && !*abort; item += gridDim.x) {
+            const Strip st = strip_of(A, item, rows_per_item);
+            const int nin = st.y1 - st.y0 + 2;
+            for (int i = 0; i < nin; ++i, ++j) {
+                if ((int)(j & 3u) != pw) continue;
+                const uint32_t s = j % (uint32_t)S, k = j / (uint32_t)S;
+                if (k > 0 && !pipe_wait(&pp.empty[s], (k - 1) & 1u, abort, A.err)) break;
+                warp_load_row<MODE, CC>(A, halo + (size_t)s * slot_bytes, st.img, st.y0 - 1 + i, st.x0, lane);
+                if (lane == 0) mbar_arrive(&pp.full[s]);
             }
-            wait_async_rows();  // rows (and, the first time, the weights)
         }
-        tc::fence_proxy_async();
-        __syncthreads();
-        for (int y = y0; y < y1; ++y, ++g) {
-            if (warp == 4) {
-                if (lane == 0) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    } else if (warp == kConvMmaWarp) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            const uint32_t halo_s = tc::smem_u32(halo), w_s = tc::smem_u32(wsm);
+            const uint32_t idesc = tc::idesc_bf16(kTileM, A.cout);
+            // descriptor bases: A at a slot's first plane (LBO = plane stride),
+            // B at the first weight plane; an MMA adds its byte offset >> 4
+            const uint64_t a_desc0 = tc::desc(halo_s, kHaloW * 16, 128);
+            const uint64_t b_desc0 = tc::desc(w_s, A.cout * 16, 128);
+            const uint32_t b_plane = (uint32_t)A.cout * 16;
+            uint32_t jin = 0, waited = 0, q = 0;  // input rows of earlier strips, rows known full, output rows
+            bool ok = true;
+            for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+                const Strip st = strip_of(A, item, rows_per_item);
+                const int R = st.y1 - st.y0;
+                for (int o = 0; o < R && ok; ++o, ++q) {
+                    // its input rows jin + o .. jin + o + 2
+                    for (; waited <= jin + o + 2 && ok; ++waited)
+                        ok = pipe_wait(&pp.full[waited % (uint32_t)S], (waited / (uint32_t)S) & 1u, abort, A.err);
+                    const uint32_t a = q % kConvAcc, ka = q / kConvAcc;
+                    if (ok && ka > 0) ok = pipe_wait(&pp.acc_empty[a], (ka - 1) & 1u, abort, A.err);
+                    if (!ok) break;
                     tc::fence_after_sync();
-                    const uint32_t dacc = tmem + (g & 1u) * ncols;
+                    const uint32_t dacc = tmem + a * ncols;
 #pragma unroll
                     for (int t = 0; t < 9; ++t) {
                         const int dy = t / 3, dx = t % 3;
-                        const uint32_t a_off = (uint32_t)((y + dy - 1 + kSlots) % kSlots) * slot_bytes + dx * 16;
+                        const uint32_t a_off = ((jin + o + dy) % (uint32_t)S) * slot_bytes + dx * 16;
 #pragma unroll
                         for (int kc = 0; kc < CC; kc += 2) {
                             const uint64_t ad = a_desc0 + ((a_off + (uint32_t)kc * kHaloW * 16) >> 4);
@@ -301,63 +372,47 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
                             tc::mma_bf16(dacc, ad, bd, idesc, (t | kc) ? 1u : 0u);
                         }
                     }
-                    tc::commit(&mbar[g & 1u]);
+                    tc::commit(&pp.acc_full[a]);
+                    // input row o is read by no later output row of the strip;
+                    // after the last output row, neither are the two below it
+                    tc::commit(&pp.empty[(jin + o) % (uint32_t)S]);
+                    if (o == R - 1) {
+                        tc::commit(&pp.empty[(jin + o + 1) % (uint32_t)S]);
+                        tc::commit(&pp.empty[(jin + o + 2) % (uint32_t)S]);
+                    }
                 }
-                __syncwarp();
+                jin += (uint32_t)(R + 2);
             }
-            if (y > y0) {
-                // row y-1: its MMAs are done, so its accumulator can be drained
-                // and the slot of row y-2 refilled
-                bool ok = true;
-                if (worker) {
-                    const uint32_t gp = g - 1;
-                    ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
-                }
-                if (__syncthreads_or(!ok)) {
-                    failed = true;
-                    break;
-                }
+            // every MMA issued has finished before the tensor memory is freed
+            tc::commit(&pp.drain);
+            tc::mbar_wait(&pp.drain, 0u, kConvWaitNs);
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp q drains TMEM lanes 32q .. 32q + 31 ----
+        uint32_t q = 0;
+        for (int item = blockIdx.x; item < items && !*abort; item += gridDim.x) {
+            const Strip st = strip_of(A, item, rows_per_item);
+            bool ok = true;
+            for (int y = st.y0; y < st.y1; ++y, ++q) {
+                const int x = st.x0 + warp * 32 + lane;
+                float din = 0.f;  // the head's input depth, fetched before the wait
+                if (A.head_w && x < A.w) din = __ldg(A.depth_in + ((size_t)st.img * A.h + y) * A.w + x);
+                const uint32_t a = q % kConvAcc, ka = q / kConvAcc;
+                if (!(ok = pipe_wait(&pp.acc_full[a], ka & 1u, abort, A.err))) break;
                 tc::fence_after_sync();
+                conv_epilogue(A, tmem + a * ncols, warp, lane, st.img, y, st.x0, din);
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&pp.acc_empty[a]);
             }
-            if (worker) {
-                unsigned char *next = halo + (size_t)((y + 2) % kSlots) * slot_bytes;
-                // the copies of row y+2 run while row y-1 is drained
-                if (MODE != SRC_POOL && y + 1 < y1) load_row_async<MODE, CC>(A, next, img, y + 2, x0, tid);
-                if (y > y0) conv_epilogue(A, tmem + ((g - 1) & 1u) * ncols, warp, lane, img, y - 1, x0);
-                if (y + 1 < y1) {
-                    if (MODE == SRC_POOL) load_row<MODE, CC>(A, next, img, y + 2, x0, tid);
-                    else wait_async_rows();
-                }
-            }
-            tc::fence_proxy_async();
-            tc::fence_before_sync();
-            __syncthreads();
+            if (!ok) break;
         }
-        if (failed) break;
-        // last row of the strip
-        bool ok = true;
-        if (worker) {
-            const uint32_t gp = g - 1;
-            ok = tc::mbar_wait(&mbar[gp & 1u], (gp >> 1) & 1u);
-        }
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        tc::fence_after_sync();
-        if (worker) conv_epilogue(A, tmem + ((g - 1) & 1u) * ncols, warp, lane, img, y1 - 1, x0);
-        tc::fence_before_sync();
-        __syncthreads();
-    }
-    if (failed) {
-        if (tid == 0) atomicExch(A.err, 1);
-        // bounded second chance for MMAs still in flight before the TMEM is freed
-        tc::mbar_wait(&mbar[0], 0u);
-        tc::mbar_wait(&mbar[1], 0u);
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 2 * ncols);
+    tc::fence_after_sync();
+    if (warp == kConvMmaWarp) tc::tmem_dealloc(tmem, tcols);
 }
 
 // (mode, input chunks) pairs the network uses: forward c2..c11 and the input
@@ -874,13 +929,6 @@ static uint32_t smem_floor_for_tmem(uint32_t ncols) {
     return kSmemPerSM / (kmax + 1) - 1024u + 16u;
 }
 
-size_t conv_smem_bytes(int cin, int cout) {
-    const int cc = cin / 8;
-    const size_t s = (size_t)kSlots * cc * kHaloW * 16 + (size_t)9 * cc * cout * 16;
-    const size_t fl = smem_floor_for_tmem(2 * tmem_cols(cout));
-    return s > fl ? s : fl;
-}
-
 int prepare_kernels() {
     // allow the largest dynamic shared memory a block may have, once, so that
     // launches (also inside stream capture) make no other runtime call
@@ -898,36 +946,47 @@ int prepare_kernels() {
     return TDE_OK;
 }
 
-int conv_blocks_per_sm(int mode, int cin, int cout, int *out) {
-    // resident blocks per SM from the limits that apply: shared memory (with
-    // the 1 KB the SM reserves per block), registers, and the tensor memory
-    // each block allocates (2 accumulators)
+int conv_plan(int mode, int cin, int cout, ConvPlan *out) {
+    // Two resident blocks per SM when the tensor memory, the registers and the
+    // shared memory allow them at least kConvMinSlots input rows each, else
+    // one; the ring takes as many rows (up to kConvMaxSlots) as then fit.  The
+    // shared memory is padded so that no further block becomes resident.
     const void *fn = conv_kernel_fn(mode, cin / 8);
     if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d input channels", mode, cin);
     cudaFuncAttributes fa;
     TDE_CUDA(cudaFuncGetAttributes(&fa, fn), "refiner: kernel attributes");
-    const size_t per_block = conv_smem_bytes(cin, cout) + fa.sharedSizeBytes + 1024;
-    int n = (int)(kSmemPerSM / per_block);
+    const size_t slot = (size_t)(cin / 8) * kHaloW * 16, wb = (size_t)9 * (cin / 8) * cout * 16;
+    const int by_tmem = (int)(512u / (kConvAcc * tmem_cols(cout)));
     const int by_regs = 65536 / (((fa.numRegs + 7) / 8) * 8 * kConvThreads);
-    const int by_tmem = (int)(512u / (2 * tmem_cols(cout)));
-    n = n < by_regs ? n : by_regs;
-    n = n < by_tmem ? n : by_tmem;
-    if (n < 1) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: cin=%d cout=%d does not fit an SM", cin, cout);
-    *out = n;
-    return TDE_OK;
+    int bps = by_tmem < by_regs ? by_tmem : by_regs;
+    bps = bps > 2 ? 2 : bps;
+    for (; bps >= 1; --bps) {
+        const size_t budget = kSmemPerSM / bps - 1024 - fa.sharedSizeBytes;
+        if (budget < wb + kConvMinSlots * slot) continue;
+        size_t S = (budget - wb) / slot;
+        S = S > (size_t)kConvMaxSlots ? (size_t)kConvMaxSlots : S;
+        size_t smem = S * slot + wb;
+        const size_t floor = kSmemPerSM / (bps + 1) - 1024 - fa.sharedSizeBytes + 16;
+        if (smem < floor) smem = floor;
+        out->per_sm = bps;
+        out->slots = (int)S;
+        out->smem = smem;
+        return TDE_OK;
+    }
+    return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: cin=%d cout=%d does not fit an SM", cin, cout);
 }
 
-int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t s) {
+int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream_t s) {
     const int cin = a.ca + a.cb;
     if (cin % 16 || a.ca % 8 || a.cout % 16 || a.cout < 16 || a.cout > 128 || cin > 128 || a.w <= 0 || a.h <= 0 ||
         a.n <= 0 || (a.head_w && a.cout != 16) || (a.mode_a == SRC_UP && (a.h % 2 || a.w % 2)))
         return set_error(TDE_ERR_INVALID_ARG, "refiner conv: unsupported shape cin=%d cout=%d", cin, a.cout);
-    const size_t smem = conv_smem_bytes(cin, a.cout);
-    if (smem > 227 * 1024 - 256) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: %zu B of shared memory", smem);
+    if (plan.slots < kConvMinSlots || plan.slots > kConvMaxSlots || plan.per_sm < 1 || plan.smem > 227 * 1024 - 256)
+        return set_error(TDE_ERR_INVALID_ARG, "refiner conv: bad launch plan");
     // rows per block: as many as keep every resident block busy
     const int tiles_x = (a.w + kTileM - 1) / kTileM;
     const long row_tiles = (long)a.n * a.h * tiles_x;
-    const long slots = (long)num_sms * blocks_per_sm;
+    const long slots = (long)num_sms * plan.per_sm;
     int rows = (int)(row_tiles / slots);
     rows = rows < 1 ? 1 : rows > 64 ? 64 : rows;
     const long items = (long)a.n * tiles_x * ((a.h + rows - 1) / rows);
@@ -935,7 +994,7 @@ int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t 
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kConvThreads);
-    cfg.dynamicSmemBytes = smem;
+    cfg.dynamicSmemBytes = plan.smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -944,7 +1003,8 @@ int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t 
     cfg.numAttrs = 1;
     const void *fn = conv_kernel_fn(a.mode_a, cin / 8);
     if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d input channels", a.mode_a, cin);
-    void *args[] = {(void *)&a, (void *)&rows};
+    int S = plan.slots;
+    void *args[] = {(void *)&a, (void *)&rows, (void *)&S};
     cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "refiner conv: %s", cudaGetErrorString(e));
     return check_launch("refiner conv");

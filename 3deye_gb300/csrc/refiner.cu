@@ -114,7 +114,7 @@ struct tde_refiner {
     bf16 *gr[GRAD_COUNT] = {};
     float *wpartial = nullptr;
     int wg_blocks = 0;
-    int fwd_per_sm[kConvs] = {}, bwd_per_sm[kConvs] = {};  // resident conv blocks per SM
+    ConvPlan fwd_plan[kConvs] = {}, bwd_plan[kConvs] = {};  // launch geometry per convolution
     float *in_partial = nullptr;
     float *loss_partial = nullptr;
     double *loss2 = nullptr;
@@ -172,7 +172,7 @@ int forward(tde_refiner *r, const uint16_t *raw, int n, uint16_t *out_mm, cudaSt
             a.depth_out = r->out_m;
             a.depth_mm = out_mm;
         }
-        TDE_TRY(launch_conv(a, r->fwd_per_sm[i], r->num_sms, s));
+        TDE_TRY(launch_conv(a, r->fwd_plan[i], r->num_sms, s));
     }
     r->last_batch = n;
     return TDE_OK;
@@ -205,7 +205,7 @@ int loss_grad(tde_refiner *r, const uint16_t *raw, const uint16_t *target, int n
         a.mask = k.mask >= 0 ? r->act[k.mask] : nullptr;
         a.n = n; a.h = h; a.w = w;
         a.err = r->err;
-        TDE_TRY(launch_conv(a, r->bwd_per_sm[i], r->num_sms, s));
+        TDE_TRY(launch_conv(a, r->bwd_plan[i], r->num_sms, s));
         if (k.post == POST_UP)
             TDE_TRY(launch_up_back(r->gr[k.gx], cin, c.ca, r->act[c.a], r->gr[k.post_out], n, h, w, s));
         else if (k.post == POST_POOL)
@@ -240,8 +240,8 @@ int tde_refiner_create(int max_batch, int rows, int cols, uint64_t seed, tde_ref
     st = prepare_kernels();
     for (int i = 0; i < kConvs && !st; ++i) {
         const int cin = kConv[i].ca + kConv[i].cb;
-        st = conv_blocks_per_sm(kConv[i].mode, cin, kConv[i].cout, &r->fwd_per_sm[i]);
-        if (!st) st = conv_blocks_per_sm(SRC_DIRECT, kConv[i].cout, cin, &r->bwd_per_sm[i]);
+        st = conv_plan(kConv[i].mode, cin, kConv[i].cout, &r->fwd_plan[i]);
+        if (!st) st = conv_plan(SRC_DIRECT, kConv[i].cout, cin, &r->bwd_plan[i]);
     }
     if (st) {
         delete r;

@@ -55,10 +55,15 @@ struct WgradArgs {
 
 // Once per process and device, before any launch: shared-memory limits.
 int prepare_kernels();
-size_t conv_smem_bytes(int cin, int cout);
-int conv_blocks_per_sm(int mode, int cin, int cout, int *out);
+// Launch geometry of one convolution shape, fixed once: resident blocks per
+// SM, input rows in each block's ring, dynamic shared memory per block.
+struct ConvPlan {
+    int per_sm, slots;
+    size_t smem;
+};
+int conv_plan(int mode, int cin, int cout, ConvPlan *out);
 // Launches only (no other runtime call), so it may be stream-captured.
-int launch_conv(const ConvArgs &a, int blocks_per_sm, int num_sms, cudaStream_t s);
+int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream_t s);
 int wgrad_blocks(int num_sms, int cin, int cout);
 size_t wgrad_partial_floats(int blocks, int cin, int cout);
 int launch_wgrad(const WgradArgs &a, int blocks, cudaStream_t s);
