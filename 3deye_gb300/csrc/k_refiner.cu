@@ -185,56 +185,41 @@ __device__ __forceinline__ const bf16 *chunk_ptr(const ConvArgs &A, int img, int
     return A.b + (((size_t)img * A.h + y) * A.w + x) * A.cb + 8 * (c - cca);
 }
 
-// One warp loads input row y (halo pixels x0-1 .. x0+128, CC chunks) into a
-// slot as planes: 16-byte copies, zero outside the image; complete (and made
-// visible to the tensor core) when it returns.
+// One warp starts the copies of input row y (halo pixels x0-1 .. x0+128, CC
+// chunks) into a slot as planes: 16-byte cp.async, zero outside the image,
+// one commit group per row.
 template <int MODE, int CC>
-__device__ __forceinline__ void warp_load_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int lane) {
+__device__ __forceinline__ void warp_issue_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int lane) {
     constexpr int n = kHaloW * CC;
-    if (MODE == SRC_POOL) {
-        constexpr int G = 4;
-        for (int base = lane; base < n; base += 32 * G) {
-            uint4 v[G];
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                const int i = base + 32 * g;
-                v[g] = make_uint4(0u, 0u, 0u, 0u);
-                if (i < n) v[g] = load_input_chunk<MODE>(A, img, y, x0 + i / CC - 1, i % CC);
-            }
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                const int i = base + 32 * g;
-                if (i < n) *reinterpret_cast<uint4 *>(slot + ((size_t)(i % CC) * kHaloW + i / CC) * 16) = v[g];
-            }
-        }
-    } else {
-        for (int i = lane; i < n; i += 32) {
-            const int c = i % CC, px = i / CC;
-            const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
-            const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
-            const int bytes = src ? 16 : 0;
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src ? src : A.a),
-                         "r"(bytes)
-                         : "memory");
-        }
-        asm volatile("cp.async.wait_all;" ::: "memory");
+    for (int i = lane; i < n; i += 32) {
+        const int c = i % CC, px = i / CC;
+        const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
+        const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
+        const int bytes = src ? 16 : 0;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src ? src : A.a), "r"(bytes)
+                     : "memory");
     }
-    tc::fence_proxy_async();
-    __syncwarp();
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 // Epilogue of one output row for one pixel (TMEM lane quarter of this warp).
+// With a pooled output, `keep` holds the row's bf16 results when y is even;
+// at the odd row below it the 2x2 maximum (the row pair in registers, the
+// pixel pair across lanes x and x ^ 1) goes to pool_out -- the same bits as
+// a max pool of the stored rows.
+constexpr int kPoolMaxChunks = 8;  // pooled outputs have at most 64 channels
 __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, int quarter, int lane, int img, int y,
-                                              int x0, float depth_in) {
+                                              int x0, float depth_in, uint4 (&keep)[kPoolMaxChunks]) {
     const int m = quarter * 32 + lane;
     const int x = x0 + m;
     const bool valid = x < A.w;
     const size_t pix = ((size_t)img * A.h + y) * A.w + (valid ? x : 0);
+    const bool pool_row = A.pool_out && (y & 1);
+    const size_t ppix = ((size_t)img * (A.h >> 1) + (y >> 1)) * (A.w >> 1) + (valid ? (x >> 1) : 0);
     float r = 0.f;
     for (int j = 0; j < A.cout; j += 16) {
         float v[16];
         tc::tmem_ld16(tacc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)j, v);
-        if (!valid) continue;
         if (A.bias) {
 #pragma unroll
             for (int k = 0; k < 16; ++k) v[k] += __ldg(A.bias + j + k);
@@ -251,10 +236,31 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
             for (int k = 0; k < 16; ++k) v[k] = mk[k] > 0.f ? v[k] : 0.f;
         }
         const uint4 q0 = pack8(v), q1 = pack8(v + 8);
-        uint4 *o = reinterpret_cast<uint4 *>(A.out + pix * A.cout + j);
-        o[0] = q0;
-        o[1] = q1;
-        if (A.head_w) {
+        if (valid) {
+            uint4 *o = reinterpret_cast<uint4 *>(A.out + pix * A.cout + j);
+            o[0] = q0;
+            o[1] = q1;
+        }
+        if (A.pool_out) {
+            const int c = j >> 3;
+            if (!pool_row) {
+                keep[c] = q0;
+                keep[c + 1] = q1;
+            } else {
+                uint4 p0 = bmax4(keep[c], q0), p1 = bmax4(keep[c + 1], q1);
+                uint4 n0, n1;
+                n0.x = __shfl_xor_sync(0xffffffffu, p0.x, 1); n0.y = __shfl_xor_sync(0xffffffffu, p0.y, 1);
+                n0.z = __shfl_xor_sync(0xffffffffu, p0.z, 1); n0.w = __shfl_xor_sync(0xffffffffu, p0.w, 1);
+                n1.x = __shfl_xor_sync(0xffffffffu, p1.x, 1); n1.y = __shfl_xor_sync(0xffffffffu, p1.y, 1);
+                n1.z = __shfl_xor_sync(0xffffffffu, p1.z, 1); n1.w = __shfl_xor_sync(0xffffffffu, p1.w, 1);
+                if (valid && !(x & 1)) {
+                    uint4 *o = reinterpret_cast<uint4 *>(A.pool_out + ppix * A.cout + j);
+                    o[0] = bmax4(p0, n0);
+                    o[1] = bmax4(p1, n1);
+                }
+            }
+        }
+        if (A.head_w && valid) {
             float f[16];
             unpack8(q0, f);
             unpack8(q1, f + 8);
@@ -322,20 +328,40 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     const int items = A.n * tiles_x * ((A.h + rows_per_item - 1) / rows_per_item);
 
     if (warp >= kConvEpiWarps && warp < kConvMmaWarp) {
-        // ---- producers ----
+        // ---- producers: warp pw loads the input rows j = pw (mod 4), two in
+        // flight; a row is marked full once its copies have landed ----
         const int pw = warp - kConvEpiWarps;
-        uint32_t j = 0;  // this block's input-row sequence
-        for (int item = blockIdx.x; item < items && !*abort; item += gridDim.x) {
+        uint32_t j = 0;                  // this block's input-row sequence
+        int pending = -1;                // slot of the row issued before the current one
+        bool ok = true;
+        auto publish = [&](int wait_groups) {
+            if (pending < 0) return;
+            if (wait_groups) asm volatile("cp.async.wait_group 1;" ::: "memory");
+            else asm volatile("cp.async.wait_group 0;" ::: "memory");
+            tc::fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&pp.full[pending]);
+            pending = -1;
+        };
+        for (int item = blockIdx.x; item < items && ok && !*abort; item += gridDim.x) {
             const Strip st = strip_of(A, item, rows_per_item);
             const int nin = st.y1 - st.y0 + 2;
             for (int i = 0; i < nin; ++i, ++j) {
                 if ((int)(j & 3u) != pw) continue;
                 const uint32_t s = j % (uint32_t)S, k = j / (uint32_t)S;
-                if (k > 0 && !pipe_wait(&pp.empty[s], (k - 1) & 1u, abort, A.err)) break;
-                warp_load_row<MODE, CC>(A, halo + (size_t)s * slot_bytes, st.img, st.y0 - 1 + i, st.x0, lane);
-                if (lane == 0) mbar_arrive(&pp.full[s]);
+                if (k > 0) {
+                    // the MMA that frees this slot reads input rows up to
+                    // j - S + 2; when that reaches this warp's previous row
+                    // (j - 4, S <= 6), publish it before waiting
+                    if (S <= 6) publish(0);
+                    if (!(ok = pipe_wait(&pp.empty[s], (k - 1) & 1u, abort, A.err))) break;
+                }
+                warp_issue_row<MODE, CC>(A, halo + (size_t)s * slot_bytes, st.img, st.y0 - 1 + i, st.x0, lane);
+                publish(1);  // the previous row of this warp, while this one is in flight
+                pending = (int)s;
             }
         }
+        publish(0);
         asm volatile("cp.async.wait_all;" ::: "memory");
     } else if (warp == kConvMmaWarp) {
         // ---- MMA issuer ----
@@ -391,6 +417,7 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     } else {
         // ---- epilogue: warp q drains TMEM lanes 32q .. 32q + 31 ----
         uint32_t q = 0;
+        uint4 keep[kPoolMaxChunks];
         for (int item = blockIdx.x; item < items && !*abort; item += gridDim.x) {
             const Strip st = strip_of(A, item, rows_per_item);
             bool ok = true;
@@ -401,7 +428,7 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
                 const uint32_t a = q % kConvAcc, ka = q / kConvAcc;
                 if (!(ok = pipe_wait(&pp.acc_full[a], ka & 1u, abort, A.err))) break;
                 tc::fence_after_sync();
-                conv_epilogue(A, tmem + a * ncols, warp, lane, st.img, y, st.x0, din);
+                conv_epilogue(A, tmem + a * ncols, warp, lane, st.img, y, st.x0, din, keep);
                 tc::fence_before_sync();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&pp.acc_empty[a]);
@@ -415,11 +442,11 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
     if (warp == kConvMmaWarp) tc::tmem_dealloc(tmem, tcols);
 }
 
-// (mode, input chunks) pairs the network uses: forward c2..c11 and the input
-// gradients of c2..c11 (direct sources with cout/8 chunks)
+// (mode, input chunks) pairs the network uses: forward c2..c11 (the encoder's
+// pooled inputs come precomputed from the epilogue of the layer before) and
+// the input gradients of c2..c11 (direct sources with cout/8 chunks)
 #define TDE_CONV_VARIANTS(X) \
     X(SRC_DIRECT, 2) X(SRC_DIRECT, 4) X(SRC_DIRECT, 6) X(SRC_DIRECT, 8) \
-    X(SRC_POOL, 2) X(SRC_POOL, 4) X(SRC_POOL, 6) \
     X(SRC_UP, 6) X(SRC_UP, 10) X(SRC_UP, 14)
 
 const void *conv_kernel_fn(int mode, int cc) {
@@ -979,7 +1006,8 @@ int conv_plan(int mode, int cin, int cout, ConvPlan *out) {
 int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream_t s) {
     const int cin = a.ca + a.cb;
     if (cin % 16 || a.ca % 8 || a.cout % 16 || a.cout < 16 || a.cout > 128 || cin > 128 || a.w <= 0 || a.h <= 0 ||
-        a.n <= 0 || (a.head_w && a.cout != 16) || (a.mode_a == SRC_UP && (a.h % 2 || a.w % 2)))
+        a.n <= 0 || (a.head_w && a.cout != 16) || (a.mode_a == SRC_UP && (a.h % 2 || a.w % 2)) ||
+        (a.pool_out && (a.h % 2 || a.w % 2 || a.cout > 8 * kPoolMaxChunks)))
         return set_error(TDE_ERR_INVALID_ARG, "refiner conv: unsupported shape cin=%d cout=%d", cin, a.cout);
     if (plan.slots < kConvMinSlots || plan.slots > kConvMaxSlots || plan.per_sm < 1 || plan.smem > 227 * 1024 - 256)
         return set_error(TDE_ERR_INVALID_ARG, "refiner conv: bad launch plan");
@@ -987,8 +1015,11 @@ int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream
     const int tiles_x = (a.w + kTileM - 1) / kTileM;
     const long row_tiles = (long)a.n * a.h * tiles_x;
     const long slots = (long)num_sms * plan.per_sm;
-    int rows = (int)(row_tiles / slots);
+    // rows per strip: enough that the strips do not outnumber the resident
+    // blocks (no second wave), even when the epilogue pools row pairs
+    int rows = (int)((row_tiles + slots - 1) / slots);
     rows = rows < 1 ? 1 : rows > 64 ? 64 : rows;
+    if (a.pool_out) rows += rows & 1;
     const long items = (long)a.n * tiles_x * ((a.h + rows - 1) / rows);
     const int grid = (int)(items < slots ? items : slots);
     cudaLaunchConfig_t cfg = {};

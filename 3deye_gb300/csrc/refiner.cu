@@ -28,21 +28,28 @@ const TensorSpec kAct[ACT_COUNT] = {{0, 16}, {0, 16}, {1, 32}, {1, 32}, {2, 48},
 const TensorSpec kGrad[GRAD_COUNT] = {{0, 16}, {0, 48}, {1, 32}, {1, 80}, {2, 48}, {2, 112}, {3, 64}, {3, 64}, {3, 48},
                                       {2, 48}, {2, 48}, {2, 32}, {1, 32}, {1, 32}, {1, 16}, {0, 16}, {0, 16}};
 
-// Convolutions c2..c11 (c1 is the FP32 input convolution).
-struct Conv { int level, a, ca, mode, b, cb, cout, out; };
+// Convolutions c2..c11 (c1 is the FP32 input convolution).  The encoder's
+// 2x2 max pools are written by the epilogues of c2, c4 and c6 (pool_out: the
+// pooled copy of `out`) and read directly by c3, c5 and c7 (pool_in: source
+// A is that copy; `a` still names the unpooled tensor, whose argmax routes
+// the pool's gradient).
+struct Conv { int level, a, ca, mode, b, cb, cout, out, pool_in, pool_out; };
 constexpr int kConvs = 10;
+constexpr int kPools = 3;
 const Conv kConv[kConvs] = {
-    {0, E0A, 16, SRC_DIRECT, -1, 0, 16, E0},  // c2
-    {1, E0, 16, SRC_POOL, -1, 0, 32, E1A},    // c3
-    {1, E1A, 32, SRC_DIRECT, -1, 0, 32, E1},  // c4
-    {2, E1, 32, SRC_POOL, -1, 0, 48, E2A},    // c5
-    {2, E2A, 48, SRC_DIRECT, -1, 0, 48, E2},  // c6
-    {3, E2, 48, SRC_POOL, -1, 0, 64, B3A},    // c7
-    {3, B3A, 64, SRC_DIRECT, -1, 0, 64, B3},  // c8
-    {2, B3, 64, SRC_UP, E2, 48, 48, D2},      // c9
-    {1, D2, 48, SRC_UP, E1, 32, 32, D1},      // c10
-    {0, D1, 32, SRC_UP, E0, 16, 16, D0},      // c11
+    {0, E0A, 16, SRC_DIRECT, -1, 0, 16, E0, -1, 0},   // c2 (+ pool of e0)
+    {1, E0, 16, SRC_POOL, -1, 0, 32, E1A, 0, -1},     // c3
+    {1, E1A, 32, SRC_DIRECT, -1, 0, 32, E1, -1, 1},   // c4 (+ pool of e1)
+    {2, E1, 32, SRC_POOL, -1, 0, 48, E2A, 1, -1},     // c5
+    {2, E2A, 48, SRC_DIRECT, -1, 0, 48, E2, -1, 2},   // c6 (+ pool of e2)
+    {3, E2, 48, SRC_POOL, -1, 0, 64, B3A, 2, -1},     // c7
+    {3, B3A, 64, SRC_DIRECT, -1, 0, 64, B3, -1, -1},  // c8
+    {2, B3, 64, SRC_UP, E2, 48, 48, D2, -1, -1},      // c9
+    {1, D2, 48, SRC_UP, E1, 32, 32, D1, -1, -1},      // c10
+    {0, D1, 32, SRC_UP, E0, 16, 16, D0, -1, -1},      // c11
 };
+// The convolution kernel's source mode for conv i: the pooled inputs are read directly.
+inline int conv_mode(const Conv &c) { return c.pool_in >= 0 ? (int)SRC_DIRECT : c.mode; }
 
 // Backward routing of conv i: its output gradient dz, the buffer its input
 // gradient goes to (masked by `mask` when the input is a ReLU output read
@@ -111,6 +118,7 @@ struct tde_refiner {
     bf16 *wq = nullptr, *wt = nullptr;
     float *depth_m = nullptr, *out_m = nullptr;
     bf16 *act[ACT_COUNT] = {};
+    bf16 *pooled[kPools] = {};  // 2x2 max pools of e0, e1, e2 (levels 1, 2, 3)
     bf16 *gr[GRAD_COUNT] = {};
     float *wpartial = nullptr;
     int wg_blocks = 0;
@@ -158,11 +166,12 @@ int forward(tde_refiner *r, const uint16_t *raw, int n, uint16_t *out_mm, cudaSt
         const Conv &c = kConv[i];
         ConvArgs a;
         std::memset(&a, 0, sizeof(a));
-        a.a = r->act[c.a]; a.ca = c.ca; a.mode_a = c.mode;
+        a.a = c.pool_in >= 0 ? r->pooled[c.pool_in] : r->act[c.a]; a.ca = c.ca; a.mode_a = conv_mode(c);
         a.b = c.b >= 0 ? r->act[c.b] : nullptr; a.cb = c.cb;
         a.wgt = r->wq + kL.wq[i];
         a.bias = r->theta + kL.b[i];
         a.out = r->act[c.out]; a.cout = c.cout; a.relu = 1;
+        a.pool_out = c.pool_out >= 0 ? r->pooled[c.pool_out] : nullptr;
         a.n = n; a.h = r->rows >> c.level; a.w = r->cols >> c.level;
         a.err = r->err;
         if (i == kConvs - 1) {
@@ -189,7 +198,7 @@ int loss_grad(tde_refiner *r, const uint16_t *raw, const uint16_t *target, int n
         const int cin = c.ca + c.cb, h = H >> c.level, w = W >> c.level;
         WgradArgs wa;
         std::memset(&wa, 0, sizeof(wa));
-        wa.a = r->act[c.a]; wa.ca = c.ca; wa.mode_a = c.mode;
+        wa.a = c.pool_in >= 0 ? r->pooled[c.pool_in] : r->act[c.a]; wa.ca = c.ca; wa.mode_a = conv_mode(c);
         wa.b = c.b >= 0 ? r->act[c.b] : nullptr; wa.cb = c.cb;
         wa.dz = r->gr[k.dz]; wa.cout = c.cout;
         wa.n = n; wa.h = h; wa.w = w;
@@ -240,7 +249,7 @@ int tde_refiner_create(int max_batch, int rows, int cols, uint64_t seed, tde_ref
     st = prepare_kernels();
     for (int i = 0; i < kConvs && !st; ++i) {
         const int cin = kConv[i].ca + kConv[i].cb;
-        st = conv_plan(kConv[i].mode, cin, kConv[i].cout, &r->fwd_plan[i]);
+        st = conv_plan(conv_mode(kConv[i]), cin, kConv[i].cout, &r->fwd_plan[i]);
         if (!st) st = conv_plan(SRC_DIRECT, kConv[i].cout, cin, &r->bwd_plan[i]);
     }
     if (st) {
@@ -264,6 +273,10 @@ int tde_refiner_create(int max_batch, int rows, int cols, uint64_t seed, tde_ref
             break;
         for (int i = 0; i < ACT_COUNT && !st; ++i)
             st = dalloc(r, &r->act[i], pixels(r, max_batch, kAct[i].level) * kAct[i].ch);
+        for (int i = 0; i < kConvs && !st; ++i)
+            if (kConv[i].pool_out >= 0)
+                st = dalloc(r, &r->pooled[kConv[i].pool_out],
+                            pixels(r, max_batch, kConv[i].level + 1) * kConv[i].cout);
         for (int i = 0; i < GRAD_COUNT && !st; ++i)
             st = dalloc(r, &r->gr[i], pixels(r, max_batch, kGrad[i].level) * kGrad[i].ch);
     } while (0);

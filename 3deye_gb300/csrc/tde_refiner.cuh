@@ -36,6 +36,9 @@ struct ConvArgs {
     uint16_t *depth_mm;   // may be null: the same depth in mm, rounded, clamped to [0, 32767]
     int n, h, w;
     int *err;  // set to 1 when a wait on the tensor core timed out
+    // optional: the 2x2 max pool of `out` ([n][h/2][w/2][cout]), written by
+    // the same epilogue (h and w even)
+    bf16 *pool_out;
 };
 
 // Weight gradient of the same convolution: partial[blk][r][co] with rows

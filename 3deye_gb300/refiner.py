@@ -44,6 +44,19 @@ LEVELS = {"e0a": 0, "e0": 0, "e1a": 1, "e1": 1, "e2a": 2, "e2": 2, "b3a": 3, "b3
           "dz5": 2, "gp2": 2, "dz4": 1, "dz3": 1, "gp1": 1, "dz2": 0, "dz1": 0}
 
 
+# The tensor-core convolutions c2..c11: (pyramid level, input channels, output channels).
+CONVS = [(0, 16, 16), (1, 16, 32), (1, 32, 32), (2, 32, 48), (2, 48, 48), (3, 48, 64), (3, 64, 64), (2, 112, 48),
+         (1, 80, 32), (0, 48, 16)]
+
+
+def conv_flops(rows: int, cols: int, batch: int = 1, train: bool = False) -> int:
+    """Multiply-add FLOPs (2 per MAC) of the tensor-core convolutions of one
+    forward pass, or of a training step (forward, input gradients and weight
+    gradients: three times as many)."""
+    f = sum(2 * (rows >> l) * (cols >> l) * 9 * ci * co for l, ci, co in CONVS) * batch
+    return 3 * f if train else f
+
+
 def param_count() -> int:
     return int(lib.tde_refiner_param_count())
 

@@ -214,6 +214,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def load_peaks_bf16():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"burst": float(d["bf16_tflops"]), "sustained": float(d["bf16_tflops_sustained"]), "kind": "measured"}
+    return {"burst": 1900.0, "sustained": 1700.0, "kind": "fallback"}
+
+
 def load_traffic():
     """DRAM bytes per integration launch from the committed ncu summary."""
     p = ROOT / "profiles" / "integrate_c2_traffic.json"
@@ -653,14 +661,53 @@ def run_ours(args, ws, rank, local):
         l_ms = max_over_ranks(ws, g0.elapsed_time(g1))
         l_launches = lp.launches_per_frame()
         lp.close()
+        # the refiner alone: batch-1 forward passes over the same frames, and
+        # batch-16 training steps (raw frames against later frames as
+        # targets: the timing does not depend on the values)
+        out_mm = torch.empty((cfg.rows, cfg.cols), dtype=torch.uint16, device=dev)
+        rs = torch.cuda.Stream(dev)
+        for i in range(W):
+            R.forward_ptr(base + i * fbytes, 1, out_mm.data_ptr(), 0, rs.cuda_stream)
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        rs.synchronize()
+        r0.record(rs)
+        for i in range(W, n):
+            R.forward_ptr(base + i * fbytes, 1, out_mm.data_ptr(), 0, rs.cuda_stream)
+        r1.record(rs)
+        rs.synchronize()
+        fwd_ms = r0.elapsed_time(r1) / K
         if R.status() != 0:
             raise RuntimeError("refiner: a tensor-core wait timed out")
         R.close()
+        B = min(16, n // 2)
+        T = rf.Refiner(B, cfg.rows, cfg.cols)
+        T.set_params(np.fromfile(wpath, dtype=np.float32))
+        for _ in range(3):
+            T.train_step_ptr(base, base + B * fbytes, B, 1e-5, rs.cuda_stream)
+        steps = 5
+        r0.record(rs)
+        for _ in range(steps):
+            T.train_step_ptr(base, base + B * fbytes, B, 1e-5, rs.cuda_stream)
+        r1.record(rs)
+        rs.synchronize()
+        train_ms = r0.elapsed_time(r1) / steps
+        if T.status() != 0:
+            raise RuntimeError("refiner: a tensor-core wait timed out")
+        T.close()
+        fwd_flops, train_flops = rf.conv_flops(cfg.rows, cfg.cols), rf.conv_flops(cfg.rows, cfg.cols, B, True)
         lest = lposes.numpy().copy()
         learned = {"value": round(ws * K / (l_ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(l_ms / K, 5),
                    "ate_m": {"vs_ground_truth": round(pl.ate_rmse(lest, traj), 6),
                              "frames_tracking_lost": int((lstat.numpy() != 0).sum())},
                    "gpu_launches": l_launches * K, "weights": wpath.name,
+                   "refiner_alone": {
+                       "forward_ms_batch1": round(fwd_ms, 5),
+                       "forward_tflops": round(fwd_flops / (fwd_ms * 1e-3) / 1e12, 1),
+                       f"train_step_ms_batch{B}": round(train_ms, 4),
+                       "train_tflops": round(train_flops / (train_ms * 1e-3) / 1e12, 1),
+                       "peak_bf16_tflops": load_peaks_bf16(),
+                       "note": "tensor-core convolution FLOPs (2 per multiply-add) over CUDA-event time on one "
+                               "stream; training = forward + input gradients + weight gradients + AdamW"},
                    "note": "bf16 U-Net (tcgen05 implicit-GEMM convolutions) replaces the bilateral filter; "
                            "frames resident in HBM, same sequence as the plain line"}
 
