@@ -141,7 +141,8 @@ struct ConvPipe {
 __device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort, int *err) {
     if (tc::mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = tc::globaltimer_ns();
-    while (!tc::mbar_try_wait(bar, parity)) {
+    // sleeping waits (up to 20 us each) leave the issue slots to the working warps
+    while (!tc::mbar_try_wait_sleep(bar, parity, 20000u)) {
         if (*abort) return false;
         if (tc::globaltimer_ns() - t0 > kConvWaitNs) {
             *abort = 1;
@@ -168,36 +169,38 @@ __device__ __forceinline__ Strip strip_of(const ConvArgs &A, int item, int rows_
     return s;
 }
 
-// Address of chunk c of the concatenated input at (img, y, x) for a source
-// that needs no arithmetic (direct or nearest-upsampled A, or B); null
-// outside the image.
-template <int MODE>
-__device__ __forceinline__ const bf16 *chunk_ptr(const ConvArgs &A, int img, int y, int x, int c) {
-    if (y < 0 || y >= A.h || x < 0 || x >= A.w) return nullptr;
-    const int cca = A.ca >> 3;
-    if (c < cca) {
-        if (MODE == SRC_UP) {
-            const int hh = A.h >> 1, ww = A.w >> 1;
-            return A.a + (((size_t)img * hh + (y >> 1)) * ww + (x >> 1)) * A.ca + 8 * c;
-        }
-        return A.a + (((size_t)img * A.h + y) * A.w + x) * A.ca + 8 * c;
-    }
-    return A.b + (((size_t)img * A.h + y) * A.w + x) * A.cb + 8 * (c - cca);
-}
-
-// One warp starts the copies of input row y (halo pixels x0-1 .. x0+128, CC
-// chunks) into a slot as planes: 16-byte cp.async, zero outside the image,
-// one commit group per row.
-template <int MODE, int CC>
-__device__ __forceinline__ void warp_issue_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int lane) {
-    constexpr int n = kHaloW * CC;
-    for (int i = lane; i < n; i += 32) {
-        const int c = i % CC, px = i / CC;
-        const bf16 *src = chunk_ptr<MODE>(A, img, y, x0 + px - 1, c);
-        const uint32_t dst = tc::smem_u32(slot + ((size_t)c * kHaloW + px) * 16);
-        const int bytes = src ? 16 : 0;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src ? src : A.a), "r"(bytes)
+// One warp starts the copies of input row y (halo pixels x0-1 .. x0+128) into
+// a slot as planes: CCA chunks of source A (read directly, or through the
+// nearest 2x upsample of an h/2 x w/2 tensor), then CCB chunks of source B;
+// 16-byte cp.async, zero outside the image; one commit group per row.
+// Consecutive lanes copy consecutive 16-byte pieces of a source row.
+template <int CP, bool UPS>
+__device__ __forceinline__ void warp_copy_part(const bf16 *row, int px_elems, int w, int x_start, int plane0, bool row_in,
+                                               unsigned char *slot, const bf16 *dummy, int lane) {
+    for (int i = lane; i < kHaloW * CP; i += 32) {
+        const int px = i / CP, c = i - px * CP;
+        const int x = x_start + px;
+        const bool in = row_in && (unsigned)x < (unsigned)w;
+        const bf16 *src = in ? row + (size_t)(UPS ? (x >> 1) : x) * px_elems + 8 * c : dummy;
+        const uint32_t dst = tc::smem_u32(slot + ((size_t)(plane0 + c) * kHaloW + px) * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(in ? 16 : 0)
                      : "memory");
+    }
+}
+template <int MODE, int CCA, int CCB>
+__device__ __forceinline__ void warp_issue_row(const ConvArgs &A, unsigned char *slot, int img, int y, int x0, int lane) {
+    const bool row_in = y >= 0 && y < A.h;
+    const int yc = row_in ? y : 0;
+    if (MODE == SRC_UP) {
+        const bf16 *ra = A.a + (((size_t)img * (A.h >> 1) + (yc >> 1)) * (A.w >> 1)) * A.ca;
+        warp_copy_part<CCA, true>(ra, A.ca, A.w, x0 - 1, 0, row_in, slot, A.a, lane);
+    } else {
+        const bf16 *ra = A.a + (((size_t)img * A.h + yc) * A.w) * A.ca;
+        warp_copy_part<CCA, false>(ra, A.ca, A.w, x0 - 1, 0, row_in, slot, A.a, lane);
+    }
+    if (CCB > 0) {
+        const bf16 *rb = A.b + (((size_t)img * A.h + yc) * A.w) * A.cb;
+        warp_copy_part<CCB, false>(rb, A.cb, A.w, x0 - 1, CCA, row_in, slot, A.a, lane);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -209,7 +212,8 @@ __device__ __forceinline__ void warp_issue_row(const ConvArgs &A, unsigned char 
 // a max pool of the stored rows.
 constexpr int kPoolMaxChunks = 8;  // pooled outputs have at most 64 channels
 __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, int quarter, int lane, int img, int y,
-                                              int x0, float depth_in, uint4 (&keep)[kPoolMaxChunks]) {
+                                              int x0, float depth_in, uint4 (&keep)[kPoolMaxChunks],
+                                              const float *s_bias, const float *s_head) {
     const int m = quarter * 32 + lane;
     const int x = x0 + m;
     const bool valid = x < A.w;
@@ -222,7 +226,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
         tc::tmem_ld16(tacc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)j, v);
         if (A.bias) {
 #pragma unroll
-            for (int k = 0; k < 16; ++k) v[k] += __ldg(A.bias + j + k);
+            for (int k = 0; k < 16; ++k) v[k] += s_bias[j + k];
         }
         if (A.relu) {
 #pragma unroll
@@ -265,11 +269,11 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
             unpack8(q0, f);
             unpack8(q1, f + 8);
 #pragma unroll
-            for (int k = 0; k < 16; ++k) r = fmaf(__ldg(A.head_w + j + k), f[k], r);
+            for (int k = 0; k < 16; ++k) r = fmaf(s_head[k], f[k], r);
         }
     }
     if (valid && A.head_w) {
-        const float o = depth_in > 0.f ? depth_in + 0.01f * (r + __ldg(A.head_b)) : 0.f;  // residual in cm
+        const float o = depth_in > 0.f ? depth_in + 0.01f * (r + s_head[16]) : 0.f;  // residual in cm
         if (A.depth_out) A.depth_out[pix] = o;
         if (A.depth_mm) {
             const float mm = fminf(fmaxf(rintf(o * 1000.f), 0.f), (float)TDE_MAX_DEPTH_VALUE);
@@ -278,10 +282,12 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs &A, uint32_t tacc, 
     }
 }
 
-template <int MODE, int CC>
+template <int MODE, int CCA, int CCB>
 __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs A, int rows_per_item, int S) {
+    constexpr int CC = CCA + CCB;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ ConvPipe pp;
+    __shared__ float s_bias[128], s_head[17];  // bias; head weights and head bias
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     constexpr uint32_t slot_bytes = (uint32_t)CC * kHaloW * 16;
     unsigned char *halo = smem;
@@ -306,6 +312,8 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
         tc::mbar_init(&pp.drain, 1);
         pp.abort = 0;
     }
+    if (A.bias && tid < A.cout) s_bias[tid] = A.bias[tid];
+    if (A.head_w && tid < 17) s_head[tid] = tid < 16 ? A.head_w[tid] : A.head_b[0];
     // weights: global [co][t][ci] -> planes (t, chunk) of cout rows x 16 B.
     // No kernel launched right before a convolution writes weights, so they
     // are fetched before waiting for the previous grid.
@@ -356,7 +364,7 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
                     if (S <= 6) publish(0);
                     if (!(ok = pipe_wait(&pp.empty[s], (k - 1) & 1u, abort, A.err))) break;
                 }
-                warp_issue_row<MODE, CC>(A, halo + (size_t)s * slot_bytes, st.img, st.y0 - 1 + i, st.x0, lane);
+                warp_issue_row<MODE, CCA, CCB>(A, halo + (size_t)s * slot_bytes, st.img, st.y0 - 1 + i, st.x0, lane);
                 publish(1);  // the previous row of this warp, while this one is in flight
                 pending = (int)s;
             }
@@ -428,7 +436,7 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
                 const uint32_t a = q % kConvAcc, ka = q / kConvAcc;
                 if (!(ok = pipe_wait(&pp.acc_full[a], ka & 1u, abort, A.err))) break;
                 tc::fence_after_sync();
-                conv_epilogue(A, tmem + a * ncols, warp, lane, st.img, y, st.x0, din, keep);
+                conv_epilogue(A, tmem + a * ncols, warp, lane, st.img, y, st.x0, din, keep, s_bias, s_head);
                 tc::fence_before_sync();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&pp.acc_empty[a]);
@@ -446,12 +454,13 @@ __global__ void __launch_bounds__(kConvThreads) conv3x3_tc_kernel(const ConvArgs
 // pooled inputs come precomputed from the epilogue of the layer before) and
 // the input gradients of c2..c11 (direct sources with cout/8 chunks)
 #define TDE_CONV_VARIANTS(X) \
-    X(SRC_DIRECT, 2) X(SRC_DIRECT, 4) X(SRC_DIRECT, 6) X(SRC_DIRECT, 8) \
-    X(SRC_UP, 6) X(SRC_UP, 10) X(SRC_UP, 14)
+    X(SRC_DIRECT, 2, 0) X(SRC_DIRECT, 4, 0) X(SRC_DIRECT, 6, 0) X(SRC_DIRECT, 8, 0) \
+    X(SRC_UP, 4, 2) X(SRC_UP, 6, 4) X(SRC_UP, 8, 6)
 
-const void *conv_kernel_fn(int mode, int cc) {
-#define TDE_CONV_FN(M, C) \
-    if (mode == M && cc == C) return (const void *)conv3x3_tc_kernel<M, C>;
+// The kernel for a source mode and the input chunks of sources A and B.
+const void *conv_kernel_fn(int mode, int cca, int ccb) {
+#define TDE_CONV_FN(M, A, B) \
+    if (mode == M && cca == A && ccb == B) return (const void *)conv3x3_tc_kernel<M, A, B>;
     TDE_CONV_VARIANTS(TDE_CONV_FN)
 #undef TDE_CONV_FN
     return nullptr;
@@ -960,7 +969,7 @@ int prepare_kernels() {
     // allow the largest dynamic shared memory a block may have, once, so that
     // launches (also inside stream capture) make no other runtime call
     std::vector<const void *> fns = {(const void *)wgrad_tc_kernel};
-#define TDE_CONV_FN(M, C) fns.push_back((const void *)conv3x3_tc_kernel<M, C>);
+#define TDE_CONV_FN(M, A, B) fns.push_back((const void *)conv3x3_tc_kernel<M, A, B>);
     TDE_CONV_VARIANTS(TDE_CONV_FN)
 #undef TDE_CONV_FN
     for (const void *fn : fns) {
@@ -973,13 +982,14 @@ int prepare_kernels() {
     return TDE_OK;
 }
 
-int conv_plan(int mode, int cin, int cout, ConvPlan *out) {
+int conv_plan(int mode, int ca, int cin, int cout, ConvPlan *out) {
     // Two resident blocks per SM when the tensor memory, the registers and the
     // shared memory allow them at least kConvMinSlots input rows each, else
     // one; the ring takes as many rows (up to kConvMaxSlots) as then fit.  The
     // shared memory is padded so that no further block becomes resident.
-    const void *fn = conv_kernel_fn(mode, cin / 8);
-    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d input channels", mode, cin);
+    const void *fn = conv_kernel_fn(mode, ca / 8, (cin - ca) / 8);
+    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d + %d input channels", mode,
+                              ca, cin - ca);
     cudaFuncAttributes fa;
     TDE_CUDA(cudaFuncGetAttributes(&fa, fn), "refiner: kernel attributes");
     const size_t slot = (size_t)(cin / 8) * kHaloW * 16, wb = (size_t)9 * (cin / 8) * cout * 16;
@@ -1032,8 +1042,9 @@ int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const void *fn = conv_kernel_fn(a.mode_a, cin / 8);
-    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d input channels", a.mode_a, cin);
+    const void *fn = conv_kernel_fn(a.mode_a, a.ca / 8, a.cb / 8);
+    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner conv: no kernel for mode %d with %d + %d input channels",
+                              a.mode_a, a.ca, a.cb);
     int S = plan.slots;
     void *args[] = {(void *)&a, (void *)&rows, (void *)&S};
     cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);

@@ -249,8 +249,8 @@ int tde_refiner_create(int max_batch, int rows, int cols, uint64_t seed, tde_ref
     st = prepare_kernels();
     for (int i = 0; i < kConvs && !st; ++i) {
         const int cin = kConv[i].ca + kConv[i].cb;
-        st = conv_plan(conv_mode(kConv[i]), cin, kConv[i].cout, &r->fwd_plan[i]);
-        if (!st) st = conv_plan(SRC_DIRECT, kConv[i].cout, cin, &r->bwd_plan[i]);
+        st = conv_plan(conv_mode(kConv[i]), kConv[i].ca, cin, kConv[i].cout, &r->fwd_plan[i]);
+        if (!st) st = conv_plan(SRC_DIRECT, kConv[i].cout, kConv[i].cout, cin, &r->bwd_plan[i]);
     }
     if (st) {
         delete r;

@@ -64,7 +64,8 @@ struct ConvPlan {
     int per_sm, slots;
     size_t smem;
 };
-int conv_plan(int mode, int cin, int cout, ConvPlan *out);
+// ca of the cin input channels come from source A (the rest from B).
+int conv_plan(int mode, int ca, int cin, int cout, ConvPlan *out);
 // Launches only (no other runtime call), so it may be stream-captured.
 int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream_t s);
 int wgrad_blocks(int num_sms, int cin, int cout);

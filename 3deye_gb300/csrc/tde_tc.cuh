@@ -108,6 +108,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity) {
     return ok != 0;
 }
 
+// As mbar_try_wait, letting the thread sleep up to `hint_ns` nanoseconds for
+// the phase to complete instead of returning at once.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *b, uint32_t parity, uint32_t hint_ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ uint64_t globaltimer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
