@@ -37,7 +37,6 @@ constexpr int kTileM = 128;             // output pixels per MMA tile
 constexpr int kHaloW = kTileM + 2;      // halo pixels per row
 constexpr int kWgK = 64;                // pixels per weight-gradient K step
 constexpr int kWgHalo = kWgK + 2;
-constexpr int kWgThreads = 256;
 constexpr uint32_t kSmemPerSM = 228 * 1024;
 
 __host__ __device__ inline uint32_t tmem_cols(int n) {
@@ -174,15 +173,15 @@ __device__ __forceinline__ Strip strip_of(const ConvArgs &A, int item, int rows_
 // nearest 2x upsample of an h/2 x w/2 tensor), then CCB chunks of source B;
 // 16-byte cp.async, zero outside the image; one commit group per row.
 // Consecutive lanes copy consecutive 16-byte pieces of a source row.
-template <int CP, bool UPS>
+template <int CP, bool UPS, int HALO = kHaloW>
 __device__ __forceinline__ void warp_copy_part(const bf16 *row, int px_elems, int w, int x_start, int plane0, bool row_in,
                                                unsigned char *slot, const bf16 *dummy, int lane) {
-    for (int i = lane; i < kHaloW * CP; i += 32) {
+    for (int i = lane; i < HALO * CP; i += 32) {
         const int px = i / CP, c = i - px * CP;
         const int x = x_start + px;
         const bool in = row_in && (unsigned)x < (unsigned)w;
         const bf16 *src = in ? row + (size_t)(UPS ? (x >> 1) : x) * px_elems + 8 * c : dummy;
-        const uint32_t dst = tc::smem_u32(slot + ((size_t)(plane0 + c) * kHaloW + px) * 16);
+        const uint32_t dst = tc::smem_u32(slot + ((size_t)(plane0 + c) * HALO + px) * 16);
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(in ? 16 : 0)
                      : "memory");
     }
@@ -485,7 +484,7 @@ constexpr int kWgPlaneZ = kWgK * 16;      // 1024 B: one 8-channel plane of dZ
 
 struct WgLayout {
     int cin, cc, mtiles, xplanes, zplanes;
-    uint32_t x_bytes, z_bytes, ones_off, total, tcols;
+    uint32_t x_bytes, z_bytes, tcols;
 };
 __host__ __device__ inline WgLayout wg_layout(int cin, int cout) {
     WgLayout L;
@@ -496,8 +495,6 @@ __host__ __device__ inline WgLayout wg_layout(int cin, int cout) {
     L.zplanes = cout / 8;
     L.x_bytes = (uint32_t)(L.xplanes * kWgPlaneX);
     L.z_bytes = (uint32_t)(L.zplanes * kWgPlaneZ);
-    L.ones_off = 2u * (L.x_bytes + L.z_bytes);        // two staging buffers, then the ones tile
-    L.total = L.ones_off + 16u * 256u;                // 16 chunks x 16 pixels x 16 B
     L.tcols = (uint32_t)(3 * L.mtiles * cout + cout);  // 3 dx x row tiles, + bias
     return L;
 }
@@ -507,115 +504,148 @@ __host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) {
     return tc::idesc_bf16(M, N) | (1u << 15) | (1u << 16);
 }
 
-__global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs A) {
+// Pipelined form: a block owns K steps k = blockIdx.x, + gridDim.x, ... (one
+// 64-pixel segment of one row each).  Up to 8 producer warps stage step k --
+// X over 3 rows x 66 halo pixels and dZ over 64 pixels, as planes, with
+// cp.async -- into ring stage k % S once the tensor core has released it
+// (step k - S done), warp k % min(S, 8) taking step k; warp 8, one lane, issues each
+// step's MMAs into the block's accumulators (3 dx x row tiles + the bias
+// column block), which stay in tensor memory across all the block's steps,
+// and commits them to the stage's "empty" barrier.  At the end every warp
+// drains the accumulators into the block's partial.  Bounded waits as in the
+// convolution: a timeout raises A.err and the block leaves cleanly.
+constexpr int kWgProdWarps = 8;
+constexpr int kWgThreadsP = 32 * (kWgProdWarps + 1);
+constexpr int kWgMaxStages = 8;
+struct WgPipe {
+    uint64_t full[kWgMaxStages], empty[kWgMaxStages], drain;
+    uint32_t tmem;
+    int abort;
+};
+
+template <int MODE, int CCA, int CCB>
+__global__ void __launch_bounds__(kWgThreadsP) wgrad_tc_kernel(const WgradArgs A, int S) {
+    constexpr int CC = CCA + CCB;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ uint32_t tmem_slot;
+    __shared__ WgPipe pp;
     const int cin = A.ca + A.cb, cout = A.cout;
     const WgLayout L = wg_layout(cin, cout);
-    const int cc = L.cc;
+    const int zc = cout / 8;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t ncols = tmem_cols((int)L.tcols);
-    unsigned char *ones = smem + L.ones_off;
+    const uint32_t stage_bytes = L.x_bytes + L.z_bytes;
+    unsigned char *ones = smem + (size_t)S * stage_bytes;
+    volatile int *abort = &pp.abort;
 
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
+    if (warp == kWgProdWarps) tc::tmem_alloc(&pp.tmem, ncols);
     if (tid == 0) {
-        tc::mbar_init(&mbar[0], 1);
-        tc::mbar_init(&mbar[1], 1);
+        for (int s = 0; s < kWgMaxStages; ++s) {
+            tc::mbar_init(&pp.full[s], 1);
+            tc::mbar_init(&pp.empty[s], 1);
+        }
+        tc::mbar_init(&pp.drain, 1);
+        pp.abort = 0;
     }
     {
         const uint4 one8 = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);  // eight bf16 1.0
-        for (int i = tid; i < 256; i += kWgThreads) *reinterpret_cast<uint4 *>(ones + (size_t)i * 16) = one8;
+        for (int i = tid; i < 256; i += kWgThreadsP) *reinterpret_cast<uint4 *>(ones + (size_t)i * 16) = one8;
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t s0 = tc::smem_u32(smem), ones_s = tc::smem_u32(ones);
-    const uint32_t idesc = idesc_bf16_mn(128, cout);
+    const uint32_t tmem = pp.tmem;
     const int tiles_x = (A.w + kWgK - 1) / kWgK;
     const int ntiles = A.n * A.h * tiles_x;
-    const int zc = cout / 8;
-    uint32_t k = 0;  // K steps staged by this block: buffer k & 1, mbarrier phase (k >> 1) & 1
-    bool failed = false;
+    // this block's steps: k-th step is tile blockIdx.x + k * gridDim.x
+    const int nsteps = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
-        const int xt = tile % tiles_x, rowi = tile / tiles_x;
-        const int y = rowi % A.h, img = rowi / A.h;
-        const int x0 = xt * kWgK;
-        const uint32_t buf = k & 1u;
-        // the MMAs that read this buffer two steps ago must be done
-        if (k >= 2) {
-            const uint32_t kp = k - 2;
-            const bool ok = tc::mbar_wait(&mbar[buf], (kp >> 1) & 1u);
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                break;
-            }
-        }
-        unsigned char *xs = smem + buf * (L.x_bytes + L.z_bytes);
-        unsigned char *zs = xs + L.x_bytes;
-        // stage X (3 rows x 66 px x cin) and dZ (64 px x cout), loads grouped before stores
-        const int nx = 3 * kWgHalo * cc, nz = kWgK * zc;
-        for (int base = tid; base < nx + nz; base += kWgThreads * 4) {
-            uint4 v[4];
-#pragma unroll
-            for (int g = 0; g < 4; ++g) {
-                const int i = base + g * kWgThreads;
-                v[g] = make_uint4(0u, 0u, 0u, 0u);
-                if (i < nx) {
-                    const int c = i % cc, px = (i / cc) % kWgHalo, dy = i / (cc * kWgHalo);
-                    v[g] = load_input_chunk(A, img, y + dy - 1, x0 + px - 1, c);
-                } else if (i < nx + nz) {
-                    const int j = i - nx, c = j % zc, px = j / zc;
-                    if (x0 + px < A.w) v[g] = ldg16(A.dz + (((size_t)img * A.h + y) * A.w + x0 + px) * cout + 8 * c);
+    // Producer warps: no more than the ring has stages, so that the stage a
+    // warp waits for was released one phase ago at most (a parity wait cannot
+    // tell phase f - 1 from f - 3): steps are released in order, and a warp's
+    // previous wait already covered step k - np - S >= k - 2S.
+    const int np = S < kWgProdWarps ? S : kWgProdWarps;
+    if (warp < np) {
+        // ---- producers ----
+        for (int k = warp; k < nsteps && !*abort; k += np) {
+            const uint32_t s = (uint32_t)k % (uint32_t)S, f = (uint32_t)k / (uint32_t)S;
+            if (f > 0 && !pipe_wait(&pp.empty[s], (f - 1) & 1u, abort, A.err)) break;
+            const int tile = blockIdx.x + k * gridDim.x;
+            const int xt = tile % tiles_x, rowi = tile / tiles_x;
+            const int y = rowi % A.h, img = rowi / A.h;
+            const int x0 = xt * kWgK;
+            unsigned char *xs = smem + (size_t)s * stage_bytes;
+            unsigned char *zs = xs + L.x_bytes;
+            // X: planes (dy, c) of 66 halo pixels; consecutive lanes take
+            // consecutive 16-byte pieces of a source pixel row
+#pragma unroll 1
+            for (int dy = 0; dy < 3; ++dy) {
+                const int yy = y + dy - 1;
+                const bool row_in = yy >= 0 && yy < A.h;
+                const int yc = row_in ? yy : 0;
+                if (MODE == SRC_UP) {
+                    const bf16 *ra = A.a + (((size_t)img * (A.h >> 1) + (yc >> 1)) * (A.w >> 1)) * A.ca;
+                    warp_copy_part<CCA, true, kWgHalo>(ra, A.ca, A.w, x0 - 1, dy * CC, row_in, xs, A.a, lane);
+                } else {
+                    const bf16 *ra = A.a + (((size_t)img * A.h + yc) * A.w) * A.ca;
+                    warp_copy_part<CCA, false, kWgHalo>(ra, A.ca, A.w, x0 - 1, dy * CC, row_in, xs, A.a, lane);
+                }
+                if (CCB > 0) {
+                    const bf16 *rb = A.b + (((size_t)img * A.h + yc) * A.w) * A.cb;
+                    warp_copy_part<CCB, false, kWgHalo>(rb, A.cb, A.w, x0 - 1, dy * CC + CCA, row_in, xs, A.a, lane);
                 }
             }
-#pragma unroll
-            for (int g = 0; g < 4; ++g) {
-                const int i = base + g * kWgThreads;
-                if (i < nx) {
-                    const int c = i % cc, px = (i / cc) % kWgHalo, dy = i / (cc * kWgHalo);
-                    *reinterpret_cast<uint4 *>(xs + (size_t)(dy * cc + c) * kWgPlaneX + px * 16) = v[g];
-                } else if (i < nx + nz) {
-                    const int j = i - nx, c = j % zc, px = j / zc;
-                    *reinterpret_cast<uint4 *>(zs + (size_t)c * kWgPlaneZ + px * 16) = v[g];
-                }
+            // dZ: planes of 8 output channels over 64 pixels, zero past the row end
+            for (int i = lane; i < kWgK * zc; i += 32) {
+                const int c = i % zc, px = i / zc;
+                const bool in = x0 + px < A.w;
+                const bf16 *src = in ? A.dz + (((size_t)img * A.h + y) * A.w + x0 + px) * cout + 8 * c : A.dz;
+                const uint32_t dst = tc::smem_u32(zs + (size_t)c * kWgPlaneZ + px * 16);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(in ? 16 : 0)
+                             : "memory");
             }
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            tc::fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&pp.full[s]);
         }
-        tc::fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    } else if (warp == kWgProdWarps && lane == 0) {
+        // ---- MMA issuer ----
+        const uint32_t s0 = tc::smem_u32(smem), ones_s = tc::smem_u32(ones);
+        const uint32_t idesc = idesc_bf16_mn(128, cout);
+        for (int k = 0; k < nsteps; ++k) {
+            const uint32_t s = (uint32_t)k % (uint32_t)S;
+            if (!pipe_wait(&pp.full[s], ((uint32_t)k / (uint32_t)S) & 1u, abort, A.err)) break;
             tc::fence_after_sync();
-            const uint32_t xb = s0 + buf * (L.x_bytes + L.z_bytes), zb = xb + L.x_bytes;
+            const uint32_t xb = s0 + s * stage_bytes, zb = xb + L.x_bytes;
             for (int kk = 0; kk < kWgK / 16; ++kk) {
-                const uint32_t first = (k == 0 && kk == 0) ? 0u : 1u;
+                const uint32_t acc = (k == 0 && kk == 0) ? 0u : 1u;
                 const uint64_t bd = tc::desc(zb + (uint32_t)(kk * 16 * 16), 128, kWgPlaneZ);
                 for (int dx = 0; dx < 3; ++dx)
                     for (int mt = 0; mt < L.mtiles; ++mt) {
                         const uint64_t ad =
                             tc::desc(xb + (uint32_t)(16 * mt * kWgPlaneX + (kk * 16 + dx) * 16), 128, kWgPlaneX);
-                        tc::mma_bf16(tmem + (uint32_t)((dx * L.mtiles + mt) * cout), ad, bd, idesc, first);
+                        tc::mma_bf16(tmem + (uint32_t)((dx * L.mtiles + mt) * cout), ad, bd, idesc, acc);
                     }
                 const uint64_t od = tc::desc(ones_s, 128, 256);
-                tc::mma_bf16(tmem + (uint32_t)(3 * L.mtiles * cout), od, bd, idesc, first);
+                tc::mma_bf16(tmem + (uint32_t)(3 * L.mtiles * cout), od, bd, idesc, acc);
             }
-            tc::commit(&mbar[buf]);
+            tc::commit(&pp.empty[s]);
+        }
+        // every MMA issued has finished before the accumulators are read
+        tc::commit(&pp.drain);
+        if (!tc::mbar_wait(&pp.drain, 0u, kConvWaitNs)) {
+            *abort = 1;
+            atomicExch(A.err, 1);
         }
     }
-    // drain: the last one or two steps
-    bool ok = true;
-    if (!failed) {
-        for (uint32_t kp = (k >= 2 ? k - 2 : 0); kp < k; ++kp) ok &= tc::mbar_wait(&mbar[kp & 1u], (kp >> 1) & 1u);
-    }
-    failed |= __syncthreads_or(!ok) != 0;
+    tc::fence_before_sync();
+    __syncthreads();
     tc::fence_after_sync();
-    if (failed) {
-        if (tid == 0) atomicExch(A.err, 1);
-    } else {
+    if (!*abort && warp < kWgProdWarps) {
         // rows R = dx * mtiles * 128 + (dy * cin + ci), bias row R = 3 * mtiles * 128;
-        // warps w and w + 4 share TMEM lane quarter w and split the tiles
+        // warps w and w + 4 share TMEM lane quarter w % 4 and split the tiles
         const int q = warp & 3;
         const size_t rows_pad = (size_t)3 * L.mtiles * 128 + 1;
         float *dst = A.partial + (size_t)blockIdx.x * rows_pad * cout;
@@ -625,7 +655,7 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs A)
             for (int j = 0; j < cout; j += 16) {
                 float v[16];
                 tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(tl * cout + j), v);
-                if (k == 0) {
+                if (nsteps == 0) {
 #pragma unroll
                     for (int e = 0; e < 16; ++e) v[e] = 0.f;
                 }
@@ -645,7 +675,17 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs A)
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+    if (warp == kWgProdWarps) tc::tmem_dealloc(tmem, ncols);
+}
+
+// The weight-gradient kernel for a source mode and the input chunks of
+// sources A and B (the convolutions' own variants).
+const void *wgrad_kernel_fn(int mode, int cca, int ccb) {
+#define TDE_WG_FN(M, A, B) \
+    if (mode == M && cca == A && ccb == B) return (const void *)wgrad_tc_kernel<M, A, B>;
+    TDE_CONV_VARIANTS(TDE_WG_FN)
+#undef TDE_WG_FN
+    return nullptr;
 }
 
 __global__ void wgrad_reduce_kernel(const float *__restrict__ partial, int blocks, int cin, int cout, int mtiles,
@@ -968,8 +1008,10 @@ static uint32_t smem_floor_for_tmem(uint32_t ncols) {
 int prepare_kernels() {
     // allow the largest dynamic shared memory a block may have, once, so that
     // launches (also inside stream capture) make no other runtime call
-    std::vector<const void *> fns = {(const void *)wgrad_tc_kernel};
-#define TDE_CONV_FN(M, A, B) fns.push_back((const void *)conv3x3_tc_kernel<M, A, B>);
+    std::vector<const void *> fns;
+#define TDE_CONV_FN(M, A, B) \
+    fns.push_back((const void *)conv3x3_tc_kernel<M, A, B>); \
+    fns.push_back((const void *)wgrad_tc_kernel<M, A, B>);
     TDE_CONV_VARIANTS(TDE_CONV_FN)
 #undef TDE_CONV_FN
     for (const void *fn : fns) {
@@ -1066,13 +1108,24 @@ size_t wgrad_partial_floats(int blocks, int cin, int cout) {
 int launch_wgrad(const WgradArgs &a, int blocks, cudaStream_t s) {
     const int cin = a.ca + a.cb;
     const WgLayout L = wg_layout(cin, a.cout);
-    if (cin % 8 || a.cout % 16 || a.cout < 16 || L.tcols > 512)
+    if (cin % 8 || a.cout % 16 || a.cout < 16 || L.tcols > 512 || a.mode_a == SRC_POOL)
         return set_error(TDE_ERR_INVALID_ARG, "refiner wgrad: unsupported shape cin=%d cout=%d", cin, a.cout);
-    size_t smem = L.total;
+    // as many ring stages as one block per SM holds (the ones tile after them)
+    const size_t stage = (size_t)L.x_bytes + L.z_bytes, ones = 16u * 256u;
+    const size_t budget = 227 * 1024 - 512 - ones;
+    int S = (int)(budget / stage);
+    S = S > kWgMaxStages ? kWgMaxStages : S;
+    if (S < 2) return set_error(TDE_ERR_UNSUPPORTED, "refiner wgrad: cin=%d cout=%d does not fit an SM", cin, a.cout);
+    size_t smem = (size_t)S * stage + ones;
     const size_t fl = smem_floor_for_tmem(tmem_cols((int)L.tcols));
     if (smem < fl) smem = fl;
-    if (smem > 227 * 1024 - 256) return set_error(TDE_ERR_UNSUPPORTED, "refiner wgrad: %zu B of shared memory", smem);
-    wgrad_tc_kernel<<<blocks, kWgThreads, smem, s>>>(a);
+    const void *fn = wgrad_kernel_fn(a.mode_a, a.ca / 8, a.cb / 8);
+    if (!fn) return set_error(TDE_ERR_UNSUPPORTED, "refiner wgrad: no kernel for mode %d with %d + %d input channels",
+                              a.mode_a, a.ca, a.cb);
+    WgradArgs args = a;
+    void *kargs[] = {(void *)&args, (void *)&S};
+    cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(kWgThreadsP), kargs, smem, s);
+    if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "refiner wgrad: %s", cudaGetErrorString(e));
     return check_launch("refiner wgrad");
 }
 
