@@ -137,13 +137,14 @@ struct ConvPipe {
 
 // Bounded wait on an mbarrier phase; false when the block aborted (here or
 // in another role).
-__device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort, int *err) {
+__device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort, int *err,
+                                          uint64_t limit_ns = kConvWaitNs) {
     if (tc::mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = tc::globaltimer_ns();
     // sleeping waits (up to 20 us each) leave the issue slots to the working warps
     while (!tc::mbar_try_wait_sleep(bar, parity, 20000u)) {
         if (*abort) return false;
-        if (tc::globaltimer_ns() - t0 > kConvWaitNs) {
+        if (tc::globaltimer_ns() - t0 > limit_ns) {
             *abort = 1;
             atomicExch(err, 1);
             return false;
@@ -151,6 +152,24 @@ __device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volati
     }
     return true;
 }
+// The bounded wait on its own: one lane waits for a phase that nothing
+// completes; after limit_ns it gives up, raises the error flag and the block
+// returns normally.  out[0] = the flag, out[1] = nanoseconds waited.
+__global__ void wait_selftest_kernel(uint64_t limit_ns, unsigned long long *out) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort_flag;
+    __shared__ int err;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        abort_flag = 0;
+        err = 0;
+        const uint64_t t0 = tc::globaltimer_ns();
+        const bool ok = pipe_wait(&bar, 0u, &abort_flag, &err, limit_ns);
+        out[0] = ok ? 0ull : (unsigned long long)err;
+        out[1] = tc::globaltimer_ns() - t0;
+    }
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
 }
@@ -1127,6 +1146,11 @@ int launch_wgrad(const WgradArgs &a, int blocks, cudaStream_t s) {
     cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(kWgThreadsP), kargs, smem, s);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "refiner wgrad: %s", cudaGetErrorString(e));
     return check_launch("refiner wgrad");
+}
+
+int launch_wait_selftest(uint64_t limit_ns, unsigned long long *out, cudaStream_t s) {
+    wait_selftest_kernel<<<1, 32, 0, s>>>(limit_ns, out);
+    return check_launch("wait selftest");
 }
 
 int launch_wgrad_reduce(const float *partial, int blocks, int cin, int cout, float *dw, float *db, cudaStream_t s) {

@@ -428,6 +428,12 @@ int tde_refiner_check_shape(tde_refiner *r, int rows, int cols) {
     return TDE_OK;
 }
 
+int tde_wait_selftest(uint64_t limit_ns, unsigned long long *out_device, void *stream) {
+    if (!out_device || limit_ns == 0 || limit_ns > 10000000000ull)
+        return set_error(TDE_ERR_INVALID_ARG, "wait_selftest: bad arguments");
+    return launch_wait_selftest(limit_ns, out_device, static_cast<cudaStream_t>(stream));
+}
+
 int tde_refiner_status(tde_refiner *r) {
     if (!r) return set_error(TDE_ERR_INVALID_ARG, "refiner_status: null");
     int e = 0;

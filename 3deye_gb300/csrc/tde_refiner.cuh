@@ -66,6 +66,9 @@ struct ConvPlan {
 };
 // ca of the cin input channels come from source A (the rest from B).
 int conv_plan(int mode, int ca, int cin, int cout, ConvPlan *out);
+// One lane waits, with the kernels' bounded wait, for a barrier phase nothing
+// completes; out (device, 2 values): the raised flag and the nanoseconds waited.
+int launch_wait_selftest(uint64_t limit_ns, unsigned long long *out, cudaStream_t s);
 // Launches only (no other runtime call), so it may be stream-captured.
 int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream_t s);
 int wgrad_blocks(int num_sms, int cin, int cout);

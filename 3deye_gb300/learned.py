@@ -137,8 +137,7 @@ def train(refiner, raw, tgt, steps, batch, lr, seed=0, log=print, log_every=250)
             losses.append((it + 1, loss * batch * raw.shape[1] * raw.shape[2] / max(cnt, 1.0)))
             if log and ((it + 1) % log_every == 0 or it == 0):
                 log(f"step {it + 1}: mean L1 {losses[-1][1] * 1000:.3f} mm ({time.time() - t0:.1f} s)")
-    if refiner.status() != 0:
-        raise RuntimeError("refiner: a tensor-core wait timed out")
+    refiner.check_status()
     return losses
 
 

@@ -27,6 +27,7 @@ declare("tde_refiner_last_loss", I, [P, C.POINTER(C.c_double), C.POINTER(C.c_dou
 declare("tde_refiner_get_tensor", I, [P, I, P, SZ])
 declare("tde_refiner_tensor_bytes", SZ, [P, I])
 declare("tde_refiner_status", I, [P])
+declare("tde_wait_selftest", I, [C.c_uint64, P, P])
 
 ACTIVATIONS = ["e0a", "e0", "e1a", "e1", "e2a", "e2", "b3a", "b3", "d2", "d1", "d0"]
 GRADIENTS = ["dz11", "gu0", "dz10", "gu1", "dz9", "gu2", "dz8", "dz7", "gp3", "dz6", "dz5", "gp2", "dz4", "dz3",
@@ -134,7 +135,12 @@ class Refiner:
         return f.reshape(-1, self.rows >> lv, self.cols >> lv, c)
 
     def status(self) -> int:
+        """0, or TDE_ERR_DEVICE_TIMEOUT once a tensor-core wait gave up (synchronises)."""
         return lib.tde_refiner_status(self._h)
+
+    def check_status(self) -> None:
+        """Raises TdeError when a tensor-core wait of an earlier launch gave up."""
+        check(self.status())
 
     # -- numpy conveniences (copies through torch) ---------------------------
     def forward(self, raw_mm: np.ndarray):

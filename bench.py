@@ -676,8 +676,7 @@ def run_ours(args, ws, rank, local):
         r1.record(rs)
         rs.synchronize()
         fwd_ms = r0.elapsed_time(r1) / K
-        if R.status() != 0:
-            raise RuntimeError("refiner: a tensor-core wait timed out")
+        R.check_status()
         R.close()
         B = min(16, n // 2)
         T = rf.Refiner(B, cfg.rows, cfg.cols)
@@ -691,8 +690,7 @@ def run_ours(args, ws, rank, local):
         r1.record(rs)
         rs.synchronize()
         train_ms = r0.elapsed_time(r1) / steps
-        if T.status() != 0:
-            raise RuntimeError("refiner: a tensor-core wait timed out")
+        T.check_status()
         T.close()
         fwd_flops, train_flops = rf.conv_flops(cfg.rows, cfg.cols), rf.conv_flops(cfg.rows, cfg.cols, B, True)
         lest = lposes.numpy().copy()

@@ -77,6 +77,13 @@ int tde_refiner_check_shape(tde_refiner *r, int rows, int cols);
 /* Device-side status: TDE_ERR_DEVICE_TIMEOUT once a tensor-core wait gave up. */
 int tde_refiner_status(tde_refiner *r);
 
+/* Self-test of the bounded wait every tensor-core kernel here uses (no
+ * counterpart in the reference): one thread waits on a barrier phase that
+ * nothing completes, gives up after limit_ns (at most 10 s), raises the flag
+ * and returns; out_device (2 device values) receives the flag (1) and the
+ * nanoseconds waited.  The context stays usable. */
+int tde_wait_selftest(uint64_t limit_ns, unsigned long long *out_device, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
