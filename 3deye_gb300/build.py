@@ -30,11 +30,12 @@ ORACLE_LIB = ORACLE / "liboracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Kernels whose float arithmetic must equal the CPU oracle's operation by
 # operation are compiled without FMA contraction.
-NO_FMAD = {"k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_render.cu", "k_synth.cu"}
+NO_FMAD = {"k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_render.cu", "k_synth.cu", "k_rgbd.cu"}
 CUDA_UNITS = ["capi.cu", "k_raycast.cu", "k_integrate.cu", "k_icp.cu", "k_depth.cu", "k_slab.cu",
-              "pipeline.cu", "k_synth.cu", "noalloc.cu", "k_refiner.cu", "refiner.cu", "k_render.cu"]
+              "pipeline.cu", "k_synth.cu", "noalloc.cu", "k_refiner.cu", "refiner.cu", "k_render.cu",
+              "k_rgbd.cu"]
 CXX_UNITS = ["wrappers.cpp"]
-ORACLE_SOURCES = ["oracle.c", "oracle_scene.c", "oracle_f64.c"]
+ORACLE_SOURCES = ["oracle.c", "oracle_scene.c", "oracle_f64.c", "oracle_rgbd.c"]
 
 
 def _nvcc() -> str:

@@ -609,6 +609,38 @@ __global__ void icp_solve_kernel(const double *__restrict__ sums, int n, double 
     if (lane == 0) okv[i] = ok;
 }
 
+// RGB-D odometry step: 256 threads sum the per-block partials of the 27
+// terms and the count (FP64; warp w takes blocks w, w + 8, ..., then the
+// eight warp sums in warp order), and with at least kIcpMinInliers pairs
+// warp 0 applies the same solve and pose update as an ICP iteration to
+// pose[12]; a failed solve keeps the pose and sets bit 0 of *status, a
+// solved step bit 1.
+__global__ void __launch_bounds__(256) rgbd_solve_kernel(const double *__restrict__ partials, int nblocks,
+                                                         double *__restrict__ pose, int *__restrict__ status) {
+    __shared__ double Rs[9], ts[3];
+    __shared__ double part[8][kIcpTerms];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane < kIcpTerms) {
+        double s = 0.0;
+        for (int b = warp; b < nblocks; b += 8) s += partials[(size_t)b * kIcpTerms + lane];
+        part[warp][lane] = s;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    double term = 0.0;
+    if (lane < kIcpTerms)
+        for (int w = 0; w < 8; ++w) term += part[w][lane];
+    const double pv = lane < 12 ? pose[lane] : 0.0;
+    if (lane < 9) Rs[lane] = pv;
+    else if (lane < 12) ts[lane - 9] = pv;
+    __syncwarp();
+    const double count = __shfl_sync(0xffffffffu, term, 27);
+    double o, xl;
+    const bool ok = count >= (double)kIcpMinInliers && warp_solve_step(term, Rs, ts, lane, o, xl);
+    if (lane < 12) pose[lane] = ok ? o : pv;
+    if (lane == 0) *status |= ok ? 2 : 1;
+}
+
 // transform_estimation.cl:4-53: group g sums its row of the partial buffer.
 __global__ void transform_estimation_kernel(const float *__restrict__ gbuf, float *__restrict__ out, int len,
                                             int stride) {
@@ -668,6 +700,11 @@ int launch_icp_solve(const double *sums, int n, double *pose, double *x, int *ok
     if (n <= 0) return TDE_OK;
     icp_solve_kernel<<<div_up(n, 4), 128, 0, stream>>>(sums, n, pose, x, ok);
     return check_launch("icp_solve");
+}
+
+int launch_rgbd_solve(const double *partials, int nblocks, double *pose, int *status, cudaStream_t stream) {
+    rgbd_solve_kernel<<<1, 256, 0, stream>>>(partials, nblocks, pose, status);
+    return check_launch("rgbd_solve");
 }
 
 int launch_transform_estimation(const float *gbuf, float *out, int len, int stride, cudaStream_t stream) {

@@ -1,0 +1,613 @@
+// k_rgbd.cu -- dense RGB-D (photometric) odometry: the reference's second
+// tracker (Estimate_Isometry_By_RGBD and its stages, common/src/
+// opencl_wrappers.cpp:345-362, 1008-1466) after the RGB-D odometry of
+// OpenCV's contrib rgbd module (Steinbruecker, Sturm, Cremers 2011).
+//
+// Per frame: 8-bit intensity and metric depth, a pyramid, 3x3 Sobel
+// derivatives of the current frame.  Per Gauss-Newton step, two passes over
+// the previous frame's pixels of the level: the first finds each pixel's
+// correspondence in the current frame (projective transform R' = K R K^-1,
+// t' = K t, depth and gradient tests) and sums the squared intensity
+// differences -- integers, so the sum is exact in any order; the second
+// forms sigma from those sums, each kept pair's weighted Jacobian row and the
+// 27 terms of [A | b], reduced per block in FP64 in a fixed order; a
+// one-warp kernel sums the blocks, solves in FP64 and moves the pose
+// (T <- exp(xi) T, the ICP path's solve).  Every step is launches only: the
+// pose lives on the device, nothing waits on the host.
+//
+// Built with -fmad=false: the pair tests and row values are the same IEEE
+// operations as the CPU oracle (oracle/oracle_rgbd.c), explicit fused
+// multiply-adds written out on both sides.
+#include <cmath>
+
+#include "tde_common.cuh"
+#include "tde_icp.cuh"
+
+namespace tde {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kPix = 8;  // pixels per thread in the odometry passes (150 blocks at 640x480)
+constexpr float kSobelScale = 0.125f;  // SOBEL_SCALE, compute_least_squares_equation.cl:8
+
+inline unsigned odo_blocks(int W, int H) { return div_up((unsigned)(W * H), (unsigned)(kThreads * kPix)); }
+
+__global__ void prepare_kernel(const uint16_t *__restrict__ depth, const uint8_t *__restrict__ rgb, int n,
+                               uint8_t *__restrict__ I, float *__restrict__ D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+    I[i] = (uint8_t)((r * 4899u + g * 9617u + b * 1868u + 8192u) >> 14);  // BT.601 luma, 14-bit fixed point
+    D[i] = __fmul_rn((float)depth[i], 0.001f);
+}
+
+__global__ void pyramid_kernel(const uint8_t *__restrict__ I, const float *__restrict__ D, int W, int H,
+                               uint8_t *__restrict__ I2, float *__restrict__ D2) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W2 = W >> 1, H2 = H >> 1;
+    if (x >= W2 || y >= H2) return;
+    const size_t s = (size_t)(2 * y) * W + 2 * x;
+    I2[(size_t)y * W2 + x] = (uint8_t)((I[s] + I[s + 1] + I[s + W] + I[s + W + 1] + 2u) >> 2);
+    D2[(size_t)y * W2 + x] = D[s];
+}
+
+__global__ void sobel_kernel(const uint8_t *__restrict__ I, int W, int H, int16_t *__restrict__ dx,
+                             int16_t *__restrict__ dy) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t o = (size_t)y * W + x;
+    if (x == 0 || y == 0 || x == W - 1 || y == H - 1) {
+        dx[o] = 0;
+        dy[o] = 0;
+        return;
+    }
+    const int a = I[o - W - 1], b = I[o - W], c = I[o - W + 1];
+    const int d = I[o - 1], f = I[o + 1];
+    const int g = I[o + W - 1], h = I[o + W], k = I[o + W + 1];
+    dx[o] = (int16_t)((c + 2 * f + k) - (a + 2 * d + g));
+    dy[o] = (int16_t)((g + 2 * h + k) - (a + 2 * b + c));
+}
+
+// ---- points of interest: per-row counts, one scan over rows, per-row scatter ----
+__device__ __forceinline__ bool textured(const int16_t *dx, const int16_t *dy, size_t i, float scale) {
+    const int g = dx[i] * dx[i] + dy[i] * dy[i];
+    return (float)g >= scale;
+}
+
+__global__ void points_count_kernel(const int16_t *__restrict__ dx, const int16_t *__restrict__ dy, int W,
+                                    float scale, uint32_t *__restrict__ counts) {
+    __shared__ unsigned s;
+    if (threadIdx.x == 0) s = 0;
+    __syncthreads();
+    const size_t row = (size_t)blockIdx.x * W;
+    unsigned c = 0;
+    for (int x = threadIdx.x; x < W; x += blockDim.x) c += textured(dx, dy, row + x, scale);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s, c);
+    __syncthreads();
+    if (threadIdx.x == 0) counts[blockIdx.x] = s;
+}
+
+// Exclusive scan of n counts in place by one block; total to *total.
+__global__ void scan_counts_kernel(uint32_t *__restrict__ a, int n, uint32_t *__restrict__ total) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + tid;
+        const uint32_t v = i < n ? a[i] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            const int nw = blockDim.x >> 5;
+            uint32_t w = lane < nw ? warp_sums[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            if (lane < nw) warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t before = carry + (warp ? warp_sums[warp - 1] : 0u) + x - v;
+        if (i < n) a[i] = before;
+        __syncthreads();
+        if (tid == blockDim.x - 1) carry = before + v;
+        __syncthreads();
+    }
+    if (tid == 0) *total = carry;
+}
+
+__global__ void points_scatter_kernel(const int16_t *__restrict__ dx, const int16_t *__restrict__ dy, int W,
+                                      float scale, const uint32_t *__restrict__ offs, tde_point2i *__restrict__ pts,
+                                      uint32_t capacity) {
+    __shared__ unsigned s_warp[kThreads / 32];
+    __shared__ unsigned s_base;
+    const int y = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_base = offs[y];
+    __syncthreads();
+    const size_t row = (size_t)y * W;
+    for (int x0 = 0; x0 < W; x0 += kThreads) {
+        const int x = x0 + threadIdx.x;
+        const bool set = x < W && textured(dx, dy, row + x, scale);
+        const unsigned m = __ballot_sync(0xffffffffu, set);
+        if (lane == 0) s_warp[warp] = __popc(m);
+        __syncthreads();
+        if (set) {
+            unsigned before = 0;
+            for (int w = 0; w < warp; ++w) before += s_warp[w];
+            const uint32_t slot = s_base + before + __popc(m & ((1u << lane) - 1u));
+            if (slot < capacity) pts[slot] = tde_point2i{x, y};
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned t = 0;
+            for (int w = 0; w < kThreads / 32; ++w) t += s_warp[w];
+            s_base += t;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- correspondences and rows: the oracle's operations, in its order ----
+struct Level {
+    const uint8_t *Ip, *Ic;
+    const float *Dp, *Dc;
+    const int16_t *dx, *dy;
+    int W, H;
+    float fx, fy, cx, cy;
+    float mdd, maxd, grad2;
+};
+
+// R' = K R K^-1, t' = K t in FP64 (explicit fused operations), then float.
+__device__ void projective(const double *R, const double *t, float fxf, float fyf, float cxf, float cyf,
+                           float *proj) {
+    const double fx = fxf, fy = fyf, cx = cxf, cy = cyf;
+    double M[9];
+    for (int j = 0; j < 3; ++j) {
+        M[j] = __fma_rn(fx, R[j], __dmul_rn(cx, R[6 + j]));
+        M[3 + j] = __fma_rn(fy, R[3 + j], __dmul_rn(cy, R[6 + j]));
+        M[6 + j] = R[6 + j];
+    }
+    for (int i = 0; i < 3; ++i) {
+        const double a = __ddiv_rn(M[3 * i], fx), b = __ddiv_rn(M[3 * i + 1], fy);
+        proj[3 * i] = (float)a;
+        proj[3 * i + 1] = (float)b;
+        proj[3 * i + 2] = (float)(M[3 * i + 2] - __fma_rn(a, cx, __dmul_rn(b, cy)));
+    }
+    proj[9] = (float)__fma_rn(fx, t[0], __dmul_rn(cx, t[2]));
+    proj[10] = (float)__fma_rn(fy, t[1], __dmul_rn(cy, t[2]));
+    proj[11] = (float)t[2];
+}
+
+__device__ __forceinline__ bool depth_ok(float z, float maxd) { return z > 0.f && z < maxd; }
+
+// Pixel i = (u, v) of the previous frame: its pair in the current frame (j)
+// and the intensity difference r, or false.
+__device__ __forceinline__ bool find_pair(const Level &L, const float *P, int u, int v, float z, int &j, float &r) {
+    if (!depth_ok(z, L.maxd)) return false;
+    const float fu = (float)u, fv = (float)v;
+    const float px = __fmaf_rn(z, __fmaf_rn(P[1], fv, __fmaf_rn(P[0], fu, P[2])), P[9]);
+    const float py = __fmaf_rn(z, __fmaf_rn(P[4], fv, __fmaf_rn(P[3], fu, P[5])), P[10]);
+    const float pz = __fmaf_rn(z, __fmaf_rn(P[7], fv, __fmaf_rn(P[6], fu, P[8])), P[11]);
+    if (!(pz > 0.f)) return false;
+    const float iz = __frcp_rn(pz);
+    const int u2 = __float2int_rn(__fmul_rn(px, iz)), v2 = __float2int_rn(__fmul_rn(py, iz));
+    if (u2 < 0 || v2 < 0 || u2 >= L.W || v2 >= L.H) return false;
+    j = v2 * L.W + u2;
+    const float z2 = __ldg(L.Dc + j);
+    if (!depth_ok(z2, L.maxd) || !(fabsf(pz - z2) < L.mdd)) return false;
+    if (L.dx) {  // no derivatives: the points were filtered beforehand
+        const int gx = __ldg(L.dx + j), gy = __ldg(L.dy + j);
+        if (!((float)(gx * gx + gy * gy) >= L.grad2)) return false;
+    }
+    r = (float)__ldg(L.Ic + j) - (float)__ldg(L.Ip + (size_t)v * L.W + u);
+    return true;
+}
+
+// The 7-vector (C0..C5, -w r) of a kept pair; M = R row-major, t (float).
+__device__ __forceinline__ void pair_row(const Level &L, const float *M, int u, int v, float z, int j, float r,
+                                         float sigma, float ifx, float ify, float row[7]) {
+    const float xn = __fmul_rn((float)u - L.cx, ifx), yn = __fmul_rn((float)v - L.cy, ify);
+    const float X = __fmul_rn(z, xn), Y = __fmul_rn(z, yn);
+    const float Px = __fmaf_rn(M[2], z, __fmaf_rn(M[1], Y, __fmul_rn(M[0], X))) + M[9];
+    const float Py = __fmaf_rn(M[5], z, __fmaf_rn(M[4], Y, __fmul_rn(M[3], X))) + M[10];
+    const float Pz = __fmaf_rn(M[8], z, __fmaf_rn(M[7], Y, __fmul_rn(M[6], X))) + M[11];
+    const float wsum = sigma + fabsf(r);
+    const float w = wsum > 2.220446049250313e-16f ? __frcp_rn(wsum) : 1.f;
+    const float s0 = __fmul_rn(w, kSobelScale);
+    const float iz = __frcp_rn(Pz);
+    const float v0 = __fmul_rn(__fmul_rn(__fmul_rn(iz, L.fx), s0), (float)__ldg(L.dx + j));
+    const float v1 = __fmul_rn(__fmul_rn(__fmul_rn(iz, L.fy), s0), (float)__ldg(L.dy + j));
+    const float v2 = __fmul_rn(-__fmaf_rn(v1, Py, __fmul_rn(v0, Px)), iz);
+    row[0] = __fmaf_rn(Py, v2, -__fmul_rn(Pz, v1));
+    row[1] = __fmaf_rn(Pz, v0, -__fmul_rn(Px, v2));
+    row[2] = __fmaf_rn(Px, v1, -__fmul_rn(Py, v0));
+    row[3] = v0;
+    row[4] = v1;
+    row[5] = v2;
+    row[6] = -__fmul_rn(w, r);
+}
+
+// Pass 1: kept count and sum of squared differences per block.
+__global__ void __launch_bounds__(kThreads) residual_kernel(const Level L, const double *__restrict__ pose,
+                                                            unsigned long long *__restrict__ partials) {
+    __shared__ float P[12];
+    __shared__ unsigned s_n;
+    __shared__ unsigned long long s_r2;
+    if (threadIdx.x == 0) {
+        projective(pose, pose + 9, L.fx, L.fy, L.cx, L.cy, P);
+        s_n = 0;
+        s_r2 = 0ull;
+    }
+    __syncthreads();
+    unsigned n = 0;
+    unsigned long long r2 = 0;  // squared integer differences: exact
+    const int npix = L.W * L.H;
+#pragma unroll
+    for (int k = 0; k < kPix; ++k) {
+        const int i = blockIdx.x * kThreads * kPix + k * kThreads + threadIdx.x;
+        if (i >= npix) continue;
+        const int u = i % L.W, v = i / L.W;
+        int j;
+        float r;
+        if (find_pair(L, P, u, v, __ldg(L.Dp + i), j, r)) {
+            ++n;
+            const int ri = (int)r;
+            r2 += (unsigned long long)(ri * ri);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n += __shfl_down_sync(0xffffffffu, n, o);
+        r2 += __shfl_down_sync(0xffffffffu, r2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&s_n, n);
+        atomicAdd(&s_r2, r2);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s_n;
+        partials[2 * blockIdx.x + 1] = s_r2;
+    }
+}
+
+// Pass 2: sigma from pass 1's blocks (integer sums: exact), the rows of the
+// kept pairs, per-block FP64 partials of the 27 terms and the count.
+__global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, const double *__restrict__ pose,
+                                                       const unsigned long long *__restrict__ res_partials, int nres,
+                                                       double *__restrict__ partials, float *__restrict__ sigma_out) {
+    __shared__ float P[12], M[12];
+    __shared__ float s_sigma;
+    __shared__ double red[kThreads / 32][28];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (warp == 0) {
+        unsigned long long n = 0, s = 0;
+        for (int b = lane; b < nres; b += 32) {
+            n += res_partials[2 * b];
+            s += res_partials[2 * b + 1];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            n += __shfl_xor_sync(0xffffffffu, n, o);
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+        }
+        if (lane == 0) {
+            projective(pose, pose + 9, L.fx, L.fy, L.cx, L.cy, P);
+            for (int k = 0; k < 12; ++k) M[k] = (float)pose[k];
+            s_sigma = n ? __fsqrt_rn((float)((double)s / (double)n)) : 0.f;
+            if (sigma_out && blockIdx.x == 0) *sigma_out = s_sigma;
+        }
+    }
+    __syncthreads();
+    const float sigma = s_sigma;
+    const float ifx = __frcp_rn(L.fx), ify = __frcp_rn(L.fy);
+    float acc[28];
+#pragma unroll
+    for (int k = 0; k < 28; ++k) acc[k] = 0.f;
+    const int npix = L.W * L.H;
+#pragma unroll 1
+    for (int k = 0; k < kPix; ++k) {
+        const int i = blockIdx.x * kThreads * kPix + k * kThreads + tid;
+        if (i >= npix) continue;
+        const int u = i % L.W, v = i / L.W;
+        const float z = __ldg(L.Dp + i);
+        int j;
+        float r;
+        if (!find_pair(L, P, u, v, z, j, r)) continue;
+        float row[7];
+        pair_row(L, M, u, v, z, j, r, sigma, ifx, ify, row);
+        int t = 0;
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int b = a; b < 7; ++b) {
+                acc[t] = __fmaf_rn(row[a], row[b], acc[t]);
+                ++t;
+            }
+        acc[27] += 1.f;
+    }
+    // warp sums (fixed butterfly order), then the warps in order in FP64
+#pragma unroll
+    for (int k = 0; k < 28; ++k) {
+        float d = acc[k];
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0) red[warp][k] = (double)d;
+    }
+    __syncthreads();
+    if (tid < 28) {
+        double s = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) s += red[w][tid];
+        partials[(size_t)blockIdx.x * 28 + tid] = s;
+    }
+}
+
+// The 28 sums of `nb` partials: warp w takes blocks w, w + 8, ..., then the
+// warp sums in order (the odometry solve's order).
+__global__ void __launch_bounds__(256) sum_partials_kernel(const double *__restrict__ partials, int nb,
+                                                           double *__restrict__ out) {
+    __shared__ double part[8][28];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane < 28) {
+        double s = 0.0;
+        for (int b = warp; b < nb; b += 8) s += partials[(size_t)b * 28 + lane];
+        part[warp][lane] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 28) {
+        double s = 0.0;
+        for (int w = 0; w < 8; ++w) s += part[w][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+struct Pose12 { double v[12]; };
+__global__ void set_pose_kernel(const Pose12 p, double *__restrict__ pose, int *__restrict__ status) {
+    if (threadIdx.x < 12) pose[threadIdx.x] = p.v[threadIdx.x];
+    if (threadIdx.x == 0 && status) *status = 0;
+}
+
+// Fill_List: correspondence of listed previous-frame points (or every pixel).
+struct Proj12 { float v[12]; };
+__global__ void correspondences_kernel(const Level L, const Proj12 proj, const tde_point2i *__restrict__ points,
+                                       uint32_t npoints, tde_point2i *__restrict__ cprev,
+                                       tde_point2i *__restrict__ ccurr, float *__restrict__ diff,
+                                       uint32_t *__restrict__ count, double *__restrict__ sum_r2) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    bool kept = false;
+    float r = 0.f;
+    if (id < npoints) {
+        int u, v;
+        if (points) {
+            u = points[id].x;
+            v = points[id].y;
+        } else {
+            u = (int)(id % (uint32_t)L.W);
+            v = (int)(id / (uint32_t)L.W);
+        }
+        int j = 0;
+        if (u >= 0 && v >= 0 && u < L.W && v < L.H)
+            kept = find_pair(L, proj.v, u, v, __ldg(L.Dp + (size_t)v * L.W + u), j, r);
+        cprev[id] = kept ? tde_point2i{u, v} : tde_point2i{0, 0};
+        ccurr[id] = kept ? tde_point2i{j % L.W, j / L.W} : tde_point2i{0, 0};
+        diff[id] = kept ? r : 100.f;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, kept);
+    double r2 = kept ? (double)r * (double)r : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_down_sync(0xffffffffu, r2, o);
+    if ((threadIdx.x & 31) == 0 && m) {
+        atomicAdd(count, (uint32_t)__popc(m));
+        atomicAdd(sum_r2, r2);  // sums of squared integers below 2^53: exact in any order
+    }
+}
+
+Level make_level(const uint8_t *ip, const float *dp, const uint8_t *ic, const float *dc, const int16_t *dx,
+                 const int16_t *dy, const tde_intrinsics &in, float mdd, float maxd, float min_gradient) {
+    Level L;
+    L.Ip = ip; L.Dp = dp; L.Ic = ic; L.Dc = dc; L.dx = dx; L.dy = dy;
+    L.W = in.cols; L.H = in.rows;
+    L.fx = in.fx; L.fy = in.fy; L.cx = in.cx; L.cy = in.cy;
+    L.mdd = mdd; L.maxd = maxd;
+    const float g = min_gradient / kSobelScale;
+    L.grad2 = g * g;
+    return L;
+}
+
+}  // namespace
+}  // namespace tde
+
+using namespace tde;
+
+extern "C" {
+
+int tde_rgbd_prepare(const uint16_t *depth_mm, const uint8_t *rgb, int cols, int rows, uint8_t *intensity,
+                     float *depth_m, void *stream) {
+    if (!depth_mm || !rgb || !intensity || !depth_m || cols <= 0 || rows <= 0)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_prepare: bad arguments");
+    const int n = cols * rows;
+    prepare_kernel<<<div_up(n, 256u), 256, 0, as_stream(stream)>>>(depth_mm, rgb, n, intensity, depth_m);
+    return check_launch("rgbd_prepare");
+}
+
+int tde_rgbd_pyramid(const uint8_t *intensity, const float *depth_m, int cols, int rows, uint8_t *intensity_half,
+                     float *depth_half, void *stream) {
+    if (!intensity || !depth_m || !intensity_half || !depth_half || cols < 2 || rows < 2)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_pyramid: bad arguments");
+    dim3 b(32, 8), g(div_up(cols >> 1, 32), div_up(rows >> 1, 8));
+    pyramid_kernel<<<g, b, 0, as_stream(stream)>>>(intensity, depth_m, cols, rows, intensity_half, depth_half);
+    return check_launch("rgbd_pyramid");
+}
+
+int tde_rgbd_derivatives(const uint8_t *intensity, int cols, int rows, int16_t *dx, int16_t *dy, void *stream) {
+    if (!intensity || !dx || !dy || cols <= 0 || rows <= 0)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_derivatives: bad arguments");
+    dim3 b(32, 8), g(div_up(cols, 32), div_up(rows, 8));
+    sobel_kernel<<<g, b, 0, as_stream(stream)>>>(intensity, cols, rows, dx, dy);
+    return check_launch("rgbd_derivatives");
+}
+
+size_t tde_rgbd_points_scratch_bytes(int cols, int rows) {
+    if (cols <= 0 || rows <= 0) return 0;
+    return ((size_t)rows * sizeof(uint32_t) + 255) & ~(size_t)255;
+}
+
+int tde_rgbd_points_of_interest(const int16_t *dx, const int16_t *dy, int cols, int rows, float scale, void *scratch,
+                                size_t scratch_bytes, tde_point2i *points, uint32_t capacity, uint32_t *count_device,
+                                void *stream) {
+    if (!dx || !dy || !scratch || !count_device || cols <= 0 || rows <= 0 || (!points && capacity))
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_points_of_interest: bad arguments");
+    if (scratch_bytes < tde_rgbd_points_scratch_bytes(cols, rows))
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_points_of_interest: scratch %zu < %zu bytes", scratch_bytes,
+                         tde_rgbd_points_scratch_bytes(cols, rows));
+    cudaStream_t s = as_stream(stream);
+    uint32_t *counts = static_cast<uint32_t *>(scratch);
+    points_count_kernel<<<rows, kThreads, 0, s>>>(dx, dy, cols, scale, counts);
+    int st = check_launch("rgbd_points/count");
+    if (st) return st;
+    scan_counts_kernel<<<1, 1024, 0, s>>>(counts, rows, count_device);
+    if ((st = check_launch("rgbd_points/scan"))) return st;
+    points_scatter_kernel<<<rows, kThreads, 0, s>>>(dx, dy, cols, scale, counts, points, capacity);
+    return check_launch("rgbd_points/scatter");
+}
+
+int tde_rgbd_projective(const double *pose12, const tde_intrinsics *intr, float *proj12) {
+    if (!pose12 || !intr || !proj12) return set_error(TDE_ERR_INVALID_ARG, "rgbd_projective: null argument");
+    // the device formula, on the host: FP64 with fused operations, then float
+    const double fx = intr->fx, fy = intr->fy, cx = intr->cx, cy = intr->cy;
+    const double *R = pose12, *t = pose12 + 9;
+    double M[9];
+    for (int j = 0; j < 3; ++j) {
+        M[j] = std::fma(fx, R[j], cx * R[6 + j]);
+        M[3 + j] = std::fma(fy, R[3 + j], cy * R[6 + j]);
+        M[6 + j] = R[6 + j];
+    }
+    for (int i = 0; i < 3; ++i) {
+        const double a = M[3 * i] / fx, b = M[3 * i + 1] / fy;
+        proj12[3 * i] = (float)a;
+        proj12[3 * i + 1] = (float)b;
+        proj12[3 * i + 2] = (float)(M[3 * i + 2] - std::fma(a, cx, b * cy));
+    }
+    proj12[9] = (float)std::fma(fx, t[0], cx * t[2]);
+    proj12[10] = (float)std::fma(fy, t[1], cy * t[2]);
+    proj12[11] = (float)t[2];
+    return TDE_OK;
+}
+
+int tde_rgbd_correspondences(const uint8_t *i_prev, const float *d_prev, const uint8_t *i_curr, const float *d_curr,
+                             const int16_t *dx, const int16_t *dy, int cols, int rows, const tde_point2i *points,
+                             uint32_t npoints, const float *proj12, float max_depth_diff, float max_depth,
+                             float min_gradient, tde_point2i *corr_prev, tde_point2i *corr_curr, float *diff,
+                             uint32_t *count_device, double *sum_r2_device, void *stream) {
+    if (!i_prev || !d_prev || !i_curr || !d_curr || !dx != !dy || !proj12 || !corr_prev || !corr_curr || !diff ||
+        !count_device || !sum_r2_device || cols <= 0 || rows <= 0)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_correspondences: bad arguments");
+    if (!points) npoints = (uint32_t)(cols * rows);
+    cudaStream_t s = as_stream(stream);
+    TDE_CUDA(cudaMemsetAsync(count_device, 0, sizeof(uint32_t), s), "rgbd_correspondences");
+    TDE_CUDA(cudaMemsetAsync(sum_r2_device, 0, sizeof(double), s), "rgbd_correspondences");
+    if (npoints == 0) return TDE_OK;
+    tde_intrinsics in = {0.f, 0.f, 0.f, 0.f, cols, rows};
+    const Level L = make_level(i_prev, d_prev, i_curr, d_curr, dx, dy, in, max_depth_diff, max_depth, min_gradient);
+    Proj12 P;
+    for (int k = 0; k < 12; ++k) P.v[k] = proj12[k];
+    correspondences_kernel<<<div_up(npoints, 256u), 256, 0, s>>>(L, P, points, npoints, corr_prev, corr_curr, diff,
+                                                                 count_device, sum_r2_device);
+    return check_launch("rgbd_correspondences");
+}
+
+size_t tde_rgbd_odometry_scratch_bytes(int cols, int rows) {
+    if (cols <= 0 || rows <= 0) return 0;
+    const size_t nb = odo_blocks(cols, rows);
+    return ((nb * 2 + nb * 28 + 12) * sizeof(double) + 255) & ~(size_t)255;
+}
+
+void tde_rgbd_default_params(tde_rgbd_params *p) {
+    if (!p) return;
+    p->levels = 4;
+    const int it[4] = {7, 7, 7, 10};
+    for (int l = 0; l < TDE_RGBD_MAX_LEVELS; ++l) {
+        p->iters[l] = it[l];
+        p->min_gradient[l] = 10.f;
+    }
+    p->max_depth_diff = 0.07f;
+    p->max_depth = 35.f;
+}
+
+int tde_rgbd_lsm(const uint8_t *i_prev, const float *d_prev, const uint8_t *i_curr, const float *d_curr,
+                 const int16_t *dx, const int16_t *dy, const tde_intrinsics *intr, const double *pose12,
+                 float max_depth_diff, float max_depth, float min_gradient, void *scratch, size_t scratch_bytes,
+                 double *sums_device, float *sigma_device, void *stream) {
+    if (!i_prev || !d_prev || !i_curr || !d_curr || !dx || !dy || !intr || !pose12 || !scratch || !sums_device ||
+        intr->cols <= 0 || intr->rows <= 0)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_lsm: bad arguments");
+    if (scratch_bytes < tde_rgbd_odometry_scratch_bytes(intr->cols, intr->rows))
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_lsm: scratch %zu < %zu bytes", scratch_bytes,
+                         tde_rgbd_odometry_scratch_bytes(intr->cols, intr->rows));
+    cudaStream_t s = as_stream(stream);
+    const unsigned nb = odo_blocks(intr->cols, intr->rows);
+    unsigned long long *res = static_cast<unsigned long long *>(scratch);
+    double *lsm = reinterpret_cast<double *>(res + 2 * nb), *pose = lsm + 28 * nb;
+    Pose12 P;
+    for (int k = 0; k < 12; ++k) P.v[k] = pose12[k];
+    set_pose_kernel<<<1, 32, 0, s>>>(P, pose, nullptr);
+    const Level L = make_level(i_prev, d_prev, i_curr, d_curr, dx, dy, *intr, max_depth_diff, max_depth, min_gradient);
+    residual_kernel<<<nb, kThreads, 0, s>>>(L, pose, res);
+    lsm_kernel<<<nb, kThreads, 0, s>>>(L, pose, res, (int)nb, lsm, sigma_device);
+    sum_partials_kernel<<<1, 256, 0, s>>>(lsm, (int)nb, sums_device);
+    return check_launch("rgbd_lsm");
+}
+
+int tde_rgbd_odometry(const tde_rgbd_frame *prev, const tde_rgbd_frame *curr, const tde_intrinsics *intr0,
+                      const tde_rgbd_params *params, const double *init_pose12, double *pose12_device,
+                      int *status_device, void *scratch, size_t scratch_bytes, void *stream) {
+    if (!prev || !curr || !intr0 || !params || !pose12_device || !status_device || !scratch)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_odometry: null argument");
+    const int levels = params->levels;
+    if (levels < 1 || levels > TDE_RGBD_MAX_LEVELS || (intr0->cols >> (levels - 1)) < 4 ||
+        (intr0->rows >> (levels - 1)) < 4)
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_odometry: %d levels for a %dx%d frame", levels, intr0->cols,
+                         intr0->rows);
+    for (int l = 0; l < levels; ++l) {
+        if (!prev->intensity[l] || !prev->depth[l] || !curr->intensity[l] || !curr->depth[l] || !curr->dx[l] ||
+            !curr->dy[l])
+            return set_error(TDE_ERR_INVALID_ARG, "rgbd_odometry: level %d is missing a buffer", l);
+        if (params->iters[l] < 0 || params->iters[l] > 100)
+            return set_error(TDE_ERR_INVALID_ARG, "rgbd_odometry: iters[%d] = %d", l, params->iters[l]);
+    }
+    if (scratch_bytes < tde_rgbd_odometry_scratch_bytes(intr0->cols, intr0->rows))
+        return set_error(TDE_ERR_INVALID_ARG, "rgbd_odometry: scratch %zu < %zu bytes", scratch_bytes,
+                         tde_rgbd_odometry_scratch_bytes(intr0->cols, intr0->rows));
+    cudaStream_t s = as_stream(stream);
+    const unsigned nb0 = odo_blocks(intr0->cols, intr0->rows);
+    unsigned long long *res = static_cast<unsigned long long *>(scratch);
+    double *lsm = reinterpret_cast<double *>(res + 2 * nb0);
+    Pose12 P;
+    const double ident[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+    for (int k = 0; k < 12; ++k) P.v[k] = init_pose12 ? init_pose12[k] : ident[k];
+    set_pose_kernel<<<1, 32, 0, s>>>(P, pose12_device, status_device);
+    int st = check_launch("rgbd_odometry");
+    if (st) return st;
+    for (int l = levels - 1; l >= 0; --l) {
+        const float div = (float)(1 << l);
+        const tde_intrinsics in = {intr0->fx / div, intr0->fy / div, intr0->cx / div, intr0->cy / div,
+                                   intr0->cols >> l, intr0->rows >> l};
+        const Level L = make_level(prev->intensity[l], prev->depth[l], curr->intensity[l], curr->depth[l], curr->dx[l],
+                                   curr->dy[l], in, params->max_depth_diff, params->max_depth,
+                                   params->min_gradient[l]);
+        const unsigned nb = odo_blocks(in.cols, in.rows);
+        for (int it = 0; it < params->iters[l]; ++it) {
+            residual_kernel<<<nb, kThreads, 0, s>>>(L, pose12_device, res);
+            lsm_kernel<<<nb, kThreads, 0, s>>>(L, pose12_device, res, (int)nb, lsm, nullptr);
+            if ((st = check_launch("rgbd_odometry"))) return st;
+            TDE_TRY(launch_rgbd_solve(lsm, (int)nb, pose12_device, status_device, s));
+        }
+    }
+    return TDE_OK;
+}
+
+}  // extern "C"

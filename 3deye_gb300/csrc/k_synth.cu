@@ -112,6 +112,31 @@ __global__ void synth_kernel(const double *__restrict__ scene, const SynthParams
     }
 }
 
+// Procedural colour of a surface point: triangle waves of its coordinates
+// (exact or correctly rounded operations; the CPU sensor's texture).
+__device__ __forceinline__ double tri(double a) { return fabs(a - floor(a) - 0.5); }
+
+__global__ void synth_rgb_kernel(const double *__restrict__ scene, const SynthParams p, uint8_t *__restrict__ rgb) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= p.intr.cols || v >= p.intr.rows) return;
+    double dc[3] = {((double)u - p.intr.cx) / p.intr.fx, ((double)v - p.intr.cy) / p.intr.fy, 1.0};
+    double d[3] = {p.R[0] * dc[0] + p.R[1] * dc[1] + p.R[2] * dc[2], p.R[3] * dc[0] + p.R[4] * dc[1] + p.R[5] * dc[2],
+                   p.R[6] * dc[0] + p.R[7] * dc[1] + p.R[8] * dc[2]};
+    double best = 1e300;
+    for (int k = 0; k < p.nprim; ++k) best = fmin(best, hit_prim(scene + 8 * k, p.t, d));
+    uint8_t *o = rgb + 3 * ((size_t)v * p.intr.cols + u);
+    if (best < 1e299) {
+        const double X[3] = {p.t[0] + best * d[0], p.t[1] + best * d[1], p.t[2] + best * d[2]};
+        const double a = tri(X[0] * 7.0 + X[1] * 3.0), b = tri(X[1] * 9.0 - X[2] * 5.0),
+                     c = tri(X[2] * 11.0 + X[0] * 4.0), e = tri((X[0] + X[1] + X[2]) * 23.0);
+        o[0] = (uint8_t)(40.0 + 400.0 * a * 0.5 + 200.0 * e * 0.5);
+        o[1] = (uint8_t)(40.0 + 400.0 * b * 0.5 + 200.0 * e * 0.5);
+        o[2] = (uint8_t)(40.0 + 400.0 * c * 0.5 + 200.0 * e * 0.5);
+    } else {
+        o[0] = o[1] = o[2] = 0;
+    }
+}
+
 }  // namespace
 }  // namespace tde
 
@@ -133,6 +158,23 @@ int tde_synth_depth(const double *scene, int nprim, const double *pose12, const 
     dim3 block(32, 8), grid(div_up(intr->cols, 32), div_up(intr->rows, 8));
     synth_kernel<<<grid, block, 0, as_stream(stream)>>>(scene, p, out_mm, out_m);
     return check_launch("synth_depth");
+}
+
+// Synthetic colour camera: the scene's procedural texture at each pixel's
+// nearest hit from pose12 (host), black without a hit; rgb: device, 3 bytes
+// a pixel.  Same ray and camera as tde_synth_depth.
+int tde_synth_rgb(const double *scene, int nprim, const double *pose12, const tde_intrinsics *intr, uint8_t *rgb,
+                  void *stream) {
+    if (!scene || nprim <= 0 || !pose12 || !intr || !rgb || intr->cols <= 0 || intr->rows <= 0)
+        return set_error(TDE_ERR_INVALID_ARG, "synth_rgb: bad arguments");
+    SynthParams p = {};
+    for (int k = 0; k < 9; ++k) p.R[k] = pose12[k];
+    for (int k = 0; k < 3; ++k) p.t[k] = pose12[9 + k];
+    p.intr = *intr;
+    p.nprim = nprim;
+    dim3 block(32, 8), grid(div_up(intr->cols, 32), div_up(intr->rows, 8));
+    synth_rgb_kernel<<<grid, block, 0, as_stream(stream)>>>(scene, p, rgb);
+    return check_launch("synth_rgb");
 }
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 // defines its own global `dim3`, so this layer reaches the GPU only through
 // tde_capi.h.  Every function completes its GPU work before returning, as the
 // reference's clFinish-after-launch does (common/src/opencl_helper.cpp:662-672).
+#include <algorithm>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -43,7 +44,10 @@ const char *const kKnown[] = {
     "resize_vertex_map", "resize_normal_map", "transform_map", "scan_slice_of_both_volumes", "extract_slice_as_cloud",
     "scan_slice_of_tsdf_volume", "extract_tsdf_slice_as_cloud", "scan_pow2", "scan_subarrays", "clean_tsdf_slice",
     "clean_color_slice", "init_tsdf", "integrate_color_volume", "scan_the_whole_array", "extract_tsdf_cloud",
-    "extract_colors", "generate_image", "scan_slice_of_color_volume", "extract_color_slice_as_cloud"};
+    "extract_colors", "generate_image", "scan_slice_of_color_volume", "extract_color_slice_as_cloud",
+    "prepare_initial_frames_rgbd", "generate_intensity_and_depth_pyramid", "create_intensity_derivatives",
+    "scan_for_interest_point", "extract_interest_points", "scan_list_of_valid_correspondence",
+    "compute_least_squares_equation"};
 
 string base_name(const string &n) {
     if (n.size() > 3 && n.compare(n.size() - 3, 3, ".cl") == 0) return n.substr(0, n.size() - 3);
@@ -489,4 +493,241 @@ void Clean_Buff(gpu_array_base *gPtr, opencl_kernel *) {
     int width = (int)gPtr->height();
     check(tde_clean_buff(static_cast<float *>(dev(gPtr, "Clean_Buff")), width, nullptr), "Clean_Buff");
     sync("Clean_Buff");
+}
+
+// ---- dense RGB-D odometry (opencl_wrappers.cpp:345-362, 1008-1466) ----
+namespace {
+
+void need_bytes(gpu_array_base *a, size_t bytes, const char *what) {
+    if (!a || !a->device() || a->bytes() < bytes)
+        throw std::runtime_error(std::string(what) + ": buffer missing or smaller than " + std::to_string(bytes) +
+                                 " bytes");
+}
+
+const int16_t *deriv(gpu_array_base *a, size_t n, const char *what) {
+    if (a && a->elem_size() != sizeof(int16_t))
+        throw std::runtime_error(std::string(what) + ": derivatives must be short (signed Sobel responses)");
+    need_bytes(a, n * sizeof(int16_t), what);
+    return static_cast<const int16_t *>(a->device());
+}
+
+// pose12 (R row-major, t) of a matrix_3f / vector_3f pair and back
+void to_pose(const matrix_3f &R, const vector_3f &t, double *p) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) p[3 * r + c] = R.data[r].data[c];
+    for (int k = 0; k < 3; ++k) p[9 + k] = t.data[k];
+}
+
+}  // namespace
+
+void Prepare_Data_For_RGBD(gpu_array_base *gDepth_Frame, gpu_array_base *gRGB_Frame, gpu_array_base *gIntensity_Image,
+                           gpu_array_base *gMetric_Depth, opencl_kernel *) {
+    const char *what = "Prepare_Data_For_RGBD";
+    if (!gDepth_Frame) throw std::runtime_error("Prepare_Data_For_RGBD: no depth frame");
+    const int W = (int)gDepth_Frame->width(), H = (int)std::max(1u, gDepth_Frame->height());
+    const size_t n = (size_t)W * H;
+    need_bytes(gDepth_Frame, n * sizeof(uint16_t), what);
+    need_bytes(gRGB_Frame, n * 3, what);
+    need_bytes(gIntensity_Image, n, what);
+    need_bytes(gMetric_Depth, n * sizeof(float), what);
+    check(tde_rgbd_prepare(static_cast<const uint16_t *>(gDepth_Frame->device()),
+                           static_cast<const uint8_t *>(gRGB_Frame->device()),
+                           W, H, static_cast<uint8_t *>(gIntensity_Image->device()),
+                           static_cast<float *>(gMetric_Depth->device()), nullptr),
+          what);
+    sync(what);
+}
+
+void Generate_Intensity_And_Depth_Pyramid(vector<gpu_array_base *> &ip, vector<gpu_array_base *> &dp, intrinsics Intr,
+                                          int levels, kernel_manager *) {
+    const char *what = "Generate_Intensity_And_Depth_Pyramid";
+    if ((int)ip.size() < levels || (int)dp.size() < levels) throw std::runtime_error(std::string(what) + ": fewer buffers than levels");
+    for (int i = 1; i < levels; ++i) {
+        const int W = Intr.cols >> (i - 1), H = Intr.rows >> (i - 1);
+        const size_t n2 = (size_t)(W >> 1) * (H >> 1);
+        need_bytes(ip[i - 1], (size_t)W * H, what);
+        need_bytes(dp[i - 1], (size_t)W * H * sizeof(float), what);
+        need_bytes(ip[i], n2, what);
+        need_bytes(dp[i], n2 * sizeof(float), what);
+        check(tde_rgbd_pyramid(static_cast<const uint8_t *>(ip[i - 1]->device()),
+                               static_cast<const float *>(dp[i - 1]->device()), W, H,
+                               static_cast<uint8_t *>(ip[i]->device()), static_cast<float *>(dp[i]->device()), nullptr),
+              what);
+    }
+    sync(what);
+}
+
+void Create_Intensity_Derivatives(vector<gpu_array_base *> &ip, vector<gpu_array_base *> &DI_dx,
+                                  vector<gpu_array_base *> &DI_dy, intrinsics Intr, int levels, kernel_manager *) {
+    const char *what = "Create_Intensity_Derivatives";
+    if ((int)ip.size() < levels || (int)DI_dx.size() < levels || (int)DI_dy.size() < levels)
+        throw std::runtime_error(std::string(what) + ": fewer buffers than levels");
+    for (int i = 0; i < levels; ++i) {
+        const int W = Intr.cols >> i, H = Intr.rows >> i;
+        const size_t n = (size_t)W * H;
+        need_bytes(ip[i], n, what);
+        deriv(DI_dx[i], n, what);
+        deriv(DI_dy[i], n, what);
+        check(tde_rgbd_derivatives(static_cast<const uint8_t *>(ip[i]->device()), W, H,
+                                   static_cast<int16_t *>(DI_dx[i]->device()),
+                                   static_cast<int16_t *>(DI_dy[i]->device()), nullptr),
+              what);
+    }
+    sync(what);
+}
+
+void Accumulate_Points_Of_Interest_For_RGBD(gpu_array_base *DI_dx, gpu_array_base *DI_dy, float Depth_Scale,
+                                            gpu_array_base *Points_Of_Interest, gpu_array_base *Num_Of_Points,
+                                            int &num_of_points, kernel_manager *) {
+    const char *what = "Accumulate_Points_Of_Interest_For_RGBD";
+    if (!DI_dx) throw std::runtime_error(std::string(what) + ": no derivatives");
+    const int W = (int)DI_dx->width(), H = (int)std::max(1u, DI_dx->height());
+    const size_t n = (size_t)W * H;
+    const int16_t *dx = deriv(DI_dx, n, what), *dy = deriv(DI_dy, n, what);
+    need_bytes(Num_Of_Points, sizeof(uint32_t), what);
+    uint32_t capacity = 0;
+    if (Points_Of_Interest) {
+        need_bytes(Points_Of_Interest, sizeof(tde_point2i), what);
+        capacity = (uint32_t)(Points_Of_Interest->bytes() / sizeof(tde_point2i));
+    }
+    const size_t sb = tde_rgbd_points_scratch_bytes(W, H);
+    void *scratch = nullptr;
+    check(tde_device_malloc(&scratch, sb), what);
+    const int st = tde_rgbd_points_of_interest(dx, dy, W, H, Depth_Scale, scratch, sb,
+                                               capacity ? static_cast<tde_point2i *>(Points_Of_Interest->device())
+                                                        : nullptr,
+                                               capacity, static_cast<uint32_t *>(Num_Of_Points->device()), nullptr);
+    const int st2 = tde_device_synchronize();
+    tde_device_free(scratch);
+    check(st, what);
+    check(st2, what);
+    uint32_t cnt = 0;
+    check(tde_memcpy(&cnt, Num_Of_Points->device(), sizeof(cnt), 1), what);
+    num_of_points = (int)cnt;
+}
+
+namespace {
+
+void fill_pairs(gpu_array_base *I_Prev, gpu_array_base *D_Prev, gpu_array_base *I_Curr, gpu_array_base *D_Curr,
+                gpu_array_base *points, float Depth_Threshold, int npoints, const matrix_3f &R, const vector_3f &t,
+                gpu_array_base *cprev, gpu_array_base *ccurr, gpu_array_base *diff, gpu_array_base *count,
+                int *h_count, float *sigma_squared) {
+    const char *what = "Fill_List_Of_Valid_Correspondence_RGBD";
+    if (!I_Prev || npoints < 0) throw std::runtime_error(std::string(what) + ": bad arguments");
+    const int W = (int)I_Prev->width(), H = (int)std::max(1u, I_Prev->height());
+    const size_t n = (size_t)W * H;
+    need_bytes(I_Prev, n, what);
+    need_bytes(D_Prev, n * sizeof(float), what);
+    need_bytes(I_Curr, n, what);
+    need_bytes(D_Curr, n * sizeof(float), what);
+    need_bytes(count, sizeof(uint32_t), what);
+    const size_t np = (size_t)npoints;
+    if (np) {
+        need_bytes(points, np * sizeof(tde_point2i), what);
+        need_bytes(cprev, np * sizeof(tde_point2i), what);
+        need_bytes(ccurr, np * sizeof(tde_point2i), what);
+        need_bytes(diff, np * sizeof(float), what);
+    }
+    float proj[12];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) proj[3 * r + c] = R.data[r].data[c];
+    for (int k = 0; k < 3; ++k) proj[9 + k] = t.data[k];
+    void *sum = nullptr;
+    check(tde_device_malloc(&sum, sizeof(double)), what);
+    const int st = np ? tde_rgbd_correspondences(
+                            static_cast<const uint8_t *>(I_Prev->device()), static_cast<const float *>(D_Prev->device()),
+                            static_cast<const uint8_t *>(I_Curr->device()), static_cast<const float *>(D_Curr->device()),
+                            nullptr, nullptr, W, H, static_cast<const tde_point2i *>(points->device()), (uint32_t)np,
+                            proj, Depth_Threshold, 35.f, 0.f, static_cast<tde_point2i *>(cprev->device()),
+                            static_cast<tde_point2i *>(ccurr->device()), static_cast<float *>(diff->device()),
+                            static_cast<uint32_t *>(count->device()), static_cast<double *>(sum), nullptr)
+                      : tde_memset(count->device(), 0, sizeof(uint32_t));
+    double s2 = 0.0;
+    int st2 = tde_device_synchronize();
+    if (st == TDE_OK && st2 == TDE_OK && np) st2 = tde_memcpy(&s2, sum, sizeof(s2), 1);
+    tde_device_free(sum);
+    check(st, what);
+    check(st2, what);
+    if (h_count) {
+        uint32_t c = 0;
+        check(tde_memcpy(&c, count->device(), sizeof(c), 1), what);
+        *h_count = (int)c;
+    }
+    if (sigma_squared) *sigma_squared = (float)s2;
+}
+
+}  // namespace
+
+void Fill_List_Of_Valid_Correspondence_RGBD(gpu_array_base *I_Prev, gpu_array_base *D_Prev, gpu_array_base *I_Curr,
+                                            gpu_array_base *D_Curr, gpu_array_base *Points_Of_Interest,
+                                            float Depth_Threshold, int Num_Of_Points_Of_Interest, matrix_3f R,
+                                            vector_3f t, gpu_array_base *cprev, gpu_array_base *ccurr,
+                                            gpu_array_base *diff, gpu_array_base *Num_Of_Correspondence,
+                                            int &hNum_Of_Correspondence, float &sigma_squared, opencl_kernel *) {
+    fill_pairs(I_Prev, D_Prev, I_Curr, D_Curr, Points_Of_Interest, Depth_Threshold, Num_Of_Points_Of_Interest, R, t,
+               cprev, ccurr, diff, Num_Of_Correspondence, &hNum_Of_Correspondence, &sigma_squared);
+}
+
+void Fill_List_Of_Valid_Correspondence_RGBD(gpu_array_base *I_Prev, gpu_array_base *D_Prev, gpu_array_base *I_Curr,
+                                            gpu_array_base *D_Curr, gpu_array_base *Points_Of_Interest,
+                                            float Depth_Threshold, int Num_Of_Points_Of_Interest, matrix_3f R,
+                                            vector_3f t, gpu_array_base *cprev, gpu_array_base *ccurr,
+                                            gpu_array_base *diff, gpu_array_base *Num_Of_Correspondence, float,
+                                            opencl_kernel *) {
+    fill_pairs(I_Prev, D_Prev, I_Curr, D_Curr, Points_Of_Interest, Depth_Threshold, Num_Of_Points_Of_Interest, R, t,
+               cprev, ccurr, diff, Num_Of_Correspondence, nullptr, nullptr);
+}
+
+bool Estimate_Isometry_By_RGBD(vector<gpu_array_base *> &I_Prev, vector<gpu_array_base *> &D_Prev,
+                               vector<gpu_array_base *> &I_Curr, vector<gpu_array_base *> &D_Curr,
+                               vector<gpu_array_base *> &DI_dx, vector<gpu_array_base *> &DI_dy, intrinsics Intr,
+                               float RGBD_Depth_Threshold, int levels, matrix_3f Init_R, vector_3f Init_t,
+                               matrix_3f &Estimated_Rotation, vector_3f &Estimated_Translation, kernel_manager *) {
+    const char *what = "Estimate_Isometry_By_RGBD";
+    if (levels < 1 || levels > TDE_RGBD_MAX_LEVELS)
+        throw std::runtime_error(std::string(what) + ": 1 to 4 pyramid levels");
+    if ((int)I_Prev.size() < levels || (int)D_Prev.size() < levels || (int)I_Curr.size() < levels ||
+        (int)D_Curr.size() < levels || (int)DI_dx.size() < levels || (int)DI_dy.size() < levels)
+        throw std::runtime_error(std::string(what) + ": fewer buffers than levels");
+    tde_rgbd_frame prev = {}, curr = {};
+    for (int l = 0; l < levels; ++l) {
+        const size_t n = (size_t)(Intr.cols >> l) * (Intr.rows >> l);
+        need_bytes(I_Prev[l], n, what);
+        need_bytes(D_Prev[l], n * sizeof(float), what);
+        need_bytes(I_Curr[l], n, what);
+        need_bytes(D_Curr[l], n * sizeof(float), what);
+        prev.intensity[l] = static_cast<const uint8_t *>(I_Prev[l]->device());
+        prev.depth[l] = static_cast<const float *>(D_Prev[l]->device());
+        curr.intensity[l] = static_cast<const uint8_t *>(I_Curr[l]->device());
+        curr.depth[l] = static_cast<const float *>(D_Curr[l]->device());
+        curr.dx[l] = deriv(DI_dx[l], n, what);
+        curr.dy[l] = deriv(DI_dy[l], n, what);
+    }
+    tde_rgbd_params params;
+    tde_rgbd_default_params(&params);
+    params.levels = levels;
+    params.max_depth_diff = RGBD_Depth_Threshold;
+    double init[12], pose[12];
+    to_pose(Init_R, Init_t, init);
+    const size_t sb = tde_rgbd_odometry_scratch_bytes(Intr.cols, Intr.rows);
+    void *scratch = nullptr, *dpose = nullptr;
+    check(tde_device_malloc(&scratch, sb), what);
+    if (tde_device_malloc(&dpose, 16 * sizeof(double)) != TDE_OK) {
+        tde_device_free(scratch);
+        check(TDE_ERR_OOM, what);
+    }
+    int *dstatus = reinterpret_cast<int *>(static_cast<double *>(dpose) + 12);
+    int st = tde_rgbd_odometry(&prev, &curr, I(Intr), &params, init, static_cast<double *>(dpose), dstatus, scratch,
+                               sb, nullptr);
+    int status = 0;
+    if (st == TDE_OK) st = tde_device_synchronize();
+    if (st == TDE_OK) st = tde_memcpy(pose, dpose, sizeof(pose), 1);
+    if (st == TDE_OK) st = tde_memcpy(&status, dstatus, sizeof(status), 1);
+    tde_device_free(scratch);
+    tde_device_free(dpose);
+    check(st, what);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Estimated_Rotation.data[r].data[c] = (float)pose[3 * r + c];
+    for (int k = 0; k < 3; ++k) Estimated_Translation.data[k] = (float)pose[9 + k];
+    return (status & 2) != 0;
 }

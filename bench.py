@@ -82,7 +82,7 @@ def parse():
                     help="frames of the CPU baseline sample (about 11 s on 16 cores; capped by the sequence length)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip", default="", help="comma list of further passes to leave out (color, learned, cyclic, "
-                                               "config1), e.g. for a short profiling run")
+                                               "config1, rgbd), e.g. for a short profiling run")
     ap.add_argument("--f64-frames", type=int, default=30,
                     help="leading frames of the sequence the full-FP64 oracle also runs (ATE of the GPU trajectory "
                          "against it)")
@@ -534,6 +534,83 @@ def color_pass(tde, pl, torch, cfg, traj, frames, W, n, ws, dev, pose_a):
     return color, export
 
 
+def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
+    """Pass R: dense RGB-D odometry (Estimate_Isometry_By_RGBD) between
+    consecutive frames of a rendered sequence with colour: per frame the
+    intensity/depth pyramid and Sobel derivatives, then 4 levels of
+    Gauss-Newton (7, 7, 7, 10 steps) against the previous frame.  Depth
+    (noisy, uint16 mm) and RGB frames are rendered by the GPU sensor and
+    resident in HBM."""
+    import numpy as np
+    rg = importlib.import_module("3deye_gb300.rgbd")
+    n = pairs + warm + 1
+    frames, traj, scene = make_frames(tde, syn, cfg, n, rank + 17, dev)
+    intr = tde.Intrinsics(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    d_scene = torch.from_numpy(np.ascontiguousarray(scene, np.float64)).to(dev)
+    rgb = torch.empty((n, cfg.rows, cfg.cols, 3), dtype=torch.uint8, device=dev)
+    for i in range(n):
+        rg.synth_rgb(d_scene, scene.shape[0], traj[i], intr, rgb[i])
+    torch.cuda.synchronize()
+    bufs = [rg.RgbdFrame(cfg.cols, cfg.rows, 4, dev) for _ in range(2)]
+    od = rg.RgbdOdometry(intr)
+    s = torch.cuda.Stream(dev)
+    poses = torch.zeros((n, 12), dtype=torch.float64, device=dev)
+    stats = torch.zeros(n, dtype=torch.int32, device=dev)
+
+    def step(i):
+        bufs[i & 1].load(frames[i], rgb[i], s)
+        od.enqueue(bufs[(i - 1) & 1], bufs[i & 1], None, s)
+        poses[i].copy_(od.pose, non_blocking=True)
+        stats[i:i + 1].copy_(od.status, non_blocking=True)
+    with torch.cuda.stream(s):
+        bufs[0].load(frames[0], rgb[0], s)
+        for i in range(1, warm + 1):
+            step(i)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.synchronize()
+        barrier_sync(ws)
+        e0.record(s)
+        for i in range(warm + 1, n):
+            step(i)
+        e1.record(s)
+    s.synchronize()
+    ms = max_over_ranks(ws, e0.elapsed_time(e1))
+    est = poses.cpu().numpy()
+    st = stats.cpu().numpy()
+    et, er = [], []
+    for i in range(1, n):
+        Rp, tp = traj[i - 1][:9].reshape(3, 3), traj[i - 1][9:]
+        Rc, tc = traj[i][:9].reshape(3, 3), traj[i][9:]
+        gR, gt = Rc.T @ Rp, Rc.T @ (tp - tc)
+        Re = est[i][:9].reshape(3, 3) @ gR.T
+        et.append(np.linalg.norm(est[i][9:] - gt))
+        er.append(np.degrees(np.arccos(np.clip((np.trace(Re) - 1) / 2, -1, 1))))
+    levels = 4
+    launches = (1 + (levels - 1) + levels) + (1 + 3 * sum(int(x) for x in od.params.iters[:levels]))
+    out = {"value": round(ws * pairs / (ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(ms / pairs, 5),
+           "gpu_launches": launches * pairs,
+           "relative_pose_error": {"mean_translation_m": round(float(np.mean(et)), 6),
+                                   "mean_rotation_deg": round(float(np.mean(er)), 5),
+                                   "mean_step_translation_m": round(float(np.mean(
+                                       [np.linalg.norm(traj[i][9:] - traj[i - 1][9:]) for i in range(1, n)])), 6),
+                                   "frames_without_a_solved_step": int(((st[1:] & 2) == 0).sum())},
+           "note": "640x480 noisy depth + rendered texture, resident in HBM; per frame: intensity, 4-level "
+                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes + 1 FP64 solve each)"}
+    if with_cpu:
+        from oracle import oracle as orc
+        fr = frames[:4].view(torch.int16).cpu().numpy().view(np.uint16)
+        cols = rgb[:4].cpu().numpy()
+        lv = [orc.rgbd_levels(fr[i], cols[i], levels) for i in range(4)]
+        io = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+        t0 = time.perf_counter()
+        for i in range(1, 4):
+            orc.rgbd_odometry(lv[i - 1], lv[i], io, [7, 7, 7, 10], [10.0] * 4)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(3 / dt, 3), "unit": "frames/s", "cores": 1, "kind": "port",
+                               "sample": "odometry of 3 frame pairs (pyramids prepared beforehand)"}
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -634,6 +711,9 @@ def run_ours(args, ws, rank, local):
         cyclic = cyclic_run(tde, syn, pl, torch, dev, rank)
     if "config1" not in skip:
         config1 = config1_run(tde, syn, pl, torch, dev, rank, ws, rank == 0 and ws == 1 and not args.no_cpu_baseline)
+    rgbd = None
+    if "rgbd" not in skip:
+        rgbd = rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, rank == 0 and ws == 1 and not args.no_cpu_baseline)
 
     # ---- pass C: the learned refiner in place of the bilateral filter -------
     learned = None
@@ -777,6 +857,7 @@ def run_ours(args, ws, rank, local):
         "model_export": export,
         "cyclic_volume": cyclic,
         "config1": config1,
+        "rgbd_odometry": rgbd,
     }
     return line
 

@@ -105,4 +105,66 @@ void Generate_Image(gpu_array_base *Vertex_Map, gpu_array_base *Normal_Map, intr
 
 void Clean_Buff(gpu_array_base *gPtr, opencl_kernel *clean_buff_kernel);
 
+/* Dense RGB-D odometry (common/inc/opencl_wrappers.h:99-103, 227-292).
+ * Buffers: gDepth_Frame unsigned short millimetres, gRGB_Frame 3 bytes a
+ * pixel, intensity unsigned char, metric depth float, DI_dx / DI_dy short
+ * (the reference declares unsigned char, which cannot hold a signed Sobel
+ * response), points of interest and correspondences point_2i.  Pyramids and
+ * derivative vectors hold one buffer per level, level 0 finest. */
+void Prepare_Data_For_RGBD(gpu_array_base *gDepth_Frame, gpu_array_base *gRGB_Frame, gpu_array_base *gIntensity_Image,
+                           gpu_array_base *gMetric_Depth, opencl_kernel *prepare_initial_frames_rgbd);
+
+void Generate_Intensity_And_Depth_Pyramid(vector<gpu_array_base *> &intensity_pyramid,
+                                          vector<gpu_array_base *> &metric_depth_pyramid, intrinsics Intr,
+                                          int Pyramid_Level_Num_RGBD, kernel_manager *Gpu_Methods);
+
+void Create_Intensity_Derivatives(vector<gpu_array_base *> &intensity_pyramid, vector<gpu_array_base *> &DI_dx,
+                                  vector<gpu_array_base *> &DI_dy, intrinsics Intr, int Pyramid_Level_Num_RGBD,
+                                  kernel_manager *Gpu_Methods);
+
+/* The pixels with DI_dx^2 + DI_dy^2 >= Depth_Scale in raster order, into
+ * Points_Of_Interest (a caller buffer of point_2i; the reference reassigns
+ * its by-value pointer, so its callers never see the list) up to its size;
+ * the count to Num_Of_Points (one int on the device) and num_of_points. */
+void Accumulate_Points_Of_Interest_For_RGBD(gpu_array_base *DI_dx, gpu_array_base *DI_dy, float Depth_Scale,
+                                            gpu_array_base *Points_Of_Interest, gpu_array_base *Num_Of_Points,
+                                            int &num_of_points, kernel_manager *Gpu_Methods);
+
+/* The pairs of Num_Of_Points_Of_Interest previous-frame points for R, t =
+ * R' = K R K^-1, t' = K t (Calculate_Supplementary_Isometry_Using_Camera_Matrix
+ * form): entry i = the point, its current-frame pixel and I_curr - I_prev, or
+ * (0, 0), (0, 0), 100; Num_Of_Correspondence (one int on the device) and
+ * hNum_Of_Correspondence receive the kept count, sigma_squared the sum of
+ * squared differences (opencl_wrappers.cpp:1121-1174). */
+void Fill_List_Of_Valid_Correspondence_RGBD(gpu_array_base *I_Prev, gpu_array_base *D_Prev, gpu_array_base *I_Curr,
+                                            gpu_array_base *D_Curr, gpu_array_base *Points_Of_Interest,
+                                            float Depth_Threshold, int Num_Of_Points_Of_Interest, matrix_3f R,
+                                            vector_3f t, gpu_array_base *Correspondent_Points_At_Prev_Frame,
+                                            gpu_array_base *Correspondent_Points_At_Curr_Frame,
+                                            gpu_array_base *Correspondence_Diff_Per_Pair,
+                                            gpu_array_base *Num_Of_Correspondence, int &hNum_Of_Correspondence,
+                                            float &sigma_squared, opencl_kernel *scan_list_of_valid_correspondence);
+/* The header's form (opencl_wrappers.h:261-276, which the reference never
+ * defines): the same, the count left on the device. */
+void Fill_List_Of_Valid_Correspondence_RGBD(gpu_array_base *I_Prev, gpu_array_base *D_Prev, gpu_array_base *I_Curr,
+                                            gpu_array_base *D_Curr, gpu_array_base *Points_Of_Interest,
+                                            float Depth_Threshold, int Num_Of_Points_Of_Interest, matrix_3f R,
+                                            vector_3f t, gpu_array_base *Correspondent_Points_At_Prev_Frame,
+                                            gpu_array_base *Correspondent_Points_At_Curr_Frame,
+                                            gpu_array_base *Correspondence_Diff_Per_Pair,
+                                            gpu_array_base *Num_Of_Correspondence, float sigma_squared,
+                                            opencl_kernel *scan_list_of_valid_correspondence);
+
+/* Gauss-Newton on the weighted photometric error, coarse to fine over
+ * Pyramid_Level_Num_RGBD levels (7, 7, 7, 10 steps, gradient threshold 10),
+ * pairs within RGBD_Depth_Threshold metres in depth, starting from Init_R,
+ * Init_t; the pose maps previous-frame camera points to current-frame ones.
+ * True when at least one step solved, as the reference's isOk. */
+bool Estimate_Isometry_By_RGBD(vector<gpu_array_base *> &I_Prev, vector<gpu_array_base *> &D_Prev,
+                               vector<gpu_array_base *> &I_Curr, vector<gpu_array_base *> &D_Curr,
+                               vector<gpu_array_base *> &DI_dx, vector<gpu_array_base *> &DI_dy, intrinsics Intr,
+                               float RGBD_Depth_Threshold, int Pyramid_Level_Num_RGBD, matrix_3f Init_R,
+                               vector_3f Init_t, matrix_3f &Estimated_Rotation, vector_3f &Estimated_Translation,
+                               kernel_manager *Gpu_Methods);
+
 #endif

@@ -395,6 +395,111 @@ int tde_generate_image(const float *vmap, const float *nmap, int cols, int rows,
                        uint8_t *image, void *stream);
 
 /* ======================================================================== */
+/* f4: dense RGB-D (photometric) odometry                                   */
+/* ======================================================================== */
+/* The reference's second tracker: Prepare_Data_For_RGBD,
+ * Generate_Intensity_And_Depth_Pyramid, Create_Intensity_Derivatives,
+ * Accumulate_Points_Of_Interest_For_RGBD, Fill_List_Of_Valid_Correspondence_RGBD,
+ * Compute_Least_Squares_Equation and Estimate_Isometry_By_RGBD
+ * (opencl_wrappers.cpp:345-362, 1008-1466; declared at opencl_wrappers.h:99-103,
+ * 227-292), after the RGB-D odometry of OpenCV's contrib rgbd module
+ * (Steinbruecker, Sturm, Cremers 2011).  The reference copy does not run as
+ * written; these entry points implement the method it follows, with its
+ * conventions: 8-bit grey intensity (BT.601 luma, 14-bit fixed point), depth
+ * in metres (raw mm x 0.001, valid in (0, max_depth)), 3x3 Sobel derivatives
+ * (int16, zero on the image border), SOBEL_SCALE 1/8,
+ * DEFAULT_DEPTH_THRESHOLD_RGBD 0.07 m.  Poses map previous-frame camera
+ * points to current-frame ones (P_curr = R P_prev + t), row-major R then t,
+ * FP64. */
+#define TDE_RGBD_MAX_LEVELS 4
+/* point_2i: common/inc/elementary_points.h */
+typedef struct tde_point2i { int x, y; } tde_point2i;
+
+/* Prepare_Data_For_RGBD: intensity (cols x rows bytes) and metric depth
+ * (floats) from a depth frame (uint16 mm) and an RGB frame (3 bytes a pixel). */
+int tde_rgbd_prepare(const uint16_t *depth_mm, const uint8_t *rgb, int cols, int rows, uint8_t *intensity,
+                     float *depth_m, void *stream);
+/* One pyramid step (Generate_Intensity_And_Depth_Pyramid's kernel
+ * generate_intensity_and_depth_pyramid, absent): intensity = rounded mean of
+ * each 2x2 block, depth = the block's top-left sample; outputs cols/2 x rows/2. */
+int tde_rgbd_pyramid(const uint8_t *intensity, const float *depth_m, int cols, int rows, uint8_t *intensity_half,
+                     float *depth_half, void *stream);
+/* Create_Intensity_Derivatives (kernel create_intensity_derivatives, absent):
+ * 3x3 Sobel dI/dx and dI/dy as int16. */
+int tde_rgbd_derivatives(const uint8_t *intensity, int cols, int rows, int16_t *dx, int16_t *dy, void *stream);
+/* Accumulate_Points_Of_Interest_For_RGBD (scan_for_interest_point.cl with its
+ * x/y indexing corrected, extract_interest_points absent): the pixels with
+ * dx^2 + dy^2 >= scale, raster order, into points (up to capacity); the count
+ * to *count_device.  Scratch: tde_rgbd_points_scratch_bytes(). */
+size_t tde_rgbd_points_scratch_bytes(int cols, int rows);
+int tde_rgbd_points_of_interest(const int16_t *dx, const int16_t *dy, int cols, int rows, float scale, void *scratch,
+                                size_t scratch_bytes, tde_point2i *points, uint32_t capacity, uint32_t *count_device,
+                                void *stream);
+/* R' = K R K^-1 and t' = K t of a pose (the projective form the
+ * correspondence search takes; Calculate_Supplementary_Isometry_Using_Camera_Matrix,
+ * opencl_wrappers.cpp:1176-1196), FP64 then float: proj12 = R' row-major, t'.
+ * Host only. */
+int tde_rgbd_projective(const double *pose12, const tde_intrinsics *intr, float *proj12);
+/* Fill_List_Of_Valid_Correspondence_RGBD (scan_list_of_valid_correspondence.cl):
+ * each point p of the previous frame (all pixels when points is NULL) with
+ * depth z maps to q = z R' [p 1] + t' and pixel round(q.xy / q.z) of the
+ * current frame; the pair is kept when that pixel lies in the image, has
+ * depth within max_depth_diff of q.z and a Sobel gradient of at least
+ * min_gradient / SOBEL_SCALE (the current frame's dx, dy; both NULL for no
+ * gradient test, as for points already filtered by
+ * tde_rgbd_points_of_interest).  corr_prev[i], corr_curr[i] = the pixels and
+ * diff[i] = I_curr - I_prev for kept pairs, (0, 0), (0, 0), 100 otherwise (the
+ * reference's marker); *count_device and *sum_r2_device (double) receive the
+ * kept count and the sum of squared differences.  proj12 is host memory. */
+int tde_rgbd_correspondences(const uint8_t *i_prev, const float *d_prev, const uint8_t *i_curr, const float *d_curr,
+                             const int16_t *dx, const int16_t *dy, int cols, int rows, const tde_point2i *points,
+                             uint32_t npoints, const float *proj12, float max_depth_diff, float max_depth,
+                             float min_gradient, tde_point2i *corr_prev, tde_point2i *corr_curr, float *diff,
+                             uint32_t *count_device, double *sum_r2_device, void *stream);
+/* Compute_Least_Squares_Equation (compute_least_squares_equation.cl with its
+ * row indexing corrected): over every kept pair of the previous frame's
+ * pixels for pose12 (host) at this level's intrinsics, sigma = sqrt(mean
+ * diff^2), w = 1 / (sigma + |diff|), C = w J (J the photometric Jacobian of the
+ * current-frame point for a left perturbation exp(xi)); sums_device[0..26] =
+ * the upper triangle of [A | b] with A = sum C C^T, b = -sum w diff C (the
+ * 27-term layout of Estimate_Combined), sums_device[27] = the pair count;
+ * *sigma_device = sigma.  Scratch: tde_rgbd_odometry_scratch_bytes(). */
+int tde_rgbd_lsm(const uint8_t *i_prev, const float *d_prev, const uint8_t *i_curr, const float *d_curr,
+                 const int16_t *dx, const int16_t *dy, const tde_intrinsics *intr, const double *pose12,
+                 float max_depth_diff, float max_depth, float min_gradient, void *scratch, size_t scratch_bytes,
+                 double *sums_device, float *sigma_device, void *stream);
+
+/* A frame's pyramid (level 0 finest; dx, dy needed for the current frame only). */
+typedef struct tde_rgbd_frame {
+    const uint8_t *intensity[TDE_RGBD_MAX_LEVELS];
+    const float *depth[TDE_RGBD_MAX_LEVELS];
+    const int16_t *dx[TDE_RGBD_MAX_LEVELS];
+    const int16_t *dy[TDE_RGBD_MAX_LEVELS];
+} tde_rgbd_frame;
+typedef struct tde_rgbd_params {
+    int levels;                                /* 1..4 (OpenCV's default 4) */
+    int iters[TDE_RGBD_MAX_LEVELS];            /* per level, 0 finest: 7, 7, 7, 10 */
+    float min_gradient[TDE_RGBD_MAX_LEVELS];   /* Sobel / 8 units: 10 each */
+    float max_depth_diff;                      /* DEFAULT_DEPTH_THRESHOLD_RGBD 0.07 m */
+    float max_depth;                           /* 35 m */
+} tde_rgbd_params;
+/* The defaults above. */
+void tde_rgbd_default_params(tde_rgbd_params *params);
+size_t tde_rgbd_odometry_scratch_bytes(int cols, int rows);
+/* Estimate_Isometry_By_RGBD: Gauss-Newton on the weighted photometric error,
+ * coarse to fine, params->iters[l] steps at level l, each T <- exp(xi) T with
+ * the FP64 6x6 solve of the ICP path; intr0 is level 0's camera.  Starts from
+ * init_pose12 (host; identity when NULL); the result goes to pose12_device
+ * and *status_device: bit 0 (1) set when a step's solve failed (too few
+ * pairs or A not positive definite) and kept its pose, bit 1 (2) when at
+ * least one step solved.
+ * Launches only, nothing synchronises; 256-byte aligned scratch of
+ * tde_rgbd_odometry_scratch_bytes(). */
+int tde_rgbd_odometry(const tde_rgbd_frame *prev, const tde_rgbd_frame *curr, const tde_intrinsics *intr0,
+                      const tde_rgbd_params *params, const double *init_pose12, double *pose12_device,
+                      int *status_device, void *scratch, size_t scratch_bytes, void *stream);
+
+/* ======================================================================== */
 /* Device memory helpers for hosts that do not include the CUDA headers      */
 /* (the C++ layer of include/3deye/ replaces gpu_array_base's cl_mem          */
 /* allocation, common/src/opencl_helper.cpp:344-420, with these).            */

@@ -30,5 +30,6 @@ build REF_CLEAN_BUFF clean_buff.cl ref_clean_buff &
 build REF_SCAN_SLICE scan_slice_of_both_volumes.cl ref_scan_slice &
 build REF_EXTRACT_SLICE extract_slice_as_cloud.cl ref_extract_slice &
 build REF_CLEAN_COLOR_SLICE clean_color_slice.cl ref_clean_color_slice &
+build REF_LSM compute_least_squares_equation.cl ref_lsm &
 wait
 ls "$OUT"

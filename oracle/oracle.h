@@ -70,6 +70,26 @@ int or_render_depth(const double *scene, int nprim, const double *pose12, const 
                     float *depth_m);
 int or_apply_noise(const float *depth_m, uint16_t *depth_mm, int W, int H, uint32_t seed, uint32_t frame,
                    float max_range_m, float dropout);
+int or_render_rgb(const double *scene, int nprim, const double *pose, const tde_intrinsics *in, uint8_t *rgb);
+
+/* dense RGB-D odometry (oracle_rgbd.c) */
+int or_rgbd_prepare(const uint16_t *depth_mm, const uint8_t *rgb, int W, int H, uint8_t *I, float *D);
+int or_rgbd_pyramid(const uint8_t *I, const float *D, int W, int H, uint8_t *I2, float *D2);
+int or_rgbd_sobel(const uint8_t *I, int W, int H, int16_t *dx, int16_t *dy);
+int or_rgbd_points(const int16_t *dx, const int16_t *dy, int W, int H, float scale, int *points, int capacity);
+void or_rgbd_projective(const double *R, const double *t, const tde_intrinsics *in, float *proj);
+int or_rgbd_pairs(const uint8_t *Ip, const float *Dp, const uint8_t *Ic, const float *Dc, const int16_t *dx,
+                  const int16_t *dy, const tde_intrinsics *in, const double *R, const double *t, float max_depth_diff,
+                  float max_depth, float min_gradient, int *kept, float *resid, double *sum_r2);
+int or_rgbd_lsm(const uint8_t *Ip, const float *Dp, const uint8_t *Ic, const float *Dc, const int16_t *dx,
+                const int16_t *dy, const tde_intrinsics *in, const double *R, const double *t, float max_depth_diff,
+                float max_depth, float min_gradient, double *sums, float *sigma_out);
+int or_rgbd_row_single(int u, int v, float z, const float *Rt12, const tde_intrinsics *in, float dIdx, float dIdy,
+                       float r, float sigma, float *row7);
+int or_rgbd_odometry(const uint8_t *const *Ip, const float *const *Dp, const uint8_t *const *Ic,
+                     const float *const *Dc, const int16_t *const *dx, const int16_t *const *dy,
+                     const tde_intrinsics *in0, int levels, const int *iters, float max_depth_diff, float max_depth,
+                     const float *min_gradient, double *pose12);
 
 #ifdef __cplusplus
 }

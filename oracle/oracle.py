@@ -87,6 +87,16 @@ _sigs = {
     "or_icp_terms_f64": (I, [P, P, P, P, P, P, P, P, pI, C.c_double, C.c_double, P]),
     "or_render_depth": (I, [P, I, P, pI, P]),
     "or_apply_noise": (I, [P, P, I, I, C.c_uint32, C.c_uint32, F, F]),
+    "or_render_rgb": (I, [P, I, P, pI, P]),
+    "or_rgbd_prepare": (I, [P, P, I, I, P, P]),
+    "or_rgbd_pyramid": (I, [P, P, I, I, P, P]),
+    "or_rgbd_sobel": (I, [P, I, I, P, P]),
+    "or_rgbd_points": (I, [P, P, I, I, F, P, I]),
+    "or_rgbd_projective": (None, [P, P, pI, P]),
+    "or_rgbd_pairs": (I, [P, P, P, P, P, P, pI, P, P, F, F, F, P, P, P]),
+    "or_rgbd_lsm": (I, [P, P, P, P, P, P, pI, P, P, F, F, F, P, P]),
+    "or_rgbd_row_single": (I, [I, I, F, P, pI, F, F, F, F, P]),
+    "or_rgbd_odometry": (I, [P, P, P, P, P, P, pI, I, P, F, F, P, P]),
 }
 for _n, (_r, _a) in _sigs.items():
     _f = getattr(lib, _n)
@@ -374,3 +384,115 @@ def icp_terms_f64(vcur, ncur, vprev, nprev, R, t, R_prev_inv, t_prev, intr, dist
                          _p(f64(R_prev_inv)), _p(f64(t_prev)), C.byref(intr), float(dist_thresh), float(angle_thresh),
                          _p(sums))
     return sums
+
+
+# ---------------------------------------------------------------------------
+# dense RGB-D odometry (oracle_rgbd.c)
+# ---------------------------------------------------------------------------
+RGBD_MAX_DEPTH = 35.0        # scan_list_of_valid_correspondence.cl:9-15
+RGBD_DEPTH_DIFF = 0.07       # DEFAULT_DEPTH_THRESHOLD_RGBD, common_defines.h:18
+
+
+def render_rgb(scene, pose12, intr):
+    out = np.zeros((intr.rows, intr.cols, 3), np.uint8)
+    sc = np.ascontiguousarray(scene, np.float64)
+    lib.or_render_rgb(_p(sc), sc.shape[0], _p(np.ascontiguousarray(pose12, np.float64)), C.byref(intr), _p(out))
+    return out
+
+
+def rgbd_prepare(depth_mm, rgb):
+    H, W = depth_mm.shape
+    I8 = np.zeros((H, W), np.uint8)
+    D = np.zeros((H, W), F32)
+    lib.or_rgbd_prepare(_p(np.ascontiguousarray(depth_mm, np.uint16)), _p(np.ascontiguousarray(rgb, np.uint8)), W, H,
+                        _p(I8), _p(D))
+    return I8, D
+
+
+def rgbd_pyramid(I8, D):
+    H, W = I8.shape
+    I2 = np.zeros((H >> 1, W >> 1), np.uint8)
+    D2 = np.zeros((H >> 1, W >> 1), F32)
+    lib.or_rgbd_pyramid(_p(np.ascontiguousarray(I8)), _p(f32(D)), W, H, _p(I2), _p(D2))
+    return I2, D2
+
+
+def rgbd_sobel(I8):
+    H, W = I8.shape
+    dx = np.zeros((H, W), np.int16)
+    dy = np.zeros((H, W), np.int16)
+    lib.or_rgbd_sobel(_p(np.ascontiguousarray(I8)), W, H, _p(dx), _p(dy))
+    return dx, dy
+
+
+def rgbd_points(dx, dy, scale):
+    H, W = dx.shape
+    n = lib.or_rgbd_points(_p(np.ascontiguousarray(dx)), _p(np.ascontiguousarray(dy)), W, H, scale, None, 0)
+    pts = np.zeros((max(n, 1), 2), np.int32)
+    lib.or_rgbd_points(_p(np.ascontiguousarray(dx)), _p(np.ascontiguousarray(dy)), W, H, scale, _p(pts), n)
+    return pts[:n]
+
+
+def rgbd_levels(depth_mm, rgb, levels):
+    """Per level (finest first): intensity, metric depth, Sobel dx, dy."""
+    I8, D = rgbd_prepare(depth_mm, rgb)
+    out = []
+    for l in range(levels):
+        if l:
+            I8, D = rgbd_pyramid(I8, D)
+        dx, dy = rgbd_sobel(I8)
+        out.append((I8, D, dx, dy))
+    return out
+
+
+def rgbd_pairs(prev, curr, intr, pose12, min_gradient, max_depth_diff=RGBD_DEPTH_DIFF, max_depth=RGBD_MAX_DEPTH):
+    """prev, curr: (I, D, dx, dy) of one level.  Returns (count, kept [H,W]
+    (1 + index of the current pixel, 0 for none), residuals, sum r^2)."""
+    H, W = prev[0].shape
+    kept = np.zeros((H, W), np.int32)
+    res = np.zeros((H, W), F32)
+    s = np.zeros(1, np.float64)
+    pose = np.ascontiguousarray(pose12, np.float64)
+    n = lib.or_rgbd_pairs(_p(prev[0]), _p(f32(prev[1])), _p(curr[0]), _p(f32(curr[1])), _p(curr[2]), _p(curr[3]),
+                          C.byref(intr), _p(pose[:9].copy()), _p(pose[9:].copy()), max_depth_diff, max_depth,
+                          min_gradient, _p(kept), _p(res), _p(s))
+    return n, kept, res, float(s[0])
+
+
+def rgbd_lsm(prev, curr, intr, pose12, min_gradient, max_depth_diff=RGBD_DEPTH_DIFF, max_depth=RGBD_MAX_DEPTH):
+    sums = np.zeros(28, np.float64)
+    sigma = np.zeros(1, F32)
+    pose = np.ascontiguousarray(pose12, np.float64)
+    lib.or_rgbd_lsm(_p(prev[0]), _p(f32(prev[1])), _p(curr[0]), _p(f32(curr[1])), _p(curr[2]), _p(curr[3]),
+                    C.byref(intr), _p(pose[:9].copy()), _p(pose[9:].copy()), max_depth_diff, max_depth, min_gradient,
+                    _p(sums), _p(sigma))
+    return sums, float(sigma[0])
+
+
+def rgbd_row_single(u, v, z, Rt12, intr, dIdx, dIdy, r, sigma):
+    row = np.zeros(7, F32)
+    lib.or_rgbd_row_single(u, v, z, _p(f32(Rt12)), C.byref(intr), dIdx, dIdy, r, sigma, _p(row))
+    return row
+
+
+def rgbd_odometry(prev_levels, curr_levels, intr, iters, min_gradient, init_pose12=None,
+                  max_depth_diff=RGBD_DEPTH_DIFF, max_depth=RGBD_MAX_DEPTH):
+    """Pose (12 doubles) mapping previous-frame camera points to current ones, and the failed-solve count."""
+    L = len(prev_levels)
+    keep = []
+
+    def arr(items, k, dtype):
+        a = (C.c_void_p * L)()
+        for l in range(L):
+            x = np.ascontiguousarray(items[l][k], dtype)
+            keep.append(x)
+            a[l] = x.ctypes.data
+        return a
+    pose = np.array([1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0], np.float64) if init_pose12 is None else \
+        np.ascontiguousarray(init_pose12, np.float64).copy()
+    it = np.ascontiguousarray(iters, np.int32)
+    mg = np.ascontiguousarray(min_gradient, F32)
+    failed = lib.or_rgbd_odometry(arr(prev_levels, 0, np.uint8), arr(prev_levels, 1, F32), arr(curr_levels, 0, np.uint8),
+                                  arr(curr_levels, 1, F32), arr(curr_levels, 2, np.int16), arr(curr_levels, 3, np.int16),
+                                  C.byref(intr), L, _p(it), max_depth_diff, max_depth, _p(mg), _p(pose))
+    return pose, failed

@@ -78,6 +78,33 @@ int or_render_depth(const double *scene, int nprim, const double *pose, const td
     return 0;
 }
 
+/* Colour of the nearest hit of each pixel's ray: the procedural texture of
+ * oracle_rgbd.c at the hit point, black without a hit (rgb: 3 bytes a pixel). */
+void or_texture_rgb(const double *X, uint8_t *rgb);
+int or_render_rgb(const double *scene, int nprim, const double *pose, const tde_intrinsics *in, uint8_t *rgb) {
+    const double *R = pose, *t = pose + 9;
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < in->rows; ++v)
+        for (int u = 0; u < in->cols; ++u) {
+            double dc[3] = {((double)u - in->cx) / in->fx, ((double)v - in->cy) / in->fy, 1.0};
+            double d[3] = {R[0] * dc[0] + R[1] * dc[1] + R[2] * dc[2], R[3] * dc[0] + R[4] * dc[1] + R[5] * dc[2],
+                           R[6] * dc[0] + R[7] * dc[1] + R[8] * dc[2]};
+            double best = 1e300;
+            for (int p = 0; p < nprim; ++p) {
+                double h = hit_prim(scene + 8 * p, t, d);
+                if (h < best) best = h;
+            }
+            uint8_t *o = rgb + 3 * ((size_t)v * in->cols + u);
+            if (best < 1e299) {
+                const double X[3] = {t[0] + best * d[0], t[1] + best * d[1], t[2] + best * d[2]};
+                or_texture_rgb(X, o);
+            } else {
+                o[0] = o[1] = o[2] = 0;
+            }
+        }
+    return 0;
+}
+
 /* 32-bit integer hash (lowbias32 constants by C. Wellons, public domain). */
 static uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352dU;

@@ -216,6 +216,35 @@ TDE_REF_EXPORT int ref_clean_color_slice(void *color, const int *mn, const int *
     tde_ref_run_plain(item, (size_t)A.rb.voxels_size.x, (size_t)A.rb.voxels_size.y, 32, 8);
     return 0;
 }
+#elif defined(REF_LSM)
+/* compute_least_squares_equation over n correspondences.  Each item writes
+ * Indexes[id + 0..5] (overlapping its neighbours' entries for n > 1), so the
+ * per-correspondence row is read with n = 1. */
+static struct {
+    Point_Intensity *ip; float *dp; Point_Intensity *ic; unsigned char *dx, *dy; point_2i *cp, *cc; float *diff;
+    float sigma; matrix_3f R; vector_3f t; intrinsics intr; int n; float *idx, *vec;
+} A;
+static void item(void) {
+    compute_least_squares_equation(A.ip, A.dp, A.ic, A.dx, A.dy, A.cp, A.cc, A.diff, A.sigma, A.R, A.t, A.intr,
+                                   A.n, A.idx, A.vec);
+}
+TDE_REF_EXPORT int ref_lsm(const void *i_prev, const float *d_prev, const void *i_curr, const unsigned char *dx,
+                           const unsigned char *dy, const int *corr_prev, const int *corr_curr, const float *diff,
+                           float sigma, const float *R, const float *t, const void *intr, int n, float *indexes,
+                           float *indexes_vector) {
+    A.ip = (Point_Intensity *)i_prev; A.dp = (float *)d_prev; A.ic = (Point_Intensity *)i_curr;
+    A.dx = (unsigned char *)dx; A.dy = (unsigned char *)dy;
+    A.cp = (point_2i *)corr_prev; A.cc = (point_2i *)corr_curr; A.diff = (float *)diff; A.sigma = sigma;
+    memcpy(&A.R, R, sizeof(A.R)); memcpy(&A.t, t, sizeof(A.t)); memcpy(&A.intr, intr, sizeof(A.intr));
+    A.n = n; A.idx = indexes; A.vec = indexes_vector;
+    tde_ref_run_plain(item, (size_t)n, 1, 1, 1);
+    return 0;
+}
+TDE_REF_EXPORT int ref_lsm_sizes(int *out) {
+    out[0] = (int)sizeof(Point_Intensity); out[1] = (int)sizeof(point_2i); out[2] = (int)sizeof(intrinsics);
+    out[3] = (int)sizeof(matrix_3f);
+    return 0;
+}
 #else
 #error "define one REF_<KERNEL>"
 #endif

@@ -25,6 +25,7 @@
 #ifndef TDE_REF_SHIM_H
 #define TDE_REF_SHIM_H
 
+#include <float.h> /* FLT_/DBL_EPSILON: OpenCL C 6.12.2.1 macros */
 #include <math.h>
 #include <stdbool.h>
 #include <stddef.h>

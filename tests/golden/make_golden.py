@@ -237,6 +237,54 @@ def gen_slices():
     return {ci: int(out[f"c{ci}_count"]) for ci in range(len(cases))}
 
 
+def gen_lsm():
+    """compute_least_squares_equation.cl, one correspondence per call (n = 1:
+    the kernel writes Indexes[id + k], so larger n overlaps rows): the six
+    coefficients C and the vector C * diff * w, for seeded poses, pixels,
+    depths, derivatives (its derivative buffers are unsigned char), residuals
+    and sigmas."""
+    rng = np.random.default_rng(17)
+    W, H = 64, 48
+    intr = orc.Intr(58.5, 61.25, 31.7, 24.3, W, H)
+    lib = orc.ref("lsm")
+    sz = np.zeros(4, np.int32)
+    lib.ref_lsm_sizes(p(sz))
+    assert sz[1] == 8 and sz[2] == 24 and sz[3] == 36, sz
+    n = 96
+    cases = {k: [] for k in ("u", "v", "z", "R", "t", "dx", "dy", "diff", "sigma", "C", "vec")}
+    ip = np.zeros(W * H * max(int(sz[0]), 1), np.uint8)
+    for _ in range(n):
+        u, v = int(rng.integers(0, W)), int(rng.integers(0, H))
+        uc, vc = int(rng.integers(0, W)), int(rng.integers(0, H))
+        z = np.float32(rng.uniform(0.4, 6.0))
+        w = rng.normal(0, 0.05, 3)
+        th = np.linalg.norm(w)
+        K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]]) / max(th, 1e-12)
+        R = (np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K).astype(np.float32)
+        t = rng.normal(0, 0.05, 3).astype(np.float32)
+        dxv, dyv = int(rng.integers(0, 256)), int(rng.integers(0, 256))
+        diff = np.float32(rng.integers(-120, 121))
+        sigma = np.float32(rng.uniform(0.5, 40.0))
+        dp = np.zeros(W * H, np.float32)
+        dp[v * W + u] = z
+        gx = np.zeros(W * H, np.uint8)
+        gy = np.zeros(W * H, np.uint8)
+        gx[vc * W + uc], gy[vc * W + uc] = dxv, dyv
+        cp = np.array([u, v], np.int32)
+        cc = np.array([uc, vc], np.int32)
+        df = np.array([diff], np.float32)
+        idx = np.zeros(6, np.float32)
+        vec = np.zeros(6, np.float32)
+        lib.ref_lsm(p(ip), p(dp), p(ip), p(gx), p(gy), p(cp), p(cc), p(df), C.c_float(sigma), p(R), p(t),
+                    C.byref(intr), 1, p(idx), p(vec))
+        for k, val in (("u", u), ("v", v), ("z", z), ("R", R), ("t", t), ("dx", dxv), ("dy", dyv), ("diff", diff),
+                       ("sigma", sigma), ("C", idx), ("vec", vec)):
+            cases[k].append(val)
+    out = {k: np.asarray(v) for k, v in cases.items()}
+    out["intr"] = np.array([intr.fx, intr.fy, intr.cx, intr.cy, W, H], np.float64)
+    np.savez_compressed(OUT / "rgbd_lsm.npz", **out)
+
+
 def gen_text_fixtures():
     """The slab clouds of slices.npz again in the reference's own text format
     (matrix<Point_XYZI> / matrix<Point_Color>::Save_To_File,
@@ -256,6 +304,7 @@ def main():
     gen_bilateral()
     gen_transform_map()
     gen_transform_estimation()
+    gen_lsm()
     print("slice counts", gen_slices())
     gen_text_fixtures()
     for f in sorted(OUT.glob("*.npz")):

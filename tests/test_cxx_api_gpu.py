@@ -11,6 +11,7 @@ from conftest import ROOT
 
 pytestmark = pytest.mark.gpu
 syn = importlib.import_module("3deye_gb300.synth")
+IDENT12 = np.array([1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0], np.float64)
 
 
 def build_caller(tmp_path):
@@ -115,3 +116,63 @@ def test_cxx_api_roundtrip_matches_oracle(cuda, orc, tmp_path, fmt):
             if j < 6:
                 assert A[j, i] == A[i, j]
             k += 1
+
+
+def test_cxx_rgbd_odometry_matches_oracle(cuda, orc, tmp_path):
+    """Prepare_Data_For_RGBD .. Estimate_Isometry_By_RGBD called from C++
+    (tests/cxx/rgbd_roundtrip.cpp) against the oracle on a rendered pair."""
+    cfg = syn.small_config("c1", frames=3, cols=320, rows=240)
+    scene = syn.make_scene(cfg, 7)
+    traj = syn.make_trajectory(cfg, 7)
+    intr = orc.Intr(cfg.fx, cfg.fy, cfg.cx, cfg.cy, cfg.cols, cfg.rows)
+    W, H, L = cfg.cols, cfg.rows, 3
+    frames = []
+    with open(tmp_path / "rgbd_in.bin", "wb") as f:
+        np.array([W, H, L], np.int32).tofile(f)
+        np.array([cfg.fx, cfg.fy, cfg.cx, cfg.cy, 0.07], np.float32).tofile(f)
+        for k in (0, 1):
+            mm = np.rint(orc.render_depth(scene, traj[k], intr) * 1000).astype(np.uint16)
+            rgb = orc.render_rgb(scene, traj[k], intr)
+            mm.tofile(f)
+            rgb.tofile(f)
+            frames.append(orc.rgbd_levels(mm, rgb, L))
+    src = ROOT / "tests" / "cxx" / "rgbd_roundtrip.cpp"
+    exe = tmp_path / "rgbd_roundtrip"
+    lib = ROOT / "3deye_gb300"
+    subprocess.run([shutil.which("g++") or "g++", "-std=c++17", "-O2", "-I", str(ROOT / "include" / "3deye"), "-I",
+                    str(ROOT / "include"), str(src), "-L", str(lib), "-l3deye_gb300", f"-Wl,-rpath,{lib}", "-o",
+                    str(exe)], check=True)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = (tmp_path / "rgbd_out.bin").read_bytes()
+    off = 0
+
+    def take(dtype, n):
+        nonlocal off
+        a = np.frombuffer(raw, dtype, n, off)
+        off += a.nbytes
+        return a
+    for l in range(L):
+        m = (W >> l) * (H >> l)
+        i8, dm, gx, gy = take(np.uint8, m), take(np.float32, m), take(np.int16, m), take(np.int16, m)
+        assert np.array_equal(i8, frames[0][l][0].ravel()) and np.array_equal(dm, frames[0][l][1].ravel())
+        assert np.array_equal(gx, frames[1][l][2].ravel()) and np.array_equal(gy, frames[1][l][3].ravel())
+    npts = int(take(np.int32, 1)[0])
+    pts = take(np.int32, 2 * npts).reshape(npts, 2)
+    want = orc.rgbd_points(frames[1][0][2], frames[1][0][3], (10 / 0.125) ** 2)
+    assert npts == len(want) > 1000 and np.array_equal(pts, want)
+    # the identity pairs of those points, without a gradient test (the list is already filtered)
+    ncorr, s2 = int(take(np.int32, 1)[0]), float(take(np.float32, 1)[0])
+    diff = take(np.float32, npts)
+    n_o, kept, res, s2_o = orc.rgbd_pairs(frames[0][0], frames[1][0], intr, IDENT12, 0.0)
+    lin = pts[:, 1] * W + pts[:, 0]
+    on = kept.ravel()[lin] > 0
+    assert ncorr == int(on.sum()) > 500
+    assert np.array_equal(diff[on], res.ravel()[lin][on]) and np.all(diff[~on] == 100.0)
+    assert s2 == np.float32(np.sum(res.ravel()[lin][on].astype(np.float64) ** 2))
+    ok = int(take(np.int32, 1)[0])
+    R, t = take(np.float32, 9), take(np.float32, 3)
+    pose_o, failed = orc.rgbd_odometry(frames[0], frames[1], intr, [7, 7, 7][:L], [10.0] * L)
+    assert ok == 1 and failed == 0
+    np.testing.assert_allclose(R, pose_o[:9], rtol=0, atol=2e-5)
+    np.testing.assert_allclose(t, pose_o[9:], rtol=0, atol=5e-5)
