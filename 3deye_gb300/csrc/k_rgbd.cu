@@ -163,27 +163,44 @@ struct Level {
     int W, H;
     float fx, fy, cx, cy;
     float mdd, maxd, grad2;
+    double ifx, ify;  // 1 / fx, 1 / fy in FP64 (host-computed)
 };
 
-// R' = K R K^-1, t' = K t in FP64 (explicit fused operations), then float.
-__device__ void projective(const double *R, const double *t, float fxf, float fyf, float cxf, float cyf,
-                           float *proj) {
-    const double fx = fxf, fy = fyf, cx = cxf, cy = cyf;
-    double M[9];
-    for (int j = 0; j < 3; ++j) {
-        M[j] = __fma_rn(fx, R[j], __dmul_rn(cx, R[6 + j]));
-        M[3 + j] = __fma_rn(fy, R[3 + j], __dmul_rn(cy, R[6 + j]));
-        M[6 + j] = R[6 + j];
-    }
-    for (int i = 0; i < 3; ++i) {
-        const double a = __ddiv_rn(M[3 * i], fx), b = __ddiv_rn(M[3 * i + 1], fy);
+// One piece of R' = K R K^-1, t' = K t (FP64, explicit fused operations,
+// then float) and of the float pose M: row t of R' for t < 3, t' for t = 3;
+// threads 4..15 convert pose entry t - 4.  Threads 0..15 of a block run it
+// side by side (the FP64 pipe is narrow: one thread doing everything
+// serialises several microseconds of dependent FP64 work).
+__device__ __forceinline__ void projective_part(int t, const double *pose, const Level &L, float *proj, float *M) {
+    const double fx = L.fx, fy = L.fy, cx = L.cx, cy = L.cy;
+    const double *R = pose, *tv = pose + 9;
+    if (t < 3) {
+        const int i = t;  // R'[i][.] = (K R)[i][.] K^-1
+        double m0, m1, m2;
+        if (i == 0) {
+            m0 = __fma_rn(fx, R[0], __dmul_rn(cx, R[6]));
+            m1 = __fma_rn(fx, R[1], __dmul_rn(cx, R[7]));
+            m2 = __fma_rn(fx, R[2], __dmul_rn(cx, R[8]));
+        } else if (i == 1) {
+            m0 = __fma_rn(fy, R[3], __dmul_rn(cy, R[6]));
+            m1 = __fma_rn(fy, R[4], __dmul_rn(cy, R[7]));
+            m2 = __fma_rn(fy, R[5], __dmul_rn(cy, R[8]));
+        } else {
+            m0 = R[6];
+            m1 = R[7];
+            m2 = R[8];
+        }
+        const double a = __dmul_rn(m0, L.ifx), b = __dmul_rn(m1, L.ify);
         proj[3 * i] = (float)a;
         proj[3 * i + 1] = (float)b;
-        proj[3 * i + 2] = (float)(M[3 * i + 2] - __fma_rn(a, cx, __dmul_rn(b, cy)));
+        proj[3 * i + 2] = (float)(m2 - __fma_rn(a, cx, __dmul_rn(b, cy)));
+    } else if (t == 3) {
+        proj[9] = (float)__fma_rn(fx, tv[0], __dmul_rn(cx, tv[2]));
+        proj[10] = (float)__fma_rn(fy, tv[1], __dmul_rn(cy, tv[2]));
+        proj[11] = (float)tv[2];
+    } else if (t < 16) {
+        M[t - 4] = (float)pose[t - 4];
     }
-    proj[9] = (float)__fma_rn(fx, t[0], __dmul_rn(cx, t[2]));
-    proj[10] = (float)__fma_rn(fy, t[1], __dmul_rn(cy, t[2]));
-    proj[11] = (float)t[2];
 }
 
 __device__ __forceinline__ bool depth_ok(float z, float maxd) { return z > 0.f && z < maxd; }
@@ -211,9 +228,61 @@ __device__ __forceinline__ bool find_pair(const Level &L, const float *P, int u,
     return true;
 }
 
+// find_pair for K pixels of the previous frame (raster indices i[k]; entries
+// at or past W*H are not pixels): the depth loads, the projections, then the
+// gathers of every candidate issued together, then the tests -- the same
+// operations and results as find_pair, with K load chains in flight instead
+// of one.  Bit k of the result is set for a kept pair; j[k], r[k], z[k] and
+// the current frame's derivatives gx[k], gy[k] at j[k] are valid for those.
+template <int K>
+__device__ __forceinline__ unsigned find_pairs(const Level &L, const float *P, const int (&i)[K], int (&j)[K],
+                                               float (&r)[K], float (&z)[K], float (&gx)[K], float (&gy)[K]) {
+    const int npix = L.W * L.H;
+    float pz[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) z[k] = i[k] < npix ? __ldg(L.Dp + i[k]) : 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        j[k] = -1;
+        pz[k] = 0.f;
+        if (!depth_ok(z[k], L.maxd)) continue;
+        const float fu = (float)(i[k] % L.W), fv = (float)(i[k] / L.W);
+        const float px = __fmaf_rn(z[k], __fmaf_rn(P[1], fv, __fmaf_rn(P[0], fu, P[2])), P[9]);
+        const float py = __fmaf_rn(z[k], __fmaf_rn(P[4], fv, __fmaf_rn(P[3], fu, P[5])), P[10]);
+        pz[k] = __fmaf_rn(z[k], __fmaf_rn(P[7], fv, __fmaf_rn(P[6], fu, P[8])), P[11]);
+        if (!(pz[k] > 0.f)) continue;
+        const float iz = __frcp_rn(pz[k]);
+        const int u2 = __float2int_rn(__fmul_rn(px, iz)), v2 = __float2int_rn(__fmul_rn(py, iz));
+        if (u2 < 0 || v2 < 0 || u2 >= L.W || v2 >= L.H) continue;
+        j[k] = v2 * L.W + u2;
+    }
+    float z2[K];
+    int ic[K], ip[K], dx[K], dy[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const bool c = j[k] >= 0;
+        z2[k] = c ? __ldg(L.Dc + j[k]) : 0.f;
+        dx[k] = c && L.dx ? __ldg(L.dx + j[k]) : 0;
+        dy[k] = c && L.dx ? __ldg(L.dy + j[k]) : 0;
+        ic[k] = c ? __ldg(L.Ic + j[k]) : 0;
+        ip[k] = c ? __ldg(L.Ip + i[k]) : 0;
+    }
+    unsigned mask = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        bool ok = j[k] >= 0 && depth_ok(z2[k], L.maxd) && fabsf(pz[k] - z2[k]) < L.mdd;
+        if (L.dx) ok = ok && (float)(dx[k] * dx[k] + dy[k] * dy[k]) >= L.grad2;
+        r[k] = (float)ic[k] - (float)ip[k];
+        gx[k] = (float)dx[k];
+        gy[k] = (float)dy[k];
+        mask |= (unsigned)ok << k;
+    }
+    return mask;
+}
+
 // The 7-vector (C0..C5, -w r) of a kept pair; M = R row-major, t (float).
-__device__ __forceinline__ void pair_row(const Level &L, const float *M, int u, int v, float z, int j, float r,
-                                         float sigma, float ifx, float ify, float row[7]) {
+__device__ __forceinline__ void pair_row(const Level &L, const float *M, int u, int v, float z, float gx, float gy,
+                                         float r, float sigma, float ifx, float ify, float row[7]) {
     const float xn = __fmul_rn((float)u - L.cx, ifx), yn = __fmul_rn((float)v - L.cy, ify);
     const float X = __fmul_rn(z, xn), Y = __fmul_rn(z, yn);
     const float Px = __fmaf_rn(M[2], z, __fmaf_rn(M[1], Y, __fmul_rn(M[0], X))) + M[9];
@@ -223,8 +292,8 @@ __device__ __forceinline__ void pair_row(const Level &L, const float *M, int u, 
     const float w = wsum > 2.220446049250313e-16f ? __frcp_rn(wsum) : 1.f;
     const float s0 = __fmul_rn(w, kSobelScale);
     const float iz = __frcp_rn(Pz);
-    const float v0 = __fmul_rn(__fmul_rn(__fmul_rn(iz, L.fx), s0), (float)__ldg(L.dx + j));
-    const float v1 = __fmul_rn(__fmul_rn(__fmul_rn(iz, L.fy), s0), (float)__ldg(L.dy + j));
+    const float v0 = __fmul_rn(__fmul_rn(__fmul_rn(iz, L.fx), s0), gx);
+    const float v1 = __fmul_rn(__fmul_rn(__fmul_rn(iz, L.fy), s0), gy);
     const float v2 = __fmul_rn(-__fmaf_rn(v1, Py, __fmul_rn(v0, Px)), iz);
     row[0] = __fmaf_rn(Py, v2, -__fmul_rn(Pz, v1));
     row[1] = __fmaf_rn(Pz, v0, -__fmul_rn(Px, v2));
@@ -238,31 +307,29 @@ __device__ __forceinline__ void pair_row(const Level &L, const float *M, int u, 
 // Pass 1: kept count and sum of squared differences per block.
 __global__ void __launch_bounds__(kThreads) residual_kernel(const Level L, const double *__restrict__ pose,
                                                             unsigned long long *__restrict__ partials) {
-    __shared__ float P[12];
+    __shared__ float P[12], M[12];
     __shared__ unsigned s_n;
     __shared__ unsigned long long s_r2;
+    if (threadIdx.x < 16) projective_part(threadIdx.x, pose, L, P, M);
     if (threadIdx.x == 0) {
-        projective(pose, pose + 9, L.fx, L.fy, L.cx, L.cy, P);
         s_n = 0;
         s_r2 = 0ull;
     }
     __syncthreads();
     unsigned n = 0;
     unsigned long long r2 = 0;  // squared integer differences: exact
-    const int npix = L.W * L.H;
+    int idx[kPix], j[kPix];
+    float r[kPix], z[kPix], gx[kPix], gy[kPix];
 #pragma unroll
-    for (int k = 0; k < kPix; ++k) {
-        const int i = blockIdx.x * kThreads * kPix + k * kThreads + threadIdx.x;
-        if (i >= npix) continue;
-        const int u = i % L.W, v = i / L.W;
-        int j;
-        float r;
-        if (find_pair(L, P, u, v, __ldg(L.Dp + i), j, r)) {
+    for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kThreads * kPix + k * kThreads + threadIdx.x;
+    const unsigned kept = find_pairs<kPix>(L, P, idx, j, r, z, gx, gy);
+#pragma unroll
+    for (int k = 0; k < kPix; ++k)
+        if ((kept >> k) & 1u) {
             ++n;
-            const int ri = (int)r;
+            const int ri = (int)r[k];
             r2 += (unsigned long long)(ri * ri);
         }
-    }
     for (int o = 16; o > 0; o >>= 1) {
         n += __shfl_down_sync(0xffffffffu, n, o);
         r2 += __shfl_down_sync(0xffffffffu, r2, o);
@@ -298,11 +365,11 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, const doub
             s += __shfl_xor_sync(0xffffffffu, s, o);
         }
         if (lane == 0) {
-            projective(pose, pose + 9, L.fx, L.fy, L.cx, L.cy, P);
-            for (int k = 0; k < 12; ++k) M[k] = (float)pose[k];
             s_sigma = n ? __fsqrt_rn((float)((double)s / (double)n)) : 0.f;
             if (sigma_out && blockIdx.x == 0) *sigma_out = s_sigma;
         }
+    } else if (warp == 1 && lane < 16) {
+        projective_part(lane, pose, L, P, M);
     }
     __syncthreads();
     const float sigma = s_sigma;
@@ -310,18 +377,16 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, const doub
     float acc[28];
 #pragma unroll
     for (int k = 0; k < 28; ++k) acc[k] = 0.f;
-    const int npix = L.W * L.H;
-#pragma unroll 1
+    int idx[kPix], j[kPix];
+    float r[kPix], z[kPix], gx[kPix], gy[kPix];
+#pragma unroll
+    for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kThreads * kPix + k * kThreads + tid;
+    const unsigned kept = find_pairs<kPix>(L, P, idx, j, r, z, gx, gy);
+#pragma unroll
     for (int k = 0; k < kPix; ++k) {
-        const int i = blockIdx.x * kThreads * kPix + k * kThreads + tid;
-        if (i >= npix) continue;
-        const int u = i % L.W, v = i / L.W;
-        const float z = __ldg(L.Dp + i);
-        int j;
-        float r;
-        if (!find_pair(L, P, u, v, z, j, r)) continue;
+        if (!((kept >> k) & 1u)) continue;
         float row[7];
-        pair_row(L, M, u, v, z, j, r, sigma, ifx, ify, row);
+        pair_row(L, M, idx[k] % L.W, idx[k] / L.W, z[k], gx[k], gy[k], r[k], sigma, ifx, ify, row);
         int t = 0;
 #pragma unroll
         for (int a = 0; a < 6; ++a)
@@ -415,6 +480,8 @@ Level make_level(const uint8_t *ip, const float *dp, const uint8_t *ic, const fl
     L.mdd = mdd; L.maxd = maxd;
     const float g = min_gradient / kSobelScale;
     L.grad2 = g * g;
+    L.ifx = 1.0 / (double)in.fx;
+    L.ify = 1.0 / (double)in.fy;
     return L;
 }
 
@@ -486,8 +553,9 @@ int tde_rgbd_projective(const double *pose12, const tde_intrinsics *intr, float 
         M[3 + j] = std::fma(fy, R[3 + j], cy * R[6 + j]);
         M[6 + j] = R[6 + j];
     }
+    const double ifx = 1.0 / fx, ify = 1.0 / fy;
     for (int i = 0; i < 3; ++i) {
-        const double a = M[3 * i] / fx, b = M[3 * i + 1] / fy;
+        const double a = M[3 * i] * ifx, b = M[3 * i + 1] * ify;
         proj12[3 * i] = (float)a;
         proj12[3 * i + 1] = (float)b;
         proj12[3 * i + 2] = (float)(M[3 * i + 2] - std::fma(a, cx, b * cy));

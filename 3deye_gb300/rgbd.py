@@ -223,3 +223,64 @@ def synth_rgb(d_scene, nprim: int, pose12, intr: Intrinsics, out, stream=None) -
     pose = np.ascontiguousarray(pose12, np.float64)
     check(lib.tde_synth_rgb(d_scene.data_ptr(), nprim, pose.ctypes.data_as(P), C.byref(intr), out.data_ptr(),
                             _stream(stream)))
+
+
+class RgbdTracker:
+    """Frame-to-frame RGB-D odometry over a stream of frames: each track()
+    copies the frame into a fixed input slot, builds its pyramid and, from
+    the second frame on, estimates the pose against the previous frame.  The
+    per-frame launches (8 for the pyramid, 1 + 3 per Gauss-Newton step) are
+    captured once per buffer parity in CUDA graphs and replayed.  Results:
+    self.pose (device float64[12], previous -> current camera) and
+    self.status (device int32[1]) after each frame."""
+
+    def __init__(self, intr: Intrinsics, params: RgbdParams | None = None, device="cuda", graphs: bool = True):
+        import torch
+        self.torch = torch
+        self.params = params if params is not None else default_params()
+        L = self.params.levels
+        self.bufs = [RgbdFrame(intr.cols, intr.rows, L, device) for _ in range(2)]
+        self.od = RgbdOdometry(intr, self.params, device)
+        self.depth_slot = torch.empty((intr.rows, intr.cols), dtype=torch.int16, device=device)
+        self.rgb_slot = torch.empty((intr.rows, intr.cols, 3), dtype=torch.uint8, device=device)
+        self.stream = torch.cuda.Stream(device)
+        self.frames = 0
+        self.graphs = None
+        if graphs:
+            self.graphs = []
+            for p in (0, 1):
+                g = torch.cuda.CUDAGraph()
+                self.stream.synchronize()
+                with torch.cuda.graph(g, stream=self.stream):
+                    self._work(p)
+                self.graphs.append(g)
+            torch.cuda.synchronize()
+
+    @property
+    def pose(self):
+        return self.od.pose
+
+    @property
+    def status(self):
+        return self.od.status
+
+    def _work(self, p: int) -> None:
+        s = self.torch.cuda.current_stream()
+        self.bufs[p].load(self.depth_slot, self.rgb_slot, s)
+        self.od.enqueue(self.bufs[1 - p], self.bufs[p], None, s)
+
+    def track(self, depth_mm, rgb) -> None:
+        """Enqueue one frame (device uint16 mm and rows x cols x 3 RGB) on
+        self.stream.  The first frame only fills the pyramid."""
+        torch = self.torch
+        p = self.frames & 1
+        with torch.cuda.stream(self.stream):
+            self.depth_slot.copy_(depth_mm.view(torch.int16), non_blocking=True)
+            self.rgb_slot.copy_(rgb, non_blocking=True)
+            if self.frames == 0:
+                self.bufs[p].load(self.depth_slot, self.rgb_slot, self.stream)
+            elif self.graphs is not None:
+                self.graphs[p].replay()
+            else:
+                self._work(p)
+        self.frames += 1

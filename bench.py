@@ -551,19 +551,19 @@ def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
     for i in range(n):
         rg.synth_rgb(d_scene, scene.shape[0], traj[i], intr, rgb[i])
     torch.cuda.synchronize()
-    bufs = [rg.RgbdFrame(cfg.cols, cfg.rows, 4, dev) for _ in range(2)]
-    od = rg.RgbdOdometry(intr)
-    s = torch.cuda.Stream(dev)
     poses = torch.zeros((n, 12), dtype=torch.float64, device=dev)
     stats = torch.zeros(n, dtype=torch.int32, device=dev)
 
-    def step(i):
-        bufs[i & 1].load(frames[i], rgb[i], s)
-        od.enqueue(bufs[(i - 1) & 1], bufs[i & 1], None, s)
-        poses[i].copy_(od.pose, non_blocking=True)
-        stats[i:i + 1].copy_(od.status, non_blocking=True)
-    with torch.cuda.stream(s):
-        bufs[0].load(frames[0], rgb[0], s)
+    def timed(graphs):
+        tr = rg.RgbdTracker(intr, device=dev, graphs=graphs)
+        s = tr.stream
+
+        def step(i):
+            tr.track(frames[i], rgb[i])
+            with torch.cuda.stream(s):
+                poses[i].copy_(tr.pose, non_blocking=True)
+                stats[i:i + 1].copy_(tr.status, non_blocking=True)
+        tr.track(frames[0], rgb[0])
         for i in range(1, warm + 1):
             step(i)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -573,8 +573,11 @@ def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
         for i in range(warm + 1, n):
             step(i)
         e1.record(s)
-    s.synchronize()
-    ms = max_over_ranks(ws, e0.elapsed_time(e1))
+        s.synchronize()
+        return max_over_ranks(ws, e0.elapsed_time(e1)), tr, poses.cpu().numpy()
+    ms_eager, _, est_eager = timed(False)
+    ms, tr, _ = timed(True)
+    od = tr.od
     est = poses.cpu().numpy()
     st = stats.cpu().numpy()
     et, er = [], []
@@ -588,14 +591,16 @@ def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
     levels = 4
     launches = (1 + (levels - 1) + levels) + (1 + 3 * sum(int(x) for x in od.params.iters[:levels]))
     out = {"value": round(ws * pairs / (ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(ms / pairs, 5),
-           "gpu_launches": launches * pairs,
+           "ms_per_step_without_graphs": round(ms_eager / pairs, 5), "gpu_launches": launches * pairs,
+           "graph_poses_equal_eager": bool(np.array_equal(est, est_eager)),
            "relative_pose_error": {"mean_translation_m": round(float(np.mean(et)), 6),
                                    "mean_rotation_deg": round(float(np.mean(er)), 5),
                                    "mean_step_translation_m": round(float(np.mean(
                                        [np.linalg.norm(traj[i][9:] - traj[i - 1][9:]) for i in range(1, n)])), 6),
                                    "frames_without_a_solved_step": int(((st[1:] & 2) == 0).sum())},
            "note": "640x480 noisy depth + rendered texture, resident in HBM; per frame: intensity, 4-level "
-                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes + 1 FP64 solve each)"}
+                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes + 1 FP64 solve each), replayed "
+                   "from CUDA graphs (RgbdTracker)"}
     if with_cpu:
         from oracle import oracle as orc
         fr = frames[:4].view(torch.int16).cpu().numpy().view(np.uint16)

@@ -109,8 +109,9 @@ int or_rgbd_points(const int16_t *dx, const int16_t *dy, int W, int H, float sca
     return n;
 }
 
-/* R' = K R K^-1 and t' = K t in FP64 with fused operations, then to float:
- * proj[0..8] = R' row-major, proj[9..11] = t'. */
+/* R' = K R K^-1 and t' = K t in FP64 with fused operations (K^-1 through
+ * the FP64 reciprocals of fx, fy), then to float: proj[0..8] = R' row-major,
+ * proj[9..11] = t'. */
 void or_rgbd_projective(const double *R, const double *t, const tde_intrinsics *in, float *proj) {
     const double fx = in->fx, fy = in->fy, cx = in->cx, cy = in->cy;
     double M[9];
@@ -119,8 +120,9 @@ void or_rgbd_projective(const double *R, const double *t, const tde_intrinsics *
         M[3 + j] = fma(fy, R[3 + j], cy * R[6 + j]);
         M[6 + j] = R[6 + j];
     }
+    const double ifx = 1.0 / fx, ify = 1.0 / fy;
     for (int i = 0; i < 3; ++i) {
-        const double a = M[3 * i] / fx, b = M[3 * i + 1] / fy;
+        const double a = M[3 * i] * ifx, b = M[3 * i + 1] * ify;
         proj[3 * i] = (float)a;
         proj[3 * i + 1] = (float)b;
         proj[3 * i + 2] = (float)(M[3 * i + 2] - fma(a, cx, b * cy));
