@@ -222,9 +222,9 @@ def load_peaks_bf16():
     return {"burst": 1900.0, "sustained": 1700.0, "kind": "fallback"}
 
 
-def load_traffic():
-    """DRAM bytes per integration launch from the committed ncu summary."""
-    p = ROOT / "profiles" / "integrate_c2_traffic.json"
+def load_traffic(name="integrate_c2_traffic.json"):
+    """DRAM bytes of one ncu capture of a kernel, from the committed summary."""
+    p = ROOT / "profiles" / name
     if p.exists():
         try:
             return json.loads(p.read_text())
@@ -818,6 +818,11 @@ def run_ours(args, ws, rank, local):
     icp_launch_ms = float(np.mean(stages["icp"])) / icp_launches
     ray_bytes = S * ray_records + 24 * cfg.rows * cfg.cols
     icp_achieved = icp_bytes / icp_launches / (icp_launch_ms * 1e-3) / 1e9
+    # DRAM bytes of one cold ncu capture of a level-0 launch, scaled to the average launch by its
+    # algorithmic bytes (traffic follows the pixels of the level)
+    icp_cap = load_traffic("icp_traffic.json")
+    icp_traffic = (int(icp_cap["dram_bytes_per_launch_captured"] * (icp_bytes / icp_launches) /
+                       icp_cap["alg_bytes_captured"]) if icp_cap else None)
     fps = ws * K / (ms * 1e-3)
     line = {
         "metric": METRIC, "value": round(fps, 2), "unit": "frames/s", "n_gpus": ws, "steps": K, "warmup": W,
@@ -828,7 +833,7 @@ def run_ours(args, ws, rank, local):
                 "d2h_bytes_per_step": 96 + 4},
         "roofline": {"kernel": "icp_step_kernel (dominant: largest share of the frame)", "bound": "hbm",
                      "achieved": round(icp_achieved, 1), "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": round(icp_achieved / hbm, 4), "traffic": None,
+                     "frac": round(icp_achieved / hbm, 4), "traffic": icp_traffic,
                      "alg_bytes_per_launch": int(icp_bytes / icp_launches), "avg_launch_ms": round(icp_launch_ms, 5),
                      "launches_per_frame": icp_launches,
                      "note": "maps are L2-resident; the iteration is latency-bound (reduction tail + FP64 solve)"},
