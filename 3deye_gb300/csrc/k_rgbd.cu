@@ -22,6 +22,7 @@
 
 #include "tde_common.cuh"
 #include "tde_icp.cuh"
+#include "tde_solve.cuh"
 
 namespace tde {
 namespace {
@@ -346,10 +347,18 @@ __global__ void __launch_bounds__(kThreads) residual_kernel(const Level L, const
 }
 
 // Pass 2: sigma from pass 1's blocks (integer sums: exact), the rows of the
-// kept pairs, per-block FP64 partials of the 27 terms and the count.
-__global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, const double *__restrict__ pose,
+// kept pairs, per-block FP64 partials of the 27 terms and the count.  With
+// SOLVE the last block to finish (a ticket on *counter, which it resets) sums
+// every block's partials (warp w takes blocks w, w + 8, ..., then the eight
+// warp sums in order), and warp 0 solves and moves the pose in place: the
+// other blocks read the pose only before taking their tickets.  Status: bit 0
+// for a failed solve (too few pairs or A not positive definite; the pose is
+// kept), bit 1 for a solved step.
+template <bool SOLVE>
+__global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, double *__restrict__ pose,
                                                        const unsigned long long *__restrict__ res_partials, int nres,
-                                                       double *__restrict__ partials, float *__restrict__ sigma_out) {
+                                                       double *__restrict__ partials, float *__restrict__ sigma_out,
+                                                       unsigned *__restrict__ counter, int *__restrict__ status) {
     __shared__ float P[12], M[12];
     __shared__ float s_sigma;
     __shared__ double red[kThreads / 32][28];
@@ -410,6 +419,35 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, const doub
         for (int w = 0; w < kThreads / 32; ++w) s += red[w][tid];
         partials[(size_t)blockIdx.x * 28 + tid] = s;
     }
+    if (!SOLVE) return;
+    __shared__ bool s_last;
+    __threadfence();  // this block's partials visible before its ticket
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (lane < 28) {
+        double v = 0.0;
+        for (int b = warp; b < (int)gridDim.x; b += kThreads / 32) v += __ldcg(partials + (size_t)b * 28 + lane);
+        red[warp][lane] = v;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    if (lane == 0) *counter = 0u;
+    __shared__ double Rs[9], ts[3];
+    double term = 0.0;
+    if (lane < 28)
+        for (int w = 0; w < kThreads / 32; ++w) term += red[w][lane];
+    const double pv = lane < 12 ? pose[lane] : 0.0;
+    if (lane < 9) Rs[lane] = pv;
+    else if (lane < 12) ts[lane - 9] = pv;
+    __syncwarp();
+    const double count = __shfl_sync(0xffffffffu, term, 27);
+    double o, xl;
+    const bool ok = count >= (double)kIcpMinInliers && warp_solve_step(term, Rs, ts, lane, o, xl);
+    if (lane < 12) pose[lane] = ok ? o : pv;
+    if (lane == 0) *status |= ok ? 2 : 1;
 }
 
 // The 28 sums of `nb` partials: warp w takes blocks w, w + 8, ..., then the
@@ -432,9 +470,11 @@ __global__ void __launch_bounds__(256) sum_partials_kernel(const double *__restr
 }
 
 struct Pose12 { double v[12]; };
-__global__ void set_pose_kernel(const Pose12 p, double *__restrict__ pose, int *__restrict__ status) {
+__global__ void set_pose_kernel(const Pose12 p, double *__restrict__ pose, int *__restrict__ status,
+                                unsigned *__restrict__ counter) {
     if (threadIdx.x < 12) pose[threadIdx.x] = p.v[threadIdx.x];
     if (threadIdx.x == 0 && status) *status = 0;
+    if (threadIdx.x == 0 && counter) *counter = 0u;
 }
 
 // Fill_List: correspondence of listed previous-frame points (or every pixel).
@@ -591,7 +631,7 @@ int tde_rgbd_correspondences(const uint8_t *i_prev, const float *d_prev, const u
 size_t tde_rgbd_odometry_scratch_bytes(int cols, int rows) {
     if (cols <= 0 || rows <= 0) return 0;
     const size_t nb = odo_blocks(cols, rows);
-    return ((nb * 2 + nb * 28 + 12) * sizeof(double) + 255) & ~(size_t)255;
+    return ((nb * 2 + nb * 28 + 12 + 1) * sizeof(double) + 255) & ~(size_t)255;  // + pose, ticket
 }
 
 void tde_rgbd_default_params(tde_rgbd_params *p) {
@@ -622,10 +662,10 @@ int tde_rgbd_lsm(const uint8_t *i_prev, const float *d_prev, const uint8_t *i_cu
     double *lsm = reinterpret_cast<double *>(res + 2 * nb), *pose = lsm + 28 * nb;
     Pose12 P;
     for (int k = 0; k < 12; ++k) P.v[k] = pose12[k];
-    set_pose_kernel<<<1, 32, 0, s>>>(P, pose, nullptr);
+    set_pose_kernel<<<1, 32, 0, s>>>(P, pose, nullptr, nullptr);
     const Level L = make_level(i_prev, d_prev, i_curr, d_curr, dx, dy, *intr, max_depth_diff, max_depth, min_gradient);
     residual_kernel<<<nb, kThreads, 0, s>>>(L, pose, res);
-    lsm_kernel<<<nb, kThreads, 0, s>>>(L, pose, res, (int)nb, lsm, sigma_device);
+    lsm_kernel<false><<<nb, kThreads, 0, s>>>(L, pose, res, (int)nb, lsm, sigma_device, nullptr, nullptr);
     sum_partials_kernel<<<1, 256, 0, s>>>(lsm, (int)nb, sums_device);
     return check_launch("rgbd_lsm");
 }
@@ -654,10 +694,11 @@ int tde_rgbd_odometry(const tde_rgbd_frame *prev, const tde_rgbd_frame *curr, co
     const unsigned nb0 = odo_blocks(intr0->cols, intr0->rows);
     unsigned long long *res = static_cast<unsigned long long *>(scratch);
     double *lsm = reinterpret_cast<double *>(res + 2 * nb0);
+    unsigned *ticket = reinterpret_cast<unsigned *>(lsm + 28 * nb0 + 12);
     Pose12 P;
     const double ident[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
     for (int k = 0; k < 12; ++k) P.v[k] = init_pose12 ? init_pose12[k] : ident[k];
-    set_pose_kernel<<<1, 32, 0, s>>>(P, pose12_device, status_device);
+    set_pose_kernel<<<1, 32, 0, s>>>(P, pose12_device, status_device, ticket);
     int st = check_launch("rgbd_odometry");
     if (st) return st;
     for (int l = levels - 1; l >= 0; --l) {
@@ -670,9 +711,9 @@ int tde_rgbd_odometry(const tde_rgbd_frame *prev, const tde_rgbd_frame *curr, co
         const unsigned nb = odo_blocks(in.cols, in.rows);
         for (int it = 0; it < params->iters[l]; ++it) {
             residual_kernel<<<nb, kThreads, 0, s>>>(L, pose12_device, res);
-            lsm_kernel<<<nb, kThreads, 0, s>>>(L, pose12_device, res, (int)nb, lsm, nullptr);
+            lsm_kernel<true><<<nb, kThreads, 0, s>>>(L, pose12_device, res, (int)nb, lsm, nullptr, ticket,
+                                                      status_device);
             if ((st = check_launch("rgbd_odometry"))) return st;
-            TDE_TRY(launch_rgbd_solve(lsm, (int)nb, pose12_device, status_device, s));
         }
     }
     return TDE_OK;

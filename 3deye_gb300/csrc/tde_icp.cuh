@@ -102,8 +102,5 @@ int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const I
 // The pipeline's FP64 solve-and-update step alone, on n systems (device
 // arrays: sums[28 n], pose[12 n] in place, x[6 n], ok[n]).
 int launch_icp_solve(const double *sums, int n, double *pose, double *x, int *ok, cudaStream_t stream);
-// RGB-D odometry step: partials[nblocks][28] (27 terms + count) -> solve and
-// pose update in place; bit 1 of *status on failure.
-int launch_rgbd_solve(const double *partials, int nblocks, double *pose, int *status, cudaStream_t stream);
 
 }  // namespace tde

@@ -229,7 +229,7 @@ class RgbdTracker:
     """Frame-to-frame RGB-D odometry over a stream of frames: each track()
     copies the frame into a fixed input slot, builds its pyramid and, from
     the second frame on, estimates the pose against the previous frame.  The
-    per-frame launches (8 for the pyramid, 1 + 3 per Gauss-Newton step) are
+    per-frame launches (8 for the pyramid, 1 + 2 per Gauss-Newton step) are
     captured once per buffer parity in CUDA graphs and replayed.  Results:
     self.pose (device float64[12], previous -> current camera) and
     self.status (device int32[1]) after each frame."""

@@ -589,7 +589,7 @@ def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
         et.append(np.linalg.norm(est[i][9:] - gt))
         er.append(np.degrees(np.arccos(np.clip((np.trace(Re) - 1) / 2, -1, 1))))
     levels = 4
-    launches = (1 + (levels - 1) + levels) + (1 + 3 * sum(int(x) for x in od.params.iters[:levels]))
+    launches = (1 + (levels - 1) + levels) + (1 + 2 * sum(int(x) for x in od.params.iters[:levels]))
     out = {"value": round(ws * pairs / (ms * 1e-3), 2), "unit": "frames/s", "ms_per_step": round(ms / pairs, 5),
            "ms_per_step_without_graphs": round(ms_eager / pairs, 5), "gpu_launches": launches * pairs,
            "graph_poses_equal_eager": bool(np.array_equal(est, est_eager)),
@@ -599,8 +599,8 @@ def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
                                        [np.linalg.norm(traj[i][9:] - traj[i - 1][9:]) for i in range(1, n)])), 6),
                                    "frames_without_a_solved_step": int(((st[1:] & 2) == 0).sum())},
            "note": "640x480 noisy depth + rendered texture, resident in HBM; per frame: intensity, 4-level "
-                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes + 1 FP64 solve each), replayed "
-                   "from CUDA graphs (RgbdTracker)"}
+                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes each, the FP64 solve in the "
+                   "second pass's last block), replayed from CUDA graphs (RgbdTracker)"}
     if with_cpu:
         from oracle import oracle as orc
         fr = frames[:4].view(torch.int16).cpu().numpy().view(np.uint16)
