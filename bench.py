@@ -98,9 +98,14 @@ def dist_init(args):
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        gpu = torch.cuda.is_available()
+        if gpu:
+            torch.cuda.set_device(local)
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        # replicas exchange only the barrier and the max of their times: NCCL
+        # between the GPU arm's ranks, gloo for the CPU reference arm (and on
+        # hosts without a GPU)
+        dist.init_process_group("nccl" if args.impl == "ours" and gpu else "gloo")
     return ws, rank, local
 
 
@@ -263,19 +268,23 @@ def make_frames(tde, syn, cfg, nframes, seed_k, dev, corridor=False):
 
 def barrier_sync(ws):
     import torch
-    torch.cuda.synchronize()
+    gpu = torch.cuda.is_available()
+    if gpu:
+        torch.cuda.synchronize()
     if ws > 1:
         import torch.distributed as dist
         dist.barrier()
-        torch.cuda.synchronize()
+        if gpu:
+            torch.cuda.synchronize()
 
 
 def max_over_ranks(ws, x):
+    """The largest of the ranks' values (every rank gets it)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
