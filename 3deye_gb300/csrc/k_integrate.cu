@@ -252,20 +252,19 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
             pxy[h] = Nv.x * wrap_mod(y + P.rb.origin_GRID.y, Nv.y) + px;
         }
         bool all_sat = true;    // every voxel this lane updated was left saturated
-        unsigned taken = 0u;    // bit j: voxel j of this lane was updated
+        unsigned taken = 0u;    // bit j: voxel j of this lane was updated; bit 16 + j: written negative
         #pragma unroll 1
         for (int j0 = 0; j0 < 16; j0 += 4) {
             size_t idx[4];
             float sdfv[4];
             bool take[4];
-            int zz[4], yy[4];
+
             #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int j = j0 + k;
                 const int h = j & 1;
                 const int y = py_[h];
                 const int z = bz * kBrick + (j >> 1);
-                yy[k] = y; zz[k] = z;
                 take[k] = false; sdfv[k] = 0.f; idx[k] = 0;
                 if (x >= Nv.x || y >= Nv.y || z >= Nv.z) continue;
                 const float gz = ((float)z + 0.5f) * P.cell.z - q.t[2];
@@ -315,13 +314,28 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
                         float fs;
                         int ws;
                         S::decode(rn, fs, ws);
-                        if (fs < 0.f) {
-                            neg_flags[physical_brick(x, yy[k], zz[k], P.rb)] = 1;
-                            neg_flags[nbricks_all + physical_superbrick(x, yy[k], zz[k], P.rb)] = 1;
-                        }
+                        if (fs < 0.f) taken |= 1u << (16 + j0 + k);
                     }
                 }
             }
+        }
+        if (unsigned negm = taken >> 16) {
+            // brick / super-brick flags of the negative writes: the brick's
+            // voxels fall in at most two physical bricks per axis, so each flag
+            // is stored once (physical_brick / physical_superbrick in 32 bits)
+            unsigned last_pb = ~0u, last_ps = ~0u;
+            do {
+                const int j = __ffs(negm) - 1;
+                negm &= negm - 1u;
+                const unsigned py = wrap_mod(py_[j & 1] + P.rb.origin_GRID.y, Nv.y);
+                const unsigned pz = wrap_mod(bz * kBrick + (j >> 1) + P.rb.origin_GRID.z, Nv.z);
+                const unsigned pb = ((unsigned)px >> 3) + ((unsigned)(Nv.x + 7) >> 3) *
+                                    ((py >> 3) + ((unsigned)(Nv.y + 7) >> 3) * (pz >> 3));
+                const unsigned ps = ((unsigned)px >> 5) + ((unsigned)(Nv.x + 31) >> 5) *
+                                    ((py >> 5) + ((unsigned)(Nv.y + 31) >> 5) * (pz >> 5));
+                if (pb != last_pb) { neg_flags[pb] = 1; last_pb = pb; }
+                if (ps != last_ps) { neg_flags[nbricks_all + ps] = 1; last_ps = ps; }
+            } while (negm);
         }
         if (sat) {
             // Saturated brick: every voxel at f = 1, maximum weight.  Only when
