@@ -125,6 +125,8 @@ constexpr int kConvMmaWarp = kConvEpiWarps + kConvProdWarps;
 constexpr int kConvAcc = 4;       // accumulators in tensor memory
 constexpr int kConvMaxSlots = 8;  // input-row ring
 constexpr int kConvMinSlots = 4;
+constexpr int kStripRowsOneWave = 8;   // longest strip of a one-wave launch
+constexpr int kStripRowsBalanced = 16;  // strip length when the work is larger
 constexpr uint64_t kConvWaitNs = 2000000000ull;
 
 struct ConvPipe {
@@ -707,26 +709,56 @@ const void *wgrad_kernel_fn(int mode, int cca, int ccb) {
     return nullptr;
 }
 
-__global__ void wgrad_reduce_kernel(const float *__restrict__ partial, int blocks, int cin, int cout, int mtiles,
-                                    float *__restrict__ dw, float *__restrict__ db) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = ((co * 9 + t) * cin + ci), then cout biases
-    const int nw = cout * 9 * cin;
-    if (i >= nw + cout) return;
-    const size_t rows_pad = (size_t)3 * mtiles * 128 + 1;
-    size_t r;
-    int co;
-    if (i < nw) {
-        const int ci = i % cin, t = (i / cin) % 9;
-        co = i / (9 * cin);
-        r = (size_t)(t % 3) * mtiles * 128 + (size_t)(t / 3) * cin + ci;
-    } else {
-        co = i - nw;
-        r = rows_pad - 1;
+// Fixed-order sum of `blocks` partial vectors of n floats ([blocks][n]): a
+// block takes 32 consecutive elements (coalesced); warp w sums the partials
+// w, w + 8, ... with eight loads in flight, then the eight warp sums are added
+// in warp order.  Deterministic; the partials' latency is paid about
+// blocks / 64 times instead of `blocks` times.
+__device__ __forceinline__ bool sum_partials(const float *__restrict__ partial, int blocks, int n, int &e,
+                                             float &total) {
+    __shared__ float part[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    e = blockIdx.x * 32 + lane;
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 0.f;
+    if (e < n) {
+        int b = w;
+        for (; b + 56 < blocks; b += 64) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] += __ldg(partial + (size_t)(b + 8 * k) * n + e);
+        }
+        for (int k = 0; b < blocks; b += 8, ++k) a[k & 7] += __ldg(partial + (size_t)b * n + e);
     }
-    float s = 0.f;
-    for (int b = 0; b < blocks; ++b) s += partial[((size_t)b * rows_pad + r) * cout + co];
-    if (i < nw) dw[i] = s;
-    else db[co] = s;
+    part[w][lane] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    __syncthreads();
+    if (w != 0 || e >= n) return false;
+    float t = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t += part[k][lane];
+    total = t;
+    return true;
+}
+
+// Weight gradients from the per-block partials [blocks][rows_pad][cout]: row
+// r = dx * mtiles * 128 + dy * cin + ci (rows past 3 cin of a dx are padding),
+// the last row the bias; dw[(co * 9 + 3 dy + dx) * cin + ci].
+__global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float *__restrict__ partial, int blocks, int cin,
+                                                           int cout, int mtiles, float *__restrict__ dw,
+                                                           float *__restrict__ db) {
+    const int rows_pad = 3 * mtiles * 128 + 1;
+    int e;
+    float t;
+    if (!sum_partials(partial, blocks, rows_pad * cout, e, t)) return;
+    const int r = e / cout, co = e % cout;
+    if (r == rows_pad - 1) {
+        db[co] = t;
+        return;
+    }
+    const int dx = r / (mtiles * 128), rem = r % (mtiles * 128);
+    if (rem >= 3 * cin) return;
+    const int dy = rem / cin, ci = rem % cin;
+    dw[((size_t)co * 9 + 3 * dy + dx) * cin + ci] = t;
 }
 
 // ---------------------------------------------------------------------------
@@ -831,12 +863,11 @@ __global__ void __launch_bounds__(256) conv_in_wgrad_kernel(const float *__restr
     }
 }
 
-__global__ void conv_in_wgrad_reduce_kernel(const float *__restrict__ partial, int blocks, float *__restrict__ dw1,
-                                            float *__restrict__ db1) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // c * 28 + k
-    if (i >= kInPartial) return;
-    float t = 0.f;
-    for (int b = 0; b < blocks; ++b) t += partial[(size_t)b * kInPartial + i];
+__global__ void __launch_bounds__(256) conv_in_wgrad_reduce_kernel(const float *__restrict__ partial, int blocks,
+                                                                   float *__restrict__ dw1, float *__restrict__ db1) {
+    int i;  // c * 28 + k
+    float t;
+    if (!sum_partials(partial, blocks, kInPartial, i, t)) return;
     const int c = i / (kInK + 1), k = i % (kInK + 1);
     if (k == kInK) db1[c] = t;
     else dw1[c * kInK + k] = t;
@@ -1087,9 +1118,11 @@ int launch_conv(const ConvArgs &a, const ConvPlan &plan, int num_sms, cudaStream
     const long row_tiles = (long)a.n * a.h * tiles_x;
     const long slots = (long)num_sms * plan.per_sm;
     // rows per strip: enough that the strips do not outnumber the resident
-    // blocks (no second wave), even when the epilogue pools row pairs
+    // blocks (no second wave), even when the epilogue pools row pairs; with
+    // more work than that (training batches), short strips that the resident
+    // blocks take in turn, which balances their load better than long ones
     int rows = (int)((row_tiles + slots - 1) / slots);
-    rows = rows < 1 ? 1 : rows > 64 ? 64 : rows;
+    rows = rows < 1 ? 1 : rows > kStripRowsOneWave ? kStripRowsBalanced : rows;
     if (a.pool_out) rows += rows & 1;
     const long items = (long)a.n * tiles_x * ((a.h + rows - 1) / rows);
     const int grid = (int)(items < slots ? items : slots);
@@ -1155,8 +1188,8 @@ int launch_wait_selftest(uint64_t limit_ns, unsigned long long *out, cudaStream_
 
 int launch_wgrad_reduce(const float *partial, int blocks, int cin, int cout, float *dw, float *db, cudaStream_t s) {
     const WgLayout L = wg_layout(cin, cout);
-    const int n = cout * 9 * cin + cout;
-    wgrad_reduce_kernel<<<div_up(n, 256), 256, 0, s>>>(partial, blocks, cin, cout, L.mtiles, dw, db);
+    const int n = (3 * L.mtiles * 128 + 1) * cout;
+    wgrad_reduce_kernel<<<div_up(n, 32), 256, 0, s>>>(partial, blocks, cin, cout, L.mtiles, dw, db);
     return check_launch("refiner wgrad reduce");
 }
 
@@ -1176,7 +1209,7 @@ int launch_conv_in_wgrad(const float *depth_m, const bf16 *dz1, int n, int h, in
         return set_error(TDE_ERR_UNSUPPORTED, "refiner: %d columns exceed the input-layer gradient kernel", w);
     conv_in_wgrad_kernel<<<blocks, 256, rows_bytes, s>>>(depth_m, dz1, n, h, w, partial);
     TDE_TRY(check_launch("refiner conv_in wgrad"));
-    conv_in_wgrad_reduce_kernel<<<div_up(kInPartial, 128), 128, 0, s>>>(partial, blocks, dw1, db1);
+    conv_in_wgrad_reduce_kernel<<<div_up(kInPartial, 32), 256, 0, s>>>(partial, blocks, dw1, db1);
     return check_launch("refiner conv_in wgrad reduce");
 }
 
