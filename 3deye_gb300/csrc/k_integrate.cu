@@ -198,10 +198,15 @@ __global__ void __launch_bounds__(256) cull_bricks_kernel(const IntegrateParams 
     if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = b;
 }
 
+// Voxels a lane projects and loads together, and the blocks per SM the
+// registers are sized for.
+constexpr int kIntGroup = 4;
+constexpr int kIntBlocksPerSM = 4;
+
 // One warp per surviving brick (16 voxels per lane), grid-strided over the
 // list so the work spreads over every SM whatever the scene's layout.
 template <int FMT>
-__global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
+__global__ void __launch_bounds__(256, kIntBlocksPerSM) integrate_bricks_kernel(const float *__restrict__ depth, void *__restrict__ vol,
                                                                const IntegrateParams P, const int *__restrict__ list,
                                                                const int *__restrict__ count,
                                                                uint8_t *__restrict__ neg_flags,
@@ -254,13 +259,13 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
         bool all_sat = true;    // every voxel this lane updated was left saturated
         unsigned taken = 0u;    // bit j: voxel j of this lane was updated; bit 16 + j: written negative
         #pragma unroll 1
-        for (int j0 = 0; j0 < 16; j0 += 4) {
-            size_t idx[4];
-            float sdfv[4];
-            bool take[4];
+        for (int j0 = 0; j0 < 16; j0 += kIntGroup) {
+            size_t idx[kIntGroup];
+            float sdfv[kIntGroup];
+            bool take[kIntGroup];
 
             #pragma unroll
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < kIntGroup; ++k) {
                 const int j = j0 + k;
                 const int h = j & 1;
                 const int y = py_[h];
@@ -288,12 +293,12 @@ __global__ void __launch_bounds__(256, 4) integrate_bricks_kernel(const float *_
                 if (a > (size_t)(long)P.rb.buffer_length) a %= (size_t)(long)P.rb.buffer_length;
                 idx[k] = a;
             }
-            typename S::Raw raw[4];
+            typename S::Raw raw[kIntGroup];
             #pragma unroll
-            for (int k = 0; k < 4; ++k)
+            for (int k = 0; k < kIntGroup; ++k)
                 if (take[k]) raw[k] = S::load_raw(vol, idx[k], P.n);
             #pragma unroll
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < kIntGroup; ++k) {
                 if (!take[k]) continue;
                 taken |= 1u << (j0 + k);
                 ++n_read;
