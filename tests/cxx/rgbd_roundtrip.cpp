@@ -115,6 +115,27 @@ int main(int argc, char **argv) {
     for (int r = 0; r < 3; ++r) wr(out, R.data[r].data, 3);
     wr(out, t.data, 3);
     fclose(out);
+
+    // derivatives declared as the reference does (unsigned char) are refused
+    vector<gpu_array_base *> DX8, DY8;
+    for (int l = 0; l < L; ++l) {
+        DX8.push_back(new gpu_array<unsigned char>(dim3(W >> l, H >> l)));
+        DY8.push_back(new gpu_array<unsigned char>(dim3(W >> l, H >> l)));
+    }
+    bool threw = false;
+    try {
+        Create_Intensity_Derivatives(I1, DX8, DY8, intr, L, &gm);
+    } catch (const std::exception &) {
+        threw = true;
+    }
+    for (int l = 0; l < L; ++l) {
+        delete DX8[l];
+        delete DY8[l];
+    }
+    if (!threw) {
+        fprintf(stderr, "unsigned char derivatives accepted\n");
+        return 5;
+    }
     for (int l = 0; l < L; ++l) {
         delete I0[l]; delete D0[l]; delete I1[l]; delete D1[l]; delete DX[l]; delete DY[l];
     }

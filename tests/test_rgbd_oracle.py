@@ -157,6 +157,41 @@ def test_rgbd_c_abi_refuses_bad_arguments(tde):
     rc = lib.tde_rgbd_odometry(C.byref(frame), C.byref(frame), C.byref(intr), C.byref(p), None, C.c_void_p(0x100),
                                C.c_void_p(0x200), scratch, nb, None)
     assert rc == tde._capi.TDE_ERR_INVALID_ARG
+    # every level present, but iterations out of range / scratch too small
+    p.levels = 2
+    bufs = [C.c_void_p(0x1000 + 0x100 * k) for k in range(8)]
+    for l in range(2):
+        frame.intensity[l], frame.depth[l], frame.dx[l], frame.dy[l] = bufs[4 * l: 4 * l + 4]
+    p.iters[1] = 101
+    rc = lib.tde_rgbd_odometry(C.byref(frame), C.byref(frame), C.byref(intr), C.byref(p), None, C.c_void_p(0x100),
+                               C.c_void_p(0x200), scratch, nb, None)
+    assert rc == tde._capi.TDE_ERR_INVALID_ARG and "iters" in tde._capi.last_error()
+    p.iters[1] = 7
+    rc = lib.tde_rgbd_odometry(C.byref(frame), C.byref(frame), C.byref(intr), C.byref(p), None, C.c_void_p(0x100),
+                               C.c_void_p(0x200), scratch, nb - 256, None)
+    assert rc == tde._capi.TDE_ERR_INVALID_ARG and "scratch" in tde._capi.last_error()
+    # a frame too small for its levels
+    small = tde._capi.Intrinsics(50.0, 50.0, 7.5, 5.5, 16, 12)
+    p.levels = 3
+    rc = lib.tde_rgbd_odometry(C.byref(frame), C.byref(frame), C.byref(small), C.byref(p), None, C.c_void_p(0x100),
+                               C.c_void_p(0x200), scratch, nb, None)
+    assert rc == tde._capi.TDE_ERR_INVALID_ARG
+    # the stage entry points refuse null buffers and sizes before any device work
+    assert lib.tde_rgbd_prepare(None, None, 640, 480, None, None, None) == tde._capi.TDE_ERR_INVALID_ARG
+    assert lib.tde_rgbd_pyramid(C.c_void_p(1), C.c_void_p(2), 1, 480, C.c_void_p(3), C.c_void_p(4), None) == \
+        tde._capi.TDE_ERR_INVALID_ARG
+    assert lib.tde_rgbd_derivatives(None, 640, 480, C.c_void_p(1), C.c_void_p(2), None) == tde._capi.TDE_ERR_INVALID_ARG
+    assert lib.tde_rgbd_points_scratch_bytes(0, 480) == 0 and lib.tde_rgbd_odometry_scratch_bytes(640, 0) == 0
+    pts_sb = lib.tde_rgbd_points_scratch_bytes(640, 480)
+    assert pts_sb >= 480 * 4 and pts_sb % 256 == 0
+    rc = lib.tde_rgbd_points_of_interest(C.c_void_p(1), C.c_void_p(2), 640, 480, 1.0, scratch, pts_sb - 256,
+                                         C.c_void_p(3), 10, C.c_void_p(4), None)
+    assert rc == tde._capi.TDE_ERR_INVALID_ARG and "scratch" in tde._capi.last_error()
+    proj = (C.c_float * 12)()
+    rc = lib.tde_rgbd_correspondences(C.c_void_p(1), C.c_void_p(2), C.c_void_p(3), C.c_void_p(4), C.c_void_p(5),
+                                      None, 640, 480, None, 0, proj, 0.07, 35.0, 10.0, C.c_void_p(6), C.c_void_p(7),
+                                      C.c_void_p(8), C.c_void_p(9), C.c_void_p(10), None)
+    assert rc == tde._capi.TDE_ERR_INVALID_ARG  # dx without dy
     d = rg.default_params()
     assert d.levels == 4 and list(d.iters) == [7, 7, 7, 10] and list(d.min_gradient) == [10.0] * 4
     assert abs(d.max_depth_diff - 0.07) < 1e-7 and d.max_depth == 35.0
