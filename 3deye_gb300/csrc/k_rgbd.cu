@@ -10,15 +10,16 @@
 // t' = K t, depth and gradient tests) and sums the squared intensity
 // differences -- integers, so the sum is exact in any order; the second
 // forms sigma from those sums, each kept pair's weighted Jacobian row and the
-// 27 terms of [A | b], reduced per block in FP64 in a fixed order; a
-// one-warp kernel sums the blocks, solves in FP64 and moves the pose
-// (T <- exp(xi) T, the ICP path's solve).  Every step is launches only: the
+// 27 terms of [A | b], reduced per block in FP64 in a fixed order; the last
+// block of that pass sums the blocks, solves in FP64 and moves the pose
+// (T <- exp(xi) T, the ICP path's solve).  Every step is two launches: the
 // pose lives on the device, nothing waits on the host.
 //
 // Built with -fmad=false: the pair tests and row values are the same IEEE
 // operations as the CPU oracle (oracle/oracle_rgbd.c), explicit fused
 // multiply-adds written out on both sides.
 #include <cmath>
+#include <utility>
 
 #include "tde_common.cuh"
 #include "tde_icp.cuh"
