@@ -48,6 +48,7 @@
 #include "oracle.h"
 
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #define RGBD_SOBEL_SCALE 0.125f
@@ -219,7 +220,8 @@ int or_rgbd_pairs(const uint8_t *Ip, const float *Dp, const uint8_t *Ic, const f
     rgbd_level_t L;
     rgbd_setup(&L, Ip, Dp, Ic, Dc, dx, dy, in, R, t, max_depth_diff, max_depth, min_gradient);
     int n = 0;
-    double s = 0.0;
+    double s = 0.0;  /* sums of squared integers: exact in any order */
+#pragma omp parallel for schedule(static) reduction(+ : n, s)
     for (int i = 0; i < L.W * L.H; ++i) {
         int j = -1;
         float r = 0.f;
@@ -240,8 +242,9 @@ int or_rgbd_lsm(const uint8_t *Ip, const float *Dp, const uint8_t *Ic, const flo
                 float max_depth, float min_gradient, double *sums, float *sigma_out) {
     rgbd_level_t L;
     rgbd_setup(&L, Ip, Dp, Ic, Dc, dx, dy, in, R, t, max_depth_diff, max_depth, min_gradient);
-    double s2 = 0.0;
+    double s2 = 0.0;  /* sums of squared integers: exact in any order */
     int n = 0;
+#pragma omp parallel for schedule(static) reduction(+ : n, s2)
     for (int i = 0; i < L.W * L.H; ++i) {
         int j;
         float r;
@@ -249,18 +252,28 @@ int or_rgbd_lsm(const uint8_t *Ip, const float *Dp, const uint8_t *Ic, const flo
     }
     const float sigma = rgbd_sigma(n, s2);
     if (sigma_out) *sigma_out = sigma;
-    for (int k = 0; k < 28; ++k) sums[k] = 0.0;
-    for (int i = 0; i < L.W * L.H; ++i) {
-        int j;
-        float r;
-        if (!rgbd_pair(&L, i, &j, &r)) continue;
-        float row[7];
-        rgbd_row(&L, i, j, r, sigma, row);
-        int s = 0;
-        for (int a = 0; a < 6; ++a)
-            for (int b = a; b < 7; ++b) sums[s++] += (double)row[a] * (double)row[b];
-        sums[27] += 1.0;
+    /* per image row, then the rows in order: the same bits for any thread count */
+    double *rs = (double *)calloc((size_t)L.H * 28, sizeof(double));
+    if (!rs) return -1;
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < L.H; ++v) {
+        double *acc = rs + (size_t)v * 28;
+        for (int i = v * L.W; i < (v + 1) * L.W; ++i) {
+            int j;
+            float r;
+            if (!rgbd_pair(&L, i, &j, &r)) continue;
+            float row[7];
+            rgbd_row(&L, i, j, r, sigma, row);
+            int s = 0;
+            for (int a = 0; a < 6; ++a)
+                for (int b = a; b < 7; ++b) acc[s++] += (double)row[a] * (double)row[b];
+            acc[27] += 1.0;
+        }
     }
+    for (int k = 0; k < 28; ++k) sums[k] = 0.0;
+    for (int v = 0; v < L.H; ++v)
+        for (int k = 0; k < 28; ++k) sums[k] += rs[(size_t)v * 28 + k];
+    free(rs);
     return n;
 }
 
