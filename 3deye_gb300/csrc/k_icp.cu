@@ -28,6 +28,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kPixPerThread = 4;
+constexpr int kPixWide = 8;                    // pixels a thread on large levels
+constexpr int kPixWideMinPixels = 1 << 18;     // "large": 640x480, not 320x240
 
 struct f2 { float hi, lo; };
 
@@ -184,22 +186,23 @@ __device__ __forceinline__ f2 warp_transpose_reduce(const float (&s)[32], int la
 
 // Association, the per-block sums, and their exact addition into
 // accumulator buffer `acc` (copy blockIdx % kIcpAccCopies).
-__device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose &P, const float3 (&nc)[kPixPerThread],
-                                                 const float3 (&vc)[kPixPerThread], f2 (*red)[32],
+template <int PIX>
+__device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose &P, const float3 (&nc)[PIX],
+                                                 const float3 (&vc)[PIX], f2 (*red)[32],
                                                  unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3]) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float s[32];
     #pragma unroll
     for (int t = 0; t < 32; ++t) s[t] = 0.f;
-    Assoc as[kPixPerThread];
+    Assoc as[PIX];
     #pragma unroll
-    for (int k = 0; k < kPixPerThread; ++k) as[k] = project(a, P, nc[k], vc[k]);
-    float3 np[kPixPerThread], vp[kPixPerThread];
+    for (int k = 0; k < PIX; ++k) as[k] = project(a, P, nc[k], vc[k]);
+    float3 np[PIX], vp[PIX];
     #pragma unroll
-    for (int k = 0; k < kPixPerThread; ++k)
+    for (int k = 0; k < PIX; ++k)
         if (as[k].j >= 0) { np[k] = ld3(a.nprev, (size_t)as[k].j); vp[k] = ld3(a.vprev, (size_t)as[k].j); }
     #pragma unroll
-    for (int k = 0; k < kPixPerThread; ++k) {
+    for (int k = 0; k < PIX; ++k) {
         float row[7];
         if (as[k].j >= 0 && pair_terms(a, as[k], np[k], vp[k], row)) {
             int t = 0;
@@ -254,12 +257,13 @@ __device__ __forceinline__ bool last_block(IcpState *st, unsigned *ticket) {
 }
 
 // Loads this thread's current-frame maps (independent of the pose).
-__device__ __forceinline__ void load_current(const IcpArgs &a, float3 (&nc)[kPixPerThread], float3 (&vc)[kPixPerThread]) {
+template <int PIX>
+__device__ __forceinline__ void load_current(const IcpArgs &a, float3 (&nc)[PIX], float3 (&vc)[PIX]) {
     const int npix = a.W * a.H;
-    const int base = blockIdx.x * kThreads * kPixPerThread + threadIdx.x;
+    const int base = blockIdx.x * kThreads * PIX + threadIdx.x;
     const float qnan = __int_as_float(0x7fffffff);
     #pragma unroll
-    for (int k = 0; k < kPixPerThread; ++k) {
+    for (int k = 0; k < PIX; ++k) {
         const int p = base + k * kThreads;
         if (p < npix) { nc[k] = ld3(a.ncur, (size_t)p); vc[k] = ld3(a.vcur, (size_t)p); }
         else { nc[k] = make_float3(qnan, qnan, qnan); vc[k] = nc[k]; }
@@ -297,7 +301,7 @@ __global__ void __launch_bounds__(kThreads) icp_sums_kernel(const IcpArgs a, Icp
 }
 
 // Pipeline form, launch `iter` of the frame (see the file comment).
-template <bool LAST>
+template <int PIX, bool LAST>
 __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, IcpState *__restrict__ st, int iter,
                                                             const IcpPublish pub) {
     __shared__ IcpPose P;
@@ -309,8 +313,8 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     // Let the next launch start: it reads this launch's accumulators and
     // pose slot only after its own griddepcontrol.wait.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    float3 nc[kPixPerThread], vc[kPixPerThread];
-    load_current(a, nc, vc);
+    float3 nc[PIX], vc[PIX];
+    load_current<PIX>(a, nc, vc);
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     // ---- the pose this launch associates with ----
@@ -496,7 +500,14 @@ int launch_icp(const IcpArgs &a, IcpState *st, float *mbuf, cudaStream_t stream)
 }
 
 int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const IcpPublish &pub, cudaStream_t stream) {
-    const unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * kPixPerThread));
+    // Large levels take kPixWide pixels a thread: half the blocks, one per
+    // SM, which leaves room to the next frame's preprocessing running beside
+    // (measured with 640x480 frames: ICP 0.1516 against 0.1531 ms per frame,
+    // 3043 against 3026 frames/s overlapped; eight pixels a thread on the
+    // coarse levels too gave 3094 frames/s but 0.162 ms and a slower
+    // end-to-end line, 3007 against 3053)
+    const bool wide = a.W * a.H >= kPixWideMinPixels;
+    const unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * (wide ? kPixWide : kPixPerThread)));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
     cfg.blockDim = dim3(kThreads);
@@ -506,8 +517,13 @@ int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const I
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<true>, a, st, iter, pub)
-                         : cudaLaunchKernelEx(&cfg, icp_step_kernel<false>, a, st, iter, pub);
+    cudaError_t e;
+    if (wide)
+        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, true>, a, st, iter, pub)
+                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, false>, a, st, iter, pub);
+    else
+        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, true>, a, st, iter, pub)
+                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, false>, a, st, iter, pub);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "icp_step: %s", cudaGetErrorString(e));
     return check_launch("icp_step");
 }
