@@ -10,7 +10,8 @@
 //
 // Pipeline form: launch i's blocks, once the programmatic dependency on
 // launch i - 1 has resolved (its atomics complete and visible), read its
-// exact totals and solve the 6x6 system in FP64 themselves -- every block the
+// exact totals and solve the 6x6 system themselves (float-float arithmetic,
+// tde_solve.cuh) -- every block the
 // same operations on the same bits, so the same pose -- instead of a last
 // block of launch i - 1 solving after a grid-wide ticket.  That takes the
 // ticket, its fence and one dependent read off every iteration; only the
@@ -130,8 +131,7 @@ __device__ __forceinline__ __int128 to_fixed(float f) {
 
 // Sum of the three 42-bit limbs modulo 2^126, read as a signed value v:
 // v * 2^-64 rounded to the nearest double (ties to even), built with integer
-// operations only (the FP64 pipe carries the solve), and the integer part
-// floor(v / 2^64) in *whole.
+// operations only, and the integer part floor(v / 2^64) in *whole.
 __device__ __forceinline__ double from_fixed(unsigned long long a0, unsigned long long a1, unsigned long long a2,
                                              long long *whole) {
     unsigned __int128 S = (unsigned __int128)a0 + ((unsigned __int128)a1 << 42) + ((unsigned __int128)a2 << 84);
@@ -153,6 +153,30 @@ __device__ __forceinline__ double from_fixed(unsigned long long a0, unsigned lon
         if (++mant == (1ull << 52)) { mant = 0ull; ++bexp; }
     }
     return __longlong_as_double((long long)(((unsigned long long)neg << 63) | (bexp << 52) | mant));
+}
+
+// The same sum as a float-float pair (hi = its leading 24 bits, lo = the next
+// 32 rounded to a float, then renormalised; relative error below 2^-48),
+// with integer operations and one integer-to-float conversion.
+__device__ __forceinline__ ffl from_fixed_ff(unsigned long long a0, unsigned long long a1, unsigned long long a2,
+                                             long long *whole) {
+    unsigned __int128 S = (unsigned __int128)a0 + ((unsigned __int128)a1 << 42) + ((unsigned __int128)a2 << 84);
+    S &= ((unsigned __int128)1 << 126) - 1;
+    const bool neg = (S >> 125) & 1;
+    __int128 v = (__int128)S;
+    if (neg) v -= (__int128)1 << 126;
+    *whole = (long long)(v >> 64);
+    const unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;  // |v| <= 2^125
+    const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+    if ((mh | ml) == 0ull) return ffl{0.f, 0.f};
+    const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);  // 2 .. 127
+    const unsigned long long top = (unsigned long long)((m << lz) >> 64);   // leading one at bit 63
+    // the leading one weighs 2^(63 - lz): biased exponent 190 - lz; bit 8 of
+    // top weighs 2^(8 - lz): the power of two with biased exponent 135 - lz
+    const float hi = __uint_as_float(((unsigned)(190 - lz) << 23) | (unsigned)((top >> 40) & 0x7fffffull));
+    const float lo = __fmul_rn(__uint2float_rn((unsigned)(top >> 8)), __uint_as_float((unsigned)(135 - lz) << 23));
+    const ffl r = ffl_fast_two_sum(hi, lo);  // lo < ulp(hi)
+    return neg ? ffl_neg(r) : r;
 }
 
 // Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
@@ -244,6 +268,20 @@ __device__ __forceinline__ double read_total(const unsigned long long (*acc)[kIc
     return from_fixed(a0, a1, a2, whole);
 }
 
+// read_total as a float-float pair.
+__device__ __forceinline__ ffl read_total_ff(const unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3], int term,
+                                            long long *whole) {
+    unsigned long long v[kIcpAccCopies][3];
+    #pragma unroll
+    for (int c = 0; c < kIcpAccCopies; ++c)
+        #pragma unroll
+        for (int l = 0; l < 3; ++l) v[c][l] = __ldcg(&(*acc)[c][term][l]);
+    unsigned long long a0 = 0, a1 = 0, a2 = 0;
+    #pragma unroll
+    for (int c = 0; c < kIcpAccCopies; ++c) { a0 += v[c][0]; a1 += v[c][1]; a2 += v[c][2]; }
+    return from_fixed_ff(a0, a1, a2, whole);
+}
+
 // Last block of a launch: true for exactly one block, after every block's
 // atomics are complete.
 __device__ __forceinline__ bool last_block(IcpState *st, unsigned *ticket) {
@@ -306,7 +344,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
                                                             const IcpPublish pub) {
     __shared__ IcpPose P;
     __shared__ f2 red[kThreads / 32][32];
-    __shared__ double Rs[9], ts[3];  // this launch's FP64 pose
+    __shared__ ffl Rs[9], ts[3];  // this launch's pose (float-float)
     __shared__ unsigned ticket;
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -320,61 +358,64 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     // ---- the pose this launch associates with ----
     // Solver warp: 0, or 2 for every other wave of blocks, so that two blocks
     // resident on one SM (blocks b and b + SM count) solve on different
-    // sub-partitions and their FP64 instruction streams do not queue on one
-    // FP64 pipe.  Warp 1 loads the frame's start pose meanwhile.
+    // sub-partitions: each solve is one long dependent instruction stream,
+    // and two of them on one scheduler interleave.  Warp 1 loads the frame's
+    // start pose meanwhile.
     const int solver = ((blockIdx.x / a.sm_count) & 1) * 2;
     if (warp == solver) {
-        const double *R0 = iter == 0 ? st->R : st->R_it[(iter - 1) & 1];
-        const double *t0 = iter == 0 ? st->t : st->t_it[(iter - 1) & 1];
-        // the previous pose and the previous launch's totals, loads in flight together
-        double pv = 0.0, term = 0.0;
+        // the previous pose and the previous launch's totals, loads in flight
+        // together; launch 0 converts the frame's FP64 start pose instead
+        ffl pv{0.f, 0.f}, term{0.f, 0.f};
+        double pd = 0.0;
         long long whole = 0;
-        if (lane < 12) pv = __ldcg(lane < 9 ? R0 + lane : t0 + (lane - 9));
-        if (iter > 0 && lane < kIcpTerms) term = read_total(&st->acc[(iter - 1) % kIcpAccBuffers], lane, &whole);
+        if (iter == 0) {
+            if (lane < 12) pd = __ldcg(lane < 9 ? st->R + lane : st->t + (lane - 9));
+            pv = ffl_from_double(pd);
+        } else {
+            if (lane < 12) {
+                const float2 q = __ldcg(&st->pose_it[(iter - 1) & 1][lane]);
+                pv = ffl{q.x, q.y};
+            }
+            if (lane < kIcpTerms) term = read_total_ff(&st->acc[(iter - 1) % kIcpAccBuffers], lane, &whole);
+        }
         if (lane < 9) Rs[lane] = pv;
         else if (lane < 12) ts[lane - 9] = pv;
         __syncwarp();
         bool ok = true;
         int inliers = 0;
-        double xl = 0.0;
         if (iter > 0) {
             inliers = __shfl_sync(0xffffffffu, (int)whole, 27);
-            double o;
+            ffl o, xl;
             ok = warp_solve_step(term, Rs, ts, lane, o, xl) && inliers >= kIcpMinInliers;
             if (ok) pv = o;
             __syncwarp();
             if (lane < 9) Rs[lane] = pv;
             else if (lane < 12) ts[lane - 9] = pv;
         }
-        if (lane < 9) P.R_cur[lane] = (float)pv;
-        else if (lane < 12) P.t_cur[lane - 9] = (float)pv;
+        if (lane < 9) P.R_cur[lane] = pv.hi;
+        else if (lane < 12) P.t_cur[lane - 9] = pv.hi;
         if (iter == 0) {
             // the frame's start pose is the association reference: R^T, t
-            if (lane < 9) P.R_prev_inv[3 * (lane % 3) + lane / 3] = (float)pv;
-            else if (lane < 12) P.t_prev[lane - 9] = (float)pv;
+            if (lane < 9) P.R_prev_inv[3 * (lane % 3) + lane / 3] = pv.hi;
+            else if (lane < 12) P.t_prev[lane - 9] = pv.hi;
         }
         if (blockIdx.x == 0) {
             // publish the pose for the next launch, and the bookkeeping of the solve
-            if (lane < 9) st->R_it[iter & 1][lane] = pv;
-            else if (lane < 12) st->t_it[iter & 1][lane - 9] = pv;
+            if (lane < 12) st->pose_it[iter & 1][lane] = make_float2(pv.hi, pv.lo);
             if (iter == 0) {
                 if (lane < 9) {
-                    st->R_start[lane] = pv;
-                    st->pose.R_prev_inv[3 * (lane % 3) + lane / 3] = (float)pv;
+                    st->R_start[lane] = pd;
+                    st->pose.R_prev_inv[3 * (lane % 3) + lane / 3] = pv.hi;
                 } else if (lane < 12) {
-                    st->t_start[lane - 9] = pv;
-                    st->pose.t_prev[lane - 9] = (float)pv;
+                    st->t_start[lane - 9] = pd;
+                    st->pose.t_prev[lane - 9] = pv.hi;
                 }
                 if (lane == 0) { st->status = 0; st->iterations = 0; }
             }
-            if (iter > 0) {
-                if (lane < kIcpTerms) st->sums[lane] = term;
-                if (ok && lane < 6) st->x[lane] = xl;
-                if (lane == 0) {
-                    st->inliers = inliers;
-                    if (!ok) st->status |= kIcpStatusSolveFailed;
-                    st->iterations += 1;
-                }
+            if (iter > 0 && lane == 0) {
+                st->inliers = inliers;
+                if (!ok) st->status |= kIcpStatusSolveFailed;
+                st->iterations += 1;
             }
         }
     } else if (iter > 0 && warp == 1 && lane < 12) {
@@ -396,9 +437,9 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
 
     // ---- the frame's last launch: its last block solves its own totals ----
     if (!last_block(st, &ticket)) return;
-    double term = 0.0;
+    ffl term{0.f, 0.f};
     long long whole = 0;
-    if (warp == 0 && lane < kIcpTerms) term = read_total(&st->acc[iter % kIcpAccBuffers], lane, &whole);
+    if (warp == 0 && lane < kIcpTerms) term = read_total_ff(&st->acc[iter % kIcpAccBuffers], lane, &whole);
     __syncthreads();
     // every launch of the frame has read what it needed: clear all buffers
     // so that the next frame's first launch adds into zeros
@@ -408,13 +449,13 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     }
     if (warp != 0) return;
     const int inliers = __shfl_sync(0xffffffffu, (int)whole, 27);
-    double o, xl;
+    ffl o, xl;
     const bool ok = warp_solve_step(term, Rs, ts, lane, o, xl) && inliers >= kIcpMinInliers;
-    // accept the estimate, or keep the start pose when any solve failed
+    // accept the estimate (in FP64), or keep the start pose when any solve failed
     const bool lost = !ok || (*(volatile int *)&st->status & kIcpStatusSolveFailed);
     double nv = 0.0;
-    if (lane < 9) nv = lost ? st->R_start[lane] : (ok ? o : Rs[lane]);
-    else if (lane < 12) nv = lost ? st->t_start[lane - 9] : (ok ? o : ts[lane - 9]);
+    if (lane < 9) nv = lost ? st->R_start[lane] : ffl_to_double(o);
+    else if (lane < 12) nv = lost ? st->t_start[lane - 9] : ffl_to_double(o);
     if (lane < 9) {
         st->R[lane] = nv;
         st->pose.R_cur[lane] = (float)nv;
@@ -427,8 +468,6 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
         pub.cam->t[lane - 9] = (float)nv;
         pub.pose12[lane] = nv;
     }
-    if (lane < kIcpTerms) st->sums[lane] = term;
-    if (ok && lane < 6) st->x[lane] = xl;
     if (lane == 0) {
         st->counter = 0u;
         st->inliers = inliers;
@@ -445,19 +484,19 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
 // updated in place, x[6 n], ok[n].
 __global__ void icp_solve_kernel(const double *__restrict__ sums, int n, double *__restrict__ pose,
                                  double *__restrict__ x, int *__restrict__ okv) {
-    __shared__ double Rs[4][9], ts[4][3];
+    __shared__ ffl Rs[4][9], ts[4][3];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * 4 + warp;
     if (i >= n) return;  // whole warps leave together
-    const double term = lane < kIcpTerms ? sums[(size_t)28 * i + lane] : 0.0;
+    const ffl term = ffl_from_double(lane < kIcpTerms ? sums[(size_t)28 * i + lane] : 0.0);
     const double pv = lane < 12 ? pose[(size_t)12 * i + lane] : 0.0;
-    if (lane < 9) Rs[warp][lane] = pv;
-    else if (lane < 12) ts[warp][lane - 9] = pv;
+    if (lane < 9) Rs[warp][lane] = ffl_from_double(pv);
+    else if (lane < 12) ts[warp][lane - 9] = ffl_from_double(pv);
     __syncwarp();
-    double o, xl;
+    ffl o, xl;
     const bool ok = warp_solve_step(term, Rs[warp], ts[warp], lane, o, xl);
-    if (lane < 12) pose[(size_t)12 * i + lane] = ok ? o : pv;
-    if (ok && lane < 6) x[(size_t)6 * i + lane] = xl;
+    if (lane < 12) pose[(size_t)12 * i + lane] = ok ? ffl_to_double(o) : pv;
+    if (ok && lane < 6) x[(size_t)6 * i + lane] = ffl_to_double(xl);
     if (lane == 0) okv[i] = ok;
 }
 

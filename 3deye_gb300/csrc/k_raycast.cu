@@ -204,15 +204,19 @@ __device__ __forceinline__ void sample_voxel(const RayParams &p, const f3 &org, 
     sz = axis_floor(fmaf(rf.d[2], ct, rf.o[2]), org.z, dir.z, p.cell.z, ct);
 }
 
+// A block takes 16 x kRayBlockRows pixels, a warp an 8 x 4 tile.
+constexpr int kRayBlockRows = 16;
+constexpr int kRayThreads = 16 * kRayBlockRows;
+
 template <int FMT, bool SKIP, bool STATS>
-__global__ void __launch_bounds__(256) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
+__global__ void __launch_bounds__(kRayThreads) raycast_kernel(const void *__restrict__ vol, float *__restrict__ vmap,
                                                      float *__restrict__ nmap, const __grid_constant__ RayParams p) {
-    // 16x16 pixels per block; each warp takes an 8x4 tile so its rays start
-    // close together and sample neighbouring voxels.
+    // each warp takes an 8x4 tile so its rays start close together and
+    // sample neighbouring voxels
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const int y = blockIdx.y * kRayBlockRows + (warp >> 1) * 4 + (lane >> 3);
     const int W = p.intr.cols, H = p.intr.rows;
     // the pose: from the parameters, or read on the device
     tde_matrix3f R = p.R;
@@ -517,8 +521,8 @@ int launch_raycast(const void *volume, int format, float *vmap, float *nmap, con
     const bool whole = rb.voxels_size.x % 32 == 0 && rb.voxels_size.y % 32 == 0 && rb.voxels_size.z % 32 == 0;
     p.super_flags = (neg_flags && whole) ? neg_flags + brick_count(rb) : nullptr;
     p.touched = touched;
-    dim3 block(256);
-    dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, 16));
+    dim3 block(kRayThreads);
+    dim3 grid(div_up(intr.cols, 16), div_up(intr.rows, kRayBlockRows));
     return dispatch_format(format, [&](auto F) {
         constexpr int FM = decltype(F)::value;
         if (touched) {

@@ -11,8 +11,8 @@
 // differences -- integers, so the sum is exact in any order; the second
 // forms sigma from those sums, each kept pair's weighted Jacobian row and the
 // 27 terms of [A | b], reduced per block in FP64 in a fixed order; the last
-// block of that pass sums the blocks, solves in FP64 and moves the pose
-// (T <- exp(xi) T, the ICP path's solve).  Every step is two launches: the
+// block of that pass sums the blocks, solves in float-float arithmetic and
+// moves the FP64 pose (T <- exp(xi) T, the ICP path's solve).  Every step is two launches: the
 // pose lives on the device, nothing waits on the host.
 //
 // Built with -fmad=false: the pair tests and row values are the same IEEE
@@ -454,18 +454,18 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, double *__
     __syncthreads();
     if (warp != 0) return;
     if (lane == 0) *counter = 0u;
-    __shared__ double Rs[9], ts[3];
+    __shared__ ffl Rs[9], ts[3];
     double term = 0.0;
     if (lane < 28)
         for (int w = 0; w < kThreads / 32; ++w) term += red[w][lane];
     const double pv = lane < 12 ? pose[lane] : 0.0;
-    if (lane < 9) Rs[lane] = pv;
-    else if (lane < 12) ts[lane - 9] = pv;
+    if (lane < 9) Rs[lane] = ffl_from_double(pv);
+    else if (lane < 12) ts[lane - 9] = ffl_from_double(pv);
     __syncwarp();
     const double count = __shfl_sync(0xffffffffu, term, 27);
-    double o, xl;
-    const bool ok = count >= (double)kIcpMinInliers && warp_solve_step(term, Rs, ts, lane, o, xl);
-    if (lane < 12) pose[lane] = ok ? o : pv;
+    ffl o, xl;
+    const bool ok = count >= (double)kIcpMinInliers && warp_solve_step(ffl_from_double(term), Rs, ts, lane, o, xl);
+    if (lane < 12) pose[lane] = ok ? ffl_to_double(o) : pv;
     if (lane == 0) *status |= ok ? 2 : 1;
 }
 

@@ -27,9 +27,10 @@ struct IcpState {
     int status, inliers, iterations, pad0;
     unsigned counter;  // blocks done in the running launch (reset by the last block)
     unsigned pad1[3];
-    // Pipeline form: the FP64 pose launch i associated with, in slot i & 1,
-    // and the pose the frame started from (kept when a solve fails).
-    double R_it[2][9], t_it[2][3];
+    // Pipeline form: the pose launch i associated with, in slot i & 1, as
+    // float-float pairs (x = hi, y = lo; R row-major, then t), and the FP64
+    // pose the frame started from (kept when a solve fails).
+    float2 pose_it[2][12];
     double R_start[9], t_start[3];
     // Cross-block sums as 126-bit fixed point (2^-64 units) in three 42-bit
     // limbs; integer atomics make the total independent of block order.
@@ -99,7 +100,7 @@ int launch_icp(const IcpArgs &a, IcpState *st, float *mbuf, cudaStream_t stream)
 // (or returns to the start pose when a solve failed), commits it to st->R /
 // st->t and publishes it through `pub`.
 int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const IcpPublish &pub, cudaStream_t stream);
-// The pipeline's FP64 solve-and-update step alone, on n systems (device
+// The pipeline's float-float solve-and-update step alone (FP64 in and out), on n systems (device
 // arrays: sums[28 n], pose[12 n] in place, x[6 n], ok[n]).
 int launch_icp_solve(const double *sums, int n, double *pose, double *x, int *ok, cudaStream_t stream);
 

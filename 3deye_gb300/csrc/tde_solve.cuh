@@ -1,50 +1,11 @@
-// tde_solve.cuh -- the FP64 6x6 solve and pose update shared by the ICP
-// iterations (k_icp.cu) and the RGB-D odometry steps (k_rgbd.cu).
+// tde_solve.cuh -- the 6x6 solve and pose update shared by the ICP
+// iterations (k_icp.cu) and the RGB-D odometry steps (k_rgbd.cu), run by one
+// warp in float-float arithmetic.
 #pragma once
 #include "tde_common.cuh"
 
 namespace tde {
 namespace {
-
-// ---------------------------------------------------------------------------
-// FP64 solve and pose update, run by one warp per block.
-//
-// GB300 executes FP64 at a small fraction of the FP32 rate: each FP64 warp
-// instruction occupies a sub-partition's FP64 pipe for ~64 cycles, whether
-// one lane or 32 are active and whether or not it depends on the previous one
-// (measured).  The solve's time is therefore its count of FP64 instructions:
-// lanes share every instruction (one matrix or vector entry each, operands
-// chosen by lane), exchange values by shuffles, test positivity on exponent
-// bits in the integer pipe, form both inverses from one reciprocal, and
-// evaluate the SO(3) exponential's two series in one instruction stream.
-// ---------------------------------------------------------------------------
-// A(theta) = sin(theta)/theta, B(theta) = (1 - cos(theta))/theta^2, for all
-// lanes of the warp: even lanes evaluate A's series, odd lanes B's, in the
-// same instructions.
-__device__ __forceinline__ void rodrigues_coeffs(double th2, int lane, double &A, double &B) {
-    if (__double_as_longlong(th2) < __double_as_longlong(1e-2)) {  // theta < 0.1 (th2 >= 0): truncation below 1e-17
-        const bool odd = lane & 1;
-        const double c4 = odd ? 1.0 / 3628800.0 : 1.0 / 362880.0, c3 = odd ? -1.0 / 40320.0 : -1.0 / 5040.0;
-        const double c2 = odd ? 1.0 / 720.0 : 1.0 / 120.0, c1 = odd ? -1.0 / 24.0 : -1.0 / 6.0, c0 = odd ? 0.5 : 1.0;
-        const double v = fma(th2, fma(th2, fma(th2, fma(th2, c4, c3), c2), c1), c0);
-        A = __shfl_sync(0xffffffffu, v, 0);
-        B = __shfl_sync(0xffffffffu, v, 1);
-    } else {
-        double th = sqrt(th2), sn, cs;
-        sincos(th, &sn, &cs);
-        A = sn / th;
-        B = (1.0 - cs) / th2;
-    }
-}
-
-// Biased binary exponent (0 for +-0 and subnormals, 2047 for Inf / NaN).
-__device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
-// x positive and finite, and x > 2^(e_ref - 1023 - 100) to within a factor of
-// two: "clearly positive" against a reference exponent (integer pipe).
-__device__ __forceinline__ bool clearly_pos(double x, int e_ref) {
-    const long long bx = __double_as_longlong(x);
-    return bx > 0 && dexp(x) < 2047 && dexp(x) > e_ref - 100;
-}
 
 // Term index of entry (r, c) of [A | b] in the 27-term upper-triangular
 // order of opencl_wrappers.cpp:426-437 (row k holds columns k..6).
@@ -53,108 +14,247 @@ __host__ __device__ __forceinline__ int term_index(int r, int c) {
     return k * 7 - (k * (k - 1)) / 2 + (j - k);
 }
 
-// 1/d for a positive normal d: the hardware approximation (relative error
-// below 2^-20, measured), then two Newton-Raphson steps x <- x + x (1 - d x),
-// each squaring the relative error (measured on 2^20 inputs from 2^-200 to
-// 2^199: equal to the IEEE quotient 1.0 / d for every one).
-__device__ __forceinline__ double rcp_nr(double d) {
-    double x;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
+// ---------------------------------------------------------------------------
+// Float-float arithmetic on the FP32 pipe.
+//
+// GB300 executes FP64 at a small fraction of the FP32 rate: an FP64 warp
+// instruction occupies a sub-partition's FP64 pipe for ~64 cycles and a
+// dependent one waits longer still (measured), so a solve written in FP64 is
+// a chain of slow steps (3.0 us per Gauss-Newton step).  Here a value is
+// hi + lo in two floats with |lo| <= ulp(hi) / 2: 48 significant bits.
+// Products are split exactly with one fused multiply-add (Dekker's product,
+// FMA form), high parts are added exactly with Knuth's TwoSum, and the
+// low-order parts are added in float in a fixed order, as in the
+// double-double algorithms of Hida, Li and Bailey (2001) with float parts.
+// The solve's chain of 2x2 determinants and 3-term dot products then runs on
+// 4-cycle float operations at about 2^-46 relative precision (against 2^-53
+// for FP64): far below the rounding of the float association terms it solves.
+// ---------------------------------------------------------------------------
+struct ffl {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ffl ffl_two_sum(float a, float b) {  // a + b exactly
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ffl{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ffl ffl_fast_two_sum(float a, float b) {  // exact when |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return ffl{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ffl ffl_neg(ffl a) { return ffl{-a.hi, -a.lo}; }
+__device__ __forceinline__ ffl ffl_scale(ffl a, float pow2) { return ffl{__fmul_rn(a.hi, pow2), __fmul_rn(a.lo, pow2)}; }
+__device__ __forceinline__ ffl ffl_mul(ffl a, ffl b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);  // p + e = a.hi b.hi exactly
+    const float x = __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi));
+    return ffl_fast_two_sum(p, __fadd_rn(e, x));
+}
+__device__ __forceinline__ ffl ffl_add(ffl a, ffl b) {
+    const ffl s = ffl_two_sum(a.hi, b.hi), t = ffl_two_sum(a.lo, b.lo);
+    const ffl u = ffl_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return ffl_fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+// z + sum_{i < N} a_i b_i (z = 0 without Z): each product's high part with
+// its exact rounding error, the high parts (and z's) added exactly in a
+// pairwise TwoSum tree, every low-order part added in float in a fixed order.
+template <int N, bool Z>
+__device__ __forceinline__ ffl ffl_dot(const ffl (&a)[N], const ffl (&b)[N], ffl z) {
+    constexpr int M = N + (Z ? 1 : 0);
+    float h[M];
+    float lo = Z ? z.lo : 0.f;
     #pragma unroll
-    for (int k = 0; k < 2; ++k) x = fma(x, fma(-d, x, 1.0), x);
-    return x;
+    for (int i = 0; i < N; ++i) {
+        h[i] = __fmul_rn(a[i].hi, b[i].hi);
+        const float e = __fmaf_rn(a[i].hi, b[i].hi, -h[i]);
+        const float x = __fmaf_rn(a[i].hi, b[i].lo, __fmul_rn(a[i].lo, b[i].hi));
+        lo = __fadd_rn(lo, __fadd_rn(e, x));
+    }
+    if constexpr (Z) h[N] = z.hi;
+    #pragma unroll
+    for (int w = 1; w < M; w *= 2)
+        #pragma unroll
+        for (int i = 0; i + w < M; i += 2 * w) {
+            const ffl s = ffl_two_sum(h[i], h[i + w]);
+            h[i] = s.hi;
+            lo = __fadd_rn(lo, s.lo);
+        }
+    return ffl_two_sum(h[0], lo);
+}
+// 1/d for a positive normal d: the hardware approximation x of 1/d.hi
+// (relative error below 2^-22), then 1/d = x / (1 - e) with e = 1 - d x
+// formed exactly up to d.lo's term: x + x (e + e^2), relative error ~e^3.
+__device__ __forceinline__ ffl ffl_rcp(ffl d) {
+    float x;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(x) : "f"(d.hi));
+    const float p = __fmul_rn(d.hi, x);
+    const float pe = __fmaf_rn(d.hi, x, -p);  // p + pe = d.hi x; 1 - p is exact (p within 2^-21 of 1)
+    const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.f, p), pe), __fmul_rn(d.lo, x));
+    return ffl_fast_two_sum(x, __fmul_rn(x, __fmaf_rn(e, e, e)));
+}
+// Conversions through the FP64 pipe: for values that enter or leave the
+// solve once per frame, not for every step.
+__device__ __forceinline__ ffl ffl_from_double(double d) {
+    const float hi = __double2float_rn(d);
+    return ffl{hi, __double2float_rn(d - (double)hi)};
+}
+__device__ __forceinline__ double ffl_to_double(ffl a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ ffl shfl(ffl v, int src) {
+    return ffl{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+__device__ __forceinline__ ffl pick3(int i, ffl a, ffl b, ffl c) { return i == 0 ? a : (i == 1 ? b : c); }
+
+// Biased binary exponent of a float (0 for +-0 and subnormals, 255 for Inf /
+// NaN), and "clearly positive" against a reference exponent, as for FP64.
+__device__ __forceinline__ int fexp(float x) { return (int)((__float_as_uint(x) >> 23) & 0xffu); }
+__device__ __forceinline__ bool clearly_pos_f(float x, int e_ref) {
+    return __float_as_int(x) > 0 && fexp(x) < 255 && fexp(x) > e_ref - 100;
+}
+// 2^-floor(e / 2) for a positive normal d = m 2^e (so d scaled by its square
+// lies in [1, 4)); 1 for anything else.
+__device__ __forceinline__ float diag_scale(float d) {
+    if (!(__float_as_int(d) > 0 && fexp(d) > 0 && fexp(d) < 255)) return 1.f;
+    const int k = -((fexp(d) - 127) >> 1);
+    return __uint_as_float((unsigned)(127 + k) << 23);
 }
 
-__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-__device__ __forceinline__ double pick3(int i, double a, double b, double c) { return i == 0 ? a : (i == 1 ? b : c); }
+// Float-float constants of the series below: hi = the float nearest the
+// coefficient, lo = the float nearest the rest (folded at compile time).
+constexpr double kInv6 = -1.0 / 6.0, kInv24 = -1.0 / 24.0, kInv120 = 1.0 / 120.0, kInv720 = 1.0 / 720.0;
+constexpr float kInv6h = (float)kInv6, kInv6l = (float)(kInv6 - (double)kInv6h);
+constexpr float kInv24h = (float)kInv24, kInv24l = (float)(kInv24 - (double)kInv24h);
+constexpr float kInv120h = (float)kInv120, kInv120l = (float)(kInv120 - (double)kInv120h);
+constexpr float kInv720h = (float)kInv720, kInv720l = (float)(kInv720 - (double)kInv720h);
 
-// One Gauss-Newton step, executed by all 32 lanes of a warp.  Lane l < 28
-// holds term l of [A | b] (27 terms, then the inlier count).  With
-// A = [[P, Q], [Q^T, R]] and adjugates (no division until the end):
+// A(theta) = sin(theta)/theta, B(theta) = (1 - cos(theta))/theta^2 for all
+// lanes (even lanes evaluate A's series, odd lanes B's): below 0.1 rad the
+// series to theta^8, in Estrin's form (c0 + c1 t) + t^2 (c2 + t (c3 + c4 t)),
+// t = theta^2, the innermost part in float (it is below 1e-6 of the sum);
+// above, sin and cos in FP64 (a step of over 0.1 rad is rare).
+__device__ __forceinline__ void rodrigues_coeffs_ff(ffl th2, int lane, ffl &A, ffl &B) {
+    if (th2.hi < 1e-2f) {
+        const bool odd = lane & 1;
+        const float c4 = odd ? 1.f / 3628800.f : 1.f / 362880.f, c3 = odd ? -1.f / 40320.f : -1.f / 5040.f;
+        const ffl c2 = odd ? ffl{kInv720h, kInv720l} : ffl{kInv120h, kInv120l};
+        const ffl c1 = odd ? ffl{kInv24h, kInv24l} : ffl{kInv6h, kInv6l};
+        const ffl c0{odd ? 0.5f : 1.f, 0.f};
+        const ffl tail{__fmaf_rn(th2.hi, c4, c3), 0.f};
+        const ffl t2 = ffl_mul(th2, th2);
+        const ffl lo_part = ffl_dot<1, true>({th2}, {c1}, c0);
+        const ffl hi_part = ffl_dot<1, true>({th2}, {tail}, c2);
+        const ffl v = ffl_dot<1, true>({t2}, {hi_part}, lo_part);
+        A = shfl(v, 0);
+        B = shfl(v, 1);
+    } else {
+        const double t2 = ffl_to_double(th2);
+        double th = sqrt(t2), sn, cs;
+        sincos(th, &sn, &cs);
+        A = ffl_from_double(sn / th);
+        B = ffl_from_double((1.0 - cs) / t2);
+    }
+}
+
+// One Gauss-Newton step, executed by all 32 lanes of a warp: lanes share every
+// instruction (one matrix or vector entry each, operands chosen by lane) and
+// exchange values by shuffles.  Lane l < 27 holds term l of [A | b] (term 27,
+// the inlier count, is not used).  [A | b] is first scaled by powers of two
+// (D A D y = D b, x = D y; D = diag(2^k) with every diagonal entry of D A D in
+// [1, 4): exact, and the adjugate products below stay far inside the float
+// range).  With A = [[P, Q], [Q^T, R]] and adjugates (no division until the
+// end):
 //   S' = det(P) R - Q^T adj(P) Q   (= det(P) S, S the Schur complement),
-//   u' = det(P) b2 - Q^T adj(P) b1,
-//   x2 = adj(S') u' / det(S'),   x1 = (adj(P) b1 - adj(P) Q x2) / det(P),
-// so 1/det(P) is formed while S' is, off the dependent chain.  The pose
-// (R_old, t_old: shared, FP64) moves by exp([x1]x), x2:
+//   u' = det(P) b2 - Q^T adj(P) b1,   U = adj(S') u',   W = (Q^T adj(P))^T U,
+//   x2 = U / det(S'),   x1 = adj(P) b1 / det(P) - W / (det(P) det(S')),
+// so both inverses come from one reciprocal of det(P) det(S') and only three
+// multiplications follow it.  The pose (R_old, t_old: shared memory) moves by
+// exp([x1]x), x2:
 //   R <- R + A (w x R) + B (w (w . R) - th2 R)   column by column, and
 //   t <- t + A (w x t) + B (w (w . t) - th2 t) + x2,   w = x1.
 // Lane l < 9 returns entry l of the new R (row-major) in `out`, lanes 9..11
 // entry l - 9 of the new t; lane l < 6 returns x[l] in `xl`.  False (out =
-// the old entry) when A is not positive definite (a pivot of P or S at or
-// below 1e-30, tested through the leading minors).
-__device__ bool warp_solve_step(double term, const double *R_old, const double *t_old, int lane, double &out,
-                                double &xl) {
+// the old entry) when A is not positive definite: a leading minor of the
+// scaled P or S at or below 2^-100 of its reference (integer tests on the
+// exponent bits), or a determinant product outside the normal float range.
+__device__ bool warp_solve_step(ffl term, const ffl *R_old, const ffl *t_old, int lane, ffl &out, ffl &xl) {
     const bool vec = lane >= 9;                       // lanes 9..11: vector entries
     const int vi = (lane >= 9 && lane < 12) ? lane - 9 : 0;
     const int l9 = lane < 9 ? lane : 0;
     const int r = l9 / 3, c = l9 % 3;
     const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-    // adj(P): cofactors (lane r, c), det(P) through the first row
-    const double CP = fma(shfl(term, term_index(r1, c1)), shfl(term, term_index(r2, c2)),
-                          -(shfl(term, term_index(r1, c2)) * shfl(term, term_index(r2, c1))));
-    const double P0 = shfl(term, 0), P1 = shfl(term, 1), P2 = shfl(term, 2);
-    const double detP = fma(P0, shfl(CP, 0), fma(P1, shfl(CP, 1), P2 * shfl(CP, 2)));
-    const double CP8 = shfl(CP, 8);  // P00 P11 - P01^2
-    // leading minors clearly positive: P00 > 2^-100, CP8 > 2^-100 P00, det P > 2^-100 CP8
-    bool ok = clearly_pos(P0, 1023) && clearly_pos(CP8, dexp(P0)) && clearly_pos(detP, dexp(CP8));
-    // T' = Q^T adj(P) (lane r, c: sum_k Q(k, r) adj(P)(k, c)); v = adj(P) b1 (lane 9 + i)
-    const int col = vec ? vi : c;
-    double TW = 0.0;
+    // ---- the scaling: lane l < 27 holds entry (i, j), i <= j (j = 6: b_i) ----
+    float sx1, sx2;  // the scales of unknowns vi and 3 + vi (lanes 9..11)
     {
-        double a[3], g[3];
-        #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            a[k] = shfl(term, vec ? term_index(k, 6) : term_index(k, 3 + r));
-            g[k] = shfl(CP, 3 * k + col);
-        }
-        TW = fma(a[0], g[0], fma(a[1], g[1], a[2] * g[2]));
+        const int i = (lane >= 7) + (lane >= 13) + (lane >= 18) + (lane >= 22) + (lane >= 25);
+        const int j = lane - term_index(i, i) + i;
+        const int jd = j < 6 ? j : 0;
+        const float si = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(i, i)));
+        const float sj = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(jd, jd)));
+        sx1 = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(vi, vi)));
+        sx2 = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(3 + vi, 3 + vi)));
+        if (lane < 27) term = ffl_scale(ffl_scale(term, si), j < 6 ? sj : 1.f);
     }
+    // adj(P): cofactors (lane r, c), det(P) through the first row
+    const ffl CP = ffl_dot<2, false>({shfl(term, term_index(r1, c1)), ffl_neg(shfl(term, term_index(r1, c2)))},
+                                     {shfl(term, term_index(r2, c2)), shfl(term, term_index(r2, c1))}, ffl{});
+    const ffl P0 = shfl(term, 0);
+    const ffl detP = ffl_dot<3, false>({P0, shfl(term, 1), shfl(term, 2)}, {shfl(CP, 0), shfl(CP, 1), shfl(CP, 2)}, ffl{});
+    const ffl CP8 = shfl(CP, 8);  // P00 P11 - P01^2
+    bool ok = clearly_pos_f(P0.hi, 127) && clearly_pos_f(CP8.hi, fexp(P0.hi)) && clearly_pos_f(detP.hi, fexp(CP8.hi));
+    // T' = Q^T adj(P) (lane r, c); v = adj(P) b1 (lane 9 + i)
+    const int col = vec ? vi : c;
+    const ffl TW = ffl_dot<3, false>(
+        {shfl(term, vec ? term_index(0, 6) : term_index(0, 3 + r)), shfl(term, vec ? term_index(1, 6) : term_index(1, 3 + r)),
+         shfl(term, vec ? term_index(2, 6) : term_index(2, 3 + r))},
+        {shfl(CP, col), shfl(CP, 3 + col), shfl(CP, 6 + col)}, ffl{});
     // S' = det(P) R - T' Q (lane r, c); u' = det(P) b2 - T' b1 (lane 9 + i)
     const int row = vec ? vi : r;
-    double SU;
-    {
-        const double base = detP * shfl(term, vec ? term_index(3 + vi, 6) : term_index(3 + r, 3 + c));
-        double t[3], y[3];
-        #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            t[k] = shfl(TW, 3 * row + k);
-            y[k] = shfl(term, vec ? term_index(k, 6) : term_index(k, 3 + c));
-        }
-        SU = fma(-t[0], y[0], fma(-t[1], y[1], fma(-t[2], y[2], base)));
-    }
-    // adj(S'), det(S'); the tests of S = S' / det(P) scaled accordingly
-    const double CS = fma(shfl(SU, 3 * r1 + c1), shfl(SU, 3 * r2 + c2), -(shfl(SU, 3 * r1 + c2) * shfl(SU, 3 * r2 + c1)));
-    const double S0 = shfl(SU, 0);
-    const double detS = fma(S0, shfl(CS, 0), fma(shfl(SU, 1), shfl(CS, 1), shfl(SU, 2) * shfl(CS, 2)));
-    const double CS8 = shfl(CS, 8);
-    // the same tests on S = S' / det(P)
-    const int eP = dexp(detP) - 1023;
-    ok = ok && clearly_pos(S0, 1023 + eP) && clearly_pos(CS8, dexp(S0) + eP) && clearly_pos(detS, dexp(CS8) + eP);
-    // both inverses from one reciprocal (of a finite product)
-    const double dPS = detP * detS;
-    ok = ok && dexp(dPS) < 2047;
-    const double rPS = rcp_nr(dPS);
-    const double rS = detP * rPS, rP = detS * rPS;
-    // x2 = adj(S') u' / det(S') (lane 9 + i)
-    const double X2 = fma(shfl(CS, 3 * vi), shfl(SU, 9), fma(shfl(CS, 3 * vi + 1), shfl(SU, 10), shfl(CS, 3 * vi + 2) * shfl(SU, 11))) * rS;
-    // x1 = (v - T'^T x2) / det(P) (lane 9 + i)
-    const double x20 = shfl(X2, 9), x21 = shfl(X2, 10), x22 = shfl(X2, 11);
-    const double X1 = fma(-shfl(TW, vi), x20, fma(-shfl(TW, 3 + vi), x21, fma(-shfl(TW, 6 + vi), x22, TW))) * rP;
-    const double wx = shfl(X1, 9), wy = shfl(X1, 10), wz = shfl(X1, 11);
+    const ffl SU = ffl_dot<4, false>(
+        {detP, ffl_neg(shfl(TW, 3 * row)), ffl_neg(shfl(TW, 3 * row + 1)), ffl_neg(shfl(TW, 3 * row + 2))},
+        {shfl(term, vec ? term_index(3 + vi, 6) : term_index(3 + r, 3 + c)), shfl(term, vec ? term_index(0, 6) : term_index(0, 3 + c)),
+         shfl(term, vec ? term_index(1, 6) : term_index(1, 3 + c)), shfl(term, vec ? term_index(2, 6) : term_index(2, 3 + c))},
+        ffl{});
+    // adj(S'), det(S'); U = adj(S') u' (lane 9 + i); the tests of S = S' / det(P)
+    const ffl CS = ffl_dot<2, false>({shfl(SU, 3 * r1 + c1), ffl_neg(shfl(SU, 3 * r1 + c2))},
+                                     {shfl(SU, 3 * r2 + c2), shfl(SU, 3 * r2 + c1)}, ffl{});
+    const ffl S0 = shfl(SU, 0);
+    const ffl detS = ffl_dot<3, false>({S0, shfl(SU, 1), shfl(SU, 2)}, {shfl(CS, 0), shfl(CS, 1), shfl(CS, 2)}, ffl{});
+    const ffl U = ffl_dot<3, false>({shfl(CS, 3 * vi), shfl(CS, 3 * vi + 1), shfl(CS, 3 * vi + 2)},
+                                    {shfl(SU, 9), shfl(SU, 10), shfl(SU, 11)}, ffl{});
+    // W = T'^T U (lane 9 + i), so that x1 = v / det(P) - W / (det(P) det(S'))
+    const ffl Wv = ffl_dot<3, false>({shfl(TW, vi), shfl(TW, 3 + vi), shfl(TW, 6 + vi)}, {shfl(U, 9), shfl(U, 10), shfl(U, 11)},
+                                     ffl{});
+    const ffl CS8 = shfl(CS, 8);
+    const int eP = fexp(detP.hi) - 127;
+    ok = ok && clearly_pos_f(S0.hi, 127 + eP) && clearly_pos_f(CS8.hi, fexp(S0.hi) + eP) &&
+         clearly_pos_f(detS.hi, fexp(CS8.hi) + eP);
+    // both inverses from one reciprocal (of a normal product)
+    const ffl dPS = ffl_mul(detP, detS);
+    ok = ok && fexp(dPS.hi) > 0 && fexp(dPS.hi) < 255;
+    const ffl rPS = ffl_rcp(dPS);
+    const ffl rS = ffl_mul(detP, rPS), rP = ffl_mul(detS, rPS);
+    const ffl rSP = ffl_mul(rS, rP);
+    // x2 = U / det(S'), x1 = v / det(P) - W / (det(P) det(S')) (lane 9 + i), then unscaled
+    const ffl X2 = ffl_scale(ffl_mul(U, rS), sx2);
+    const ffl X1 = ffl_scale(ffl_dot<2, false>({TW, ffl_neg(Wv)}, {rP, rSP}, ffl{}), sx1);
+    const ffl wx = shfl(X1, 9), wy = shfl(X1, 10), wz = shfl(X1, 11);
+    const ffl x20 = shfl(X2, 9), x21 = shfl(X2, 10), x22 = shfl(X2, 11);
     xl = lane < 3 ? pick3(lane, wx, wy, wz) : pick3(lane - 3, x20, x21, x22);
     // the pose update: this lane's column (of R, or t) and row
-    const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
-    double A, B;
-    rodrigues_coeffs(th2, lane, A, B);
-    const double k0 = vec ? t_old[0] : R_old[c], k1 = vec ? t_old[1] : R_old[3 + c], k2 = vec ? t_old[2] : R_old[6 + c];
+    const ffl th2 = ffl_dot<3, false>({wx, wy, wz}, {wx, wy, wz}, ffl{});
+    const ffl k0 = vec ? t_old[0] : R_old[c], k1 = vec ? t_old[1] : R_old[3 + c], k2 = vec ? t_old[2] : R_old[6 + c];
     // (w x k)[row] = w[row+1] k[row+2] - w[row+2] k[row+1]
     const int ra = row == 2 ? 0 : row + 1, rb = row == 0 ? 2 : row - 1;
-    const double cr = fma(pick3(ra, wx, wy, wz), pick3(rb, k0, k1, k2), -(pick3(rb, wx, wy, wz) * pick3(ra, k0, k1, k2)));
-    const double dt = fma(wx, k0, fma(wy, k1, wz * k2));
-    const double kr = pick3(row, k0, k1, k2);
-    const double M = fma(pick3(row, wx, wy, wz), dt, -(th2 * kr));
-    double o = fma(A, cr, fma(B, M, kr));
-    if (vec) o += pick3(vi, x20, x21, x22);
+    const ffl cr = ffl_dot<2, false>({pick3(ra, wx, wy, wz), ffl_neg(pick3(rb, wx, wy, wz))},
+                                     {pick3(rb, k0, k1, k2), pick3(ra, k0, k1, k2)}, ffl{});
+    const ffl dt = ffl_dot<3, false>({wx, wy, wz}, {k0, k1, k2}, ffl{});
+    const ffl kr = pick3(row, k0, k1, k2);
+    const ffl M = ffl_dot<2, false>({pick3(row, wx, wy, wz), ffl_neg(th2)}, {dt, kr}, ffl{});
+    const ffl base = vec ? ffl_add(kr, pick3(vi, x20, x21, x22)) : kr;
+    ffl A, B;
+    rodrigues_coeffs_ff(th2, lane, A, B);
+    const ffl o = ffl_dot<2, true>({A, B}, {cr, M}, base);
     out = ok ? o : kr;
     return ok;
 }
