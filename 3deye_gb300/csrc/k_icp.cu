@@ -2,17 +2,16 @@
 //
 // One launch per ICP iteration: every thread associates a few pixels and
 // accumulates the 27 upper-triangular terms of [J^T J | J^T r] (+ an inlier
-// count); a warp transpose-reduction with TwoSum pairs and a block pass give
-// each block's totals as float-float values; each block adds them, converted
-// exactly to 126-bit fixed point, into integer accumulators with atomics --
-// integer addition is associative, so the grid total is the same bits in any
-// block order.
+// count); a warp transpose-reduction and a block pass give each block's
+// totals in float, in a fixed order; each block adds them, converted exactly
+// to 126-bit fixed point, into integer accumulators with atomics -- integer
+// addition is associative, so the grid total is the same bits in any block
+// order.
 //
 // Pipeline form: launch i's blocks, once the programmatic dependency on
 // launch i - 1 has resolved (its atomics complete and visible), read its
-// exact totals and solve the 6x6 system themselves (float-float arithmetic,
-// tde_solve.cuh) -- every block the
-// same operations on the same bits, so the same pose -- instead of a last
+// exact totals and solve the 6x6 system themselves (tde_solve.cuh) -- every
+// block the same operations on the same bits, so the same pose -- instead of a last
 // block of launch i - 1 solving after a grid-wide ticket.  That takes the
 // ticket, its fence and one dependent read off every iteration; only the
 // frame's last launch keeps the ticket, to solve its own totals.
@@ -29,29 +28,9 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kPixPerThread = 4;
-constexpr int kPixWide = 8;                    // pixels a thread on large levels
+constexpr int kPixWide = 4;                    // pixels a thread on large levels
+constexpr int kWideThreads = 512;              // threads a block on large levels
 constexpr int kPixWideMinPixels = 1 << 18;     // "large": 640x480, not 320x240
-
-struct f2 { float hi, lo; };
-
-// Knuth TwoSum: hi + lo == a + b exactly.
-__device__ __forceinline__ f2 two_sum(float a, float b) {
-    float s = a + b;
-    float bp = s - a;
-    float ap = s - bp;
-    float e = (a - ap) + (b - bp);
-    return f2{s, e};
-}
-__device__ __forceinline__ f2 add_ff(f2 a, f2 b) {
-    f2 s = two_sum(a.hi, b.hi);
-    float lo = s.lo + (a.lo + b.lo);
-    return two_sum(s.hi, lo);
-}
-__device__ __forceinline__ f2 add_f(f2 a, float b) {
-    f2 s = two_sum(a.hi, b);
-    s.lo = s.lo + a.lo;
-    return two_sum(s.hi, s.lo);
-}
 
 // The association's float operations, written as explicit fused
 // multiply-adds (one rounding each, as C's fmaf in the CPU oracle); the unit
@@ -181,17 +160,22 @@ __device__ __forceinline__ ffl from_fixed_ff(unsigned long long a0, unsigned lon
 
 // Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
 // five butterfly stages, each halving the values a lane keeps, leave lane l
-// with the warp total of term l as a float-float pair (31 compensated adds
-// and 62 shuffles instead of 32 x 5 of each).
-__device__ __forceinline__ f2 warp_transpose_reduce(const float (&s)[32], int lane) {
-    f2 v[16];
+// with the warp total of term l (31 additions and 31 shuffles instead of
+// 32 x 5 of each), in a fixed order: float sums like the reference's
+// transform_estimation.cl.  Compensated (TwoSum) additions here measured
+// 0.55-0.84 us of a 640x480 iteration's 3.3 us association at 16 warps per
+// SM (about 440 instructions a thread against 125), for sums already
+// rounded per thread; the rounding they add averages to ~1e-8 of a frame's
+// totals.
+__device__ __forceinline__ float warp_transpose_reduce(const float (&s)[32], int lane) {
+    float v[16];
     {
         const bool up = lane & 16;
         #pragma unroll
         for (int i = 0; i < 16; ++i) {
             const float send = up ? s[i] : s[i + 16];
             const float keep = up ? s[i + 16] : s[i];
-            v[i] = two_sum(keep, __shfl_xor_sync(0xffffffffu, send, 16));
+            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, 16));
         }
     }
     #pragma unroll
@@ -199,10 +183,9 @@ __device__ __forceinline__ f2 warp_transpose_reduce(const float (&s)[32], int la
         const bool up = lane & o;
         #pragma unroll
         for (int i = 0; i < o; ++i) {
-            const f2 send = up ? v[i] : v[i + o];
-            const f2 keep = up ? v[i + o] : v[i];
-            const f2 recv{__shfl_xor_sync(0xffffffffu, send.hi, o), __shfl_xor_sync(0xffffffffu, send.lo, o)};
-            v[i] = add_ff(keep, recv);
+            const float send = up ? v[i] : v[i + o];
+            const float keep = up ? v[i + o] : v[i];
+            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, o));
         }
     }
     return v[0];
@@ -210,9 +193,9 @@ __device__ __forceinline__ f2 warp_transpose_reduce(const float (&s)[32], int la
 
 // Association, the per-block sums, and their exact addition into
 // accumulator buffer `acc` (copy blockIdx % kIcpAccCopies).
-template <int PIX>
+template <int PIX, int THREADS>
 __device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose &P, const float3 (&nc)[PIX],
-                                                 const float3 (&vc)[PIX], f2 (*red)[32],
+                                                 const float3 (&vc)[PIX], float (*red)[32],
                                                  unsigned long long (*acc)[kIcpAccCopies][kIcpTerms][3]) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float s[32];
@@ -237,14 +220,13 @@ __device__ __forceinline__ void accumulate_block(const IcpArgs &a, const IcpPose
             s[27] = s[27] + 1.f;
         }
     }
-    const f2 wsum = warp_transpose_reduce(s, lane);
-    red[warp][lane] = wsum;
+    red[warp][lane] = warp_transpose_reduce(s, lane);
     __syncthreads();
     if (tid < kIcpTerms) {
-        f2 v = red[0][tid];
+        float v = red[0][tid];
         #pragma unroll
-        for (int w = 1; w < kThreads / 32; ++w) v = add_ff(v, red[w][tid]);
-        const unsigned __int128 q = (unsigned __int128)(to_fixed(v.hi) + to_fixed(v.lo));
+        for (int w = 1; w < THREADS / 32; ++w) v = __fadd_rn(v, red[w][tid]);
+        const unsigned __int128 q = (unsigned __int128)to_fixed(v);
         const unsigned long long m42 = (1ull << 42) - 1ull;
         unsigned long long *dst = (*acc)[blockIdx.x % kIcpAccCopies][tid];
         atomicAdd(dst + 0, (unsigned long long)q & m42);
@@ -295,14 +277,14 @@ __device__ __forceinline__ bool last_block(IcpState *st, unsigned *ticket) {
 }
 
 // Loads this thread's current-frame maps (independent of the pose).
-template <int PIX>
+template <int PIX, int THREADS>
 __device__ __forceinline__ void load_current(const IcpArgs &a, float3 (&nc)[PIX], float3 (&vc)[PIX]) {
     const int npix = a.W * a.H;
-    const int base = blockIdx.x * kThreads * PIX + threadIdx.x;
+    const int base = blockIdx.x * THREADS * PIX + threadIdx.x;
     const float qnan = __int_as_float(0x7fffffff);
     #pragma unroll
     for (int k = 0; k < PIX; ++k) {
-        const int p = base + k * kThreads;
+        const int p = base + k * THREADS;
         if (p < npix) { nc[k] = ld3(a.ncur, (size_t)p); vc[k] = ld3(a.vcur, (size_t)p); }
         else { nc[k] = make_float3(qnan, qnan, qnan); vc[k] = nc[k]; }
     }
@@ -314,15 +296,15 @@ __device__ __forceinline__ void load_current(const IcpArgs &a, float3 (&nc)[PIX]
 __global__ void __launch_bounds__(kThreads) icp_sums_kernel(const IcpArgs a, IcpState *__restrict__ st,
                                                             float *__restrict__ mbuf) {
     __shared__ IcpPose P;
-    __shared__ f2 red[kThreads / 32][32];
+    __shared__ float red[kThreads / 32][32];
     __shared__ unsigned ticket;
     const int tid = threadIdx.x;
     float3 nc[kPixPerThread], vc[kPixPerThread];
-    load_current(a, nc, vc);
+    load_current<kPixPerThread, kThreads>(a, nc, vc);
     if (tid < (int)(sizeof(IcpPose) / sizeof(float)))
         reinterpret_cast<float *>(&P)[tid] = reinterpret_cast<const float *>(&st->pose)[tid];
     __syncthreads();
-    accumulate_block(a, P, nc, vc, red, &st->acc[0]);
+    accumulate_block<kPixPerThread, kThreads>(a, P, nc, vc, red, &st->acc[0]);
     if (!last_block(st, &ticket)) return;
     if (tid < kIcpTerms) {
         long long whole;
@@ -339,11 +321,11 @@ __global__ void __launch_bounds__(kThreads) icp_sums_kernel(const IcpArgs a, Icp
 }
 
 // Pipeline form, launch `iter` of the frame (see the file comment).
-template <int PIX, bool LAST>
-__global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, IcpState *__restrict__ st, int iter,
-                                                            const IcpPublish pub) {
+template <int PIX, int THREADS, bool LAST>
+__global__ void __launch_bounds__(THREADS) icp_step_kernel(const IcpArgs a, IcpState *__restrict__ st, int iter,
+                                                           const IcpPublish pub) {
     __shared__ IcpPose P;
-    __shared__ f2 red[kThreads / 32][32];
+    __shared__ float red[THREADS / 32][32];
     __shared__ ffl Rs[9], ts[3];  // this launch's pose (float-float)
     __shared__ unsigned ticket;
     const int tid = threadIdx.x;
@@ -352,7 +334,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     // pose slot only after its own griddepcontrol.wait.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     float3 nc[PIX], vc[PIX];
-    load_current<PIX>(a, nc, vc);
+    load_current<PIX, THREADS>(a, nc, vc);
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     // ---- the pose this launch associates with ----
@@ -413,9 +395,11 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
                 if (lane == 0) { st->status = 0; st->iterations = 0; }
             }
             if (iter > 0 && lane == 0) {
+                // stores only: a read-modify-write here would put an L2
+                // round trip before this block's association
                 st->inliers = inliers;
                 if (!ok) st->status |= kIcpStatusSolveFailed;
-                st->iterations += 1;
+                st->iterations = iter;
             }
         }
     } else if (iter > 0 && warp == 1 && lane < 12) {
@@ -426,13 +410,15 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     }
     if (blockIdx.x == 0) {
         // the buffer launch iter + 1 adds into; launch iter - 1 read its
-        // previous contents, and it has completed
+        // previous contents, and it has completed (zeroing it from every
+        // block, a few words each, measured slower: the stores of 150 blocks
+        // meet on the same few lines)
         unsigned long long *z = &st->acc[(iter + 1) % kIcpAccBuffers][0][0][0];
-        for (int i = tid; i < kIcpAccCopies * kIcpTerms * 3; i += kThreads) z[i] = 0ull;
+        for (int i = tid; i < kIcpAccCopies * kIcpTerms * 3; i += THREADS) z[i] = 0ull;
     }
     __syncthreads();
 
-    accumulate_block(a, P, nc, vc, red, &st->acc[iter % kIcpAccBuffers]);
+    accumulate_block<PIX, THREADS>(a, P, nc, vc, red, &st->acc[iter % kIcpAccBuffers]);
     if (!LAST) return;
 
     // ---- the frame's last launch: its last block solves its own totals ----
@@ -445,7 +431,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
     // so that the next frame's first launch adds into zeros
     {
         unsigned long long *z = &st->acc[0][0][0][0];
-        for (int i = tid; i < kIcpAccBuffers * kIcpAccCopies * kIcpTerms * 3; i += kThreads) z[i] = 0ull;
+        for (int i = tid; i < kIcpAccBuffers * kIcpAccCopies * kIcpTerms * 3; i += THREADS) z[i] = 0ull;
     }
     if (warp != 0) return;
     const int inliers = __shfl_sync(0xffffffffu, (int)whole, 27);
@@ -472,7 +458,7 @@ __global__ void __launch_bounds__(kThreads) icp_step_kernel(const IcpArgs a, Icp
         st->counter = 0u;
         st->inliers = inliers;
         if (!ok) st->status |= kIcpStatusSolveFailed;
-        st->iterations += 1;
+        st->iterations = iter + 1;
         pub.cam->tracking_ok = !lost;
         *pub.status = lost ? pub.lost_status : 0;
         *pub.inliers = inliers;
@@ -539,17 +525,20 @@ int launch_icp(const IcpArgs &a, IcpState *st, float *mbuf, cudaStream_t stream)
 }
 
 int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const IcpPublish &pub, cudaStream_t stream) {
-    // Large levels take kPixWide pixels a thread: half the blocks, one per
-    // SM, which leaves room to the next frame's preprocessing running beside
-    // (measured with 640x480 frames: ICP 0.1516 against 0.1531 ms per frame,
-    // 3043 against 3026 frames/s overlapped; eight pixels a thread on the
-    // coarse levels too gave 3094 frames/s but 0.162 ms and a slower
-    // end-to-end line, 3007 against 3053)
+    // Large levels take blocks of kWideThreads threads with kPixWide pixels
+    // each: 150 blocks at 640x480, one per SM, which leaves room to the next
+    // frame's preprocessing running beside.  Measured with 640x480 frames
+    // (ICP per frame, frames/s overlapped): 256 threads x 4 pixels (300
+    // blocks) 0.1531 ms, 3026; 256 x 8 0.1516 ms, 3043 (0.1489 ms, 3095 after
+    // the float-float solve); 512 x 4 0.1452 ms, 3147 -- the same pixels per
+    // SM with twice the warps to cover the gather and reduction latencies.
+    // Eight pixels a thread on the coarse levels too gave 3094 frames/s but
+    // 0.162 ms and a slower end-to-end line (3007 against 3053).
     const bool wide = a.W * a.H >= kPixWideMinPixels;
-    const unsigned nb = div_up((unsigned)(a.W * a.H), (unsigned)(kThreads * (wide ? kPixWide : kPixPerThread)));
+    const unsigned nb = div_up((unsigned)(a.W * a.H), wide ? (unsigned)(kWideThreads * kPixWide) : (unsigned)(kThreads * kPixPerThread));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(wide ? kWideThreads : kThreads);
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -558,11 +547,11 @@ int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const I
     cfg.numAttrs = 1;
     cudaError_t e;
     if (wide)
-        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, true>, a, st, iter, pub)
-                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, false>, a, st, iter, pub);
+        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, kWideThreads, true>, a, st, iter, pub)
+                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, kWideThreads, false>, a, st, iter, pub);
     else
-        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, true>, a, st, iter, pub)
-                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, false>, a, st, iter, pub);
+        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, kThreads, true>, a, st, iter, pub)
+                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, kThreads, false>, a, st, iter, pub);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "icp_step: %s", cudaGetErrorString(e));
     return check_launch("icp_step");
 }

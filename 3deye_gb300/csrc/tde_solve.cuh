@@ -20,15 +20,15 @@ __host__ __device__ __forceinline__ int term_index(int r, int c) {
 // GB300 executes FP64 at a small fraction of the FP32 rate: an FP64 warp
 // instruction occupies a sub-partition's FP64 pipe for ~64 cycles and a
 // dependent one waits longer still (measured), so a solve written in FP64 is
-// a chain of slow steps (3.0 us per Gauss-Newton step).  Here a value is
-// hi + lo in two floats with |lo| <= ulp(hi) / 2: 48 significant bits.
-// Products are split exactly with one fused multiply-add (Dekker's product,
-// FMA form), high parts are added exactly with Knuth's TwoSum, and the
-// low-order parts are added in float in a fixed order, as in the
-// double-double algorithms of Hida, Li and Bailey (2001) with float parts.
-// The solve's chain of 2x2 determinants and 3-term dot products then runs on
-// 4-cycle float operations at about 2^-46 relative precision (against 2^-53
-// for FP64): far below the rounding of the float association terms it solves.
+// a chain of slow steps.  Here a value is hi + lo in two floats with
+// |lo| <= ulp(hi) / 2: 48 significant bits.  Products are split exactly with
+// one fused multiply-add (Dekker's product, FMA form), high parts are added
+// exactly with Knuth's TwoSum, and the low-order parts are added in float in
+// a fixed order, as in the double-double algorithms of Hida, Li and Bailey
+// (2001) with float parts: about 2^-46 relative precision (against 2^-53 for
+// FP64), far below the rounding of the float association terms the solve
+// takes.  The solve below uses it only where precision is made: the residual
+// of iterative refinement and the pose update.
 // ---------------------------------------------------------------------------
 struct ffl {
     float hi, lo;
@@ -50,6 +50,10 @@ __device__ __forceinline__ ffl ffl_mul(ffl a, ffl b) {
     const float e = __fmaf_rn(a.hi, b.hi, -p);  // p + e = a.hi b.hi exactly
     const float x = __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi));
     return ffl_fast_two_sum(p, __fadd_rn(e, x));
+}
+__device__ __forceinline__ ffl ffl_add_f(ffl a, float b) {
+    const ffl s = ffl_two_sum(a.hi, b);
+    return ffl_fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
 }
 __device__ __forceinline__ ffl ffl_add(ffl a, ffl b) {
     const ffl s = ffl_two_sum(a.hi, b.hi), t = ffl_two_sum(a.lo, b.lo);
@@ -156,20 +160,30 @@ __device__ __forceinline__ void rodrigues_coeffs_ff(ffl th2, int lane, ffl &A, f
     }
 }
 
+// Refinement steps after the FP32 solve: one leaves a relative error of about
+// (cond(DAD) 2^-24)^2 (2.5e-13 of max |x| on the device solve's test systems,
+// in a float-float emulation), two reach the float-float precision (2.2e-14)
+// and cost 0.2 us more per Gauss-Newton step (ICP at 640x480: 0.1361 against
+// 0.1404 ms per frame).
+constexpr int kSolveRefinements = 1;
+
 // One Gauss-Newton step, executed by all 32 lanes of a warp: lanes share every
 // instruction (one matrix or vector entry each, operands chosen by lane) and
 // exchange values by shuffles.  Lane l < 27 holds term l of [A | b] (term 27,
 // the inlier count, is not used).  [A | b] is first scaled by powers of two
 // (D A D y = D b, x = D y; D = diag(2^k) with every diagonal entry of D A D in
 // [1, 4): exact, and the adjugate products below stay far inside the float
-// range).  With A = [[P, Q], [Q^T, R]] and adjugates (no division until the
-// end):
+// range).  The scaled system is factored and solved in FP32 -- with
+// A = [[P, Q], [Q^T, R]] and adjugates, no division until the end:
 //   S' = det(P) R - Q^T adj(P) Q   (= det(P) S, S the Schur complement),
 //   u' = det(P) b2 - Q^T adj(P) b1,   U = adj(S') u',   W = (Q^T adj(P))^T U,
-//   x2 = U / det(S'),   x1 = adj(P) b1 / det(P) - W / (det(P) det(S')),
-// so both inverses come from one reciprocal of det(P) det(S') and only three
-// multiplications follow it.  The pose (R_old, t_old: shared memory) moves by
-// exp([x1]x), x2:
+//   y2 = U / det(S'),   y1 = adj(P) b1 / det(P) - W / (det(P) det(S')),
+// both inverses from one reciprocal of det(P) det(S') -- and then refined,
+// y <- y + A^-1 (b - A y), the residual formed in float-float from the exact
+// float-float sums and the correction solved with the FP32 factors
+// (mixed-precision iterative refinement: each step multiplies the error by
+// about cond(DAD) 2^-24).  The pose (R_old, t_old: shared memory) moves by
+// exp([x1]x), x2 in float-float:
 //   R <- R + A (w x R) + B (w (w . R) - th2 R)   column by column, and
 //   t <- t + A (w x t) + B (w (w . t) - th2 t) + x2,   w = x1.
 // Lane l < 9 returns entry l of the new R (row-major) in `out`, lanes 9..11
@@ -178,6 +192,7 @@ __device__ __forceinline__ void rodrigues_coeffs_ff(ffl th2, int lane, ffl &A, f
 // scaled P or S at or below 2^-100 of its reference (integer tests on the
 // exponent bits), or a determinant product outside the normal float range.
 __device__ bool warp_solve_step(ffl term, const ffl *R_old, const ffl *t_old, int lane, ffl &out, ffl &xl) {
+    const unsigned full = 0xffffffffu;
     const bool vec = lane >= 9;                       // lanes 9..11: vector entries
     const int vi = (lane >= 9 && lane < 12) ? lane - 9 : 0;
     const int l9 = lane < 9 ? lane : 0;
@@ -189,59 +204,108 @@ __device__ bool warp_solve_step(ffl term, const ffl *R_old, const ffl *t_old, in
         const int i = (lane >= 7) + (lane >= 13) + (lane >= 18) + (lane >= 22) + (lane >= 25);
         const int j = lane - term_index(i, i) + i;
         const int jd = j < 6 ? j : 0;
-        const float si = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(i, i)));
-        const float sj = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(jd, jd)));
-        sx1 = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(vi, vi)));
-        sx2 = diag_scale(__shfl_sync(0xffffffffu, term.hi, term_index(3 + vi, 3 + vi)));
+        const float si = diag_scale(__shfl_sync(full, term.hi, term_index(i, i)));
+        const float sj = diag_scale(__shfl_sync(full, term.hi, term_index(jd, jd)));
+        sx1 = diag_scale(__shfl_sync(full, term.hi, term_index(vi, vi)));
+        sx2 = diag_scale(__shfl_sync(full, term.hi, term_index(3 + vi, 3 + vi)));
         if (lane < 27) term = ffl_scale(ffl_scale(term, si), j < 6 ? sj : 1.f);
     }
+    const float th = term.hi;
+    auto T = [&](int src) { return __shfl_sync(full, th, src); };
+    // ---- FP32 factors and first solution ----
     // adj(P): cofactors (lane r, c), det(P) through the first row
-    const ffl CP = ffl_dot<2, false>({shfl(term, term_index(r1, c1)), ffl_neg(shfl(term, term_index(r1, c2)))},
-                                     {shfl(term, term_index(r2, c2)), shfl(term, term_index(r2, c1))}, ffl{});
-    const ffl P0 = shfl(term, 0);
-    const ffl detP = ffl_dot<3, false>({P0, shfl(term, 1), shfl(term, 2)}, {shfl(CP, 0), shfl(CP, 1), shfl(CP, 2)}, ffl{});
-    const ffl CP8 = shfl(CP, 8);  // P00 P11 - P01^2
-    bool ok = clearly_pos_f(P0.hi, 127) && clearly_pos_f(CP8.hi, fexp(P0.hi)) && clearly_pos_f(detP.hi, fexp(CP8.hi));
+    const float CP = __fmaf_rn(T(term_index(r1, c1)), T(term_index(r2, c2)),
+                               -__fmul_rn(T(term_index(r1, c2)), T(term_index(r2, c1))));
+    auto CPs = [&](int src) { return __shfl_sync(full, CP, src); };
+    const float P0 = T(0);
+    const float detP = __fmaf_rn(P0, CPs(0), __fmaf_rn(T(1), CPs(1), __fmul_rn(T(2), CPs(2))));
+    const float CP8 = CPs(8);  // P00 P11 - P01^2
+    bool ok = clearly_pos_f(P0, 127) && clearly_pos_f(CP8, fexp(P0)) && clearly_pos_f(detP, fexp(CP8));
+    // the factors' entries a vector lane (9 + vi) needs for a right-hand side
+    float cpv[3], twr[3], csr[3], twc[3];
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) cpv[k] = CPs(3 * k + vi);
     // T' = Q^T adj(P) (lane r, c); v = adj(P) b1 (lane 9 + i)
-    const int col = vec ? vi : c;
-    const ffl TW = ffl_dot<3, false>(
-        {shfl(term, vec ? term_index(0, 6) : term_index(0, 3 + r)), shfl(term, vec ? term_index(1, 6) : term_index(1, 3 + r)),
-         shfl(term, vec ? term_index(2, 6) : term_index(2, 3 + r))},
-        {shfl(CP, col), shfl(CP, 3 + col), shfl(CP, 6 + col)}, ffl{});
+    float TW;
+    {
+        const int col = vec ? vi : c;
+        const float a0 = T(vec ? term_index(0, 6) : term_index(0, 3 + r));
+        const float a1 = T(vec ? term_index(1, 6) : term_index(1, 3 + r));
+        const float a2 = T(vec ? term_index(2, 6) : term_index(2, 3 + r));
+        TW = __fmaf_rn(a0, CPs(col), __fmaf_rn(a1, CPs(3 + col), __fmul_rn(a2, CPs(6 + col))));
+    }
+    auto TWs = [&](int src) { return __shfl_sync(full, TW, src); };
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) { twr[k] = TWs(3 * vi + k); twc[k] = TWs(3 * k + vi); }
     // S' = det(P) R - T' Q (lane r, c); u' = det(P) b2 - T' b1 (lane 9 + i)
-    const int row = vec ? vi : r;
-    const ffl SU = ffl_dot<4, false>(
-        {detP, ffl_neg(shfl(TW, 3 * row)), ffl_neg(shfl(TW, 3 * row + 1)), ffl_neg(shfl(TW, 3 * row + 2))},
-        {shfl(term, vec ? term_index(3 + vi, 6) : term_index(3 + r, 3 + c)), shfl(term, vec ? term_index(0, 6) : term_index(0, 3 + c)),
-         shfl(term, vec ? term_index(1, 6) : term_index(1, 3 + c)), shfl(term, vec ? term_index(2, 6) : term_index(2, 3 + c))},
-        ffl{});
+    float SU;
+    {
+        const int row = vec ? vi : r;
+        const float base = __fmul_rn(detP, T(vec ? term_index(3 + vi, 6) : term_index(3 + r, 3 + c)));
+        SU = __fmaf_rn(-TWs(3 * row), T(vec ? term_index(0, 6) : term_index(0, 3 + c)),
+                       __fmaf_rn(-TWs(3 * row + 1), T(vec ? term_index(1, 6) : term_index(1, 3 + c)),
+                                 __fmaf_rn(-TWs(3 * row + 2), T(vec ? term_index(2, 6) : term_index(2, 3 + c)), base)));
+    }
+    auto SUs = [&](int src) { return __shfl_sync(full, SU, src); };
     // adj(S'), det(S'); U = adj(S') u' (lane 9 + i); the tests of S = S' / det(P)
-    const ffl CS = ffl_dot<2, false>({shfl(SU, 3 * r1 + c1), ffl_neg(shfl(SU, 3 * r1 + c2))},
-                                     {shfl(SU, 3 * r2 + c2), shfl(SU, 3 * r2 + c1)}, ffl{});
-    const ffl S0 = shfl(SU, 0);
-    const ffl detS = ffl_dot<3, false>({S0, shfl(SU, 1), shfl(SU, 2)}, {shfl(CS, 0), shfl(CS, 1), shfl(CS, 2)}, ffl{});
-    const ffl U = ffl_dot<3, false>({shfl(CS, 3 * vi), shfl(CS, 3 * vi + 1), shfl(CS, 3 * vi + 2)},
-                                    {shfl(SU, 9), shfl(SU, 10), shfl(SU, 11)}, ffl{});
-    // W = T'^T U (lane 9 + i), so that x1 = v / det(P) - W / (det(P) det(S'))
-    const ffl Wv = ffl_dot<3, false>({shfl(TW, vi), shfl(TW, 3 + vi), shfl(TW, 6 + vi)}, {shfl(U, 9), shfl(U, 10), shfl(U, 11)},
-                                     ffl{});
-    const ffl CS8 = shfl(CS, 8);
-    const int eP = fexp(detP.hi) - 127;
-    ok = ok && clearly_pos_f(S0.hi, 127 + eP) && clearly_pos_f(CS8.hi, fexp(S0.hi) + eP) &&
-         clearly_pos_f(detS.hi, fexp(CS8.hi) + eP);
-    // both inverses from one reciprocal (of a normal product)
-    const ffl dPS = ffl_mul(detP, detS);
-    ok = ok && fexp(dPS.hi) > 0 && fexp(dPS.hi) < 255;
-    const ffl rPS = ffl_rcp(dPS);
-    const ffl rS = ffl_mul(detP, rPS), rP = ffl_mul(detS, rPS);
-    const ffl rSP = ffl_mul(rS, rP);
-    // x2 = U / det(S'), x1 = v / det(P) - W / (det(P) det(S')) (lane 9 + i), then unscaled
-    const ffl X2 = ffl_scale(ffl_mul(U, rS), sx2);
-    const ffl X1 = ffl_scale(ffl_dot<2, false>({TW, ffl_neg(Wv)}, {rP, rSP}, ffl{}), sx1);
+    const float CS = __fmaf_rn(SUs(3 * r1 + c1), SUs(3 * r2 + c2), -__fmul_rn(SUs(3 * r1 + c2), SUs(3 * r2 + c1)));
+    auto CSs = [&](int src) { return __shfl_sync(full, CS, src); };
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) csr[k] = CSs(3 * vi + k);
+    const float S0 = SUs(0);
+    const float detS = __fmaf_rn(S0, CSs(0), __fmaf_rn(SUs(1), CSs(1), __fmul_rn(SUs(2), CSs(2))));
+    const float CS8 = CSs(8);
+    const int eP = fexp(detP) - 127;
+    ok = ok && clearly_pos_f(S0, 127 + eP) && clearly_pos_f(CS8, fexp(S0) + eP) && clearly_pos_f(detS, fexp(CS8) + eP);
+    // both inverses from one reciprocal (of a normal product), one Newton step
+    const float dPS = __fmul_rn(detP, detS);
+    ok = ok && fexp(dPS) > 0 && fexp(dPS) < 255;
+    float rPS;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rPS) : "f"(dPS));
+    rPS = __fmaf_rn(rPS, __fmaf_rn(-dPS, rPS, 1.f), rPS);
+    const float rS = __fmul_rn(detP, rPS), rP = __fmul_rn(detS, rPS), rSP = __fmul_rn(rS, rP);
+    // y for a right-hand side: v = adj(P) h1 and u' (lane 9 + i) in, y1 and
+    // y2 (lane 9 + i) out
+    auto back = [&](float v, float u, float &y1, float &y2) {
+        const float u0 = __shfl_sync(full, u, 9), u1 = __shfl_sync(full, u, 10), u2 = __shfl_sync(full, u, 11);
+        const float U = __fmaf_rn(csr[0], u0, __fmaf_rn(csr[1], u1, __fmul_rn(csr[2], u2)));
+        const float U0 = __shfl_sync(full, U, 9), U1 = __shfl_sync(full, U, 10), U2 = __shfl_sync(full, U, 11);
+        const float W = __fmaf_rn(twc[0], U0, __fmaf_rn(twc[1], U1, __fmul_rn(twc[2], U2)));
+        y2 = __fmul_rn(U, rS);
+        y1 = __fmaf_rn(-W, rSP, __fmul_rn(v, rP));
+    };
+    float y1f, y2f;
+    back(TW, SU, y1f, y2f);
+    ffl y1{y1f, 0.f}, y2{y2f, 0.f};
+    // ---- refinement: residual b - A y in float-float (lane i < 6 takes row
+    // i), correction from the FP32 factors ----
+    {
+        const int ri = lane < 6 ? lane : 0;
+        ffl Arow[6];
+        #pragma unroll
+        for (int j = 0; j < 6; ++j) Arow[j] = ffl_neg(shfl(term, term_index(ri, j)));
+        const ffl brow = shfl(term, term_index(ri, 6));
+        #pragma unroll
+        for (int step = 0; step < kSolveRefinements; ++step) {
+            const ffl yv[6] = {shfl(y1, 9), shfl(y1, 10), shfl(y1, 11), shfl(y2, 9), shfl(y2, 10), shfl(y2, 11)};
+            const float res = ffl_dot<6, true>(Arow, yv, brow).hi;
+            const float h0 = __shfl_sync(full, res, 0), h1 = __shfl_sync(full, res, 1), h2 = __shfl_sync(full, res, 2);
+            const float hb = __shfl_sync(full, res, 3 + vi);
+            const float v = __fmaf_rn(cpv[0], h0, __fmaf_rn(cpv[1], h1, __fmul_rn(cpv[2], h2)));
+            const float u = __fmaf_rn(-twr[0], h0, __fmaf_rn(-twr[1], h1, __fmaf_rn(-twr[2], h2, __fmul_rn(detP, hb))));
+            float d1, d2;
+            back(v, u, d1, d2);
+            y1 = ffl_add_f(y1, d1);
+            y2 = ffl_add_f(y2, d2);
+        }
+    }
+    // x = D y (lane 9 + i)
+    const ffl X1 = ffl_scale(y1, sx1), X2 = ffl_scale(y2, sx2);
     const ffl wx = shfl(X1, 9), wy = shfl(X1, 10), wz = shfl(X1, 11);
     const ffl x20 = shfl(X2, 9), x21 = shfl(X2, 10), x22 = shfl(X2, 11);
     xl = lane < 3 ? pick3(lane, wx, wy, wz) : pick3(lane - 3, x20, x21, x22);
     // the pose update: this lane's column (of R, or t) and row
+    const int row = vec ? vi : r;
     const ffl th2 = ffl_dot<3, false>({wx, wy, wz}, {wx, wy, wz}, ffl{});
     const ffl k0 = vec ? t_old[0] : R_old[c], k1 = vec ? t_old[1] : R_old[3 + c], k2 = vec ? t_old[2] : R_old[6 + c];
     // (w x k)[row] = w[row+1] k[row+2] - w[row+2] k[row+1]

@@ -277,7 +277,8 @@ def test_estimate_combined_matches_oracle(tde, orc, cuda, small):
                                 cfg.dist_thresh, cfg.angle_thresh))
     ref = sums[:27]
     scale = np.abs(ref).max()
-    # compensated FP32 (TwoSum pairs) vs FP64 sums of the same float terms
+    # float sums in a fixed order (per thread, warp butterfly, block) made
+    # exact across blocks, vs FP64 sums of the same float terms
     np.testing.assert_allclose(m, ref, rtol=1e-6, atol=1e-7 * scale)
 
 
@@ -505,7 +506,7 @@ def test_clean_color_slice_golden(tde, cuda):
 
 
 # ---------------------------------------------------------------------------
-# float-float solve-and-update step (the one every ICP launch and RGB-D step runs)
+# solve-and-update step (the one every ICP launch and RGB-D step runs)
 # ---------------------------------------------------------------------------
 def terms_of(A, b):
     out = []
@@ -516,9 +517,10 @@ def terms_of(A, b):
 
 
 def test_device_icp_solve_matches_fp64_oracle(tde, orc, cuda):
-    """The device solve (float-float arithmetic, power-of-two scaling, 3x3
-    blocks, adjugates, a Newton-refined reciprocal, Taylor / Rodrigues update)
-    against the oracle's FP64 Cholesky solve and
+    """The device solve (power-of-two scaling, FP32 3x3 blocks with
+    adjugates and one reciprocal, a refinement step with the residual in
+    float-float, Taylor / Rodrigues update in float-float) against the
+    oracle's FP64 Cholesky solve and
     exponential, over systems with entries from 1e-3 to 1e7, rotation steps
     from 1e-5 to 0.5 rad (both branches of the exponential), and systems that
     are not positive definite (rejected, pose unchanged)."""
@@ -565,10 +567,9 @@ def test_device_icp_solve_matches_fp64_oracle(tde, orc, cuda):
             continue
         st, R2, t2, x2 = orc.icp_solve(sums[i, :27], pose[i, :9], pose[i, 9:])
         assert st == 0
-        # both solves are backward stable, the device one at ~2^-46 relative
-        # precision: agreement to ~cond(A) x 1e-14 (measured in a float-float
-        # emulation of the device solve on these systems: 5.2e-14 of max|x|,
-        # 1.3e-14 in R, 1.8e-14 in t)
+        # the device solve refines its FP32 solution once: agreement to about
+        # (cond 2^-24)^2 of max|x| (an emulation of the device arithmetic on
+        # these systems: 2.5e-13 of max|x|, 1.3e-14 in R, 2.3e-14 in t)
         np.testing.assert_allclose(got_x[i], x2, rtol=1e-10, atol=1e-12 * np.abs(x2).max())
         np.testing.assert_allclose(got_pose[i, :9], R2.ravel(), rtol=0, atol=1e-12)
         np.testing.assert_allclose(got_pose[i, 9:], t2, rtol=0, atol=1e-11)
