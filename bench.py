@@ -855,7 +855,7 @@ def run_ours(args, ws, rank, local):
                      "frac": round(icp_achieved / hbm, 4), "traffic": icp_traffic,
                      "alg_bytes_per_launch": int(icp_bytes / icp_launches), "avg_launch_ms": round(icp_launch_ms, 5),
                      "launches_per_frame": icp_launches,
-                     "note": "maps are L2-resident; the iteration is latency-bound (reduction tail + FP64 solve)"},
+                     "note": "maps are L2-resident; the iteration is latency-bound (grid hand-off, totals read, 6x6 solve, association and reduction)"},
         "kernels": {
             "integrate_bricks_kernel<fp16>": {
                 "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
