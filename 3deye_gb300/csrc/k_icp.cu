@@ -26,8 +26,10 @@
 namespace tde {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;                  // the one-shot sums
 constexpr int kPixPerThread = 4;
+constexpr int kPixCoarse = 4;                  // pixels a thread on the coarse levels
+constexpr int kCoarseThreads = 256;            // threads a block on the coarse levels
 constexpr int kPixWide = 4;                    // pixels a thread on large levels
 constexpr int kWideThreads = 512;              // threads a block on large levels
 constexpr int kPixWideMinPixels = 1 << 18;     // "large": 640x480, not 320x240
@@ -156,39 +158,6 @@ __device__ __forceinline__ ffl from_fixed_ff(unsigned long long a0, unsigned lon
     const float lo = __fmul_rn(__uint2float_rn((unsigned)(top >> 8)), __uint_as_float((unsigned)(135 - lz) << 23));
     const ffl r = ffl_fast_two_sum(hi, lo);  // lo < ulp(hi)
     return neg ? ffl_neg(r) : r;
-}
-
-// Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
-// five butterfly stages, each halving the values a lane keeps, leave lane l
-// with the warp total of term l (31 additions and 31 shuffles instead of
-// 32 x 5 of each), in a fixed order: float sums like the reference's
-// transform_estimation.cl.  Compensated (TwoSum) additions here measured
-// 0.55-0.84 us of a 640x480 iteration's 3.3 us association at 16 warps per
-// SM (about 440 instructions a thread against 125), for sums already
-// rounded per thread; the rounding they add averages to ~1e-8 of a frame's
-// totals.
-__device__ __forceinline__ float warp_transpose_reduce(const float (&s)[32], int lane) {
-    float v[16];
-    {
-        const bool up = lane & 16;
-        #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const float send = up ? s[i] : s[i + 16];
-            const float keep = up ? s[i + 16] : s[i];
-            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, 16));
-        }
-    }
-    #pragma unroll
-    for (int o = 8; o >= 1; o >>= 1) {
-        const bool up = lane & o;
-        #pragma unroll
-        for (int i = 0; i < o; ++i) {
-            const float send = up ? v[i] : v[i + o];
-            const float keep = up ? v[i + o] : v[i];
-            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, o));
-        }
-    }
-    return v[0];
 }
 
 // Association, the per-block sums, and their exact addition into
@@ -533,12 +502,17 @@ int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const I
     // the float-float solve); 512 x 4 0.1452 ms, 3147 -- the same pixels per
     // SM with twice the warps to cover the gather and reduction latencies.
     // Eight pixels a thread on the coarse levels too gave 3094 frames/s but
-    // 0.162 ms and a slower end-to-end line (3007 against 3053).
+    // 0.162 ms and a slower end-to-end line (3007 against 3053).  Coarse
+    // levels with 256 x 4 against 512 x 2, 256 x 2 and 512 x 1 (later build,
+    // ICP ms / frames/s / end-to-end frames/s): 0.1206 / 3364 / 3338,
+    // 0.1198 / 3391 / 3330, 0.1165 / 3345 / 3320, 0.1181 / 3363 / 3309 --
+    // a faster serial ICP with more blocks loses to the overlapped
+    // preprocessing they crowd.
     const bool wide = a.W * a.H >= kPixWideMinPixels;
-    const unsigned nb = div_up((unsigned)(a.W * a.H), wide ? (unsigned)(kWideThreads * kPixWide) : (unsigned)(kThreads * kPixPerThread));
+    const unsigned nb = div_up((unsigned)(a.W * a.H), wide ? (unsigned)(kWideThreads * kPixWide) : (unsigned)(kCoarseThreads * kPixCoarse));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
-    cfg.blockDim = dim3(wide ? kWideThreads : kThreads);
+    cfg.blockDim = dim3(wide ? kWideThreads : kCoarseThreads);
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -550,8 +524,8 @@ int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const I
         e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, kWideThreads, true>, a, st, iter, pub)
                  : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixWide, kWideThreads, false>, a, st, iter, pub);
     else
-        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, kThreads, true>, a, st, iter, pub)
-                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixPerThread, kThreads, false>, a, st, iter, pub);
+        e = last ? cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixCoarse, kCoarseThreads, true>, a, st, iter, pub)
+                 : cudaLaunchKernelEx(&cfg, icp_step_kernel<kPixCoarse, kCoarseThreads, false>, a, st, iter, pub);
     if (e != cudaSuccess) return set_error(TDE_ERR_CUDA, "icp_step: %s", cudaGetErrorString(e));
     return check_launch("icp_step");
 }

@@ -10,10 +10,10 @@
 // t' = K t, depth and gradient tests) and sums the squared intensity
 // differences -- integers, so the sum is exact in any order; the second
 // forms sigma from those sums, each kept pair's weighted Jacobian row and the
-// 27 terms of [A | b], reduced per block in FP64 in a fixed order; the last
-// block of that pass sums the blocks, solves in float-float arithmetic and
-// moves the FP64 pose (T <- exp(xi) T, the ICP path's solve).  Every step is two launches: the
-// pose lives on the device, nothing waits on the host.
+// 27 terms of [A | b], reduced per block in float in a fixed order; the last
+// block of that pass sums the blocks in float-float, solves (the ICP path's
+// solve) and moves the FP64 pose (T <- exp(xi) T).  Every step is two
+// launches: the pose lives on the device, nothing waits on the host.
 //
 // Built with -fmad=false: the pair tests and row values are the same IEEE
 // operations as the CPU oracle (oracle/oracle_rgbd.c), explicit fused
@@ -29,10 +29,15 @@ namespace tde {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kPix = 8;  // pixels per thread in the odometry passes (150 blocks at 640x480)
+// The odometry passes: 512 threads x 4 pixels, 150 blocks at 640x480 (one per
+// SM).  Measured per 640x480 frame (graphs): 0.504 ms against 0.579 with
+// 256 x 8 -- the same pixels per SM with twice the warps to cover the
+// gathers' and reductions' latencies.
+constexpr int kOdoThreads = 512;  // threads a block in the odometry passes
+constexpr int kPix = 4;           // pixels per thread in the odometry passes
 constexpr float kSobelScale = 0.125f;  // SOBEL_SCALE, compute_least_squares_equation.cl:8
 
-inline unsigned odo_blocks(int W, int H) { return div_up((unsigned)(W * H), (unsigned)(kThreads * kPix)); }
+inline unsigned odo_blocks(int W, int H) { return div_up((unsigned)(W * H), (unsigned)(kOdoThreads * kPix)); }
 
 __global__ void prepare_kernel(const uint16_t *__restrict__ depth, const uint8_t *__restrict__ rgb, int n,
                                uint8_t *__restrict__ I, float *__restrict__ D) {
@@ -313,7 +318,7 @@ __device__ __forceinline__ void pair_row(const Level &L, const float *M, int u, 
 }
 
 // Pass 1: kept count and sum of squared differences per block.
-__global__ void __launch_bounds__(kThreads) residual_kernel(const Level L, const double *__restrict__ pose,
+__global__ void __launch_bounds__(kOdoThreads) residual_kernel(const Level L, const double *__restrict__ pose,
                                                             unsigned long long *__restrict__ partials) {
     __shared__ float P[12], M[12];
     __shared__ unsigned s_n;
@@ -324,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) residual_kernel(const Level L, const
     int idx[kPix], j[kPix];
     float r[kPix], z[kPix], gx[kPix], gy[kPix];
 #pragma unroll
-    for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kThreads * kPix + k * kThreads + threadIdx.x;
+    for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kOdoThreads * kPix + k * kOdoThreads + threadIdx.x;
     load_depths<kPix>(L, idx, z);
     // this pass is launched after the previous step has completed (a plain
     // launch: the wait returns at once); programmatic serialisation of it
@@ -362,27 +367,30 @@ __global__ void __launch_bounds__(kThreads) residual_kernel(const Level L, const
 }
 
 // Pass 2: sigma from pass 1's blocks (integer sums: exact), the rows of the
-// kept pairs, per-block FP64 partials of the 27 terms and the count.  With
+// kept pairs, per-block float partials of the 27 terms and the count.  With
 // SOLVE the last block to finish (a ticket on *counter, which it resets) sums
-// every block's partials (warp w takes blocks w, w + 8, ..., then the eight
-// warp sums in order), and warp 0 solves and moves the pose in place: the
-// other blocks read the pose only before taking their tickets.  Status: bit 0
-// for a failed solve (too few pairs or A not positive definite; the pose is
-// kept), bit 1 for a solved step.
+// every block's partials in float-float (warp w takes blocks w, w + NW, ...,
+// then the warp sums in order), and warp 0 solves and moves the pose in
+// place: the other blocks read the pose only before taking their tickets.
+// Status: bit 0 for a failed solve (too few pairs or A not positive definite;
+// the pose is kept), bit 1 for a solved step.  Against per-term butterflies
+// with FP64 block and cross-block sums (28 conversions a warp on the FP64
+// pipe), these reductions took the frame from 0.640 to 0.579 ms.
 template <bool SOLVE>
-__global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, double *__restrict__ pose,
-                                                       const unsigned long long *__restrict__ res_partials, int nres,
-                                                       double *__restrict__ partials, float *__restrict__ sigma_out,
-                                                       unsigned *__restrict__ counter, int *__restrict__ status) {
+__global__ void __launch_bounds__(kOdoThreads) lsm_kernel(const Level L, double *__restrict__ pose,
+                                                          const unsigned long long *__restrict__ res_partials, int nres,
+                                                          float *__restrict__ partials, float *__restrict__ sigma_out,
+                                                          unsigned *__restrict__ counter, int *__restrict__ status) {
+    constexpr int NW = kOdoThreads / 32;
     __shared__ float P[12], M[12];
     __shared__ float s_sigma;
-    __shared__ double red[kThreads / 32][28];
+    __shared__ float red[NW][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     int idx[kPix], j[kPix];
     float r[kPix], z[kPix], gx[kPix], gy[kPix];
 #pragma unroll
-    for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kThreads * kPix + k * kThreads + tid;
+    for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kOdoThreads * kPix + k * kOdoThreads + tid;
     load_depths<kPix>(L, idx, z);
     // the first pass's partials and the pose are complete past this point
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -406,9 +414,9 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, double *__
     __syncthreads();
     const float sigma = s_sigma;
     const float ifx = __frcp_rn(L.fx), ify = __frcp_rn(L.fy);
-    float acc[28];
+    float acc[32];  // 27 terms and the count; 4 unused
 #pragma unroll
-    for (int k = 0; k < 28; ++k) acc[k] = 0.f;
+    for (int k = 0; k < 32; ++k) acc[k] = 0.f;
     const unsigned kept = find_pairs<kPix>(L, P, idx, j, r, z, gx, gy);
 #pragma unroll
     for (int k = 0; k < kPix; ++k) {
@@ -425,17 +433,14 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, double *__
             }
         acc[27] += 1.f;
     }
-    // warp sums (fixed butterfly order), then the warps in order in FP64
-#pragma unroll
-    for (int k = 0; k < 28; ++k) {
-        float d = acc[k];
-        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-        if (lane == 0) red[warp][k] = (double)d;
-    }
+    // warp totals (transpose butterfly: lane l holds term l), then the warps
+    // in order: float sums in a fixed order
+    red[warp][lane] = warp_transpose_reduce(acc, lane);
     __syncthreads();
     if (tid < 28) {
-        double s = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) s += red[w][tid];
+        float s = red[0][tid];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) s = __fadd_rn(s, red[w][tid]);
         partials[(size_t)blockIdx.x * 28 + tid] = s;
     }
     if (!SOLVE) return;
@@ -446,38 +451,43 @@ __global__ void __launch_bounds__(kThreads) lsm_kernel(const Level L, double *__
     __syncthreads();
     if (!s_last) return;
     __threadfence();
+    // the blocks' partials in float-float: warp w takes blocks w, w + NW, ...,
+    // then the warp sums in order
+    __shared__ ffl redf[NW][28];
     if (lane < 28) {
-        double v = 0.0;
-        for (int b = warp; b < (int)gridDim.x; b += kThreads / 32) v += __ldcg(partials + (size_t)b * 28 + lane);
-        red[warp][lane] = v;
+        ffl v{0.f, 0.f};
+        for (int b = warp; b < (int)gridDim.x; b += NW) v = ffl_add_f(v, __ldcg(partials + (size_t)b * 28 + lane));
+        redf[warp][lane] = v;
     }
     __syncthreads();
     if (warp != 0) return;
     if (lane == 0) *counter = 0u;
     __shared__ ffl Rs[9], ts[3];
-    double term = 0.0;
-    if (lane < 28)
-        for (int w = 0; w < kThreads / 32; ++w) term += red[w][lane];
+    ffl term{0.f, 0.f};
+    if (lane < 28) {
+        term = redf[0][lane];
+        for (int w = 1; w < NW; ++w) term = ffl_add(term, redf[w][lane]);
+    }
     const double pv = lane < 12 ? pose[lane] : 0.0;
     if (lane < 9) Rs[lane] = ffl_from_double(pv);
     else if (lane < 12) ts[lane - 9] = ffl_from_double(pv);
     __syncwarp();
-    const double count = __shfl_sync(0xffffffffu, term, 27);
+    const float count = __shfl_sync(0xffffffffu, term.hi, 27);  // an integer below 2^24: exact
     ffl o, xl;
-    const bool ok = count >= (double)kIcpMinInliers && warp_solve_step(ffl_from_double(term), Rs, ts, lane, o, xl);
+    const bool ok = count >= (float)kIcpMinInliers && warp_solve_step(term, Rs, ts, lane, o, xl);
     if (lane < 12) pose[lane] = ok ? ffl_to_double(o) : pv;
     if (lane == 0) *status |= ok ? 2 : 1;
 }
 
-// The 28 sums of `nb` partials: warp w takes blocks w, w + 8, ..., then the
-// warp sums in order (the odometry solve's order).
-__global__ void __launch_bounds__(256) sum_partials_kernel(const double *__restrict__ partials, int nb,
+// The 28 sums of `nb` float partials in FP64: warp w takes blocks w, w + 8,
+// ..., then the warp sums in order (the odometry solve's order).
+__global__ void __launch_bounds__(256) sum_partials_kernel(const float *__restrict__ partials, int nb,
                                                            double *__restrict__ out) {
     __shared__ double part[8][28];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane < 28) {
         double s = 0.0;
-        for (int b = warp; b < nb; b += 8) s += partials[(size_t)b * 28 + lane];
+        for (int b = warp; b < nb; b += 8) s += (double)partials[(size_t)b * 28 + lane];
         part[warp][lane] = s;
     }
     __syncthreads();
@@ -537,7 +547,7 @@ template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, cudaStream_t s, Args &&...args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(kOdoThreads);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -700,9 +710,10 @@ int tde_rgbd_lsm(const uint8_t *i_prev, const float *d_prev, const uint8_t *i_cu
     for (int k = 0; k < 12; ++k) P.v[k] = pose12[k];
     set_pose_kernel<<<1, 32, 0, s>>>(P, pose, nullptr, nullptr);
     const Level L = make_level(i_prev, d_prev, i_curr, d_curr, dx, dy, *intr, max_depth_diff, max_depth, min_gradient);
-    residual_kernel<<<nb, kThreads, 0, s>>>(L, pose, res);
-    lsm_kernel<false><<<nb, kThreads, 0, s>>>(L, pose, res, (int)nb, lsm, sigma_device, nullptr, nullptr);
-    sum_partials_kernel<<<1, 256, 0, s>>>(lsm, (int)nb, sums_device);
+    float *lsm_partials = reinterpret_cast<float *>(lsm);  // 28 floats a block in the room of 28 doubles
+    residual_kernel<<<nb, kOdoThreads, 0, s>>>(L, pose, res);
+    lsm_kernel<false><<<nb, kOdoThreads, 0, s>>>(L, pose, res, (int)nb, lsm_partials, sigma_device, nullptr, nullptr);
+    sum_partials_kernel<<<1, 256, 0, s>>>(lsm_partials, (int)nb, sums_device);
     return check_launch("rgbd_lsm");
 }
 
@@ -746,9 +757,9 @@ int tde_rgbd_odometry(const tde_rgbd_frame *prev, const tde_rgbd_frame *curr, co
                                    params->min_gradient[l]);
         const unsigned nb = odo_blocks(in.cols, in.rows);
         for (int it = 0; it < params->iters[l]; ++it) {
-            residual_kernel<<<nb, kThreads, 0, s>>>(L, pose12_device, res);
+            residual_kernel<<<nb, kOdoThreads, 0, s>>>(L, pose12_device, res);
             TDE_CUDA(launch_pdl(lsm_kernel<true>, nb, s, L, pose12_device, (const unsigned long long *)res, (int)nb,
-                                lsm, (float *)nullptr, ticket, status_device),
+                                reinterpret_cast<float *>(lsm), (float *)nullptr, ticket, status_device),
                      "rgbd_odometry");
         }
     }

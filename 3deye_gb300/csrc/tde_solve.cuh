@@ -160,6 +160,39 @@ __device__ __forceinline__ void rodrigues_coeffs_ff(ffl th2, int lane, ffl &A, f
     }
 }
 
+// Warp transpose-reduction: every lane holds 32 per-thread sums (28 used);
+// five butterfly stages, each halving the values a lane keeps, leave lane l
+// with the warp total of term l (31 additions and 31 shuffles instead of
+// 32 x 5 of each), in a fixed order: float sums like the reference's
+// transform_estimation.cl.  Compensated (TwoSum) additions here measured
+// 0.55-0.84 us of a 640x480 ICP iteration's 3.3 us association at 16 warps
+// per SM (about 440 instructions a thread against 125), for sums already
+// rounded per thread; the rounding they add averages to ~1e-8 of a frame's
+// totals.  Used by the ICP association and the RGB-D least-squares pass.
+__device__ __forceinline__ float warp_transpose_reduce(const float (&s)[32], int lane) {
+    float v[16];
+    {
+        const bool up = lane & 16;
+        #pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const float send = up ? s[i] : s[i + 16];
+            const float keep = up ? s[i + 16] : s[i];
+            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, 16));
+        }
+    }
+    #pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) {
+        const bool up = lane & o;
+        #pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const float send = up ? v[i] : v[i + o];
+            const float keep = up ? v[i + o] : v[i];
+            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, o));
+        }
+    }
+    return v[0];
+}
+
 // Refinement steps after the FP32 solve: one leaves a relative error of about
 // (cond(DAD) 2^-24)^2 (2.5e-13 of max |x| on the device solve's test systems,
 // in a float-float emulation), two reach the float-float precision (2.2e-14)
