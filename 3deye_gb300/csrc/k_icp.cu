@@ -507,8 +507,13 @@ int launch_icp_step(const IcpArgs &a, IcpState *st, int iter, bool last, const I
     // ICP ms / frames/s / end-to-end frames/s): 0.1206 / 3364 / 3338,
     // 0.1198 / 3391 / 3330, 0.1165 / 3345 / 3320, 0.1181 / 3363 / 3309 --
     // a faster serial ICP with more blocks loses to the overlapped
-    // preprocessing they crowd.
-    const bool wide = a.W * a.H >= kPixWideMinPixels;
+    // preprocessing they crowd.  With a.narrow (the learned refiner running
+    // beside the tracking) large levels take 256 x 4 too: such a block (24.6k
+    // registers) fits on an SM beside one of the refiner's convolution blocks
+    // (113.7 KB of shared memory, at most 32.5k registers), a 512 x 4 one
+    // (47.6k) does not -- learned line 2553 against 2500 frames/s, while the
+    // plain line prefers 512 x 4 (3381 against 3275).
+    const bool wide = a.W * a.H >= kPixWideMinPixels && !a.narrow;
     const unsigned nb = div_up((unsigned)(a.W * a.H), wide ? (unsigned)(kWideThreads * kPixWide) : (unsigned)(kCoarseThreads * kPixCoarse));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);

@@ -192,6 +192,7 @@ int record_segment(tde_pipeline *p, Segment seg, int set, cudaStream_t s) {
             a.fx = p->intr[l].fx; a.fy = p->intr[l].fy; a.cx = p->intr[l].cx; a.cy = p->intr[l].cy;
             icp_set_thresholds(a, c.dist_thresh, c.angle_thresh);
             a.sm_count = p->sm_count;
+            a.narrow = p->refiner != nullptr;  // blocks that fit beside the refiner's convolutions
             for (int it = 0; it < c.icp_iters[l]; ++it, ++iter)
                 TDE_TRY(launch_icp_step(a, p->st, iter, iter == total - 1, pub, s));
         }

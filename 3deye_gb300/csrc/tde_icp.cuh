@@ -63,11 +63,13 @@ struct IcpArgs {
     // kept when |dv|^2 <= dist2 and |n x n_model|^2 < angle2
     float dist2, angle2;
     int sm_count;  // multiprocessors of the device (spreads the per-block solves)
+    int narrow;    // 1: small blocks on every level (kernels of another stream share the SMs)
 };
 inline void icp_set_thresholds(IcpArgs &a, float dist_thresh, float angle_thresh) {
     a.dist2 = dist_thresh * dist_thresh;
     a.angle2 = angle_thresh * angle_thresh;
     a.sm_count = 1;
+    a.narrow = 0;
 }
 
 // exp of the rotation part x[0..2] (Rodrigues), row-major 3x3.
