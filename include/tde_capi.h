@@ -178,8 +178,10 @@ int tde_clean_buff(float *gbuf, int width, void *stream);
  * x = (w, v).  Returns TDE_ERR_INVALID_ARG if A is not positive definite. */
 int tde_icp_solve_update_host(const float *mbuf27, double *R9, double *t3, double *x6);
 
-/* The pipeline's on-device FP64 solve-and-update step on n independent
- * systems (one warp each; device pointers): sums28[28 n] = the 27 terms in
+/* The pipeline's on-device solve-and-update step on n independent systems
+ * (one warp each; device pointers; FP64 in and out: the system is solved in
+ * FP32 with one float-float refinement step and the pose moved in
+ * float-float): sums28[28 n] = the 27 terms in
  * the order above and an inlier count (not read), pose12[12 n] = row-major R
  * then t, updated in place, x6[6 n] = the step (w, v), ok[n] = 1 when A is
  * positive definite (else the pose is left unchanged).  Enqueued on
@@ -488,7 +490,7 @@ void tde_rgbd_default_params(tde_rgbd_params *params);
 size_t tde_rgbd_odometry_scratch_bytes(int cols, int rows);
 /* Estimate_Isometry_By_RGBD: Gauss-Newton on the weighted photometric error,
  * coarse to fine, params->iters[l] steps at level l, each T <- exp(xi) T with
- * the FP64 6x6 solve of the ICP path; intr0 is level 0's camera.  Starts from
+ * the 6x6 solve of the ICP path; intr0 is level 0's camera.  Starts from
  * init_pose12 (host; identity when NULL); the result goes to pose12_device
  * and *status_device: bit 0 (1) set when a step's solve failed (too few
  * pairs or A not positive definite) and kept its pose, bit 1 (2) when at

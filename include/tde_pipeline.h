@@ -7,9 +7,11 @@
  * maps, coarse-to-fine ICP (10/5/4 iterations), TSDF integration, raycast of
  * the model and its map pyramid.
  *
- * GB300 design: everything stays on the device; the ICP solve and the pose
- * update run in FP64 inside the last block of each ICP launch, so one frame is
- * a fixed sequence of launches with no host round trip.  That sequence is
+ * GB300 design: everything stays on the device; each ICP launch starts by
+ * solving the previous launch's exact totals and updating the pose in every
+ * block (the frame's last launch also solves its own and publishes the FP64
+ * pose), so one frame is a fixed sequence of launches with no host round
+ * trip.  That sequence is
  * captured once into CUDA graphs and replayed every frame.  A frame's only
  * host traffic is the depth upload and the pose download.
  */
