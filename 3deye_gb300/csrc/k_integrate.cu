@@ -532,7 +532,9 @@ int launch_integrate(const float *depth_scaled, void *volume, int format, const 
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned blocks = std::min(div_up(nb, 8u), (unsigned)sms * 8u);
+    // one resident wave (measured at 640x480 / 512^3: 4 blocks per SM
+    // 0.0655 ms, 6: 0.0696, 8: 0.0658, 12: 0.0658)
+    const unsigned blocks = std::min(div_up(nb, 8u), (unsigned)(sms * kIntBlocksPerSM));
     return dispatch_format(format, [&](auto F) {
         integrate_bricks_kernel<decltype(F)::value><<<blocks, 256, 0, stream>>>(depth_scaled, volume, P, list, count,
                                                                                neg_flags, stats, sat_flags);
