@@ -608,7 +608,7 @@ def rgbd_pass(tde, syn, torch, cfg, dev, ws, rank, with_cpu, pairs=48, warm=4):
                                        [np.linalg.norm(traj[i][9:] - traj[i - 1][9:]) for i in range(1, n)])), 6),
                                    "frames_without_a_solved_step": int(((st[1:] & 2) == 0).sum())},
            "note": "640x480 noisy depth + rendered texture, resident in HBM; per frame: intensity, 4-level "
-                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes each, the FP64 solve in the "
+                   "pyramid, Sobel derivatives and 31 Gauss-Newton steps (2 passes each, the 6x6 solve in the "
                    "second pass's last block), replayed from CUDA graphs (RgbdTracker)"}
     if with_cpu:
         from oracle import oracle as orc

@@ -8,7 +8,8 @@ FP64 oracle runs the same ten level-0 steps -- FP64 point-to-plane terms, sums
 and Cholesky solve, T <- exp(xi) T -- on the pipeline's own maps: frame 1's
 current vertex and normal maps and the model maps raycast after frame 0.  The
 comparison thus isolates the iteration (FP32 association, exact fixed-point
-sums, FP64 solve on the GPU): every step's pose stays within 5e-6 m and
+sums, the GPU's FP32 solve with a float-float refinement step): every step's
+pose stays within 5e-6 m and
 5e-6 rad of the FP64 one, and the last within 5e-7 m.
 """
 import dataclasses
@@ -20,8 +21,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 syn = importlib.import_module("3deye_gb300.synth")
-# measured: 0.8-2.5e-7 m on most steps, 1.0e-6 m / 1.2e-6 rad at the step
-# where a few FP32 association decisions differ, 7.6e-8 m after step 10
+# measured: 0.8-2.5e-7 m on most steps, 1.0e-6 m / 1.1e-6 rad at the step
+# where a few FP32 association decisions differ, 8.2e-8 m after step 10
 TOL_T_M, TOL_R_RAD, STEPS = 5e-6, 5e-6, 10
 TOL_FINAL_M = 5e-7
 
