@@ -331,9 +331,10 @@ __global__ void __launch_bounds__(kOdoThreads) residual_kernel(const Level L, co
 #pragma unroll
     for (int k = 0; k < kPix; ++k) idx[k] = blockIdx.x * kOdoThreads * kPix + k * kOdoThreads + threadIdx.x;
     load_depths<kPix>(L, idx, z);
-    // this pass is launched after the previous step has completed (a plain
-    // launch: the wait returns at once); programmatic serialisation of it
-    // measured slower with graph replay (0.684 against 0.654 ms per frame)
+    // launched with programmatic serialisation after the previous step's
+    // second pass: its pose update and this pass's writes of the partials
+    // that pass read come after this wait (0.507 against 0.514 ms per frame
+    // with graphs, 0.551 against 0.595 eager, than a plain launch)
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (threadIdx.x < 16) projective_part(threadIdx.x, pose, L, P, M);
     if (threadIdx.x == 0) {
@@ -757,7 +758,7 @@ int tde_rgbd_odometry(const tde_rgbd_frame *prev, const tde_rgbd_frame *curr, co
                                    params->min_gradient[l]);
         const unsigned nb = odo_blocks(in.cols, in.rows);
         for (int it = 0; it < params->iters[l]; ++it) {
-            residual_kernel<<<nb, kOdoThreads, 0, s>>>(L, pose12_device, res);
+            TDE_CUDA(launch_pdl(residual_kernel, nb, s, L, (const double *)pose12_device, res), "rgbd_odometry");
             TDE_CUDA(launch_pdl(lsm_kernel<true>, nb, s, L, pose12_device, (const unsigned long long *)res, (int)nb,
                                 reinterpret_cast<float *>(lsm), (float *)nullptr, ticket, status_device),
                      "rgbd_odometry");
