@@ -47,12 +47,6 @@ bool valid_round_buffer(const tde_round_buffer *rb) {
 
 namespace {
 
-__global__ void tsdf_init_kernel(uint32_t *p, size_t words) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (; i < words; i += stride) p[i] = 0u;
-}
-
 bool valid_intr(const tde_intrinsics *in) {
     return in && in->cols > 0 && in->rows > 0 && in->fx != 0.f && in->fy != 0.f && std::isfinite(in->fx) &&
            std::isfinite(in->fy) && std::isfinite(in->cx) && std::isfinite(in->cy);

@@ -86,17 +86,6 @@ __device__ __forceinline__ ffl ffl_dot(const ffl (&a)[N], const ffl (&b)[N], ffl
         }
     return ffl_two_sum(h[0], lo);
 }
-// 1/d for a positive normal d: the hardware approximation x of 1/d.hi
-// (relative error below 2^-22), then 1/d = x / (1 - e) with e = 1 - d x
-// formed exactly up to d.lo's term: x + x (e + e^2), relative error ~e^3.
-__device__ __forceinline__ ffl ffl_rcp(ffl d) {
-    float x;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(x) : "f"(d.hi));
-    const float p = __fmul_rn(d.hi, x);
-    const float pe = __fmaf_rn(d.hi, x, -p);  // p + pe = d.hi x; 1 - p is exact (p within 2^-21 of 1)
-    const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.f, p), pe), __fmul_rn(d.lo, x));
-    return ffl_fast_two_sum(x, __fmul_rn(x, __fmaf_rn(e, e, e)));
-}
 // Conversions through the FP64 pipe: for values that enter or leave the
 // solve once per frame, not for every step.
 __device__ __forceinline__ ffl ffl_from_double(double d) {
