@@ -252,7 +252,7 @@ class RgbdTracker:
                 g = torch.cuda.CUDAGraph()
                 self.stream.synchronize()
                 with torch.cuda.graph(g, stream=self.stream):
-                    self._work(p)
+                    self._frame_step(p)
                 self.graphs.append(g)
             torch.cuda.synchronize()
 
@@ -264,7 +264,7 @@ class RgbdTracker:
     def status(self):
         return self.od.status
 
-    def _work(self, p: int) -> None:
+    def _frame_step(self, p: int) -> None:
         s = self.torch.cuda.current_stream()
         self.bufs[p].load(self.depth_slot, self.rgb_slot, s)
         self.od.enqueue(self.bufs[1 - p], self.bufs[p], None, s)
@@ -282,5 +282,5 @@ class RgbdTracker:
             elif self.graphs is not None:
                 self.graphs[p].replay()
             else:
-                self._work(p)
+                self._frame_step(p)
         self.frames += 1
